@@ -1,0 +1,151 @@
+/*
+ * voxelcore_gb300.h -- C ABI of the GB300 (sm_103a) Voxel Cores hot path.
+ *
+ * One context = one CUDA stream on one device.  Every entry point returns an
+ * int status (VC_OK or a VC_ERR_* code); nothing exits the process and no
+ * exception crosses the ABI.  Array arguments are plain pointers; `mem` says
+ * whether a pointer is host memory (VC_MEM_HOST) or device memory on the
+ * context's device (VC_MEM_DEVICE).  The context owns every intermediate
+ * buffer; getters copy out and, for host destinations, synchronize.
+ *
+ * Each group of entry points replaces one reference interface; the citations
+ * are into the reference project (danielyan86129/voxel_ma).
+ */
+#ifndef VOXELCORE_GB300_H
+#define VOXELCORE_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define VC_OK 0
+#define VC_ERR_ARG 1       /* bad argument, size or degenerate input            */
+#define VC_ERR_OOM 2       /* device allocation failed                           */
+#define VC_ERR_TIMEOUT 3   /* a bounded device-side wait gave up                 */
+#define VC_ERR_INVARIANT 4 /* the reference's exit(1) check (ccthin.cpp:570-584) */
+#define VC_ERR_CUDA 5      /* CUDA runtime error (see vc_ctx_last_error)         */
+#define VC_ERR_STATE 6     /* entry point called before its inputs exist         */
+
+#define VC_MEM_HOST 0
+#define VC_MEM_DEVICE 1
+
+typedef struct vc_ctx vc_ctx;
+
+/* ---- context ----------------------------------------------------------- */
+int vc_version(void);
+const char* vc_status_string(int status);
+/* Create a context on `device`, with its own non-blocking stream. */
+int vc_ctx_create(vc_ctx** ctx, int device);
+int vc_ctx_destroy(vc_ctx* ctx);
+/* The context's cudaStream_t (as void*), for event timing by the caller. */
+void* vc_ctx_stream(vc_ctx* ctx);
+int vc_ctx_sync(vc_ctx* ctx);
+const char* vc_ctx_last_error(vc_ctx* ctx);
+/* Bytes of device memory currently held by the context's buffers. */
+int64_t vc_ctx_device_bytes(vc_ctx* ctx);
+
+/* ---- volume and boundary sites -----------------------------------------
+ * Replaces Surfacer::extractBoundaryVts(const shared_ptr<Volume3DScalar>&,
+ * vector<point>&) (include/surfacing.h:57-58, src/surfacing.cpp:223-321).
+ * occ: X*Y*Z bytes, x-major (z fastest), inside <=> value > 0; voxels outside
+ * the box count as outside (include/spaceinfo.h:122-129).  Sites come out in
+ * the reference's first-encounter order as float xyz voxel coordinates.   */
+int vc_set_volume(vc_ctx* ctx, const uint8_t* occ, int X, int Y, int Z, int mem);
+int vc_extract_sites(vc_ctx* ctx, int64_t* n_sites);
+int vc_get_sites(vc_ctx* ctx, float* xyz, int mem);
+
+/* ---- exact feature transform -------------------------------------------
+ * No reference function: the reference keeps the nearest-boundary-point
+ * relation only implicitly, as the two sites of each Voronoi face
+ * (src/voroinfo.cpp:185-231).  On the (X+1)(Y+1)(Z+1) corner lattice (point
+ * (a,b,c) at voxel coordinates (a-.5,b-.5,c-.5)) d2 = exact squared distance
+ * to the nearest site, id = that site's index; ties -> lowest index.       */
+int vc_feature_transform(vc_ctx* ctx);
+int vc_get_ft(vc_ctx* ctx, int32_t* d2, int32_t* id, int mem);
+
+/* ---- lattice Voronoi complex, inside part, with lambda measures ---------
+ * Replaces VoroInfo::extractInsideWithMeasure(MeasureForMA::LAMBDA, vts,
+ * edges, tris, from_fi, vts_msure, edges_msure, faces_msure)
+ * (include/voroinfo.h:127-131, src/voroinfo.cpp:624-729) for the Voronoi
+ * complex read off the feature transform; lambda as in
+ * MeasureForMA::lambdaForFace (include/measureforMA_imp.h:1-4) and
+ * src/voroinfo.cpp:1432-1574.  The resulting complex is also installed as
+ * the context's (already finalized) cell complex.                         */
+typedef struct {
+    int64_t nv, ne, nt, nface;
+    float inside_size; /* VoroInfo::getInsidePartSize (voroinfo.cpp:496)   */
+} vc_vd_sizes;
+int vc_lattice_vd(vc_ctx* ctx, vc_vd_sizes* sizes);
+int vc_get_vd(vc_ctx* ctx, float* vts, int32_t* edges, int32_t* tris, int32_t* tri_face, float* vm, float* em,
+              float* fm, int32_t* face_sites, int mem);
+
+/* ---- cell complex in ----------------------------------------------------
+ * Replaces cellcomplex(const vector<point>&, const vector<ivec2>&,
+ * const vector<uTriFace>&, bool finalize = true) + cellcomplex::finalize()
+ * (include/cellcomplex.h:33-34, 106; src/cellcomplex.cpp:13-26, 364-491):
+ * edge ids keep the given order, new face sides are appended in face order,
+ * V->E lists are in edge-id order and E->F lists in face-id order.
+ * Triangles with a repeated vertex and loop edges are rejected (VC_ERR_ARG). */
+int vc_set_complex(vc_ctx* ctx, int64_t nv, const float* vts, int64_t ne, const int32_t* edges, int64_t nt,
+                   const int32_t* tris, int mem);
+int vc_finalize(vc_ctx* ctx, int64_t* ne_final);
+int vc_get_finalized(vc_ctx* ctx, int32_t* edges, int32_t* tri_edges, int32_t* ve_off, int32_t* ve_ids,
+                     int32_t* ef_off, int32_t* ef_ids, int mem);
+
+/* ---- measures -----------------------------------------------------------
+ * Replaces CellComplexThinning::assignElementValues (src/ccthin.cpp:178-189):
+ * vm per vertex, em per FINALIZED edge, fm per triangle.                   */
+int vc_set_measures(vc_ctx* ctx, const float* vm, const float* em, const float* fm, int mem);
+
+/* ---- thinning -----------------------------------------------------------
+ * Replaces CellComplexThinning::prune(float f_t, float l_t, bool)
+ * (src/ccthin.cpp:201-424, 514-771): the same surviving set as the
+ * reference's FIFO queue, replayed generation by generation on the GPU.   */
+typedef struct {
+    int64_t pushes, processed, skipped, generations;
+} vc_thin_stats;
+int vc_thin(vc_ctx* ctx, float f_t, float l_t, vc_thin_stats* stats);
+/* keep_v: !removed; keep_e: !removed && no remaining face
+ * (getRemainedEdges, ccthin.cpp:156-166); keep_f: !removed;
+ * removed_e: getEdgeRemovedTags (ccthin.cpp:117-120).  Any may be NULL.    */
+int vc_get_thin_flags(vc_ctx* ctx, uint8_t* keep_v, uint8_t* keep_e, uint8_t* keep_f, uint8_t* removed_e, int mem);
+
+/* ---- remaining complex --------------------------------------------------
+ * Replaces CellComplexThinning::remainingCC(vector<point>&, vector<ivec2>&,
+ * vector<uTriFace>&, vector<int>*) (src/ccthin.cpp:467-512), including the
+ * re-triangulation (a,b,c)->(c,a,b) and util::compactify.                 */
+typedef struct {
+    int64_t nv, ne, nt;
+} vc_rem_sizes;
+int vc_remaining(vc_ctx* ctx, vc_rem_sizes* sizes);
+int vc_get_remaining(vc_ctx* ctx, float* vts, int32_t* edges, int32_t* tris, int mem);
+
+/* ---- topology of the remaining complex ----------------------------------
+ * util::computeEulerChar(vts, edges, tris, eulerchar&)
+ * (src/geomalgo.cpp:181-214) on the remainingCC output.                    */
+typedef struct {
+    int64_t V, E, F, C, euler;
+} vc_euler_info;
+int vc_euler_remaining(vc_ctx* ctx, vc_euler_info* out);
+
+/* ---- the plain single-volume path ---------------------------------------
+ * Sites, feature transform, lattice Voronoi complex with measures,
+ * thinning at thresh = float(inside_size * t) (highlevelalgo.cpp:825-837)
+ * and the remaining complex, in one call (exportInsideVoroMesh's .ply
+ * branch without file output, highlevelalgo.cpp:731-961).                 */
+typedef struct {
+    int64_t n_sites;
+    vc_vd_sizes vd;
+    float thresh;
+    vc_thin_stats thin;
+    vc_rem_sizes rem;
+} vc_plain_result;
+int vc_run_plain(vc_ctx* ctx, const uint8_t* occ, int X, int Y, int Z, int mem, double t, vc_plain_result* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VOXELCORE_GB300_H */

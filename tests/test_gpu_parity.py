@@ -1,0 +1,189 @@
+"""GPU parity: every stage of the sm_103a library, called through the C ABI,
+against the CPU oracle (itself pinned to the reference's compiled sources)
+and against the golden vectors recorded from the reference.  Integer and
+index results must be bit-identical; lambda measures are exact too (integer
+squared distances below 2^24 and a correctly rounded square root)."""
+import numpy as np
+import pytest
+
+import oracle as O
+from complexes import grid_surface, octahedron_shell, random_measures
+from helpers import golden_flags, golden_volume, golden_volume_names, lattice_case, rem_hash
+from voxel_ma_gb300 import _lib, volumes
+
+pytestmark = pytest.mark.gpu
+
+
+def _volumes():
+    rng = np.random.default_rng(9)
+    yield "torus64", volumes.torus_mesh(64)
+    yield "grf48", volumes.grf(48, sigma=6.0, seed=1)
+    yield "spheres64", volumes.spheres(64, count=32, seed=0)
+    yield "csg", volumes.csg(2, 32, 64)
+    yield "noise", (rng.uniform(size=(17, 23, 31)) < 0.5).astype(np.uint8)
+    yield "tiny", np.ones((1, 1, 1), np.uint8)
+    yield "full", np.ones((6, 7, 8), np.uint8)
+
+
+VOLS = list(_volumes())
+
+
+@pytest.mark.parametrize("name,occ", VOLS, ids=[v[0] for v in VOLS])
+def test_sites_ft_vd_match_oracle(gpu_ctx, name, occ):
+    ctx = gpu_ctx
+    L = lattice_case(O, occ)
+    ctx.set_volume(occ)
+    n = ctx.extract_sites()
+    assert n == len(L["xyz"])
+    assert np.array_equal(ctx.sites(), L["xyz"])
+    ctx.feature_transform()
+    d2, ids = ctx.ft()
+    assert np.array_equal(d2, L["d2"]), "squared distances differ"
+    assert np.array_equal(ids, L["ids"]), "nearest-site indices differ"
+    s = ctx.lattice_vd()
+    vd = ctx.vd()
+    ovd = L["vd"]
+    assert (s["nv"], s["ne"], s["nt"]) == (len(ovd["vts"]), len(ovd["edges"]), len(ovd["tris"]))
+    assert s["inside_size"] == ovd["inside_size"]
+    for k in ("vts", "edges", "tris", "vm", "em", "fm", "tri_face", "face_sites"):
+        assert np.array_equal(vd[k], ovd[k]), k
+
+
+def test_empty_volume(gpu_ctx):
+    occ = np.zeros((5, 6, 7), np.uint8)
+    gpu_ctx.set_volume(occ)
+    assert gpu_ctx.extract_sites() == 0
+    gpu_ctx.feature_transform()
+    d2, ids = gpu_ctx.ft()
+    assert (ids == -1).all() and (d2 == np.iinfo(np.int32).max).all()
+    s = gpu_ctx.lattice_vd()
+    assert s["nv"] == s["ne"] == s["nt"] == 0
+
+
+def test_sites_match_reference_golden(gpu_ctx, golden):
+    for name in golden_volume_names(golden):
+        occ = golden_volume(golden, name)
+        gpu_ctx.set_volume(occ)
+        gpu_ctx.extract_sites()
+        ref = golden[f"sites_{name}"].astype(np.float32) - 0.5
+        assert np.array_equal(gpu_ctx.sites(), ref), name
+
+
+def _gpu_thin(ctx, vts, edges, tris, em_fin, fm, thr):
+    ctx.set_complex(vts, edges, tris)
+    ne = ctx.finalize()
+    assert ne == len(em_fin)
+    ctx.set_measures(np.zeros(len(vts), np.float32), em_fin, fm)
+    st = ctx.thin(thr, thr)
+    return st, ctx.thin_flags()
+
+
+@pytest.mark.parametrize("seed", range(10))
+def test_finalize_and_thin_generic_complexes(gpu_ctx, seed):
+    rng = np.random.default_rng(200 + seed)
+    vts, edges, tris = grid_surface(int(rng.integers(3, 40)), int(rng.integers(3, 40)), seed=seed,
+                                    drop=float(rng.uniform(0, 0.3)), extra_edges=int(rng.integers(0, 40)),
+                                    unsorted=float(rng.uniform(0, 0.3)), omit=float(rng.uniform(0, 0.3)))
+    fin = O.finalize(len(vts), edges, tris)
+    gpu_ctx.set_complex(vts, edges, tris)
+    gpu_ctx.finalize()
+    g = gpu_ctx.finalized()
+    for k in ("edges", "tri_edges", "ve_off", "ve_ids", "ef_off", "ef_ids"):
+        assert np.array_equal(g[k], fin[k]), k
+    _, em, fm = random_measures(len(fin["edges"]), len(tris), seed=seed, levels=int(rng.integers(2, 6)))
+    for thr in (0.5, 1.0, 2.0, 9.0):
+        r = O.thin(len(vts), edges, tris, em, fm, thr, thr)
+        st, fl = _gpu_thin(gpu_ctx, vts, edges, tris, em, fm, thr)
+        for key in ("keep_v", "keep_e", "keep_f", "removed_e"):
+            assert np.array_equal(fl[key], r[key]), (thr, key)
+        assert st["processed"] == r["stats"]["processed"]
+
+
+@pytest.mark.parametrize("case", ["grid_a", "grid_b", "grid_c", "octa"])
+@pytest.mark.parametrize("tag", ["lo", "hi"])
+def test_thin_matches_reference_golden(gpu_ctx, golden, case, tag):
+    vts, edges, tris, em, fm = (golden[f"cc_{case}_{k}"] for k in ("vts", "edges", "tris", "em", "fm"))
+    p = f"cc_{case}_{tag}_"
+    thr = float(golden[p + "thr"][0])
+    st, fl = _gpu_thin(gpu_ctx, vts, edges, tris, em, fm, thr)
+    g = gpu_ctx.finalized()
+    assert np.array_equal(g["edges"], golden[f"cc_{case}_fin_edges"])
+    assert np.array_equal(g["tri_edges"], golden[f"cc_{case}_fin_tri_edges"])
+    for k, n in (("keep_v", len(vts)), ("keep_e", len(em)), ("keep_f", len(tris)), ("removed_e", len(em))):
+        assert np.array_equal(fl[k], golden_flags(golden, p + k, n)), k
+    gpu_ctx.remaining()
+    rv, re_, rt = gpu_ctx.remaining_arrays()
+    assert [len(rv), len(re_), len(rt)] == list(golden[p + "rem_sizes"])
+    assert rem_hash(rv, re_, rt) == golden[p + "rem_hash"].tobytes()
+    eu = gpu_ctx.euler_remaining()
+    assert [eu["V"], eu["E"], eu["F"], eu["C"], eu["euler"]] == list(golden[p + "euler"])
+
+
+@pytest.mark.parametrize("name", ["torus32", "grf24", "spheres28", "csg11", "edge_touch"])
+def test_lattice_pipeline_matches_reference_golden(gpu_ctx, golden, name):
+    occ = golden_volume(golden, name)
+    for t in (0.04, 0.2):
+        p = f"vd_{name}_{t}_"
+        r = gpu_ctx.run_plain(occ, t)
+        assert r["thresh"] == float(golden[p + "thr"][0])
+        sizes = golden[f"vd_{name}_sizes"]
+        assert [r["vd"]["nv"], r["vd"]["ne"], r["vd"]["nt"]] == list(sizes)
+        fl = gpu_ctx.thin_flags()
+        for k, n in (("keep_v", sizes[0]), ("keep_e", sizes[1]), ("keep_f", sizes[2])):
+            assert np.array_equal(fl[k], golden_flags(golden, p + k, int(n))), (t, k)
+        assert [r["rem"]["nv"], r["rem"]["ne"], r["rem"]["nt"]] == list(golden[p + "rem_sizes"])
+        eu = gpu_ctx.euler_remaining()
+        assert [eu["V"], eu["E"], eu["F"], eu["C"], eu["euler"]] == list(golden[p + "euler"])
+
+
+@pytest.mark.parametrize("name,occ", VOLS[:4], ids=[v[0] for v in VOLS[:4]])
+@pytest.mark.parametrize("t", [0.0, 0.04, 0.1])
+def test_plain_path_matches_oracle(gpu_ctx, name, occ, t):
+    ref = O.run_plain(occ, t=t)
+    r = gpu_ctx.run_plain(occ, t)
+    assert r["thresh"] == ref["thresh"]
+    fl = gpu_ctx.thin_flags()
+    for k in ("keep_v", "keep_e", "keep_f", "removed_e"):
+        assert np.array_equal(fl[k], ref["thin"][k]), k
+    assert r["thin"]["processed"] == ref["thin"]["stats"]["processed"]
+    rv, re_, rt = gpu_ctx.remaining_arrays()
+    assert np.array_equal(rv, ref["rem_vts"]) and np.array_equal(re_, ref["rem_edges"])
+    assert np.array_equal(rt, ref["rem_tris"])
+    eu = gpu_ctx.euler_remaining()
+    assert eu == O.euler(len(rv), re_, rt)
+
+
+def test_closed_pocket_and_errors(gpu_ctx):
+    vts, edges, tris = octahedron_shell()
+    st, fl = _gpu_thin(gpu_ctx, vts, edges, tris, np.zeros(12, np.float32), np.zeros(8, np.float32), 1.0)
+    assert fl["keep_f"].all() and st["processed"] == 0
+    # a triangle with a repeated vertex is rejected, not thinned
+    bad = np.array([[0, 0, 1]], np.int32)
+    gpu_ctx.set_complex(vts, np.zeros((0, 2), np.int32), bad)
+    with pytest.raises(_lib.VoxelCoreError) as ei:
+        gpu_ctx.finalize()
+    assert ei.value.status == _lib.VC_ERR_ARG
+    # the context stays usable after the rejected call
+    st, fl = _gpu_thin(gpu_ctx, vts, edges, tris, np.zeros(12, np.float32), np.zeros(8, np.float32), 1.0)
+    assert fl["keep_f"].all()
+
+
+def test_call_order_is_checked(gpu_ctx):
+    from voxel_ma_gb300 import api
+    ctx = api.Context(0)
+    try:
+        with pytest.raises(_lib.VoxelCoreError) as ei:
+            ctx.feature_transform()
+        assert ei.value.status == _lib.VC_ERR_STATE
+    finally:
+        ctx.close()
+
+
+def test_device_resident_inputs(gpu_ctx):
+    torch = pytest.importorskip("torch")
+    occ = volumes.torus_mesh(32)
+    ref = O.run_plain(occ, t=0.04)
+    r = gpu_ctx.run_plain(torch.from_numpy(occ).cuda(), 0.04)
+    fl = gpu_ctx.thin_flags(device=True)
+    assert np.array_equal(fl["keep_f"].cpu().numpy(), ref["thin"]["keep_f"])
+    assert r["rem"]["nt"] == len(ref["rem_tris"])

@@ -1,0 +1,104 @@
+"""ctypes binding of libvoxelcore_gb300.so (the C ABI in include/voxelcore_gb300.h).
+
+The library is the only compute path: when it is missing or cannot be loaded
+on a machine with a GPU, every call raises -- there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libvoxelcore_gb300.so")
+
+VC_OK, VC_ERR_ARG, VC_ERR_OOM, VC_ERR_TIMEOUT, VC_ERR_INVARIANT, VC_ERR_CUDA, VC_ERR_STATE = range(7)
+VC_MEM_HOST, VC_MEM_DEVICE = 0, 1
+
+c_i64 = ctypes.c_int64
+c_vp = ctypes.c_void_p
+c_int = ctypes.c_int
+c_float = ctypes.c_float
+
+
+class VdSizes(ctypes.Structure):
+    _fields_ = [("nv", c_i64), ("ne", c_i64), ("nt", c_i64), ("nface", c_i64), ("inside_size", c_float)]
+
+
+class ThinStats(ctypes.Structure):
+    _fields_ = [("pushes", c_i64), ("processed", c_i64), ("skipped", c_i64), ("generations", c_i64)]
+
+
+class RemSizes(ctypes.Structure):
+    _fields_ = [("nv", c_i64), ("ne", c_i64), ("nt", c_i64)]
+
+
+class EulerInfo(ctypes.Structure):
+    _fields_ = [("V", c_i64), ("E", c_i64), ("F", c_i64), ("C", c_i64), ("euler", c_i64)]
+
+
+class PlainResult(ctypes.Structure):
+    _fields_ = [("n_sites", c_i64), ("vd", VdSizes), ("thresh", c_float), ("thin", ThinStats), ("rem", RemSizes)]
+
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "vc_version": (c_int, []),
+    "vc_status_string": (ctypes.c_char_p, [c_int]),
+    "vc_ctx_create": (c_int, [ctypes.POINTER(c_vp), c_int]),
+    "vc_ctx_destroy": (c_int, [c_vp]),
+    "vc_ctx_stream": (c_vp, [c_vp]),
+    "vc_ctx_sync": (c_int, [c_vp]),
+    "vc_ctx_last_error": (ctypes.c_char_p, [c_vp]),
+    "vc_ctx_device_bytes": (c_i64, [c_vp]),
+    "vc_set_volume": (c_int, [c_vp, c_vp, c_int, c_int, c_int, c_int]),
+    "vc_extract_sites": (c_int, [c_vp, ctypes.POINTER(c_i64)]),
+    "vc_get_sites": (c_int, [c_vp, c_vp, c_int]),
+    "vc_feature_transform": (c_int, [c_vp]),
+    "vc_get_ft": (c_int, [c_vp, c_vp, c_vp, c_int]),
+    "vc_lattice_vd": (c_int, [c_vp, ctypes.POINTER(VdSizes)]),
+    "vc_get_vd": (c_int, [c_vp] + [c_vp] * 8 + [c_int]),
+    "vc_set_complex": (c_int, [c_vp, c_i64, c_vp, c_i64, c_vp, c_i64, c_vp, c_int]),
+    "vc_finalize": (c_int, [c_vp, ctypes.POINTER(c_i64)]),
+    "vc_get_finalized": (c_int, [c_vp] + [c_vp] * 6 + [c_int]),
+    "vc_set_measures": (c_int, [c_vp, c_vp, c_vp, c_vp, c_int]),
+    "vc_thin": (c_int, [c_vp, c_float, c_float, ctypes.POINTER(ThinStats)]),
+    "vc_get_thin_flags": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_int]),
+    "vc_remaining": (c_int, [c_vp, ctypes.POINTER(RemSizes)]),
+    "vc_get_remaining": (c_int, [c_vp, c_vp, c_vp, c_vp, c_int]),
+    "vc_euler_remaining": (c_int, [c_vp, ctypes.POINTER(EulerInfo)]),
+    "vc_run_plain": (c_int, [c_vp, c_vp, c_int, c_int, c_int, c_int, ctypes.c_double, ctypes.POINTER(PlainResult)]),
+}
+
+_lib = None
+_lock = threading.Lock()
+
+
+class VoxelCoreError(RuntimeError):
+    def __init__(self, status: int, where: str, detail: str = ""):
+        self.status = status
+        super().__init__(f"{where}: status {status} ({STATUS_NAMES.get(status, '?')}) {detail}".strip())
+
+
+STATUS_NAMES = {VC_OK: "ok", VC_ERR_ARG: "VC_ERR_ARG", VC_ERR_OOM: "VC_ERR_OOM", VC_ERR_TIMEOUT: "VC_ERR_TIMEOUT",
+                VC_ERR_INVARIANT: "VC_ERR_INVARIANT", VC_ERR_CUDA: "VC_ERR_CUDA", VC_ERR_STATE: "VC_ERR_STATE"}
+
+
+def load(build_if_missing: bool = True):
+    """Load (building first if needed) libvoxelcore_gb300.so and bind every entry point."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if build_if_missing:
+            from . import build as _build
+            _build.build()
+        if not os.path.exists(LIB_PATH):
+            raise FileNotFoundError(f"{LIB_PATH} is missing; run voxel_ma_gb300.build.build()")
+        lib = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+        return lib

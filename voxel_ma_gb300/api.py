@@ -1,0 +1,361 @@
+"""Python host layer over the C ABI, mirroring the reference's C++ surfaces.
+
+``Context`` wraps one ``vc_ctx`` (one CUDA stream on one device).  Arrays may
+be numpy arrays (host) or torch CUDA tensors (device); outputs come back as
+numpy arrays unless ``device=True`` is asked for, in which case they are
+torch tensors on the context's device.
+
+The classes ``Surfacer``, ``cellcomplex``, ``CellComplexThinning`` and the
+function ``extract_inside_with_measure`` keep the reference's names, argument
+meaning and call order (include/surfacing.h:57-58, include/cellcomplex.h:33,
+include/ccthin.h:57-113, include/voroinfo.h:127-131) so that code written
+against the reference reads the same.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Optional
+
+import numpy as np
+
+from . import _lib as L
+
+
+def _is_torch(x) -> bool:
+    return type(x).__module__.startswith("torch")
+
+
+def _ptr_mem(x):
+    """(pointer, mem flag) of a numpy array or a torch tensor."""
+    if x is None:
+        return None, L.VC_MEM_HOST
+    if _is_torch(x):
+        if not x.is_contiguous():
+            raise ValueError("tensor must be contiguous")
+        return ctypes.c_void_p(x.data_ptr()), (L.VC_MEM_DEVICE if x.is_cuda else L.VC_MEM_HOST)
+    if not x.flags["C_CONTIGUOUS"]:
+        raise ValueError("array must be C-contiguous")
+    return x.ctypes.data_as(ctypes.c_void_p), L.VC_MEM_HOST
+
+
+class Context:
+    """One GPU context of the hot path (vc_ctx)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = L.load()
+        self.device = device
+        h = ctypes.c_void_p()
+        st = self.lib.vc_ctx_create(ctypes.byref(h), device)
+        if st != L.VC_OK:
+            raise L.VoxelCoreError(st, "vc_ctx_create")
+        self.h = h
+        self.shape = None
+
+    # -- plumbing ---------------------------------------------------------
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.vc_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def check(self, st: int, where: str):
+        if st != L.VC_OK:
+            detail = self.lib.vc_ctx_last_error(self.h)
+            raise L.VoxelCoreError(st, where, detail.decode() if detail else "")
+
+    @property
+    def stream_ptr(self) -> int:
+        return int(self.lib.vc_ctx_stream(self.h) or 0)
+
+    def torch_stream(self):
+        import torch
+        return torch.cuda.ExternalStream(self.stream_ptr, device=torch.device("cuda", self.device))
+
+    def sync(self):
+        self.check(self.lib.vc_ctx_sync(self.h), "vc_ctx_sync")
+
+    def device_bytes(self) -> int:
+        return int(self.lib.vc_ctx_device_bytes(self.h))
+
+    def _out(self, shape, dtype, device: bool):
+        if device:
+            import torch
+            tdt = {np.float32: torch.float32, np.int32: torch.int32, np.uint8: torch.uint8}[dtype]
+            return torch.empty(shape, dtype=tdt, device=torch.device("cuda", self.device))
+        return np.empty(shape, dtype=dtype)
+
+    # -- volume / sites / FT ----------------------------------------------
+    def set_volume(self, occ):
+        X, Y, Z = (int(s) for s in occ.shape)
+        p, mem = _ptr_mem(occ)
+        self.check(self.lib.vc_set_volume(self.h, p, X, Y, Z, mem), "vc_set_volume")
+        self.shape = (X, Y, Z)
+
+    def extract_sites(self) -> int:
+        n = ctypes.c_int64()
+        self.check(self.lib.vc_extract_sites(self.h, ctypes.byref(n)), "vc_extract_sites")
+        self.n_sites = int(n.value)
+        return self.n_sites
+
+    def sites(self, device: bool = False):
+        out = self._out((self.n_sites, 3), np.float32, device)
+        p, mem = _ptr_mem(out)
+        self.check(self.lib.vc_get_sites(self.h, p, mem), "vc_get_sites")
+        return out
+
+    def feature_transform(self):
+        self.check(self.lib.vc_feature_transform(self.h), "vc_feature_transform")
+
+    def ft(self, device: bool = False):
+        X, Y, Z = self.shape
+        shp = (X + 1, Y + 1, Z + 1)
+        d2, ids = self._out(shp, np.int32, device), self._out(shp, np.int32, device)
+        (p1, mem), (p2, _) = _ptr_mem(d2), _ptr_mem(ids)
+        self.check(self.lib.vc_get_ft(self.h, p1, p2, mem), "vc_get_ft")
+        return d2, ids
+
+    # -- lattice Voronoi complex ------------------------------------------
+    def lattice_vd(self) -> dict:
+        s = L.VdSizes()
+        self.check(self.lib.vc_lattice_vd(self.h, ctypes.byref(s)), "vc_lattice_vd")
+        self.vd_sizes = dict(nv=s.nv, ne=s.ne, nt=s.nt, nface=s.nface, inside_size=s.inside_size)
+        return self.vd_sizes
+
+    def vd(self, device: bool = False) -> dict:
+        s = self.vd_sizes
+        o = dict(vts=self._out((s["nv"], 3), np.float32, device), edges=self._out((s["ne"], 2), np.int32, device),
+                 tris=self._out((s["nt"], 3), np.int32, device), tri_face=self._out((s["nt"],), np.int32, device),
+                 vm=self._out((s["nv"],), np.float32, device), em=self._out((s["ne"],), np.float32, device),
+                 fm=self._out((s["nt"],), np.float32, device),
+                 face_sites=self._out((s["nface"], 2), np.int32, device))
+        keys = ("vts", "edges", "tris", "tri_face", "vm", "em", "fm", "face_sites")
+        ptrs = [_ptr_mem(o[k])[0] for k in keys]
+        mem = L.VC_MEM_DEVICE if device else L.VC_MEM_HOST
+        self.check(self.lib.vc_get_vd(self.h, *ptrs, mem), "vc_get_vd")
+        o["inside_size"] = s["inside_size"]
+        return o
+
+    # -- cell complex -----------------------------------------------------
+    def set_complex(self, vts, edges, tris):
+        vts = vts.reshape(-1, 3) if vts is not None else None
+        nv, ne, nt = int(vts.shape[0]), int(edges.reshape(-1, 2).shape[0]), int(tris.reshape(-1, 3).shape[0])
+        (pv, mem), (pe, _), (pt, _) = _ptr_mem(vts), _ptr_mem(edges), _ptr_mem(tris)
+        self.check(self.lib.vc_set_complex(self.h, nv, pv, ne, pe, nt, pt, mem), "vc_set_complex")
+        self.nv, self.nt = nv, nt
+
+    def finalize(self) -> int:
+        n = ctypes.c_int64()
+        self.check(self.lib.vc_finalize(self.h, ctypes.byref(n)), "vc_finalize")
+        self.ne = int(n.value)
+        return self.ne
+
+    def finalized(self) -> dict:
+        nv, ne, nt = self.nv, self.ne, self.nt
+        o = dict(edges=np.empty((ne, 2), np.int32), tri_edges=np.empty((nt, 3), np.int32),
+                 ve_off=np.empty(nv + 1, np.int32), ve_ids=np.empty(2 * ne, np.int32),
+                 ef_off=np.empty(ne + 1, np.int32), ef_ids=np.empty(3 * nt, np.int32))
+        ptrs = [_ptr_mem(o[k])[0] for k in ("edges", "tri_edges", "ve_off", "ve_ids", "ef_off", "ef_ids")]
+        self.check(self.lib.vc_get_finalized(self.h, *ptrs, L.VC_MEM_HOST), "vc_get_finalized")
+        return o
+
+    def use_vd_as_complex(self):
+        s = self.vd_sizes
+        self.nv, self.ne, self.nt = s["nv"], s["ne"], s["nt"]
+
+    def set_measures(self, vm, em, fm):
+        (p1, mem), (p2, _), (p3, _) = _ptr_mem(vm), _ptr_mem(em), _ptr_mem(fm)
+        self.check(self.lib.vc_set_measures(self.h, p1, p2, p3, mem), "vc_set_measures")
+
+    def thin(self, f_t: float, l_t: float) -> dict:
+        st = L.ThinStats()
+        self.check(self.lib.vc_thin(self.h, ctypes.c_float(f_t), ctypes.c_float(l_t), ctypes.byref(st)), "vc_thin")
+        return dict(pushes=st.pushes, processed=st.processed, skipped=st.skipped, generations=st.generations)
+
+    def thin_flags(self, device: bool = False) -> dict:
+        o = dict(keep_v=self._out((self.nv,), np.uint8, device), keep_e=self._out((self.ne,), np.uint8, device),
+                 keep_f=self._out((self.nt,), np.uint8, device), removed_e=self._out((self.ne,), np.uint8, device))
+        ptrs = [_ptr_mem(o[k])[0] for k in ("keep_v", "keep_e", "keep_f", "removed_e")]
+        mem = L.VC_MEM_DEVICE if device else L.VC_MEM_HOST
+        self.check(self.lib.vc_get_thin_flags(self.h, *ptrs, mem), "vc_get_thin_flags")
+        return o
+
+    def remaining(self) -> dict:
+        s = L.RemSizes()
+        self.check(self.lib.vc_remaining(self.h, ctypes.byref(s)), "vc_remaining")
+        self.rem_sizes = dict(nv=s.nv, ne=s.ne, nt=s.nt)
+        return self.rem_sizes
+
+    def remaining_arrays(self, device: bool = False):
+        s = self.rem_sizes
+        v = self._out((s["nv"], 3), np.float32, device)
+        e = self._out((s["ne"], 2), np.int32, device)
+        t = self._out((s["nt"], 3), np.int32, device)
+        mem = L.VC_MEM_DEVICE if device else L.VC_MEM_HOST
+        self.check(self.lib.vc_get_remaining(self.h, _ptr_mem(v)[0], _ptr_mem(e)[0], _ptr_mem(t)[0], mem),
+                   "vc_get_remaining")
+        return v, e, t
+
+    def euler_remaining(self) -> dict:
+        s = L.EulerInfo()
+        self.check(self.lib.vc_euler_remaining(self.h, ctypes.byref(s)), "vc_euler_remaining")
+        return dict(V=s.V, E=s.E, F=s.F, C=s.C, euler=s.euler)
+
+    def run_plain(self, occ, t: float = 0.04) -> dict:
+        X, Y, Z = (int(s) for s in occ.shape)
+        p, mem = _ptr_mem(occ)
+        r = L.PlainResult()
+        self.check(self.lib.vc_run_plain(self.h, p, X, Y, Z, mem, ctypes.c_double(t), ctypes.byref(r)),
+                   "vc_run_plain")
+        self.shape = (X, Y, Z)
+        self.n_sites = r.n_sites
+        self.vd_sizes = dict(nv=r.vd.nv, ne=r.vd.ne, nt=r.vd.nt, nface=r.vd.nface, inside_size=r.vd.inside_size)
+        self.use_vd_as_complex()
+        self.rem_sizes = dict(nv=r.rem.nv, ne=r.rem.ne, nt=r.rem.nt)
+        return dict(n_sites=r.n_sites, vd=dict(self.vd_sizes), thresh=r.thresh,
+                    thin=dict(pushes=r.thin.pushes, processed=r.thin.processed, skipped=r.thin.skipped,
+                              generations=r.thin.generations),
+                    rem=dict(self.rem_sizes))
+
+
+# ---------------------------------------------------------------------------
+# Reference-shaped surfaces
+
+class Surfacer:
+    """Surfacer::extractBoundaryVts (include/surfacing.h:57-58) on the GPU."""
+
+    def __init__(self, ctx: Optional[Context] = None):
+        self.ctx = ctx or Context()
+
+    def extractBoundaryVts(self, vol, vts: Optional[list] = None):
+        self.ctx.set_volume(vol)
+        self.ctx.extract_sites()
+        pts = self.ctx.sites()
+        if vts is not None:
+            vts.clear()
+            vts.extend(pts)
+        return pts
+
+
+def extract_inside_with_measure(ctx: Context, occ) -> dict:
+    """VoroInfo::extractInsideWithMeasure(LAMBDA, ...) for the lattice Voronoi complex of ``occ``.
+
+    Returns vts, edges, tris, from_fi (polygon face per triangle), vts_msure,
+    edges_msure, faces_msure, face_sites and inside_size.
+    """
+    ctx.set_volume(occ)
+    ctx.extract_sites()
+    ctx.feature_transform()
+    ctx.lattice_vd()
+    o = ctx.vd()
+    return dict(vts=o["vts"], edges=o["edges"], tris=o["tris"], from_fi=o["tri_face"], vts_msure=o["vm"],
+                edges_msure=o["em"], faces_msure=o["fm"], face_sites=o["face_sites"], inside_size=o["inside_size"])
+
+
+class cellcomplex:  # noqa: N801 - reference name
+    """cellcomplex(vts, edges, tris, finalize=True) backed by a GPU context."""
+
+    def __init__(self, vts, edges, tris, perform_finalize: bool = True, ctx: Optional[Context] = None):
+        self.ctx = ctx or Context()
+        self.ctx.set_complex(np.ascontiguousarray(vts, np.float32).reshape(-1, 3),
+                             np.ascontiguousarray(edges, np.int32).reshape(-1, 2),
+                             np.ascontiguousarray(tris, np.int32).reshape(-1, 3))
+        self.vts = np.ascontiguousarray(vts, np.float32).reshape(-1, 3)
+        self._fin = None
+        if perform_finalize:
+            self.finalize()
+
+    def finalize(self):
+        self.ctx.finalize()
+        self._fin = None
+
+    def _f(self):
+        if self._fin is None:
+            self._fin = self.ctx.finalized()
+        return self._fin
+
+    def numVts(self):
+        return self.ctx.nv
+
+    def numEdges(self):
+        return self.ctx.ne
+
+    def numFaces(self):
+        return self.ctx.nt
+
+    def getEdge(self, i):
+        return tuple(self._f()["edges"][i])
+
+    def getFaceERep(self, fi):
+        return list(self._f()["tri_edges"][fi])
+
+    def nbEdgesofVert(self, v):
+        f = self._f()
+        return list(f["ve_ids"][f["ve_off"][v]:f["ve_off"][v + 1]])
+
+    def nbFacesofEdge(self, e):
+        f = self._f()
+        return list(f["ef_ids"][f["ef_off"][e]:f["ef_off"][e + 1]])
+
+    def refCntPerVert(self):
+        return np.diff(self._f()["ve_off"])
+
+    def refCntPerEdge(self):
+        return np.diff(self._f()["ef_off"])
+
+
+class CellComplexThinning:
+    """CellComplexThinning (include/ccthin.h:57-113) with prune() on the GPU."""
+
+    def __init__(self):
+        self.cc: Optional[cellcomplex] = None
+        self._flags = None
+
+    def setup(self, cc: cellcomplex):
+        self.cc = cc
+
+    def reset(self):
+        self.cc = None
+        self._flags = None
+
+    def assignElementValues(self, vert_measures, edge_measures, face_measures):
+        self.cc.ctx.set_measures(np.ascontiguousarray(vert_measures, np.float32),
+                                 np.ascontiguousarray(edge_measures, np.float32),
+                                 np.ascontiguousarray(face_measures, np.float32))
+
+    def preprocess(self):
+        self._flags = None
+
+    def prune(self, f_t: float, l_t: float, remove_small_components: bool = False):
+        self.stats = self.cc.ctx.thin(f_t, l_t)
+        self._flags = self.cc.ctx.thin_flags()
+        return self.stats
+
+    def getEdgeRemovedTags(self):
+        return self._flags["removed_e"].astype(bool)
+
+    def getFaceRemovedTags(self):
+        return ~self._flags["keep_f"].astype(bool)
+
+    def getRemainedVts(self):
+        return np.nonzero(self._flags["keep_v"])[0].astype(np.int32)
+
+    def getRemainedEdges(self):
+        return np.nonzero(self._flags["keep_e"])[0].astype(np.int32)
+
+    def getRemainedFaces(self):
+        return np.nonzero(self._flags["keep_f"])[0].astype(np.int32)
+
+    def remainingCC(self):
+        self.cc.ctx.remaining()
+        return self.cc.ctx.remaining_arrays()

@@ -1,0 +1,207 @@
+// extern "C" entry points of libvoxelcore_gb300.so (declared in
+// include/voxelcore_gb300.h).  Argument checks, device selection, buffer
+// staging and the plain single-volume pipeline live here; the kernels live
+// in the per-stage files.
+#include "vc_internal.cuh"
+
+namespace vc {
+int run_sites(vc_ctx* c, int64_t* n_sites);
+int run_ft(vc_ctx* c);
+int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes);
+int run_finalize(vc_ctx* c, int64_t* ne_final);
+int build_adjacency(vc_ctx* c);
+int run_thin(vc_ctx* c, float f_t, float l_t, vc_thin_stats* stats);
+int get_thin_flags(vc_ctx* c, uint8_t* kv, uint8_t* ke, uint8_t* kf, uint8_t* re, int mem);
+int run_remaining(vc_ctx* c, vc_rem_sizes* sizes);
+int run_euler_remaining(vc_ctx* c, vc_euler_info* out);
+}  // namespace vc
+
+using namespace vc;
+
+namespace {
+int enter(vc_ctx* c) {
+    if (!c) return VC_ERR_ARG;
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaSetDevice");
+    return VC_OK;
+}
+bool good_mem(int mem) { return mem == VC_MEM_HOST || mem == VC_MEM_DEVICE; }
+}  // namespace
+
+extern "C" {
+
+int vc_set_volume(vc_ctx* c, const uint8_t* occ, int X, int Y, int Z, int mem) {
+    VC_TRY(enter(c));
+    if (X <= 0 || Y <= 0 || Z <= 0 || !occ || !good_mem(mem)) return VC_ERR_ARG;
+    if ((int64_t)(X + 1) * (Y + 1) * (Z + 1) >= ((int64_t)1 << 33) || X > 32766 || Y > 32766 || Z > 32766)
+        return VC_ERR_ARG;
+    const int64_t n = (int64_t)X * Y * Z;
+    VC_TRY(ensure_n<uint8_t>(c, c->occ, n));
+    VC_TRY(copy_in(c, c->occ.p, occ, (size_t)n, mem));
+    c->X = X;
+    c->Y = Y;
+    c->Z = Z;
+    c->n_sites = -1;
+    c->ft_valid = c->vd_valid = false;
+    return VC_OK;
+}
+
+int vc_extract_sites(vc_ctx* c, int64_t* n_sites) {
+    VC_TRY(enter(c));
+    VC_TRY(run_sites(c, n_sites));
+    return sync_check(c);
+}
+
+int vc_get_sites(vc_ctx* c, float* xyz, int mem) {
+    VC_TRY(enter(c));
+    if (c->n_sites < 0) return VC_ERR_STATE;
+    if (!good_mem(mem)) return VC_ERR_ARG;
+    VC_TRY(copy_out(c, xyz, c->site_xyz.p, (size_t)c->n_sites * 3 * sizeof(float), mem));
+    return sync_check(c);
+}
+
+int vc_feature_transform(vc_ctx* c) {
+    VC_TRY(enter(c));
+    VC_TRY(run_ft(c));
+    return sync_check(c);
+}
+
+int vc_get_ft(vc_ctx* c, int32_t* d2, int32_t* id, int mem) {
+    VC_TRY(enter(c));
+    if (!c->ft_valid) return VC_ERR_STATE;
+    if (!good_mem(mem)) return VC_ERR_ARG;
+    const size_t n = (size_t)(c->X + 1) * (c->Y + 1) * (c->Z + 1);
+    VC_TRY(copy_out(c, d2, c->ft_d2.p, n * sizeof(int32_t), mem));
+    VC_TRY(copy_out(c, id, c->ft_id.p, n * sizeof(int32_t), mem));
+    return sync_check(c);
+}
+
+int vc_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes) {
+    VC_TRY(enter(c));
+    VC_TRY(run_lattice_vd(c, sizes));
+    return sync_check(c);
+}
+
+int vc_get_vd(vc_ctx* c, float* vts, int32_t* edges, int32_t* tris, int32_t* tri_face, float* vm, float* em,
+              float* fm, int32_t* face_sites, int mem) {
+    VC_TRY(enter(c));
+    if (!c->vd_valid) return VC_ERR_STATE;
+    if (!good_mem(mem)) return VC_ERR_ARG;
+    const vc_vd_sizes& s = c->vd;
+    VC_TRY(copy_out(c, vts, c->vts.p, (size_t)s.nv * 3 * sizeof(float), mem));
+    VC_TRY(copy_out(c, edges, c->edges.p, (size_t)s.ne * 2 * sizeof(int32_t), mem));
+    VC_TRY(copy_out(c, tris, c->tris.p, (size_t)s.nt * 3 * sizeof(int32_t), mem));
+    VC_TRY(copy_out(c, tri_face, c->vd_tri_face.p, (size_t)s.nt * sizeof(int32_t), mem));
+    VC_TRY(copy_out(c, vm, c->vm.p, (size_t)s.nv * sizeof(float), mem));
+    VC_TRY(copy_out(c, em, c->em.p, (size_t)s.ne * sizeof(float), mem));
+    VC_TRY(copy_out(c, fm, c->fm.p, (size_t)s.nt * sizeof(float), mem));
+    VC_TRY(copy_out(c, face_sites, c->vd_face_sites.p, (size_t)s.nface * 2 * sizeof(int32_t), mem));
+    return sync_check(c);
+}
+
+int vc_set_complex(vc_ctx* c, int64_t nv, const float* vts, int64_t ne, const int32_t* edges, int64_t nt,
+                   const int32_t* tris, int mem) {
+    VC_TRY(enter(c));
+    if (nv < 0 || ne < 0 || nt < 0 || !good_mem(mem)) return VC_ERR_ARG;
+    if (nv >= INT32_MAX || ne + 3 * nt >= INT32_MAX) return VC_ERR_ARG;
+    if ((nv && !vts) || (ne && !edges) || (nt && !tris)) return VC_ERR_ARG;
+    VC_TRY(ensure_n<float>(c, c->vts, 3 * nv));
+    VC_TRY(ensure_n<int2>(c, c->edges_in, ne));
+    VC_TRY(ensure_n<int32_t>(c, c->tris, 3 * nt));
+    VC_TRY(copy_in(c, c->vts.p, vts, (size_t)nv * 3 * sizeof(float), mem));
+    VC_TRY(copy_in(c, c->edges_in.p, edges, (size_t)ne * 2 * sizeof(int32_t), mem));
+    VC_TRY(copy_in(c, c->tris.p, tris, (size_t)nt * 3 * sizeof(int32_t), mem));
+    c->nv = nv;
+    c->ne_in = ne;
+    c->ne = 0;
+    c->nt = nt;
+    c->cc_valid = true;
+    c->cc_finalized = c->meas_valid = c->thin_valid = c->rem_valid = false;
+    c->vd_valid = false;  // the complex no longer comes from the lattice VD
+    return VC_OK;
+}
+
+int vc_finalize(vc_ctx* c, int64_t* ne_final) {
+    VC_TRY(enter(c));
+    VC_TRY(run_finalize(c, ne_final));
+    return sync_check(c);
+}
+
+int vc_get_finalized(vc_ctx* c, int32_t* edges, int32_t* tri_edges, int32_t* ve_off, int32_t* ve_ids,
+                     int32_t* ef_off, int32_t* ef_ids, int mem) {
+    VC_TRY(enter(c));
+    if (!c->cc_finalized) return VC_ERR_STATE;
+    if (!good_mem(mem)) return VC_ERR_ARG;
+    VC_TRY(copy_out(c, edges, c->edges.p, (size_t)c->ne * 2 * sizeof(int32_t), mem));
+    VC_TRY(copy_out(c, tri_edges, c->tri_edges.p, (size_t)c->nt * 3 * sizeof(int32_t), mem));
+    VC_TRY(copy_out(c, ve_off, c->ve_off.p, (size_t)(c->nv + 1) * sizeof(int32_t), mem));
+    VC_TRY(copy_out(c, ve_ids, c->ve_ids.p, (size_t)c->ne * 2 * sizeof(int32_t), mem));
+    VC_TRY(copy_out(c, ef_off, c->ef_off.p, (size_t)(c->ne + 1) * sizeof(int32_t), mem));
+    VC_TRY(copy_out(c, ef_ids, c->ef_ids.p, (size_t)c->nt * 3 * sizeof(int32_t), mem));
+    return sync_check(c);
+}
+
+int vc_set_measures(vc_ctx* c, const float* vm, const float* em, const float* fm, int mem) {
+    VC_TRY(enter(c));
+    if (!c->cc_finalized) return VC_ERR_STATE;
+    if (!good_mem(mem) || (c->ne && !em) || (c->nt && !fm)) return VC_ERR_ARG;
+    VC_TRY(ensure_n<float>(c, c->vm, c->nv));
+    VC_TRY(ensure_n<float>(c, c->em, c->ne));
+    VC_TRY(ensure_n<float>(c, c->fm, c->nt));
+    if (vm) VC_TRY(copy_in(c, c->vm.p, vm, (size_t)c->nv * sizeof(float), mem));
+    VC_TRY(copy_in(c, c->em.p, em, (size_t)c->ne * sizeof(float), mem));
+    VC_TRY(copy_in(c, c->fm.p, fm, (size_t)c->nt * sizeof(float), mem));
+    c->meas_valid = true;
+    c->thin_valid = c->rem_valid = false;
+    return VC_OK;
+}
+
+int vc_thin(vc_ctx* c, float f_t, float l_t, vc_thin_stats* stats) {
+    VC_TRY(enter(c));
+    VC_TRY(run_thin(c, f_t, l_t, stats));
+    return VC_OK;
+}
+
+int vc_get_thin_flags(vc_ctx* c, uint8_t* keep_v, uint8_t* keep_e, uint8_t* keep_f, uint8_t* removed_e, int mem) {
+    VC_TRY(enter(c));
+    if (!good_mem(mem)) return VC_ERR_ARG;
+    return get_thin_flags(c, keep_v, keep_e, keep_f, removed_e, mem);
+}
+
+int vc_remaining(vc_ctx* c, vc_rem_sizes* sizes) {
+    VC_TRY(enter(c));
+    VC_TRY(run_remaining(c, sizes));
+    return sync_check(c);
+}
+
+int vc_get_remaining(vc_ctx* c, float* vts, int32_t* edges, int32_t* tris, int mem) {
+    VC_TRY(enter(c));
+    if (!c->rem_valid) return VC_ERR_STATE;
+    if (!good_mem(mem)) return VC_ERR_ARG;
+    VC_TRY(copy_out(c, vts, c->rem_vts.p, (size_t)c->rem.nv * 3 * sizeof(float), mem));
+    VC_TRY(copy_out(c, edges, c->rem_edges.p, (size_t)c->rem.ne * 2 * sizeof(int32_t), mem));
+    VC_TRY(copy_out(c, tris, c->rem_tris.p, (size_t)c->rem.nt * 3 * sizeof(int32_t), mem));
+    return sync_check(c);
+}
+
+int vc_euler_remaining(vc_ctx* c, vc_euler_info* out) {
+    VC_TRY(enter(c));
+    if (!out) return VC_ERR_ARG;
+    return run_euler_remaining(c, out);
+}
+
+int vc_run_plain(vc_ctx* c, const uint8_t* occ, int X, int Y, int Z, int mem, double t, vc_plain_result* out) {
+    VC_TRY(enter(c));
+    if (!out) return VC_ERR_ARG;
+    VC_TRY(vc_set_volume(c, occ, X, Y, Z, mem));
+    VC_TRY(run_sites(c, &out->n_sites));
+    VC_TRY(run_ft(c));
+    VC_TRY(run_lattice_vd(c, &out->vd));
+    // highlevelalgo.cpp:836: float thresh = getInsidePartSize() * t (float * double -> float)
+    out->thresh = (float)((double)out->vd.inside_size * t);
+    VC_TRY(run_thin(c, out->thresh, out->thresh, &out->thin));
+    VC_TRY(run_remaining(c, &out->rem));
+    return sync_check(c);
+}
+
+}  // extern "C"

@@ -1,0 +1,244 @@
+// Context lifetime, device buffers, copies, error plumbing and device-wide
+// exclusive scans for the Voxel Cores GB300 library.
+#include "vc_internal.cuh"
+
+#include <algorithm>
+#include <cstring>
+
+namespace vc {
+
+int cuda_fail(vc_ctx* c, cudaError_t e, const char* what) {
+    if (c) {
+        c->last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    }
+    cudaGetLastError();  // clear sticky-free errors so the context stays usable
+    return e == cudaErrorMemoryAllocation ? VC_ERR_OOM : VC_ERR_CUDA;
+}
+
+int ensure_ctx(vc_ctx* c, DevBuf& b, size_t bytes) {
+    if (b.cap >= bytes && b.p) return VC_OK;
+    if (b.p) {
+        VC_CUDA(c, cudaFreeAsync(b.p, c->stream));
+        c->bytes_held -= (int64_t)b.cap;
+        b.p = nullptr;
+        b.cap = 0;
+    }
+    size_t want = std::max<size_t>(bytes, 256);
+    cudaError_t e = cudaMallocAsync(&b.p, want, c->stream);
+    if (e != cudaSuccess) {
+        b.p = nullptr;
+        return cuda_fail(c, e, "cudaMallocAsync");
+    }
+    b.cap = want;
+    c->bytes_held += (int64_t)want;
+    return VC_OK;
+}
+
+int* dev_err(vc_ctx* c) { return ptr<int>(c->err); }
+
+int sync_check(vc_ctx* c) {
+    VC_CUDA(c, cudaStreamSynchronize(c->stream));
+    VC_CUDA(c, cudaGetLastError());
+    int h = 0;
+    VC_CUDA(c, cudaMemcpy(&h, c->err.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (h != 0) {
+        int zero = 0;
+        VC_CUDA(c, cudaMemcpy(c->err.p, &zero, sizeof(int), cudaMemcpyHostToDevice));
+        c->last_error = std::string("device-side error: ") + vc_status_string(h);
+        return h;
+    }
+    return VC_OK;
+}
+
+int copy_out(vc_ctx* c, void* dst, const void* src, size_t bytes, int mem) {
+    if (!dst || bytes == 0) return VC_OK;
+    if (mem == VC_MEM_DEVICE) {
+        VC_CUDA(c, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, c->stream));
+        return VC_OK;
+    }
+    VC_CUDA(c, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->stream));
+    return sync_check(c);
+}
+
+int copy_in(vc_ctx* c, void* dst, const void* src, size_t bytes, int mem) {
+    if (bytes == 0) return VC_OK;
+    if (!src) return VC_ERR_ARG;
+    VC_CUDA(c, cudaMemcpyAsync(dst, src, bytes, mem == VC_MEM_DEVICE ? cudaMemcpyDeviceToDevice
+                                                                     : cudaMemcpyHostToDevice,
+                               c->stream));
+    return VC_OK;
+}
+
+int read_i64(vc_ctx* c, const int64_t* src, int64_t* out) {
+    VC_CUDA(c, cudaMemcpyAsync(out, src, sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
+    return sync_check(c);
+}
+
+// ---------------------------------------------------------------------------
+// Device-wide exclusive scan: reduce tiles, scan tile sums in one block,
+// then rescan each tile with its offset.  Tiles are ITEMS rows of blockDim
+// consecutive elements, so every global access is coalesced.
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 8;
+constexpr int64_t kScanTile = (int64_t)kScanThreads * kScanItems;
+
+template <class T>
+__global__ void __launch_bounds__(kScanThreads) scan_tile_sums(const T* __restrict__ in, int64_t n, int64_t* sums) {
+    __shared__ int64_t sm[33];
+    int64_t base = (int64_t)blockIdx.x * kScanTile;
+    int64_t acc = 0;
+#pragma unroll
+    for (int r = 0; r < kScanItems; ++r) {
+        int64_t i = base + (int64_t)r * kScanThreads + threadIdx.x;
+        if (i < n) acc += (int64_t)in[i];
+    }
+    int64_t tot;
+    block_exclusive_sum<int64_t>(acc, sm, &tot);
+    if (threadIdx.x == 0) sums[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(1024) scan_sums_single(int64_t* sums, int64_t n, int64_t* total) {
+    __shared__ int64_t sm[33];
+    int64_t carry = 0;
+    for (int64_t b = 0; b < n; b += blockDim.x) {
+        int64_t i = b + threadIdx.x;
+        int64_t v = i < n ? sums[i] : 0;
+        int64_t tot;
+        int64_t ex = block_exclusive_sum<int64_t>(v, sm, &tot);
+        if (i < n) sums[i] = carry + ex;
+        carry += tot;
+    }
+    if (threadIdx.x == 0 && total) *total = carry;
+}
+
+template <class T>
+__global__ void __launch_bounds__(kScanThreads) scan_apply(const T* in, T* out, int64_t n, const int64_t* sums) {
+    __shared__ int64_t sm[33];
+    int64_t base = (int64_t)blockIdx.x * kScanTile;
+    int64_t carry = sums[blockIdx.x];
+    for (int r = 0; r < kScanItems; ++r) {
+        int64_t i = base + (int64_t)r * kScanThreads + threadIdx.x;
+        int64_t v = i < n ? (int64_t)in[i] : 0;
+        int64_t tot;
+        int64_t ex = block_exclusive_sum<int64_t>(v, sm, &tot);
+        if (i < n) out[i] = (T)(carry + ex);
+        carry += tot;
+    }
+}
+
+template <class T>
+static int scan_impl(vc_ctx* c, const T* in, T* out, int64_t n, int64_t* total_dev) {
+    if (n <= 0) {
+        if (total_dev) VC_CUDA(c, cudaMemsetAsync(total_dev, 0, sizeof(int64_t), c->stream));
+        return VC_OK;
+    }
+    int64_t tiles = (n + kScanTile - 1) / kScanTile;
+    VC_TRY(ensure_n<int64_t>(c, c->scratch, tiles + 1));
+    int64_t* sums = ptr<int64_t>(c->scratch);
+    scan_tile_sums<T><<<(unsigned)tiles, kScanThreads, 0, c->stream>>>(in, n, sums);
+    scan_sums_single<<<1, 1024, 0, c->stream>>>(sums, tiles, total_dev);
+    scan_apply<T><<<(unsigned)tiles, kScanThreads, 0, c->stream>>>(in, out, n, sums);
+    VC_CUDA(c, cudaGetLastError());
+    return VC_OK;
+}
+
+int scan_exclusive_i32(vc_ctx* c, const int32_t* in, int32_t* out, int64_t n, int64_t* total_dev) {
+    return scan_impl<int32_t>(c, in, out, n, total_dev);
+}
+int scan_exclusive_i64(vc_ctx* c, const int64_t* in, int64_t* out, int64_t n, int64_t* total_dev) {
+    return scan_impl<int64_t>(c, in, out, n, total_dev);
+}
+
+}  // namespace vc
+
+// ---------------------------------------------------------------------------
+// Context entry points.
+extern "C" {
+
+int vc_version(void) { return 100; }
+
+const char* vc_status_string(int s) {
+    switch (s) {
+        case VC_OK: return "ok";
+        case VC_ERR_ARG: return "invalid argument";
+        case VC_ERR_OOM: return "out of device memory";
+        case VC_ERR_TIMEOUT: return "device-side wait timed out";
+        case VC_ERR_INVARIANT: return "thinning invariant violated (reference exit(1) case)";
+        case VC_ERR_CUDA: return "CUDA error";
+        case VC_ERR_STATE: return "inputs for this call are missing";
+        default: return "unknown status";
+    }
+}
+
+int vc_ctx_create(vc_ctx** out, int device) {
+    if (!out) return VC_ERR_ARG;
+    *out = nullptr;
+    vc_ctx* c = new vc_ctx();
+    c->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) {
+        delete c;
+        cudaGetLastError();
+        return VC_ERR_CUDA;
+    }
+    e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete c;
+        cudaGetLastError();
+        return VC_ERR_CUDA;
+    }
+    cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+    int s = vc::ensure_n<int64_t>(c, c->err, 16);
+    if (s == VC_OK) {
+        e = cudaMemsetAsync(c->err.p, 0, 16 * sizeof(int64_t), c->stream);
+        if (e != cudaSuccess) s = vc::cuda_fail(c, e, "memset");
+    }
+    if (s == VC_OK) s = vc::sync_check(c);
+    if (s != VC_OK) {
+        vc_ctx_destroy(c);
+        return s;
+    }
+    *out = c;
+    return VC_OK;
+}
+
+static void free_buf(vc_ctx* c, vc::DevBuf& b) {
+    if (b.p) cudaFreeAsync(b.p, c->stream);
+    b.p = nullptr;
+    b.cap = 0;
+}
+
+int vc_ctx_destroy(vc_ctx* c) {
+    if (!c) return VC_OK;
+    cudaSetDevice(c->device);
+    vc::DevBuf* all[] = {&c->err, &c->scratch, &c->scratch2, &c->occ, &c->site_xyz, &c->site_count,
+                         &c->site_id_lat, &c->ft_d2, &c->ft_id, &c->ft_tmp, &c->vd_flags, &c->vd_voff,
+                         &c->vd_eoff, &c->vd_foff, &c->vd_tri_face, &c->vd_face_sites, &c->vd_vm, &c->vd_bbox,
+                         &c->vts, &c->edges_in, &c->edges, &c->tris, &c->tri_edges, &c->ve_off, &c->ve_ids,
+                         &c->ef_off, &c->ef_ids, &c->hash_keys, &c->hash_pos, &c->hash_id, &c->side_slot,
+                         &c->vm, &c->em, &c->fm, &c->rm_f, &c->rm_e, &c->rm_v, &c->ref_e, &c->ref_v,
+                         &c->trig_e, &c->trig_v, &c->q0, &c->q1, &c->child, &c->child_cnt, &c->blk_cnt,
+                         &c->thr, &c->rem_voff, &c->rem_eoff, &c->rem_foff, &c->rem_vts, &c->rem_edges,
+                         &c->rem_tris, &c->uf_parent, &c->euler_tmp};
+    for (auto* b : all) free_buf(c, *b);
+    if (c->stream) {
+        cudaStreamSynchronize(c->stream);
+        cudaStreamDestroy(c->stream);
+    }
+    cudaGetLastError();
+    delete c;
+    return VC_OK;
+}
+
+void* vc_ctx_stream(vc_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+int vc_ctx_sync(vc_ctx* c) {
+    if (!c) return VC_ERR_ARG;
+    return vc::sync_check(c);
+}
+
+const char* vc_ctx_last_error(vc_ctx* c) { return c ? c->last_error.c_str() : "no context"; }
+
+int64_t vc_ctx_device_bytes(vc_ctx* c) { return c ? c->bytes_held : 0; }
+
+}  // extern "C"

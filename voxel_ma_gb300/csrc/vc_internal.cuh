@@ -1,0 +1,204 @@
+// Internal definitions shared by the sm_103a kernels of the Voxel Cores hot
+// path: the context, its device buffers, error plumbing, block/device scans
+// and a bounded grid barrier for cooperative (persistent) kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+
+#include "../../include/voxelcore_gb300.h"
+
+namespace vc {
+
+// ---------------------------------------------------------------------------
+// Device-side error word: kernels never trap; they record the first error
+// code here and return.  The host reads it back at the next sync point.
+enum DeviceError : int {
+    kDevOk = 0,
+    kDevTimeout = VC_ERR_TIMEOUT,
+    kDevInvariant = VC_ERR_INVARIANT,
+    kDevArg = VC_ERR_ARG,
+};
+
+__device__ __forceinline__ void set_error(int* err, int code) { atomicCAS(err, 0, code); }
+
+// ---------------------------------------------------------------------------
+// A growable device buffer owned by the context (stream-ordered allocation).
+struct DevBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+};
+
+template <class T>
+T* ptr(const DevBuf& b) {
+    return static_cast<T*>(b.p);
+}
+
+}  // namespace vc
+
+// The opaque context.  Members are grouped by pipeline stage.
+struct vc_ctx {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    std::string last_error;
+    int64_t bytes_held = 0;
+
+    vc::DevBuf err;      // int device error word + control words
+    vc::DevBuf scratch;  // scan tile sums and small temporaries
+    vc::DevBuf scratch2;
+
+    // volume
+    int X = 0, Y = 0, Z = 0;
+    vc::DevBuf occ;  // uint8 X*Y*Z
+    // sites
+    int64_t n_sites = -1;
+    vc::DevBuf site_xyz;    // float3 per site
+    vc::DevBuf site_count;  // int32 per-voxel new-corner counts, then offsets
+    vc::DevBuf site_id_lat; // int32 per lattice point: site id or -1
+    // feature transform
+    bool ft_valid = false;
+    vc::DevBuf ft_d2, ft_id;  // int32 per lattice point
+    vc::DevBuf ft_tmp;        // int64 per lattice point (separable pass scratch)
+    // lattice Voronoi complex
+    bool vd_valid = false;
+    vc_vd_sizes vd{};
+    vc::DevBuf vd_flags;              // uint8 per lattice point
+    vc::DevBuf vd_voff, vd_eoff, vd_foff;  // int32 exclusive offsets per lattice point
+    vc::DevBuf vd_tri_face, vd_face_sites, vd_vm;
+    vc::DevBuf vd_bbox;  // int32[6]
+    // cell complex (finalized, CSR)
+    bool cc_valid = false;
+    bool cc_finalized = false;
+    int64_t nv = 0, ne_in = 0, ne = 0, nt = 0;
+    vc::DevBuf vts;        // float3 [nv]
+    vc::DevBuf edges_in;   // int2 [ne_in]
+    vc::DevBuf edges;      // int2 [ne] finalized
+    vc::DevBuf tris;       // int3 [nt]
+    vc::DevBuf tri_edges;  // int3 [nt]
+    vc::DevBuf ve_off, ve_ids, ef_off, ef_ids;
+    vc::DevBuf hash_keys, hash_pos, hash_id, side_slot;  // finalize hash table
+    // measures
+    bool meas_valid = false;
+    vc::DevBuf vm, em, fm;
+    // thinning state
+    bool thin_valid = false;
+    vc_thin_stats thin_stats{};
+    vc::DevBuf rm_f, rm_e, rm_v, ref_e, ref_v, trig_e, trig_v;
+    vc::DevBuf q0, q1, child, child_cnt, blk_cnt, thr;
+    // remaining complex
+    bool rem_valid = false;
+    vc_rem_sizes rem{};
+    vc::DevBuf rem_voff, rem_eoff, rem_foff;
+    vc::DevBuf rem_vts, rem_edges, rem_tris;
+    vc::DevBuf uf_parent, euler_tmp;
+};
+
+namespace vc {
+
+// Record a CUDA error into the context and map it to a status.
+int cuda_fail(vc_ctx* c, cudaError_t e, const char* what);
+#define VC_CUDA(ctx, call)                                   \
+    do {                                                     \
+        cudaError_t _e = (call);                             \
+        if (_e != cudaSuccess) return vc::cuda_fail((ctx), _e, #call); \
+    } while (0)
+#define VC_TRY(expr)                 \
+    do {                             \
+        int _s = (expr);             \
+        if (_s != VC_OK) return _s;  \
+    } while (0)
+
+int ensure_ctx(vc_ctx* c, DevBuf& b, size_t bytes);
+template <class T>
+inline int ensure_n(vc_ctx* c, DevBuf& b, int64_t n) {
+    return ensure_ctx(c, b, (size_t)(n > 0 ? n : 1) * sizeof(T));
+}
+// Synchronize the stream and fold the device error word into a status.
+int sync_check(vc_ctx* c);
+// Copy n bytes between a context buffer and a caller pointer.
+int copy_out(vc_ctx* c, void* dst, const void* src, size_t bytes, int mem);
+int copy_in(vc_ctx* c, void* dst, const void* src, size_t bytes, int mem);
+int* dev_err(vc_ctx* c);
+// Exclusive scan helpers (device-wide), results and optional total on device.
+// out may alias in.  total_dev may be null.
+int scan_exclusive_i32(vc_ctx* c, const int32_t* in, int32_t* out, int64_t n, int64_t* total_dev);
+int scan_exclusive_i64(vc_ctx* c, const int64_t* in, int64_t* out, int64_t n, int64_t* total_dev);
+// Read one int64 from device memory (synchronizes).
+int read_i64(vc_ctx* c, const int64_t* src, int64_t* out);
+
+// ---------------------------------------------------------------------------
+// Warp / block scans (inclusive), blockDim.x a multiple of 32, <= 1024.
+template <class T>
+__device__ __forceinline__ T warp_inclusive_sum(T v) {
+    const unsigned lane = threadIdx.x & 31u;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        T n = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= (unsigned)o) v += n;
+    }
+    return v;
+}
+
+// Block-wide exclusive sum; returns the exclusive prefix of `v` and writes
+// the block total to *total.  blockDim.x must be a multiple of 32; `smem`
+// must hold 33 Ts.  All threads of the block call it.
+template <class T>
+__device__ __forceinline__ T block_exclusive_sum(T v, T* smem, T* total) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    T inc = warp_inclusive_sum(v);
+    if (lane == 31) smem[wid] = inc;
+    __syncthreads();
+    if (wid == 0) {
+        T s = lane < nw ? smem[lane] : T(0);
+        T si = warp_inclusive_sum(s);
+        if (lane < nw) smem[lane] = si - s;
+        if (lane == 31) smem[32] = si;
+    }
+    __syncthreads();
+    T res = smem[wid] + inc - v;
+    *total = smem[32];
+    __syncthreads();
+    return res;
+}
+
+// ---------------------------------------------------------------------------
+// Bounded grid barrier for cooperative launches.  `bar` points to two
+// unsigned words {arrived, generation}.  Every block calls it with all its
+// threads.  A block that waits longer than `limit` polls records
+// VC_ERR_TIMEOUT in *err and proceeds; callers check *err after the barrier
+// and leave their loop, so no block can wait forever.
+__device__ __forceinline__ void grid_barrier(unsigned* bar, int* err, unsigned long long limit) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned* vgen = bar + 1;
+        unsigned my_gen = *vgen;
+        __threadfence();
+        unsigned arrived = atomicAdd(bar, 1u);
+        if (arrived == gridDim.x - 1) {
+            atomicExch(bar, 0u);
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            unsigned long long spins = 0;
+            while (*vgen == my_gen) {
+                if (++spins > limit) {
+                    set_error(err, VC_ERR_TIMEOUT);
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ int ld_cg(const int* p) { return __ldcg(p); }
+
+inline int div_up(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
+
+}  // namespace vc

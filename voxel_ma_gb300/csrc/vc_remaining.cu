@@ -1,0 +1,217 @@
+// Remaining complex after thinning (replaces CellComplexThinning::remainingCC,
+// src/ccthin.cpp:467-512) and its Euler characteristic / component count
+// (util::computeEulerChar(vts, edges, tris), src/geomalgo.cpp:181-214).
+//
+// remainingCC keeps, in id order, the vertices not removed, the edges not
+// removed and referenced by no remaining face, and the faces not removed;
+// each surviving triangle (a,b,c) goes through util::simpleTriangulate, which
+// returns (c,a,b); util::compactify then renames vertex ids in the order the
+// vertices were kept.  computeEulerChar counts the given edges together with
+// the triangles' sides as a set (every one of them is a finalized edge of the
+// thinned complex, so the set is the set of their edge ids), all given
+// vertices, and the connected components of that edge set.
+#include "vc_internal.cuh"
+
+namespace vc {
+namespace {
+
+constexpr int32_t kAlive = INT32_MAX;
+
+__global__ void rem_flags_kernel(const int32_t* __restrict__ rm_v, const int32_t* __restrict__ rm_e,
+                                 const int32_t* __restrict__ ref_e, const int32_t* __restrict__ rm_f, int32_t nv,
+                                 int32_t ne, int32_t nt, int32_t* __restrict__ fv, int32_t* __restrict__ fe,
+                                 int32_t* __restrict__ ff) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (int64_t)nv + ne + nt; i += stride) {
+        if (i < nv) fv[i] = rm_v[i] == kAlive;
+        else if (i < (int64_t)nv + ne) fe[i - nv] = rm_e[i - nv] == kAlive && ref_e[i - nv] == 0;
+        else ff[i - nv - ne] = rm_f[i - nv - ne] == kAlive;
+    }
+}
+
+// After the exclusive scans: fv/fe/ff hold output positions; the keep test is
+// recomputed from the removal state.
+__global__ void rem_write_kernel(const int32_t* __restrict__ rm_v, const int32_t* __restrict__ rm_e,
+                                 const int32_t* __restrict__ ref_e, const int32_t* __restrict__ rm_f, int32_t nv,
+                                 int32_t ne, int32_t nt, const int32_t* __restrict__ pv, const int32_t* __restrict__ pe,
+                                 const int32_t* __restrict__ pf, const float* __restrict__ vts,
+                                 const int2* __restrict__ edges, const int32_t* __restrict__ tris,
+                                 float* __restrict__ ovts, int2* __restrict__ oedges, int32_t* __restrict__ otris) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (int64_t)nv + ne + nt; i += stride) {
+        if (i < nv) {
+            if (rm_v[i] != kAlive) continue;
+            const int64_t o = pv[i];
+            ovts[3 * o + 0] = vts[3 * i + 0];
+            ovts[3 * o + 1] = vts[3 * i + 1];
+            ovts[3 * o + 2] = vts[3 * i + 2];
+        } else if (i < (int64_t)nv + ne) {
+            const int64_t e = i - nv;
+            if (!(rm_e[e] == kAlive && ref_e[e] == 0)) continue;
+            const int2 ev = edges[e];
+            oedges[pe[e]] = make_int2(pv[ev.x], pv[ev.y]);
+        } else {
+            const int64_t f = i - nv - ne;
+            if (rm_f[f] != kAlive) continue;
+            const int64_t o = pf[f];
+            otris[3 * o + 0] = pv[tris[3 * f + 2]];
+            otris[3 * o + 1] = pv[tris[3 * f + 0]];
+            otris[3 * o + 2] = pv[tris[3 * f + 1]];
+        }
+    }
+}
+
+// Euler: mark every finalized edge that is a remaining edge or a side of a
+// remaining face.
+__global__ void euler_mark_kernel(const int32_t* __restrict__ rm_e, const int32_t* __restrict__ ref_e,
+                                  const int32_t* __restrict__ rm_f, const int32_t* __restrict__ tri_edges, int32_t ne,
+                                  int32_t nt, int32_t* __restrict__ mark) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (int64_t)ne + nt; i += stride) {
+        if (i < ne) {
+            if (rm_e[i] == kAlive && ref_e[i] == 0) mark[i] = 1;
+        } else {
+            const int64_t f = i - ne;
+            if (rm_f[f] != kAlive) continue;
+            mark[tri_edges[3 * f + 0]] = 1;
+            mark[tri_edges[3 * f + 1]] = 1;
+            mark[tri_edges[3 * f + 2]] = 1;
+        }
+    }
+}
+
+__device__ __forceinline__ int32_t uf_find(int32_t* parent, int32_t x) {
+    int32_t p = __ldcg(parent + x);
+    while (p != x) {
+        const int32_t gp = __ldcg(parent + p);
+        if (gp != p) parent[x] = gp;  // path halving (benign race)
+        x = p;
+        p = gp;
+    }
+    return x;
+}
+
+__global__ void uf_init_kernel(int32_t* parent, int32_t n) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) parent[i] = (int32_t)i;
+}
+
+__global__ void uf_union_kernel(const int32_t* __restrict__ mark, const int2* __restrict__ edges,
+                                const int32_t* __restrict__ pv, int32_t ne, int32_t* parent, int* err) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += stride) {
+        if (!mark[e]) continue;
+        const int2 ev = edges[e];
+        int32_t a = pv[ev.x], b = pv[ev.y];
+        bool done = false;
+        for (int it = 0; it < (1 << 20); ++it) {
+            a = uf_find(parent, a);
+            b = uf_find(parent, b);
+            if (a == b) {
+                done = true;
+                break;
+            }
+            if (a > b) {
+                const int32_t t = a;
+                a = b;
+                b = t;
+            }
+            if (atomicCAS(&parent[b], b, a) == b) {
+                done = true;
+                break;
+            }
+        }
+        if (!done) set_error(err, VC_ERR_TIMEOUT);
+    }
+}
+
+__global__ void uf_roots_kernel(int32_t* parent, int32_t n, unsigned long long* roots) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    unsigned long long local = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        if (uf_find(parent, (int32_t)i) == i) ++local;
+    if (local) atomicAdd(roots, local);
+}
+
+__global__ void count_kernel(const int32_t* __restrict__ mark, int64_t n, unsigned long long* cnt) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    unsigned long long local = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) local += mark[i] != 0;
+    if (local) atomicAdd(cnt, local);
+}
+
+inline int grid_for(vc_ctx* c, int64_t n, int threads) {
+    int64_t b = (n + threads - 1) / threads;
+    return (int)std::max<int64_t>(1, std::min<int64_t>(b, (int64_t)c->num_sms * 16));
+}
+
+}  // namespace
+
+int run_remaining(vc_ctx* c, vc_rem_sizes* sizes) {
+    if (!c->thin_valid) return VC_ERR_STATE;
+    const int64_t nv = c->nv, ne = c->ne, nt = c->nt;
+    VC_TRY(ensure_n<int32_t>(c, c->rem_voff, nv + 1));
+    VC_TRY(ensure_n<int32_t>(c, c->rem_eoff, ne + 1));
+    VC_TRY(ensure_n<int32_t>(c, c->rem_foff, nt + 1));
+    VC_TRY(ensure_n<int64_t>(c, c->scratch2, 4));
+    int32_t *pv = ptr<int32_t>(c->rem_voff), *pe = ptr<int32_t>(c->rem_eoff), *pf = ptr<int32_t>(c->rem_foff);
+    rem_flags_kernel<<<grid_for(c, nv + ne + nt, 256), 256, 0, c->stream>>>(
+        ptr<int32_t>(c->rm_v), ptr<int32_t>(c->rm_e), ptr<int32_t>(c->ref_e), ptr<int32_t>(c->rm_f), (int32_t)nv,
+        (int32_t)ne, (int32_t)nt, pv, pe, pf);
+    VC_CUDA(c, cudaGetLastError());
+    int64_t* tot = ptr<int64_t>(c->scratch2);
+    VC_TRY(scan_exclusive_i32(c, pv, pv, nv, tot + 0));
+    VC_TRY(scan_exclusive_i32(c, pe, pe, ne, tot + 1));
+    VC_TRY(scan_exclusive_i32(c, pf, pf, nt, tot + 2));
+    int64_t h[3] = {0, 0, 0};
+    VC_CUDA(c, cudaMemcpyAsync(h, tot, 3 * sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
+    VC_TRY(sync_check(c));
+    VC_TRY(ensure_n<float>(c, c->rem_vts, 3 * h[0]));
+    VC_TRY(ensure_n<int2>(c, c->rem_edges, h[1]));
+    VC_TRY(ensure_n<int32_t>(c, c->rem_tris, 3 * h[2]));
+    rem_write_kernel<<<grid_for(c, nv + ne + nt, 256), 256, 0, c->stream>>>(
+        ptr<int32_t>(c->rm_v), ptr<int32_t>(c->rm_e), ptr<int32_t>(c->ref_e), ptr<int32_t>(c->rm_f), (int32_t)nv,
+        (int32_t)ne, (int32_t)nt, pv, pe, pf, ptr<float>(c->vts), ptr<int2>(c->edges), ptr<int32_t>(c->tris),
+        ptr<float>(c->rem_vts), ptr<int2>(c->rem_edges), ptr<int32_t>(c->rem_tris));
+    VC_CUDA(c, cudaGetLastError());
+    c->rem = vc_rem_sizes{h[0], h[1], h[2]};
+    c->rem_valid = true;
+    if (sizes) *sizes = c->rem;
+    return VC_OK;
+}
+
+int run_euler_remaining(vc_ctx* c, vc_euler_info* out) {
+    if (!c->rem_valid) return VC_ERR_STATE;
+    const int64_t ne = c->ne, nt = c->nt, nvr = c->rem.nv;
+    VC_TRY(ensure_n<int32_t>(c, c->uf_parent, std::max<int64_t>(nvr, ne) + 1));
+    VC_TRY(ensure_n<int32_t>(c, c->scratch, ne + 1));
+    VC_TRY(ensure_n<int64_t>(c, c->scratch2, 4));
+    int32_t* mark = ptr<int32_t>(c->scratch);
+    auto* cnt = reinterpret_cast<unsigned long long*>(ptr<int64_t>(c->scratch2));
+    VC_CUDA(c, cudaMemsetAsync(mark, 0, (ne + 1) * sizeof(int32_t), c->stream));
+    VC_CUDA(c, cudaMemsetAsync(cnt, 0, 2 * sizeof(unsigned long long), c->stream));
+    euler_mark_kernel<<<grid_for(c, ne + nt, 256), 256, 0, c->stream>>>(
+        ptr<int32_t>(c->rm_e), ptr<int32_t>(c->ref_e), ptr<int32_t>(c->rm_f), ptr<int32_t>(c->tri_edges),
+        (int32_t)ne, (int32_t)nt, mark);
+    count_kernel<<<grid_for(c, ne, 256), 256, 0, c->stream>>>(mark, ne, cnt);
+    int32_t* parent = ptr<int32_t>(c->uf_parent);
+    if (nvr > 0) {
+        uf_init_kernel<<<grid_for(c, nvr, 256), 256, 0, c->stream>>>(parent, (int32_t)nvr);
+        uf_union_kernel<<<grid_for(c, ne, 256), 256, 0, c->stream>>>(mark, ptr<int2>(c->edges),
+                                                                      ptr<int32_t>(c->rem_voff), (int32_t)ne, parent,
+                                                                      dev_err(c));
+        uf_roots_kernel<<<grid_for(c, nvr, 256), 256, 0, c->stream>>>(parent, (int32_t)nvr, cnt + 1);
+    }
+    VC_CUDA(c, cudaGetLastError());
+    unsigned long long h[2];
+    VC_CUDA(c, cudaMemcpyAsync(h, cnt, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    VC_TRY(sync_check(c));
+    out->V = nvr;
+    out->E = (int64_t)h[0];
+    out->F = c->rem.nt;
+    out->C = (int64_t)h[1];
+    out->euler = out->V - out->E + out->F;
+    return VC_OK;
+}
+
+}  // namespace vc

@@ -1,0 +1,158 @@
+// Boundary-corner site extraction on the GPU (replaces
+// Surfacer::extractBoundaryVts, src/surfacing.cpp:223-321).
+//
+// The reference sweeps voxels i -> j -> k and, for each face neighbour
+// (-x,+x,-y,+y,-z,+z) whose occupancy differs, appends the four shared
+// corners it has not seen before.  A corner is therefore first met at the
+// earliest voxel (in sweep order) of the 2x2x2 block around it that is inside
+// the box and has a differing block neighbour; inside that voxel its rank is
+// the first (direction, corner slot) that names it.  Each thread decides this
+// per voxel from the voxel's 3x3x3 neighbourhood, so the site list comes out
+// in the reference's order after one exclusive scan of per-voxel counts.
+#include "vc_internal.cuh"
+
+namespace vc {
+namespace {
+
+// Corner c of a voxel as the lattice offset {0,1}^3 from the voxel's lowest
+// corner, in the reference's corner numbering (surfacing.h:74-96).
+__constant__ int8_t kCornerOff[8][3] = {{1, 0, 0}, {1, 1, 0}, {0, 0, 0}, {0, 1, 0},
+                                        {1, 0, 1}, {1, 1, 1}, {0, 0, 1}, {0, 1, 1}};
+// Face-neighbour offsets in sweep order (surfacing.h:170-179).
+__constant__ int8_t kNbOff[6][3] = {{-1, 0, 0}, {1, 0, 0}, {0, -1, 0}, {0, 1, 0}, {0, 0, -1}, {0, 0, 1}};
+// The four corners shared with each face neighbour, in visiting order
+// (surfacing.h:182-190).
+__constant__ int8_t kShared[6][4] = {{2, 3, 7, 6}, {0, 1, 5, 4}, {4, 6, 2, 0},
+                                     {1, 3, 7, 5}, {0, 2, 3, 1}, {5, 7, 6, 4}};
+
+struct Vol {
+    const uint8_t* occ;
+    int X, Y, Z;
+    __device__ __forceinline__ int at(int i, int j, int k) const {
+        if (i < 0 || j < 0 || k < 0 || i >= X || j >= Y || k >= Z) return 0;
+        return occ[((int64_t)i * Y + j) * Z + k] > 0 ? 1 : 0;
+    }
+};
+
+// 27-bit neighbourhood: bit (dx+1)*9 + (dy+1)*3 + (dz+1) = occupancy of
+// voxel (i+dx, j+dy, k+dz); out-of-box voxels read 0.
+__device__ __forceinline__ uint32_t load_nbhd(const Vol& v, int i, int j, int k) {
+    uint32_t m = 0;
+#pragma unroll
+    for (int dx = -1; dx <= 1; ++dx)
+#pragma unroll
+        for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+            for (int dz = -1; dz <= 1; ++dz)
+                m |= (uint32_t)v.at(i + dx, j + dy, k + dz) << ((dx + 1) * 9 + (dy + 1) * 3 + (dz + 1));
+    return m;
+}
+__device__ __forceinline__ int nb_bit(uint32_t m, int dx, int dy, int dz) {
+    return (m >> ((dx + 1) * 9 + (dy + 1) * 3 + (dz + 1))) & 1;
+}
+
+// Mask of the corners of voxel (i,j,k) that are first encountered there.
+__device__ __forceinline__ uint32_t new_corner_mask(const Vol& v, uint32_t nb, int i, int j, int k) {
+    uint32_t res = 0;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        const int ox = kCornerOff[c][0], oy = kCornerOff[c][1], oz = kCornerOff[c][2];
+        // block voxel q = (qx,qy,qz) sits at offset (ox-1+qx, oy-1+qy, oz-1+qz) from (i,j,k)
+        const int own = ((1 - ox) << 2) | ((1 - oy) << 1) | (1 - oz);
+        int first = -1;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int qx = (q >> 2) & 1, qy = (q >> 1) & 1, qz = q & 1;
+            const int dx = ox - 1 + qx, dy = oy - 1 + qy, dz = oz - 1 + qz;
+            const bool inb = (i + dx >= 0) && (i + dx < v.X) && (j + dy >= 0) && (j + dy < v.Y) &&
+                             (k + dz >= 0) && (k + dz < v.Z);
+            if (!inb || first >= 0) continue;
+            const int val = nb_bit(nb, dx, dy, dz);
+            // block neighbours: flip one of the three coordinates inside the block
+            const int vx = nb_bit(nb, ox - 1 + (qx ^ 1), dy, dz);
+            const int vy = nb_bit(nb, dx, oy - 1 + (qy ^ 1), dz);
+            const int vz = nb_bit(nb, dx, dy, oz - 1 + (qz ^ 1));
+            if (val != vx || val != vy || val != vz) first = q;
+        }
+        if (first == own) res |= 1u << c;
+    }
+    return res;
+}
+
+__global__ void sites_count_kernel(Vol v, int32_t* __restrict__ cnt) {
+    const int64_t n = (int64_t)v.X * v.Y * v.Z;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+        const int k = (int)(t % v.Z);
+        const int j = (int)((t / v.Z) % v.Y);
+        const int i = (int)(t / ((int64_t)v.Z * v.Y));
+        uint32_t nb = load_nbhd(v, i, j, k);
+        cnt[t] = __popc(new_corner_mask(v, nb, i, j, k));
+    }
+}
+
+__global__ void sites_emit_kernel(Vol v, const int32_t* __restrict__ off, float* __restrict__ xyz,
+                                  int32_t* __restrict__ site_id_lat) {
+    const int64_t n = (int64_t)v.X * v.Y * v.Z;
+    const int64_t NB = v.Y + 1, NC = v.Z + 1;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+        const int k = (int)(t % v.Z);
+        const int j = (int)((t / v.Z) % v.Y);
+        const int i = (int)(t / ((int64_t)v.Z * v.Y));
+        uint32_t nb = load_nbhd(v, i, j, k);
+        uint32_t mask = new_corner_mask(v, nb, i, j, k);
+        if (!mask) continue;
+        int32_t o = off[t];
+        const int cur = nb_bit(nb, 0, 0, 0);
+        uint32_t done = 0;
+        for (int d = 0; d < 6; ++d) {
+            if (nb_bit(nb, kNbOff[d][0], kNbOff[d][1], kNbOff[d][2]) == cur) continue;
+            for (int s = 0; s < 4; ++s) {
+                const int c = kShared[d][s];
+                if (!(mask & (1u << c)) || (done & (1u << c))) continue;
+                done |= 1u << c;
+                const int a = i + kCornerOff[c][0], b = j + kCornerOff[c][1], cc = k + kCornerOff[c][2];
+                xyz[3 * (int64_t)o + 0] = (float)a - 0.5f;
+                xyz[3 * (int64_t)o + 1] = (float)b - 0.5f;
+                xyz[3 * (int64_t)o + 2] = (float)cc - 0.5f;
+                site_id_lat[((int64_t)a * NB + b) * NC + cc] = o;
+                ++o;
+            }
+        }
+    }
+}
+
+inline int grid_for(vc_ctx* c, int64_t n, int threads) {
+    int64_t b = (n + threads - 1) / threads;
+    int64_t cap = (int64_t)c->num_sms * 16;
+    return (int)std::max<int64_t>(1, std::min<int64_t>(b, cap));
+}
+
+}  // namespace
+
+int run_sites(vc_ctx* c, int64_t* n_sites) {
+    if (!c->occ.p || c->X <= 0) return VC_ERR_STATE;
+    const int64_t nvox = (int64_t)c->X * c->Y * c->Z;
+    const int64_t nlat = (int64_t)(c->X + 1) * (c->Y + 1) * (c->Z + 1);
+    VC_TRY(ensure_n<int32_t>(c, c->site_count, nvox));
+    VC_TRY(ensure_n<int32_t>(c, c->site_id_lat, nlat));
+    VC_TRY(ensure_n<int64_t>(c, c->scratch2, 4));
+    Vol v{ptr<uint8_t>(c->occ), c->X, c->Y, c->Z};
+    int32_t* cnt = ptr<int32_t>(c->site_count);
+    sites_count_kernel<<<grid_for(c, nvox, 256), 256, 0, c->stream>>>(v, cnt);
+    VC_CUDA(c, cudaGetLastError());
+    int64_t* total = ptr<int64_t>(c->scratch2);
+    VC_TRY(scan_exclusive_i32(c, cnt, cnt, nvox, total));
+    int64_t n = 0;
+    VC_TRY(read_i64(c, total, &n));
+    if (n > INT32_MAX) return VC_ERR_ARG;
+    VC_TRY(ensure_n<float>(c, c->site_xyz, 3 * n));
+    VC_CUDA(c, cudaMemsetAsync(c->site_id_lat.p, 0xff, (size_t)nlat * sizeof(int32_t), c->stream));
+    sites_emit_kernel<<<grid_for(c, nvox, 256), 256, 0, c->stream>>>(v, cnt, ptr<float>(c->site_xyz),
+                                                                       ptr<int32_t>(c->site_id_lat));
+    VC_CUDA(c, cudaGetLastError());
+    c->n_sites = n;
+    if (n_sites) *n_sites = n;
+    return VC_OK;
+}
+
+}  // namespace vc
