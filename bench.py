@@ -1,0 +1,353 @@
+#!/usr/bin/env python3
+"""Benchmark of the Voxel Cores hot path on GB300: end-to-end voxels/s.
+
+A step is one pass of the whole path over one synthetic volume: boundary
+sites, exact feature transform, lattice Voronoi complex with lambda measures,
+FIFO-exact thinning at thresh = inside_size * t, and the remaining complex.
+The default workload is the 512^3 thresholded Gaussian random field (white
+noise blurred with sigma = 6 voxels, level 0).
+
+  value : voxels/s with the volume already resident in HBM (device pointer in,
+          device-resident results), timed with CUDA events on the library's
+          stream.
+  e2e   : the same metric through the public C-ABI call with HOST buffers:
+          the volume is copied from pinned host memory every step and the
+          remaining complex is read back to pinned host memory.
+
+``--impl reference`` times the CPU implementation of the same path (the
+restated reference algorithm in oracle/, single-threaded like the reference)
+on a bounded sample of the workload, with the same metric and JSON line.
+Under torchrun, ranks are independent replicas (each processes its own
+volume); the timed region is bracketed by a barrier and the max over ranks
+is taken.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "end-to-end voxels/s at 512^3 (EDT+measure+thin), batched vs plain GPU; p99 ms"
+UNIT = "voxels/s"
+FALLBACK_HBM_GBS = 6800.0
+CPU_SAMPLE_N = 128  # edge of the GRF sample timed on the host cores
+
+
+def measured_hbm_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_workload(name: str, device=None):
+    from voxel_ma_gb300 import volumes
+    if name == "grf512":
+        return volumes.grf(512, sigma=6.0, seed=0, device=device), "grf512_sigma6_level0"
+    if name == "grf256":
+        return volumes.grf(256, sigma=6.0, seed=0, device=device), "grf256_sigma6_level0"
+    if name == "spheres256":
+        return volumes.spheres(256, count=32, seed=0), "spheres256_32_seed0"
+    if name == "torus64":
+        return volumes.torus_mesh(64), "torus64_mesh"
+    raise SystemExit(f"unknown workload {name}")
+
+
+# ---------------------------------------------------------------------------
+# CPU side (reference arm and cpu_baseline): the oracle's restatement of the
+# reference algorithm, timed on a bounded sample of the workload.
+
+def cpu_path_once(occ, t):
+    import oracle
+    t0 = time.perf_counter()
+    oracle.run_plain(occ, t=t, threads=1)
+    return time.perf_counter() - t0
+
+
+def cpu_sample():
+    from voxel_ma_gb300 import volumes
+    occ = volumes.grf(CPU_SAMPLE_N, sigma=6.0, seed=0)
+    return occ, f"GRF sigma=6 level 0 at {CPU_SAMPLE_N}^3 (same field statistics as the 512^3 workload)"
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    import oracle
+    oracle.build(reference=False)
+    occ, sample = cpu_sample()
+    nvox = occ.size
+    for _ in range(args.warmup):
+        cpu_path_once(occ, args.t)
+    times = [cpu_path_once(occ, args.t) for _ in range(args.steps)]
+    mean = statistics.mean(times)
+    value = nvox / mean
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": mean * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32+f32",
+        "data": "synthetic (seeded thresholded Gaussian random field)",
+        "config": {"workload": "grf512_sigma6_level0", "sample": sample, "t": args.t},
+        "latency_ms": {"p50": float(np.percentile(times, 50) * 1e3), "p99": float(np.percentile(times, 99) * 1e3)},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                       "-lms", "200", "-i", str(device_index)], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is not None:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except Exception:
+                self.p.kill()
+        self.f.flush()
+        rows = []
+        try:
+            for line in open(self.f.name):
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9 and parts[1].replace(".", "").isdigit():
+                    rows.append(parts)
+        finally:
+            os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["clock sampling unavailable"]}
+        sm = [float(r[1]) for r in rows]
+        mx = max(float(r[2]) for r in rows)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": reasons, "samples": len(rows),
+                "power_w_max": max(float(r[3]) for r in rows if r[3].replace(".", "").isdigit())
+                if any(r[3].replace(".", "").isdigit() for r in rows) else None}
+
+
+# ---------------------------------------------------------------------------
+
+KERNEL_REGIONS = ("thin_generations", "ft_rows", "ft_envelope_y", "ft_envelope_x", "vd_flags", "vd_emit",
+                  "adjacency", "stage_sites", "stage_remaining")
+
+
+def algorithmic_bytes(region: str, shape, vd: dict, nsites: int) -> float:
+    """Compulsory bytes one launch of `region` moves (definitions in the design doc)."""
+    X, Y, Z = shape
+    N = (X + 1) * (Y + 1) * (Z + 1)
+    nvox = X * Y * Z
+    V, E, T, F = vd["nv"], vd["ne"], vd["nt"], vd["nface"]
+    if region == "thin_generations":
+        return 4 * (V + E + T) + 8 * E + 12 * T + 4 * (2 * E + 3 * T) + (V + E + T)
+    if region == "ft_rows":
+        return 12.0 * N
+    if region in ("ft_envelope_y", "ft_envelope_x"):
+        return 16.0 * N
+    if region == "vd_flags":
+        return 17.0 * N + nvox
+    if region == "vd_emit":
+        return 17.0 * N + 16 * V + 12 * E + 32 * T + 8 * F
+    if region == "adjacency":
+        return 8 * E + 12 * T + 4 * (V + 1) + 8 * E + 4 * (E + 1) + 12 * T
+    if region == "stage_sites":
+        return nvox + 4.0 * N + 12 * nsites
+    if region == "stage_remaining":
+        return 4 * (V + E + T) * 2
+    return 0.0
+
+
+def run_gpu(args):
+    import torch
+
+    from voxel_ma_gb300 import api
+
+    rank, world, local = dist_env()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    occ_np, workload = make_workload(args.workload, device=dev if args.workload.startswith("grf") else None)
+    occ_dev = torch.from_numpy(occ_np).to(dev)
+    occ_host = torch.from_numpy(occ_np).pin_memory()
+    shape = tuple(occ_np.shape)
+    nvox = int(np.prod(shape))
+
+    ctx = api.Context(local)
+    stream = ctx.torch_stream()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+        ctx.sync()
+
+    # ---- device-resident value ------------------------------------------
+    for _ in range(args.warmup):
+        r = ctx.run_plain(occ_dev, args.t)
+    barrier()
+    ctx.set_timing(True)
+    ctx.reset_timings()
+    launches0 = ctx.launch_count()
+    clocks = ClockSampler(local)
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    evs[0].record(stream)
+    for k in range(args.steps):
+        r = ctx.run_plain(occ_dev, args.t)
+        evs[k + 1].record(stream)
+    torch.cuda.synchronize(dev)
+    ctx.sync()
+    launches = ctx.launch_count() - launches0
+    timings = ctx.timings()
+    ctx.set_timing(False)
+    step_ms = [evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)]
+    total_ms = evs[0].elapsed_time(evs[-1])
+    if dist is not None:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * nvox * args.steps / (total_ms / 1e3)
+
+    # ---- end to end through the C ABI with host buffers -------------------
+    rem = r["rem"]
+    h_v = torch.empty((max(rem["nv"], 1), 3), dtype=torch.float32).pin_memory()
+    h_e = torch.empty((max(rem["ne"], 1), 2), dtype=torch.int32).pin_memory()
+    h_t = torch.empty((max(rem["nt"], 1), 3), dtype=torch.int32).pin_memory()
+
+    def e2e_step():
+        rr = ctx.run_plain(occ_host, args.t)
+        s = rr["rem"]
+        ctx.remaining_arrays_into(h_v[: s["nv"]], h_e[: s["ne"]], h_t[: s["nt"]])
+        return rr
+
+    for _ in range(max(1, args.warmup // 2)):
+        e2e_step()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    w0 = time.perf_counter()
+    e0.record(stream)
+    for _ in range(args.steps):
+        rr = e2e_step()
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    wall_e2e = time.perf_counter() - w0
+    e2e_ms = e0.elapsed_time(e1)
+    if dist is not None:
+        t = torch.tensor([e2e_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    clk = clocks.stop()
+    s = rr["rem"]
+    d2h = s["nv"] * 12 + s["ne"] * 8 + s["nt"] * 12
+    e2e_value = world * nvox * args.steps / (e2e_ms / 1e3)
+
+    # ---- roofline of the dominant kernel -----------------------------------
+    peak, peak_kind = measured_hbm_peak()
+    regions = {k: v for k, v in timings.items() if k in KERNEL_REGIONS}
+    dom = max(regions, key=lambda k: regions[k][0]) if regions else None
+    roof = None
+    if dom:
+        ms, cnt = regions[dom]
+        per_launch_s = ms / cnt / 1e3
+        ab = algorithmic_bytes(dom, shape, r["vd"], r["n_sites"])
+        ach = ab / per_launch_s / 1e9
+        roof = {"kernel": dom, "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+                "frac": ach / peak, "peak_kind": peak_kind, "algorithmic_bytes_per_launch": ab,
+                "traffic": TRAFFIC.get(dom, {}).get("bytes_per_launch") if args.workload == "grf512" else None,
+                "traffic_source": TRAFFIC.get(dom, {}).get("source")}
+    stage_ms = {k: v[0] / max(v[1], 1) for k, v in sorted(timings.items())}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32+f32",
+        "data": "synthetic (seeded thresholded Gaussian random field, generated on device)",
+        "config": {"workload": workload, "shape": list(shape), "t": args.t, "path": "plain single-volume",
+                   "l2": "inputs larger than L2 (per-step working set %.1f GB)" % (ctx.device_bytes() / 1e9),
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99))},
+        "complex": {"sites": r["n_sites"], "V": r["vd"]["nv"], "E": r["vd"]["ne"], "T": r["vd"]["nt"],
+                    "thresh": r["thresh"], "generations": r["thin"]["generations"],
+                    "processed": r["thin"]["processed"], "remaining": r["rem"]},
+        "region_ms_per_step": stage_ms,
+        "roofline": roof,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nvox, "d2h_bytes_per_step": d2h,
+                "ms_per_step": e2e_ms / args.steps, "wall_s": wall_e2e},
+        "gpu_launches": launches,
+        "clocks": clk,
+        "fp64_rescues": 0,
+        "lambda_note": "lambda = sqrt of an exact integer squared distance (< 2^24) in IEEE f32: no FP64 rescue needed",
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        occ_s, sample = cpu_sample()
+        times = [cpu_path_once(occ_s, args.t) for _ in range(2)]
+        line["cpu_baseline"] = {"value": occ_s.size / min(times), "unit": UNIT, "cores": 1, "kind": "port",
+                                "sample": sample + "; best of 2 runs of the oracle restatement"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+# Per-launch DRAM traffic of the kernels from an ncu capture of the same
+# workload (profiles/ summaries give the commands and figures).
+TRAFFIC: dict = {}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--workload", default="grf512")
+    ap.add_argument("--t", type=float, default=0.04)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

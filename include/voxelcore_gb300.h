@@ -46,6 +46,15 @@ int vc_ctx_sync(vc_ctx* ctx);
 const char* vc_ctx_last_error(vc_ctx* ctx);
 /* Bytes of device memory currently held by the context's buffers. */
 int64_t vc_ctx_device_bytes(vc_ctx* ctx);
+/* Number of kernels the library has launched on this context. */
+int64_t vc_ctx_launch_count(vc_ctx* ctx);
+/* CUDA-event timing of the library's named regions on the context stream
+ * (off by default).  get_timings writes up to `cap` entries: region names
+ * (each `name_len` bytes, NUL-terminated), accumulated ms and counts; *n is
+ * the number of regions recorded.                                          */
+int vc_ctx_set_timing(vc_ctx* ctx, int enable);
+int vc_ctx_reset_timings(vc_ctx* ctx);
+int vc_ctx_get_timings(vc_ctx* ctx, char* names, int name_len, double* ms, int64_t* counts, int cap, int* n);
 
 /* ---- volume and boundary sites -----------------------------------------
  * Replaces Surfacer::extractBoundaryVts(const shared_ptr<Volume3DScalar>&,

@@ -51,6 +51,11 @@ SIGNATURES = {
     "vc_ctx_sync": (c_int, [c_vp]),
     "vc_ctx_last_error": (ctypes.c_char_p, [c_vp]),
     "vc_ctx_device_bytes": (c_i64, [c_vp]),
+    "vc_ctx_launch_count": (c_i64, [c_vp]),
+    "vc_ctx_set_timing": (c_int, [c_vp, c_int]),
+    "vc_ctx_reset_timings": (c_int, [c_vp]),
+    "vc_ctx_get_timings": (c_int, [c_vp, ctypes.c_char_p, c_int, ctypes.POINTER(ctypes.c_double),
+                                   ctypes.POINTER(c_i64), c_int, ctypes.POINTER(c_int)]),
     "vc_set_volume": (c_int, [c_vp, c_vp, c_int, c_int, c_int, c_int]),
     "vc_extract_sites": (c_int, [c_vp, ctypes.POINTER(c_i64)]),
     "vc_get_sites": (c_int, [c_vp, c_vp, c_int]),

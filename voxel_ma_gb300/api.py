@@ -88,6 +88,29 @@ class Context:
     def device_bytes(self) -> int:
         return int(self.lib.vc_ctx_device_bytes(self.h))
 
+    def launch_count(self) -> int:
+        return int(self.lib.vc_ctx_launch_count(self.h))
+
+    def set_timing(self, on: bool):
+        self.check(self.lib.vc_ctx_set_timing(self.h, 1 if on else 0), "vc_ctx_set_timing")
+
+    def reset_timings(self):
+        self.check(self.lib.vc_ctx_reset_timings(self.h), "vc_ctx_reset_timings")
+
+    def timings(self) -> dict:
+        """{region: (total ms, count)} of the CUDA-event-timed library regions."""
+        cap, nl = 64, 48
+        names = ctypes.create_string_buffer(cap * nl)
+        ms = (ctypes.c_double * cap)()
+        cnt = (ctypes.c_int64 * cap)()
+        n = ctypes.c_int()
+        self.check(self.lib.vc_ctx_get_timings(self.h, names, nl, ms, cnt, cap, ctypes.byref(n)), "vc_ctx_get_timings")
+        out = {}
+        for i in range(min(n.value, cap)):
+            nm = names.raw[i * nl:(i + 1) * nl].split(b"\0", 1)[0].decode()
+            out[nm] = (float(ms[i]), int(cnt[i]))
+        return out
+
     def _out(self, shape, dtype, device: bool):
         if device:
             import torch
@@ -205,6 +228,11 @@ class Context:
         self.check(self.lib.vc_get_remaining(self.h, _ptr_mem(v)[0], _ptr_mem(e)[0], _ptr_mem(t)[0], mem),
                    "vc_get_remaining")
         return v, e, t
+
+    def remaining_arrays_into(self, vts, edges, tris):
+        """Copy the remaining complex into caller buffers (numpy, pinned host or CUDA tensors)."""
+        (pv, mem), (pe, _), (pt, _) = _ptr_mem(vts), _ptr_mem(edges), _ptr_mem(tris)
+        self.check(self.lib.vc_get_remaining(self.h, pv, pe, pt, mem), "vc_get_remaining")
 
     def euler_remaining(self) -> dict:
         s = L.EulerInfo()

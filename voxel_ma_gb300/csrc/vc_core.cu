@@ -36,9 +36,57 @@ int ensure_ctx(vc_ctx* c, DevBuf& b, size_t bytes) {
 
 int* dev_err(vc_ctx* c) { return ptr<int>(c->err); }
 
+static cudaEvent_t take_event(vc_ctx* c) {
+    if (!c->event_pool.empty()) {
+        cudaEvent_t e = c->event_pool.back();
+        c->event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return e;
+}
+
+Region::Region(vc_ctx* ctx, const char* n) : c(ctx), name(n) {
+    if (!c->timing) return;
+    a = take_event(c);
+    if (a) cudaEventRecord(a, c->stream);
+}
+
+Region::~Region() {
+    if (!c->timing || !a) return;
+    cudaEvent_t b = take_event(c);
+    if (!b) {
+        c->event_pool.push_back(a);
+        return;
+    }
+    cudaEventRecord(b, c->stream);
+    c->pending.push_back({name, a, b});
+}
+
+void resolve_timers(vc_ctx* c) {
+    for (auto& p : c->pending) {
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+            auto& t = c->timers[p.name];
+            t.first += ms;
+            t.second += 1;
+        } else {
+            cudaGetLastError();
+        }
+        c->event_pool.push_back(p.a);
+        c->event_pool.push_back(p.b);
+    }
+    c->pending.clear();
+}
+
 int sync_check(vc_ctx* c) {
     VC_CUDA(c, cudaStreamSynchronize(c->stream));
     VC_CUDA(c, cudaGetLastError());
+    if (!c->pending.empty()) resolve_timers(c);
     int h = 0;
     VC_CUDA(c, cudaMemcpy(&h, c->err.p, sizeof(int), cudaMemcpyDeviceToHost));
     if (h != 0) {
@@ -138,6 +186,7 @@ static int scan_impl(vc_ctx* c, const T* in, T* out, int64_t n, int64_t* total_d
     scan_tile_sums<T><<<(unsigned)tiles, kScanThreads, 0, c->stream>>>(in, n, sums);
     scan_sums_single<<<1, 1024, 0, c->stream>>>(sums, tiles, total_dev);
     scan_apply<T><<<(unsigned)tiles, kScanThreads, 0, c->stream>>>(in, out, n, sums);
+    launched(c, 3);
     VC_CUDA(c, cudaGetLastError());
     return VC_OK;
 }
@@ -221,6 +270,12 @@ int vc_ctx_destroy(vc_ctx* c) {
                          &c->thr, &c->rem_voff, &c->rem_eoff, &c->rem_foff, &c->rem_vts, &c->rem_edges,
                          &c->rem_tris, &c->uf_parent, &c->euler_tmp};
     for (auto* b : all) free_buf(c, *b);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (auto& p : c->pending) {
+        cudaEventDestroy(p.a);
+        cudaEventDestroy(p.b);
+    }
+    for (auto e : c->event_pool) cudaEventDestroy(e);
     if (c->stream) {
         cudaStreamSynchronize(c->stream);
         cudaStreamDestroy(c->stream);
@@ -240,5 +295,40 @@ int vc_ctx_sync(vc_ctx* c) {
 const char* vc_ctx_last_error(vc_ctx* c) { return c ? c->last_error.c_str() : "no context"; }
 
 int64_t vc_ctx_device_bytes(vc_ctx* c) { return c ? c->bytes_held : 0; }
+
+int64_t vc_ctx_launch_count(vc_ctx* c) { return c ? c->launches : 0; }
+
+int vc_ctx_set_timing(vc_ctx* c, int enable) {
+    if (!c) return VC_ERR_ARG;
+    int s = vc::sync_check(c);
+    c->timing = enable != 0;
+    return s;
+}
+
+int vc_ctx_reset_timings(vc_ctx* c) {
+    if (!c) return VC_ERR_ARG;
+    int s = vc::sync_check(c);
+    c->timers.clear();
+    return s;
+}
+
+int vc_ctx_get_timings(vc_ctx* c, char* names, int name_len, double* ms, int64_t* counts, int cap, int* n) {
+    if (!c || !n || name_len <= 1) return VC_ERR_ARG;
+    int s = vc::sync_check(c);
+    int k = 0;
+    for (auto& kv : c->timers) {
+        if (k < cap) {
+            if (names) {
+                std::strncpy(names + (size_t)k * name_len, kv.first.c_str(), (size_t)name_len - 1);
+                names[(size_t)k * name_len + name_len - 1] = 0;
+            }
+            if (ms) ms[k] = kv.second.first;
+            if (counts) counts[k] = kv.second.second;
+        }
+        ++k;
+    }
+    *n = k;
+    return s;
+}
 
 }  // extern "C"

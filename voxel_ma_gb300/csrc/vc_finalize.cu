@@ -169,6 +169,7 @@ inline int grid_for(vc_ctx* c, int64_t n, int threads) {
 // Build V->E and E->F lists of the context's finalized edges / tri_edges.
 int build_adjacency(vc_ctx* c) {
     const int64_t nv = c->nv, ne = c->ne, nt = c->nt;
+    Region stage(c, "adjacency");
     VC_TRY(ensure_n<int32_t>(c, c->ve_off, nv + 1));
     VC_TRY(ensure_n<int32_t>(c, c->ve_ids, 2 * ne));
     VC_TRY(ensure_n<int32_t>(c, c->ef_off, ne + 1));
@@ -180,22 +181,37 @@ int build_adjacency(vc_ctx* c) {
     // V->E
     int32_t* ve_off = ptr<int32_t>(c->ve_off);
     VC_CUDA(c, cudaMemsetAsync(ve_off, 0, (nv + 1) * sizeof(int32_t), c->stream));
-    if (ne > 0) ve_count_kernel<<<grid_for(c, ne, 256), 256, 0, c->stream>>>(edges, ne, ve_off);
+    if (ne > 0) {
+        ve_count_kernel<<<grid_for(c, ne, 256), 256, 0, c->stream>>>(edges, ne, ve_off);
+        launched(c);
+    }
     VC_TRY(scan_exclusive_i32(c, ve_off, ve_off, nv + 1, nullptr));
     VC_CUDA(c, cudaMemcpyAsync(cur, ve_off, (nv + 1) * sizeof(int32_t), cudaMemcpyDeviceToDevice, c->stream));
-    if (ne > 0) ve_fill_kernel<<<grid_for(c, ne, 256), 256, 0, c->stream>>>(edges, ne, cur, ptr<int32_t>(c->ve_ids));
-    if (nv > 0)
+    if (ne > 0) {
+        ve_fill_kernel<<<grid_for(c, ne, 256), 256, 0, c->stream>>>(edges, ne, cur, ptr<int32_t>(c->ve_ids));
+        launched(c);
+    }
+    if (nv > 0) {
         sort_segments_kernel<<<grid_for(c, nv, 256), 256, 0, c->stream>>>(ve_off, ptr<int32_t>(c->ve_ids), nv);
+        launched(c);
+    }
     // E->F
     int32_t* ef_off = ptr<int32_t>(c->ef_off);
     VC_CUDA(c, cudaMemsetAsync(ef_off, 0, (ne + 1) * sizeof(int32_t), c->stream));
-    if (nt > 0) ef_count_kernel<<<grid_for(c, 3 * nt, 256), 256, 0, c->stream>>>(te, 3 * nt, ef_off);
+    if (nt > 0) {
+        ef_count_kernel<<<grid_for(c, 3 * nt, 256), 256, 0, c->stream>>>(te, 3 * nt, ef_off);
+        launched(c);
+    }
     VC_TRY(scan_exclusive_i32(c, ef_off, ef_off, ne + 1, nullptr));
     VC_CUDA(c, cudaMemcpyAsync(cur, ef_off, (ne + 1) * sizeof(int32_t), cudaMemcpyDeviceToDevice, c->stream));
-    if (nt > 0)
+    if (nt > 0) {
         ef_fill_kernel<<<grid_for(c, 3 * nt, 256), 256, 0, c->stream>>>(te, 3 * nt, cur, ptr<int32_t>(c->ef_ids));
-    if (ne > 0)
+        launched(c);
+    }
+    if (ne > 0) {
         sort_segments_kernel<<<grid_for(c, ne, 256), 256, 0, c->stream>>>(ef_off, ptr<int32_t>(c->ef_ids), ne);
+        launched(c);
+    }
     VC_CUDA(c, cudaGetLastError());
     return VC_OK;
 }
@@ -210,6 +226,7 @@ int run_finalize(vc_ctx* c, int64_t* ne_final) {
     const int64_t n = ne + 3 * nt;
     validate_kernel<<<grid_for(c, ne + nt, 256), 256, 0, c->stream>>>(ptr<int2>(c->edges_in), ne,
                                                                        ptr<int32_t>(c->tris), nt, nv, dev_err(c));
+    launched(c);
     VC_TRY(sync_check(c));
     unsigned long long cap = 1024;
     while (cap < (unsigned long long)(2 * n)) cap <<= 1;
@@ -224,12 +241,17 @@ int run_finalize(vc_ctx* c, int64_t* ne_final) {
     VC_CUDA(c, cudaMemsetAsync(keys, 0xff, cap * sizeof(unsigned long long), c->stream));
     VC_CUDA(c, cudaMemsetAsync(minpos, 0x7f, cap * sizeof(int64_t), c->stream));
     int64_t* slot_of = ptr<int64_t>(c->side_slot);
-    if (n > 0)
+    if (n > 0) {
         hash_insert_kernel<<<grid_for(c, n, 256), 256, 0, c->stream>>>(ptr<int2>(c->edges_in), ne,
                                                                         ptr<int32_t>(c->tris), nt, keys, minpos,
                                                                         slot_of, cap - 1, dev_err(c));
+        launched(c);
+    }
     int32_t* rank = ptr<int32_t>(c->scratch2);
-    if (n > 0) first_flags_kernel<<<grid_for(c, n, 256), 256, 0, c->stream>>>(slot_of, minpos, rank, n);
+    if (n > 0) {
+        first_flags_kernel<<<grid_for(c, n, 256), 256, 0, c->stream>>>(slot_of, minpos, rank, n);
+        launched(c);
+    }
     int64_t* total = ptr<int64_t>(c->euler_tmp);
     VC_TRY(scan_exclusive_i32(c, rank, rank, n, total));
     int64_t ne_out = 0;
@@ -238,13 +260,17 @@ int run_finalize(vc_ctx* c, int64_t* ne_final) {
     VC_TRY(ensure_n<int2>(c, c->edges, ne_out));
     VC_TRY(ensure_n<int32_t>(c, c->tri_edges, 3 * nt));
     int32_t* slot_id = ptr<int32_t>(c->hash_id);
-    if (n > 0)
+    if (n > 0) {
         assign_ids_kernel<<<grid_for(c, n, 256), 256, 0, c->stream>>>(ptr<int2>(c->edges_in), ne,
                                                                        ptr<int32_t>(c->tris), slot_of, minpos, rank,
                                                                        slot_id, ptr<int2>(c->edges), n);
-    if (nt > 0)
+        launched(c);
+    }
+    if (nt > 0) {
         side_ids_kernel<<<grid_for(c, 3 * nt, 256), 256, 0, c->stream>>>(slot_of, slot_id,
                                                                           ptr<int32_t>(c->tri_edges), ne, 3 * nt);
+        launched(c);
+    }
     VC_CUDA(c, cudaGetLastError());
     c->ne = ne_out;
     VC_TRY(build_adjacency(c));

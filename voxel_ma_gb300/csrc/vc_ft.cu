@@ -199,6 +199,7 @@ int run_ft(vc_ctx* c) {
     VC_TRY(ensure_n<int32_t>(c, c->ft_d2, N));
     VC_TRY(ensure_n<int32_t>(c, c->ft_id, N));
     VC_TRY(ensure_n<int64_t>(c, c->ft_tmp, 2 * N));
+    Region stage(c, "stage_ft");
     int64_t* A = ptr<int64_t>(c->ft_tmp);
     int64_t* B = A + N;
     // envelope stacks reuse the d2 output buffer for pass 2 (int32 per point);
@@ -213,8 +214,10 @@ int run_ft(vc_ctx* c) {
         const int64_t nrows = NA * NB;
         int blocks = (int)std::min<int64_t>((nrows + warps_per_block - 1) / warps_per_block,
                                             (int64_t)c->num_sms * 8);
+        Region r(c, "ft_rows");
         ft_rows_kernel<<<blocks, warps_per_block * 32, smem, c->stream>>>(ptr<int32_t>(c->site_id_lat), A, nrows,
                                                                           (int)NC);
+        launched(c);
         VC_CUDA(c, cudaGetLastError());
     }
     {
@@ -222,8 +225,10 @@ int run_ft(vc_ctx* c) {
         const int64_t nlines = NA * NC;
         int blocks = (int)std::min<int64_t>((nlines + 255) / 256, (int64_t)c->num_sms * 8);
         int32_t* stack = ptr<int32_t>(c->ft_d2);  // NA*NC*NB int32 fits the d2 buffer exactly
+        Region r(c, "ft_envelope_y");
         ft_envelope_kernel<false><<<blocks, 256, 0, c->stream>>>(A, B, nullptr, nullptr, stack, nlines, (int)NB, NC,
                                                                  NB * NC, NC);
+        launched(c);
         VC_CUDA(c, cudaGetLastError());
     }
     {
@@ -231,9 +236,11 @@ int run_ft(vc_ctx* c) {
         const int64_t nlines = NB * NC;
         int blocks = (int)std::min<int64_t>((nlines + 255) / 256, (int64_t)c->num_sms * 8);
         int32_t* stack = reinterpret_cast<int32_t*>(A);  // pass-1 output is dead now
+        Region r(c, "ft_envelope_x");
         ft_envelope_kernel<true><<<blocks, 256, 0, c->stream>>>(B, nullptr, ptr<int32_t>(c->ft_d2),
                                                                 ptr<int32_t>(c->ft_id), stack, nlines, (int)NA,
                                                                 NB * NC, 0, NB * NC);
+        launched(c);
         VC_CUDA(c, cudaGetLastError());
     }
     c->ft_valid = true;

@@ -7,7 +7,9 @@
 
 #include <cstdint>
 #include <cstdio>
+#include <map>
 #include <string>
+#include <vector>
 
 #include "../../include/voxelcore_gb300.h"
 
@@ -95,6 +97,18 @@ struct vc_ctx {
     vc::DevBuf rem_voff, rem_eoff, rem_foff;
     vc::DevBuf rem_vts, rem_edges, rem_tris;
     vc::DevBuf uf_parent, euler_tmp;
+
+    // instrumentation: kernels launched, and optional CUDA-event timing of
+    // named regions on the context stream (resolved at the next sync)
+    int64_t launches = 0;
+    bool timing = false;
+    struct PendingTimer {
+        std::string name;
+        cudaEvent_t a, b;
+    };
+    std::vector<PendingTimer> pending;
+    std::vector<cudaEvent_t> event_pool;
+    std::map<std::string, std::pair<double, int64_t>> timers;  // name -> (ms, count)
 };
 
 namespace vc {
@@ -123,6 +137,18 @@ int sync_check(vc_ctx* c);
 int copy_out(vc_ctx* c, void* dst, const void* src, size_t bytes, int mem);
 int copy_in(vc_ctx* c, void* dst, const void* src, size_t bytes, int mem);
 int* dev_err(vc_ctx* c);
+// Count kernel launches issued by the library on this context.
+inline void launched(vc_ctx* c, int n = 1) { c->launches += n; }
+// Resolve finished timing events into c->timers (called after a sync).
+void resolve_timers(vc_ctx* c);
+// RAII timing of a named region on the context stream (no-op when disabled).
+struct Region {
+    vc_ctx* c;
+    const char* name;
+    cudaEvent_t a = nullptr;
+    Region(vc_ctx* ctx, const char* n);
+    ~Region();
+};
 // Exclusive scan helpers (device-wide), results and optional total on device.
 // out may alias in.  total_dev may be null.
 int scan_exclusive_i32(vc_ctx* c, const int32_t* in, int32_t* out, int64_t n, int64_t* total_dev);

@@ -154,10 +154,12 @@ int run_remaining(vc_ctx* c, vc_rem_sizes* sizes) {
     VC_TRY(ensure_n<int32_t>(c, c->rem_eoff, ne + 1));
     VC_TRY(ensure_n<int32_t>(c, c->rem_foff, nt + 1));
     VC_TRY(ensure_n<int64_t>(c, c->scratch2, 4));
+    Region stage(c, "stage_remaining");
     int32_t *pv = ptr<int32_t>(c->rem_voff), *pe = ptr<int32_t>(c->rem_eoff), *pf = ptr<int32_t>(c->rem_foff);
     rem_flags_kernel<<<grid_for(c, nv + ne + nt, 256), 256, 0, c->stream>>>(
         ptr<int32_t>(c->rm_v), ptr<int32_t>(c->rm_e), ptr<int32_t>(c->ref_e), ptr<int32_t>(c->rm_f), (int32_t)nv,
         (int32_t)ne, (int32_t)nt, pv, pe, pf);
+    launched(c);
     VC_CUDA(c, cudaGetLastError());
     int64_t* tot = ptr<int64_t>(c->scratch2);
     VC_TRY(scan_exclusive_i32(c, pv, pv, nv, tot + 0));
@@ -173,6 +175,7 @@ int run_remaining(vc_ctx* c, vc_rem_sizes* sizes) {
         ptr<int32_t>(c->rm_v), ptr<int32_t>(c->rm_e), ptr<int32_t>(c->ref_e), ptr<int32_t>(c->rm_f), (int32_t)nv,
         (int32_t)ne, (int32_t)nt, pv, pe, pf, ptr<float>(c->vts), ptr<int2>(c->edges), ptr<int32_t>(c->tris),
         ptr<float>(c->rem_vts), ptr<int2>(c->rem_edges), ptr<int32_t>(c->rem_tris));
+    launched(c);
     VC_CUDA(c, cudaGetLastError());
     c->rem = vc_rem_sizes{h[0], h[1], h[2]};
     c->rem_valid = true;
@@ -193,14 +196,19 @@ int run_euler_remaining(vc_ctx* c, vc_euler_info* out) {
     euler_mark_kernel<<<grid_for(c, ne + nt, 256), 256, 0, c->stream>>>(
         ptr<int32_t>(c->rm_e), ptr<int32_t>(c->ref_e), ptr<int32_t>(c->rm_f), ptr<int32_t>(c->tri_edges),
         (int32_t)ne, (int32_t)nt, mark);
+    launched(c);
     count_kernel<<<grid_for(c, ne, 256), 256, 0, c->stream>>>(mark, ne, cnt);
+    launched(c);
     int32_t* parent = ptr<int32_t>(c->uf_parent);
     if (nvr > 0) {
         uf_init_kernel<<<grid_for(c, nvr, 256), 256, 0, c->stream>>>(parent, (int32_t)nvr);
+        launched(c);
         uf_union_kernel<<<grid_for(c, ne, 256), 256, 0, c->stream>>>(mark, ptr<int2>(c->edges),
                                                                       ptr<int32_t>(c->rem_voff), (int32_t)ne, parent,
                                                                       dev_err(c));
+        launched(c);
         uf_roots_kernel<<<grid_for(c, nvr, 256), 256, 0, c->stream>>>(parent, (int32_t)nvr, cnt + 1);
+        launched(c);
     }
     VC_CUDA(c, cudaGetLastError());
     unsigned long long h[2];

@@ -136,9 +136,11 @@ int run_sites(vc_ctx* c, int64_t* n_sites) {
     VC_TRY(ensure_n<int32_t>(c, c->site_count, nvox));
     VC_TRY(ensure_n<int32_t>(c, c->site_id_lat, nlat));
     VC_TRY(ensure_n<int64_t>(c, c->scratch2, 4));
+    Region stage(c, "stage_sites");
     Vol v{ptr<uint8_t>(c->occ), c->X, c->Y, c->Z};
     int32_t* cnt = ptr<int32_t>(c->site_count);
     sites_count_kernel<<<grid_for(c, nvox, 256), 256, 0, c->stream>>>(v, cnt);
+    launched(c);
     VC_CUDA(c, cudaGetLastError());
     int64_t* total = ptr<int64_t>(c->scratch2);
     VC_TRY(scan_exclusive_i32(c, cnt, cnt, nvox, total));
@@ -149,6 +151,7 @@ int run_sites(vc_ctx* c, int64_t* n_sites) {
     VC_CUDA(c, cudaMemsetAsync(c->site_id_lat.p, 0xff, (size_t)nlat * sizeof(int32_t), c->stream));
     sites_emit_kernel<<<grid_for(c, nvox, 256), 256, 0, c->stream>>>(v, cnt, ptr<float>(c->site_xyz),
                                                                        ptr<int32_t>(c->site_id_lat));
+    launched(c);
     VC_CUDA(c, cudaGetLastError());
     c->n_sites = n;
     if (n_sites) *n_sites = n;

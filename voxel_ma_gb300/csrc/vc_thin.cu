@@ -361,6 +361,7 @@ int run_thin(vc_ctx* c, float f_t, float l_t, vc_thin_stats* stats) {
     if (!c->cc_finalized || !c->meas_valid) return VC_ERR_STATE;
     VC_TRY(ensure_n<float>(c, c->thr, 2));
     set_thr_kernel<<<1, 1, 0, c->stream>>>(ptr<float>(c->thr), f_t, l_t);
+    launched(c);
     VC_CUDA(c, cudaGetLastError());
     return run_thin_with_device_thr(c, stats);
 }
@@ -372,6 +373,7 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats) {
     const int64_t nv = c->nv, ne = c->ne, nt = c->nt;
     if (nv + ne >= INT32_MAX) return VC_ERR_ARG;
     const int64_t qcap = nv + ne + 1;
+    Region stage(c, "stage_thin");
     VC_TRY(ensure_n<int32_t>(c, c->rm_f, nt));
     VC_TRY(ensure_n<int32_t>(c, c->rm_e, ne));
     VC_TRY(ensure_n<int32_t>(c, c->rm_v, nv));
@@ -414,12 +416,15 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats) {
     thin_init_kernel<<<grid_for(c, nv + ne + nt, 256), 256, 0, c->stream>>>(
         A.ve_off, A.ef_off, (int32_t)nv, (int32_t)ne, (int32_t)nt, A.rm_f, A.rm_e, A.rm_v, A.ref_e, A.ref_v,
         A.trig_e, A.trig_v);
+    launched(c);
     int32_t* flag = ptr<int32_t>(c->scratch2);
     int32_t* pos = flag + (nv + ne + 1);
     gen0_flags_kernel<<<grid_for(c, nv + ne, 256), 256, 0, c->stream>>>(A, (int32_t)nv, (int32_t)ne, flag);
+    launched(c);
     VC_CUDA(c, cudaMemsetAsync(ctl, 0, 16 * sizeof(int64_t), c->stream));
     VC_TRY(scan_exclusive_i32(c, flag, pos, nv + ne, ctl + 0));
     gen0_write_kernel<<<grid_for(c, nv + ne, 256), 256, 0, c->stream>>>(A, (int32_t)nv, (int32_t)ne, flag, pos);
+    launched(c);
     VC_CUDA(c, cudaGetLastError());
     // persistent cooperative launch: every block resident
     int per_sm = 0;
@@ -429,8 +434,12 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats) {
     VC_TRY(ensure_n<int64_t>(c, c->blk_cnt, G));
     A.blk_cnt = ptr<int64_t>(c->blk_cnt);
     void* args[] = {&A};
-    VC_CUDA(c, cudaLaunchCooperativeKernel((void*)thin_generations_kernel, dim3(G), dim3(kThreads), args, 0,
-                                           c->stream));
+    {
+        Region r(c, "thin_generations");
+        VC_CUDA(c, cudaLaunchCooperativeKernel((void*)thin_generations_kernel, dim3(G), dim3(kThreads), args, 0,
+                                               c->stream));
+        launched(c);
+    }
     int64_t h[5];
     VC_CUDA(c, cudaMemcpyAsync(h, ctl, 5 * sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
     int s = sync_check(c);
@@ -451,6 +460,7 @@ int get_thin_flags(vc_ctx* c, uint8_t* kv, uint8_t* ke, uint8_t* kf, uint8_t* re
     thin_flags_kernel<<<grid_for(c, nv + ne + nt, 256), 256, 0, c->stream>>>(
         ptr<int32_t>(c->rm_v), ptr<int32_t>(c->rm_e), ptr<int32_t>(c->ref_e), ptr<int32_t>(c->rm_f), (int32_t)nv,
         (int32_t)ne, (int32_t)nt, dkv, dke, dkf, dre);
+    launched(c);
     VC_CUDA(c, cudaGetLastError());
     VC_TRY(copy_out(c, kv, dkv, nv, mem));
     VC_TRY(copy_out(c, ke, dke, ne, mem));

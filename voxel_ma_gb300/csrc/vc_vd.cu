@@ -312,12 +312,17 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes) {
     VC_TRY(ensure_n<int32_t>(c, c->vd_foff, N));
     VC_TRY(ensure_n<int64_t>(c, c->scratch2, 4));
     VC_TRY(ensure_n<int32_t>(c, c->vd_bbox, 8));
+    Region stage(c, "stage_vd");
     Grid g{ptr<uint8_t>(c->occ), ptr<int32_t>(c->ft_id), c->X, c->Y, c->Z, NB, NC};
     uint8_t* flags = ptr<uint8_t>(c->vd_flags);
     int32_t* voff = ptr<int32_t>(c->vd_voff);
     int32_t* eoff = ptr<int32_t>(c->vd_eoff);
     int32_t* foff = ptr<int32_t>(c->vd_foff);
+    {
+    Region r(c, "vd_flags");
     vd_flags_kernel<<<grid_for(c, N, 256), 256, 0, c->stream>>>(g, flags, voff, eoff, foff, N);
+    launched(c);
+    }
     VC_CUDA(c, cudaGetLastError());
     int64_t* tot = ptr<int64_t>(c->scratch2);
     VC_TRY(scan_exclusive_i32(c, voff, voff, N, tot + 0));
@@ -342,15 +347,22 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes) {
     VC_TRY(ensure_n<int2>(c, c->vd_face_sites, nface));
     int32_t* bbox = ptr<int32_t>(c->vd_bbox);
     init_bbox_kernel<<<1, 32, 0, c->stream>>>(bbox);
+    launched(c);
     const float* sxyz = ptr<float>(c->site_xyz);
+    {
+    Region r(c, "vd_emit");
     vd_vertices_kernel<<<grid_for(c, N, 256), 256, 0, c->stream>>>(g, flags, voff, sxyz, ptr<float>(c->vts),
                                                                     ptr<float>(c->vm), bbox, N);
+    launched(c);
     vd_edges_kernel<<<grid_for(c, N, 256), 256, 0, c->stream>>>(g, flags, voff, eoff, sxyz, ptr<int2>(c->edges),
                                                                  ptr<float>(c->em), N);
+    launched(c);
     vd_faces_kernel<<<grid_for(c, N, 256), 256, 0, c->stream>>>(
         g, flags, voff, eoff, foff, sxyz, (int32_t)ne_axis, ptr<int2>(c->edges), ptr<float>(c->em),
         ptr<int32_t>(c->tris), ptr<int32_t>(c->tri_edges), ptr<float>(c->fm), ptr<int32_t>(c->vd_tri_face),
         ptr<int2>(c->vd_face_sites), N);
+    launched(c);
+    }
     VC_CUDA(c, cudaGetLastError());
     int32_t hb[6];
     VC_CUDA(c, cudaMemcpyAsync(hb, bbox, 6 * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
