@@ -63,6 +63,8 @@ def make_workload(name: str, device=None):
     from voxel_ma_gb300 import volumes
     if name == "grf512":
         return volumes.grf(512, sigma=6.0, seed=0, device=device), "grf512_sigma6_level0"
+    if name == "grf192":
+        return volumes.grf(192, sigma=6.0, seed=0, device=device), "grf192_sigma6_level0"
     if name == "grf256":
         return volumes.grf(256, sigma=6.0, seed=0, device=device), "grf256_sigma6_level0"
     if name == "spheres256":
