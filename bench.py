@@ -129,12 +129,27 @@ class ClockSampler:
     def __init__(self, device_index: int):
         self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
         self.p = None
+        self.t_start = None
         try:
             self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
                                        "-lms", "200", "-i", str(device_index)], stdout=self.f,
                                       stderr=subprocess.DEVNULL)
         except Exception:
             self.p = None
+
+    def wait_ready(self, timeout: float = 20.0):
+        """Block until the sampler has written its first line, so that its
+        start-up (which can stall driver calls) happens before timing."""
+        t0 = time.time()
+        while self.p is not None and time.time() - t0 < timeout:
+            if os.path.getsize(self.f.name) > 0:
+                break
+            time.sleep(0.05)
+
+    def mark(self):
+        """Only samples taken after mark() are summarised."""
+        self.f.flush()
+        self.t_start = os.path.getsize(self.f.name)
 
     def stop(self):
         if self.p is not None:
@@ -146,7 +161,11 @@ class ClockSampler:
         self.f.flush()
         rows = []
         try:
-            for line in open(self.f.name):
+            fh = open(self.f.name)
+            if self.t_start:
+                fh.seek(self.t_start)
+                fh.readline()  # possibly partial line
+            for line in fh:
                 parts = [x.strip() for x in line.split(",")]
                 if len(parts) >= 9 and parts[1].replace(".", "").isdigit():
                     rows.append(parts)
@@ -223,13 +242,15 @@ def run_gpu(args):
         ctx.sync()
 
     # ---- device-resident value ------------------------------------------
+    clocks = ClockSampler(local)
+    clocks.wait_ready()
     for _ in range(args.warmup):
         r = ctx.run_plain(occ_dev, args.t)
     barrier()
     ctx.set_timing(True)
     ctx.reset_timings()
     launches0 = ctx.launch_count()
-    clocks = ClockSampler(local)
+    clocks.mark()
     evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
     evs[0].record(stream)
     for k in range(args.steps):

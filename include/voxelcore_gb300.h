@@ -154,6 +154,14 @@ typedef struct {
 } vc_plain_result;
 int vc_run_plain(vc_ctx* ctx, const uint8_t* occ, int X, int Y, int Z, int mem, double t, vc_plain_result* out);
 
+/* ---- diagnostics ---------------------------------------------------------
+ * Per-generation trace of the thinning kernel: with cap > 0 the next vc_thin
+ * records, for up to `cap` generations, {items, t_phaseA, t_phaseB, t_phaseC}
+ * (GPU global timer, ns).  blocks_per_sm overrides the persistent grid's
+ * blocks per SM (0 = default).                                             */
+int vc_debug_thin_trace(vc_ctx* ctx, int cap, int blocks_per_sm);
+int vc_debug_get_thin_trace(vc_ctx* ctx, int64_t* out, int cap, int* ngen);
+
 #ifdef __cplusplus
 }
 #endif

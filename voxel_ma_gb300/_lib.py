@@ -72,6 +72,8 @@ SIGNATURES = {
     "vc_remaining": (c_int, [c_vp, ctypes.POINTER(RemSizes)]),
     "vc_get_remaining": (c_int, [c_vp, c_vp, c_vp, c_vp, c_int]),
     "vc_euler_remaining": (c_int, [c_vp, ctypes.POINTER(EulerInfo)]),
+    "vc_debug_thin_trace": (c_int, [c_vp, c_int, c_int]),
+    "vc_debug_get_thin_trace": (c_int, [c_vp, c_vp, c_int, ctypes.POINTER(c_int)]),
     "vc_run_plain": (c_int, [c_vp, c_vp, c_int, c_int, c_int, c_int, ctypes.c_double, ctypes.POINTER(PlainResult)]),
 }
 

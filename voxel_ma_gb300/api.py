@@ -111,6 +111,17 @@ class Context:
             out[nm] = (float(ms[i]), int(cnt[i]))
         return out
 
+    def debug_thin_trace(self, cap: int = 4096, blocks_per_sm: int = 0):
+        self.check(self.lib.vc_debug_thin_trace(self.h, cap, blocks_per_sm), "vc_debug_thin_trace")
+
+    def thin_trace(self):
+        n = ctypes.c_int()
+        self.check(self.lib.vc_debug_get_thin_trace(self.h, None, 0, ctypes.byref(n)), "vc_debug_get_thin_trace")
+        out = np.zeros((max(n.value, 1), 4), np.int64)
+        self.check(self.lib.vc_debug_get_thin_trace(self.h, out.ctypes.data_as(ctypes.c_void_p), n.value,
+                                                     ctypes.byref(n)), "vc_debug_get_thin_trace")
+        return out[: n.value]
+
     def _out(self, shape, dtype, device: bool):
         if device:
             import torch

@@ -265,8 +265,9 @@ int vc_ctx_destroy(vc_ctx* c) {
                          &c->vd_eoff, &c->vd_foff, &c->vd_tri_face, &c->vd_face_sites, &c->vd_vm, &c->vd_bbox,
                          &c->vts, &c->edges_in, &c->edges, &c->tris, &c->tri_edges, &c->ve_off, &c->ve_ids,
                          &c->ef_off, &c->ef_ids, &c->hash_keys, &c->hash_pos, &c->hash_id, &c->side_slot,
-                         &c->vm, &c->em, &c->fm, &c->rm_f, &c->rm_e, &c->rm_v, &c->ref_e, &c->ref_v,
-                         &c->trig_e, &c->trig_v, &c->q0, &c->q1, &c->child, &c->child_cnt, &c->blk_cnt,
+                         &c->vm, &c->em, &c->fm, &c->face_rec, &c->edge_rec, &c->vert_rec,
+                         &c->q0, &c->q1, &c->cand, &c->child, &c->child_cnt, &c->cells, &c->blk_cnt, &c->keep_v,
+                         &c->keep_e, &c->keep_f, &c->removed_e, &c->trace,
                          &c->thr, &c->rem_voff, &c->rem_eoff, &c->rem_foff, &c->rem_vts, &c->rem_edges,
                          &c->rem_tris, &c->uf_parent, &c->euler_tmp};
     for (auto* b : all) free_buf(c, *b);

@@ -89,8 +89,12 @@ struct vc_ctx {
     // thinning state
     bool thin_valid = false;
     vc_thin_stats thin_stats{};
-    vc::DevBuf rm_f, rm_e, rm_v, ref_e, ref_v, trig_e, trig_v;
-    vc::DevBuf q0, q1, child, child_cnt, blk_cnt, thr;
+    vc::DevBuf face_rec, edge_rec, vert_rec;  // 32-byte per-cell thinning records
+    vc::DevBuf q0, q1, cand, child, child_cnt, cells, blk_cnt, thr;
+    vc::DevBuf keep_v, keep_e, keep_f, removed_e;  // uint8 survivor flags of the last thinning
+    vc::DevBuf trace;           // optional per-generation trace of the thinning kernel
+    int trace_cap = 0, trace_gens = 0;
+    int thin_blocks_per_sm = 0;  // 0 = library default
     // remaining complex
     bool rem_valid = false;
     vc_rem_sizes rem{};

@@ -15,44 +15,40 @@
 namespace vc {
 namespace {
 
-constexpr int32_t kAlive = INT32_MAX;
-
-__global__ void rem_flags_kernel(const int32_t* __restrict__ rm_v, const int32_t* __restrict__ rm_e,
-                                 const int32_t* __restrict__ ref_e, const int32_t* __restrict__ rm_f, int32_t nv,
-                                 int32_t ne, int32_t nt, int32_t* __restrict__ fv, int32_t* __restrict__ fe,
-                                 int32_t* __restrict__ ff) {
+__global__ void rem_flags_kernel(const uint8_t* __restrict__ kv, const uint8_t* __restrict__ ke,
+                                 const uint8_t* __restrict__ kf, int32_t nv, int32_t ne, int32_t nt,
+                                 int32_t* __restrict__ fv, int32_t* __restrict__ fe, int32_t* __restrict__ ff) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (int64_t)nv + ne + nt; i += stride) {
-        if (i < nv) fv[i] = rm_v[i] == kAlive;
-        else if (i < (int64_t)nv + ne) fe[i - nv] = rm_e[i - nv] == kAlive && ref_e[i - nv] == 0;
-        else ff[i - nv - ne] = rm_f[i - nv - ne] == kAlive;
+        if (i < nv) fv[i] = kv[i];
+        else if (i < (int64_t)nv + ne) fe[i - nv] = ke[i - nv];
+        else ff[i - nv - ne] = kf[i - nv - ne];
     }
 }
 
-// After the exclusive scans: fv/fe/ff hold output positions; the keep test is
-// recomputed from the removal state.
-__global__ void rem_write_kernel(const int32_t* __restrict__ rm_v, const int32_t* __restrict__ rm_e,
-                                 const int32_t* __restrict__ ref_e, const int32_t* __restrict__ rm_f, int32_t nv,
-                                 int32_t ne, int32_t nt, const int32_t* __restrict__ pv, const int32_t* __restrict__ pe,
+// After the exclusive scans pv/pe/pf hold output positions.
+__global__ void rem_write_kernel(const uint8_t* __restrict__ kv, const uint8_t* __restrict__ ke,
+                                 const uint8_t* __restrict__ kf, int32_t nv, int32_t ne, int32_t nt,
+                                 const int32_t* __restrict__ pv, const int32_t* __restrict__ pe,
                                  const int32_t* __restrict__ pf, const float* __restrict__ vts,
                                  const int2* __restrict__ edges, const int32_t* __restrict__ tris,
                                  float* __restrict__ ovts, int2* __restrict__ oedges, int32_t* __restrict__ otris) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (int64_t)nv + ne + nt; i += stride) {
         if (i < nv) {
-            if (rm_v[i] != kAlive) continue;
+            if (!kv[i]) continue;
             const int64_t o = pv[i];
             ovts[3 * o + 0] = vts[3 * i + 0];
             ovts[3 * o + 1] = vts[3 * i + 1];
             ovts[3 * o + 2] = vts[3 * i + 2];
         } else if (i < (int64_t)nv + ne) {
             const int64_t e = i - nv;
-            if (!(rm_e[e] == kAlive && ref_e[e] == 0)) continue;
+            if (!ke[e]) continue;
             const int2 ev = edges[e];
             oedges[pe[e]] = make_int2(pv[ev.x], pv[ev.y]);
         } else {
             const int64_t f = i - nv - ne;
-            if (rm_f[f] != kAlive) continue;
+            if (!kf[f]) continue;
             const int64_t o = pf[f];
             otris[3 * o + 0] = pv[tris[3 * f + 2]];
             otris[3 * o + 1] = pv[tris[3 * f + 0]];
@@ -63,16 +59,16 @@ __global__ void rem_write_kernel(const int32_t* __restrict__ rm_v, const int32_t
 
 // Euler: mark every finalized edge that is a remaining edge or a side of a
 // remaining face.
-__global__ void euler_mark_kernel(const int32_t* __restrict__ rm_e, const int32_t* __restrict__ ref_e,
-                                  const int32_t* __restrict__ rm_f, const int32_t* __restrict__ tri_edges, int32_t ne,
-                                  int32_t nt, int32_t* __restrict__ mark) {
+__global__ void euler_mark_kernel(const uint8_t* __restrict__ ke, const uint8_t* __restrict__ kf,
+                                  const int32_t* __restrict__ tri_edges, int32_t ne, int32_t nt,
+                                  int32_t* __restrict__ mark) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (int64_t)ne + nt; i += stride) {
         if (i < ne) {
-            if (rm_e[i] == kAlive && ref_e[i] == 0) mark[i] = 1;
+            if (ke[i]) mark[i] = 1;
         } else {
             const int64_t f = i - ne;
-            if (rm_f[f] != kAlive) continue;
+            if (!kf[f]) continue;
             mark[tri_edges[3 * f + 0]] = 1;
             mark[tri_edges[3 * f + 1]] = 1;
             mark[tri_edges[3 * f + 2]] = 1;
@@ -157,8 +153,8 @@ int run_remaining(vc_ctx* c, vc_rem_sizes* sizes) {
     Region stage(c, "stage_remaining");
     int32_t *pv = ptr<int32_t>(c->rem_voff), *pe = ptr<int32_t>(c->rem_eoff), *pf = ptr<int32_t>(c->rem_foff);
     rem_flags_kernel<<<grid_for(c, nv + ne + nt, 256), 256, 0, c->stream>>>(
-        ptr<int32_t>(c->rm_v), ptr<int32_t>(c->rm_e), ptr<int32_t>(c->ref_e), ptr<int32_t>(c->rm_f), (int32_t)nv,
-        (int32_t)ne, (int32_t)nt, pv, pe, pf);
+        ptr<uint8_t>(c->keep_v), ptr<uint8_t>(c->keep_e), ptr<uint8_t>(c->keep_f), (int32_t)nv, (int32_t)ne,
+        (int32_t)nt, pv, pe, pf);
     launched(c);
     VC_CUDA(c, cudaGetLastError());
     int64_t* tot = ptr<int64_t>(c->scratch2);
@@ -172,8 +168,8 @@ int run_remaining(vc_ctx* c, vc_rem_sizes* sizes) {
     VC_TRY(ensure_n<int2>(c, c->rem_edges, h[1]));
     VC_TRY(ensure_n<int32_t>(c, c->rem_tris, 3 * h[2]));
     rem_write_kernel<<<grid_for(c, nv + ne + nt, 256), 256, 0, c->stream>>>(
-        ptr<int32_t>(c->rm_v), ptr<int32_t>(c->rm_e), ptr<int32_t>(c->ref_e), ptr<int32_t>(c->rm_f), (int32_t)nv,
-        (int32_t)ne, (int32_t)nt, pv, pe, pf, ptr<float>(c->vts), ptr<int2>(c->edges), ptr<int32_t>(c->tris),
+        ptr<uint8_t>(c->keep_v), ptr<uint8_t>(c->keep_e), ptr<uint8_t>(c->keep_f), (int32_t)nv, (int32_t)ne,
+        (int32_t)nt, pv, pe, pf, ptr<float>(c->vts), ptr<int2>(c->edges), ptr<int32_t>(c->tris),
         ptr<float>(c->rem_vts), ptr<int2>(c->rem_edges), ptr<int32_t>(c->rem_tris));
     launched(c);
     VC_CUDA(c, cudaGetLastError());
@@ -194,8 +190,8 @@ int run_euler_remaining(vc_ctx* c, vc_euler_info* out) {
     VC_CUDA(c, cudaMemsetAsync(mark, 0, (ne + 1) * sizeof(int32_t), c->stream));
     VC_CUDA(c, cudaMemsetAsync(cnt, 0, 2 * sizeof(unsigned long long), c->stream));
     euler_mark_kernel<<<grid_for(c, ne + nt, 256), 256, 0, c->stream>>>(
-        ptr<int32_t>(c->rm_e), ptr<int32_t>(c->ref_e), ptr<int32_t>(c->rm_f), ptr<int32_t>(c->tri_edges),
-        (int32_t)ne, (int32_t)nt, mark);
+        ptr<uint8_t>(c->keep_e), ptr<uint8_t>(c->keep_f), ptr<int32_t>(c->tri_edges), (int32_t)ne, (int32_t)nt,
+        mark);
     launched(c);
     count_kernel<<<grid_for(c, ne, 256), 256, 0, c->stream>>>(mark, ne, cnt);
     launched(c);

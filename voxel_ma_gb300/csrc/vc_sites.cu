@@ -16,7 +16,7 @@ namespace {
 
 // Corner c of a voxel as the lattice offset {0,1}^3 from the voxel's lowest
 // corner, in the reference's corner numbering (surfacing.h:74-96).
-__constant__ int8_t kCornerOff[8][3] = {{1, 0, 0}, {1, 1, 0}, {0, 0, 0}, {0, 1, 0},
+__device__ constexpr int8_t kCornerOff[8][3] = {{1, 0, 0}, {1, 1, 0}, {0, 0, 0}, {0, 1, 0},
                                         {1, 0, 1}, {1, 1, 1}, {0, 0, 1}, {0, 1, 1}};
 // Face-neighbour offsets in sweep order (surfacing.h:170-179).
 __constant__ int8_t kNbOff[6][3] = {{-1, 0, 0}, {1, 0, 0}, {0, -1, 0}, {0, 1, 0}, {0, 0, -1}, {0, 0, 1}};
@@ -51,30 +51,45 @@ __device__ __forceinline__ int nb_bit(uint32_t m, int dx, int dy, int dz) {
     return (m >> ((dx + 1) * 9 + (dy + 1) * 3 + (dz + 1))) & 1;
 }
 
+// 27-bit in-box mask of the same neighbourhood.
+__device__ __forceinline__ uint32_t inbox_nbhd(const Vol& v, int i, int j, int k) {
+    const uint32_t xm = (i > 0 ? 1u : 0u) | 2u | (i < v.X - 1 ? 4u : 0u);
+    const uint32_t ym = (j > 0 ? 1u : 0u) | 2u | (j < v.Y - 1 ? 4u : 0u);
+    const uint32_t zm = (k > 0 ? 1u : 0u) | 2u | (k < v.Z - 1 ? 4u : 0u);
+    uint32_t m = 0;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b)
+            if (((xm >> a) & 1u) && ((ym >> b) & 1u)) m |= zm << (a * 9 + b * 3);
+    return m;
+}
+
+// The 2x2x2 block of voxels around corner c of the voxel, as 8 bits:
+// bit q = qx<<2 | qy<<1 | qz is the voxel at offset (ox-1+qx, oy-1+qy,
+// oz-1+qz), i.e. neighbourhood bit (ox+qx)*9 + (oy+qy)*3 + (oz+qz).
+__device__ __forceinline__ uint32_t block_bits(uint32_t m27, int ox, int oy, int oz) {
+    const uint32_t t = m27 >> (ox * 9 + oy * 3 + oz);
+    return (t & 3u) | ((t >> 1) & 0xCu) | ((t >> 5) & 0x30u) | ((t >> 6) & 0xC0u);
+}
+
 // Mask of the corners of voxel (i,j,k) that are first encountered there.
-__device__ __forceinline__ uint32_t new_corner_mask(const Vol& v, uint32_t nb, int i, int j, int k) {
+// Within a corner's block, the sweep meets first the in-box voxel of lowest
+// (qx,qy,qz) that differs from one of its three block neighbours; the corner
+// is new at (i,j,k) iff that voxel is (i,j,k) itself.
+__device__ __forceinline__ uint32_t new_corner_mask(uint32_t nb, uint32_t inb) {
     uint32_t res = 0;
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
         const int ox = kCornerOff[c][0], oy = kCornerOff[c][1], oz = kCornerOff[c][2];
-        // block voxel q = (qx,qy,qz) sits at offset (ox-1+qx, oy-1+qy, oz-1+qz) from (i,j,k)
+        const uint32_t P = block_bits(nb, ox, oy, oz);
+        const uint32_t M = block_bits(inb, ox, oy, oz);
+        const uint32_t sx = ((P >> 4) & 0x0Fu) | ((P << 4) & 0xF0u);
+        const uint32_t sy = ((P >> 2) & 0x33u) | ((P << 2) & 0xCCu);
+        const uint32_t sz = ((P >> 1) & 0x55u) | ((P << 1) & 0xAAu);
+        const uint32_t D = ((P ^ sx) | (P ^ sy) | (P ^ sz)) & M;
         const int own = ((1 - ox) << 2) | ((1 - oy) << 1) | (1 - oz);
-        int first = -1;
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            const int qx = (q >> 2) & 1, qy = (q >> 1) & 1, qz = q & 1;
-            const int dx = ox - 1 + qx, dy = oy - 1 + qy, dz = oz - 1 + qz;
-            const bool inb = (i + dx >= 0) && (i + dx < v.X) && (j + dy >= 0) && (j + dy < v.Y) &&
-                             (k + dz >= 0) && (k + dz < v.Z);
-            if (!inb || first >= 0) continue;
-            const int val = nb_bit(nb, dx, dy, dz);
-            // block neighbours: flip one of the three coordinates inside the block
-            const int vx = nb_bit(nb, ox - 1 + (qx ^ 1), dy, dz);
-            const int vy = nb_bit(nb, dx, oy - 1 + (qy ^ 1), dz);
-            const int vz = nb_bit(nb, dx, dy, oz - 1 + (qz ^ 1));
-            if (val != vx || val != vy || val != vz) first = q;
-        }
-        if (first == own) res |= 1u << c;
+        if (D && (__ffs(D) - 1) == own) res |= 1u << c;
     }
     return res;
 }
@@ -85,8 +100,8 @@ __global__ void sites_count_kernel(Vol v, int32_t* __restrict__ cnt) {
         const int k = (int)(t % v.Z);
         const int j = (int)((t / v.Z) % v.Y);
         const int i = (int)(t / ((int64_t)v.Z * v.Y));
-        uint32_t nb = load_nbhd(v, i, j, k);
-        cnt[t] = __popc(new_corner_mask(v, nb, i, j, k));
+        const uint32_t nb = load_nbhd(v, i, j, k);
+        cnt[t] = __popc(new_corner_mask(nb, inbox_nbhd(v, i, j, k)));
     }
 }
 
@@ -98,8 +113,8 @@ __global__ void sites_emit_kernel(Vol v, const int32_t* __restrict__ off, float*
         const int k = (int)(t % v.Z);
         const int j = (int)((t / v.Z) % v.Y);
         const int i = (int)(t / ((int64_t)v.Z * v.Y));
-        uint32_t nb = load_nbhd(v, i, j, k);
-        uint32_t mask = new_corner_mask(v, nb, i, j, k);
+        const uint32_t nb = load_nbhd(v, i, j, k);
+        const uint32_t mask = new_corner_mask(nb, inbox_nbhd(v, i, j, k));
         if (!mask) continue;
         int32_t o = off[t];
         const int cur = nb_bit(nb, 0, 0, 0);

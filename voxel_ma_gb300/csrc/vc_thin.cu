@@ -24,9 +24,21 @@
 //     the removed edge's two ends (ccthin.cpp:659-767), or the other end of
 //     an EV pair's edge (ccthin.cpp:610-636).
 // One persistent cooperative kernel runs all generations with three bounded
-// grid barriers per generation; the claims of generation g+1 are made while
-// generation g writes it.  Removal state is kept as the queue position of the
-// removing item (INT32_MAX = alive), so every check is position-exact.
+// grid barriers per generation:
+//   A (per item)  claims are checked, removals applied, counts decremented;
+//                 the decrement that takes a count from 2 to 1 lists its cell;
+//   B (per listed cell)  a cell still at 1 gives its child to the item at
+//                 its last-decrement position, in the cell's slot;
+//   C (per item)  children are written in order as generation g+1 and that
+//                 generation's claims are made.
+// Removal state is the queue position of the removing item (INT32_MAX =
+// alive), so every check is position-exact.
+//
+// Memory layout: the accesses are random, so every cell's static data and
+// thinning state share one 32-byte record (one DRAM sector per touch):
+//   face   {e0, e1, e2, fm, rm}
+//   edge   {v0, v1, em, ef_off, ef_cnt, rm, ref, trig}
+//   vertex {ve_off, ve_cnt, rm, ref, trig}
 #include "vc_internal.cuh"
 
 namespace vc {
@@ -35,61 +47,102 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int32_t kAlive = INT32_MAX;
 constexpr unsigned kFE = 0x80000000u;
+constexpr int32_t kEdgeBit = (int32_t)0x80000000u;
+
+struct __align__(32) FaceRec {
+    int32_t e0, e1, e2;
+    float fm;
+    int32_t rm;
+    int32_t pad0, pad1, pad2;
+};
+struct __align__(32) EdgeRec {
+    int32_t v0, v1;
+    float em;
+    int32_t ef_off, ef_cnt;
+    int32_t rm, ref, trig;
+};
+struct __align__(32) VertRec {
+    int32_t ve_off, ve_cnt;
+    int32_t rm, ref, trig;
+    int32_t pad0, pad1, pad2;
+};
+static_assert(sizeof(FaceRec) == 32 && sizeof(EdgeRec) == 32 && sizeof(VertRec) == 32, "record size");
 
 struct ThinArgs {
-    const int2* edges;
-    const int32_t* tri_edges;
-    const int32_t* ve_off;
+    FaceRec* F;
+    EdgeRec* E;
+    VertRec* V;
     const int32_t* ve_ids;
-    const int32_t* ef_off;
     const int32_t* ef_ids;
-    const float* em;
-    const float* fm;
     const float* thr;  // [0] f_t, [1] l_t
-    int32_t* rm_f;
-    int32_t* rm_e;
-    int32_t* rm_v;
-    int32_t* ref_e;
-    int32_t* ref_v;
-    int32_t* trig_e;
-    int32_t* trig_v;
     int2* qa;
     int2* qb;
-    int2* child;
-    uint8_t* child_cnt;
-    int64_t* blk_cnt;
+    int4* cand;            // per item: the cells it decremented (-1 = none)
+    int2* child;           // per item: up to 4 children, by slot
+    unsigned* child_mask;  // per item one byte (4 items per word): bit s = child in slot s
+    int32_t* cells;        // cells whose count reached 1 in this generation (kEdgeBit: edge)
+    int* ncells;           // [2] list lengths, by generation parity
+    int64_t* blk_cnt;      // [2 * G] children per block, by generation parity
     unsigned* bar;
     int* err;
     int64_t* ctl;  // [0] gen-0 size; out: [1] pushes, [2] processed, [3] skipped, [4] generations
     unsigned long long spin_limit;
+    int64_t* trace;  // optional: per generation {items, t_A, t_B, t_C} (global timer, ns)
+    int trace_cap;
 };
+
+__device__ __forceinline__ int64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return (int64_t)t;
+}
 
 __device__ __forceinline__ int2 make_fe(int32_t f, int32_t e) { return make_int2((int32_t)((unsigned)f | kFE), e); }
 __device__ __forceinline__ int2 make_ev(int32_t e, int32_t v) { return make_int2(e, v); }
 __device__ __forceinline__ bool is_fe(int2 it) { return ((unsigned)it.x & kFE) != 0; }
 __device__ __forceinline__ int32_t idx0(int2 it) { return (int32_t)((unsigned)it.x & ~kFE); }
 
-__device__ __forceinline__ int2 ld_item(const int2* p) {
-    return __ldcg(p);
-}
-
-__global__ void thin_init_kernel(const int32_t* __restrict__ ve_off, const int32_t* __restrict__ ef_off, int32_t nv,
-                                 int32_t ne, int32_t nt, int32_t* rm_f, int32_t* rm_e, int32_t* rm_v, int32_t* ref_e,
-                                 int32_t* ref_v, int32_t* trig_e, int32_t* trig_v) {
+// Build the records from the finalized complex (CSR) and the measures, and
+// reset the thinning state.
+__global__ void build_records_kernel(const int2* __restrict__ edges, const int32_t* __restrict__ tri_edges,
+                                     const int32_t* __restrict__ ve_off, const int32_t* __restrict__ ef_off,
+                                     const float* __restrict__ em, const float* __restrict__ fm, int32_t nv,
+                                     int32_t ne, int32_t nt, FaceRec* F, EdgeRec* E, VertRec* V) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     const int64_t n = (int64_t)nv + ne + nt;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        if (i < ne) {
-            ref_e[i] = ef_off[i + 1] - ef_off[i];
-            rm_e[i] = kAlive;
-            trig_e[i] = -1;
-        } else if (i < (int64_t)ne + nv) {
-            const int64_t v = i - ne;
-            ref_v[v] = ve_off[v + 1] - ve_off[v];
-            rm_v[v] = kAlive;
-            trig_v[v] = -1;
+        if (i < nt) {
+            FaceRec r;
+            r.e0 = tri_edges[3 * i];
+            r.e1 = tri_edges[3 * i + 1];
+            r.e2 = tri_edges[3 * i + 2];
+            r.fm = fm[i];
+            r.rm = kAlive;
+            r.pad0 = r.pad1 = r.pad2 = 0;
+            F[i] = r;
+        } else if (i < (int64_t)nt + ne) {
+            const int64_t e = i - nt;
+            EdgeRec r;
+            const int2 ev = edges[e];
+            r.v0 = ev.x;
+            r.v1 = ev.y;
+            r.em = em[e];
+            r.ef_off = ef_off[e];
+            r.ef_cnt = ef_off[e + 1] - ef_off[e];
+            r.rm = kAlive;
+            r.ref = r.ef_cnt;
+            r.trig = -1;
+            E[e] = r;
         } else {
-            rm_f[i - ne - nv] = kAlive;
+            const int64_t v = i - nt - ne;
+            VertRec r;
+            r.ve_off = ve_off[v];
+            r.ve_cnt = ve_off[v + 1] - ve_off[v];
+            r.rm = kAlive;
+            r.ref = r.ve_cnt;
+            r.trig = -1;
+            r.pad0 = r.pad1 = r.pad2 = 0;
+            V[v] = r;
         }
     }
 }
@@ -102,10 +155,11 @@ __global__ void gen0_flags_kernel(ThinArgs A, int32_t nv, int32_t ne, int32_t* _
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (int64_t)ne + nv; i += stride) {
         int32_t ok = 0;
         if (i < ne) {
-            if (A.ref_e[i] == 1) ok = A.fm[A.ef_ids[A.ef_off[i]]] < f_t;
+            const EdgeRec& r = A.E[i];
+            if (r.ref == 1) ok = A.F[A.ef_ids[r.ef_off]].fm < f_t;
         } else {
-            const int64_t v = i - ne;
-            if (A.ref_v[v] == 1) ok = A.em[A.ve_ids[A.ve_off[v]]] < l_t;
+            const VertRec& r = A.V[i - ne];
+            if (r.ref == 1) ok = A.E[A.ve_ids[r.ve_off]].em < l_t;
         }
         flag[i] = ok;
     }
@@ -118,34 +172,45 @@ __global__ void gen0_write_kernel(ThinArgs A, int32_t nv, int32_t ne, const int3
         if (!flag[i]) continue;
         const int32_t p = pos[i];
         if (i < ne) {
-            const int32_t f = A.ef_ids[A.ef_off[i]];
+            const int32_t f = A.ef_ids[A.E[i].ef_off];
             A.qa[p] = make_fe(f, (int32_t)i);
-            atomicMin(&A.rm_f[f], p);
+            atomicMin(&A.F[f].rm, p);
         } else {
             const int32_t v = (int32_t)(i - ne);
-            const int32_t e = A.ve_ids[A.ve_off[v]];
+            const int32_t e = A.ve_ids[A.V[v].ve_off];
             A.qa[p] = make_ev(e, v);
-            atomicMin(&A.rm_e[e], p);
+            atomicMin(&A.E[e].rm, p);
         }
     }
 }
 
-// Unique remaining face of edge e (the first with no removal position).
-__device__ __forceinline__ int32_t live_face(const ThinArgs& A, int32_t e) {
-    const int32_t b = A.ef_off[e], t = A.ef_off[e + 1];
-    for (int32_t k = b; k < t; ++k) {
-        const int32_t f = A.ef_ids[k];
-        if (__ldcg(A.rm_f + f) == kAlive) return f;
+// Unique remaining face of an edge / edge of a vertex (first with no removal).
+__device__ __forceinline__ int32_t live_face(const ThinArgs& A, int32_t off, int32_t cnt) {
+    for (int32_t k = 0; k < cnt; ++k) {
+        const int32_t f = A.ef_ids[off + k];
+        if (__ldcg(&A.F[f].rm) == kAlive) return f;
     }
     return -1;
 }
-__device__ __forceinline__ int32_t live_edge(const ThinArgs& A, int32_t v) {
-    const int32_t b = A.ve_off[v], t = A.ve_off[v + 1];
-    for (int32_t k = b; k < t; ++k) {
-        const int32_t e = A.ve_ids[k];
-        if (__ldcg(A.rm_e + e) == kAlive) return e;
+__device__ __forceinline__ int32_t live_edge(const ThinArgs& A, int32_t off, int32_t cnt) {
+    for (int32_t k = 0; k < cnt; ++k) {
+        const int32_t e = A.ve_ids[off + k];
+        if (__ldcg(&A.E[e].rm) == kAlive) return e;
     }
     return -1;
+}
+
+// Warp-aggregated append of a cell whose count fell from 2 to 1.  All lanes
+// of the warp call it (want may be false).
+__device__ __forceinline__ void append_cell(int32_t* cells, int* ncells, bool want, int32_t code) {
+    const unsigned m = __ballot_sync(0xffffffffu, want);
+    if (!m) return;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(m) - 1;
+    int basei = 0;
+    if (lane == leader) basei = atomicAdd(ncells, __popc(m));
+    basei = __shfl_sync(0xffffffffu, basei, leader);
+    if (want) cells[basei + __popc(m & ((1u << lane) - 1u))] = code;
 }
 
 __global__ void __launch_bounds__(kThreads) thin_generations_kernel(ThinArgs A) {
@@ -158,127 +223,136 @@ __global__ void __launch_bounds__(kThreads) thin_generations_kernel(ThinArgs A) 
     int gen = 0;
     int64_t my_processed = 0, my_skipped = 0;
     while (n > 0) {
-        const int2* cur = (gen & 1) ? A.qb : A.qa;
-        int2* nxt = (gen & 1) ? A.qa : A.qb;
+        const int par = gen & 1;
+        const int2* cur = par ? A.qb : A.qa;
+        int2* nxt = par ? A.qa : A.qb;
+        int* ncells = A.ncells + par;
+        int64_t* blk = A.blk_cnt + (int64_t)par * G;
         const int64_t chunk = (n + G - 1) / G;
         const int64_t i0 = min(n, (int64_t)b * chunk), i1 = min(n, i0 + chunk);
+        const bool tr = A.trace && b == 0 && threadIdx.x == 0 && gen < A.trace_cap;
+        if (tr) {
+            A.trace[4 * gen + 0] = n;
+            A.trace[4 * gen + 1] = global_ns();
+        }
         // ---- phase A: apply the removals of the items that won their claim
-        for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-            const int2 it = ld_item(cur + i);
-            const int32_t p = (int32_t)(base + i);
-            if (is_fe(it)) {
-                const int32_t f = idx0(it), e = it.y;
-                if (__ldcg(A.rm_f + f) != p) {
-                    ++my_skipped;
-                    continue;
-                }
-                if (__ldcg(A.ref_e + e) != 1) {
-                    set_error(A.err, VC_ERR_INVARIANT);
-                    continue;
-                }
-                ++my_processed;
-                atomicMin(&A.rm_e[e], p);
-                A.ref_e[e] = 0;
+        for (int64_t r0 = i0; r0 < i1; r0 += blockDim.x) {
+            const int64_t i = r0 + threadIdx.x;
+            int32_t one[4] = {-1, -1, -1, -1};  // cells whose count fell to 1 here
+            if (i < i1) {
+                const int2 it = __ldcg(cur + i);
+                const int32_t p = (int32_t)(base + i);
+                int4 cd = make_int4(-1, -1, -1, -1);
+                if (is_fe(it)) {
+                    const int32_t f = idx0(it), e = it.y;
+                    const int32_t frm = __ldcg(&A.F[f].rm);
+                    const int32_t eref = __ldcg(&A.E[e].ref);
+                    if (frm != p) {
+                        ++my_skipped;
+                    } else if (eref != 1) {
+                        set_error(A.err, VC_ERR_INVARIANT);
+                    } else {
+                        ++my_processed;
+                        atomicMin(&A.E[e].rm, p);
+                        A.E[e].ref = 0;
+                        const int32_t sd[3] = {A.F[f].e0, A.F[f].e1, A.F[f].e2};
+                        const int32_t v0 = A.E[e].v0, v1 = A.E[e].v1;
+                        int k = 0;
 #pragma unroll
-                for (int s = 0; s < 3; ++s) {
-                    const int32_t e2 = A.tri_edges[3 * (int64_t)f + s];
-                    if (e2 == e || __ldcg(A.rm_e + e2) < p) continue;
-                    atomicSub(&A.ref_e[e2], 1);
-                    atomicMax(&A.trig_e[e2], p);
+                        for (int q = 0; q < 3; ++q) {
+                            const int32_t e2 = sd[q];
+                            if (e2 == e || k >= 2 || __ldcg(&A.E[e2].rm) < p) continue;
+                            atomicMax(&A.E[e2].trig, p);
+                            if (atomicSub(&A.E[e2].ref, 1) == 2) one[k] = e2 | kEdgeBit;
+                            if (k == 0) cd.x = e2;
+                            else cd.y = e2;
+                            ++k;
+                        }
+                        atomicMax(&A.V[v0].trig, p);
+                        atomicMax(&A.V[v1].trig, p);
+                        if (atomicSub(&A.V[v0].ref, 1) == 2) one[2] = v0;
+                        if (atomicSub(&A.V[v1].ref, 1) == 2) one[3] = v1;
+                        cd.z = v0;
+                        cd.w = v1;
+                    }
+                } else {
+                    const int32_t e = it.x, v = it.y;
+                    const int32_t erm = __ldcg(&A.E[e].rm);
+                    const int32_t vref = __ldcg(&A.V[v].ref);
+                    if (erm != p) {
+                        ++my_skipped;
+                    } else if (vref != 1) {
+                        set_error(A.err, VC_ERR_INVARIANT);
+                    } else {
+                        ++my_processed;
+                        A.V[v].rm = p;
+                        const int32_t v0 = A.E[e].v0, v1 = A.E[e].v1;
+                        const int32_t u = v0 != v ? v0 : v1;
+                        A.V[v].ref = 0;
+                        atomicMax(&A.V[u].trig, p);
+                        if (atomicSub(&A.V[u].ref, 1) == 2) one[2] = u;
+                        cd.z = u;
+                    }
                 }
-                const int2 ev = A.edges[e];
-                atomicSub(&A.ref_v[ev.x], 1);
-                atomicMax(&A.trig_v[ev.x], p);
-                atomicSub(&A.ref_v[ev.y], 1);
-                atomicMax(&A.trig_v[ev.y], p);
-            } else {
-                const int32_t e = it.x, v = it.y;
-                if (__ldcg(A.rm_e + e) != p) {
-                    ++my_skipped;
-                    continue;
-                }
-                if (__ldcg(A.ref_v + v) != 1) {
-                    set_error(A.err, VC_ERR_INVARIANT);
-                    continue;
-                }
-                ++my_processed;
-                A.rm_v[v] = p;
-                const int2 ev = A.edges[e];
-                atomicSub(&A.ref_v[ev.x], 1);
-                atomicMax(&A.trig_v[ev.x], p);
-                atomicSub(&A.ref_v[ev.y], 1);
-                atomicMax(&A.trig_v[ev.y], p);
+                __stcg(A.cand + i, cd);
             }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) append_cell(A.cells, ncells, one[q] != -1, one[q]);
         }
         grid_barrier(A.bar, A.err, A.spin_limit);
         if (*((volatile int*)A.err)) break;
-        // ---- phase B: find each processed item's children (in slot order)
-        int64_t local = 0;
-        for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-            const int2 it = ld_item(cur + i);
-            const int32_t p = (int32_t)(base + i);
-            int cnt = 0;
-            int2* out = A.child + 4 * i;
-            if (is_fe(it)) {
-                const int32_t f = idx0(it), e = it.y;
-                if (__ldcg(A.rm_f + f) == p) {
-#pragma unroll
-                    for (int s = 0; s < 3; ++s) {
-                        const int32_t e2 = A.tri_edges[3 * (int64_t)f + s];
-                        if (e2 == e) continue;
-                        if (__ldcg(A.trig_e + e2) == p && __ldcg(A.ref_e + e2) == 1) {
-                            const int32_t f2 = live_face(A, e2);
-                            if (f2 < 0) {
-                                set_error(A.err, VC_ERR_INVARIANT);
-                            } else if (A.fm[f2] < f_t) {
-                                out[cnt++] = make_fe(f2, e2);
-                            }
-                        }
-                    }
-                    const int2 ev = A.edges[e];
-#pragma unroll
-                    for (int s = 0; s < 2; ++s) {
-                        const int32_t u = s == 0 ? ev.x : ev.y;
-                        if (__ldcg(A.trig_v + u) == p && __ldcg(A.ref_v + u) == 1) {
-                            const int32_t e3 = live_edge(A, u);
-                            if (e3 < 0) {
-                                set_error(A.err, VC_ERR_INVARIANT);
-                            } else if (A.em[e3] < l_t) {
-                                out[cnt++] = make_ev(e3, u);
-                            }
-                        }
-                    }
-                }
-            } else {
-                const int32_t e = it.x, v = it.y;
-                if (__ldcg(A.rm_e + e) == p) {
-                    const int2 ev = A.edges[e];
-                    const int32_t u = ev.x != v ? ev.x : ev.y;
-                    if (__ldcg(A.trig_v + u) == p && __ldcg(A.ref_v + u) == 1) {
-                        const int32_t e3 = live_edge(A, u);
-                        if (e3 < 0) {
-                            set_error(A.err, VC_ERR_INVARIANT);
-                        } else if (A.em[e3] < l_t) {
-                            out[cnt++] = make_ev(e3, u);
-                        }
-                    }
-                }
-            }
-            A.child_cnt[i] = (uint8_t)cnt;
-            local += cnt;
-        }
+        // ---- phase B: a listed cell still at 1 gives its child to the item
+        // that decremented it last (its trig position), in the cell's slot
+        if (tr) A.trace[4 * gen + 2] = global_ns();
         {
-            int64_t tot;
-            block_exclusive_sum<int64_t>(local, sm, &tot);
-            if (threadIdx.x == 0) A.blk_cnt[b] = tot;
+            const int m = __ldcg(ncells);
+            for (int64_t j = (int64_t)b * blockDim.x + threadIdx.x; j < m; j += (int64_t)G * blockDim.x) {
+                const int32_t code = __ldcg(A.cells + j);
+                int64_t i;
+                int slot;
+                int2 ch;
+                if (code & kEdgeBit) {
+                    const int32_t e2 = code & ~kEdgeBit;
+                    if (__ldcg(&A.E[e2].ref) != 1) continue;
+                    i = (int64_t)__ldcg(&A.E[e2].trig) - base;
+                    const int32_t f2 = live_face(A, A.E[e2].ef_off, A.E[e2].ef_cnt);
+                    if (f2 < 0) {
+                        set_error(A.err, VC_ERR_INVARIANT);
+                        continue;
+                    }
+                    if (!(A.F[f2].fm < f_t)) continue;
+                    slot = __ldcg(&A.cand[i].x) == e2 ? 0 : 1;
+                    ch = make_fe(f2, e2);
+                } else {
+                    const int32_t u = code;
+                    if (__ldcg(&A.V[u].ref) != 1) continue;
+                    i = (int64_t)__ldcg(&A.V[u].trig) - base;
+                    const int32_t e3 = live_edge(A, A.V[u].ve_off, A.V[u].ve_cnt);
+                    if (e3 < 0) {
+                        set_error(A.err, VC_ERR_INVARIANT);
+                        continue;
+                    }
+                    if (!(A.E[e3].em < l_t)) continue;
+                    slot = __ldcg(&A.cand[i].z) == u ? 2 : 3;
+                    ch = make_ev(e3, u);
+                }
+                if (i < 0 || i >= n) {
+                    set_error(A.err, VC_ERR_INVARIANT);
+                    continue;
+                }
+                __stcg(A.child + 4 * i + slot, ch);
+                atomicOr(A.child_mask + (i >> 2), 1u << (((unsigned)i & 3u) * 8u + (unsigned)slot));
+                atomicAdd((unsigned long long*)(blk + i / chunk), 1ull);
+            }
         }
         grid_barrier(A.bar, A.err, A.spin_limit);
         if (*((volatile int*)A.err)) break;
         // ---- phase C: block prefix, write generation g+1 and make its claims
+        if (tr) A.trace[4 * gen + 3] = global_ns();
         {
             int64_t before = 0, all = 0;
             for (int k = threadIdx.x; k < G; k += blockDim.x) {
-                const int64_t v = __ldcg(A.blk_cnt + k);
+                const int64_t v = __ldcg(blk + k);
                 all += v;
                 if (k < b) before += v;
             }
@@ -294,20 +368,34 @@ __global__ void __launch_bounds__(kThreads) thin_generations_kernel(ThinArgs A) 
         const int64_t prefix = s_red[0], total = s_red[1];
         const int64_t nbase = base + n;
         int64_t running = prefix;
-        for (int64_t r = i0; r < i1; r += blockDim.x) {
-            const int64_t i = r + threadIdx.x;
-            const int cnt = i < i1 ? (int)A.child_cnt[i] : 0;
+        for (int64_t r0 = i0; r0 < i1; r0 += blockDim.x) {
+            const int64_t i = r0 + threadIdx.x;
+            unsigned msk = 0;
+            if (i < i1) {
+                const unsigned sh = ((unsigned)i & 3u) * 8u;
+                msk = (__ldcg(A.child_mask + (i >> 2)) >> sh) & 0xFu;
+                if (msk) atomicAnd(A.child_mask + (i >> 2), ~(0xFFu << sh));
+            }
             int64_t tot;
-            const int64_t ex = block_exclusive_sum<int64_t>((int64_t)cnt, sm, &tot);
-            for (int k = 0; k < cnt; ++k) {
-                const int2 ch = A.child[4 * i + k];
+            const int64_t ex = block_exclusive_sum<int64_t>((int64_t)__popc(msk), sm, &tot);
+            int k = 0;
+#pragma unroll
+            for (int sl = 0; sl < 4; ++sl) {
+                if (!(msk & (1u << sl))) continue;
+                const int2 ch = __ldcg(A.child + 4 * i + sl);
                 const int64_t slot = running + ex + k;
-                nxt[slot] = ch;
+                ++k;
+                __stcg(nxt + slot, ch);
                 const int32_t q = (int32_t)(nbase + slot);
-                if (is_fe(ch)) atomicMin(&A.rm_f[idx0(ch)], q);
-                else atomicMin(&A.rm_e[ch.x], q);
+                if (is_fe(ch)) atomicMin(&A.F[idx0(ch)].rm, q);
+                else atomicMin(&A.E[ch.x].rm, q);
             }
             running += tot;
+        }
+        // counters of the next generation start at zero
+        if (threadIdx.x == 0) {
+            A.blk_cnt[(int64_t)(par ^ 1) * G + b] = 0;
+            if (b == 0) A.ncells[par ^ 1] = 0;
         }
         __syncthreads();
         base = nbase;
@@ -330,20 +418,24 @@ __global__ void set_thr_kernel(float* thr, float f_t, float l_t) {
     thr[1] = l_t;
 }
 
-__global__ void thin_flags_kernel(const int32_t* __restrict__ rm_v, const int32_t* __restrict__ rm_e,
-                                  const int32_t* __restrict__ ref_e, const int32_t* __restrict__ rm_f, int32_t nv,
-                                  int32_t ne, int32_t nt, uint8_t* kv, uint8_t* ke, uint8_t* kf, uint8_t* re) {
+// Survivor flags from the records: keep_v = vertex not removed; keep_e =
+// edge not removed and referenced by no remaining face (getRemainedEdges);
+// keep_f = face not removed; removed_e = edge removal tag.
+__global__ void export_flags_kernel(const FaceRec* __restrict__ F, const EdgeRec* __restrict__ E,
+                                    const VertRec* __restrict__ V, int32_t nv, int32_t ne, int32_t nt, uint8_t* kv,
+                                    uint8_t* ke, uint8_t* kf, uint8_t* re) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (int64_t)nv + ne + nt; i += stride) {
         if (i < nv) {
-            if (kv) kv[i] = rm_v[i] == kAlive;
+            kv[i] = V[i].rm == kAlive;
         } else if (i < (int64_t)nv + ne) {
             const int64_t e = i - nv;
-            if (ke) ke[e] = rm_e[e] == kAlive && ref_e[e] == 0;
-            if (re) re[e] = rm_e[e] != kAlive;
+            const int32_t rm = E[e].rm, ref = E[e].ref;
+            ke[e] = rm == kAlive && ref == 0;
+            re[e] = rm != kAlive;
         } else {
             const int64_t f = i - nv - ne;
-            if (kf) kf[f] = rm_f[f] == kAlive;
+            kf[f] = F[f].rm == kAlive;
         }
     }
 }
@@ -366,72 +458,78 @@ int run_thin(vc_ctx* c, float f_t, float l_t, vc_thin_stats* stats) {
     return run_thin_with_device_thr(c, stats);
 }
 
-// Thinning with thresholds already in c->thr (device), e.g. computed from the
-// complex's inside size on the device.
+// Thinning with thresholds already in c->thr (device).
 int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats) {
     if (!c->cc_finalized || !c->meas_valid) return VC_ERR_STATE;
     const int64_t nv = c->nv, ne = c->ne, nt = c->nt;
-    if (nv + ne >= INT32_MAX) return VC_ERR_ARG;
+    if (nv + ne >= INT32_MAX || nt >= INT32_MAX) return VC_ERR_ARG;
     const int64_t qcap = nv + ne + 1;
     Region stage(c, "stage_thin");
-    VC_TRY(ensure_n<int32_t>(c, c->rm_f, nt));
-    VC_TRY(ensure_n<int32_t>(c, c->rm_e, ne));
-    VC_TRY(ensure_n<int32_t>(c, c->rm_v, nv));
-    VC_TRY(ensure_n<int32_t>(c, c->ref_e, ne));
-    VC_TRY(ensure_n<int32_t>(c, c->ref_v, nv));
-    VC_TRY(ensure_n<int32_t>(c, c->trig_e, ne));
-    VC_TRY(ensure_n<int32_t>(c, c->trig_v, nv));
+    VC_TRY(ensure_n<FaceRec>(c, c->face_rec, nt));
+    VC_TRY(ensure_n<EdgeRec>(c, c->edge_rec, ne));
+    VC_TRY(ensure_n<VertRec>(c, c->vert_rec, nv));
     VC_TRY(ensure_n<int2>(c, c->q0, qcap));
     VC_TRY(ensure_n<int2>(c, c->q1, qcap));
+    VC_TRY(ensure_n<int4>(c, c->cand, qcap));
     VC_TRY(ensure_n<int2>(c, c->child, 4 * qcap));
-    VC_TRY(ensure_n<uint8_t>(c, c->child_cnt, qcap));
+    VC_TRY(ensure_n<unsigned>(c, c->child_cnt, qcap / 4 + 2));  // child masks
+    VC_TRY(ensure_n<int32_t>(c, c->cells, qcap));
     VC_TRY(ensure_n<int32_t>(c, c->scratch2, 2 * (nv + ne) + 2));
     VC_TRY(ensure_n<int64_t>(c, c->euler_tmp, 16));
+    VC_TRY(ensure_n<uint8_t>(c, c->keep_v, nv));
+    VC_TRY(ensure_n<uint8_t>(c, c->keep_e, ne));
+    VC_TRY(ensure_n<uint8_t>(c, c->keep_f, nt));
+    VC_TRY(ensure_n<uint8_t>(c, c->removed_e, ne));
     ThinArgs A{};
-    A.edges = ptr<int2>(c->edges);
-    A.tri_edges = ptr<int32_t>(c->tri_edges);
-    A.ve_off = ptr<int32_t>(c->ve_off);
+    A.F = ptr<FaceRec>(c->face_rec);
+    A.E = ptr<EdgeRec>(c->edge_rec);
+    A.V = ptr<VertRec>(c->vert_rec);
     A.ve_ids = ptr<int32_t>(c->ve_ids);
-    A.ef_off = ptr<int32_t>(c->ef_off);
     A.ef_ids = ptr<int32_t>(c->ef_ids);
-    A.em = ptr<float>(c->em);
-    A.fm = ptr<float>(c->fm);
     A.thr = ptr<float>(c->thr);
-    A.rm_f = ptr<int32_t>(c->rm_f);
-    A.rm_e = ptr<int32_t>(c->rm_e);
-    A.rm_v = ptr<int32_t>(c->rm_v);
-    A.ref_e = ptr<int32_t>(c->ref_e);
-    A.ref_v = ptr<int32_t>(c->ref_v);
-    A.trig_e = ptr<int32_t>(c->trig_e);
-    A.trig_v = ptr<int32_t>(c->trig_v);
     A.qa = ptr<int2>(c->q0);
     A.qb = ptr<int2>(c->q1);
+    A.cand = ptr<int4>(c->cand);
     A.child = ptr<int2>(c->child);
-    A.child_cnt = ptr<uint8_t>(c->child_cnt);
+    A.child_mask = ptr<unsigned>(c->child_cnt);
+    A.cells = ptr<int32_t>(c->cells);
     A.err = dev_err(c);
     int64_t* ctl = ptr<int64_t>(c->euler_tmp);
     A.ctl = ctl;
     A.bar = reinterpret_cast<unsigned*>(ctl + 8);
+    A.ncells = reinterpret_cast<int*>(ctl + 9);
     A.spin_limit = 1ull << 26;
-    thin_init_kernel<<<grid_for(c, nv + ne + nt, 256), 256, 0, c->stream>>>(
-        A.ve_off, A.ef_off, (int32_t)nv, (int32_t)ne, (int32_t)nt, A.rm_f, A.rm_e, A.rm_v, A.ref_e, A.ref_v,
-        A.trig_e, A.trig_v);
-    launched(c);
-    int32_t* flag = ptr<int32_t>(c->scratch2);
-    int32_t* pos = flag + (nv + ne + 1);
-    gen0_flags_kernel<<<grid_for(c, nv + ne, 256), 256, 0, c->stream>>>(A, (int32_t)nv, (int32_t)ne, flag);
-    launched(c);
-    VC_CUDA(c, cudaMemsetAsync(ctl, 0, 16 * sizeof(int64_t), c->stream));
-    VC_TRY(scan_exclusive_i32(c, flag, pos, nv + ne, ctl + 0));
-    gen0_write_kernel<<<grid_for(c, nv + ne, 256), 256, 0, c->stream>>>(A, (int32_t)nv, (int32_t)ne, flag, pos);
-    launched(c);
-    VC_CUDA(c, cudaGetLastError());
+    if (c->trace_cap > 0) {
+        VC_TRY(ensure_n<int64_t>(c, c->trace, 4 * (int64_t)c->trace_cap));
+        VC_CUDA(c, cudaMemsetAsync(c->trace.p, 0, 4 * sizeof(int64_t) * c->trace_cap, c->stream));
+        A.trace = ptr<int64_t>(c->trace);
+        A.trace_cap = c->trace_cap;
+    }
+    {
+        Region r(c, "thin_setup");
+        build_records_kernel<<<grid_for(c, nv + ne + nt, 256), 256, 0, c->stream>>>(
+            ptr<int2>(c->edges), ptr<int32_t>(c->tri_edges), ptr<int32_t>(c->ve_off), ptr<int32_t>(c->ef_off),
+            ptr<float>(c->em), ptr<float>(c->fm), (int32_t)nv, (int32_t)ne, (int32_t)nt, A.F, A.E, A.V);
+        launched(c);
+        int32_t* flag = ptr<int32_t>(c->scratch2);
+        int32_t* pos = flag + (nv + ne + 1);
+        gen0_flags_kernel<<<grid_for(c, nv + ne, 256), 256, 0, c->stream>>>(A, (int32_t)nv, (int32_t)ne, flag);
+        launched(c);
+        VC_CUDA(c, cudaMemsetAsync(ctl, 0, 16 * sizeof(int64_t), c->stream));
+        VC_CUDA(c, cudaMemsetAsync(c->child_cnt.p, 0, (qcap / 4 + 2) * sizeof(unsigned), c->stream));
+        VC_TRY(scan_exclusive_i32(c, flag, pos, nv + ne, ctl + 0));
+        gen0_write_kernel<<<grid_for(c, nv + ne, 256), 256, 0, c->stream>>>(A, (int32_t)nv, (int32_t)ne, flag,
+                                                                             pos);
+        launched(c);
+        VC_CUDA(c, cudaGetLastError());
+    }
     // persistent cooperative launch: every block resident
     int per_sm = 0;
     VC_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, thin_generations_kernel, kThreads, 0));
     if (per_sm <= 0) return VC_ERR_CUDA;
-    int G = c->num_sms * std::min(per_sm, 4);
-    VC_TRY(ensure_n<int64_t>(c, c->blk_cnt, G));
+    const int G = c->num_sms * std::min(per_sm, c->thin_blocks_per_sm > 0 ? c->thin_blocks_per_sm : 8);
+    VC_TRY(ensure_n<int64_t>(c, c->blk_cnt, 2 * (int64_t)G));
+    VC_CUDA(c, cudaMemsetAsync(c->blk_cnt.p, 0, 2 * sizeof(int64_t) * G, c->stream));
     A.blk_cnt = ptr<int64_t>(c->blk_cnt);
     void* args[] = {&A};
     {
@@ -440,11 +538,16 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats) {
                                                c->stream));
         launched(c);
     }
+    export_flags_kernel<<<grid_for(c, nv + ne + nt, 256), 256, 0, c->stream>>>(
+        A.F, A.E, A.V, (int32_t)nv, (int32_t)ne, (int32_t)nt, ptr<uint8_t>(c->keep_v), ptr<uint8_t>(c->keep_e),
+        ptr<uint8_t>(c->keep_f), ptr<uint8_t>(c->removed_e));
+    launched(c);
     int64_t h[5];
     VC_CUDA(c, cudaMemcpyAsync(h, ctl, 5 * sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
     int s = sync_check(c);
     if (s != VC_OK) return s;
     c->thin_stats = vc_thin_stats{h[1], h[2], h[3], h[4]};
+    c->trace_gens = (int)std::min<int64_t>(h[4], c->trace_cap);
     c->thin_valid = true;
     c->rem_valid = false;
     if (stats) *stats = c->thin_stats;
@@ -453,20 +556,30 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats) {
 
 int get_thin_flags(vc_ctx* c, uint8_t* kv, uint8_t* ke, uint8_t* kf, uint8_t* re, int mem) {
     if (!c->thin_valid) return VC_ERR_STATE;
-    const int64_t nv = c->nv, ne = c->ne, nt = c->nt;
-    VC_TRY(ensure_n<uint8_t>(c, c->scratch, nv + 2 * ne + nt + 16));
-    uint8_t* d = ptr<uint8_t>(c->scratch);
-    uint8_t *dkv = d, *dke = d + nv, *dre = d + nv + ne, *dkf = d + nv + 2 * ne;
-    thin_flags_kernel<<<grid_for(c, nv + ne + nt, 256), 256, 0, c->stream>>>(
-        ptr<int32_t>(c->rm_v), ptr<int32_t>(c->rm_e), ptr<int32_t>(c->ref_e), ptr<int32_t>(c->rm_f), (int32_t)nv,
-        (int32_t)ne, (int32_t)nt, dkv, dke, dkf, dre);
-    launched(c);
-    VC_CUDA(c, cudaGetLastError());
-    VC_TRY(copy_out(c, kv, dkv, nv, mem));
-    VC_TRY(copy_out(c, ke, dke, ne, mem));
-    VC_TRY(copy_out(c, kf, dkf, nt, mem));
-    VC_TRY(copy_out(c, re, dre, ne, mem));
+    VC_TRY(copy_out(c, kv, c->keep_v.p, c->nv, mem));
+    VC_TRY(copy_out(c, ke, c->keep_e.p, c->ne, mem));
+    VC_TRY(copy_out(c, kf, c->keep_f.p, c->nt, mem));
+    VC_TRY(copy_out(c, re, c->removed_e.p, c->ne, mem));
     return sync_check(c);
 }
 
 }  // namespace vc
+
+extern "C" {
+
+int vc_debug_thin_trace(vc_ctx* c, int cap, int blocks_per_sm) {
+    if (!c) return VC_ERR_ARG;
+    c->trace_cap = cap > 0 ? cap : 0;
+    c->thin_blocks_per_sm = blocks_per_sm;
+    return VC_OK;
+}
+
+int vc_debug_get_thin_trace(vc_ctx* c, int64_t* out, int cap, int* ngen) {
+    if (!c || !ngen) return VC_ERR_ARG;
+    *ngen = c->trace_gens;
+    if (!out || c->trace_gens == 0) return VC_OK;
+    const int n = std::min(cap, c->trace_gens);
+    return vc::copy_out(c, out, c->trace.p, 4 * sizeof(int64_t) * n, VC_MEM_HOST);
+}
+
+}  // extern "C"
