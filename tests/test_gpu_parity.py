@@ -47,6 +47,12 @@ def test_sites_ft_vd_match_oracle(gpu_ctx, name, occ):
     assert s["inside_size"] == ovd["inside_size"]
     for k in ("vts", "edges", "tris", "vm", "em", "fm", "tri_face", "face_sites"):
         assert np.array_equal(vd[k], ovd[k]), k
+    # the lattice complex is installed already finalized: its adjacency must be
+    # what cellcomplex::finalize builds from (vts, edges, tris)
+    ctx.use_vd_as_complex()
+    fin = ctx.finalized()
+    for k in ("edges", "tri_edges", "ve_off", "ve_ids", "ef_off", "ef_ids"):
+        assert np.array_equal(fin[k], L["fin"][k]), k
 
 
 def test_empty_volume(gpu_ctx):

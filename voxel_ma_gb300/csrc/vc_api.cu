@@ -117,6 +117,7 @@ int vc_set_complex(vc_ctx* c, int64_t nv, const float* vts, int64_t ne, const in
     c->nt = nt;
     c->cc_valid = true;
     c->cc_finalized = c->meas_valid = c->thin_valid = c->rem_valid = false;
+    c->records_fresh = false;
     c->vd_valid = false;  // the complex no longer comes from the lattice VD
     return VC_OK;
 }
@@ -152,6 +153,7 @@ int vc_set_measures(vc_ctx* c, const float* vm, const float* em, const float* fm
     VC_TRY(copy_in(c, c->em.p, em, (size_t)c->ne * sizeof(float), mem));
     VC_TRY(copy_in(c, c->fm.p, fm, (size_t)c->nt * sizeof(float), mem));
     c->meas_valid = true;
+    c->records_fresh = false;
     c->thin_valid = c->rem_valid = false;
     return VC_OK;
 }

@@ -39,6 +39,28 @@ T* ptr(const DevBuf& b) {
     return static_cast<T*>(b.p);
 }
 
+// Per-cell records of the thinning kernel: static data and thinning state of
+// one cell in one 32-byte DRAM sector (its accesses are random).
+constexpr int32_t kAlive = INT32_MAX;  // removal position of a cell still present
+struct __align__(32) FaceRec {
+    int32_t e0, e1, e2;  // edge ids of the sides, in face order
+    float fm;
+    int32_t rm;
+    int32_t pad0, pad1, pad2;
+};
+struct __align__(32) EdgeRec {
+    int32_t v0, v1;
+    float em;
+    int32_t ef_off, ef_cnt;  // E->F list
+    int32_t rm, ref, trig;
+};
+struct __align__(32) VertRec {
+    int32_t ve_off, ve_cnt;  // V->E list
+    int32_t rm, ref, trig;
+    int32_t pad0, pad1, pad2;
+};
+static_assert(sizeof(FaceRec) == 32 && sizeof(EdgeRec) == 32 && sizeof(VertRec) == 32, "record size");
+
 }  // namespace vc
 
 // The opaque context.  Members are grouped by pipeline stage.
@@ -70,7 +92,7 @@ struct vc_ctx {
     vc_vd_sizes vd{};
     vc::DevBuf vd_flags;              // uint8 per lattice point
     vc::DevBuf vd_voff, vd_eoff, vd_foff;  // int32 exclusive offsets per lattice point
-    vc::DevBuf vd_tri_face, vd_face_sites, vd_vm;
+    vc::DevBuf vd_tri_face, vd_face_sites, vd_vm, vd_lam, vd_efoff, vd_veoff;
     vc::DevBuf vd_bbox;  // int32[6]
     // cell complex (finalized, CSR)
     bool cc_valid = false;
@@ -90,6 +112,7 @@ struct vc_ctx {
     bool thin_valid = false;
     vc_thin_stats thin_stats{};
     vc::DevBuf face_rec, edge_rec, vert_rec;  // 32-byte per-cell thinning records
+    bool records_fresh = false;               // records already hold this complex in reset state
     vc::DevBuf q0, q1, cand, child, child_cnt, cells, blk_cnt, thr;
     vc::DevBuf keep_v, keep_e, keep_f, removed_e;  // uint8 survivor flags of the last thinning
     vc::DevBuf trace;           // optional per-generation trace of the thinning kernel

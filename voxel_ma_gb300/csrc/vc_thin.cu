@@ -45,28 +45,8 @@ namespace vc {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int32_t kAlive = INT32_MAX;
 constexpr unsigned kFE = 0x80000000u;
 constexpr int32_t kEdgeBit = (int32_t)0x80000000u;
-
-struct __align__(32) FaceRec {
-    int32_t e0, e1, e2;
-    float fm;
-    int32_t rm;
-    int32_t pad0, pad1, pad2;
-};
-struct __align__(32) EdgeRec {
-    int32_t v0, v1;
-    float em;
-    int32_t ef_off, ef_cnt;
-    int32_t rm, ref, trig;
-};
-struct __align__(32) VertRec {
-    int32_t ve_off, ve_cnt;
-    int32_t rm, ref, trig;
-    int32_t pad0, pad1, pad2;
-};
-static_assert(sizeof(FaceRec) == 32 && sizeof(EdgeRec) == 32 && sizeof(VertRec) == 32, "record size");
 
 struct ThinArgs {
     FaceRec* F;
@@ -80,8 +60,8 @@ struct ThinArgs {
     int4* cand;            // per item: the cells it decremented (-1 = none)
     int2* child;           // per item: up to 4 children, by slot
     unsigned* child_mask;  // per item one byte (4 items per word): bit s = child in slot s
-    int32_t* cells;        // cells whose count reached 1 in this generation (kEdgeBit: edge)
-    int* ncells;           // [2] list lengths, by generation parity
+    int32_t* cells;        // per block: cells whose count reached 1 in this generation (kEdgeBit: edge)
+    int* ncell_blk;        // [G] list length of each block's region
     int64_t* blk_cnt;      // [2 * G] children per block, by generation parity
     unsigned* bar;
     int* err;
@@ -200,22 +180,24 @@ __device__ __forceinline__ int32_t live_edge(const ThinArgs& A, int32_t off, int
     return -1;
 }
 
-// Warp-aggregated append of a cell whose count fell from 2 to 1.  All lanes
-// of the warp call it (want may be false).
-__device__ __forceinline__ void append_cell(int32_t* cells, int* ncells, bool want, int32_t code) {
+// Block-local append of the cells whose count fell from 2 to 1: each block
+// owns the region cells[b * cap .. b * cap + count), its count kept in
+// shared memory during phase A and published to ncell_blk[b] at its end.
+__device__ __forceinline__ void append_cell(int32_t* region, int* s_count, bool want, int32_t code) {
     const unsigned m = __ballot_sync(0xffffffffu, want);
     if (!m) return;
     const int lane = threadIdx.x & 31;
     const int leader = __ffs(m) - 1;
     int basei = 0;
-    if (lane == leader) basei = atomicAdd(ncells, __popc(m));
+    if (lane == leader) basei = atomicAdd(s_count, __popc(m));
     basei = __shfl_sync(0xffffffffu, basei, leader);
-    if (want) cells[basei + __popc(m & ((1u << lane) - 1u))] = code;
+    if (want) region[basei + __popc(m & ((1u << lane) - 1u))] = code;
 }
 
 __global__ void __launch_bounds__(kThreads) thin_generations_kernel(ThinArgs A) {
     __shared__ int64_t sm[33];
     __shared__ int64_t s_red[2];
+    __shared__ int s_ncell;
     const int G = gridDim.x, b = blockIdx.x;
     const float f_t = A.thr[0], l_t = A.thr[1];
     int64_t n = A.ctl[0];
@@ -226,9 +208,12 @@ __global__ void __launch_bounds__(kThreads) thin_generations_kernel(ThinArgs A) 
         const int par = gen & 1;
         const int2* cur = par ? A.qb : A.qa;
         int2* nxt = par ? A.qa : A.qb;
-        int* ncells = A.ncells + par;
         int64_t* blk = A.blk_cnt + (int64_t)par * G;
         const int64_t chunk = (n + G - 1) / G;
+        const int64_t region_cap = 4 * chunk;
+        int32_t* region = A.cells + (int64_t)b * region_cap;
+        if (threadIdx.x == 0) s_ncell = 0;
+        __syncthreads();
         const int64_t i0 = min(n, (int64_t)b * chunk), i1 = min(n, i0 + chunk);
         const bool tr = A.trace && b == 0 && threadIdx.x == 0 && gen < A.trace_cap;
         if (tr) {
@@ -253,27 +238,27 @@ __global__ void __launch_bounds__(kThreads) thin_generations_kernel(ThinArgs A) 
                         set_error(A.err, VC_ERR_INVARIANT);
                     } else {
                         ++my_processed;
+                        // the face's other two sides, in face order (the sides of a
+                        // live face other than e are never removed)
+                        const int32_t s0 = A.F[f].e0, s1 = A.F[f].e1, s2 = A.F[f].e2;
+                        const int32_t sa = s0 == e ? s1 : s0;
+                        const int32_t sb = (s0 == e || s1 == e) ? s2 : s1;
+                        const int32_t v0 = A.E[e].v0, v1 = A.E[e].v1;
                         atomicMin(&A.E[e].rm, p);
                         A.E[e].ref = 0;
-                        const int32_t sd[3] = {A.F[f].e0, A.F[f].e1, A.F[f].e2};
-                        const int32_t v0 = A.E[e].v0, v1 = A.E[e].v1;
-                        int k = 0;
-#pragma unroll
-                        for (int q = 0; q < 3; ++q) {
-                            const int32_t e2 = sd[q];
-                            if (e2 == e || k >= 2 || __ldcg(&A.E[e2].rm) < p) continue;
-                            atomicMax(&A.E[e2].trig, p);
-                            if (atomicSub(&A.E[e2].ref, 1) == 2) one[k] = e2 | kEdgeBit;
-                            if (k == 0) cd.x = e2;
-                            else cd.y = e2;
-                            ++k;
-                        }
+                        atomicMax(&A.E[sa].trig, p);
+                        atomicMax(&A.E[sb].trig, p);
                         atomicMax(&A.V[v0].trig, p);
                         atomicMax(&A.V[v1].trig, p);
-                        if (atomicSub(&A.V[v0].ref, 1) == 2) one[2] = v0;
-                        if (atomicSub(&A.V[v1].ref, 1) == 2) one[3] = v1;
-                        cd.z = v0;
-                        cd.w = v1;
+                        const int oa = atomicSub(&A.E[sa].ref, 1);
+                        const int ob = atomicSub(&A.E[sb].ref, 1);
+                        const int o0 = atomicSub(&A.V[v0].ref, 1);
+                        const int o1 = atomicSub(&A.V[v1].ref, 1);
+                        if (oa == 2) one[0] = sa | kEdgeBit;
+                        if (ob == 2) one[1] = sb | kEdgeBit;
+                        if (o0 == 2) one[2] = v0;
+                        if (o1 == 2) one[3] = v1;
+                        cd = make_int4(sa, sb, v0, v1);
                     }
                 } else {
                     const int32_t e = it.x, v = it.y;
@@ -297,17 +282,19 @@ __global__ void __launch_bounds__(kThreads) thin_generations_kernel(ThinArgs A) 
                 __stcg(A.cand + i, cd);
             }
 #pragma unroll
-            for (int q = 0; q < 4; ++q) append_cell(A.cells, ncells, one[q] != -1, one[q]);
+            for (int q = 0; q < 4; ++q) append_cell(region, &s_ncell, one[q] != -1, one[q]);
         }
+        __syncthreads();
+        if (threadIdx.x == 0) A.ncell_blk[b] = s_ncell;
         grid_barrier(A.bar, A.err, A.spin_limit);
         if (*((volatile int*)A.err)) break;
         // ---- phase B: a listed cell still at 1 gives its child to the item
         // that decremented it last (its trig position), in the cell's slot
         if (tr) A.trace[4 * gen + 2] = global_ns();
         {
-            const int m = __ldcg(ncells);
-            for (int64_t j = (int64_t)b * blockDim.x + threadIdx.x; j < m; j += (int64_t)G * blockDim.x) {
-                const int32_t code = __ldcg(A.cells + j);
+            const int m = __ldcg(A.ncell_blk + b);
+            for (int j = threadIdx.x; j < m; j += blockDim.x) {
+                const int32_t code = __ldcg(region + j);
                 int64_t i;
                 int slot;
                 int2 ch;
@@ -393,10 +380,7 @@ __global__ void __launch_bounds__(kThreads) thin_generations_kernel(ThinArgs A) 
             running += tot;
         }
         // counters of the next generation start at zero
-        if (threadIdx.x == 0) {
-            A.blk_cnt[(int64_t)(par ^ 1) * G + b] = 0;
-            if (b == 0) A.ncells[par ^ 1] = 0;
-        }
+        if (threadIdx.x == 0) A.blk_cnt[(int64_t)(par ^ 1) * G + b] = 0;
         __syncthreads();
         base = nbase;
         n = total;
@@ -465,15 +449,17 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats) {
     if (nv + ne >= INT32_MAX || nt >= INT32_MAX) return VC_ERR_ARG;
     const int64_t qcap = nv + ne + 1;
     Region stage(c, "stage_thin");
-    VC_TRY(ensure_n<FaceRec>(c, c->face_rec, nt));
-    VC_TRY(ensure_n<EdgeRec>(c, c->edge_rec, ne));
-    VC_TRY(ensure_n<VertRec>(c, c->vert_rec, nv));
+    if (!c->records_fresh) {
+        VC_TRY(ensure_n<FaceRec>(c, c->face_rec, nt));
+        VC_TRY(ensure_n<EdgeRec>(c, c->edge_rec, ne));
+        VC_TRY(ensure_n<VertRec>(c, c->vert_rec, nv));
+    }
     VC_TRY(ensure_n<int2>(c, c->q0, qcap));
     VC_TRY(ensure_n<int2>(c, c->q1, qcap));
     VC_TRY(ensure_n<int4>(c, c->cand, qcap));
     VC_TRY(ensure_n<int2>(c, c->child, 4 * qcap));
     VC_TRY(ensure_n<unsigned>(c, c->child_cnt, qcap / 4 + 2));  // child masks
-    VC_TRY(ensure_n<int32_t>(c, c->cells, qcap));
+    VC_TRY(ensure_n<int32_t>(c, c->cells, 4 * qcap + 4 * 8 * (int64_t)c->num_sms));
     VC_TRY(ensure_n<int32_t>(c, c->scratch2, 2 * (nv + ne) + 2));
     VC_TRY(ensure_n<int64_t>(c, c->euler_tmp, 16));
     VC_TRY(ensure_n<uint8_t>(c, c->keep_v, nv));
@@ -497,7 +483,7 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats) {
     int64_t* ctl = ptr<int64_t>(c->euler_tmp);
     A.ctl = ctl;
     A.bar = reinterpret_cast<unsigned*>(ctl + 8);
-    A.ncells = reinterpret_cast<int*>(ctl + 9);
+
     A.spin_limit = 1ull << 26;
     if (c->trace_cap > 0) {
         VC_TRY(ensure_n<int64_t>(c, c->trace, 4 * (int64_t)c->trace_cap));
@@ -507,10 +493,14 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats) {
     }
     {
         Region r(c, "thin_setup");
-        build_records_kernel<<<grid_for(c, nv + ne + nt, 256), 256, 0, c->stream>>>(
-            ptr<int2>(c->edges), ptr<int32_t>(c->tri_edges), ptr<int32_t>(c->ve_off), ptr<int32_t>(c->ef_off),
-            ptr<float>(c->em), ptr<float>(c->fm), (int32_t)nv, (int32_t)ne, (int32_t)nt, A.F, A.E, A.V);
-        launched(c);
+        if (c->records_fresh) {
+            c->records_fresh = false;  // the next thinning of this complex rebuilds them
+        } else {
+            build_records_kernel<<<grid_for(c, nv + ne + nt, 256), 256, 0, c->stream>>>(
+                ptr<int2>(c->edges), ptr<int32_t>(c->tri_edges), ptr<int32_t>(c->ve_off), ptr<int32_t>(c->ef_off),
+                ptr<float>(c->em), ptr<float>(c->fm), (int32_t)nv, (int32_t)ne, (int32_t)nt, A.F, A.E, A.V);
+            launched(c);
+        }
         int32_t* flag = ptr<int32_t>(c->scratch2);
         int32_t* pos = flag + (nv + ne + 1);
         gen0_flags_kernel<<<grid_for(c, nv + ne, 256), 256, 0, c->stream>>>(A, (int32_t)nv, (int32_t)ne, flag);
@@ -528,9 +518,10 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats) {
     VC_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, thin_generations_kernel, kThreads, 0));
     if (per_sm <= 0) return VC_ERR_CUDA;
     const int G = c->num_sms * std::min(per_sm, c->thin_blocks_per_sm > 0 ? c->thin_blocks_per_sm : 8);
-    VC_TRY(ensure_n<int64_t>(c, c->blk_cnt, 2 * (int64_t)G));
-    VC_CUDA(c, cudaMemsetAsync(c->blk_cnt.p, 0, 2 * sizeof(int64_t) * G, c->stream));
+    VC_TRY(ensure_n<int64_t>(c, c->blk_cnt, 3 * (int64_t)G));
+    VC_CUDA(c, cudaMemsetAsync(c->blk_cnt.p, 0, 3 * sizeof(int64_t) * G, c->stream));
     A.blk_cnt = ptr<int64_t>(c->blk_cnt);
+    A.ncell_blk = reinterpret_cast<int*>(A.blk_cnt + 2 * (int64_t)G);
     void* args[] = {&A};
     {
         Region r(c, "thin_generations");

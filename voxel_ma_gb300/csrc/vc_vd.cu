@@ -28,8 +28,6 @@
 
 namespace vc {
 
-int build_adjacency(vc_ctx* c);
-
 namespace {
 
 struct Grid {
@@ -93,16 +91,24 @@ __device__ __forceinline__ bool face_valid(const Grid& g, int a, int b, int c, i
     return true;
 }
 
-// flags: bits 0-2 valid face along axis d; bit 3 vertex; bits 4-6 valid edge along d.
-__global__ void vd_flags_kernel(Grid g, uint8_t* __restrict__ flags, int32_t* __restrict__ vcnt,
-                                int32_t* __restrict__ ecnt, int32_t* __restrict__ fcnt, int64_t n) {
+// flags: bits 0-2 valid face along axis d; bit 3 vertex; bits 4-6 valid edge
+// along d.  lam[3p+d]: lambda of the valid face (p, d), computed once here.
+__global__ void vd_flags_kernel(Grid g, const float* __restrict__ sxyz, uint8_t* __restrict__ flags,
+                                float* __restrict__ lam, int64_t n) {
     for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
         int a, b, c;
         decode(p, g.NB, g.NC, a, b, c);
         uint32_t f = 0;
+        float l3[3] = {0.0f, 0.0f, 0.0f};
 #pragma unroll
-        for (int d = 0; d < 3; ++d)
-            if (face_valid(g, a, b, c, d)) f |= 1u << d;
+        for (int d = 0; d < 3; ++d) {
+            if (face_valid(g, a, b, c, d)) {
+                f |= 1u << d;
+                int e[3] = {a, b, c};
+                e[d] += 1;
+                l3[d] = lambda_of(sxyz, g.lab[p], g.label(e[0], e[1], e[2]));
+            }
+        }
         if (a < g.X && b < g.Y && c < g.Z && g.inside(a, b, c)) {
             int32_t L[8];
 #pragma unroll
@@ -112,12 +118,11 @@ __global__ void vd_flags_kernel(Grid g, uint8_t* __restrict__ flags, int32_t* __
             for (int q = 1; q < 8; ++q) alleq &= (L[q] == L[0]);
             if (!alleq) {
                 f |= 8u;
-                // plaquette of axis d: corners with offset 1 along d
 #pragma unroll
                 for (int d = 0; d < 3; ++d) {
-                    int ni = a + (d == 0), nj = b + (d == 1), nk = c + (d == 2);
+                    const int ni = a + (d == 0), nj = b + (d == 1), nk = c + (d == 2);
                     if (!g.inside(ni, nj, nk)) continue;
-                    const int bit = 1 << (2 - d);  // q bit of axis d: x->4, y->2, z->1
+                    const int bit = 1 << (2 - d);  // corner offset bit of axis d: x->4, y->2, z->1
                     int32_t ref = -2;
                     bool eq = true;
 #pragma unroll
@@ -131,30 +136,132 @@ __global__ void vd_flags_kernel(Grid g, uint8_t* __restrict__ flags, int32_t* __
             }
         }
         flags[p] = (uint8_t)f;
-        vcnt[p] = (f >> 3) & 1;
-        ecnt[p] = __popc((f >> 4) & 7u);
-        fcnt[p] = __popc(f & 7u);
+        lam[3 * p + 0] = l3[0];
+        lam[3 * p + 1] = l3[1];
+        lam[3 * p + 2] = l3[2];
     }
 }
 
-__device__ __forceinline__ int32_t edge_id(const uint8_t* flags, const int32_t* eoff, int64_t lp, int axis) {
-    const uint32_t f = flags[lp];
-    return eoff[lp] + __popc((f >> 4) & ((1u << axis) - 1u));
+__device__ __forceinline__ int32_t rank_below(uint32_t bits, int d) { return __popc(bits & ((1u << d) - 1u)); }
+
+// Valid faces incident to the axis edge (voxel (a,b,c), axis d): the lattice
+// edges of the plaquette shared by the voxel and its +d neighbour.  For each,
+// the lattice point, its axis and which of the face's two triangles carries
+// the edge (0: (q3,q0,q1), 1: (q3,q1,q2)).
+struct Inc {
+    int64_t lp;
+    int axis;
+    int tri;
+};
+__device__ __forceinline__ int plaquette_faces(const Grid& g, const uint8_t* __restrict__ flags, int a, int b, int c,
+                                               int d, Inc out[4]) {
+    const int u = (d + 1) % 3, w = (d + 2) % 3;
+    const int v[3] = {a, b, c};
+    int nb[3] = {a, b, c};
+    nb[d] += 1;
+    int k = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        // j < 2: lattice edge along u from nb + j e_w; j >= 2: along w from nb + (j-2) e_u
+        int cc[3] = {nb[0], nb[1], nb[2]};
+        const int ax = j < 2 ? u : w;
+        if (j < 2) cc[w] += j;
+        else cc[u] += j - 2;
+        const int64_t lp = g.lid(cc[0], cc[1], cc[2]);
+        if (!(flags[lp] & (1u << ax))) continue;
+        // position (s,t) of the edge's lower voxel in the face's quad
+        const int u2 = (ax + 1) % 3, w2 = (ax + 2) % 3;
+        const int s = v[u2] - (cc[u2] - 1), t = v[w2] - (cc[w2] - 1);
+        const int tri = d == u2 ? (t == 0 ? 0 : 1) : (s == 0 ? 0 : 1);
+        out[k++] = Inc{lp, ax, tri};
+    }
+    return k;
 }
 
-__global__ void vd_vertices_kernel(Grid g, const uint8_t* __restrict__ flags, const int32_t* __restrict__ voff,
-                                   const float* __restrict__ sxyz, float* __restrict__ vts, float* __restrict__ vm,
-                                   int32_t* __restrict__ bbox, int64_t n) {
+// Per lattice point: 1 if vertex; edges; faces; E->F entries of its axis
+// edges; V->E entries of its vertex.
+__global__ void vd_counts_kernel(Grid g, const uint8_t* __restrict__ flags, int32_t* __restrict__ cv,
+                                 int32_t* __restrict__ ce, int32_t* __restrict__ cf, int32_t* __restrict__ cef,
+                                 int32_t* __restrict__ cve, int64_t n) {
     for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
-        if (!(flags[p] & 8u)) continue;
+        const uint32_t fl = flags[p];
         int a, b, c;
         decode(p, g.NB, g.NC, a, b, c);
-        const int32_t v = voff[p];
+        int nef = 0, nve = 0;
+        if (fl & 0x70u) {
+            Inc inc[4];
+#pragma unroll
+            for (int d = 0; d < 3; ++d)
+                if (fl & (16u << d)) nef += plaquette_faces(g, flags, a, b, c, d, inc);
+        }
+        if (fl & 8u) {
+            const int v[3] = {a, b, c};
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                if (v[d] > 0) {
+                    int q[3] = {a, b, c};
+                    q[d] -= 1;
+                    if (flags[g.lid(q[0], q[1], q[2])] & (16u << d)) ++nve;
+                }
+                if (fl & (16u << d)) ++nve;
+                const int u = (d + 1) % 3, w = (d + 2) % 3;
+                int p1[3] = {a, b, c}, p3[3] = {a, b, c};
+                p1[w] += 1;  // the vertex is q1 of face (p1, d)
+                p3[u] += 1;  // the vertex is q3 of face (p3, d)
+                if (flags[g.lid(p1[0], p1[1], p1[2])] & (1u << d)) ++nve;
+                if (flags[g.lid(p3[0], p3[1], p3[2])] & (1u << d)) ++nve;
+            }
+        }
+        cv[p] = (fl >> 3) & 1u;
+        ce[p] = __popc((fl >> 4) & 7u);
+        cf[p] = __popc(fl & 7u);
+        cef[p] = nef;
+        cve[p] = nve;
+    }
+}
+
+struct Offs {
+    const int32_t* voff;
+    const int32_t* eoff;
+    const int32_t* foff;
+    const int32_t* efoff;
+    const int32_t* veoff;
+};
+
+__device__ __forceinline__ int32_t edge_id(const uint8_t* flags, const Offs& o, int64_t lp, int d) {
+    return o.eoff[lp] + rank_below((flags[lp] >> 4) & 7u, d);
+}
+__device__ __forceinline__ int32_t face_id(const uint8_t* flags, const Offs& o, int64_t lp, int d) {
+    return o.foff[lp] + rank_below(flags[lp] & 7u, d);
+}
+
+template <int N>
+__device__ __forceinline__ void sort_small(int32_t* x, int k) {
+    for (int i = 1; i < k; ++i) {
+        const int32_t v = x[i];
+        int j = i - 1;
+        while (j >= 0 && x[j] > v) {
+            x[j + 1] = x[j];
+            --j;
+        }
+        x[j + 1] = v;
+    }
+}
+
+__global__ void vd_vertices_kernel(Grid g, const uint8_t* __restrict__ flags, Offs o, const float* __restrict__ lam,
+                                   int32_t ne_axis, float* __restrict__ vts, float* __restrict__ vm,
+                                   int32_t* __restrict__ ve_off, int32_t* __restrict__ ve_ids, VertRec* __restrict__ V,
+                                   int32_t* __restrict__ bbox, int64_t n) {
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t fl = flags[p];
+        if (!(fl & 8u)) continue;
+        int a, b, c;
+        decode(p, g.NB, g.NC, a, b, c);
+        const int32_t v = o.voff[p];
         vts[3 * (int64_t)v + 0] = (float)a;
         vts[3 * (int64_t)v + 1] = (float)b;
         vts[3 * (int64_t)v + 2] = (float)c;
-        // the 12 cube edges of voxel (a,b,c): along d, starting at the cube
-        // corners whose d-offset is 0
+        // vertex lambda: max over the valid faces of the voxel's 12 cube edges
         float m = 0.0f;
 #pragma unroll
         for (int d = 0; d < 3; ++d)
@@ -162,17 +269,52 @@ __global__ void vd_vertices_kernel(Grid g, const uint8_t* __restrict__ flags, co
             for (int s = 0; s < 2; ++s)
 #pragma unroll
                 for (int t = 0; t < 2; ++t) {
-                    int o[3];
-                    o[d] = 0;
-                    o[(d + 1) % 3] = s;
-                    o[(d + 2) % 3] = t;
-                    const int64_t lp = g.lid(a + o[0], b + o[1], c + o[2]);
-                    if (!(flags[lp] & (1u << d))) continue;
-                    int e[3] = {a + o[0], b + o[1], c + o[2]};
-                    e[d] += 1;
-                    m = fmaxf(m, lambda_of(sxyz, g.lab[lp], g.label(e[0], e[1], e[2])));
+                    int q[3] = {a, b, c};
+                    q[(d + 1) % 3] += s;
+                    q[(d + 2) % 3] += t;
+                    const int64_t lp = g.lid(q[0], q[1], q[2]);
+                    if (flags[lp] & (1u << d)) m = fmaxf(m, lam[3 * lp + d]);
                 }
         vm[v] = m;
+        // V->E list in edge-id order: axis edges (their lower voxels precede
+        // this one in lattice order, then this voxel's own), then diagonals
+        const int32_t off = o.veoff[p];
+        int k = 0;
+        const int vv[3] = {a, b, c};
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            if (vv[d] == 0) continue;
+            int q[3] = {a, b, c};
+            q[d] -= 1;
+            const int64_t lq = g.lid(q[0], q[1], q[2]);
+            if (flags[lq] & (16u << d)) ve_ids[off + k++] = edge_id(flags, o, lq, d);
+        }
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+            if (fl & (16u << d)) ve_ids[off + k++] = edge_id(flags, o, p, d);
+        int32_t dg[6];
+        int nd = 0;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const int u = (d + 1) % 3, w = (d + 2) % 3;
+            int p1[3] = {a, b, c}, p3[3] = {a, b, c};
+            p1[w] += 1;
+            p3[u] += 1;
+            const int64_t l1 = g.lid(p1[0], p1[1], p1[2]), l3 = g.lid(p3[0], p3[1], p3[2]);
+            if (flags[l1] & (1u << d)) dg[nd++] = face_id(flags, o, l1, d);
+            if (flags[l3] & (1u << d)) dg[nd++] = face_id(flags, o, l3, d);
+        }
+        sort_small<6>(dg, nd);
+        for (int i = 0; i < nd; ++i) ve_ids[off + k++] = ne_axis + dg[i];
+        ve_off[v] = off;
+        VertRec r;
+        r.ve_off = off;
+        r.ve_cnt = k;
+        r.rm = kAlive;
+        r.ref = k;
+        r.trig = -1;
+        r.pad0 = r.pad1 = r.pad2 = 0;
+        V[v] = r;
         atomicMin(&bbox[0], a);
         atomicMin(&bbox[1], b);
         atomicMin(&bbox[2], c);
@@ -182,66 +324,63 @@ __global__ void vd_vertices_kernel(Grid g, const uint8_t* __restrict__ flags, co
     }
 }
 
-__global__ void vd_edges_kernel(Grid g, const uint8_t* __restrict__ flags, const int32_t* __restrict__ voff,
-                                const int32_t* __restrict__ eoff, const float* __restrict__ sxyz,
-                                int2* __restrict__ edges, float* __restrict__ em, int64_t n) {
+__global__ void vd_edges_kernel(Grid g, const uint8_t* __restrict__ flags, Offs o, const float* __restrict__ lam,
+                                int2* __restrict__ edges, float* __restrict__ em, int32_t* __restrict__ ef_off,
+                                int32_t* __restrict__ ef_ids, EdgeRec* __restrict__ E, int64_t n) {
     for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
-        const uint32_t f = flags[p];
-        if (!(f & 0x70u)) continue;
+        const uint32_t fl = flags[p];
+        if (!(fl & 0x70u)) continue;
         int a, b, c;
         decode(p, g.NB, g.NC, a, b, c);
-        int32_t e = eoff[p];
+        int32_t e = o.eoff[p];
+        int32_t efo = o.efoff[p];
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-            if (!(f & (16u << d))) continue;
-            const int u = (d + 1) % 3, w = (d + 2) % 3;
+            if (!(fl & (16u << d))) continue;
             int nb[3] = {a, b, c};
             nb[d] += 1;
-            const int32_t v0 = voff[p], v1 = voff[g.lid(nb[0], nb[1], nb[2])];
-            // plaquette corners: (v + e_d) + s e_u + t e_w; its lattice edges run
-            // along u from the t corners with s = 0 and along w from the s corners with t = 0
+            const int32_t v0 = o.voff[p], v1 = o.voff[g.lid(nb[0], nb[1], nb[2])];
+            Inc inc[4];
+            const int k = plaquette_faces(g, flags, a, b, c, d, inc);
             float m = 0.0f;
-#pragma unroll
-            for (int t = 0; t < 2; ++t) {
-                int cc[3] = {nb[0], nb[1], nb[2]};
-                cc[w] += t;
-                const int64_t lp = g.lid(cc[0], cc[1], cc[2]);
-                if (flags[lp] & (1u << u)) {
-                    int ee[3] = {cc[0], cc[1], cc[2]};
-                    ee[u] += 1;
-                    m = fmaxf(m, lambda_of(sxyz, g.lab[lp], g.label(ee[0], ee[1], ee[2])));
-                }
+            int32_t tl[4];
+            for (int j = 0; j < k; ++j) {
+                m = fmaxf(m, lam[3 * inc[j].lp + inc[j].axis]);
+                tl[j] = 2 * face_id(flags, o, inc[j].lp, inc[j].axis) + inc[j].tri;
             }
-#pragma unroll
-            for (int s = 0; s < 2; ++s) {
-                int cc[3] = {nb[0], nb[1], nb[2]};
-                cc[u] += s;
-                const int64_t lp = g.lid(cc[0], cc[1], cc[2]);
-                if (flags[lp] & (1u << w)) {
-                    int ee[3] = {cc[0], cc[1], cc[2]};
-                    ee[w] += 1;
-                    m = fmaxf(m, lambda_of(sxyz, g.lab[lp], g.label(ee[0], ee[1], ee[2])));
-                }
-            }
+            sort_small<4>(tl, k);
+            for (int j = 0; j < k; ++j) ef_ids[efo + j] = tl[j];
             edges[e] = make_int2(v0, v1);
             em[e] = m;
+            ef_off[e] = efo;
+            EdgeRec r;
+            r.v0 = v0;
+            r.v1 = v1;
+            r.em = m;
+            r.ef_off = efo;
+            r.ef_cnt = k;
+            r.rm = kAlive;
+            r.ref = k;
+            r.trig = -1;
+            E[e] = r;
+            efo += k;
             ++e;
         }
     }
 }
 
-__global__ void vd_faces_kernel(Grid g, const uint8_t* __restrict__ flags, const int32_t* __restrict__ voff,
-                                const int32_t* __restrict__ eoff, const int32_t* __restrict__ foff,
-                                const float* __restrict__ sxyz, int32_t ne_axis, int2* __restrict__ edges,
-                                float* __restrict__ em, int32_t* __restrict__ tris, int32_t* __restrict__ tri_edges,
-                                float* __restrict__ fm, int32_t* __restrict__ tri_face,
-                                int2* __restrict__ face_sites, int64_t n) {
+__global__ void vd_faces_kernel(Grid g, const uint8_t* __restrict__ flags, Offs o, const float* __restrict__ lam,
+                                int32_t ne_axis, int32_t ef_axis, int2* __restrict__ edges, float* __restrict__ em,
+                                int32_t* __restrict__ ef_off, int32_t* __restrict__ ef_ids, int32_t* __restrict__ tris,
+                                int32_t* __restrict__ tri_edges, float* __restrict__ fm,
+                                int32_t* __restrict__ tri_face, int2* __restrict__ face_sites,
+                                FaceRec* __restrict__ F, EdgeRec* __restrict__ E, int64_t n) {
     for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
         const uint32_t fl = flags[p];
         if (!(fl & 7u)) continue;
         int a, b, c;
         decode(p, g.NB, g.NC, a, b, c);
-        int32_t f = foff[p];
+        int32_t f = o.foff[p];
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             if (!(fl & (1u << d))) continue;
@@ -249,7 +388,7 @@ __global__ void vd_faces_kernel(Grid g, const uint8_t* __restrict__ flags, const
             int e1[3] = {a, b, c};
             e1[d] += 1;
             const int32_t s0 = g.lab[p], s1 = g.label(e1[0], e1[1], e1[2]);
-            const float lam = lambda_of(sxyz, s0, s1);
+            const float lm = lam[3 * p + d];
             int64_t ql[4];
             int32_t q[4];
 #pragma unroll
@@ -257,13 +396,13 @@ __global__ void vd_faces_kernel(Grid g, const uint8_t* __restrict__ flags, const
                 int i, j, k;
                 quad_voxel(a, b, c, d, m, i, j, k);
                 ql[m] = g.lid(i, j, k);
-                q[m] = voff[ql[m]];
+                q[m] = o.voff[ql[m]];
             }
             const int32_t diag = ne_axis + f;
-            const int32_t e01 = edge_id(flags, eoff, ql[0], u);
-            const int32_t e12 = edge_id(flags, eoff, ql[1], w);
-            const int32_t e32 = edge_id(flags, eoff, ql[3], u);
-            const int32_t e03 = edge_id(flags, eoff, ql[0], w);
+            const int32_t e01 = edge_id(flags, o, ql[0], u);
+            const int32_t e12 = edge_id(flags, o, ql[1], w);
+            const int32_t e32 = edge_id(flags, o, ql[3], u);
+            const int32_t e03 = edge_id(flags, o, ql[0], w);
             const int64_t t0 = 2 * (int64_t)f, t1 = t0 + 1;
             tris[3 * t0 + 0] = q[3];
             tris[3 * t0 + 1] = q[0];
@@ -278,15 +417,51 @@ __global__ void vd_faces_kernel(Grid g, const uint8_t* __restrict__ flags, const
             tri_edges[3 * t1 + 0] = diag;
             tri_edges[3 * t1 + 1] = e12;
             tri_edges[3 * t1 + 2] = e32;
-            fm[t0] = lam;
-            fm[t1] = lam;
+            fm[t0] = lm;
+            fm[t1] = lm;
             tri_face[t0] = f;
             tri_face[t1] = f;
             face_sites[f] = make_int2(s0, s1);
-            edges[diag] = make_int2(min(q[1], q[3]), max(q[1], q[3]));
-            em[diag] = lam;
+            FaceRec fr;
+            fr.fm = lm;
+            fr.rm = kAlive;
+            fr.pad0 = fr.pad1 = fr.pad2 = 0;
+            fr.e0 = e03;
+            fr.e1 = e01;
+            fr.e2 = diag;
+            F[t0] = fr;
+            fr.e0 = diag;
+            fr.e1 = e12;
+            fr.e2 = e32;
+            F[t1] = fr;
+            // the diagonal: new edge of this face, incident to both triangles
+            const int32_t dv0 = min(q[1], q[3]), dv1 = max(q[1], q[3]);
+            const int32_t efo = ef_axis + 2 * f;
+            edges[diag] = make_int2(dv0, dv1);
+            em[diag] = lm;
+            ef_off[diag] = efo;
+            ef_ids[efo] = (int32_t)t0;
+            ef_ids[efo + 1] = (int32_t)t1;
+            EdgeRec er;
+            er.v0 = dv0;
+            er.v1 = dv1;
+            er.em = lm;
+            er.ef_off = efo;
+            er.ef_cnt = 2;
+            er.rm = kAlive;
+            er.ref = 2;
+            er.trig = -1;
+            E[diag] = er;
             ++f;
         }
+    }
+}
+
+__global__ void vd_tail_kernel(int32_t* bbox, int32_t* ve_off, int32_t nv, int32_t nve, int32_t* ef_off, int32_t ne,
+                               int32_t nef) {
+    if (threadIdx.x == 0) {
+        ve_off[nv] = nve;
+        ef_off[ne] = nef;
     }
 }
 
@@ -306,36 +481,49 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes) {
     if (!c->ft_valid) return VC_ERR_STATE;
     const int64_t NB = c->Y + 1, NC = c->Z + 1;
     const int64_t N = (int64_t)(c->X + 1) * NB * NC;
+    Region stage(c, "stage_vd");
     VC_TRY(ensure_n<uint8_t>(c, c->vd_flags, N));
+    VC_TRY(ensure_n<float>(c, c->vd_lam, 3 * N));
     VC_TRY(ensure_n<int32_t>(c, c->vd_voff, N));
     VC_TRY(ensure_n<int32_t>(c, c->vd_eoff, N));
     VC_TRY(ensure_n<int32_t>(c, c->vd_foff, N));
-    VC_TRY(ensure_n<int64_t>(c, c->scratch2, 4));
+    VC_TRY(ensure_n<int32_t>(c, c->vd_efoff, N));
+    VC_TRY(ensure_n<int32_t>(c, c->vd_veoff, N));
+    VC_TRY(ensure_n<int64_t>(c, c->scratch2, 8));
     VC_TRY(ensure_n<int32_t>(c, c->vd_bbox, 8));
-    Region stage(c, "stage_vd");
     Grid g{ptr<uint8_t>(c->occ), ptr<int32_t>(c->ft_id), c->X, c->Y, c->Z, NB, NC};
     uint8_t* flags = ptr<uint8_t>(c->vd_flags);
-    int32_t* voff = ptr<int32_t>(c->vd_voff);
-    int32_t* eoff = ptr<int32_t>(c->vd_eoff);
-    int32_t* foff = ptr<int32_t>(c->vd_foff);
+    float* lam = ptr<float>(c->vd_lam);
+    int32_t* cnt[5] = {ptr<int32_t>(c->vd_voff), ptr<int32_t>(c->vd_eoff), ptr<int32_t>(c->vd_foff),
+                       ptr<int32_t>(c->vd_efoff), ptr<int32_t>(c->vd_veoff)};
+    const float* sxyz = ptr<float>(c->site_xyz);
     {
-    Region r(c, "vd_flags");
-    vd_flags_kernel<<<grid_for(c, N, 256), 256, 0, c->stream>>>(g, flags, voff, eoff, foff, N);
-    launched(c);
+        Region r(c, "vd_flags");
+        vd_flags_kernel<<<grid_for(c, N, 256), 256, 0, c->stream>>>(g, sxyz, flags, lam, N);
+        launched(c);
+        vd_counts_kernel<<<grid_for(c, N, 256), 256, 0, c->stream>>>(g, flags, cnt[0], cnt[1], cnt[2], cnt[3],
+                                                                      cnt[4], N);
+        launched(c);
+        VC_CUDA(c, cudaGetLastError());
     }
-    VC_CUDA(c, cudaGetLastError());
     int64_t* tot = ptr<int64_t>(c->scratch2);
-    VC_TRY(scan_exclusive_i32(c, voff, voff, N, tot + 0));
-    VC_TRY(scan_exclusive_i32(c, eoff, eoff, N, tot + 1));
-    VC_TRY(scan_exclusive_i32(c, foff, foff, N, tot + 2));
-    int64_t h[3];
-    VC_CUDA(c, cudaMemcpyAsync(h, tot, 3 * sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
+    {
+        Region r(c, "vd_scan");
+        for (int k = 0; k < 5; ++k) VC_TRY(scan_exclusive_i32(c, cnt[k], cnt[k], N, tot + k));
+    }
+    int64_t h[5];
+    VC_CUDA(c, cudaMemcpyAsync(h, tot, 5 * sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
     VC_TRY(sync_check(c));
-    const int64_t nv = h[0], ne_axis = h[1], nface = h[2];
+    const int64_t nv = h[0], ne_axis = h[1], nface = h[2], nef_axis = h[3], nve = h[4];
     const int64_t ne = ne_axis + nface, nt = 2 * nface;
-    if (ne >= INT32_MAX || nt >= INT32_MAX || nv >= INT32_MAX) return VC_ERR_ARG;
+    if (ne >= INT32_MAX || 3 * nt >= INT32_MAX || nv >= INT32_MAX || nve >= INT32_MAX) return VC_ERR_ARG;
+    if (nef_axis != 4 * nface || nve != 2 * ne) {
+        c->last_error = "lattice complex incidence counts are inconsistent";
+        return VC_ERR_INVARIANT;
+    }
     // the complex becomes the context's finalized cell complex
     c->cc_valid = c->cc_finalized = c->meas_valid = c->thin_valid = c->rem_valid = false;
+    c->records_fresh = false;
     VC_TRY(ensure_n<float>(c, c->vts, 3 * nv));
     VC_TRY(ensure_n<int2>(c, c->edges, ne));
     VC_TRY(ensure_n<int32_t>(c, c->tris, 3 * nt));
@@ -345,25 +533,38 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes) {
     VC_TRY(ensure_n<float>(c, c->fm, nt));
     VC_TRY(ensure_n<int32_t>(c, c->vd_tri_face, nt));
     VC_TRY(ensure_n<int2>(c, c->vd_face_sites, nface));
+    VC_TRY(ensure_n<int32_t>(c, c->ve_off, nv + 1));
+    VC_TRY(ensure_n<int32_t>(c, c->ve_ids, 2 * ne));
+    VC_TRY(ensure_n<int32_t>(c, c->ef_off, ne + 1));
+    VC_TRY(ensure_n<int32_t>(c, c->ef_ids, 3 * nt));
+    VC_TRY(ensure_n<FaceRec>(c, c->face_rec, nt));
+    VC_TRY(ensure_n<EdgeRec>(c, c->edge_rec, ne));
+    VC_TRY(ensure_n<VertRec>(c, c->vert_rec, nv));
     int32_t* bbox = ptr<int32_t>(c->vd_bbox);
     init_bbox_kernel<<<1, 32, 0, c->stream>>>(bbox);
     launched(c);
-    const float* sxyz = ptr<float>(c->site_xyz);
+    Offs o{cnt[0], cnt[1], cnt[2], cnt[3], cnt[4]};
     {
-    Region r(c, "vd_emit");
-    vd_vertices_kernel<<<grid_for(c, N, 256), 256, 0, c->stream>>>(g, flags, voff, sxyz, ptr<float>(c->vts),
-                                                                    ptr<float>(c->vm), bbox, N);
-    launched(c);
-    vd_edges_kernel<<<grid_for(c, N, 256), 256, 0, c->stream>>>(g, flags, voff, eoff, sxyz, ptr<int2>(c->edges),
-                                                                 ptr<float>(c->em), N);
-    launched(c);
-    vd_faces_kernel<<<grid_for(c, N, 256), 256, 0, c->stream>>>(
-        g, flags, voff, eoff, foff, sxyz, (int32_t)ne_axis, ptr<int2>(c->edges), ptr<float>(c->em),
-        ptr<int32_t>(c->tris), ptr<int32_t>(c->tri_edges), ptr<float>(c->fm), ptr<int32_t>(c->vd_tri_face),
-        ptr<int2>(c->vd_face_sites), N);
-    launched(c);
+        Region r(c, "vd_emit");
+        vd_vertices_kernel<<<grid_for(c, N, 256), 256, 0, c->stream>>>(
+            g, flags, o, lam, (int32_t)ne_axis, ptr<float>(c->vts), ptr<float>(c->vm), ptr<int32_t>(c->ve_off),
+            ptr<int32_t>(c->ve_ids), ptr<VertRec>(c->vert_rec), bbox, N);
+        launched(c);
+        vd_edges_kernel<<<grid_for(c, N, 256), 256, 0, c->stream>>>(
+            g, flags, o, lam, ptr<int2>(c->edges), ptr<float>(c->em), ptr<int32_t>(c->ef_off),
+            ptr<int32_t>(c->ef_ids), ptr<EdgeRec>(c->edge_rec), N);
+        launched(c);
+        vd_faces_kernel<<<grid_for(c, N, 256), 256, 0, c->stream>>>(
+            g, flags, o, lam, (int32_t)ne_axis, (int32_t)nef_axis, ptr<int2>(c->edges), ptr<float>(c->em),
+            ptr<int32_t>(c->ef_off), ptr<int32_t>(c->ef_ids), ptr<int32_t>(c->tris), ptr<int32_t>(c->tri_edges),
+            ptr<float>(c->fm), ptr<int32_t>(c->vd_tri_face), ptr<int2>(c->vd_face_sites),
+            ptr<FaceRec>(c->face_rec), ptr<EdgeRec>(c->edge_rec), N);
+        launched(c);
+        vd_tail_kernel<<<1, 32, 0, c->stream>>>(bbox, ptr<int32_t>(c->ve_off), (int32_t)nv, (int32_t)nve,
+                                                ptr<int32_t>(c->ef_off), (int32_t)ne, (int32_t)(3 * nt));
+        launched(c);
+        VC_CUDA(c, cudaGetLastError());
     }
-    VC_CUDA(c, cudaGetLastError());
     int32_t hb[6];
     VC_CUDA(c, cudaMemcpyAsync(hb, bbox, 6 * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
     VC_TRY(sync_check(c));
@@ -381,9 +582,9 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes) {
     c->vd = vc_vd_sizes{nv, ne, nt, nface, isz};
     c->vd_valid = true;
     c->cc_valid = true;
-    VC_TRY(build_adjacency(c));
     c->cc_finalized = true;
     c->meas_valid = true;
+    c->records_fresh = true;
     if (sizes) *sizes = c->vd;
     return VC_OK;
 }
