@@ -1,0 +1,57 @@
+"""The C++ adapters (include/voxelcore_gb300.hpp) keep the reference's class
+surfaces; a driver written like exportInsideVoroMesh compiles against them
+and, on a GPU, reproduces the oracle's surviving cell set."""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
+SRC = os.path.join(ROOT, "tests", "cpp", "adapter_main.cpp")
+
+
+def _compile(out, syntax_only=False):
+    from voxel_ma_gb300 import _lib
+    _lib.load()  # builds the library if needed
+    cmd = ["g++", "-std=c++17", "-O2", "-I" + os.path.join(ROOT, "include"), SRC]
+    if syntax_only:
+        cmd += ["-fsyntax-only"]
+    else:
+        libdir = os.path.join(ROOT, "voxel_ma_gb300")
+        cmd += ["-o", out, "-L" + libdir, "-lvoxelcore_gb300", "-Wl,-rpath," + libdir]
+    subprocess.run(cmd, check=True, capture_output=True, text=True)
+
+
+@pytest.mark.skipif(shutil.which("g++") is None, reason="no g++")
+def test_adapter_header_compiles():
+    _compile(None, syntax_only=True)
+
+
+@pytest.mark.gpu
+@pytest.mark.skipif(shutil.which("g++") is None, reason="no g++")
+@pytest.mark.parametrize("t", [0.04, 0.2])
+def test_adapter_drives_gpu_path_like_the_reference(tmp_path, t):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import oracle
+    from voxel_ma_gb300 import volumes
+    exe = str(tmp_path / "adapter_main")
+    _compile(exe)
+    occ = volumes.csg(7, 24, 40)
+    vol = tmp_path / "vol.bin"
+    with open(vol, "wb") as f:
+        f.write(np.array(occ.shape, np.int32).tobytes())
+        f.write(np.ascontiguousarray(occ).tobytes())
+    out = subprocess.run([exe, str(vol), str(t)], check=True, capture_output=True, text=True).stdout
+    lines = dict(line.split(" ", 1) if " " in line else (line, "") for line in out.strip().splitlines())
+    ref = oracle.run_plain(occ, t=t)
+    assert int(lines["sites"]) == len(ref["sites"])
+    assert np.float32(float(lines["thresh"])) == np.float32(ref["thresh"])
+    for key in ("keep_v", "keep_e", "keep_f"):
+        got = np.array([int(x) for x in lines[key].split()], np.int64)
+        assert np.array_equal(got, np.nonzero(ref["thin"][key])[0]), key
+    nv, ne, nt = (int(x) for x in lines["remaining"].split())
+    assert (nv, ne, nt) == (len(ref["rem_vts"]), len(ref["rem_edges"]), len(ref["rem_tris"]))
