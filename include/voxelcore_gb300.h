@@ -154,6 +154,25 @@ typedef struct {
 } vc_plain_result;
 int vc_run_plain(vc_ctx* ctx, const uint8_t* occ, int X, int Y, int Z, int mem, double t, vc_plain_result* out);
 
+/* ---- site extraction without device allocation ---------------------------
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc
+ * (a host framework or allocator that owns the device heap, or a plugin that
+ * must not grow the process's device footprint): the same sites as
+ * vc_extract_sites + vc_get_sites, computed with no context and no
+ * allocation.  The scratch is a fixed array inside the library that every
+ * GPU loading the library holds until the process exits; volumes are
+ * limited to 4,194,304 voxels (X*Y*Z), larger ones return VC_ERR_ARG.
+ * occ: device pointer to X*Y*Z bytes; xyz: device pointer with room for
+ * `capacity` sites (3 floats each); *n_sites (host) receives the site count
+ * -- when it exceeds `capacity` the call returns VC_ERR_ARG and writes no
+ * site.  stream: a cudaStream_t (NULL = the legacy default stream); the
+ * call synchronizes it.  The first call on a device looks up the scratch
+ * addresses, so make it before capturing a stream on that device.  All
+ * calls share the scratch: calls that overlap on the GPU (other streams or
+ * host threads) race and must be serialized by the caller.                */
+int vc_extract_sites_noalloc(const uint8_t* occ, int X, int Y, int Z, float* xyz, int64_t capacity, int64_t* n_sites,
+                             void* stream);
+
 /* ---- diagnostics ---------------------------------------------------------
  * Per-generation trace of the thinning kernel: with cap > 0 the next vc_thin
  * records, for up to `cap` generations, {items, t_phaseA, t_phaseB, t_phaseC}

@@ -10,6 +10,9 @@
 // per voxel from the voxel's 3x3x3 neighbourhood, so the site list comes out
 // in the reference's order after one exclusive scan of per-voxel counts.
 #include "vc_internal.cuh"
+#include "vc_scan.cuh"
+
+#include <mutex>
 
 namespace vc {
 namespace {
@@ -129,7 +132,7 @@ __global__ void sites_emit_kernel(Vol v, const int32_t* __restrict__ off, float*
                 xyz[3 * (int64_t)o + 0] = (float)a - 0.5f;
                 xyz[3 * (int64_t)o + 1] = (float)b - 0.5f;
                 xyz[3 * (int64_t)o + 2] = (float)cc - 0.5f;
-                site_id_lat[((int64_t)a * NB + b) * NC + cc] = o;
+                if (site_id_lat) site_id_lat[((int64_t)a * NB + b) * NC + cc] = o;
                 ++o;
             }
         }
@@ -173,4 +176,105 @@ int run_sites(vc_ctx* c, int64_t* n_sites) {
     return VC_OK;
 }
 
+
+// ---------------------------------------------------------------------------
+// Site extraction for callers that cannot allocate device memory.
+//
+// Code that runs where cudaMalloc is unavailable or unwanted -- inside a
+// memory-capped allocator that owns the whole device heap, a host framework
+// that forbids allocation on its hot path, or a plugin that must not change
+// the process's memory footprint after start-up -- still needs scratch for the
+// per-voxel counts and the scan.  This variant takes that scratch from a
+// fixed-size array in this file instead of allocating: every GPU that loads
+// the library holds it (16 MiB of counts plus the scan's tile sums) until the
+// process exits.  Volumes are limited to kNoAllocMaxVoxels voxels.
+namespace {
+
+constexpr int64_t kNoAllocMaxVoxels = (int64_t)1 << 22;  // 4,194,304 voxels, e.g. 128 x 128 x 256
+constexpr int64_t kNoAllocTiles = kNoAllocMaxVoxels / kScanTile + 1;
+
+// Device-side scratch.  In host code these names are host-side stand-ins,
+// not device addresses: the host takes their addresses with
+// cudaGetSymbolAddress (once per device) and passes those to the kernels.
+static __device__ __align__(256) int32_t g_noalloc_counts[kNoAllocMaxVoxels];
+static __device__ __align__(256) int64_t g_noalloc_tiles[kNoAllocTiles + 1];  // last entry: the total
+
+struct NoAllocScratch {
+    int32_t* counts = nullptr;
+    int64_t* tiles = nullptr;
+    int64_t* total = nullptr;
+    int num_sms = 0;
+    bool ready = false;
+};
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+NoAllocScratch g_noalloc[kMaxDevices];
+
+// Device addresses of the scratch arrays for the current device; the first
+// call on a device looks them up (so that first call must not be made while
+// a stream is being captured).
+int noalloc_scratch(NoAllocScratch* out) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+        cudaGetLastError();
+        return VC_ERR_CUDA;
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    NoAllocScratch& s = g_noalloc[dev];
+    if (!s.ready) {
+        void* counts = nullptr;
+        void* tiles = nullptr;
+        if (cudaGetSymbolAddress(&counts, g_noalloc_counts) != cudaSuccess ||
+            cudaGetSymbolAddress(&tiles, g_noalloc_tiles) != cudaSuccess ||
+            cudaDeviceGetAttribute(&s.num_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+            cudaGetLastError();
+            return VC_ERR_CUDA;
+        }
+        s.counts = static_cast<int32_t*>(counts);
+        s.tiles = static_cast<int64_t*>(tiles);
+        s.total = s.tiles + kNoAllocTiles;
+        s.ready = true;
+    }
+    *out = s;
+    return VC_OK;
+}
+
+}  // namespace
 }  // namespace vc
+
+extern "C" int vc_extract_sites_noalloc(const uint8_t* occ, int X, int Y, int Z, float* xyz, int64_t capacity,
+                                        int64_t* n_sites, void* stream) {
+    using namespace vc;
+    if (!occ || !n_sites || X <= 0 || Y <= 0 || Z <= 0 || capacity < 0) return VC_ERR_ARG;
+    const int64_t nvox = (int64_t)X * Y * Z;
+    if (nvox > kNoAllocMaxVoxels) return VC_ERR_ARG;  // beyond the static scratch
+    NoAllocScratch s;
+    VC_TRY(noalloc_scratch(&s));
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const Vol v{occ, X, Y, Z};
+    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((nvox + 255) / 256, (int64_t)s.num_sms * 16));
+    // every scratch word read below is written first in this call: counts by
+    // the count kernel, tile sums and the total by the scan
+    sites_count_kernel<<<blocks, 256, 0, st>>>(v, s.counts);
+    const int64_t tiles = (nvox + kScanTile - 1) / kScanTile;
+    scan_tile_sums<int32_t><<<(unsigned)tiles, kScanThreads, 0, st>>>(s.counts, nvox, s.tiles);
+    scan_sums_single<<<1, 1024, 0, st>>>(s.tiles, tiles, s.total);
+    scan_apply<int32_t><<<(unsigned)tiles, kScanThreads, 0, st>>>(s.counts, s.counts, nvox, s.tiles);
+    int64_t n = 0;
+    if (cudaMemcpyAsync(&n, s.total, sizeof(int64_t), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess) {
+        cudaGetLastError();
+        return VC_ERR_CUDA;
+    }
+    *n_sites = n;
+    if (n > capacity) return VC_ERR_ARG;  // *n_sites tells the caller how much room is needed
+    if (n > 0) {
+        if (!xyz) return VC_ERR_ARG;
+        sites_emit_kernel<<<blocks, 256, 0, st>>>(v, s.counts, xyz, nullptr);
+    }
+    if (cudaStreamSynchronize(st) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
+        cudaGetLastError();
+        return VC_ERR_CUDA;
+    }
+    return VC_OK;
+}
