@@ -98,52 +98,51 @@ __device__ __forceinline__ uint32_t new_corner_mask(uint32_t nb, uint32_t inb) {
 }
 
 __global__ void sites_count_kernel(Vol v, int32_t* __restrict__ cnt) {
-    const int64_t n = (int64_t)v.X * v.Y * v.Z;
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
-        const int k = (int)(t % v.Z);
-        const int j = (int)((t / v.Z) % v.Y);
-        const int i = (int)(t / ((int64_t)v.Z * v.Y));
-        const uint32_t nb = load_nbhd(v, i, j, k);
-        cnt[t] = __popc(new_corner_mask(nb, inbox_nbhd(v, i, j, k)));
+    for (int64_t row = blockIdx.x; row < (int64_t)v.X * v.Y; row += gridDim.x) {
+        const int i = (int)(row / v.Y), j = (int)(row - (int64_t)i * v.Y);
+        for (int k = threadIdx.x; k < v.Z; k += blockDim.x) {
+            const int64_t t = row * v.Z + k;
+            const uint32_t nb = load_nbhd(v, i, j, k);
+            cnt[t] = __popc(new_corner_mask(nb, inbox_nbhd(v, i, j, k)));
+        }
     }
 }
 
 __global__ void sites_emit_kernel(Vol v, const int32_t* __restrict__ off, float* __restrict__ xyz,
                                   int32_t* __restrict__ site_id_lat) {
-    const int64_t n = (int64_t)v.X * v.Y * v.Z;
     const int64_t NB = v.Y + 1, NC = v.Z + 1;
-    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
-        const int k = (int)(t % v.Z);
-        const int j = (int)((t / v.Z) % v.Y);
-        const int i = (int)(t / ((int64_t)v.Z * v.Y));
-        const uint32_t nb = load_nbhd(v, i, j, k);
-        const uint32_t mask = new_corner_mask(nb, inbox_nbhd(v, i, j, k));
-        if (!mask) continue;
-        int32_t o = off[t];
-        const int cur = nb_bit(nb, 0, 0, 0);
-        uint32_t done = 0;
-        for (int d = 0; d < 6; ++d) {
-            if (nb_bit(nb, kNbOff[d][0], kNbOff[d][1], kNbOff[d][2]) == cur) continue;
-            for (int s = 0; s < 4; ++s) {
-                const int c = kShared[d][s];
-                if (!(mask & (1u << c)) || (done & (1u << c))) continue;
-                done |= 1u << c;
-                const int a = i + kCornerOff[c][0], b = j + kCornerOff[c][1], cc = k + kCornerOff[c][2];
-                xyz[3 * (int64_t)o + 0] = (float)a - 0.5f;
-                xyz[3 * (int64_t)o + 1] = (float)b - 0.5f;
-                xyz[3 * (int64_t)o + 2] = (float)cc - 0.5f;
-                if (site_id_lat) site_id_lat[((int64_t)a * NB + b) * NC + cc] = o;
-                ++o;
+    for (int64_t row = blockIdx.x; row < (int64_t)v.X * v.Y; row += gridDim.x) {
+        const int i = (int)(row / v.Y), j = (int)(row - (int64_t)i * v.Y);
+        for (int k = threadIdx.x; k < v.Z; k += blockDim.x) {
+            const int64_t t = row * v.Z + k;
+            const uint32_t nb = load_nbhd(v, i, j, k);
+            const uint32_t mask = new_corner_mask(nb, inbox_nbhd(v, i, j, k));
+            if (!mask) continue;
+            int32_t o = off[t];
+            const int cur = nb_bit(nb, 0, 0, 0);
+            uint32_t done = 0;
+            for (int d = 0; d < 6; ++d) {
+                if (nb_bit(nb, kNbOff[d][0], kNbOff[d][1], kNbOff[d][2]) == cur) continue;
+                for (int s = 0; s < 4; ++s) {
+                    const int c = kShared[d][s];
+                    if (!(mask & (1u << c)) || (done & (1u << c))) continue;
+                    done |= 1u << c;
+                    const int a = i + kCornerOff[c][0], b = j + kCornerOff[c][1], cc = k + kCornerOff[c][2];
+                    xyz[3 * (int64_t)o + 0] = (float)a - 0.5f;
+                    xyz[3 * (int64_t)o + 1] = (float)b - 0.5f;
+                    xyz[3 * (int64_t)o + 2] = (float)cc - 0.5f;
+                    if (site_id_lat) site_id_lat[((int64_t)a * NB + b) * NC + cc] = o;
+                    ++o;
+                }
             }
         }
     }
 }
 
-inline int grid_for(vc_ctx* c, int64_t n, int threads) {
-    int64_t b = (n + threads - 1) / threads;
-    int64_t cap = (int64_t)c->num_sms * 16;
-    return (int)std::max<int64_t>(1, std::min<int64_t>(b, cap));
+inline int row_grid(int num_sms, int64_t rows) {
+    return (int)std::max<int64_t>(1, std::min<int64_t>(rows, (int64_t)num_sms * 32));
 }
+
 
 }  // namespace
 
@@ -157,7 +156,7 @@ int run_sites(vc_ctx* c, int64_t* n_sites) {
     Region stage(c, "stage_sites");
     Vol v{ptr<uint8_t>(c->occ), c->X, c->Y, c->Z};
     int32_t* cnt = ptr<int32_t>(c->site_count);
-    sites_count_kernel<<<grid_for(c, nvox, 256), 256, 0, c->stream>>>(v, cnt);
+    sites_count_kernel<<<row_grid(c->num_sms, (int64_t)c->X * c->Y), 128, 0, c->stream>>>(v, cnt);
     launched(c);
     VC_CUDA(c, cudaGetLastError());
     int64_t* total = ptr<int64_t>(c->scratch2);
@@ -167,7 +166,7 @@ int run_sites(vc_ctx* c, int64_t* n_sites) {
     if (n > INT32_MAX) return VC_ERR_ARG;
     VC_TRY(ensure_n<float>(c, c->site_xyz, 3 * n));
     VC_CUDA(c, cudaMemsetAsync(c->site_id_lat.p, 0xff, (size_t)nlat * sizeof(int32_t), c->stream));
-    sites_emit_kernel<<<grid_for(c, nvox, 256), 256, 0, c->stream>>>(v, cnt, ptr<float>(c->site_xyz),
+    sites_emit_kernel<<<row_grid(c->num_sms, (int64_t)c->X * c->Y), 128, 0, c->stream>>>(v, cnt, ptr<float>(c->site_xyz),
                                                                        ptr<int32_t>(c->site_id_lat));
     launched(c);
     VC_CUDA(c, cudaGetLastError());
@@ -252,10 +251,9 @@ extern "C" int vc_extract_sites_noalloc(const uint8_t* occ, int X, int Y, int Z,
     VC_TRY(noalloc_scratch(&s));
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const Vol v{occ, X, Y, Z};
-    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((nvox + 255) / 256, (int64_t)s.num_sms * 16));
     // every scratch word read below is written first in this call: counts by
     // the count kernel, tile sums and the total by the scan
-    sites_count_kernel<<<blocks, 256, 0, st>>>(v, s.counts);
+    sites_count_kernel<<<row_grid(s.num_sms, (int64_t)X * Y), 128, 0, st>>>(v, s.counts);
     const int64_t tiles = (nvox + kScanTile - 1) / kScanTile;
     scan_tile_sums<int32_t><<<(unsigned)tiles, kScanThreads, 0, st>>>(s.counts, nvox, s.tiles);
     scan_sums_single<<<1, 1024, 0, st>>>(s.tiles, tiles, s.total);
@@ -270,7 +268,7 @@ extern "C" int vc_extract_sites_noalloc(const uint8_t* occ, int X, int Y, int Z,
     if (n > capacity) return VC_ERR_ARG;  // *n_sites tells the caller how much room is needed
     if (n > 0) {
         if (!xyz) return VC_ERR_ARG;
-        sites_emit_kernel<<<blocks, 256, 0, st>>>(v, s.counts, xyz, nullptr);
+        sites_emit_kernel<<<row_grid(s.num_sms, (int64_t)X * Y), 128, 0, st>>>(v, s.counts, xyz, nullptr);
     }
     if (cudaStreamSynchronize(st) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
         cudaGetLastError();

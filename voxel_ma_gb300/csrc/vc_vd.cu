@@ -43,10 +43,14 @@ struct Grid {
     __device__ __forceinline__ int32_t label(int a, int b, int c) const { return lab[lid(a, b, c)]; }
 };
 
-__device__ __forceinline__ void decode(int64_t p, int64_t NB, int64_t NC, int& a, int& b, int& c) {
-    c = (int)(p % NC);
-    b = (int)((p / NC) % NB);
-    a = (int)(p / (NB * NC));
+
+// Lattice coordinates of point p (the lattice has fewer than 2^32 points).
+__device__ __forceinline__ void decode32(int64_t p, int64_t NB, int64_t NC, int& a, int& b, int& c) {
+    const uint32_t q = (uint32_t)p, nc = (uint32_t)NC, nb = (uint32_t)NB;
+    const uint32_t r = q / nc;
+    c = (int)(q - r * nc);
+    a = (int)(r / nb);
+    b = (int)(r - (uint32_t)a * nb);
 }
 
 // quad vertex m of the dual square of lattice edge (a,b,c)+axis d
@@ -95,50 +99,52 @@ __device__ __forceinline__ bool face_valid(const Grid& g, int a, int b, int c, i
 // along d.  lam[3p+d]: lambda of the valid face (p, d), computed once here.
 __global__ void vd_flags_kernel(Grid g, const float* __restrict__ sxyz, uint8_t* __restrict__ flags,
                                 float* __restrict__ lam, int64_t n) {
-    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
-        int a, b, c;
-        decode(p, g.NB, g.NC, a, b, c);
-        uint32_t f = 0;
-        float l3[3] = {0.0f, 0.0f, 0.0f};
+    for (int64_t row = blockIdx.x; row < (int64_t)(g.X + 1) * g.NB; row += gridDim.x) {
+        const int a = (int)(row / g.NB), b = (int)(row - (int64_t)a * g.NB);
+        for (int c = threadIdx.x; c < (int)g.NC; c += blockDim.x) {
+            const int64_t p = row * g.NC + c;
+            uint32_t f = 0;
+            float l3[3] = {0.0f, 0.0f, 0.0f};
 #pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            if (face_valid(g, a, b, c, d)) {
-                f |= 1u << d;
-                int e[3] = {a, b, c};
-                e[d] += 1;
-                l3[d] = lambda_of(sxyz, g.lab[p], g.label(e[0], e[1], e[2]));
-            }
-        }
-        if (a < g.X && b < g.Y && c < g.Z && g.inside(a, b, c)) {
-            int32_t L[8];
-#pragma unroll
-            for (int q = 0; q < 8; ++q) L[q] = g.label(a + ((q >> 2) & 1), b + ((q >> 1) & 1), c + (q & 1));
-            bool alleq = true;
-#pragma unroll
-            for (int q = 1; q < 8; ++q) alleq &= (L[q] == L[0]);
-            if (!alleq) {
-                f |= 8u;
-#pragma unroll
-                for (int d = 0; d < 3; ++d) {
-                    const int ni = a + (d == 0), nj = b + (d == 1), nk = c + (d == 2);
-                    if (!g.inside(ni, nj, nk)) continue;
-                    const int bit = 1 << (2 - d);  // corner offset bit of axis d: x->4, y->2, z->1
-                    int32_t ref = -2;
-                    bool eq = true;
-#pragma unroll
-                    for (int q = 0; q < 8; ++q) {
-                        if (!(q & bit)) continue;
-                        if (ref == -2) ref = L[q];
-                        else eq &= (L[q] == ref);
-                    }
-                    if (!eq) f |= 16u << d;
+            for (int d = 0; d < 3; ++d) {
+                if (face_valid(g, a, b, c, d)) {
+                    f |= 1u << d;
+                    int e[3] = {a, b, c};
+                    e[d] += 1;
+                    l3[d] = lambda_of(sxyz, g.lab[p], g.label(e[0], e[1], e[2]));
                 }
             }
+            if (a < g.X && b < g.Y && c < g.Z && g.inside(a, b, c)) {
+                int32_t L[8];
+#pragma unroll
+                for (int q = 0; q < 8; ++q) L[q] = g.label(a + ((q >> 2) & 1), b + ((q >> 1) & 1), c + (q & 1));
+                bool alleq = true;
+#pragma unroll
+                for (int q = 1; q < 8; ++q) alleq &= (L[q] == L[0]);
+                if (!alleq) {
+                    f |= 8u;
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) {
+                        const int ni = a + (d == 0), nj = b + (d == 1), nk = c + (d == 2);
+                        if (!g.inside(ni, nj, nk)) continue;
+                        const int bit = 1 << (2 - d);  // corner offset bit of axis d: x->4, y->2, z->1
+                        int32_t ref = -2;
+                        bool eq = true;
+#pragma unroll
+                        for (int q = 0; q < 8; ++q) {
+                            if (!(q & bit)) continue;
+                            if (ref == -2) ref = L[q];
+                            else eq &= (L[q] == ref);
+                        }
+                        if (!eq) f |= 16u << d;
+                    }
+                }
+            }
+            flags[p] = (uint8_t)f;
+            lam[3 * p + 0] = l3[0];
+            lam[3 * p + 1] = l3[1];
+            lam[3 * p + 2] = l3[2];
         }
-        flags[p] = (uint8_t)f;
-        lam[3 * p + 0] = l3[0];
-        lam[3 * p + 1] = l3[1];
-        lam[3 * p + 2] = l3[2];
     }
 }
 
@@ -183,40 +189,42 @@ __device__ __forceinline__ int plaquette_faces(const Grid& g, const uint8_t* __r
 __global__ void vd_counts_kernel(Grid g, const uint8_t* __restrict__ flags, int32_t* __restrict__ cv,
                                  int32_t* __restrict__ ce, int32_t* __restrict__ cf, int32_t* __restrict__ cef,
                                  int32_t* __restrict__ cve, int64_t n) {
-    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
-        const uint32_t fl = flags[p];
-        int a, b, c;
-        decode(p, g.NB, g.NC, a, b, c);
-        int nef = 0, nve = 0;
-        if (fl & 0x70u) {
-            Inc inc[4];
+    for (int64_t row = blockIdx.x; row < (int64_t)(g.X + 1) * g.NB; row += gridDim.x) {
+        const int a = (int)(row / g.NB), b = (int)(row - (int64_t)a * g.NB);
+        for (int c = threadIdx.x; c < (int)g.NC; c += blockDim.x) {
+            const int64_t p = row * g.NC + c;
+            const uint32_t fl = flags[p];
+            int nef = 0, nve = 0;
+            if (fl & 0x70u) {
+                Inc inc[4];
 #pragma unroll
-            for (int d = 0; d < 3; ++d)
-                if (fl & (16u << d)) nef += plaquette_faces(g, flags, a, b, c, d, inc);
-        }
-        if (fl & 8u) {
-            const int v[3] = {a, b, c};
-#pragma unroll
-            for (int d = 0; d < 3; ++d) {
-                if (v[d] > 0) {
-                    int q[3] = {a, b, c};
-                    q[d] -= 1;
-                    if (flags[g.lid(q[0], q[1], q[2])] & (16u << d)) ++nve;
-                }
-                if (fl & (16u << d)) ++nve;
-                const int u = (d + 1) % 3, w = (d + 2) % 3;
-                int p1[3] = {a, b, c}, p3[3] = {a, b, c};
-                p1[w] += 1;  // the vertex is q1 of face (p1, d)
-                p3[u] += 1;  // the vertex is q3 of face (p3, d)
-                if (flags[g.lid(p1[0], p1[1], p1[2])] & (1u << d)) ++nve;
-                if (flags[g.lid(p3[0], p3[1], p3[2])] & (1u << d)) ++nve;
+                for (int d = 0; d < 3; ++d)
+                    if (fl & (16u << d)) nef += plaquette_faces(g, flags, a, b, c, d, inc);
             }
+            if (fl & 8u) {
+                const int v[3] = {a, b, c};
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    if (v[d] > 0) {
+                        int q[3] = {a, b, c};
+                        q[d] -= 1;
+                        if (flags[g.lid(q[0], q[1], q[2])] & (16u << d)) ++nve;
+                    }
+                    if (fl & (16u << d)) ++nve;
+                    const int u = (d + 1) % 3, w = (d + 2) % 3;
+                    int p1[3] = {a, b, c}, p3[3] = {a, b, c};
+                    p1[w] += 1;  // the vertex is q1 of face (p1, d)
+                    p3[u] += 1;  // the vertex is q3 of face (p3, d)
+                    if (flags[g.lid(p1[0], p1[1], p1[2])] & (1u << d)) ++nve;
+                    if (flags[g.lid(p3[0], p3[1], p3[2])] & (1u << d)) ++nve;
+                }
+            }
+            cv[p] = (fl >> 3) & 1u;
+            ce[p] = __popc((fl >> 4) & 7u);
+            cf[p] = __popc(fl & 7u);
+            cef[p] = nef;
+            cve[p] = nve;
         }
-        cv[p] = (fl >> 3) & 1u;
-        ce[p] = __popc((fl >> 4) & 7u);
-        cf[p] = __popc(fl & 7u);
-        cef[p] = nef;
-        cve[p] = nve;
     }
 }
 
@@ -248,211 +256,243 @@ __device__ __forceinline__ void sort_small(int32_t* x, int k) {
     }
 }
 
-__global__ void vd_vertices_kernel(Grid g, const uint8_t* __restrict__ flags, Offs o, const float* __restrict__ lam,
-                                   int32_t ne_axis, float* __restrict__ vts, float* __restrict__ vm,
-                                   int32_t* __restrict__ ve_off, int32_t* __restrict__ ve_ids, VertRec* __restrict__ V,
-                                   int32_t* __restrict__ bbox, int64_t n) {
-    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
-        const uint32_t fl = flags[p];
-        if (!(fl & 8u)) continue;
-        int a, b, c;
-        decode(p, g.NB, g.NC, a, b, c);
-        const int32_t v = o.voff[p];
-        vts[3 * (int64_t)v + 0] = (float)a;
-        vts[3 * (int64_t)v + 1] = (float)b;
-        vts[3 * (int64_t)v + 2] = (float)c;
-        // vertex lambda: max over the valid faces of the voxel's 12 cube edges
-        float m = 0.0f;
+// After the scans: the lattice position of every vertex, axis edge and face
+// (p, or p*4 + axis), so that the emit kernels run one thread per cell with
+// coalesced writes; also each vertex's V->E and each axis edge's E->F offset.
+__global__ void vd_positions_kernel(Grid g, const uint8_t* __restrict__ flags, Offs o, int64_t* __restrict__ vpos,
+                                    int64_t* __restrict__ epos, int64_t* __restrict__ fpos,
+                                    int32_t* __restrict__ ve_off, int32_t* __restrict__ ef_off) {
+    for (int64_t row = blockIdx.x; row < (int64_t)(g.X + 1) * g.NB; row += gridDim.x) {
+        const int a = (int)(row / g.NB), b = (int)(row - (int64_t)a * g.NB);
+        for (int c = threadIdx.x; c < (int)g.NC; c += blockDim.x) {
+            const int64_t p = row * g.NC + c;
+            const uint32_t fl = flags[p];
+            if (fl & 8u) {
+                const int32_t v = o.voff[p];
+                vpos[v] = p;
+                ve_off[v] = o.veoff[p];
+            }
+            if (fl & 0x70u) {
+                int32_t e = o.eoff[p], efo = o.efoff[p];
+                Inc inc[4];
 #pragma unroll
-        for (int d = 0; d < 3; ++d)
-#pragma unroll
-            for (int s = 0; s < 2; ++s)
-#pragma unroll
-                for (int t = 0; t < 2; ++t) {
-                    int q[3] = {a, b, c};
-                    q[(d + 1) % 3] += s;
-                    q[(d + 2) % 3] += t;
-                    const int64_t lp = g.lid(q[0], q[1], q[2]);
-                    if (flags[lp] & (1u << d)) m = fmaxf(m, lam[3 * lp + d]);
+                for (int d = 0; d < 3; ++d) {
+                    if (!(fl & (16u << d))) continue;
+                    epos[e] = p * 4 + d;
+                    ef_off[e] = efo;
+                    efo += plaquette_faces(g, flags, a, b, c, d, inc);
+                    ++e;
                 }
-        vm[v] = m;
-        // V->E list in edge-id order: axis edges (their lower voxels precede
-        // this one in lattice order, then this voxel's own), then diagonals
-        const int32_t off = o.veoff[p];
-        int k = 0;
-        const int vv[3] = {a, b, c};
+            }
+            if (fl & 7u) {
+                int32_t f = o.foff[p];
 #pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            if (vv[d] == 0) continue;
-            int q[3] = {a, b, c};
-            q[d] -= 1;
-            const int64_t lq = g.lid(q[0], q[1], q[2]);
-            if (flags[lq] & (16u << d)) ve_ids[off + k++] = edge_id(flags, o, lq, d);
+                for (int d = 0; d < 3; ++d)
+                    if (fl & (1u << d)) fpos[f++] = p * 4 + d;
+            }
         }
+    }
+}
+
+__global__ void vd_vertices_kernel(Grid g, const uint8_t* __restrict__ flags, Offs o, const float* __restrict__ lam,
+                                   const int64_t* __restrict__ vpos, int32_t ne_axis, int32_t nv, float* __restrict__ vts,
+                                   float* __restrict__ vm, const int32_t* __restrict__ ve_off,
+                                   int32_t* __restrict__ ve_ids, VertRec* __restrict__ V, int32_t* __restrict__ bbox) {
+    for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += gridDim.x * blockDim.x) {
+        {
+            const int64_t p = vpos[v];
+            int a, b, c;
+            decode32(p, g.NB, g.NC, a, b, c);
+            const uint32_t fl = flags[p];
+            vts[3 * (int64_t)v + 0] = (float)a;
+            vts[3 * (int64_t)v + 1] = (float)b;
+            vts[3 * (int64_t)v + 2] = (float)c;
+            // vertex lambda: max over the valid faces of the voxel's 12 cube edges
+            float m = 0.0f;
 #pragma unroll
-        for (int d = 0; d < 3; ++d)
-            if (fl & (16u << d)) ve_ids[off + k++] = edge_id(flags, o, p, d);
-        int32_t dg[6];
-        int nd = 0;
+            for (int d = 0; d < 3; ++d)
 #pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            const int u = (d + 1) % 3, w = (d + 2) % 3;
-            int p1[3] = {a, b, c}, p3[3] = {a, b, c};
-            p1[w] += 1;
-            p3[u] += 1;
-            const int64_t l1 = g.lid(p1[0], p1[1], p1[2]), l3 = g.lid(p3[0], p3[1], p3[2]);
-            if (flags[l1] & (1u << d)) dg[nd++] = face_id(flags, o, l1, d);
-            if (flags[l3] & (1u << d)) dg[nd++] = face_id(flags, o, l3, d);
+                for (int s = 0; s < 2; ++s)
+#pragma unroll
+                    for (int t = 0; t < 2; ++t) {
+                        int q[3] = {a, b, c};
+                        q[(d + 1) % 3] += s;
+                        q[(d + 2) % 3] += t;
+                        const int64_t lp = g.lid(q[0], q[1], q[2]);
+                        if (flags[lp] & (1u << d)) m = fmaxf(m, lam[3 * lp + d]);
+                    }
+            vm[v] = m;
+            // V->E list in edge-id order: axis edges (their lower voxels precede
+            // this one in lattice order, then this voxel's own), then diagonals
+            const int32_t off = ve_off[v];
+            int k = 0;
+            const int vv[3] = {a, b, c};
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                if (vv[d] == 0) continue;
+                int q[3] = {a, b, c};
+                q[d] -= 1;
+                const int64_t lq = g.lid(q[0], q[1], q[2]);
+                if (flags[lq] & (16u << d)) ve_ids[off + k++] = edge_id(flags, o, lq, d);
+            }
+#pragma unroll
+            for (int d = 0; d < 3; ++d)
+                if (fl & (16u << d)) ve_ids[off + k++] = edge_id(flags, o, p, d);
+            int32_t dg[6];
+            int nd = 0;
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                const int u = (d + 1) % 3, w = (d + 2) % 3;
+                int p1[3] = {a, b, c}, p3[3] = {a, b, c};
+                p1[w] += 1;
+                p3[u] += 1;
+                const int64_t l1 = g.lid(p1[0], p1[1], p1[2]), l3 = g.lid(p3[0], p3[1], p3[2]);
+                if (flags[l1] & (1u << d)) dg[nd++] = face_id(flags, o, l1, d);
+                if (flags[l3] & (1u << d)) dg[nd++] = face_id(flags, o, l3, d);
+            }
+            sort_small<6>(dg, nd);
+            for (int i = 0; i < nd; ++i) ve_ids[off + k++] = ne_axis + dg[i];
+            VertRec r;
+            r.ve_off = off;
+            r.ve_cnt = k;
+            r.rm = kAlive;
+            r.ref = k;
+            r.trig = -1;
+            r.pad0 = r.pad1 = r.pad2 = 0;
+            V[v] = r;
+            atomicMin(&bbox[0], a);
+            atomicMin(&bbox[1], b);
+            atomicMin(&bbox[2], c);
+            atomicMax(&bbox[3], a);
+            atomicMax(&bbox[4], b);
+            atomicMax(&bbox[5], c);
         }
-        sort_small<6>(dg, nd);
-        for (int i = 0; i < nd; ++i) ve_ids[off + k++] = ne_axis + dg[i];
-        ve_off[v] = off;
-        VertRec r;
-        r.ve_off = off;
-        r.ve_cnt = k;
-        r.rm = kAlive;
-        r.ref = k;
-        r.trig = -1;
-        r.pad0 = r.pad1 = r.pad2 = 0;
-        V[v] = r;
-        atomicMin(&bbox[0], a);
-        atomicMin(&bbox[1], b);
-        atomicMin(&bbox[2], c);
-        atomicMax(&bbox[3], a);
-        atomicMax(&bbox[4], b);
-        atomicMax(&bbox[5], c);
     }
 }
 
 __global__ void vd_edges_kernel(Grid g, const uint8_t* __restrict__ flags, Offs o, const float* __restrict__ lam,
-                                int2* __restrict__ edges, float* __restrict__ em, int32_t* __restrict__ ef_off,
-                                int32_t* __restrict__ ef_ids, EdgeRec* __restrict__ E, int64_t n) {
-    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
-        const uint32_t fl = flags[p];
-        if (!(fl & 0x70u)) continue;
+                                const int64_t* __restrict__ epos, int32_t ne_axis, int2* __restrict__ edges,
+                                float* __restrict__ em, const int32_t* __restrict__ ef_off, int32_t* __restrict__ ef_ids,
+                                EdgeRec* __restrict__ E) {
+    for (int32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < ne_axis; e += gridDim.x * blockDim.x) {
+        const int64_t q = epos[e];
+        const int64_t p = q >> 2;
+        const int d = (int)(q & 3);
         int a, b, c;
-        decode(p, g.NB, g.NC, a, b, c);
-        int32_t e = o.eoff[p];
-        int32_t efo = o.efoff[p];
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            if (!(fl & (16u << d))) continue;
-            int nb[3] = {a, b, c};
-            nb[d] += 1;
-            const int32_t v0 = o.voff[p], v1 = o.voff[g.lid(nb[0], nb[1], nb[2])];
-            Inc inc[4];
-            const int k = plaquette_faces(g, flags, a, b, c, d, inc);
-            float m = 0.0f;
-            int32_t tl[4];
-            for (int j = 0; j < k; ++j) {
-                m = fmaxf(m, lam[3 * inc[j].lp + inc[j].axis]);
-                tl[j] = 2 * face_id(flags, o, inc[j].lp, inc[j].axis) + inc[j].tri;
-            }
-            sort_small<4>(tl, k);
-            for (int j = 0; j < k; ++j) ef_ids[efo + j] = tl[j];
-            edges[e] = make_int2(v0, v1);
-            em[e] = m;
-            ef_off[e] = efo;
-            EdgeRec r;
-            r.v0 = v0;
-            r.v1 = v1;
-            r.em = m;
-            r.ef_off = efo;
-            r.ef_cnt = k;
-            r.rm = kAlive;
-            r.ref = k;
-            r.trig = -1;
-            E[e] = r;
-            efo += k;
-            ++e;
+        decode32(p, g.NB, g.NC, a, b, c);
+        int nb[3] = {a, b, c};
+        nb[d] += 1;
+        const int32_t v0 = o.voff[p], v1 = o.voff[g.lid(nb[0], nb[1], nb[2])];
+        Inc inc[4];
+        const int k = plaquette_faces(g, flags, a, b, c, d, inc);
+        float m = 0.0f;
+        int32_t tl[4];
+        for (int j = 0; j < k; ++j) {
+            m = fmaxf(m, lam[3 * inc[j].lp + inc[j].axis]);
+            tl[j] = 2 * face_id(flags, o, inc[j].lp, inc[j].axis) + inc[j].tri;
         }
+        sort_small<4>(tl, k);
+        const int32_t efo = ef_off[e];
+        for (int j = 0; j < k; ++j) ef_ids[efo + j] = tl[j];
+        edges[e] = make_int2(v0, v1);
+        em[e] = m;
+        EdgeRec r;
+        r.v0 = v0;
+        r.v1 = v1;
+        r.em = m;
+        r.ef_off = efo;
+        r.ef_cnt = k;
+        r.rm = kAlive;
+        r.ref = k;
+        r.trig = -1;
+        E[e] = r;
     }
 }
 
 __global__ void vd_faces_kernel(Grid g, const uint8_t* __restrict__ flags, Offs o, const float* __restrict__ lam,
-                                int32_t ne_axis, int32_t ef_axis, int2* __restrict__ edges, float* __restrict__ em,
-                                int32_t* __restrict__ ef_off, int32_t* __restrict__ ef_ids, int32_t* __restrict__ tris,
+                                const int64_t* __restrict__ fpos, int32_t nface, int32_t ne_axis, int32_t ef_axis,
+                                int2* __restrict__ edges, float* __restrict__ em, int32_t* __restrict__ ef_off,
+                                int32_t* __restrict__ ef_ids, int32_t* __restrict__ tris,
                                 int32_t* __restrict__ tri_edges, float* __restrict__ fm,
                                 int32_t* __restrict__ tri_face, int2* __restrict__ face_sites,
-                                FaceRec* __restrict__ F, EdgeRec* __restrict__ E, int64_t n) {
-    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
-        const uint32_t fl = flags[p];
-        if (!(fl & 7u)) continue;
+                                FaceRec* __restrict__ F, EdgeRec* __restrict__ E) {
+    for (int32_t f = blockIdx.x * blockDim.x + threadIdx.x; f < nface; f += gridDim.x * blockDim.x) {
+        const int64_t qq = fpos[f];
+        const int64_t p = qq >> 2;
+        const int d = (int)(qq & 3);
         int a, b, c;
-        decode(p, g.NB, g.NC, a, b, c);
-        int32_t f = o.foff[p];
+        decode32(p, g.NB, g.NC, a, b, c);
+        {
+            {
+                const int u = (d + 1) % 3, w = (d + 2) % 3;
+                int e1[3] = {a, b, c};
+                e1[d] += 1;
+                const int32_t s0 = g.lab[p], s1 = g.label(e1[0], e1[1], e1[2]);
+                const float lm = lam[3 * p + d];
+                int64_t ql[4];
+                int32_t q[4];
 #pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            if (!(fl & (1u << d))) continue;
-            const int u = (d + 1) % 3, w = (d + 2) % 3;
-            int e1[3] = {a, b, c};
-            e1[d] += 1;
-            const int32_t s0 = g.lab[p], s1 = g.label(e1[0], e1[1], e1[2]);
-            const float lm = lam[3 * p + d];
-            int64_t ql[4];
-            int32_t q[4];
-#pragma unroll
-            for (int m = 0; m < 4; ++m) {
-                int i, j, k;
-                quad_voxel(a, b, c, d, m, i, j, k);
-                ql[m] = g.lid(i, j, k);
-                q[m] = o.voff[ql[m]];
+                for (int m = 0; m < 4; ++m) {
+                    int i, j, k;
+                    quad_voxel(a, b, c, d, m, i, j, k);
+                    ql[m] = g.lid(i, j, k);
+                    q[m] = o.voff[ql[m]];
+                }
+                const int32_t diag = ne_axis + f;
+                const int32_t e01 = edge_id(flags, o, ql[0], u);
+                const int32_t e12 = edge_id(flags, o, ql[1], w);
+                const int32_t e32 = edge_id(flags, o, ql[3], u);
+                const int32_t e03 = edge_id(flags, o, ql[0], w);
+                const int64_t t0 = 2 * (int64_t)f, t1 = t0 + 1;
+                tris[3 * t0 + 0] = q[3];
+                tris[3 * t0 + 1] = q[0];
+                tris[3 * t0 + 2] = q[1];
+                tris[3 * t1 + 0] = q[3];
+                tris[3 * t1 + 1] = q[1];
+                tris[3 * t1 + 2] = q[2];
+                // sides in traceFace order: (t0,t1), (t1,t2), (t2,t0)
+                tri_edges[3 * t0 + 0] = e03;
+                tri_edges[3 * t0 + 1] = e01;
+                tri_edges[3 * t0 + 2] = diag;
+                tri_edges[3 * t1 + 0] = diag;
+                tri_edges[3 * t1 + 1] = e12;
+                tri_edges[3 * t1 + 2] = e32;
+                fm[t0] = lm;
+                fm[t1] = lm;
+                tri_face[t0] = f;
+                tri_face[t1] = f;
+                face_sites[f] = make_int2(s0, s1);
+                FaceRec fr;
+                fr.fm = lm;
+                fr.rm = kAlive;
+                fr.pad0 = fr.pad1 = fr.pad2 = 0;
+                fr.e0 = e03;
+                fr.e1 = e01;
+                fr.e2 = diag;
+                F[t0] = fr;
+                fr.e0 = diag;
+                fr.e1 = e12;
+                fr.e2 = e32;
+                F[t1] = fr;
+                // the diagonal: new edge of this face, incident to both triangles
+                const int32_t dv0 = min(q[1], q[3]), dv1 = max(q[1], q[3]);
+                const int32_t efo = ef_axis + 2 * f;
+                edges[diag] = make_int2(dv0, dv1);
+                em[diag] = lm;
+                ef_off[diag] = efo;
+                ef_ids[efo] = (int32_t)t0;
+                ef_ids[efo + 1] = (int32_t)t1;
+                EdgeRec er;
+                er.v0 = dv0;
+                er.v1 = dv1;
+                er.em = lm;
+                er.ef_off = efo;
+                er.ef_cnt = 2;
+                er.rm = kAlive;
+                er.ref = 2;
+                er.trig = -1;
+                E[diag] = er;
             }
-            const int32_t diag = ne_axis + f;
-            const int32_t e01 = edge_id(flags, o, ql[0], u);
-            const int32_t e12 = edge_id(flags, o, ql[1], w);
-            const int32_t e32 = edge_id(flags, o, ql[3], u);
-            const int32_t e03 = edge_id(flags, o, ql[0], w);
-            const int64_t t0 = 2 * (int64_t)f, t1 = t0 + 1;
-            tris[3 * t0 + 0] = q[3];
-            tris[3 * t0 + 1] = q[0];
-            tris[3 * t0 + 2] = q[1];
-            tris[3 * t1 + 0] = q[3];
-            tris[3 * t1 + 1] = q[1];
-            tris[3 * t1 + 2] = q[2];
-            // sides in traceFace order: (t0,t1), (t1,t2), (t2,t0)
-            tri_edges[3 * t0 + 0] = e03;
-            tri_edges[3 * t0 + 1] = e01;
-            tri_edges[3 * t0 + 2] = diag;
-            tri_edges[3 * t1 + 0] = diag;
-            tri_edges[3 * t1 + 1] = e12;
-            tri_edges[3 * t1 + 2] = e32;
-            fm[t0] = lm;
-            fm[t1] = lm;
-            tri_face[t0] = f;
-            tri_face[t1] = f;
-            face_sites[f] = make_int2(s0, s1);
-            FaceRec fr;
-            fr.fm = lm;
-            fr.rm = kAlive;
-            fr.pad0 = fr.pad1 = fr.pad2 = 0;
-            fr.e0 = e03;
-            fr.e1 = e01;
-            fr.e2 = diag;
-            F[t0] = fr;
-            fr.e0 = diag;
-            fr.e1 = e12;
-            fr.e2 = e32;
-            F[t1] = fr;
-            // the diagonal: new edge of this face, incident to both triangles
-            const int32_t dv0 = min(q[1], q[3]), dv1 = max(q[1], q[3]);
-            const int32_t efo = ef_axis + 2 * f;
-            edges[diag] = make_int2(dv0, dv1);
-            em[diag] = lm;
-            ef_off[diag] = efo;
-            ef_ids[efo] = (int32_t)t0;
-            ef_ids[efo + 1] = (int32_t)t1;
-            EdgeRec er;
-            er.v0 = dv0;
-            er.v1 = dv1;
-            er.em = lm;
-            er.ef_off = efo;
-            er.ef_cnt = 2;
-            er.rm = kAlive;
-            er.ref = 2;
-            er.trig = -1;
-            E[diag] = er;
-            ++f;
         }
     }
 }
@@ -470,10 +510,14 @@ __global__ void init_bbox_kernel(int32_t* bbox) {
     else if (threadIdx.x < 6) bbox[threadIdx.x] = INT32_MIN;
 }
 
-inline int grid_for(vc_ctx* c, int64_t n, int threads) {
-    int64_t b = (n + threads - 1) / threads;
-    return (int)std::max<int64_t>(1, std::min<int64_t>(b, (int64_t)c->num_sms * 16));
+inline int cell_grid(vc_ctx* c, int64_t n) {
+    return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)c->num_sms * 16));
 }
+
+inline int row_grid(vc_ctx* c, int64_t rows) {
+    return (int)std::max<int64_t>(1, std::min<int64_t>(rows, (int64_t)c->num_sms * 32));
+}
+
 
 }  // namespace
 
@@ -481,6 +525,7 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes) {
     if (!c->ft_valid) return VC_ERR_STATE;
     const int64_t NB = c->Y + 1, NC = c->Z + 1;
     const int64_t N = (int64_t)(c->X + 1) * NB * NC;
+    if (N >= ((int64_t)1 << 32)) return VC_ERR_ARG;
     Region stage(c, "stage_vd");
     VC_TRY(ensure_n<uint8_t>(c, c->vd_flags, N));
     VC_TRY(ensure_n<float>(c, c->vd_lam, 3 * N));
@@ -499,9 +544,9 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes) {
     const float* sxyz = ptr<float>(c->site_xyz);
     {
         Region r(c, "vd_flags");
-        vd_flags_kernel<<<grid_for(c, N, 256), 256, 0, c->stream>>>(g, sxyz, flags, lam, N);
+        vd_flags_kernel<<<row_grid(c, (int64_t)(c->X + 1) * NB), 128, 0, c->stream>>>(g, sxyz, flags, lam, N);
         launched(c);
-        vd_counts_kernel<<<grid_for(c, N, 256), 256, 0, c->stream>>>(g, flags, cnt[0], cnt[1], cnt[2], cnt[3],
+        vd_counts_kernel<<<row_grid(c, (int64_t)(c->X + 1) * NB), 128, 0, c->stream>>>(g, flags, cnt[0], cnt[1], cnt[2], cnt[3],
                                                                       cnt[4], N);
         launched(c);
         VC_CUDA(c, cudaGetLastError());
@@ -540,25 +585,32 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes) {
     VC_TRY(ensure_n<FaceRec>(c, c->face_rec, nt));
     VC_TRY(ensure_n<EdgeRec>(c, c->edge_rec, ne));
     VC_TRY(ensure_n<VertRec>(c, c->vert_rec, nv));
+    VC_TRY(ensure_n<int64_t>(c, c->vd_vpos, nv));
+    VC_TRY(ensure_n<int64_t>(c, c->vd_epos, ne_axis));
+    VC_TRY(ensure_n<int64_t>(c, c->vd_fpos, nface));
     int32_t* bbox = ptr<int32_t>(c->vd_bbox);
     init_bbox_kernel<<<1, 32, 0, c->stream>>>(bbox);
     launched(c);
     Offs o{cnt[0], cnt[1], cnt[2], cnt[3], cnt[4]};
     {
         Region r(c, "vd_emit");
-        vd_vertices_kernel<<<grid_for(c, N, 256), 256, 0, c->stream>>>(
-            g, flags, o, lam, (int32_t)ne_axis, ptr<float>(c->vts), ptr<float>(c->vm), ptr<int32_t>(c->ve_off),
-            ptr<int32_t>(c->ve_ids), ptr<VertRec>(c->vert_rec), bbox, N);
+        vd_positions_kernel<<<row_grid(c, (int64_t)(c->X + 1) * NB), 128, 0, c->stream>>>(
+            g, flags, o, ptr<int64_t>(c->vd_vpos), ptr<int64_t>(c->vd_epos), ptr<int64_t>(c->vd_fpos),
+            ptr<int32_t>(c->ve_off), ptr<int32_t>(c->ef_off));
         launched(c);
-        vd_edges_kernel<<<grid_for(c, N, 256), 256, 0, c->stream>>>(
-            g, flags, o, lam, ptr<int2>(c->edges), ptr<float>(c->em), ptr<int32_t>(c->ef_off),
-            ptr<int32_t>(c->ef_ids), ptr<EdgeRec>(c->edge_rec), N);
+        vd_vertices_kernel<<<cell_grid(c, nv), 256, 0, c->stream>>>(
+            g, flags, o, lam, ptr<int64_t>(c->vd_vpos), (int32_t)ne_axis, (int32_t)nv, ptr<float>(c->vts),
+            ptr<float>(c->vm), ptr<int32_t>(c->ve_off), ptr<int32_t>(c->ve_ids), ptr<VertRec>(c->vert_rec), bbox);
         launched(c);
-        vd_faces_kernel<<<grid_for(c, N, 256), 256, 0, c->stream>>>(
-            g, flags, o, lam, (int32_t)ne_axis, (int32_t)nef_axis, ptr<int2>(c->edges), ptr<float>(c->em),
-            ptr<int32_t>(c->ef_off), ptr<int32_t>(c->ef_ids), ptr<int32_t>(c->tris), ptr<int32_t>(c->tri_edges),
-            ptr<float>(c->fm), ptr<int32_t>(c->vd_tri_face), ptr<int2>(c->vd_face_sites),
-            ptr<FaceRec>(c->face_rec), ptr<EdgeRec>(c->edge_rec), N);
+        vd_edges_kernel<<<cell_grid(c, ne_axis), 256, 0, c->stream>>>(
+            g, flags, o, lam, ptr<int64_t>(c->vd_epos), (int32_t)ne_axis, ptr<int2>(c->edges), ptr<float>(c->em),
+            ptr<int32_t>(c->ef_off), ptr<int32_t>(c->ef_ids), ptr<EdgeRec>(c->edge_rec));
+        launched(c);
+        vd_faces_kernel<<<cell_grid(c, nface), 256, 0, c->stream>>>(
+            g, flags, o, lam, ptr<int64_t>(c->vd_fpos), (int32_t)nface, (int32_t)ne_axis, (int32_t)nef_axis,
+            ptr<int2>(c->edges), ptr<float>(c->em), ptr<int32_t>(c->ef_off), ptr<int32_t>(c->ef_ids),
+            ptr<int32_t>(c->tris), ptr<int32_t>(c->tri_edges), ptr<float>(c->fm), ptr<int32_t>(c->vd_tri_face),
+            ptr<int2>(c->vd_face_sites), ptr<FaceRec>(c->face_rec), ptr<EdgeRec>(c->edge_rec));
         launched(c);
         vd_tail_kernel<<<1, 32, 0, c->stream>>>(bbox, ptr<int32_t>(c->ve_off), (int32_t)nv, (int32_t)nve,
                                                 ptr<int32_t>(c->ef_off), (int32_t)ne, (int32_t)(3 * nt));
