@@ -314,8 +314,10 @@ def run_gpu(args):
         ach = ab / per_launch_s / 1e9
         roof = {"kernel": dom, "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
                 "frac": ach / peak, "peak_kind": peak_kind, "algorithmic_bytes_per_launch": ab,
-                "traffic": TRAFFIC.get(dom, {}).get("bytes_per_launch") if args.workload == "grf512" else None,
-                "traffic_source": TRAFFIC.get(dom, {}).get("source")}
+                "traffic": (TRAFFIC_PER_CELL[dom] * (r["vd"]["nv"] + r["vd"]["ne"] + r["vd"]["nt"])
+                            if dom in TRAFFIC_PER_CELL else None),
+                "traffic_source": ("ncu capture of the 192^3 case scaled by cells (profiles/kernels_grf192.md)"
+                                   if dom in TRAFFIC_PER_CELL else None)}
     stage_ms = {k: v[0] / max(v[1], 1) for k, v in sorted(timings.items())}
 
     line = {
@@ -352,9 +354,12 @@ def run_gpu(args):
     return 0
 
 
-# Per-launch DRAM traffic of the kernels from an ncu capture of the same
-# workload (profiles/ summaries give the commands and figures).
-TRAFFIC: dict = {}
+# DRAM traffic per cell of the complex (V + E + T) of the thinning kernel,
+# from one ncu capture of the 192^3 case of this workload
+# (profiles/kernels_grf192.md: 8.655 GB read + 2.297 GB written for
+# 3,385,169 + 14,026,594 + 10,679,482 cells); the traffic grows with the
+# complex, so the per-launch figure at 512^3 is this rate times its cells.
+TRAFFIC_PER_CELL = {"thin_generations": (8.655230e9 + 2.296893e9) / (3385169 + 14026594 + 10679482)}
 
 
 def main():
