@@ -26,7 +26,9 @@
 // One persistent cooperative kernel runs all generations with three bounded
 // grid barriers per generation:
 //   A (per item)  claims are checked, removals applied, counts decremented;
-//                 the decrement that takes a count from 2 to 1 lists its cell;
+//                 the decrement that takes a count from 2 to 1 lists its cell
+//                 (items are handed out to blocks in 256-item pieces from a
+//                 shared cursor, so the blocks stay balanced);
 //   B (per listed cell)  a cell still at 1 gives its child to the item at
 //                 its last-decrement position, in the cell's slot;
 //   C (per item)  children are written in order as generation g+1 and that
@@ -60,8 +62,8 @@ struct ThinArgs {
     int4* cand;            // per item: the cells it decremented (-1 = none)
     int2* child;           // per item: up to 4 children, by slot
     unsigned* child_mask;  // per item one byte (4 items per word): bit s = child in slot s
-    int32_t* cells;        // per block: cells whose count reached 1 in this generation (kEdgeBit: edge)
-    int* ncell_blk;        // [G] list length of each block's region
+    int32_t* cells;        // cells whose count reached 1 in this generation (kEdgeBit: edge)
+    int* counters;         // [2][4] by generation parity: list length, phase-A work cursor
     int64_t* blk_cnt;      // [2 * G] children per block, by generation parity
     unsigned* bar;
     int* err;
@@ -180,9 +182,8 @@ __device__ __forceinline__ int32_t live_edge(const ThinArgs& A, int32_t off, int
     return -1;
 }
 
-// Block-local append of the cells whose count fell from 2 to 1: each block
-// owns the region cells[b * cap .. b * cap + count), its count kept in
-// shared memory during phase A and published to ncell_blk[b] at its end.
+// Warp-aggregated append of a cell whose count fell from 2 to 1 to the
+// block's shared-memory list of the current 256-item piece (all lanes call).
 __device__ __forceinline__ void append_cell(int32_t* region, int* s_count, bool want, int32_t code) {
     const unsigned m = __ballot_sync(0xffffffffu, want);
     if (!m) return;
@@ -197,7 +198,8 @@ __device__ __forceinline__ void append_cell(int32_t* region, int* s_count, bool 
 __global__ void __launch_bounds__(kThreads) thin_generations_kernel(ThinArgs A) {
     __shared__ int64_t sm[33];
     __shared__ int64_t s_red[2];
-    __shared__ int s_ncell;
+    __shared__ int s_ncell, s_start, s_gbase;
+    __shared__ int32_t s_cells[4 * kThreads];
     const int G = gridDim.x, b = blockIdx.x;
     const float f_t = A.thr[0], l_t = A.thr[1];
     int64_t n = A.ctl[0];
@@ -210,10 +212,7 @@ __global__ void __launch_bounds__(kThreads) thin_generations_kernel(ThinArgs A) 
         int2* nxt = par ? A.qa : A.qb;
         int64_t* blk = A.blk_cnt + (int64_t)par * G;
         const int64_t chunk = (n + G - 1) / G;
-        const int64_t region_cap = 4 * chunk;
-        int32_t* region = A.cells + (int64_t)b * region_cap;
-        if (threadIdx.x == 0) s_ncell = 0;
-        __syncthreads();
+        int* ctr = A.counters + 4 * par;  // [0] list length, [1] phase-A cursor
         const int64_t i0 = min(n, (int64_t)b * chunk), i1 = min(n, i0 + chunk);
         const bool tr = A.trace && b == 0 && threadIdx.x == 0 && gen < A.trace_cap;
         if (tr) {
@@ -221,10 +220,19 @@ __global__ void __launch_bounds__(kThreads) thin_generations_kernel(ThinArgs A) 
             A.trace[4 * gen + 1] = global_ns();
         }
         // ---- phase A: apply the removals of the items that won their claim
-        for (int64_t r0 = i0; r0 < i1; r0 += blockDim.x) {
+        // items are taken in 256-item pieces from a shared cursor, so that
+        // blocks finishing early take more (the per-item cost varies)
+        for (;;) {
+            if (threadIdx.x == 0) {
+                s_start = atomicAdd(ctr + 1, (int)blockDim.x);
+                s_ncell = 0;
+            }
+            __syncthreads();
+            const int64_t r0 = s_start;
+            if (r0 >= n) break;
             const int64_t i = r0 + threadIdx.x;
             int32_t one[4] = {-1, -1, -1, -1};  // cells whose count fell to 1 here
-            if (i < i1) {
+            if (i < n) {
                 const int2 it = __ldcg(cur + i);
                 const int32_t p = (int32_t)(base + i);
                 int4 cd = make_int4(-1, -1, -1, -1);
@@ -282,19 +290,26 @@ __global__ void __launch_bounds__(kThreads) thin_generations_kernel(ThinArgs A) 
                 __stcg(A.cand + i, cd);
             }
 #pragma unroll
-            for (int q = 0; q < 4; ++q) append_cell(region, &s_ncell, one[q] != -1, one[q]);
+            for (int q = 0; q < 4; ++q) append_cell(s_cells, &s_ncell, one[q] != -1, one[q]);
+            __syncthreads();
+            if (threadIdx.x == 0) s_gbase = s_ncell ? atomicAdd(ctr + 0, s_ncell) : 0;
+            __syncthreads();
+            for (int k = threadIdx.x; k < s_ncell; k += blockDim.x) A.cells[s_gbase + k] = s_cells[k];
+            __syncthreads();
         }
-        __syncthreads();
-        if (threadIdx.x == 0) A.ncell_blk[b] = s_ncell;
         grid_barrier(A.bar, A.err, A.spin_limit);
         if (*((volatile int*)A.err)) break;
         // ---- phase B: a listed cell still at 1 gives its child to the item
         // that decremented it last (its trig position), in the cell's slot
         if (tr) A.trace[4 * gen + 2] = global_ns();
         {
-            const int m = __ldcg(A.ncell_blk + b);
-            for (int j = threadIdx.x; j < m; j += blockDim.x) {
-                const int32_t code = __ldcg(region + j);
+            // contiguous share of the list: cells listed by neighbouring items
+            // stay together, as do the records they touch
+            const int64_t m = __ldcg(ctr + 0);
+            const int64_t mchunk = (m + G - 1) / G;
+            const int64_t j1 = min(m, ((int64_t)b + 1) * mchunk);
+            for (int64_t j = (int64_t)b * mchunk + threadIdx.x; j < j1; j += blockDim.x) {
+                const int32_t code = __ldcg(A.cells + j);
                 int64_t i;
                 int slot;
                 int2 ch;
@@ -380,7 +395,13 @@ __global__ void __launch_bounds__(kThreads) thin_generations_kernel(ThinArgs A) 
             running += tot;
         }
         // counters of the next generation start at zero
-        if (threadIdx.x == 0) A.blk_cnt[(int64_t)(par ^ 1) * G + b] = 0;
+        if (threadIdx.x == 0) {
+            A.blk_cnt[(int64_t)(par ^ 1) * G + b] = 0;
+            if (b == 0) {
+                int* nc = A.counters + 4 * (par ^ 1);
+                nc[0] = nc[1] = nc[2] = 0;
+            }
+        }
         __syncthreads();
         base = nbase;
         n = total;
@@ -459,7 +480,7 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats) {
     VC_TRY(ensure_n<int4>(c, c->cand, qcap));
     VC_TRY(ensure_n<int2>(c, c->child, 4 * qcap));
     VC_TRY(ensure_n<unsigned>(c, c->child_cnt, qcap / 4 + 2));  // child masks
-    VC_TRY(ensure_n<int32_t>(c, c->cells, 4 * qcap + 4 * 8 * (int64_t)c->num_sms));
+    VC_TRY(ensure_n<int32_t>(c, c->cells, 4 * qcap));
     VC_TRY(ensure_n<int32_t>(c, c->scratch2, 2 * (nv + ne) + 2));
     VC_TRY(ensure_n<int64_t>(c, c->euler_tmp, 16));
     VC_TRY(ensure_n<uint8_t>(c, c->keep_v, nv));
@@ -518,10 +539,10 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats) {
     VC_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, thin_generations_kernel, kThreads, 0));
     if (per_sm <= 0) return VC_ERR_CUDA;
     const int G = c->num_sms * std::min(per_sm, c->thin_blocks_per_sm > 0 ? c->thin_blocks_per_sm : 8);
-    VC_TRY(ensure_n<int64_t>(c, c->blk_cnt, 3 * (int64_t)G));
-    VC_CUDA(c, cudaMemsetAsync(c->blk_cnt.p, 0, 3 * sizeof(int64_t) * G, c->stream));
+    VC_TRY(ensure_n<int64_t>(c, c->blk_cnt, 2 * (int64_t)G + 8));
+    VC_CUDA(c, cudaMemsetAsync(c->blk_cnt.p, 0, (2 * (int64_t)G + 8) * sizeof(int64_t), c->stream));
     A.blk_cnt = ptr<int64_t>(c->blk_cnt);
-    A.ncell_blk = reinterpret_cast<int*>(A.blk_cnt + 2 * (int64_t)G);
+    A.counters = reinterpret_cast<int*>(A.blk_cnt + 2 * (int64_t)G);
     void* args[] = {&A};
     {
         Region r(c, "thin_generations");
