@@ -91,6 +91,14 @@ int vc_lattice_vd(vc_ctx* ctx, vc_vd_sizes* sizes);
 int vc_get_vd(vc_ctx* ctx, float* vts, int32_t* edges, int32_t* tris, int32_t* tri_face, float* vm, float* em,
               float* fm, int32_t* face_sites, int mem);
 
+/* Radius per vertex of the lattice complex (nv floats, vc_get_vd's vertex
+ * order).  Replaces VoroInfo::computeInfoRelatedtoSites
+ * (src/voroinfo.cpp:286-325) + VoroInfo::getRadii (include/voroinfo.h):
+ * r = dist(vertex, first site of the last Voronoi face, in face order, that
+ * has the vertex); the values writeRadiiToFile (src/exporters.cpp:478-552)
+ * writes for the valid vertices.  Needs vc_lattice_vd.                    */
+int vc_vertex_radii(vc_ctx* ctx, float* radius, int mem);
+
 /* ---- cell complex in ----------------------------------------------------
  * Replaces cellcomplex(const vector<point>&, const vector<ivec2>&,
  * const vector<uTriFace>&, bool finalize = true) + cellcomplex::finalize()

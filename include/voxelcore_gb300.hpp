@@ -15,6 +15,7 @@
 //     remainingCC}  (include/ccthin.h:57-113)
 //   VoroInfo::extractInsideWithMeasure          vcgpu::extractInsideWithMeasure
 //     (include/voroinfo.h:127-131), for the lattice Voronoi complex
+//   VoroInfo::getRadii (voroinfo.cpp:286-325)   vcgpu::getRadii
 //
 // Point types are any type with operator[] over 3 floats (trimesh::point),
 // edges any type with operator[] over 2 ints (trimesh::ivec2), triangles any
@@ -123,6 +124,16 @@ float extractInsideWithMeasure(Context& ctx, const DenseVolume& vol, std::vector
         for (int k = 0; k < 3; ++k) tris[i][k] = t[3 * i + k];
     from_fi.assign(tf.begin(), tf.end());
     return s.inside_size;
+}
+
+// VoroInfo::getRadii after computeInfoRelatedtoSites (voroinfo.cpp:286-325),
+// for the vertices extractInsideWithMeasure returned (the valid vertices
+// writeRadiiToFile writes, exporters.cpp:478-552).
+// `vts` is the vertex list extractInsideWithMeasure filled.
+template <class P>
+void getRadii(Context& ctx, const std::vector<P>& vts, std::vector<float>& radii) {
+    radii.resize(vts.size());
+    check(ctx.get(), vc_vertex_radii(ctx.get(), radii.data(), VC_MEM_HOST), "vc_vertex_radii");
 }
 
 // cellcomplex(vts, edges, tris, finalize=true): the complex lives on the GPU.

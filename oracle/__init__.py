@@ -60,6 +60,7 @@ def lib():
         L.vco_lattice_vd.argtypes = [c_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, c_vp, c_vp]
         L.vco_vd_sizes.argtypes = [c_vp] * 6
         L.vco_vd_get.argtypes = [c_vp] * 9
+        L.vco_vd_radius.argtypes = [c_vp, c_vp]
         L.vco_vd_free.argtypes = [c_vp]
         L.vco_finalize.restype = c_i64
         L.vco_finalize.argtypes = [c_i64, c_i64, c_vp, c_i64, c_vp] + [c_vp] * 6
@@ -154,6 +155,8 @@ def lattice_vd(occ: np.ndarray, ft_id: np.ndarray, site_xyz: np.ndarray) -> dict
         em=np.zeros(ne.value, np.float32), fm=np.zeros(nt.value, np.float32),
         tri_face=np.zeros(nt.value, np.int32), face_sites=np.zeros((nf.value, 2), np.int32))
     L.vco_vd_get(h, *[_ptr(out[k]) for k in ("vts", "edges", "tris", "vm", "em", "fm", "tri_face", "face_sites")])
+    out["radius"] = np.zeros(nv.value, np.float32)
+    L.vco_vd_radius(h, _ptr(out["radius"]))
     L.vco_vd_free(h)
     out["inside_size"] = float(isz.value)
     return out

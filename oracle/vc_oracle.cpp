@@ -129,7 +129,7 @@ inline float lambda_of(const float* sxyz, int32_t s0, int32_t s1) {
 }
 
 struct VD {
-    std::vector<float> vts, vm, em, fm;
+    std::vector<float> vts, vm, em, fm, radius;
     std::vector<int32_t> edges, tris, tri_face, face_sites;
     long long nface = 0;
     float inside_size = 0.0f;
@@ -427,6 +427,32 @@ void* vco_lattice_vd(const uint8_t* occ, int X, int Y, int Z, const int32_t* ft_
             m = std::max(m, face_l[f]);
         }
     }
+    // 3b) radius per vertex, VoroInfo::computeInfoRelatedtoSites
+    // (voroinfo.cpp:286-325): for every Voronoi face in face order (here all
+    // candidate faces, valid or not, in (lattice point, axis) order), each
+    // vertex of the face gets r = dist(first site of the face, vertex); the
+    // last face to touch a vertex wins (voroinfo.cpp:316).  The first site of
+    // face (p, d) is the label of its lower end p.
+    R->radius.assign((size_t)nvv, 0.0f);
+    for (int64_t a = 0; a <= X; ++a)
+        for (int64_t b = 0; b <= Y; ++b)
+            for (int64_t c = 0; c <= Z; ++c)
+                for (int d = 0; d < 3; ++d) {
+                    if (!cand(a, b, c, d)) continue;
+                    const int32_t s0 = ft_id[lid(a, b, c)];
+                    int64_t p[3] = {a, b, c}, v[3];
+                    for (int q = 0; q < 4; ++q) {
+                        quad_voxel(p, d, q, v);
+                        if (!inside(v[0], v[1], v[2])) continue;
+                        const int32_t vi = vid[vox(v[0], v[1], v[2])];
+                        float r = 0.0f;  // trimesh::dist(site_p, v_p), float accumulation
+                        for (int k = 0; k < 3; ++k) {
+                            float t = (float)v[k] - sxyz[3 * (int64_t)s0 + k];
+                            r += t * t;
+                        }
+                        R->radius[(size_t)vi] = std::sqrt(r);
+                    }
+                }
     // 4) valid edges (both ends inside, side of some candidate face) in
     // (voxel, axis) order; measure = max lambda over incident valid faces.
     // The dual edge (v, v+e_d) is a side of the dual squares of the four
@@ -545,6 +571,11 @@ void vco_vd_get(void* h, float* vts, int32_t* edges, int32_t* tris, float* vm, f
     cp(fm, R->fm);
     cp(tri_face, R->tri_face);
     cp(face_sites, R->face_sites);
+}
+
+void vco_vd_radius(void* h, float* radius) {
+    auto* R = static_cast<VD*>(h);
+    if (radius && !R->radius.empty()) std::memcpy(radius, R->radius.data(), R->radius.size() * sizeof(float));
 }
 
 void vco_vd_free(void* h) { delete static_cast<VD*>(h); }

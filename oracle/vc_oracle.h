@@ -47,6 +47,10 @@ void vco_vd_sizes(void* h, long long* nv, long long* ne, long long* nt, long lon
 // triangle); tri_face: polygon face index per triangle; face_sites: nface*2.
 void vco_vd_get(void* h, float* vts, int32_t* edges, int32_t* tris, float* vm, float* em, float* fm,
                 int32_t* tri_face, int32_t* face_sites);
+// Radius per vertex (nv floats), VoroInfo::computeInfoRelatedtoSites
+// (voroinfo.cpp:286-325): distance from the vertex to the first site of the
+// last Voronoi face, in face order, that has the vertex.
+void vco_vd_radius(void* h, float* radius);
 void vco_vd_free(void* h);
 
 // cellcomplex(vts, edges, tris).finalize() (cellcomplex.cpp:13-26, 364-491):

@@ -35,6 +35,8 @@ int main(int argc, char** argv) {
         std::vector<int> from_fi;
         std::vector<float> vm, em, fm;
         const float inside = vcgpu::extractInsideWithMeasure(ctx, vol, vts, edges, tris, from_fi, vm, em, fm);
+        std::vector<float> radii;
+        vcgpu::getRadii(ctx, vts, radii);
         vcgpu::Context ctx2(0);
         vcgpu::cellcomplex cc(ctx2, vts, edges, tris);
         vcgpu::CellComplexThinning ccthin;
@@ -60,6 +62,8 @@ int main(int argc, char** argv) {
         for (int i : re) std::printf(" %d", i);
         std::printf("\nkeep_f");
         for (int i : rf) std::printf(" %d", i);
+        std::printf("\nradius");
+        for (float r : radii) std::printf(" %.9g", r);
         std::printf("\n");
     } catch (const vcgpu::Error& e) {
         std::cerr << e.what() << "\n";

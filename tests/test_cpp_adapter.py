@@ -53,5 +53,8 @@ def test_adapter_drives_gpu_path_like_the_reference(tmp_path, t):
     for key in ("keep_v", "keep_e", "keep_f"):
         got = np.array([int(x) for x in lines[key].split()], np.int64)
         assert np.array_equal(got, np.nonzero(ref["thin"][key])[0]), key
+    from helpers import lattice_case
+    radius = np.array([float(x) for x in lines["radius"].split()], np.float32)
+    assert np.array_equal(radius, lattice_case(oracle, occ)["vd"]["radius"])
     nv, ne, nt = (int(x) for x in lines["remaining"].split())
     assert (nv, ne, nt) == (len(ref["rem_vts"]), len(ref["rem_edges"]), len(ref["rem_tris"]))

@@ -44,3 +44,43 @@ def test_ties_go_to_lowest_index():
     d2, ids = O.ft(occ.shape, li)
     d2b, idb = O.ft(occ.shape, li, brute=True)
     assert np.array_equal(ids, idb) and np.array_equal(d2, d2b)
+
+
+@pytest.mark.parametrize("name,occ", list(_cases())[:3])
+def test_radius_follows_the_reference_loop(name, occ):
+    """VoroInfo::computeInfoRelatedtoSites (voroinfo.cpp:286-325) restated as
+    a plain loop: every Voronoi face, in face order, writes the distance from
+    its first site to each of its vertices; the last write wins."""
+    xyz, li = O.extract_sites(occ)
+    _, ids = O.ft(occ.shape, li)
+    vd = O.lattice_vd(occ, ids, xyz)
+    X, Y, Z = occ.shape
+    vid = {tuple(int(c) for c in v): i for i, v in enumerate(vd["vts"])}
+    r = np.zeros(len(vd["vts"]), np.float32)
+    for a in range(X + 1):
+        for b in range(Y + 1):
+            for c in range(Z + 1):
+                for d in range(3):
+                    e = [a, b, c]
+                    e[d] += 1
+                    if e[0] > X or e[1] > Y or e[2] > Z:
+                        continue
+                    s0, s1 = ids[a, b, c], ids[e[0], e[1], e[2]]
+                    if s0 < 0 or s1 < 0 or s0 == s1:
+                        continue
+                    u, w = (d + 1) % 3, (d + 2) % 3
+                    for s, t in ((0, 0), (1, 0), (1, 1), (0, 1)):
+                        v = [0, 0, 0]
+                        v[d], v[u], v[w] = (a, b, c)[d], (a, b, c)[u] - 1 + s, (a, b, c)[w] - 1 + t
+                        i = vid.get(tuple(v))
+                        if i is None:
+                            continue
+                        diff = np.float32(v) - xyz[s0]
+                        acc = np.float32(0)
+                        for k in range(3):
+                            acc = np.float32(acc + np.float32(diff[k] * diff[k]))
+                        r[i] = np.sqrt(acc, dtype=np.float32)
+    assert len(vd["radius"]) == len(vd["vts"])
+    assert np.array_equal(vd["radius"], r)
+    # every vertex lies on some Voronoi face, so every radius was written
+    assert (vd["radius"] > 0).all() or len(r) == 0

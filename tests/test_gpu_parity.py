@@ -47,6 +47,7 @@ def test_sites_ft_vd_match_oracle(gpu_ctx, name, occ):
     assert s["inside_size"] == ovd["inside_size"]
     for k in ("vts", "edges", "tris", "vm", "em", "fm", "tri_face", "face_sites"):
         assert np.array_equal(vd[k], ovd[k]), k
+    assert np.array_equal(ctx.vertex_radii(), ovd["radius"]), "radius"
     # the lattice complex is installed already finalized: its adjacency must be
     # what cellcomplex::finalize builds from (vts, edges, tris)
     ctx.use_vd_as_complex()
@@ -64,6 +65,7 @@ def test_empty_volume(gpu_ctx):
     assert (ids == -1).all() and (d2 == np.iinfo(np.int32).max).all()
     s = gpu_ctx.lattice_vd()
     assert s["nv"] == s["ne"] == s["nt"] == 0
+    assert len(gpu_ctx.vertex_radii()) == 0
 
 
 def test_sites_match_reference_golden(gpu_ctx, golden):

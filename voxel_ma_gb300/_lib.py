@@ -63,6 +63,7 @@ SIGNATURES = {
     "vc_get_ft": (c_int, [c_vp, c_vp, c_vp, c_int]),
     "vc_lattice_vd": (c_int, [c_vp, ctypes.POINTER(VdSizes)]),
     "vc_get_vd": (c_int, [c_vp] + [c_vp] * 8 + [c_int]),
+    "vc_vertex_radii": (c_int, [c_vp, c_vp, c_int]),
     "vc_set_complex": (c_int, [c_vp, c_i64, c_vp, c_i64, c_vp, c_i64, c_vp, c_int]),
     "vc_finalize": (c_int, [c_vp, ctypes.POINTER(c_i64)]),
     "vc_get_finalized": (c_int, [c_vp] + [c_vp] * 6 + [c_int]),

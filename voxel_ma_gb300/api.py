@@ -180,6 +180,13 @@ class Context:
         o["inside_size"] = s["inside_size"]
         return o
 
+    def vertex_radii(self, device: bool = False):
+        """VoroInfo::getRadii for the lattice complex's vertices (voroinfo.cpp:286-325)."""
+        r = self._out((self.vd_sizes["nv"],), np.float32, device)
+        p, mem = _ptr_mem(r)
+        self.check(self.lib.vc_vertex_radii(self.h, p, mem), "vc_vertex_radii")
+        return r
+
     # -- cell complex -----------------------------------------------------
     def set_complex(self, vts, edges, tris):
         vts = vts.reshape(-1, 3) if vts is not None else None

@@ -8,6 +8,7 @@ namespace vc {
 int run_sites(vc_ctx* c, int64_t* n_sites);
 int run_ft(vc_ctx* c);
 int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes);
+int run_vertex_radii(vc_ctx* c);
 int run_finalize(vc_ctx* c, int64_t* ne_final);
 int build_adjacency(vc_ctx* c);
 int run_thin(vc_ctx* c, float f_t, float l_t, vc_thin_stats* stats);
@@ -96,6 +97,14 @@ int vc_get_vd(vc_ctx* c, float* vts, int32_t* edges, int32_t* tris, int32_t* tri
     VC_TRY(copy_out(c, em, c->em.p, (size_t)s.ne * sizeof(float), mem));
     VC_TRY(copy_out(c, fm, c->fm.p, (size_t)s.nt * sizeof(float), mem));
     VC_TRY(copy_out(c, face_sites, c->vd_face_sites.p, (size_t)s.nface * 2 * sizeof(int32_t), mem));
+    return sync_check(c);
+}
+
+int vc_vertex_radii(vc_ctx* c, float* radius, int mem) {
+    VC_TRY(enter(c));
+    if (!good_mem(mem)) return VC_ERR_ARG;
+    VC_TRY(run_vertex_radii(c));
+    VC_TRY(copy_out(c, radius, c->vd_radius.p, (size_t)c->vd.nv * sizeof(float), mem));
     return sync_check(c);
 }
 

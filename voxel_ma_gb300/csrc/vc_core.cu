@@ -223,7 +223,7 @@ int vc_ctx_destroy(vc_ctx* c) {
     vc::DevBuf* all[] = {&c->err, &c->scratch, &c->scratch2, &c->occ, &c->site_xyz, &c->site_count,
                          &c->site_id_lat, &c->ft_d2, &c->ft_id, &c->ft_tmp, &c->vd_flags, &c->vd_voff,
                          &c->vd_eoff, &c->vd_foff, &c->vd_tri_face, &c->vd_face_sites, &c->vd_vm, &c->vd_bbox, &c->vd_lam,
-                         &c->vd_efoff, &c->vd_veoff, &c->vd_vpos, &c->vd_epos, &c->vd_fpos,
+                         &c->vd_efoff, &c->vd_veoff, &c->vd_vpos, &c->vd_epos, &c->vd_fpos, &c->vd_radius,
                          &c->vts, &c->edges_in, &c->edges, &c->tris, &c->tri_edges, &c->ve_off, &c->ve_ids,
                          &c->ef_off, &c->ef_ids, &c->hash_keys, &c->hash_pos, &c->hash_id, &c->side_slot,
                          &c->vm, &c->em, &c->fm, &c->face_rec, &c->edge_rec, &c->vert_rec,

@@ -93,6 +93,7 @@ struct vc_ctx {
     vc::DevBuf vd_flags;              // uint8 per lattice point
     vc::DevBuf vd_voff, vd_eoff, vd_foff;  // int32 exclusive offsets per lattice point
     vc::DevBuf vd_tri_face, vd_face_sites, vd_vm, vd_lam, vd_efoff, vd_veoff, vd_vpos, vd_epos, vd_fpos;
+    vc::DevBuf vd_radius;             // float per vertex of the lattice complex
     vc::DevBuf vd_bbox;  // int32[6]
     // cell complex (finalized, CSR)
     bool cc_valid = false;

@@ -514,6 +514,48 @@ inline int cell_grid(vc_ctx* c, int64_t n) {
     return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)c->num_sms * 16));
 }
 
+// Radius per vertex, VoroInfo::computeInfoRelatedtoSites
+// (voroinfo.cpp:286-325): every Voronoi face, in face order, writes
+// r = dist(first site of the face, vertex) into each of its vertices, so a
+// vertex keeps the value of the LAST face that has it (voroinfo.cpp:316).
+// The Voronoi faces through voxel v are the candidate edges among the 12
+// edges of v's cube; in (lattice point, axis) order the last one is found by
+// scanning the cube corners q = 7..0 (corner order is lattice order) and the
+// axes 2..0.  The first site of face (p, d) is the label of p.  The distance
+// is accumulated in float in trimesh's order and rounded by one correctly
+// rounded square root (exact for boxes up to 2^11 per side).
+__global__ void vd_radius_kernel(Grid g, const float* __restrict__ sxyz, const int64_t* __restrict__ vpos, int32_t nv,
+                                 float* __restrict__ radius) {
+    for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += gridDim.x * blockDim.x) {
+        int a, b, c;
+        decode32(vpos[v], g.NB, g.NC, a, b, c);
+        int32_t L[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) L[q] = g.label(a + ((q >> 2) & 1), b + ((q >> 1) & 1), c + (q & 1));
+        int32_t s = L[0];
+        bool found = false;
+#pragma unroll
+        for (int q = 7; q >= 0; --q)
+#pragma unroll
+            for (int d = 2; d >= 0; --d) {
+                const int bit = 4 >> d;
+                if (found || (q & bit)) continue;
+                if (L[q] != L[q | bit]) {
+                    s = L[q];
+                    found = true;
+                }
+            }
+        const float dx = (float)a - sxyz[3 * (int64_t)s + 0];
+        const float dy = (float)b - sxyz[3 * (int64_t)s + 1];
+        const float dz = (float)c - sxyz[3 * (int64_t)s + 2];
+        float r = 0.0f;
+        r = __fadd_rn(r, __fmul_rn(dx, dx));
+        r = __fadd_rn(r, __fmul_rn(dy, dy));
+        r = __fadd_rn(r, __fmul_rn(dz, dz));
+        radius[v] = __fsqrt_rn(r);
+    }
+}
+
 inline int row_grid(vc_ctx* c, int64_t rows) {
     return (int)std::max<int64_t>(1, std::min<int64_t>(rows, (int64_t)c->num_sms * 32));
 }
@@ -638,6 +680,20 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes) {
     c->meas_valid = true;
     c->records_fresh = true;
     if (sizes) *sizes = c->vd;
+    return VC_OK;
+}
+
+int run_vertex_radii(vc_ctx* c) {
+    if (!c->vd_valid || !c->ft_valid) return VC_ERR_STATE;
+    const int64_t nv = c->vd.nv;
+    VC_TRY(ensure_n<float>(c, c->vd_radius, nv));
+    if (nv == 0) return VC_OK;
+    Grid g{ptr<uint8_t>(c->occ), ptr<int32_t>(c->ft_id), c->X, c->Y, c->Z, (int64_t)c->Y + 1, (int64_t)c->Z + 1};
+    Region r(c, "vd_radius");
+    vd_radius_kernel<<<cell_grid(c, nv), 256, 0, c->stream>>>(g, ptr<float>(c->site_xyz), ptr<int64_t>(c->vd_vpos),
+                                                              (int32_t)nv, ptr<float>(c->vd_radius));
+    launched(c);
+    VC_CUDA(c, cudaGetLastError());
     return VC_OK;
 }
 
