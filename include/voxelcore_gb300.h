@@ -162,6 +162,37 @@ typedef struct {
 } vc_plain_result;
 int vc_run_plain(vc_ctx* ctx, const uint8_t* occ, int X, int Y, int Z, int mem, double t, vc_plain_result* out);
 
+/* ---- batched path --------------------------------------------------------
+ * Many volumes through one pass of the pipeline: every stage is one set of
+ * launches over all volumes of the batch (per-volume tables on the device)
+ * and the thinning replays the FIFO of all their complexes at once.  The
+ * reference processes one volume per exportInsideVoroMesh call
+ * (src/highlevelalgo.cpp:731-961); each volume's results here are those of
+ * vc_run_plain on that volume alone (its own site order, threshold
+ * float(inside_size_b * t) and surviving set): the volumes' complexes share
+ * no cell, and the FIFO order restricted to one complex is the order of
+ * that complex alone.
+ *
+ * vc_batch_set_volumes: dims = 3 ints (X, Y, Z) per volume, each in
+ * [1, 32766]; occ = the volumes' voxels one after another (each x-major, z
+ * fastest), host or device per `mem`.                                      */
+typedef struct {
+    int64_t n_sites;
+    vc_vd_sizes vd;        /* the volume's lattice complex and inside-part size */
+    float thresh;          /* float(inside_size * t) */
+    vc_rem_sizes rem;      /* its remaining complex */
+    vc_euler_info euler;   /* of its remaining complex (with_euler != 0) */
+    int64_t site_off;                   /* first site in vc_get_sites */
+    int64_t v_off, e_off, t_off;        /* first cell in the batch complex (vc_get_vd, vc_get_thin_flags) */
+    int64_t rem_v_off, rem_e_off, rem_t_off;  /* first cell in vc_get_remaining (ids local to the volume) */
+} vc_batch_volume;
+int vc_batch_set_volumes(vc_ctx* ctx, int nvol, const int32_t* dims, const uint8_t* occ, int mem);
+/* Runs sites -> feature transform -> lattice complex with lambda -> thinning
+ * -> remaining complex (-> Euler characteristic and components) for every
+ * volume; out (host) receives nvol entries, stats (optional) the totals of
+ * the batch's thinning.                                                    */
+int vc_batch_run(vc_ctx* ctx, double t, int with_euler, vc_thin_stats* stats, vc_batch_volume* out);
+
 /* ---- site extraction without device allocation ---------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc
  * (a host framework or allocator that owns the device heap, or a plugin that

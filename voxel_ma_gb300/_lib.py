@@ -41,6 +41,12 @@ class PlainResult(ctypes.Structure):
     _fields_ = [("n_sites", c_i64), ("vd", VdSizes), ("thresh", c_float), ("thin", ThinStats), ("rem", RemSizes)]
 
 
+class BatchVolume(ctypes.Structure):
+    _fields_ = [("n_sites", c_i64), ("vd", VdSizes), ("thresh", c_float), ("rem", RemSizes), ("euler", EulerInfo),
+                ("site_off", c_i64), ("v_off", c_i64), ("e_off", c_i64), ("t_off", c_i64),
+                ("rem_v_off", c_i64), ("rem_e_off", c_i64), ("rem_t_off", c_i64)]
+
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "vc_version": (c_int, []),
@@ -64,6 +70,8 @@ SIGNATURES = {
     "vc_lattice_vd": (c_int, [c_vp, ctypes.POINTER(VdSizes)]),
     "vc_get_vd": (c_int, [c_vp] + [c_vp] * 8 + [c_int]),
     "vc_vertex_radii": (c_int, [c_vp, c_vp, c_int]),
+    "vc_batch_set_volumes": (c_int, [c_vp, c_int, c_vp, c_vp, c_int]),
+    "vc_batch_run": (c_int, [c_vp, ctypes.c_double, c_int, ctypes.POINTER(ThinStats), c_vp]),
     "vc_set_complex": (c_int, [c_vp, c_i64, c_vp, c_i64, c_vp, c_i64, c_vp, c_int]),
     "vc_finalize": (c_int, [c_vp, ctypes.POINTER(c_i64)]),
     "vc_get_finalized": (c_int, [c_vp] + [c_vp] * 6 + [c_int]),

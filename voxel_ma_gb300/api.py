@@ -273,6 +273,69 @@ class Context:
                               generations=r.thin.generations),
                     rem=dict(self.rem_sizes))
 
+    # -- batched path ------------------------------------------------------
+    def batch_set_volumes(self, vols=None, *, occ=None, dims=None):
+        """Install a batch: a list of volumes, or their voxels concatenated
+        (1-D, host array or CUDA tensor) with dims (nvol x 3)."""
+        if vols is not None:
+            dims = np.array([tuple(int(x) for x in v.shape) for v in vols], np.int32)
+            if _is_torch(vols[0]):
+                import torch
+                occ = torch.cat([v.contiguous().reshape(-1) for v in vols])
+            else:
+                occ = np.concatenate([np.ascontiguousarray(v, dtype=np.uint8).reshape(-1) for v in vols])
+        dims = np.ascontiguousarray(np.asarray(dims, np.int32).reshape(-1, 3))
+        p, mem = _ptr_mem(occ)
+        self.check(self.lib.vc_batch_set_volumes(self.h, len(dims), dims.ctypes.data_as(ctypes.c_void_p), p, mem),
+                   "vc_batch_set_volumes")
+        self.batch_dims = dims
+        self.shape = tuple(int(x) for x in dims[0])
+
+    def batch_run(self, t: float = 0.04, euler: bool = True) -> list:
+        """vc_batch_run: per-volume results (sizes, threshold, Euler and the
+        volume's offsets into the batch-wide outputs)."""
+        n = len(self.batch_dims)
+        out = (L.BatchVolume * n)()
+        st = L.ThinStats()
+        self.check(self.lib.vc_batch_run(self.h, ctypes.c_double(t), int(euler), ctypes.byref(st), out),
+                   "vc_batch_run")
+        res = []
+        for o in out:
+            res.append(dict(
+                n_sites=o.n_sites, thresh=o.thresh,
+                vd=dict(nv=o.vd.nv, ne=o.vd.ne, nt=o.vd.nt, nface=o.vd.nface, inside_size=o.vd.inside_size),
+                rem=dict(nv=o.rem.nv, ne=o.rem.ne, nt=o.rem.nt),
+                euler=dict(V=o.euler.V, E=o.euler.E, F=o.euler.F, C=o.euler.C, euler=o.euler.euler),
+                site_off=o.site_off, v_off=o.v_off, e_off=o.e_off, t_off=o.t_off,
+                rem_v_off=o.rem_v_off, rem_e_off=o.rem_e_off, rem_t_off=o.rem_t_off))
+        self.batch_stats = dict(pushes=st.pushes, processed=st.processed, skipped=st.skipped,
+                                generations=st.generations)
+        self.n_sites = sum(r["n_sites"] for r in res)
+        self.vd_sizes = dict(nv=sum(r["vd"]["nv"] for r in res), ne=sum(r["vd"]["ne"] for r in res),
+                             nt=sum(r["vd"]["nt"] for r in res), nface=sum(r["vd"]["nface"] for r in res),
+                             inside_size=res[0]["vd"]["inside_size"])
+        self.use_vd_as_complex()
+        self.rem_sizes = dict(nv=sum(r["rem"]["nv"] for r in res), ne=sum(r["rem"]["ne"] for r in res),
+                              nt=sum(r["rem"]["nt"] for r in res))
+        return res
+
+    def batch_split(self, res: list, device: bool = False) -> list:
+        """Per-volume (sites, keep flags, remaining arrays) of the last batch_run."""
+        sites = self.sites()
+        fl = self.thin_flags()
+        rv, re_, rt = self.remaining_arrays(device)
+        out = []
+        for r in res:
+            v0, e0, t0 = r["v_off"], r["e_off"], r["t_off"]
+            a, b, c = r["rem_v_off"], r["rem_e_off"], r["rem_t_off"]
+            out.append(dict(
+                sites=sites[r["site_off"]:r["site_off"] + r["n_sites"]],
+                keep_v=fl["keep_v"][v0:v0 + r["vd"]["nv"]], keep_e=fl["keep_e"][e0:e0 + r["vd"]["ne"]],
+                keep_f=fl["keep_f"][t0:t0 + r["vd"]["nt"]], removed_e=fl["removed_e"][e0:e0 + r["vd"]["ne"]],
+                rem_vts=rv[a:a + r["rem"]["nv"]], rem_edges=re_[b:b + r["rem"]["ne"]],
+                rem_tris=rt[c:c + r["rem"]["nt"]]))
+        return out
+
 
 # ---------------------------------------------------------------------------
 # Reference-shaped surfaces

@@ -7,11 +7,12 @@
 namespace vc {
 int run_sites(vc_ctx* c, int64_t* n_sites);
 int run_ft(vc_ctx* c);
-int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes);
+int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes, double t_thr);
 int run_vertex_radii(vc_ctx* c);
 int run_finalize(vc_ctx* c, int64_t* ne_final);
 int build_adjacency(vc_ctx* c);
 int run_thin(vc_ctx* c, float f_t, float l_t, vc_thin_stats* stats);
+int run_thin_folded(vc_ctx* c, vc_thin_stats* stats);
 int get_thin_flags(vc_ctx* c, uint8_t* kv, uint8_t* ke, uint8_t* kf, uint8_t* re, int mem);
 int run_remaining(vc_ctx* c, vc_rem_sizes* sizes);
 int run_euler_remaining(vc_ctx* c, vc_euler_info* out);
@@ -39,6 +40,8 @@ int vc_set_volume(vc_ctx* c, const uint8_t* occ, int X, int Y, int Z, int mem) {
     const int64_t n = (int64_t)X * Y * Z;
     VC_TRY(ensure_n<uint8_t>(c, c->occ, n));
     VC_TRY(copy_in(c, c->occ.p, occ, (size_t)n, mem));
+    const int32_t dims[3] = {X, Y, Z};
+    VC_TRY(set_volume_table(c, 1, dims));
     c->X = X;
     c->Y = Y;
     c->Z = Z;
@@ -71,7 +74,7 @@ int vc_get_ft(vc_ctx* c, int32_t* d2, int32_t* id, int mem) {
     VC_TRY(enter(c));
     if (!c->ft_valid) return VC_ERR_STATE;
     if (!good_mem(mem)) return VC_ERR_ARG;
-    const size_t n = (size_t)(c->X + 1) * (c->Y + 1) * (c->Z + 1);
+    const size_t n = (size_t)c->h_off[kLat][c->nvol];  // all lattice points of the batch
     VC_TRY(copy_out(c, d2, c->ft_d2.p, n * sizeof(int32_t), mem));
     VC_TRY(copy_out(c, id, c->ft_id.p, n * sizeof(int32_t), mem));
     return sync_check(c);
@@ -79,7 +82,7 @@ int vc_get_ft(vc_ctx* c, int32_t* d2, int32_t* id, int mem) {
 
 int vc_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes) {
     VC_TRY(enter(c));
-    VC_TRY(run_lattice_vd(c, sizes));
+    VC_TRY(run_lattice_vd(c, sizes, -1.0));
     return sync_check(c);
 }
 
@@ -127,6 +130,7 @@ int vc_set_complex(vc_ctx* c, int64_t nv, const float* vts, int64_t ne, const in
     c->cc_valid = true;
     c->cc_finalized = c->meas_valid = c->thin_valid = c->rem_valid = false;
     c->records_fresh = false;
+    c->cc_batched = false;
     c->vd_valid = false;  // the complex no longer comes from the lattice VD
     return VC_OK;
 }
@@ -207,12 +211,88 @@ int vc_run_plain(vc_ctx* c, const uint8_t* occ, int X, int Y, int Z, int mem, do
     VC_TRY(vc_set_volume(c, occ, X, Y, Z, mem));
     VC_TRY(run_sites(c, &out->n_sites));
     VC_TRY(run_ft(c));
-    VC_TRY(run_lattice_vd(c, &out->vd));
+    VC_TRY(run_lattice_vd(c, &out->vd, -1.0));
     // highlevelalgo.cpp:836: float thresh = getInsidePartSize() * t (float * double -> float)
     out->thresh = (float)((double)out->vd.inside_size * t);
     VC_TRY(run_thin(c, out->thresh, out->thresh, &out->thin));
     VC_TRY(run_remaining(c, &out->rem));
     return sync_check(c);
+}
+
+int vc_batch_set_volumes(vc_ctx* c, int nvol, const int32_t* dims, const uint8_t* occ, int mem) {
+    VC_TRY(enter(c));
+    if (nvol <= 0 || !dims || !occ || !good_mem(mem)) return VC_ERR_ARG;
+    int64_t nvox = 0;
+    for (int b = 0; b < nvol; ++b) {
+        const int X = dims[3 * b], Y = dims[3 * b + 1], Z = dims[3 * b + 2];
+        if (X <= 0 || Y <= 0 || Z <= 0 || X > 32766 || Y > 32766 || Z > 32766) return VC_ERR_ARG;
+        if (space_size(kLat, X, Y, Z) >= ((int64_t)1 << 32)) return VC_ERR_ARG;
+        nvox += (int64_t)X * Y * Z;
+    }
+    VC_TRY(ensure_n<uint8_t>(c, c->occ, nvox));
+    VC_TRY(copy_in(c, c->occ.p, occ, (size_t)nvox, mem));
+    VC_TRY(set_volume_table(c, nvol, dims));
+    c->X = dims[0];
+    c->Y = dims[1];
+    c->Z = dims[2];
+    c->n_sites = -1;
+    c->ft_valid = c->vd_valid = false;
+    return VC_OK;
+}
+
+int vc_batch_run(vc_ctx* c, double t, int with_euler, vc_thin_stats* stats, vc_batch_volume* out) {
+    VC_TRY(enter(c));
+    if (!out || c->nvol <= 0) return c->nvol <= 0 ? VC_ERR_STATE : VC_ERR_ARG;
+    const int nvol = c->nvol;
+    int64_t n_sites = 0;
+    vc_vd_sizes vd{};
+    vc_thin_stats th{};
+    vc_rem_sizes rem{};
+    VC_TRY(run_sites(c, &n_sites));
+    VC_TRY(run_ft(c));
+    VC_TRY(run_lattice_vd(c, &vd, t));
+    VC_TRY(run_thin_folded(c, &th));
+    VC_TRY(run_remaining(c, &rem));
+    vc_euler_info eu{};
+    if (with_euler) VC_TRY(run_euler_remaining(c, &eu));
+    // per-volume bookkeeping: the base tables
+    const size_t n1 = (size_t)nvol + 1;
+    std::vector<int64_t> hb((size_t)kNumBases * n1);
+    std::vector<float> hthr((size_t)nvol);
+    VC_CUDA(c, cudaMemcpyAsync(hb.data(), c->bases.b[0], hb.size() * sizeof(int64_t), cudaMemcpyDeviceToHost,
+                               c->stream));
+    VC_CUDA(c, cudaMemcpyAsync(hthr.data(), c->bases.thr, hthr.size() * sizeof(float), cudaMemcpyDeviceToHost,
+                               c->stream));
+    VC_TRY(sync_check(c));
+    auto B = [&](int k, int b) { return hb[(size_t)k * n1 + b]; };
+    for (int b = 0; b < nvol; ++b) {
+        vc_batch_volume& o = out[b];
+        o = vc_batch_volume{};
+        o.n_sites = B(kBSite, b + 1) - B(kBSite, b);
+        const int64_t nf = B(kBFace, b + 1) - B(kBFace, b);
+        o.vd.nv = B(kBVert, b + 1) - B(kBVert, b);
+        o.vd.ne = B(kBAxis, b + 1) - B(kBAxis, b) + nf;
+        o.vd.nt = 2 * nf;
+        o.vd.nface = nf;
+        o.vd.inside_size = c->vol_inside[b];
+        o.thresh = hthr[b];
+        o.site_off = B(kBSite, b);
+        o.v_off = B(kBVert, b);
+        o.e_off = B(kBAxis, b) + B(kBFace, b);
+        o.t_off = 2 * B(kBFace, b);
+        if (nvol > 1) {
+            const auto& r = c->h_rem_bases;
+            o.rem = vc_rem_sizes{r[b + 1] - r[b], r[n1 + b + 1] - r[n1 + b], r[2 * n1 + b + 1] - r[2 * n1 + b]};
+            o.rem_v_off = r[b];
+            o.rem_e_off = r[n1 + b];
+            o.rem_t_off = r[2 * n1 + b];
+        } else {
+            o.rem = rem;
+        }
+        if (with_euler) o.euler = c->vol_euler[b];
+    }
+    if (stats) *stats = th;
+    return VC_OK;
 }
 
 }  // extern "C"

@@ -118,6 +118,67 @@ int copy_in(vc_ctx* c, void* dst, const void* src, size_t bytes, int mem) {
     return VC_OK;
 }
 
+int set_volume_table(vc_ctx* c, int nvol, const int32_t* dims) {
+    if (nvol <= 0 || !dims) return VC_ERR_ARG;
+    c->nvol = nvol;
+    c->h_dims.assign(dims, dims + 3 * (size_t)nvol);
+    for (int s = 0; s < kNumSpaces; ++s) {
+        auto& o = c->h_off[s];
+        o.assign((size_t)nvol + 1, 0);
+        for (int b = 0; b < nvol; ++b) o[b + 1] = o[b] + space_size(s, dims[3 * b], dims[3 * b + 1], dims[3 * b + 2]);
+    }
+    VolTab t;
+    t.nvol = nvol;
+    t.d0 = make_int4(dims[0], dims[1], dims[2], 0);
+    if (nvol > 1) {
+        // device copy: int4 dims[nvol], then the starts of every space
+        const size_t n4 = (size_t)nvol, n8 = (size_t)nvol + 1;
+        const size_t bytes = n4 * sizeof(int4) + kNumSpaces * n8 * sizeof(int64_t);
+        c->h_tab_stage.resize(bytes);
+        auto* d4 = reinterpret_cast<int4*>(c->h_tab_stage.data());
+        for (int b = 0; b < nvol; ++b) d4[b] = make_int4(dims[3 * b], dims[3 * b + 1], dims[3 * b + 2], 0);
+        auto* o8 = reinterpret_cast<int64_t*>(c->h_tab_stage.data() + n4 * sizeof(int4));
+        for (int s = 0; s < kNumSpaces; ++s)
+            for (size_t b = 0; b < n8; ++b) o8[s * n8 + b] = c->h_off[s][b];
+        VC_TRY(ensure_n<uint8_t>(c, c->tab_buf, (int64_t)bytes));
+        VC_CUDA(c, cudaMemcpyAsync(c->tab_buf.p, c->h_tab_stage.data(), bytes, cudaMemcpyHostToDevice, c->stream));
+        VC_CUDA(c, cudaStreamSynchronize(c->stream));
+        t.dims = ptr<int4>(c->tab_buf);
+        const int64_t* d8 = reinterpret_cast<const int64_t*>(ptr<uint8_t>(c->tab_buf) + n4 * sizeof(int4));
+        for (int s = 0; s < kNumSpaces; ++s) t.off[s] = d8 + s * n8;
+    }
+    c->tab = t;
+    // per-volume bases: kNumBases int64 arrays, bbox, inside size, threshold
+    const size_t n8 = (size_t)nvol + 1;
+    const size_t bytes = kNumBases * n8 * sizeof(int64_t) + 6 * (size_t)nvol * sizeof(int32_t) +
+                         2 * (size_t)nvol * sizeof(float);
+    VC_TRY(ensure_n<uint8_t>(c, c->bases_buf, (int64_t)bytes));
+    uint8_t* p = ptr<uint8_t>(c->bases_buf);
+    for (int k = 0; k < kNumBases; ++k) c->bases.b[k] = reinterpret_cast<int64_t*>(p) + k * n8;
+    p += kNumBases * n8 * sizeof(int64_t);
+    c->bases.bbox = reinterpret_cast<int32_t*>(p);
+    p += 6 * (size_t)nvol * sizeof(int32_t);
+    c->bases.inside = reinterpret_cast<float*>(p);
+    c->bases.thr = c->bases.inside + nvol;
+    return VC_OK;
+}
+
+namespace {
+__global__ void fill_bases_kernel(VolTab T, int space, const int32_t* __restrict__ scan, const int64_t* total,
+                                  int64_t* __restrict__ out) {
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b <= T.nvol; b += gridDim.x * blockDim.x)
+        out[b] = b < T.nvol ? (int64_t)scan[T.start(space, b)] : *total;
+}
+}  // namespace
+
+int fill_bases(vc_ctx* c, int base, int space, const int32_t* scan, const int64_t* total_dev) {
+    const int n = c->nvol + 1;
+    fill_bases_kernel<<<(n + 255) / 256, 256, 0, c->stream>>>(c->tab, space, scan, total_dev, c->bases.b[base]);
+    launched(c);
+    VC_CUDA(c, cudaGetLastError());
+    return VC_OK;
+}
+
 int read_i64(vc_ctx* c, const int64_t* src, int64_t* out) {
     VC_CUDA(c, cudaMemcpyAsync(out, src, sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
     return sync_check(c);
@@ -222,8 +283,8 @@ int vc_ctx_destroy(vc_ctx* c) {
     cudaSetDevice(c->device);
     vc::DevBuf* all[] = {&c->err, &c->scratch, &c->scratch2, &c->occ, &c->site_xyz, &c->site_count,
                          &c->site_id_lat, &c->ft_d2, &c->ft_id, &c->ft_tmp, &c->vd_flags, &c->vd_voff,
-                         &c->vd_eoff, &c->vd_foff, &c->vd_tri_face, &c->vd_face_sites, &c->vd_vm, &c->vd_bbox, &c->vd_lam,
-                         &c->vd_efoff, &c->vd_veoff, &c->vd_vpos, &c->vd_epos, &c->vd_fpos, &c->vd_radius,
+                         &c->vd_eoff, &c->vd_foff, &c->vd_tri_face, &c->vd_face_sites, &c->vd_vm, &c->vd_lam,
+                         &c->vd_efoff, &c->vd_veoff, &c->vd_vpos, &c->vd_epos, &c->vd_fpos, &c->vd_radius, &c->tab_buf, &c->bases_buf,
                          &c->vts, &c->edges_in, &c->edges, &c->tris, &c->tri_edges, &c->ve_off, &c->ve_ids,
                          &c->ef_off, &c->ef_ids, &c->hash_keys, &c->hash_pos, &c->hash_id, &c->side_slot,
                          &c->vm, &c->em, &c->fm, &c->face_rec, &c->edge_rec, &c->vert_rec,

@@ -43,16 +43,21 @@ __device__ __forceinline__ int64_t cross_threshold(int64_t qp, int64_t gp, int32
     return fl + 1;
 }
 
-// Pass 1: one warp per row of NC points along z.
+// Pass 1: one warp per lattice row along z (volume b, a, b'), NC = Z_b + 1
+// points; `ncmax` is the longest row of the batch (shared memory per warp).
 __global__ void __launch_bounds__(256) ft_rows_kernel(const int32_t* __restrict__ site_id, int64_t* __restrict__ out,
-                                                      int64_t nrows, int NC) {
-    extern __shared__ int64_t left_sm[];  // per warp: NC entries
+                                                      VolTab T, int ncmax) {
+    extern __shared__ int64_t left_sm[];  // per warp: ncmax entries
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
-    int64_t* left = left_sm + (int64_t)wib * NC;
+    int64_t* left = left_sm + (int64_t)wib * ncmax;
     const int64_t warps_total = (int64_t)gridDim.x * (blockDim.x >> 5);
+    const int64_t nrows = T.total(kLRow);
     for (int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + wib; row < nrows; row += warps_total) {
-        const int32_t* in = site_id + row * NC;
+        const int bv = T.find(kLRow, row);
+        const int NC = T.dim(bv).z + 1;
+        const int64_t rbase = T.start(kLat, bv) + (row - T.start(kLRow, bv)) * NC;
+        const int32_t* in = site_id + rbase;
         // forward: latest site at or before c, packed (pos << 32 | id); -1 = none
         int64_t carry = -1;
         for (int c0 = 0; c0 < NC; c0 += 32) {
@@ -94,27 +99,38 @@ __global__ void __launch_bounds__(256) ft_rows_kernel(const int32_t* __restrict_
                     int64_t d = (v >> 32) - c;
                     best = min(best, pack(d * d, (int32_t)(uint32_t)(v & 0xffffffffLL)));
                 }
-                out[row * NC + c] = best;
+                out[rbase + c] = best;
             }
         }
         __syncwarp();
     }
 }
 
-// Passes 2 and 3: lower envelope along lines of length L.  Line l starts at
-// (l / M) * SB + (l % M) and steps by `stride`; consecutive l are
-// consecutive addresses, so each step is a coalesced access across the warp.
-// The envelope stack (position | start threshold << 16, both < 2^15) lives in
-// `stack` at [l * L + k].
-template <bool FINAL>
+// Passes 2 and 3: lower envelope along the lattice lines of every volume:
+// PASS 2 along y (local line (a, c), L = Y+1 points, stride Z+1), PASS 3
+// along x (local line (b, c), L = X+1 points, stride (Y+1)(Z+1)).
+// Consecutive lines of a volume are consecutive addresses, so each step is a
+// coalesced access across the warp.  The envelope stack (position | start
+// threshold << 16, both < 2^15) of local line l of volume b lives in `stack`
+// at lattice start of b + l * L + k.
+template <int PASS>
 __global__ void __launch_bounds__(256) ft_envelope_kernel(const int64_t* __restrict__ in, int64_t* __restrict__ out,
                                                           int32_t* __restrict__ d2o, int32_t* __restrict__ ido,
-                                                          int32_t* __restrict__ stack, int64_t nlines, int L,
-                                                          int64_t M, int64_t SB, int64_t stride) {
-    for (int64_t l = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; l < nlines;
-         l += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t base = (l / M) * SB + (l % M);
-        int32_t* st = stack + l * L;
+                                                          int32_t* __restrict__ stack, VolTab T) {
+    constexpr bool FINAL = PASS == 3;
+    constexpr int kSpace = PASS == 2 ? kYLine : kXLine;
+    const int64_t nlines = T.total(kSpace);
+    for (int64_t gl = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; gl < nlines;
+         gl += (int64_t)gridDim.x * blockDim.x) {
+        const int bv = T.find(kSpace, gl);
+        const int4 dm = T.dim(bv);
+        const int64_t NB = dm.y + 1, NC = dm.z + 1;
+        const int64_t lat0 = T.start(kLat, bv);
+        const int64_t l = gl - T.start(kSpace, bv);
+        const int L = PASS == 2 ? (int)NB : dm.x + 1;
+        const int64_t stride = PASS == 2 ? NC : NB * NC;
+        const int64_t base = lat0 + (PASS == 2 ? (l / NC) * NB * NC + (l % NC) : l);
+        int32_t* st = stack + lat0 + l * L;
         int k = 0;
         // cached top of stack
         int64_t tq = 0, tg = 0, tz = 0;
@@ -193,53 +209,52 @@ __global__ void __launch_bounds__(256) ft_envelope_kernel(const int64_t* __restr
 
 int run_ft(vc_ctx* c) {
     if (c->n_sites < 0) return VC_ERR_STATE;
-    const int64_t NA = c->X + 1, NB = c->Y + 1, NC = c->Z + 1;
-    if (NA > 32767 || NB > 32767 || NC > 32767) return VC_ERR_ARG;
-    const int64_t N = NA * NB * NC;
+    const int nvol = c->nvol;
+    int ncmax = 0;
+    for (int b = 0; b < nvol; ++b) {
+        const int64_t NA = c->h_dims[3 * b] + 1, NB = c->h_dims[3 * b + 1] + 1, NC = c->h_dims[3 * b + 2] + 1;
+        if (NA > 32767 || NB > 32767 || NC > 32767) return VC_ERR_ARG;
+        ncmax = std::max<int>(ncmax, (int)NC);
+    }
+    const int64_t N = c->h_off[kLat][nvol];
     VC_TRY(ensure_n<int32_t>(c, c->ft_d2, N));
     VC_TRY(ensure_n<int32_t>(c, c->ft_id, N));
     VC_TRY(ensure_n<int64_t>(c, c->ft_tmp, 2 * N));
     Region stage(c, "stage_ft");
     int64_t* A = ptr<int64_t>(c->ft_tmp);
     int64_t* B = A + N;
-    // envelope stacks reuse the d2 output buffer for pass 2 (int32 per point);
-    // pass 3 writes d2/id directly, so it takes its stack from the id buffer?
-    // No: pass 3 writes both outputs; its stack goes to B (free after pass 2 read).
     {
         const int warps_per_block = 8;
-        const size_t smem = (size_t)warps_per_block * NC * sizeof(int64_t);
+        const size_t smem = (size_t)warps_per_block * ncmax * sizeof(int64_t);
         if (smem > 200 * 1024) return VC_ERR_ARG;
         if (smem > 48 * 1024)
             VC_CUDA(c, cudaFuncSetAttribute(ft_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        const int64_t nrows = NA * NB;
+        const int64_t nrows = c->h_off[kLRow][nvol];
         int blocks = (int)std::min<int64_t>((nrows + warps_per_block - 1) / warps_per_block,
                                             (int64_t)c->num_sms * 8);
         Region r(c, "ft_rows");
-        ft_rows_kernel<<<blocks, warps_per_block * 32, smem, c->stream>>>(ptr<int32_t>(c->site_id_lat), A, nrows,
-                                                                          (int)NC);
+        ft_rows_kernel<<<blocks, warps_per_block * 32, smem, c->stream>>>(ptr<int32_t>(c->site_id_lat), A, c->tab,
+                                                                          ncmax);
         launched(c);
         VC_CUDA(c, cudaGetLastError());
     }
     {
-        // pass 2 along y: lines (a, c), base = a*NB*NC + c, stride NC
-        const int64_t nlines = NA * NC;
+        // pass 2 along y; its envelope stacks (one int32 per lattice point)
+        // live in the d2 output, which pass 3 writes last
+        const int64_t nlines = c->h_off[kYLine][nvol];
         int blocks = (int)std::min<int64_t>((nlines + 255) / 256, (int64_t)c->num_sms * 8);
-        int32_t* stack = ptr<int32_t>(c->ft_d2);  // NA*NC*NB int32 fits the d2 buffer exactly
         Region r(c, "ft_envelope_y");
-        ft_envelope_kernel<false><<<blocks, 256, 0, c->stream>>>(A, B, nullptr, nullptr, stack, nlines, (int)NB, NC,
-                                                                 NB * NC, NC);
+        ft_envelope_kernel<2><<<blocks, 256, 0, c->stream>>>(A, B, nullptr, nullptr, ptr<int32_t>(c->ft_d2), c->tab);
         launched(c);
         VC_CUDA(c, cudaGetLastError());
     }
     {
-        // pass 3 along x: lines (b, c), base = b*NC + c, stride NB*NC
-        const int64_t nlines = NB * NC;
+        // pass 3 along x; its stacks take the pass-1 buffer, dead by now
+        const int64_t nlines = c->h_off[kXLine][nvol];
         int blocks = (int)std::min<int64_t>((nlines + 255) / 256, (int64_t)c->num_sms * 8);
-        int32_t* stack = reinterpret_cast<int32_t*>(A);  // pass-1 output is dead now
         Region r(c, "ft_envelope_x");
-        ft_envelope_kernel<true><<<blocks, 256, 0, c->stream>>>(B, nullptr, ptr<int32_t>(c->ft_d2),
-                                                                ptr<int32_t>(c->ft_id), stack, nlines, (int)NA,
-                                                                NB * NC, 0, NB * NC);
+        ft_envelope_kernel<3><<<blocks, 256, 0, c->stream>>>(B, nullptr, ptr<int32_t>(c->ft_d2), ptr<int32_t>(c->ft_id),
+                                                             reinterpret_cast<int32_t*>(A), c->tab);
         launched(c);
         VC_CUDA(c, cudaGetLastError());
     }

@@ -61,6 +61,69 @@ struct __align__(32) VertRec {
 };
 static_assert(sizeof(FaceRec) == 32 && sizeof(EdgeRec) == 32 && sizeof(VertRec) == 32, "record size");
 
+// ---------------------------------------------------------------------------
+// Volume table.  Every stage runs over a batch of volumes stored one after
+// another (volume-major) in each per-voxel, per-lattice-point, per-site and
+// per-cell array; one volume is a batch of one.  For each index space a
+// kernel walks (voxels, lattice points, voxel rows along z, lattice rows
+// along z, lattice lines along y and along x) the table holds the start of
+// every volume and, at index nvol, the total.  With one volume nothing is
+// read from memory: the starts follow from the dims held in the table.
+enum Space : int { kVox = 0, kLat, kVRow, kLRow, kYLine, kXLine, kNumSpaces };
+
+__host__ __device__ __forceinline__ int64_t space_size(int s, int X, int Y, int Z) {
+    const int64_t x = X, y = Y, z = Z;
+    switch (s) {
+        case kVox: return x * y * z;
+        case kLat: return (x + 1) * (y + 1) * (z + 1);
+        case kVRow: return x * y;
+        case kLRow: return (x + 1) * (y + 1);
+        case kYLine: return (x + 1) * (z + 1);
+        default: return (y + 1) * (z + 1);
+    }
+}
+
+struct VolTab {
+    int nvol = 0;
+    int4 d0{};                      // dims of volume 0 (the only one when nvol == 1)
+    const int4* dims = nullptr;     // nvol entries (x, y, z, 0)
+    const int64_t* off[kNumSpaces] = {};  // nvol + 1 starts per space
+
+    __device__ __forceinline__ int4 dim(int b) const { return nvol == 1 ? d0 : dims[b]; }
+    __device__ __forceinline__ int64_t start(int s, int b) const {
+        if (nvol == 1) return b == 0 ? 0 : space_size(s, d0.x, d0.y, d0.z);
+        return off[s][b];
+    }
+    __device__ __forceinline__ int64_t total(int s) const { return start(s, nvol); }
+    // the volume whose range of space s holds index x
+    __device__ __forceinline__ int find(int s, int64_t x) const {
+        if (nvol == 1) return 0;
+        const int64_t* o = off[s];
+        int lo = 0, hi = nvol - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(o + mid) <= x) lo = mid;
+            else hi = mid - 1;
+        }
+        return lo;
+    }
+};
+
+// Per-volume bases of the outputs, filled on the device after the scans
+// (nvol + 1 entries each, the last one the total): first site, vertex, axis
+// edge, face, axis-edge E->F entry and V->E entry of every volume, and its
+// first vertex, edge and triangle of the remaining complex.  The cell
+// ids of volume b are volume-major: its vertices, then its axis edges
+// followed by its triangulation diagonals, then its triangles, all after
+// those of volumes < b.
+enum Base : int { kBSite = 0, kBVert, kBAxis, kBFace, kBEfAxis, kBVe, kBRemV, kBRemE, kBRemT, kNumBases };
+struct Bases {
+    int64_t* b[kNumBases] = {};
+    int32_t* bbox = nullptr;  // 6 per volume: min xyz, max xyz of the vertices
+    float* inside = nullptr;  // per volume: inside-part size
+    float* thr = nullptr;     // per volume: thinning threshold (batched runs)
+};
+
 }  // namespace vc
 
 // The opaque context.  Members are grouped by pipeline stage.
@@ -75,9 +138,17 @@ struct vc_ctx {
     vc::DevBuf scratch;  // scan tile sums and small temporaries
     vc::DevBuf scratch2;
 
-    // volume
+    // volumes: one (X, Y, Z) or a batch described by the table
     int X = 0, Y = 0, Z = 0;
-    vc::DevBuf occ;  // uint8 X*Y*Z
+    int nvol = 0;
+    std::vector<int32_t> h_dims;                      // 3 per volume
+    std::vector<int64_t> h_off[vc::kNumSpaces];       // nvol + 1 per space
+    vc::VolTab tab;
+    vc::DevBuf tab_buf;  // device copy of the table's arrays (batches only)
+    std::vector<uint8_t> h_tab_stage;
+    vc::Bases bases;
+    vc::DevBuf bases_buf;
+    vc::DevBuf occ;  // uint8, all voxels of all volumes
     // sites
     int64_t n_sites = -1;
     vc::DevBuf site_xyz;    // float3 per site
@@ -94,7 +165,8 @@ struct vc_ctx {
     vc::DevBuf vd_voff, vd_eoff, vd_foff;  // int32 exclusive offsets per lattice point
     vc::DevBuf vd_tri_face, vd_face_sites, vd_vm, vd_lam, vd_efoff, vd_veoff, vd_vpos, vd_epos, vd_fpos;
     vc::DevBuf vd_radius;             // float per vertex of the lattice complex
-    vc::DevBuf vd_bbox;  // int32[6]
+    std::vector<float> vol_inside;  // inside-part size per volume
+    bool cc_batched = false;        // the complex is the lattice complex of a batch of > 1 volumes
     // cell complex (finalized, CSR)
     bool cc_valid = false;
     bool cc_finalized = false;
@@ -114,6 +186,7 @@ struct vc_ctx {
     vc_thin_stats thin_stats{};
     vc::DevBuf face_rec, edge_rec, vert_rec;  // 32-byte per-cell thinning records
     bool records_fresh = false;               // records already hold this complex in reset state
+    bool records_thr_folded = false;          // ... with the per-volume thresholds folded in (threshold 0)
     vc::DevBuf q0, q1, cand, child, child_cnt, cells, blk_cnt, thr;
     vc::DevBuf keep_v, keep_e, keep_f, removed_e;  // uint8 survivor flags of the last thinning
     vc::DevBuf trace;           // optional per-generation trace of the thinning kernel
@@ -125,6 +198,8 @@ struct vc_ctx {
     vc::DevBuf rem_voff, rem_eoff, rem_foff;
     vc::DevBuf rem_vts, rem_edges, rem_tris;
     vc::DevBuf uf_parent, euler_tmp;
+    std::vector<int64_t> h_rem_bases;         // batches: remaining V / E / T starts, nvol + 1 each
+    std::vector<vc_euler_info> vol_euler;     // per volume, from the last vc_euler_remaining
 
     // instrumentation: kernels launched, and optional CUDA-event timing of
     // named regions on the context stream (resolved at the next sync)
@@ -165,6 +240,23 @@ int sync_check(vc_ctx* c);
 int copy_out(vc_ctx* c, void* dst, const void* src, size_t bytes, int mem);
 int copy_in(vc_ctx* c, void* dst, const void* src, size_t bytes, int mem);
 int* dev_err(vc_ctx* c);
+// Describe the context's volumes (dims: 3 ints per volume) and size the
+// per-volume base arrays.
+int set_volume_table(vc_ctx* c, int nvol, const int32_t* dims);
+// The entry of a base array (nvol + 1 ascending starts) whose range holds x.
+__device__ __forceinline__ int find_base(const int64_t* base, int nvol, int64_t x) {
+    if (nvol <= 1) return 0;
+    int lo = 0, hi = nvol - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(base + mid) <= x) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+// Fill one base array from an exclusive scan over a space: entry b = the scan
+// at volume b's start, entry nvol = the total (device, from total_dev).
+int fill_bases(vc_ctx* c, int base, int space, const int32_t* scan, const int64_t* total_dev);
 // Count kernel launches issued by the library on this context.
 inline void launched(vc_ctx* c, int n = 1) { c->launches += n; }
 // Resolve finished timing events into c->timers (called after a sync).

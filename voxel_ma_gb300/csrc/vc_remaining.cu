@@ -26,13 +26,28 @@ __global__ void rem_flags_kernel(const uint8_t* __restrict__ kv, const uint8_t* 
     }
 }
 
-// After the exclusive scans pv/pe/pf hold output positions.
+// Per-volume starts of the remaining complex (batches): the scans at each
+// volume's first vertex, edge and triangle.
+__global__ void rem_bases_kernel(Bases B, int nvol, int32_t nv, int32_t ne, int32_t nt, const int32_t* __restrict__ pv,
+                                 const int32_t* __restrict__ pe, const int32_t* __restrict__ pf,
+                                 const int64_t* __restrict__ tot) {
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b <= nvol; b += gridDim.x * blockDim.x) {
+        const int64_t v0 = B.b[kBVert][b], e0 = B.b[kBAxis][b] + B.b[kBFace][b], t0 = 2 * B.b[kBFace][b];
+        B.b[kBRemV][b] = v0 < nv ? pv[v0] : tot[0];
+        B.b[kBRemE][b] = e0 < ne ? pe[e0] : tot[1];
+        B.b[kBRemT][b] = t0 < nt ? pf[t0] : tot[2];
+    }
+}
+
+// After the exclusive scans pv/pe/pf hold output positions.  In a batch
+// (nmap > 1) vertex ids are made local to each volume's remaining complex.
 __global__ void rem_write_kernel(const uint8_t* __restrict__ kv, const uint8_t* __restrict__ ke,
                                  const uint8_t* __restrict__ kf, int32_t nv, int32_t ne, int32_t nt,
                                  const int32_t* __restrict__ pv, const int32_t* __restrict__ pe,
                                  const int32_t* __restrict__ pf, const float* __restrict__ vts,
                                  const int2* __restrict__ edges, const int32_t* __restrict__ tris,
-                                 float* __restrict__ ovts, int2* __restrict__ oedges, int32_t* __restrict__ otris) {
+                                 float* __restrict__ ovts, int2* __restrict__ oedges, int32_t* __restrict__ otris,
+                                 Bases B, int nmap) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (int64_t)nv + ne + nt; i += stride) {
         if (i < nv) {
@@ -45,14 +60,16 @@ __global__ void rem_write_kernel(const uint8_t* __restrict__ kv, const uint8_t* 
             const int64_t e = i - nv;
             if (!ke[e]) continue;
             const int2 ev = edges[e];
-            oedges[pe[e]] = make_int2(pv[ev.x], pv[ev.y]);
+            const int32_t sh = nmap > 1 ? (int32_t)B.b[kBRemV][find_base(B.b[kBVert], nmap, ev.x)] : 0;
+            oedges[pe[e]] = make_int2(pv[ev.x] - sh, pv[ev.y] - sh);
         } else {
             const int64_t f = i - nv - ne;
             if (!kf[f]) continue;
             const int64_t o = pf[f];
-            otris[3 * o + 0] = pv[tris[3 * f + 2]];
-            otris[3 * o + 1] = pv[tris[3 * f + 0]];
-            otris[3 * o + 2] = pv[tris[3 * f + 1]];
+            const int32_t sh = nmap > 1 ? (int32_t)B.b[kBRemV][find_base(B.b[kBVert], nmap, tris[3 * f])] : 0;
+            otris[3 * o + 0] = pv[tris[3 * f + 2]] - sh;
+            otris[3 * o + 1] = pv[tris[3 * f + 0]] - sh;
+            otris[3 * o + 2] = pv[tris[3 * f + 1]] - sh;
         }
     }
 }
@@ -121,18 +138,29 @@ __global__ void uf_union_kernel(const int32_t* __restrict__ mark, const int2* __
     }
 }
 
-__global__ void uf_roots_kernel(int32_t* parent, int32_t n, unsigned long long* roots) {
+// Components: roots of the union-find forest, per volume in a batch
+// (remaining vertex -> volume through the remaining-complex vertex starts).
+__global__ void uf_roots_kernel(int32_t* parent, int32_t n, unsigned long long* roots, Bases B, int nmap) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     unsigned long long local = 0;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
-        if (uf_find(parent, (int32_t)i) == i) ++local;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        if (uf_find(parent, (int32_t)i) != i) continue;
+        if (nmap > 1) atomicAdd(roots + find_base(B.b[kBRemV], nmap, i), 1ull);
+        else ++local;
+    }
     if (local) atomicAdd(roots, local);
 }
 
-__global__ void count_kernel(const int32_t* __restrict__ mark, int64_t n, unsigned long long* cnt) {
+// Marked edges, per volume in a batch (edge -> volume through its vertex).
+__global__ void count_kernel(const int32_t* __restrict__ mark, const int2* __restrict__ edges, int64_t n,
+                             unsigned long long* cnt, Bases B, int nmap) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     unsigned long long local = 0;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) local += mark[i] != 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        if (mark[i] == 0) continue;
+        if (nmap > 1) atomicAdd(cnt + find_base(B.b[kBVert], nmap, edges[i].x), 1ull);
+        else ++local;
+    }
     if (local) atomicAdd(cnt, local);
 }
 
@@ -161,6 +189,16 @@ int run_remaining(vc_ctx* c, vc_rem_sizes* sizes) {
     VC_TRY(scan_exclusive_i32(c, pv, pv, nv, tot + 0));
     VC_TRY(scan_exclusive_i32(c, pe, pe, ne, tot + 1));
     VC_TRY(scan_exclusive_i32(c, pf, pf, nt, tot + 2));
+    const int nmap = c->cc_batched ? c->nvol : 1;
+    if (nmap > 1) {
+        rem_bases_kernel<<<(nmap + 256) / 256, 256, 0, c->stream>>>(c->bases, nmap, (int32_t)nv, (int32_t)ne,
+                                                                    (int32_t)nt, pv, pe, pf, tot);
+        launched(c);
+        c->h_rem_bases.resize(3 * ((size_t)nmap + 1));
+        for (int k = 0; k < 3; ++k)
+            VC_CUDA(c, cudaMemcpyAsync(c->h_rem_bases.data() + k * ((size_t)nmap + 1), c->bases.b[kBRemV + k],
+                                       ((size_t)nmap + 1) * sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
+    }
     int64_t h[3] = {0, 0, 0};
     VC_CUDA(c, cudaMemcpyAsync(h, tot, 3 * sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
     VC_TRY(sync_check(c));
@@ -170,7 +208,7 @@ int run_remaining(vc_ctx* c, vc_rem_sizes* sizes) {
     rem_write_kernel<<<grid_for(c, nv + ne + nt, 256), 256, 0, c->stream>>>(
         ptr<uint8_t>(c->keep_v), ptr<uint8_t>(c->keep_e), ptr<uint8_t>(c->keep_f), (int32_t)nv, (int32_t)ne,
         (int32_t)nt, pv, pe, pf, ptr<float>(c->vts), ptr<int2>(c->edges), ptr<int32_t>(c->tris),
-        ptr<float>(c->rem_vts), ptr<int2>(c->rem_edges), ptr<int32_t>(c->rem_tris));
+        ptr<float>(c->rem_vts), ptr<int2>(c->rem_edges), ptr<int32_t>(c->rem_tris), c->bases, nmap);
     launched(c);
     VC_CUDA(c, cudaGetLastError());
     c->rem = vc_rem_sizes{h[0], h[1], h[2]};
@@ -184,16 +222,18 @@ int run_euler_remaining(vc_ctx* c, vc_euler_info* out) {
     const int64_t ne = c->ne, nt = c->nt, nvr = c->rem.nv;
     VC_TRY(ensure_n<int32_t>(c, c->uf_parent, std::max<int64_t>(nvr, ne) + 1));
     VC_TRY(ensure_n<int32_t>(c, c->scratch, ne + 1));
-    VC_TRY(ensure_n<int64_t>(c, c->scratch2, 4));
+    const int nmap = c->cc_batched ? c->nvol : 1;
+    VC_TRY(ensure_n<int64_t>(c, c->scratch2, 2 * (int64_t)nmap + 2));
     int32_t* mark = ptr<int32_t>(c->scratch);
+    // [0, nmap): marked edges per volume; [nmap, 2 nmap): components per volume
     auto* cnt = reinterpret_cast<unsigned long long*>(ptr<int64_t>(c->scratch2));
     VC_CUDA(c, cudaMemsetAsync(mark, 0, (ne + 1) * sizeof(int32_t), c->stream));
-    VC_CUDA(c, cudaMemsetAsync(cnt, 0, 2 * sizeof(unsigned long long), c->stream));
+    VC_CUDA(c, cudaMemsetAsync(cnt, 0, 2 * (size_t)nmap * sizeof(unsigned long long), c->stream));
     euler_mark_kernel<<<grid_for(c, ne + nt, 256), 256, 0, c->stream>>>(
         ptr<uint8_t>(c->keep_e), ptr<uint8_t>(c->keep_f), ptr<int32_t>(c->tri_edges), (int32_t)ne, (int32_t)nt,
         mark);
     launched(c);
-    count_kernel<<<grid_for(c, ne, 256), 256, 0, c->stream>>>(mark, ne, cnt);
+    count_kernel<<<grid_for(c, ne, 256), 256, 0, c->stream>>>(mark, ptr<int2>(c->edges), ne, cnt, c->bases, nmap);
     launched(c);
     int32_t* parent = ptr<int32_t>(c->uf_parent);
     if (nvr > 0) {
@@ -203,18 +243,37 @@ int run_euler_remaining(vc_ctx* c, vc_euler_info* out) {
                                                                       ptr<int32_t>(c->rem_voff), (int32_t)ne, parent,
                                                                       dev_err(c));
         launched(c);
-        uf_roots_kernel<<<grid_for(c, nvr, 256), 256, 0, c->stream>>>(parent, (int32_t)nvr, cnt + 1);
+        uf_roots_kernel<<<grid_for(c, nvr, 256), 256, 0, c->stream>>>(parent, (int32_t)nvr, cnt + nmap, c->bases,
+                                                                       nmap);
         launched(c);
     }
     VC_CUDA(c, cudaGetLastError());
-    unsigned long long h[2];
-    VC_CUDA(c, cudaMemcpyAsync(h, cnt, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    std::vector<unsigned long long> h(2 * (size_t)nmap);
+    VC_CUDA(c, cudaMemcpyAsync(h.data(), cnt, h.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                               c->stream));
     VC_TRY(sync_check(c));
-    out->V = nvr;
-    out->E = (int64_t)h[0];
-    out->F = c->rem.nt;
-    out->C = (int64_t)h[1];
-    out->euler = out->V - out->E + out->F;
+    c->vol_euler.assign((size_t)nmap, vc_euler_info{});
+    vc_euler_info all{};
+    for (int b = 0; b < nmap; ++b) {
+        vc_euler_info& e = c->vol_euler[b];
+        if (nmap > 1) {
+            const size_t n1 = (size_t)nmap + 1;
+            e.V = c->h_rem_bases[b + 1] - c->h_rem_bases[b];
+            e.F = c->h_rem_bases[2 * n1 + b + 1] - c->h_rem_bases[2 * n1 + b];
+        } else {
+            e.V = nvr;
+            e.F = c->rem.nt;
+        }
+        e.E = (int64_t)h[b];
+        e.C = (int64_t)h[nmap + b];
+        e.euler = e.V - e.E + e.F;
+        all.V += e.V;
+        all.E += e.E;
+        all.F += e.F;
+        all.C += e.C;
+    }
+    all.euler = all.V - all.E + all.F;
+    *out = all;
     return VC_OK;
 }
 

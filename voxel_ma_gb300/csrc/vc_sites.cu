@@ -97,41 +97,57 @@ __device__ __forceinline__ uint32_t new_corner_mask(uint32_t nb, uint32_t inb) {
     return res;
 }
 
-__global__ void sites_count_kernel(Vol v, int32_t* __restrict__ cnt) {
-    for (int64_t row = blockIdx.x; row < (int64_t)v.X * v.Y; row += gridDim.x) {
-        const int i = (int)(row / v.Y), j = (int)(row - (int64_t)i * v.Y);
+// One block per voxel row (volume b, x, y) of the batch, threads along z.
+__global__ void sites_count_kernel(const uint8_t* __restrict__ occ, VolTab T, int32_t* __restrict__ cnt) {
+    const int64_t nrows = T.total(kVRow);
+    for (int64_t row = blockIdx.x; row < nrows; row += gridDim.x) {
+        const int bv = T.find(kVRow, row);
+        const int4 d = T.dim(bv);
+        const Vol v{occ + T.start(kVox, bv), d.x, d.y, d.z};
+        const int64_t r = row - T.start(kVRow, bv);
+        const int i = (int)(r / v.Y), j = (int)(r - (int64_t)i * v.Y);
+        int32_t* out = cnt + T.start(kVox, bv) + r * v.Z;
         for (int k = threadIdx.x; k < v.Z; k += blockDim.x) {
-            const int64_t t = row * v.Z + k;
             const uint32_t nb = load_nbhd(v, i, j, k);
-            cnt[t] = __popc(new_corner_mask(nb, inbox_nbhd(v, i, j, k)));
+            out[k] = __popc(new_corner_mask(nb, inbox_nbhd(v, i, j, k)));
         }
     }
 }
 
-__global__ void sites_emit_kernel(Vol v, const int32_t* __restrict__ off, float* __restrict__ xyz,
-                                  int32_t* __restrict__ site_id_lat) {
-    const int64_t NB = v.Y + 1, NC = v.Z + 1;
-    for (int64_t row = blockIdx.x; row < (int64_t)v.X * v.Y; row += gridDim.x) {
-        const int i = (int)(row / v.Y), j = (int)(row - (int64_t)i * v.Y);
+// Sites are written at their batch-wide index; volume b's sites are the
+// contiguous range starting at its first site, in the reference's order.
+// site_id_lat (optional) receives the batch-wide index at each site's
+// lattice point.
+__global__ void sites_emit_kernel(const uint8_t* __restrict__ occ, VolTab T, const int32_t* __restrict__ off,
+                                  float* __restrict__ xyz, int32_t* __restrict__ site_id_lat) {
+    const int64_t nrows = T.total(kVRow);
+    for (int64_t row = blockIdx.x; row < nrows; row += gridDim.x) {
+        const int bv = T.find(kVRow, row);
+        const int4 d = T.dim(bv);
+        const Vol v{occ + T.start(kVox, bv), d.x, d.y, d.z};
+        const int64_t NB = v.Y + 1, NC = v.Z + 1;
+        const int64_t r = row - T.start(kVRow, bv);
+        const int i = (int)(r / v.Y), j = (int)(r - (int64_t)i * v.Y);
+        const int32_t* offr = off + T.start(kVox, bv) + r * v.Z;
+        int32_t* lat = site_id_lat ? site_id_lat + T.start(kLat, bv) : nullptr;
         for (int k = threadIdx.x; k < v.Z; k += blockDim.x) {
-            const int64_t t = row * v.Z + k;
             const uint32_t nb = load_nbhd(v, i, j, k);
             const uint32_t mask = new_corner_mask(nb, inbox_nbhd(v, i, j, k));
             if (!mask) continue;
-            int32_t o = off[t];
+            int32_t o = offr[k];
             const int cur = nb_bit(nb, 0, 0, 0);
             uint32_t done = 0;
-            for (int d = 0; d < 6; ++d) {
-                if (nb_bit(nb, kNbOff[d][0], kNbOff[d][1], kNbOff[d][2]) == cur) continue;
+            for (int dd = 0; dd < 6; ++dd) {
+                if (nb_bit(nb, kNbOff[dd][0], kNbOff[dd][1], kNbOff[dd][2]) == cur) continue;
                 for (int s = 0; s < 4; ++s) {
-                    const int c = kShared[d][s];
+                    const int c = kShared[dd][s];
                     if (!(mask & (1u << c)) || (done & (1u << c))) continue;
                     done |= 1u << c;
                     const int a = i + kCornerOff[c][0], b = j + kCornerOff[c][1], cc = k + kCornerOff[c][2];
                     xyz[3 * (int64_t)o + 0] = (float)a - 0.5f;
                     xyz[3 * (int64_t)o + 1] = (float)b - 0.5f;
                     xyz[3 * (int64_t)o + 2] = (float)cc - 0.5f;
-                    if (site_id_lat) site_id_lat[((int64_t)a * NB + b) * NC + cc] = o;
+                    if (lat) lat[((int64_t)a * NB + b) * NC + cc] = o;
                     ++o;
                 }
             }
@@ -147,27 +163,29 @@ inline int row_grid(int num_sms, int64_t rows) {
 }  // namespace
 
 int run_sites(vc_ctx* c, int64_t* n_sites) {
-    if (!c->occ.p || c->X <= 0) return VC_ERR_STATE;
-    const int64_t nvox = (int64_t)c->X * c->Y * c->Z;
-    const int64_t nlat = (int64_t)(c->X + 1) * (c->Y + 1) * (c->Z + 1);
+    if (!c->occ.p || c->nvol <= 0) return VC_ERR_STATE;
+    const int64_t nvox = c->h_off[kVox][c->nvol];
+    const int64_t nlat = c->h_off[kLat][c->nvol];
+    const int64_t nrows = c->h_off[kVRow][c->nvol];
     VC_TRY(ensure_n<int32_t>(c, c->site_count, nvox));
     VC_TRY(ensure_n<int32_t>(c, c->site_id_lat, nlat));
     VC_TRY(ensure_n<int64_t>(c, c->scratch2, 4));
     Region stage(c, "stage_sites");
-    Vol v{ptr<uint8_t>(c->occ), c->X, c->Y, c->Z};
+    const uint8_t* occ = ptr<uint8_t>(c->occ);
     int32_t* cnt = ptr<int32_t>(c->site_count);
-    sites_count_kernel<<<row_grid(c->num_sms, (int64_t)c->X * c->Y), 128, 0, c->stream>>>(v, cnt);
+    sites_count_kernel<<<row_grid(c->num_sms, nrows), 128, 0, c->stream>>>(occ, c->tab, cnt);
     launched(c);
     VC_CUDA(c, cudaGetLastError());
     int64_t* total = ptr<int64_t>(c->scratch2);
     VC_TRY(scan_exclusive_i32(c, cnt, cnt, nvox, total));
+    VC_TRY(fill_bases(c, kBSite, kVox, cnt, total));
     int64_t n = 0;
     VC_TRY(read_i64(c, total, &n));
     if (n > INT32_MAX) return VC_ERR_ARG;
     VC_TRY(ensure_n<float>(c, c->site_xyz, 3 * n));
     VC_CUDA(c, cudaMemsetAsync(c->site_id_lat.p, 0xff, (size_t)nlat * sizeof(int32_t), c->stream));
-    sites_emit_kernel<<<row_grid(c->num_sms, (int64_t)c->X * c->Y), 128, 0, c->stream>>>(v, cnt, ptr<float>(c->site_xyz),
-                                                                       ptr<int32_t>(c->site_id_lat));
+    sites_emit_kernel<<<row_grid(c->num_sms, nrows), 128, 0, c->stream>>>(occ, c->tab, cnt, ptr<float>(c->site_xyz),
+                                                                         ptr<int32_t>(c->site_id_lat));
     launched(c);
     VC_CUDA(c, cudaGetLastError());
     c->n_sites = n;
@@ -250,10 +268,13 @@ extern "C" int vc_extract_sites_noalloc(const uint8_t* occ, int X, int Y, int Z,
     NoAllocScratch s;
     VC_TRY(noalloc_scratch(&s));
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    const Vol v{occ, X, Y, Z};
+    // a one-volume table lives entirely in the kernel arguments
+    VolTab one;
+    one.nvol = 1;
+    one.d0 = make_int4(X, Y, Z, 0);
     // every scratch word read below is written first in this call: counts by
     // the count kernel, tile sums and the total by the scan
-    sites_count_kernel<<<row_grid(s.num_sms, (int64_t)X * Y), 128, 0, st>>>(v, s.counts);
+    sites_count_kernel<<<row_grid(s.num_sms, (int64_t)X * Y), 128, 0, st>>>(occ, one, s.counts);
     const int64_t tiles = (nvox + kScanTile - 1) / kScanTile;
     scan_tile_sums<int32_t><<<(unsigned)tiles, kScanThreads, 0, st>>>(s.counts, nvox, s.tiles);
     scan_sums_single<<<1, 1024, 0, st>>>(s.tiles, tiles, s.total);
@@ -268,7 +289,7 @@ extern "C" int vc_extract_sites_noalloc(const uint8_t* occ, int X, int Y, int Z,
     if (n > capacity) return VC_ERR_ARG;  // *n_sites tells the caller how much room is needed
     if (n > 0) {
         if (!xyz) return VC_ERR_ARG;
-        sites_emit_kernel<<<row_grid(s.num_sms, (int64_t)X * Y), 128, 0, st>>>(v, s.counts, xyz, nullptr);
+        sites_emit_kernel<<<row_grid(s.num_sms, (int64_t)X * Y), 128, 0, st>>>(occ, one, s.counts, xyz, nullptr);
     }
     if (cudaStreamSynchronize(st) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
         cudaGetLastError();

@@ -456,10 +456,27 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats);
 
 int run_thin(vc_ctx* c, float f_t, float l_t, vc_thin_stats* stats) {
     if (!c->cc_finalized || !c->meas_valid) return VC_ERR_STATE;
+    if (c->records_thr_folded) {
+        // records hold filter signs, not measures: rebuild them from em / fm
+        c->records_fresh = false;
+        c->records_thr_folded = false;
+    }
     VC_TRY(ensure_n<float>(c, c->thr, 2));
     set_thr_kernel<<<1, 1, 0, c->stream>>>(ptr<float>(c->thr), f_t, l_t);
     launched(c);
     VC_CUDA(c, cudaGetLastError());
+    return run_thin_with_device_thr(c, stats);
+}
+
+// Thinning of a batch whose per-volume thresholds were folded into the
+// records by the lattice emission: the filter is then "record < 0".
+int run_thin_folded(vc_ctx* c, vc_thin_stats* stats) {
+    if (!c->records_thr_folded || !c->records_fresh) return VC_ERR_STATE;
+    VC_TRY(ensure_n<float>(c, c->thr, 2));
+    set_thr_kernel<<<1, 1, 0, c->stream>>>(ptr<float>(c->thr), 0.0f, 0.0f);
+    launched(c);
+    VC_CUDA(c, cudaGetLastError());
+    c->records_thr_folded = false;
     return run_thin_with_device_thr(c, stats);
 }
 

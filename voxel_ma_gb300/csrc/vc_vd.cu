@@ -43,6 +43,13 @@ struct Grid {
     __device__ __forceinline__ int32_t label(int a, int b, int c) const { return lab[lid(a, b, c)]; }
 };
 
+// The grid of volume bv of the batch: its voxels and its lattice labels
+// (labels are batch-wide site indices, so they index the batch's site list).
+__device__ __forceinline__ Grid grid_of(const VolTab& T, int bv, const uint8_t* occ, const int32_t* lab) {
+    const int4 d = T.dim(bv);
+    return Grid{occ + T.start(kVox, bv), lab + T.start(kLat, bv), d.x, d.y, d.z, (int64_t)d.y + 1, (int64_t)d.z + 1};
+}
+
 
 // Lattice coordinates of point p (the lattice has fewer than 2^32 points).
 __device__ __forceinline__ void decode32(int64_t p, int64_t NB, int64_t NC, int& a, int& b, int& c) {
@@ -97,9 +104,18 @@ __device__ __forceinline__ bool face_valid(const Grid& g, int a, int b, int c, i
 
 // flags: bits 0-2 valid face along axis d; bit 3 vertex; bits 4-6 valid edge
 // along d.  lam[3p+d]: lambda of the valid face (p, d), computed once here.
-__global__ void vd_flags_kernel(Grid g, const float* __restrict__ sxyz, uint8_t* __restrict__ flags,
-                                float* __restrict__ lam, int64_t n) {
-    for (int64_t row = blockIdx.x; row < (int64_t)(g.X + 1) * g.NB; row += gridDim.x) {
+// One block per lattice row along z (volume bv, a, b) of the batch.
+__global__ void vd_flags_kernel(const uint8_t* __restrict__ occ, const int32_t* __restrict__ lab, VolTab T,
+                                const float* __restrict__ sxyz, uint8_t* __restrict__ flags_all,
+                                float* __restrict__ lam_all) {
+    const int64_t nrows = T.total(kLRow);
+    for (int64_t grow = blockIdx.x; grow < nrows; grow += gridDim.x) {
+        const int bv = T.find(kLRow, grow);
+        const Grid g = grid_of(T, bv, occ, lab);
+        const int64_t lat0 = T.start(kLat, bv);
+        uint8_t* flags = flags_all + lat0;
+        float* lam = lam_all + 3 * lat0;
+        const int64_t row = grow - T.start(kLRow, bv);
         const int a = (int)(row / g.NB), b = (int)(row - (int64_t)a * g.NB);
         for (int c = threadIdx.x; c < (int)g.NC; c += blockDim.x) {
             const int64_t p = row * g.NC + c;
@@ -186,10 +202,19 @@ __device__ __forceinline__ int plaquette_faces(const Grid& g, const uint8_t* __r
 
 // Per lattice point: 1 if vertex; edges; faces; E->F entries of its axis
 // edges; V->E entries of its vertex.
-__global__ void vd_counts_kernel(Grid g, const uint8_t* __restrict__ flags, int32_t* __restrict__ cv,
-                                 int32_t* __restrict__ ce, int32_t* __restrict__ cf, int32_t* __restrict__ cef,
-                                 int32_t* __restrict__ cve, int64_t n) {
-    for (int64_t row = blockIdx.x; row < (int64_t)(g.X + 1) * g.NB; row += gridDim.x) {
+__global__ void vd_counts_kernel(const uint8_t* __restrict__ occ, const int32_t* __restrict__ lab, VolTab T,
+                                 const uint8_t* __restrict__ flags_all, int32_t* __restrict__ cv_all,
+                                 int32_t* __restrict__ ce_all, int32_t* __restrict__ cf_all,
+                                 int32_t* __restrict__ cef_all, int32_t* __restrict__ cve_all) {
+    const int64_t nrows = T.total(kLRow);
+    for (int64_t grow = blockIdx.x; grow < nrows; grow += gridDim.x) {
+        const int bv = T.find(kLRow, grow);
+        const Grid g = grid_of(T, bv, occ, lab);
+        const int64_t lat0 = T.start(kLat, bv);
+        const uint8_t* flags = flags_all + lat0;
+        int32_t *cv = cv_all + lat0, *ce = ce_all + lat0, *cf = cf_all + lat0, *cef = cef_all + lat0,
+                *cve = cve_all + lat0;
+        const int64_t row = grow - T.start(kLRow, bv);
         const int a = (int)(row / g.NB), b = (int)(row - (int64_t)a * g.NB);
         for (int c = threadIdx.x; c < (int)g.NC; c += blockDim.x) {
             const int64_t p = row * g.NC + c;
@@ -234,7 +259,27 @@ struct Offs {
     const int32_t* foff;
     const int32_t* efoff;
     const int32_t* veoff;
+    // the same scans seen from a volume whose lattice starts at lat0
+    __device__ __forceinline__ Offs at(int64_t lat0) const {
+        return Offs{voff + lat0, eoff + lat0, foff + lat0, efoff + lat0, veoff + lat0};
+    }
 };
+
+// Batch-wide cell ids are volume-major (vertices; axis edges then diagonals;
+// triangles).  The scans count axis edges and faces over the whole batch, so
+// in volume bv an axis edge of scan rank e has id e + (faces before bv), the
+// diagonal of face f has id (axis edges up to and including bv) + f, an axis
+// edge's E->F list starts at its scan offset + 2 (faces before bv) and a
+// diagonal's at (axis E->F entries up to and including bv) + 2 f.
+struct Shift {
+    int64_t fb;    // faces before the volume
+    int64_t eb1;   // axis edges of volumes <= bv
+    int64_t efb1;  // axis-edge E->F entries of volumes <= bv
+    int64_t site;  // first site of the volume
+};
+__device__ __forceinline__ Shift shift_of(const Bases& B, int bv) {
+    return Shift{B.b[kBFace][bv], B.b[kBAxis][bv + 1], B.b[kBEfAxis][bv + 1], B.b[kBSite][bv]};
+}
 
 __device__ __forceinline__ int32_t edge_id(const uint8_t* flags, const Offs& o, int64_t lp, int d) {
     return o.eoff[lp] + rank_below((flags[lp] >> 4) & 7u, d);
@@ -259,27 +304,40 @@ __device__ __forceinline__ void sort_small(int32_t* x, int k) {
 // After the scans: the lattice position of every vertex, axis edge and face
 // (p, or p*4 + axis), so that the emit kernels run one thread per cell with
 // coalesced writes; also each vertex's V->E and each axis edge's E->F offset.
-__global__ void vd_positions_kernel(Grid g, const uint8_t* __restrict__ flags, Offs o, int64_t* __restrict__ vpos,
-                                    int64_t* __restrict__ epos, int64_t* __restrict__ fpos,
-                                    int32_t* __restrict__ ve_off, int32_t* __restrict__ ef_off) {
-    for (int64_t row = blockIdx.x; row < (int64_t)(g.X + 1) * g.NB; row += gridDim.x) {
+// Positions are batch-wide lattice indices; epos is indexed by axis-edge
+// scan rank, ef_off by edge id.
+__global__ void vd_positions_kernel(const uint8_t* __restrict__ occ, const int32_t* __restrict__ lab, VolTab T,
+                                    Bases B, const uint8_t* __restrict__ flags_all, Offs oall,
+                                    int64_t* __restrict__ vpos, int64_t* __restrict__ epos,
+                                    int64_t* __restrict__ fpos, int32_t* __restrict__ ve_off,
+                                    int32_t* __restrict__ ef_off) {
+    const int64_t nrows = T.total(kLRow);
+    for (int64_t grow = blockIdx.x; grow < nrows; grow += gridDim.x) {
+        const int bv = T.find(kLRow, grow);
+        const Grid g = grid_of(T, bv, occ, lab);
+        const int64_t lat0 = T.start(kLat, bv);
+        const uint8_t* flags = flags_all + lat0;
+        const Offs o = oall.at(lat0);
+        const int64_t fb = B.b[kBFace][bv];
+        const int64_t row = grow - T.start(kLRow, bv);
         const int a = (int)(row / g.NB), b = (int)(row - (int64_t)a * g.NB);
         for (int c = threadIdx.x; c < (int)g.NC; c += blockDim.x) {
             const int64_t p = row * g.NC + c;
             const uint32_t fl = flags[p];
             if (fl & 8u) {
                 const int32_t v = o.voff[p];
-                vpos[v] = p;
+                vpos[v] = lat0 + p;
                 ve_off[v] = o.veoff[p];
             }
             if (fl & 0x70u) {
-                int32_t e = o.eoff[p], efo = o.efoff[p];
+                int32_t e = o.eoff[p];
+                int64_t efo = o.efoff[p] + 2 * fb;
                 Inc inc[4];
 #pragma unroll
                 for (int d = 0; d < 3; ++d) {
                     if (!(fl & (16u << d))) continue;
-                    epos[e] = p * 4 + d;
-                    ef_off[e] = efo;
+                    epos[e] = (lat0 + p) * 4 + d;
+                    ef_off[e + fb] = (int32_t)efo;
                     efo += plaquette_faces(g, flags, a, b, c, d, inc);
                     ++e;
                 }
@@ -288,19 +346,29 @@ __global__ void vd_positions_kernel(Grid g, const uint8_t* __restrict__ flags, O
                 int32_t f = o.foff[p];
 #pragma unroll
                 for (int d = 0; d < 3; ++d)
-                    if (fl & (1u << d)) fpos[f++] = p * 4 + d;
+                    if (fl & (1u << d)) fpos[f++] = (lat0 + p) * 4 + d;
             }
         }
     }
 }
 
-__global__ void vd_vertices_kernel(Grid g, const uint8_t* __restrict__ flags, Offs o, const float* __restrict__ lam,
-                                   const int64_t* __restrict__ vpos, int32_t ne_axis, int32_t nv, float* __restrict__ vts,
-                                   float* __restrict__ vm, const int32_t* __restrict__ ve_off,
-                                   int32_t* __restrict__ ve_ids, VertRec* __restrict__ V, int32_t* __restrict__ bbox) {
+__global__ void vd_vertices_kernel(const uint8_t* __restrict__ occ, const int32_t* __restrict__ lab, VolTab T,
+                                   Bases B, const uint8_t* __restrict__ flags_all, Offs oall,
+                                   const float* __restrict__ lam_all, const int64_t* __restrict__ vpos, int32_t nv,
+                                   float* __restrict__ vts, float* __restrict__ vm, const int32_t* __restrict__ ve_off,
+                                   int32_t* __restrict__ ve_ids, VertRec* __restrict__ V) {
     for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += gridDim.x * blockDim.x) {
         {
-            const int64_t p = vpos[v];
+            const int64_t gp = vpos[v];
+            const int bv = T.find(kLat, gp);
+            const Grid g = grid_of(T, bv, occ, lab);
+            const int64_t lat0 = T.start(kLat, bv);
+            const uint8_t* flags = flags_all + lat0;
+            const float* lam = lam_all + 3 * lat0;
+            const Offs o = oall.at(lat0);
+            const Shift sh = shift_of(B, bv);
+            int32_t* bbox = B.bbox + 6 * bv;
+            const int64_t p = gp - lat0;
             int a, b, c;
             decode32(p, g.NB, g.NC, a, b, c);
             const uint32_t fl = flags[p];
@@ -333,11 +401,11 @@ __global__ void vd_vertices_kernel(Grid g, const uint8_t* __restrict__ flags, Of
                 int q[3] = {a, b, c};
                 q[d] -= 1;
                 const int64_t lq = g.lid(q[0], q[1], q[2]);
-                if (flags[lq] & (16u << d)) ve_ids[off + k++] = edge_id(flags, o, lq, d);
+                if (flags[lq] & (16u << d)) ve_ids[off + k++] = edge_id(flags, o, lq, d) + (int32_t)sh.fb;
             }
 #pragma unroll
             for (int d = 0; d < 3; ++d)
-                if (fl & (16u << d)) ve_ids[off + k++] = edge_id(flags, o, p, d);
+                if (fl & (16u << d)) ve_ids[off + k++] = edge_id(flags, o, p, d) + (int32_t)sh.fb;
             int32_t dg[6];
             int nd = 0;
 #pragma unroll
@@ -351,7 +419,7 @@ __global__ void vd_vertices_kernel(Grid g, const uint8_t* __restrict__ flags, Of
                 if (flags[l3] & (1u << d)) dg[nd++] = face_id(flags, o, l3, d);
             }
             sort_small<6>(dg, nd);
-            for (int i = 0; i < nd; ++i) ve_ids[off + k++] = ne_axis + dg[i];
+            for (int i = 0; i < nd; ++i) ve_ids[off + k++] = (int32_t)sh.eb1 + dg[i];
             VertRec r;
             r.ve_off = off;
             r.ve_cnt = k;
@@ -370,14 +438,31 @@ __global__ void vd_vertices_kernel(Grid g, const uint8_t* __restrict__ flags, Of
     }
 }
 
-__global__ void vd_edges_kernel(Grid g, const uint8_t* __restrict__ flags, Offs o, const float* __restrict__ lam,
+// Thinning filter folded into the records (batched runs): with `thr` set,
+// a record's measure becomes -1 when it is below its volume's threshold and
+// +1 otherwise, and the thinning then runs with threshold 0.
+__device__ __forceinline__ float rec_measure(float m, const float* thr, int bv) {
+    if (!thr) return m;
+    return m < thr[bv] ? -1.0f : 1.0f;
+}
+
+__global__ void vd_edges_kernel(const uint8_t* __restrict__ occ, const int32_t* __restrict__ lab, VolTab T, Bases B,
+                                const uint8_t* __restrict__ flags_all, Offs oall, const float* __restrict__ lam_all,
                                 const int64_t* __restrict__ epos, int32_t ne_axis, int2* __restrict__ edges,
                                 float* __restrict__ em, const int32_t* __restrict__ ef_off, int32_t* __restrict__ ef_ids,
-                                EdgeRec* __restrict__ E) {
-    for (int32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < ne_axis; e += gridDim.x * blockDim.x) {
-        const int64_t q = epos[e];
-        const int64_t p = q >> 2;
+                                EdgeRec* __restrict__ E, const float* __restrict__ thr) {
+    for (int32_t ea = blockIdx.x * blockDim.x + threadIdx.x; ea < ne_axis; ea += gridDim.x * blockDim.x) {
+        const int64_t q = epos[ea];
+        const int64_t gp = q >> 2;
         const int d = (int)(q & 3);
+        const int bv = T.find(kLat, gp);
+        const Grid g = grid_of(T, bv, occ, lab);
+        const int64_t lat0 = T.start(kLat, bv);
+        const uint8_t* flags = flags_all + lat0;
+        const float* lam = lam_all + 3 * lat0;
+        const Offs o = oall.at(lat0);
+        const int32_t e = ea + (int32_t)B.b[kBFace][bv];
+        const int64_t p = gp - lat0;
         int a, b, c;
         decode32(p, g.NB, g.NC, a, b, c);
         int nb[3] = {a, b, c};
@@ -399,7 +484,7 @@ __global__ void vd_edges_kernel(Grid g, const uint8_t* __restrict__ flags, Offs 
         EdgeRec r;
         r.v0 = v0;
         r.v1 = v1;
-        r.em = m;
+        r.em = rec_measure(m, thr, bv);
         r.ef_off = efo;
         r.ef_cnt = k;
         r.rm = kAlive;
@@ -409,17 +494,28 @@ __global__ void vd_edges_kernel(Grid g, const uint8_t* __restrict__ flags, Offs 
     }
 }
 
-__global__ void vd_faces_kernel(Grid g, const uint8_t* __restrict__ flags, Offs o, const float* __restrict__ lam,
-                                const int64_t* __restrict__ fpos, int32_t nface, int32_t ne_axis, int32_t ef_axis,
-                                int2* __restrict__ edges, float* __restrict__ em, int32_t* __restrict__ ef_off,
-                                int32_t* __restrict__ ef_ids, int32_t* __restrict__ tris,
-                                int32_t* __restrict__ tri_edges, float* __restrict__ fm,
+// tri_face and face_sites are per volume: the face's index within its
+// volume and the volume's own site indices.
+__global__ void vd_faces_kernel(const uint8_t* __restrict__ occ, const int32_t* __restrict__ lab, VolTab T, Bases B,
+                                const uint8_t* __restrict__ flags_all, Offs oall, const float* __restrict__ lam_all,
+                                const int64_t* __restrict__ fpos, int32_t nface, int2* __restrict__ edges,
+                                float* __restrict__ em, int32_t* __restrict__ ef_off, int32_t* __restrict__ ef_ids,
+                                int32_t* __restrict__ tris, int32_t* __restrict__ tri_edges, float* __restrict__ fm,
                                 int32_t* __restrict__ tri_face, int2* __restrict__ face_sites,
-                                FaceRec* __restrict__ F, EdgeRec* __restrict__ E) {
+                                FaceRec* __restrict__ F, EdgeRec* __restrict__ E, const float* __restrict__ thr) {
     for (int32_t f = blockIdx.x * blockDim.x + threadIdx.x; f < nface; f += gridDim.x * blockDim.x) {
         const int64_t qq = fpos[f];
-        const int64_t p = qq >> 2;
+        const int64_t gp = qq >> 2;
         const int d = (int)(qq & 3);
+        const int bv = T.find(kLat, gp);
+        const Grid g = grid_of(T, bv, occ, lab);
+        const int64_t lat0 = T.start(kLat, bv);
+        const uint8_t* flags = flags_all + lat0;
+        const float* lam = lam_all + 3 * lat0;
+        const Offs o = oall.at(lat0);
+        const Shift sh = shift_of(B, bv);
+        const int32_t fbs = (int32_t)sh.fb;
+        const int64_t p = gp - lat0;
         int a, b, c;
         decode32(p, g.NB, g.NC, a, b, c);
         {
@@ -438,11 +534,11 @@ __global__ void vd_faces_kernel(Grid g, const uint8_t* __restrict__ flags, Offs 
                     ql[m] = g.lid(i, j, k);
                     q[m] = o.voff[ql[m]];
                 }
-                const int32_t diag = ne_axis + f;
-                const int32_t e01 = edge_id(flags, o, ql[0], u);
-                const int32_t e12 = edge_id(flags, o, ql[1], w);
-                const int32_t e32 = edge_id(flags, o, ql[3], u);
-                const int32_t e03 = edge_id(flags, o, ql[0], w);
+                const int32_t diag = (int32_t)sh.eb1 + f;
+                const int32_t e01 = edge_id(flags, o, ql[0], u) + fbs;
+                const int32_t e12 = edge_id(flags, o, ql[1], w) + fbs;
+                const int32_t e32 = edge_id(flags, o, ql[3], u) + fbs;
+                const int32_t e03 = edge_id(flags, o, ql[0], w) + fbs;
                 const int64_t t0 = 2 * (int64_t)f, t1 = t0 + 1;
                 tris[3 * t0 + 0] = q[3];
                 tris[3 * t0 + 1] = q[0];
@@ -459,11 +555,12 @@ __global__ void vd_faces_kernel(Grid g, const uint8_t* __restrict__ flags, Offs 
                 tri_edges[3 * t1 + 2] = e32;
                 fm[t0] = lm;
                 fm[t1] = lm;
-                tri_face[t0] = f;
-                tri_face[t1] = f;
-                face_sites[f] = make_int2(s0, s1);
+                tri_face[t0] = f - fbs;
+                tri_face[t1] = f - fbs;
+                face_sites[f] = make_int2(s0 - (int32_t)sh.site, s1 - (int32_t)sh.site);
+                const float lr = rec_measure(lm, thr, bv);
                 FaceRec fr;
-                fr.fm = lm;
+                fr.fm = lr;
                 fr.rm = kAlive;
                 fr.pad0 = fr.pad1 = fr.pad2 = 0;
                 fr.e0 = e03;
@@ -476,7 +573,7 @@ __global__ void vd_faces_kernel(Grid g, const uint8_t* __restrict__ flags, Offs 
                 F[t1] = fr;
                 // the diagonal: new edge of this face, incident to both triangles
                 const int32_t dv0 = min(q[1], q[3]), dv1 = max(q[1], q[3]);
-                const int32_t efo = ef_axis + 2 * f;
+                const int32_t efo = (int32_t)sh.efb1 + 2 * f;
                 edges[diag] = make_int2(dv0, dv1);
                 em[diag] = lm;
                 ef_off[diag] = efo;
@@ -485,7 +582,7 @@ __global__ void vd_faces_kernel(Grid g, const uint8_t* __restrict__ flags, Offs 
                 EdgeRec er;
                 er.v0 = dv0;
                 er.v1 = dv1;
-                er.em = lm;
+                er.em = lr;
                 er.ef_off = efo;
                 er.ef_cnt = 2;
                 er.rm = kAlive;
@@ -497,17 +594,35 @@ __global__ void vd_faces_kernel(Grid g, const uint8_t* __restrict__ flags, Offs 
     }
 }
 
-__global__ void vd_tail_kernel(int32_t* bbox, int32_t* ve_off, int32_t nv, int32_t nve, int32_t* ef_off, int32_t ne,
-                               int32_t nef) {
+__global__ void vd_tail_kernel(int32_t* ve_off, int32_t nv, int32_t nve, int32_t* ef_off, int32_t ne, int32_t nef) {
     if (threadIdx.x == 0) {
         ve_off[nv] = nve;
         ef_off[ne] = nef;
     }
 }
 
-__global__ void init_bbox_kernel(int32_t* bbox) {
-    if (threadIdx.x < 3) bbox[threadIdx.x] = INT32_MAX;
-    else if (threadIdx.x < 6) bbox[threadIdx.x] = INT32_MIN;
+__global__ void init_bbox_kernel(int32_t* bbox, int nvol) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 6 * nvol; i += gridDim.x * blockDim.x)
+        bbox[i] = (i % 6) < 3 ? INT32_MAX : INT32_MIN;
+}
+
+// Inside-part size of every volume, VoroInfo::getInsidePartSize
+// (voroinfo.cpp:496): trimesh::box::size().max() of the float vertex
+// coordinates (0 without vertices); with t >= 0 also the thinning threshold
+// float(size * t) of exportInsideVoroMesh (highlevelalgo.cpp:836), the float
+// times double product rounded to float.
+__global__ void inside_size_kernel(Bases B, int nvol, double t) {
+    for (int bv = blockIdx.x * blockDim.x + threadIdx.x; bv < nvol; bv += gridDim.x * blockDim.x) {
+        const int32_t* bb = B.bbox + 6 * bv;
+        float isz = 0.0f;
+        if (B.b[kBVert][bv + 1] > B.b[kBVert][bv]) {
+            const float sx = (float)bb[3] - (float)bb[0], sy = (float)bb[4] - (float)bb[1],
+                        sz = (float)bb[5] - (float)bb[2];
+            isz = fmaxf(sx, fmaxf(sy, sz));
+        }
+        B.inside[bv] = isz;
+        if (t >= 0.0) B.thr[bv] = (float)__dmul_rn((double)isz, t);
+    }
 }
 
 inline int cell_grid(vc_ctx* c, int64_t n) {
@@ -524,11 +639,15 @@ inline int cell_grid(vc_ctx* c, int64_t n) {
 // axes 2..0.  The first site of face (p, d) is the label of p.  The distance
 // is accumulated in float in trimesh's order and rounded by one correctly
 // rounded square root (exact for boxes up to 2^11 per side).
-__global__ void vd_radius_kernel(Grid g, const float* __restrict__ sxyz, const int64_t* __restrict__ vpos, int32_t nv,
+__global__ void vd_radius_kernel(const uint8_t* __restrict__ occ, const int32_t* __restrict__ lab, VolTab T,
+                                 const float* __restrict__ sxyz, const int64_t* __restrict__ vpos, int32_t nv,
                                  float* __restrict__ radius) {
     for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += gridDim.x * blockDim.x) {
+        const int64_t gp = vpos[v];
+        const int bv = T.find(kLat, gp);
+        const Grid g = grid_of(T, bv, occ, lab);
         int a, b, c;
-        decode32(vpos[v], g.NB, g.NC, a, b, c);
+        decode32(gp - T.start(kLat, bv), g.NB, g.NC, a, b, c);
         int32_t L[8];
 #pragma unroll
         for (int q = 0; q < 8; ++q) L[q] = g.label(a + ((q >> 2) & 1), b + ((q >> 1) & 1), c + (q & 1));
@@ -563,11 +682,16 @@ inline int row_grid(vc_ctx* c, int64_t rows) {
 
 }  // namespace
 
-int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes) {
+// t_thr >= 0: also compute every volume's thinning threshold float(size *
+// t_thr) and fold it into the thinning records (see rec_measure).
+int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes, double t_thr) {
     if (!c->ft_valid) return VC_ERR_STATE;
-    const int64_t NB = c->Y + 1, NC = c->Z + 1;
-    const int64_t N = (int64_t)(c->X + 1) * NB * NC;
-    if (N >= ((int64_t)1 << 32)) return VC_ERR_ARG;
+    const int nvol = c->nvol;
+    for (int b = 0; b < nvol; ++b)
+        if (space_size(kLat, c->h_dims[3 * b], c->h_dims[3 * b + 1], c->h_dims[3 * b + 2]) >= ((int64_t)1 << 32))
+            return VC_ERR_ARG;
+    const int64_t N = c->h_off[kLat][nvol];
+    const int64_t nrows = c->h_off[kLRow][nvol];
     Region stage(c, "stage_vd");
     VC_TRY(ensure_n<uint8_t>(c, c->vd_flags, N));
     VC_TRY(ensure_n<float>(c, c->vd_lam, 3 * N));
@@ -577,8 +701,8 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes) {
     VC_TRY(ensure_n<int32_t>(c, c->vd_efoff, N));
     VC_TRY(ensure_n<int32_t>(c, c->vd_veoff, N));
     VC_TRY(ensure_n<int64_t>(c, c->scratch2, 8));
-    VC_TRY(ensure_n<int32_t>(c, c->vd_bbox, 8));
-    Grid g{ptr<uint8_t>(c->occ), ptr<int32_t>(c->ft_id), c->X, c->Y, c->Z, NB, NC};
+    const uint8_t* occ = ptr<uint8_t>(c->occ);
+    const int32_t* lab = ptr<int32_t>(c->ft_id);
     uint8_t* flags = ptr<uint8_t>(c->vd_flags);
     float* lam = ptr<float>(c->vd_lam);
     int32_t* cnt[5] = {ptr<int32_t>(c->vd_voff), ptr<int32_t>(c->vd_eoff), ptr<int32_t>(c->vd_foff),
@@ -586,17 +710,21 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes) {
     const float* sxyz = ptr<float>(c->site_xyz);
     {
         Region r(c, "vd_flags");
-        vd_flags_kernel<<<row_grid(c, (int64_t)(c->X + 1) * NB), 128, 0, c->stream>>>(g, sxyz, flags, lam, N);
+        vd_flags_kernel<<<row_grid(c, nrows), 128, 0, c->stream>>>(occ, lab, c->tab, sxyz, flags, lam);
         launched(c);
-        vd_counts_kernel<<<row_grid(c, (int64_t)(c->X + 1) * NB), 128, 0, c->stream>>>(g, flags, cnt[0], cnt[1], cnt[2], cnt[3],
-                                                                      cnt[4], N);
+        vd_counts_kernel<<<row_grid(c, nrows), 128, 0, c->stream>>>(occ, lab, c->tab, flags, cnt[0], cnt[1], cnt[2],
+                                                                     cnt[3], cnt[4]);
         launched(c);
         VC_CUDA(c, cudaGetLastError());
     }
     int64_t* tot = ptr<int64_t>(c->scratch2);
     {
         Region r(c, "vd_scan");
-        for (int k = 0; k < 5; ++k) VC_TRY(scan_exclusive_i32(c, cnt[k], cnt[k], N, tot + k));
+        const int base_of[5] = {kBVert, kBAxis, kBFace, kBEfAxis, kBVe};
+        for (int k = 0; k < 5; ++k) {
+            VC_TRY(scan_exclusive_i32(c, cnt[k], cnt[k], N, tot + k));
+            VC_TRY(fill_bases(c, base_of[k], kLat, cnt[k], tot + k));
+        }
     }
     int64_t h[5];
     VC_CUDA(c, cudaMemcpyAsync(h, tot, 5 * sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
@@ -630,55 +758,53 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes) {
     VC_TRY(ensure_n<int64_t>(c, c->vd_vpos, nv));
     VC_TRY(ensure_n<int64_t>(c, c->vd_epos, ne_axis));
     VC_TRY(ensure_n<int64_t>(c, c->vd_fpos, nface));
-    int32_t* bbox = ptr<int32_t>(c->vd_bbox);
-    init_bbox_kernel<<<1, 32, 0, c->stream>>>(bbox);
+    init_bbox_kernel<<<(6 * nvol + 255) / 256, 256, 0, c->stream>>>(c->bases.bbox, nvol);
     launched(c);
     Offs o{cnt[0], cnt[1], cnt[2], cnt[3], cnt[4]};
+    const float* thr = t_thr >= 0.0 ? c->bases.thr : nullptr;
     {
         Region r(c, "vd_emit");
-        vd_positions_kernel<<<row_grid(c, (int64_t)(c->X + 1) * NB), 128, 0, c->stream>>>(
-            g, flags, o, ptr<int64_t>(c->vd_vpos), ptr<int64_t>(c->vd_epos), ptr<int64_t>(c->vd_fpos),
-            ptr<int32_t>(c->ve_off), ptr<int32_t>(c->ef_off));
+        vd_positions_kernel<<<row_grid(c, nrows), 128, 0, c->stream>>>(
+            occ, lab, c->tab, c->bases, flags, o, ptr<int64_t>(c->vd_vpos), ptr<int64_t>(c->vd_epos),
+            ptr<int64_t>(c->vd_fpos), ptr<int32_t>(c->ve_off), ptr<int32_t>(c->ef_off));
         launched(c);
         vd_vertices_kernel<<<cell_grid(c, nv), 256, 0, c->stream>>>(
-            g, flags, o, lam, ptr<int64_t>(c->vd_vpos), (int32_t)ne_axis, (int32_t)nv, ptr<float>(c->vts),
-            ptr<float>(c->vm), ptr<int32_t>(c->ve_off), ptr<int32_t>(c->ve_ids), ptr<VertRec>(c->vert_rec), bbox);
+            occ, lab, c->tab, c->bases, flags, o, lam, ptr<int64_t>(c->vd_vpos), (int32_t)nv, ptr<float>(c->vts),
+            ptr<float>(c->vm), ptr<int32_t>(c->ve_off), ptr<int32_t>(c->ve_ids), ptr<VertRec>(c->vert_rec));
+        launched(c);
+        inside_size_kernel<<<(nvol + 255) / 256, 256, 0, c->stream>>>(c->bases, nvol, t_thr);
         launched(c);
         vd_edges_kernel<<<cell_grid(c, ne_axis), 256, 0, c->stream>>>(
-            g, flags, o, lam, ptr<int64_t>(c->vd_epos), (int32_t)ne_axis, ptr<int2>(c->edges), ptr<float>(c->em),
-            ptr<int32_t>(c->ef_off), ptr<int32_t>(c->ef_ids), ptr<EdgeRec>(c->edge_rec));
+            occ, lab, c->tab, c->bases, flags, o, lam, ptr<int64_t>(c->vd_epos), (int32_t)ne_axis, ptr<int2>(c->edges),
+            ptr<float>(c->em), ptr<int32_t>(c->ef_off), ptr<int32_t>(c->ef_ids), ptr<EdgeRec>(c->edge_rec), thr);
         launched(c);
         vd_faces_kernel<<<cell_grid(c, nface), 256, 0, c->stream>>>(
-            g, flags, o, lam, ptr<int64_t>(c->vd_fpos), (int32_t)nface, (int32_t)ne_axis, (int32_t)nef_axis,
-            ptr<int2>(c->edges), ptr<float>(c->em), ptr<int32_t>(c->ef_off), ptr<int32_t>(c->ef_ids),
-            ptr<int32_t>(c->tris), ptr<int32_t>(c->tri_edges), ptr<float>(c->fm), ptr<int32_t>(c->vd_tri_face),
-            ptr<int2>(c->vd_face_sites), ptr<FaceRec>(c->face_rec), ptr<EdgeRec>(c->edge_rec));
+            occ, lab, c->tab, c->bases, flags, o, lam, ptr<int64_t>(c->vd_fpos), (int32_t)nface, ptr<int2>(c->edges),
+            ptr<float>(c->em), ptr<int32_t>(c->ef_off), ptr<int32_t>(c->ef_ids), ptr<int32_t>(c->tris),
+            ptr<int32_t>(c->tri_edges), ptr<float>(c->fm), ptr<int32_t>(c->vd_tri_face), ptr<int2>(c->vd_face_sites),
+            ptr<FaceRec>(c->face_rec), ptr<EdgeRec>(c->edge_rec), thr);
         launched(c);
-        vd_tail_kernel<<<1, 32, 0, c->stream>>>(bbox, ptr<int32_t>(c->ve_off), (int32_t)nv, (int32_t)nve,
+        vd_tail_kernel<<<1, 32, 0, c->stream>>>(ptr<int32_t>(c->ve_off), (int32_t)nv, (int32_t)nve,
                                                 ptr<int32_t>(c->ef_off), (int32_t)ne, (int32_t)(3 * nt));
         launched(c);
         VC_CUDA(c, cudaGetLastError());
     }
-    int32_t hb[6];
-    VC_CUDA(c, cudaMemcpyAsync(hb, bbox, 6 * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
+    c->vol_inside.resize((size_t)nvol);
+    VC_CUDA(c, cudaMemcpyAsync(c->vol_inside.data(), c->bases.inside, (size_t)nvol * sizeof(float),
+                               cudaMemcpyDeviceToHost, c->stream));
     VC_TRY(sync_check(c));
-    float isz = 0.0f;
-    if (nv > 0) {
-        // trimesh::box::size().max() over float vertex coordinates
-        const float sx = (float)hb[3] - (float)hb[0], sy = (float)hb[4] - (float)hb[1],
-                    sz = (float)hb[5] - (float)hb[2];
-        isz = std::max(sx, std::max(sy, sz));
-    }
     c->nv = nv;
     c->ne_in = ne;
     c->ne = ne;
     c->nt = nt;
-    c->vd = vc_vd_sizes{nv, ne, nt, nface, isz};
+    c->vd = vc_vd_sizes{nv, ne, nt, nface, c->vol_inside[0]};
     c->vd_valid = true;
     c->cc_valid = true;
     c->cc_finalized = true;
     c->meas_valid = true;
     c->records_fresh = true;
+    c->records_thr_folded = t_thr >= 0.0;
+    c->cc_batched = nvol > 1;
     if (sizes) *sizes = c->vd;
     return VC_OK;
 }
@@ -688,9 +814,9 @@ int run_vertex_radii(vc_ctx* c) {
     const int64_t nv = c->vd.nv;
     VC_TRY(ensure_n<float>(c, c->vd_radius, nv));
     if (nv == 0) return VC_OK;
-    Grid g{ptr<uint8_t>(c->occ), ptr<int32_t>(c->ft_id), c->X, c->Y, c->Z, (int64_t)c->Y + 1, (int64_t)c->Z + 1};
     Region r(c, "vd_radius");
-    vd_radius_kernel<<<cell_grid(c, nv), 256, 0, c->stream>>>(g, ptr<float>(c->site_xyz), ptr<int64_t>(c->vd_vpos),
+    vd_radius_kernel<<<cell_grid(c, nv), 256, 0, c->stream>>>(ptr<uint8_t>(c->occ), ptr<int32_t>(c->ft_id), c->tab,
+                                                              ptr<float>(c->site_xyz), ptr<int64_t>(c->vd_vpos),
                                                               (int32_t)nv, ptr<float>(c->vd_radius));
     launched(c);
     VC_CUDA(c, cudaGetLastError());
