@@ -341,6 +341,9 @@ def run_gpu(args):
         "fp64_rescues": 0,
         "lambda_note": "lambda = sqrt of an exact integer squared distance (< 2^24) in IEEE f32: no FP64 rescue needed",
     }
+    if not args.no_batch:
+        line["batched"] = run_batched(ctx, dev, args, stream)
+        line["config"]["batched_workload"] = line["batched"]["workload"]
     if rank == 0 and not args.no_cpu_baseline:
         occ_s, sample = cpu_sample()
         times = [cpu_path_once(occ_s, args.t) for _ in range(2)]
@@ -352,6 +355,94 @@ def run_gpu(args):
     if dist is not None:
         dist.destroy_process_group()
     return 0
+
+
+# ---------------------------------------------------------------------------
+# Batched path: 256 random CSG volumes of per-axis sizes log-uniform in
+# [32, 192] through one vc_batch_run per step, against the plain path looping
+# over the same volumes one vc_run_plain at a time.
+
+BATCH_N, BATCH_LO, BATCH_HI = 256, 32, 192
+
+
+def run_batched(ctx, dev, args, stream):
+    import torch
+
+    from voxel_ma_gb300 import volumes
+    vols = [volumes.csg(1000 + i, BATCH_LO, BATCH_HI, device=dev) for i in range(BATCH_N)]
+    dims = np.array([tuple(v.shape) for v in vols], np.int32)
+    sizes = [int(np.prod(d)) for d in dims]
+    offs = np.concatenate([[0], np.cumsum(sizes)])
+    occ_dev = torch.cat([v.reshape(-1) for v in vols])
+    del vols
+    occ_host = occ_dev.cpu().pin_memory()
+    nvox = int(offs[-1])
+    views = [occ_dev[offs[i]:offs[i + 1]].view(*(int(x) for x in dims[i])) for i in range(BATCH_N)]
+
+    def batched():
+        ctx.batch_set_volumes(occ=occ_dev, dims=dims)
+        return ctx.batch_run(args.t, euler=False)
+
+    def loop():
+        return [ctx.run_plain(v, args.t)["rem"] for v in views]
+
+    def timed(fn, steps):
+        evs = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+        evs[0].record(stream)
+        out = None
+        for k in range(steps):
+            out = fn()
+            evs[k + 1].record(stream)
+        torch.cuda.synchronize(dev)
+        ctx.sync()
+        return out, [evs[k].elapsed_time(evs[k + 1]) for k in range(steps)]
+
+    for _ in range(args.warmup):
+        res = batched()
+    launches0 = ctx.launch_count()
+    res, b_ms = timed(batched, args.steps)
+    b_launches = (ctx.launch_count() - launches0) / args.steps
+    for _ in range(max(1, args.warmup // 2)):
+        loop()
+    launches0 = ctx.launch_count()
+    rem_loop, l_ms = timed(loop, max(1, args.steps // 2))
+    l_launches = (ctx.launch_count() - launches0) / max(1, args.steps // 2)
+    same = sum(1 for r, q in zip(res, rem_loop) if r["rem"] == q)
+
+    # end to end: host volumes in, remaining complexes out, every step
+    tot = {k: sum(r["rem"][k] for r in res) for k in ("nv", "ne", "nt")}
+    h_v = torch.empty((max(tot["nv"], 1), 3), dtype=torch.float32).pin_memory()
+    h_e = torch.empty((max(tot["ne"], 1), 2), dtype=torch.int32).pin_memory()
+    h_t = torch.empty((max(tot["nt"], 1), 3), dtype=torch.int32).pin_memory()
+
+    def e2e():
+        ctx.batch_set_volumes(occ=occ_host, dims=dims)
+        out = ctx.batch_run(args.t, euler=False)
+        s = ctx.rem_sizes
+        ctx.remaining_arrays_into(h_v[: s["nv"]], h_e[: s["ne"]], h_t[: s["nt"]])
+        return out
+
+    e2e()
+    _, e_ms = timed(e2e, args.steps)
+    s = ctx.rem_sizes
+    b_mean, l_mean, e_mean = statistics.mean(b_ms), statistics.mean(l_ms), statistics.mean(e_ms)
+    return {
+        "workload": f"csg{BATCH_N}_loguniform_{BATCH_LO}_{BATCH_HI}",
+        "volumes": BATCH_N, "voxels": nvox,
+        "value": nvox / (b_mean / 1e3), "unit": UNIT,
+        "volumes_per_s": BATCH_N / (b_mean / 1e3),
+        "ms_per_batch": b_mean,
+        "latency_ms": {"p50": float(np.percentile(b_ms, 50)), "p99": float(np.percentile(b_ms, 99))},
+        "plain_loop": {"value": nvox / (l_mean / 1e3), "volumes_per_s": BATCH_N / (l_mean / 1e3),
+                       "ms_per_pass": l_mean, "gpu_launches_per_pass": l_launches},
+        "speedup_vs_plain_loop": l_mean / b_mean,
+        "gpu_launches_per_batch": b_launches,
+        "e2e": {"value": nvox / (e_mean / 1e3), "unit": UNIT, "h2d_bytes_per_step": nvox,
+                "d2h_bytes_per_step": s["nv"] * 12 + s["ne"] * 8 + s["nt"] * 12, "ms_per_step": e_mean},
+        "parity": f"{same}/{BATCH_N} volumes: batched remaining-complex sizes equal the plain path's",
+        "thin_generations": ctx.batch_stats["generations"],
+        "cells": {"V": ctx.vd_sizes["nv"], "E": ctx.vd_sizes["ne"], "T": ctx.vd_sizes["nt"]},
+    }
 
 
 # DRAM traffic per cell of the complex (V + E + T) of the thinning kernel,
@@ -371,6 +462,7 @@ def main():
     ap.add_argument("--workload", default="grf512")
     ap.add_argument("--t", type=float, default=0.04)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-path measurement")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -428,12 +428,21 @@ __global__ void vd_vertices_kernel(const uint8_t* __restrict__ occ, const int32_
             r.trig = -1;
             r.pad0 = r.pad1 = r.pad2 = 0;
             V[v] = r;
-            atomicMin(&bbox[0], a);
-            atomicMin(&bbox[1], b);
-            atomicMin(&bbox[2], c);
-            atomicMax(&bbox[3], a);
-            atomicMax(&bbox[4], b);
-            atomicMax(&bbox[5], c);
+            // the volume's bounding box: lanes of the same volume reduce in
+            // the warp first, so each warp issues one set of atomics per volume
+            const unsigned grp = __match_any_sync(__activemask(), bv);
+            const int mn0 = __reduce_min_sync(grp, a), mn1 = __reduce_min_sync(grp, b),
+                      mn2 = __reduce_min_sync(grp, c);
+            const int mx0 = __reduce_max_sync(grp, a), mx1 = __reduce_max_sync(grp, b),
+                      mx2 = __reduce_max_sync(grp, c);
+            if ((int)(threadIdx.x & 31) == __ffs(grp) - 1) {
+                atomicMin(&bbox[0], mn0);
+                atomicMin(&bbox[1], mn1);
+                atomicMin(&bbox[2], mn2);
+                atomicMax(&bbox[3], mx0);
+                atomicMax(&bbox[4], mx1);
+                atomicMax(&bbox[5], mx2);
+            }
         }
     }
 }
@@ -764,26 +773,39 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes, double t_thr) {
     const float* thr = t_thr >= 0.0 ? c->bases.thr : nullptr;
     {
         Region r(c, "vd_emit");
-        vd_positions_kernel<<<row_grid(c, nrows), 128, 0, c->stream>>>(
-            occ, lab, c->tab, c->bases, flags, o, ptr<int64_t>(c->vd_vpos), ptr<int64_t>(c->vd_epos),
-            ptr<int64_t>(c->vd_fpos), ptr<int32_t>(c->ve_off), ptr<int32_t>(c->ef_off));
-        launched(c);
-        vd_vertices_kernel<<<cell_grid(c, nv), 256, 0, c->stream>>>(
-            occ, lab, c->tab, c->bases, flags, o, lam, ptr<int64_t>(c->vd_vpos), (int32_t)nv, ptr<float>(c->vts),
-            ptr<float>(c->vm), ptr<int32_t>(c->ve_off), ptr<int32_t>(c->ve_ids), ptr<VertRec>(c->vert_rec));
-        launched(c);
-        inside_size_kernel<<<(nvol + 255) / 256, 256, 0, c->stream>>>(c->bases, nvol, t_thr);
-        launched(c);
-        vd_edges_kernel<<<cell_grid(c, ne_axis), 256, 0, c->stream>>>(
-            occ, lab, c->tab, c->bases, flags, o, lam, ptr<int64_t>(c->vd_epos), (int32_t)ne_axis, ptr<int2>(c->edges),
-            ptr<float>(c->em), ptr<int32_t>(c->ef_off), ptr<int32_t>(c->ef_ids), ptr<EdgeRec>(c->edge_rec), thr);
-        launched(c);
-        vd_faces_kernel<<<cell_grid(c, nface), 256, 0, c->stream>>>(
-            occ, lab, c->tab, c->bases, flags, o, lam, ptr<int64_t>(c->vd_fpos), (int32_t)nface, ptr<int2>(c->edges),
-            ptr<float>(c->em), ptr<int32_t>(c->ef_off), ptr<int32_t>(c->ef_ids), ptr<int32_t>(c->tris),
-            ptr<int32_t>(c->tri_edges), ptr<float>(c->fm), ptr<int32_t>(c->vd_tri_face), ptr<int2>(c->vd_face_sites),
-            ptr<FaceRec>(c->face_rec), ptr<EdgeRec>(c->edge_rec), thr);
-        launched(c);
+        {
+            Region k(c, "vd_positions");
+            vd_positions_kernel<<<row_grid(c, nrows), 128, 0, c->stream>>>(
+                occ, lab, c->tab, c->bases, flags, o, ptr<int64_t>(c->vd_vpos), ptr<int64_t>(c->vd_epos),
+                ptr<int64_t>(c->vd_fpos), ptr<int32_t>(c->ve_off), ptr<int32_t>(c->ef_off));
+            launched(c);
+        }
+        {
+            Region k(c, "vd_vertices");
+            vd_vertices_kernel<<<cell_grid(c, nv), 256, 0, c->stream>>>(
+                occ, lab, c->tab, c->bases, flags, o, lam, ptr<int64_t>(c->vd_vpos), (int32_t)nv, ptr<float>(c->vts),
+                ptr<float>(c->vm), ptr<int32_t>(c->ve_off), ptr<int32_t>(c->ve_ids), ptr<VertRec>(c->vert_rec));
+            launched(c);
+            inside_size_kernel<<<(nvol + 255) / 256, 256, 0, c->stream>>>(c->bases, nvol, t_thr);
+            launched(c);
+        }
+        {
+            Region k(c, "vd_edges");
+            vd_edges_kernel<<<cell_grid(c, ne_axis), 256, 0, c->stream>>>(
+                occ, lab, c->tab, c->bases, flags, o, lam, ptr<int64_t>(c->vd_epos), (int32_t)ne_axis,
+                ptr<int2>(c->edges), ptr<float>(c->em), ptr<int32_t>(c->ef_off), ptr<int32_t>(c->ef_ids),
+                ptr<EdgeRec>(c->edge_rec), thr);
+            launched(c);
+        }
+        {
+            Region k(c, "vd_faces");
+            vd_faces_kernel<<<cell_grid(c, nface), 256, 0, c->stream>>>(
+                occ, lab, c->tab, c->bases, flags, o, lam, ptr<int64_t>(c->vd_fpos), (int32_t)nface,
+                ptr<int2>(c->edges), ptr<float>(c->em), ptr<int32_t>(c->ef_off), ptr<int32_t>(c->ef_ids),
+                ptr<int32_t>(c->tris), ptr<int32_t>(c->tri_edges), ptr<float>(c->fm), ptr<int32_t>(c->vd_tri_face),
+                ptr<int2>(c->vd_face_sites), ptr<FaceRec>(c->face_rec), ptr<EdgeRec>(c->edge_rec), thr);
+            launched(c);
+        }
         vd_tail_kernel<<<1, 32, 0, c->stream>>>(ptr<int32_t>(c->ve_off), (int32_t)nv, (int32_t)nve,
                                                 ptr<int32_t>(c->ef_off), (int32_t)ne, (int32_t)(3 * nt));
         launched(c);

@@ -123,36 +123,75 @@ def grf(n: int = 512, sigma: float = 6.0, seed: int = 0, device=None) -> np.ndar
     return (out > 0).astype(np.uint8)
 
 
-def csg(seed: int, lo: int = 32, hi: int = 192) -> np.ndarray:
-    """Random CSG of 1-8 primitives (spheres, boxes, capsules) in a box of log-uniform sizes."""
+def _csg_plan(seed: int, lo: int, hi: int):
+    """Dims and primitive list of one random CSG volume (numpy RNG, seeded)."""
     rng = np.random.default_rng(seed)
     dims = np.exp(rng.uniform(math.log(lo), math.log(hi), size=3)).astype(int)
     dims = np.clip(dims, lo, hi)
-    X, Y, Z = (int(d) for d in dims)
-    ax = [(np.arange(d) + 0.5) / d for d in (X, Y, Z)]
-    P = np.meshgrid(*ax, indexing="ij")
-    occ = np.zeros((X, Y, Z), bool)
+    prims = []
     nprim = int(rng.integers(1, 9))
     for p in range(nprim):
         kind = int(rng.integers(0, 3))
         c = rng.uniform(0.25, 0.75, size=3)
         if kind == 0:
-            rad = rng.uniform(0.08, 0.3)
-            m = (P[0] - c[0]) ** 2 + (P[1] - c[1]) ** 2 + (P[2] - c[2]) ** 2 <= rad * rad
+            prm = (rng.uniform(0.08, 0.3),)
         elif kind == 1:
-            h = rng.uniform(0.08, 0.3, size=3)
-            m = (np.abs(P[0] - c[0]) <= h[0]) & (np.abs(P[1] - c[1]) <= h[1]) & (np.abs(P[2] - c[2]) <= h[2])
+            prm = (rng.uniform(0.08, 0.3, size=3),)
         else:
             d = rng.normal(size=3)
             d /= np.linalg.norm(d)
             ln = rng.uniform(0.1, 0.4)
             rad = rng.uniform(0.05, 0.18)
+            prm = (d, ln, rad)
+        subtract = p > 0 and rng.uniform() < 0.25
+        prims.append((kind, c, prm, subtract))
+    return tuple(int(x) for x in dims), prims
+
+
+def csg(seed: int, lo: int = 32, hi: int = 192, device=None):
+    """Random CSG of 1-8 primitives (spheres, boxes, capsules) in a box of log-uniform sizes.
+
+    With ``device`` (a torch CUDA device) the volume is evaluated there and a
+    uint8 tensor is returned; the primitives are the same, but capsule
+    boundaries may round differently from the numpy evaluation."""
+    (X, Y, Z), prims = _csg_plan(seed, lo, hi)
+    if device is not None:
+        import torch
+        ax = [(torch.arange(d, device=device, dtype=torch.float64) + 0.5) / d for d in (X, Y, Z)]
+        P = torch.meshgrid(*ax, indexing="ij")
+        occ = torch.zeros((X, Y, Z), dtype=torch.bool, device=device)
+        for kind, c, prm, subtract in prims:
+            if kind == 0:
+                m = (P[0] - c[0]) ** 2 + (P[1] - c[1]) ** 2 + (P[2] - c[2]) ** 2 <= prm[0] * prm[0]
+            elif kind == 1:
+                h = prm[0]
+                m = (torch.abs(P[0] - c[0]) <= h[0]) & (torch.abs(P[1] - c[1]) <= h[1]) & \
+                    (torch.abs(P[2] - c[2]) <= h[2])
+            else:
+                d, ln, rad = prm
+                a = c - d * ln / 2
+                r0, r1, r2 = P[0] - a[0], P[1] - a[1], P[2] - a[2]
+                t = torch.clamp(r0 * d[0] + r1 * d[1] + r2 * d[2], 0.0, ln)
+                m = (r0 - t * d[0]) ** 2 + (r1 - t * d[1]) ** 2 + (r2 - t * d[2]) ** 2 <= rad * rad
+            occ = occ & ~m if subtract else occ | m
+        return occ.to(torch.uint8)
+    ax = [(np.arange(d) + 0.5) / d for d in (X, Y, Z)]
+    P = np.meshgrid(*ax, indexing="ij")
+    occ = np.zeros((X, Y, Z), bool)
+    for kind, c, prm, subtract in prims:
+        if kind == 0:
+            m = (P[0] - c[0]) ** 2 + (P[1] - c[1]) ** 2 + (P[2] - c[2]) ** 2 <= prm[0] * prm[0]
+        elif kind == 1:
+            h = prm[0]
+            m = (np.abs(P[0] - c[0]) <= h[0]) & (np.abs(P[1] - c[1]) <= h[1]) & (np.abs(P[2] - c[2]) <= h[2])
+        else:
+            d, ln, rad = prm
             a = c - d * ln / 2
             rel = np.stack([P[0] - a[0], P[1] - a[1], P[2] - a[2]], -1)
             t = np.clip(rel @ d, 0.0, ln)
             q = rel - t[..., None] * d
             m = (q ** 2).sum(-1) <= rad * rad
-        if p > 0 and rng.uniform() < 0.25:
+        if subtract:
             occ &= ~m
         else:
             occ |= m
