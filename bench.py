@@ -344,6 +344,10 @@ def run_gpu(args):
     if not args.no_batch:
         line["batched"] = run_batched(ctx, dev, args, stream)
         line["config"]["batched_workload"] = line["batched"]["workload"]
+    if not args.no_serve and world == 1:
+        ctx.close()
+        line["serving"] = run_serving(dev, args)
+        line["config"]["serving_workload"] = line["serving"]["workload"]
     if rank == 0 and not args.no_cpu_baseline:
         occ_s, sample = cpu_sample()
         times = [cpu_path_once(occ_s, args.t) for _ in range(2)]
@@ -445,6 +449,103 @@ def run_batched(ctx, dev, args, stream):
     }
 
 
+# ---------------------------------------------------------------------------
+# Request stream: Poisson arrivals at 200 req/s of volumes drawn from the
+# torus, spheres and GRF generators with edges log-uniform in [32, 384],
+# served by the continuous-batching request loop (vc_server_*) under a
+# 120 GB memory cap, against one plain context serving the same arrivals
+# first come first served (vc_run_plain per request).
+
+SERVE_RATE, SERVE_SECONDS, SERVE_POOL, SERVE_CAP = 200.0, 6.0, 18, 120 << 30
+
+
+def serve_pool(dev):
+    from voxel_ma_gb300 import volumes
+    rng = np.random.default_rng(2024)
+    pool = []
+    for i in range(SERVE_POOL):
+        n = int(np.clip(np.exp(rng.uniform(np.log(32), np.log(384))), 32, 384))
+        kind = i % 3
+        if kind == 0:
+            occ = volumes.torus_mesh(n)
+        elif kind == 1:
+            occ = volumes.spheres(n, count=32, seed=i)
+        else:
+            occ = volumes.grf(n, sigma=6.0, seed=i, device=dev)
+        pool.append(np.ascontiguousarray(occ))
+    return pool
+
+
+def run_serving(dev, args):
+    import threading
+
+    from voxel_ma_gb300 import api
+    pool = serve_pool(dev)
+    rng = np.random.default_rng(7)
+    gaps = rng.exponential(1.0 / SERVE_RATE, size=int(SERVE_RATE * SERVE_SECONDS * 1.5))
+    arrivals = np.cumsum(gaps)
+    arrivals = arrivals[arrivals < SERVE_SECONDS]
+    picks = rng.integers(0, len(pool), size=len(arrivals))
+    voxels = np.array([pool[k].size for k in picks], np.int64)
+
+    # continuous batching
+    srv = api.Server(dev.index or 0, workers=2, mem_cap_bytes=SERVE_CAP, max_batch=64)
+    warm = [srv.submit(pool[k], args.t) for k in range(len(pool))]
+    for i in warm:
+        srv.wait(i)
+        srv.release(i)
+    ids = []
+    t0 = time.perf_counter()
+    for a, k in zip(arrivals, picks):
+        d = t0 + a - time.perf_counter()
+        if d > 0:
+            time.sleep(d)
+        ids.append(srv.submit(pool[k], args.t))
+    res = [srv.wait(i) for i in ids]
+    t_end = time.perf_counter()
+    rem_srv = [r["rem"] for r in res]
+    for i in ids:
+        srv.release(i)
+    st = srv.stats()
+    srv.close()
+    lat = np.array([r["latency_ms"] for r in res])
+    span = t_end - t0
+
+    # the plain path: one context, first come first served, same arrivals
+    ctx = api.Context(dev.index or 0)
+    for k in range(len(pool)):
+        ctx.run_plain(pool[k], args.t)
+    plain_lat, rem_plain = [], []
+    t0 = time.perf_counter()
+    for a, k in zip(arrivals, picks):
+        d = t0 + a - time.perf_counter()
+        if d > 0:
+            time.sleep(d)
+        r = ctx.run_plain(pool[k], args.t)
+        ctx.remaining_arrays()
+        plain_lat.append((time.perf_counter() - (t0 + a)) * 1e3)
+        rem_plain.append(r["rem"])
+    p_span = time.perf_counter() - t0
+    ctx.close()
+    plain_lat = np.array(plain_lat)
+    same = sum(1 for a, b in zip(rem_srv, rem_plain) if a == b)
+    n = len(arrivals)
+    return {
+        "workload": f"poisson{int(SERVE_RATE)}_torus_spheres_grf_edge32_384",
+        "arrival_rate_req_s": SERVE_RATE, "requests": n, "duration_s": SERVE_SECONDS,
+        "pool": f"{SERVE_POOL} volumes (torus mesh, 32 spheres, GRF sigma 6), edge log-uniform in [32, 384]",
+        "mem_cap_bytes": SERVE_CAP, "workers": 2, "max_batch": 64,
+        "value": float(voxels.sum() / span), "unit": UNIT, "throughput_req_s": n / span,
+        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
+        "batches": st["batches"] - SERVE_POOL,  # the warm-up served each pool volume alone
+        "device_bytes_end": st["device_bytes"],
+        "plain": {"value": float(voxels.sum() / p_span), "throughput_req_s": n / p_span,
+                  "latency_ms": {"p50": float(np.percentile(plain_lat, 50)),
+                                 "p99": float(np.percentile(plain_lat, 99))}},
+        "parity": f"{same}/{n} requests: remaining-complex sizes equal the plain path's",
+    }
+
+
 # DRAM traffic per cell of the complex (V + E + T) of the thinning kernel,
 # from one ncu capture of the 192^3 case of this workload
 # (profiles/kernels_grf192.md: 8.655 GB read + 2.297 GB written for
@@ -463,6 +564,7 @@ def main():
     ap.add_argument("--t", type=float, default=0.04)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-path measurement")
+    ap.add_argument("--no-serve", action="store_true", help="skip the request-stream measurement")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -193,6 +193,55 @@ int vc_batch_set_volumes(vc_ctx* ctx, int nvol, const int32_t* dims, const uint8
  * the batch's thinning.                                                    */
 int vc_batch_run(vc_ctx* ctx, double t, int with_euler, vc_thin_stats* stats, vc_batch_volume* out);
 
+/* ---- request loop (continuous batching) ---------------------------------
+ * The reference serves one volume per process run (src/voroUtility.cpp
+ * main -> exportInsideVoroMesh, src/highlevelalgo.cpp:731-961).  A server
+ * queues volumes as they are submitted and `workers` threads, each with its
+ * own context and stream, serve them: a worker that becomes free takes the
+ * oldest pending requests that fit as one batch (vc_batch_run), so requests
+ * that arrive while other batches are on the GPU join the next batch, and
+ * the workers' batches overlap on the device.  Memory admission: a request's
+ * footprint is estimated as bytes_per_voxel (default 640) x voxels; a batch
+ * must fit mem_cap_bytes / workers, a request that cannot is refused at
+ * submission (VC_ERR_ARG), and a worker whose context holds more than its
+ * share after a batch frees its buffers.  Each result equals the plain
+ * single-volume result for that volume.  Submission copies the volume
+ * (host memory); results stay until vc_server_release.                     */
+typedef struct vc_server vc_server;
+typedef struct {
+    int status;        /* VC_OK, or the status of the batch the request ran in */
+    int batch_size;    /* requests in that batch */
+    int64_t n_sites;
+    vc_vd_sizes vd;
+    float thresh;
+    vc_rem_sizes rem;
+    vc_euler_info euler;
+    double queue_ms;   /* submission -> start of its batch */
+    double run_ms;     /* start of its batch -> results on the host */
+    double latency_ms; /* submission -> results on the host */
+} vc_request_result;
+typedef struct {
+    int64_t submitted, completed, failed, refused, batches, pending, device_bytes;
+} vc_server_stats;
+int vc_server_create(vc_server** server, int device, int workers, int64_t mem_cap_bytes, int max_batch);
+int vc_server_set_bytes_per_voxel(vc_server* server, double bytes_per_voxel);
+int vc_server_submit(vc_server* server, const uint8_t* occ, int X, int Y, int Z, double t, int64_t* request_id);
+/* Blocks until the request is served (timeout_s < 0: no limit; a host-side
+ * wait that returns VC_ERR_TIMEOUT when the limit passes).                 */
+int vc_server_wait(vc_server* server, int64_t request_id, double timeout_s, vc_request_result* out);
+/* The request's remaining complex (sizes in its vc_request_result.rem).    */
+int vc_server_get_remaining(vc_server* server, int64_t request_id, float* vts, int32_t* edges, int32_t* tris);
+int vc_server_release(vc_server* server, int64_t request_id);
+int vc_server_get_stats(vc_server* server, vc_server_stats* out);
+int vc_server_destroy(vc_server* server);
+/* The batching rule the workers apply, on a list of requests in arrival
+ * order: consecutive requests share a batch while they have the same t, the
+ * batch holds fewer than max_batch requests and bytes_per_voxel x voxels
+ * summed over it stays within share_bytes; batch_of[i] receives request i's
+ * batch number, or -1 when the request alone exceeds the share.  Host only. */
+int vc_plan_batches(int n, const int64_t* voxels, const double* t, int64_t share_bytes, double bytes_per_voxel,
+                    int max_batch, int32_t* batch_of);
+
 /* ---- site extraction without device allocation ---------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc
  * (a host framework or allocator that owns the device heap, or a plugin that

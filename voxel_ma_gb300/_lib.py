@@ -47,6 +47,17 @@ class BatchVolume(ctypes.Structure):
                 ("rem_v_off", c_i64), ("rem_e_off", c_i64), ("rem_t_off", c_i64)]
 
 
+class RequestResult(ctypes.Structure):
+    _fields_ = [("status", c_int), ("batch_size", c_int), ("n_sites", c_i64), ("vd", VdSizes), ("thresh", c_float),
+                ("rem", RemSizes), ("euler", EulerInfo), ("queue_ms", ctypes.c_double), ("run_ms", ctypes.c_double),
+                ("latency_ms", ctypes.c_double)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", c_i64), ("completed", c_i64), ("failed", c_i64), ("refused", c_i64),
+                ("batches", c_i64), ("pending", c_i64), ("device_bytes", c_i64)]
+
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "vc_version": (c_int, []),
@@ -72,6 +83,15 @@ SIGNATURES = {
     "vc_vertex_radii": (c_int, [c_vp, c_vp, c_int]),
     "vc_batch_set_volumes": (c_int, [c_vp, c_int, c_vp, c_vp, c_int]),
     "vc_batch_run": (c_int, [c_vp, ctypes.c_double, c_int, ctypes.POINTER(ThinStats), c_vp]),
+    "vc_server_create": (c_int, [ctypes.POINTER(c_vp), c_int, c_int, c_i64, c_int]),
+    "vc_server_set_bytes_per_voxel": (c_int, [c_vp, ctypes.c_double]),
+    "vc_server_submit": (c_int, [c_vp, c_vp, c_int, c_int, c_int, ctypes.c_double, ctypes.POINTER(c_i64)]),
+    "vc_server_wait": (c_int, [c_vp, c_i64, ctypes.c_double, ctypes.POINTER(RequestResult)]),
+    "vc_server_get_remaining": (c_int, [c_vp, c_i64, c_vp, c_vp, c_vp]),
+    "vc_server_release": (c_int, [c_vp, c_i64]),
+    "vc_server_get_stats": (c_int, [c_vp, ctypes.POINTER(ServerStats)]),
+    "vc_server_destroy": (c_int, [c_vp]),
+    "vc_plan_batches": (c_int, [c_int, c_vp, c_vp, c_i64, ctypes.c_double, c_int, c_vp]),
     "vc_set_complex": (c_int, [c_vp, c_i64, c_vp, c_i64, c_vp, c_i64, c_vp, c_int]),
     "vc_finalize": (c_int, [c_vp, ctypes.POINTER(c_i64)]),
     "vc_get_finalized": (c_int, [c_vp] + [c_vp] * 6 + [c_int]),

@@ -337,6 +337,87 @@ class Context:
         return out
 
 
+class Server:
+    """The request loop (vc_server_*): submit host volumes, wait for results."""
+
+    def __init__(self, device: int = 0, workers: int = 2, mem_cap_bytes: int = 120 << 30, max_batch: int = 64,
+                 bytes_per_voxel: Optional[float] = None):
+        self.lib = L.load()
+        h = ctypes.c_void_p()
+        st = self.lib.vc_server_create(ctypes.byref(h), device, workers, mem_cap_bytes, max_batch)
+        if st != L.VC_OK:
+            raise L.VoxelCoreError(st, "vc_server_create", "")
+        self.h = h
+        if bytes_per_voxel is not None:
+            self._check(self.lib.vc_server_set_bytes_per_voxel(self.h, float(bytes_per_voxel)),
+                        "vc_server_set_bytes_per_voxel")
+
+    def _check(self, st, where):
+        if st != L.VC_OK:
+            raise L.VoxelCoreError(st, where, "")
+
+    def submit(self, occ, t: float = 0.04) -> int:
+        occ = np.ascontiguousarray(occ, dtype=np.uint8)
+        X, Y, Z = (int(x) for x in occ.shape)
+        rid = ctypes.c_int64()
+        self._check(self.lib.vc_server_submit(self.h, occ.ctypes.data_as(ctypes.c_void_p), X, Y, Z,
+                                              ctypes.c_double(t), ctypes.byref(rid)), "vc_server_submit")
+        return int(rid.value)
+
+    def wait(self, rid: int, timeout_s: float = -1.0) -> dict:
+        r = L.RequestResult()
+        self._check(self.lib.vc_server_wait(self.h, rid, ctypes.c_double(timeout_s), ctypes.byref(r)),
+                    "vc_server_wait")
+        return dict(status=r.status, batch_size=r.batch_size, n_sites=r.n_sites, thresh=r.thresh,
+                    vd=dict(nv=r.vd.nv, ne=r.vd.ne, nt=r.vd.nt, nface=r.vd.nface, inside_size=r.vd.inside_size),
+                    rem=dict(nv=r.rem.nv, ne=r.rem.ne, nt=r.rem.nt),
+                    euler=dict(V=r.euler.V, E=r.euler.E, F=r.euler.F, C=r.euler.C, euler=r.euler.euler),
+                    queue_ms=r.queue_ms, run_ms=r.run_ms, latency_ms=r.latency_ms)
+
+    def remaining(self, rid: int, res: dict):
+        n = res["rem"]
+        v = np.empty((n["nv"], 3), np.float32)
+        e = np.empty((n["ne"], 2), np.int32)
+        t = np.empty((n["nt"], 3), np.int32)
+        self._check(self.lib.vc_server_get_remaining(self.h, rid, v.ctypes.data_as(ctypes.c_void_p),
+                                                     e.ctypes.data_as(ctypes.c_void_p),
+                                                     t.ctypes.data_as(ctypes.c_void_p)), "vc_server_get_remaining")
+        return v, e, t
+
+    def release(self, rid: int):
+        self._check(self.lib.vc_server_release(self.h, rid), "vc_server_release")
+
+    def stats(self) -> dict:
+        s = L.ServerStats()
+        self._check(self.lib.vc_server_get_stats(self.h, ctypes.byref(s)), "vc_server_get_stats")
+        return {k: getattr(s, k) for k, _ in L.ServerStats._fields_}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.vc_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def plan_batches(voxels, t, share_bytes: int, bytes_per_voxel: float = 640.0, max_batch: int = 64) -> np.ndarray:
+    """vc_plan_batches: the batch number each request (in arrival order) gets."""
+    lib = L.load()
+    v = np.ascontiguousarray(voxels, np.int64)
+    tt = np.ascontiguousarray(np.broadcast_to(np.asarray(t, np.float64), v.shape))
+    out = np.empty(len(v), np.int32)
+    st = lib.vc_plan_batches(len(v), v.ctypes.data_as(ctypes.c_void_p), tt.ctypes.data_as(ctypes.c_void_p),
+                             int(share_bytes), float(bytes_per_voxel), int(max_batch),
+                             out.ctypes.data_as(ctypes.c_void_p))
+    if st != L.VC_OK:
+        raise L.VoxelCoreError(st, "vc_plan_batches", "")
+    return out
+
+
 # ---------------------------------------------------------------------------
 # Reference-shaped surfaces
 

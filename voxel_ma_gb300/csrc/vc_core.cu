@@ -208,6 +208,43 @@ int scan_exclusive_i64(vc_ctx* c, const int64_t* in, int64_t* out, int64_t n, in
     return scan_impl<int64_t>(c, in, out, n, total_dev);
 }
 
+// Every device buffer of a context except its error word.
+std::vector<DevBuf*> ctx_buffers(vc_ctx* c) {
+    return {&c->scratch, &c->scratch2, &c->occ, &c->site_xyz, &c->site_count, &c->site_id_lat, &c->ft_d2,
+            &c->ft_id, &c->ft_tmp, &c->vd_flags, &c->vd_voff, &c->vd_eoff, &c->vd_foff, &c->vd_tri_face,
+            &c->vd_face_sites, &c->vd_vm, &c->vd_lam, &c->vd_efoff, &c->vd_veoff, &c->vd_vpos, &c->vd_epos,
+            &c->vd_fpos, &c->vd_radius, &c->tab_buf, &c->bases_buf, &c->vts, &c->edges_in, &c->edges, &c->tris,
+            &c->tri_edges, &c->ve_off, &c->ve_ids, &c->ef_off, &c->ef_ids, &c->hash_keys, &c->hash_pos,
+            &c->hash_id, &c->side_slot, &c->vm, &c->em, &c->fm, &c->face_rec, &c->edge_rec, &c->vert_rec, &c->q0,
+            &c->q1, &c->cand, &c->child, &c->child_cnt, &c->cells, &c->blk_cnt, &c->keep_v, &c->keep_e,
+            &c->keep_f, &c->removed_e, &c->trace, &c->thr, &c->rem_voff, &c->rem_eoff, &c->rem_foff,
+            &c->rem_vts, &c->rem_edges, &c->rem_tris, &c->uf_parent, &c->euler_tmp};
+}
+
+// Free every buffer of the context (it keeps its stream and error word);
+// all results are gone and the next call starts from vc_set_volume,
+// vc_batch_set_volumes or vc_set_complex.
+int ctx_release_buffers(vc_ctx* c) {
+    VC_CUDA(c, cudaSetDevice(c->device));
+    VC_CUDA(c, cudaStreamSynchronize(c->stream));
+    for (DevBuf* b : ctx_buffers(c)) {
+        if (b->p) {
+            cudaFreeAsync(b->p, c->stream);
+            c->bytes_held -= (int64_t)b->cap;
+        }
+        b->p = nullptr;
+        b->cap = 0;
+    }
+    c->n_sites = -1;
+    c->ft_valid = c->vd_valid = c->cc_valid = c->cc_finalized = c->meas_valid = c->thin_valid = c->rem_valid = false;
+    c->records_fresh = c->records_thr_folded = c->cc_batched = false;
+    c->nvol = 0;
+    c->tab = VolTab{};
+    c->bases = Bases{};
+    VC_CUDA(c, cudaStreamSynchronize(c->stream));
+    return VC_OK;
+}
+
 }  // namespace vc
 
 // ---------------------------------------------------------------------------
@@ -281,18 +318,8 @@ static void free_buf(vc_ctx* c, vc::DevBuf& b) {
 int vc_ctx_destroy(vc_ctx* c) {
     if (!c) return VC_OK;
     cudaSetDevice(c->device);
-    vc::DevBuf* all[] = {&c->err, &c->scratch, &c->scratch2, &c->occ, &c->site_xyz, &c->site_count,
-                         &c->site_id_lat, &c->ft_d2, &c->ft_id, &c->ft_tmp, &c->vd_flags, &c->vd_voff,
-                         &c->vd_eoff, &c->vd_foff, &c->vd_tri_face, &c->vd_face_sites, &c->vd_vm, &c->vd_lam,
-                         &c->vd_efoff, &c->vd_veoff, &c->vd_vpos, &c->vd_epos, &c->vd_fpos, &c->vd_radius, &c->tab_buf, &c->bases_buf,
-                         &c->vts, &c->edges_in, &c->edges, &c->tris, &c->tri_edges, &c->ve_off, &c->ve_ids,
-                         &c->ef_off, &c->ef_ids, &c->hash_keys, &c->hash_pos, &c->hash_id, &c->side_slot,
-                         &c->vm, &c->em, &c->fm, &c->face_rec, &c->edge_rec, &c->vert_rec,
-                         &c->q0, &c->q1, &c->cand, &c->child, &c->child_cnt, &c->cells, &c->blk_cnt, &c->keep_v,
-                         &c->keep_e, &c->keep_f, &c->removed_e, &c->trace,
-                         &c->thr, &c->rem_voff, &c->rem_eoff, &c->rem_foff, &c->rem_vts, &c->rem_edges,
-                         &c->rem_tris, &c->uf_parent, &c->euler_tmp};
-    for (auto* b : all) free_buf(c, *b);
+    for (auto* b : vc::ctx_buffers(c)) free_buf(c, *b);
+    free_buf(c, c->err);
     if (c->stream) cudaStreamSynchronize(c->stream);
     for (auto& p : c->pending) {
         cudaEventDestroy(p.a);
