@@ -8,6 +8,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -192,6 +193,7 @@ struct vc_ctx {
     vc::DevBuf trace;           // optional per-generation trace of the thinning kernel
     int trace_cap = 0, trace_gens = 0;
     int thin_blocks_per_sm = 0;  // 0 = library default
+    std::mutex* thin_lock = nullptr;  // shared by contexts whose thinning kernels must not overlap
     // remaining complex
     bool rem_valid = false;
     vc_rem_sizes rem{};

@@ -60,6 +60,7 @@ struct vc_server {
     double bytes_per_voxel = 640.0;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
+    std::mutex thin_lock;
     std::deque<Request*> pending;
     std::unordered_map<int64_t, std::unique_ptr<Request>> reqs;
     int64_t next_id = 1;
@@ -102,8 +103,35 @@ extern "C" int vc_plan_batches(int n, const int64_t* voxels, const double* t, in
 
 namespace {
 
+// Page-locked host staging that grows on demand (host <-> device copies at
+// full link speed, asynchronous on the worker's stream).
+struct Pinned {
+    void* p = nullptr;
+    size_t cap = 0;
+    void* get(size_t bytes) {
+        if (bytes <= cap) return p;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        cap = 0;
+        if (cudaMallocHost(&p, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            p = nullptr;
+            return nullptr;
+        }
+        cap = bytes;
+        return p;
+    }
+    ~Pinned() {
+        if (p) cudaFreeHost(p);
+    }
+};
+
+struct Staging {
+    Pinned occ, vts, edges, tris;
+};
+
 // One batch on one worker context; fills every request's result.
-void serve_batch(vc_server* s, vc_ctx* c, std::vector<Request*>& batch, std::vector<uint8_t>& stage) {
+void serve_batch(vc_server* s, vc_ctx* c, std::vector<Request*>& batch, Staging& stage) {
     const int n = (int)batch.size();
     std::vector<int32_t> dims(3 * (size_t)n);
     size_t total = 0;
@@ -113,17 +141,20 @@ void serve_batch(vc_server* s, vc_ctx* c, std::vector<Request*>& batch, std::vec
         dims[3 * i + 2] = batch[i]->Z;
         total += batch[i]->occ.size();
     }
-    stage.resize(total);
-    size_t off = 0;
-    for (Request* r : batch) {
-        std::memcpy(stage.data() + off, r->occ.data(), r->occ.size());
-        off += r->occ.size();
-    }
+    auto* occ = static_cast<uint8_t*>(stage.occ.get(total));
     std::vector<vc_batch_volume> out((size_t)n);
-    int st = vc_batch_set_volumes(c, n, dims.data(), stage.data(), VC_MEM_HOST);
+    int st = occ ? VC_OK : VC_ERR_OOM;
+    if (st == VC_OK) {
+        size_t off = 0;
+        for (Request* r : batch) {
+            std::memcpy(occ + off, r->occ.data(), r->occ.size());
+            off += r->occ.size();
+        }
+        st = vc_batch_set_volumes(c, n, dims.data(), occ, VC_MEM_HOST);
+    }
     if (st == VC_OK) st = vc_batch_run(c, batch[0]->t, 1, nullptr, out.data());
-    std::vector<float> vts;
-    std::vector<int32_t> edges, tris;
+    float* vts = nullptr;
+    int32_t *edges = nullptr, *tris = nullptr;
     if (st == VC_OK) {
         int64_t nv = 0, ne = 0, nt = 0;
         for (const auto& o : out) {
@@ -131,10 +162,10 @@ void serve_batch(vc_server* s, vc_ctx* c, std::vector<Request*>& batch, std::vec
             ne += o.rem.ne;
             nt += o.rem.nt;
         }
-        vts.resize(3 * (size_t)nv);
-        edges.resize(2 * (size_t)ne);
-        tris.resize(3 * (size_t)nt);
-        st = vc_get_remaining(c, vts.data(), edges.data(), tris.data(), VC_MEM_HOST);
+        vts = static_cast<float*>(stage.vts.get(12 * (size_t)nv + 4));
+        edges = static_cast<int32_t*>(stage.edges.get(8 * (size_t)ne + 4));
+        tris = static_cast<int32_t*>(stage.tris.get(12 * (size_t)nt + 4));
+        st = (vts && edges && tris) ? vc_get_remaining(c, vts, edges, tris, VC_MEM_HOST) : VC_ERR_OOM;
     }
     const double t_done = now_s();
     {
@@ -151,9 +182,9 @@ void serve_batch(vc_server* s, vc_ctx* c, std::vector<Request*>& batch, std::vec
                 q.thresh = o.thresh;
                 q.rem = o.rem;
                 q.euler = o.euler;
-                r->vts.assign(vts.begin() + 3 * o.rem_v_off, vts.begin() + 3 * (o.rem_v_off + o.rem.nv));
-                r->edges.assign(edges.begin() + 2 * o.rem_e_off, edges.begin() + 2 * (o.rem_e_off + o.rem.ne));
-                r->tris.assign(tris.begin() + 3 * o.rem_t_off, tris.begin() + 3 * (o.rem_t_off + o.rem.nt));
+                r->vts.assign(vts + 3 * o.rem_v_off, vts + 3 * (o.rem_v_off + o.rem.nv));
+                r->edges.assign(edges + 2 * o.rem_e_off, edges + 2 * (o.rem_e_off + o.rem.ne));
+                r->tris.assign(tris + 3 * o.rem_t_off, tris + 3 * (o.rem_t_off + o.rem.nt));
             }
             r->t_done = t_done;
             q.queue_ms = (r->t_start - r->t_submit) * 1e3;
@@ -171,7 +202,8 @@ void serve_batch(vc_server* s, vc_ctx* c, std::vector<Request*>& batch, std::vec
 
 void worker_main(vc_server* s, int w) {
     vc_ctx* c = s->ctxs[w];
-    std::vector<uint8_t> stage;
+    cudaSetDevice(s->device);
+    Staging stage;
     for (;;) {
         std::vector<Request*> batch;
         {
@@ -227,9 +259,9 @@ int vc_server_create(vc_server** out, int device, int workers, int64_t mem_cap_b
             for (vc_ctx* x : s->ctxs) vc_ctx_destroy(x);
             return st;
         }
-        // the workers' persistent thinning kernels share the SMs: each gets
-        // an equal slice of the resident blocks so all can be co-resident
-        c->thin_blocks_per_sm = std::max(1, 8 / workers);
+        // the workers' persistent thinning kernels each take the whole GPU,
+        // one at a time; their other stages overlap freely
+        c->thin_lock = &s->thin_lock;
         s->ctxs.push_back(c);
     }
     vc_server* raw = s.release();

@@ -562,10 +562,19 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats) {
     A.counters = reinterpret_cast<int*>(A.blk_cnt + 2 * (int64_t)G);
     void* args[] = {&A};
     {
+        // Contexts that share a thinning lock (the request loop's workers)
+        // run their persistent kernels one at a time, each on the whole GPU;
+        // the lock is held from the launch until the kernel has finished.
+        std::unique_lock<std::mutex> lk;
+        if (c->thin_lock) {
+            VC_CUDA(c, cudaStreamSynchronize(c->stream));
+            lk = std::unique_lock<std::mutex>(*c->thin_lock);
+        }
         Region r(c, "thin_generations");
         VC_CUDA(c, cudaLaunchCooperativeKernel((void*)thin_generations_kernel, dim3(G), dim3(kThreads), args, 0,
                                                c->stream));
         launched(c);
+        if (c->thin_lock) VC_CUDA(c, cudaStreamSynchronize(c->stream));
     }
     export_flags_kernel<<<grid_for(c, nv + ne + nt, 256), 256, 0, c->stream>>>(
         A.F, A.E, A.V, (int32_t)nv, (int32_t)ne, (int32_t)nt, ptr<uint8_t>(c->keep_v), ptr<uint8_t>(c->keep_e),
