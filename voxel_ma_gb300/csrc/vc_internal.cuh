@@ -43,6 +43,22 @@ T* ptr(const DevBuf& b) {
 // Per-cell records of the thinning kernel: static data and thinning state of
 // one cell in one 32-byte DRAM sector (its accesses are random).
 constexpr int32_t kAlive = INT32_MAX;  // removal position of a cell still present
+// An edge's faces (a vertex's edges) still present, as one 64-bit word: their
+// count in the low kRefBits bits and the sum of their ids (mod 2^40) above.
+// Removing incident cell x subtracts (x << kRefBits) + 1 in one atomic; when
+// the count is 1 the sum is the id of the one cell left.
+constexpr int kRefBits = 24;
+constexpr unsigned long long kRefMask = (1ull << kRefBits) - 1ull;
+__host__ __device__ __forceinline__ unsigned long long rs_make(unsigned long long count, unsigned long long id_sum) {
+    return (id_sum << kRefBits) | count;
+}
+__host__ __device__ __forceinline__ unsigned long long rs_drop(int32_t id) {
+    return ~(((unsigned long long)(uint32_t)id << kRefBits) + 1ull) + 1ull;  // -(id << kRefBits) - 1
+}
+__host__ __device__ __forceinline__ int32_t rs_count(unsigned long long w) { return (int32_t)(w & kRefMask); }
+__host__ __device__ __forceinline__ int32_t rs_last(unsigned long long w) {
+    return (int32_t)(uint32_t)((w >> kRefBits) & 0xFFFFFFFFull);
+}
 struct __align__(32) FaceRec {
     int32_t e0, e1, e2;  // edge ids of the sides, in face order
     float fm;
@@ -51,14 +67,14 @@ struct __align__(32) FaceRec {
 };
 struct __align__(32) EdgeRec {
     int32_t v0, v1;
+    unsigned long long rs;  // faces still present: count | id sum
     float em;
-    int32_t ef_off, ef_cnt;  // E->F list
-    int32_t rm, ref, trig;
+    int32_t rm, trig, pad;
 };
 struct __align__(32) VertRec {
-    int32_t ve_off, ve_cnt;  // V->E list
-    int32_t rm, ref, trig;
-    int32_t pad0, pad1, pad2;
+    unsigned long long rs;  // edges still present: count | id sum
+    int32_t rm, trig;
+    int32_t pad0, pad1, pad2, pad3;
 };
 static_assert(sizeof(FaceRec) == 32 && sizeof(EdgeRec) == 32 && sizeof(VertRec) == 32, "record size");
 

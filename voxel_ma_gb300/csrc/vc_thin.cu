@@ -39,8 +39,12 @@
 // Memory layout: the accesses are random, so every cell's static data and
 // thinning state share one 32-byte record (one DRAM sector per touch):
 //   face   {e0, e1, e2, fm, rm}
-//   edge   {v0, v1, em, ef_off, ef_cnt, rm, ref, trig}
-//   vertex {ve_off, ve_cnt, rm, ref, trig}
+//   edge   {v0, v1, rs, em, rm, trig}
+//   vertex {rs, rm, trig}
+// rs packs the count of incident faces (edges) still present with the sum of
+// their ids: one atomic removes an incident cell, and when the count is 1
+// the sum names the remaining cell, so no incidence list is read while
+// thinning.
 #include "vc_internal.cuh"
 
 namespace vc {
@@ -54,8 +58,6 @@ struct ThinArgs {
     FaceRec* F;
     EdgeRec* E;
     VertRec* V;
-    const int32_t* ve_ids;
-    const int32_t* ef_ids;
     const float* thr;  // [0] f_t, [1] l_t
     int2* qa;
     int2* qb;
@@ -85,11 +87,13 @@ __device__ __forceinline__ bool is_fe(int2 it) { return ((unsigned)it.x & kFE) !
 __device__ __forceinline__ int32_t idx0(int2 it) { return (int32_t)((unsigned)it.x & ~kFE); }
 
 // Build the records from the finalized complex (CSR) and the measures, and
-// reset the thinning state.
+// reset the thinning state.  A cell with 2^24 or more incident cells cannot
+// be represented (VC_ERR_ARG).
 __global__ void build_records_kernel(const int2* __restrict__ edges, const int32_t* __restrict__ tri_edges,
-                                     const int32_t* __restrict__ ve_off, const int32_t* __restrict__ ef_off,
+                                     const int32_t* __restrict__ ve_off, const int32_t* __restrict__ ve_ids,
+                                     const int32_t* __restrict__ ef_off, const int32_t* __restrict__ ef_ids,
                                      const float* __restrict__ em, const float* __restrict__ fm, int32_t nv,
-                                     int32_t ne, int32_t nt, FaceRec* F, EdgeRec* E, VertRec* V) {
+                                     int32_t ne, int32_t nt, FaceRec* F, EdgeRec* E, VertRec* V, int* err) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     const int64_t n = (int64_t)nv + ne + nt;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
@@ -104,26 +108,31 @@ __global__ void build_records_kernel(const int2* __restrict__ edges, const int32
             F[i] = r;
         } else if (i < (int64_t)nt + ne) {
             const int64_t e = i - nt;
+            const int32_t o0 = ef_off[e], o1 = ef_off[e + 1];
+            unsigned long long idsum = 0;
+            for (int32_t k = o0; k < o1; ++k) idsum += (unsigned)ef_ids[k];
+            if ((unsigned long long)(o1 - o0) > kRefMask) set_error(err, VC_ERR_ARG);
             EdgeRec r;
             const int2 ev = edges[e];
             r.v0 = ev.x;
             r.v1 = ev.y;
+            r.rs = rs_make((unsigned)(o1 - o0), idsum);
             r.em = em[e];
-            r.ef_off = ef_off[e];
-            r.ef_cnt = ef_off[e + 1] - ef_off[e];
             r.rm = kAlive;
-            r.ref = r.ef_cnt;
             r.trig = -1;
+            r.pad = 0;
             E[e] = r;
         } else {
             const int64_t v = i - nt - ne;
+            const int32_t o0 = ve_off[v], o1 = ve_off[v + 1];
+            unsigned long long idsum = 0;
+            for (int32_t k = o0; k < o1; ++k) idsum += (unsigned)ve_ids[k];
+            if ((unsigned long long)(o1 - o0) > kRefMask) set_error(err, VC_ERR_ARG);
             VertRec r;
-            r.ve_off = ve_off[v];
-            r.ve_cnt = ve_off[v + 1] - ve_off[v];
+            r.rs = rs_make((unsigned)(o1 - o0), idsum);
             r.rm = kAlive;
-            r.ref = r.ve_cnt;
             r.trig = -1;
-            r.pad0 = r.pad1 = r.pad2 = 0;
+            r.pad0 = r.pad1 = r.pad2 = r.pad3 = 0;
             V[v] = r;
         }
     }
@@ -137,11 +146,11 @@ __global__ void gen0_flags_kernel(ThinArgs A, int32_t nv, int32_t ne, int32_t* _
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (int64_t)ne + nv; i += stride) {
         int32_t ok = 0;
         if (i < ne) {
-            const EdgeRec& r = A.E[i];
-            if (r.ref == 1) ok = A.F[A.ef_ids[r.ef_off]].fm < f_t;
+            const unsigned long long rs = A.E[i].rs;
+            if (rs_count(rs) == 1) ok = A.F[rs_last(rs)].fm < f_t;
         } else {
-            const VertRec& r = A.V[i - ne];
-            if (r.ref == 1) ok = A.E[A.ve_ids[r.ve_off]].em < l_t;
+            const unsigned long long rs = A.V[i - ne].rs;
+            if (rs_count(rs) == 1) ok = A.E[rs_last(rs)].em < l_t;
         }
         flag[i] = ok;
     }
@@ -154,32 +163,16 @@ __global__ void gen0_write_kernel(ThinArgs A, int32_t nv, int32_t ne, const int3
         if (!flag[i]) continue;
         const int32_t p = pos[i];
         if (i < ne) {
-            const int32_t f = A.ef_ids[A.E[i].ef_off];
+            const int32_t f = rs_last(A.E[i].rs);
             A.qa[p] = make_fe(f, (int32_t)i);
             atomicMin(&A.F[f].rm, p);
         } else {
             const int32_t v = (int32_t)(i - ne);
-            const int32_t e = A.ve_ids[A.V[v].ve_off];
+            const int32_t e = rs_last(A.V[v].rs);
             A.qa[p] = make_ev(e, v);
             atomicMin(&A.E[e].rm, p);
         }
     }
-}
-
-// Unique remaining face of an edge / edge of a vertex (first with no removal).
-__device__ __forceinline__ int32_t live_face(const ThinArgs& A, int32_t off, int32_t cnt) {
-    for (int32_t k = 0; k < cnt; ++k) {
-        const int32_t f = A.ef_ids[off + k];
-        if (__ldcg(&A.F[f].rm) == kAlive) return f;
-    }
-    return -1;
-}
-__device__ __forceinline__ int32_t live_edge(const ThinArgs& A, int32_t off, int32_t cnt) {
-    for (int32_t k = 0; k < cnt; ++k) {
-        const int32_t e = A.ve_ids[off + k];
-        if (__ldcg(&A.E[e].rm) == kAlive) return e;
-    }
-    return -1;
 }
 
 // Warp-aggregated append of a cell whose count fell from 2 to 1 to the
@@ -239,7 +232,7 @@ __global__ void __launch_bounds__(kThreads) thin_generations_kernel(ThinArgs A) 
                 if (is_fe(it)) {
                     const int32_t f = idx0(it), e = it.y;
                     const int32_t frm = __ldcg(&A.F[f].rm);
-                    const int32_t eref = __ldcg(&A.E[e].ref);
+                    const int32_t eref = rs_count(__ldcg(&A.E[e].rs));
                     if (frm != p) {
                         ++my_skipped;
                     } else if (eref != 1) {
@@ -253,15 +246,16 @@ __global__ void __launch_bounds__(kThreads) thin_generations_kernel(ThinArgs A) 
                         const int32_t sb = (s0 == e || s1 == e) ? s2 : s1;
                         const int32_t v0 = A.E[e].v0, v1 = A.E[e].v1;
                         atomicMin(&A.E[e].rm, p);
-                        A.E[e].ref = 0;
+                        A.E[e].rs = 0;
                         atomicMax(&A.E[sa].trig, p);
                         atomicMax(&A.E[sb].trig, p);
                         atomicMax(&A.V[v0].trig, p);
                         atomicMax(&A.V[v1].trig, p);
-                        const int oa = atomicSub(&A.E[sa].ref, 1);
-                        const int ob = atomicSub(&A.E[sb].ref, 1);
-                        const int o0 = atomicSub(&A.V[v0].ref, 1);
-                        const int o1 = atomicSub(&A.V[v1].ref, 1);
+                        const unsigned long long df = rs_drop(f), de = rs_drop(e);
+                        const int oa = rs_count(atomicAdd(&A.E[sa].rs, df));
+                        const int ob = rs_count(atomicAdd(&A.E[sb].rs, df));
+                        const int o0 = rs_count(atomicAdd(&A.V[v0].rs, de));
+                        const int o1 = rs_count(atomicAdd(&A.V[v1].rs, de));
                         if (oa == 2) one[0] = sa | kEdgeBit;
                         if (ob == 2) one[1] = sb | kEdgeBit;
                         if (o0 == 2) one[2] = v0;
@@ -271,7 +265,7 @@ __global__ void __launch_bounds__(kThreads) thin_generations_kernel(ThinArgs A) 
                 } else {
                     const int32_t e = it.x, v = it.y;
                     const int32_t erm = __ldcg(&A.E[e].rm);
-                    const int32_t vref = __ldcg(&A.V[v].ref);
+                    const int32_t vref = rs_count(__ldcg(&A.V[v].rs));
                     if (erm != p) {
                         ++my_skipped;
                     } else if (vref != 1) {
@@ -281,9 +275,9 @@ __global__ void __launch_bounds__(kThreads) thin_generations_kernel(ThinArgs A) 
                         A.V[v].rm = p;
                         const int32_t v0 = A.E[e].v0, v1 = A.E[e].v1;
                         const int32_t u = v0 != v ? v0 : v1;
-                        A.V[v].ref = 0;
+                        A.V[v].rs = 0;
                         atomicMax(&A.V[u].trig, p);
-                        if (atomicSub(&A.V[u].ref, 1) == 2) one[2] = u;
+                        if (rs_count(atomicAdd(&A.V[u].rs, rs_drop(e))) == 2) one[2] = u;
                         cd.z = u;
                     }
                 }
@@ -315,25 +309,19 @@ __global__ void __launch_bounds__(kThreads) thin_generations_kernel(ThinArgs A) 
                 int2 ch;
                 if (code & kEdgeBit) {
                     const int32_t e2 = code & ~kEdgeBit;
-                    if (__ldcg(&A.E[e2].ref) != 1) continue;
+                    const unsigned long long rs = __ldcg(&A.E[e2].rs);
+                    if (rs_count(rs) != 1) continue;
                     i = (int64_t)__ldcg(&A.E[e2].trig) - base;
-                    const int32_t f2 = live_face(A, A.E[e2].ef_off, A.E[e2].ef_cnt);
-                    if (f2 < 0) {
-                        set_error(A.err, VC_ERR_INVARIANT);
-                        continue;
-                    }
+                    const int32_t f2 = rs_last(rs);
                     if (!(A.F[f2].fm < f_t)) continue;
                     slot = __ldcg(&A.cand[i].x) == e2 ? 0 : 1;
                     ch = make_fe(f2, e2);
                 } else {
                     const int32_t u = code;
-                    if (__ldcg(&A.V[u].ref) != 1) continue;
+                    const unsigned long long rs = __ldcg(&A.V[u].rs);
+                    if (rs_count(rs) != 1) continue;
                     i = (int64_t)__ldcg(&A.V[u].trig) - base;
-                    const int32_t e3 = live_edge(A, A.V[u].ve_off, A.V[u].ve_cnt);
-                    if (e3 < 0) {
-                        set_error(A.err, VC_ERR_INVARIANT);
-                        continue;
-                    }
+                    const int32_t e3 = rs_last(rs);
                     if (!(A.E[e3].em < l_t)) continue;
                     slot = __ldcg(&A.cand[i].z) == u ? 2 : 3;
                     ch = make_ev(e3, u);
@@ -435,7 +423,7 @@ __global__ void export_flags_kernel(const FaceRec* __restrict__ F, const EdgeRec
             kv[i] = V[i].rm == kAlive;
         } else if (i < (int64_t)nv + ne) {
             const int64_t e = i - nv;
-            const int32_t rm = E[e].rm, ref = E[e].ref;
+            const int32_t rm = E[e].rm, ref = rs_count(E[e].rs);
             ke[e] = rm == kAlive && ref == 0;
             re[e] = rm != kAlive;
         } else {
@@ -508,8 +496,6 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats) {
     A.F = ptr<FaceRec>(c->face_rec);
     A.E = ptr<EdgeRec>(c->edge_rec);
     A.V = ptr<VertRec>(c->vert_rec);
-    A.ve_ids = ptr<int32_t>(c->ve_ids);
-    A.ef_ids = ptr<int32_t>(c->ef_ids);
     A.thr = ptr<float>(c->thr);
     A.qa = ptr<int2>(c->q0);
     A.qb = ptr<int2>(c->q1);
@@ -535,8 +521,9 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats) {
             c->records_fresh = false;  // the next thinning of this complex rebuilds them
         } else {
             build_records_kernel<<<grid_for(c, nv + ne + nt, 256), 256, 0, c->stream>>>(
-                ptr<int2>(c->edges), ptr<int32_t>(c->tri_edges), ptr<int32_t>(c->ve_off), ptr<int32_t>(c->ef_off),
-                ptr<float>(c->em), ptr<float>(c->fm), (int32_t)nv, (int32_t)ne, (int32_t)nt, A.F, A.E, A.V);
+                ptr<int2>(c->edges), ptr<int32_t>(c->tri_edges), ptr<int32_t>(c->ve_off), ptr<int32_t>(c->ve_ids),
+                ptr<int32_t>(c->ef_off), ptr<int32_t>(c->ef_ids), ptr<float>(c->em), ptr<float>(c->fm), (int32_t)nv,
+                (int32_t)ne, (int32_t)nt, A.F, A.E, A.V, dev_err(c));
             launched(c);
         }
         int32_t* flag = ptr<int32_t>(c->scratch2);

@@ -420,13 +420,13 @@ __global__ void vd_vertices_kernel(const uint8_t* __restrict__ occ, const int32_
             }
             sort_small<6>(dg, nd);
             for (int i = 0; i < nd; ++i) ve_ids[off + k++] = (int32_t)sh.eb1 + dg[i];
+            unsigned long long idsum = 0;
+            for (int q = 0; q < k; ++q) idsum += (unsigned)ve_ids[off + q];
             VertRec r;
-            r.ve_off = off;
-            r.ve_cnt = k;
+            r.rs = rs_make((unsigned)k, idsum);
             r.rm = kAlive;
-            r.ref = k;
             r.trig = -1;
-            r.pad0 = r.pad1 = r.pad2 = 0;
+            r.pad0 = r.pad1 = r.pad2 = r.pad3 = 0;
             V[v] = r;
             // the volume's bounding box: lanes of the same volume reduce in
             // the warp first, so each warp issues one set of atomics per volume
@@ -490,15 +490,16 @@ __global__ void vd_edges_kernel(const uint8_t* __restrict__ occ, const int32_t* 
         for (int j = 0; j < k; ++j) ef_ids[efo + j] = tl[j];
         edges[e] = make_int2(v0, v1);
         em[e] = m;
+        unsigned long long idsum = 0;
+        for (int j = 0; j < k; ++j) idsum += (unsigned)tl[j];
         EdgeRec r;
         r.v0 = v0;
         r.v1 = v1;
+        r.rs = rs_make((unsigned)k, idsum);
         r.em = rec_measure(m, thr, bv);
-        r.ef_off = efo;
-        r.ef_cnt = k;
         r.rm = kAlive;
-        r.ref = k;
         r.trig = -1;
+        r.pad = 0;
         E[e] = r;
     }
 }
@@ -591,12 +592,11 @@ __global__ void vd_faces_kernel(const uint8_t* __restrict__ occ, const int32_t* 
                 EdgeRec er;
                 er.v0 = dv0;
                 er.v1 = dv1;
+                er.rs = rs_make(2, (unsigned long long)t0 + (unsigned long long)t1);
                 er.em = lr;
-                er.ef_off = efo;
-                er.ef_cnt = 2;
                 er.rm = kAlive;
-                er.ref = 2;
                 er.trig = -1;
+                er.pad = 0;
                 E[diag] = er;
             }
         }
