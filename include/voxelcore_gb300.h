@@ -268,6 +268,10 @@ int vc_extract_sites_noalloc(const uint8_t* occ, int X, int Y, int Z, float* xyz
  * blocks per SM (0 = default).                                             */
 int vc_debug_thin_trace(vc_ctx* ctx, int cap, int blocks_per_sm);
 int vc_debug_get_thin_trace(vc_ctx* ctx, int64_t* out, int cap, int* ngen);
+/* With wide != 0 the feature transform's envelope passes use 64-bit
+ * arithmetic even when every lattice axis is below 2048 (where 32-bit
+ * arithmetic is exact and is the default); results are identical.         */
+int vc_debug_ft_wide(vc_ctx* ctx, int wide);
 
 #ifdef __cplusplus
 }

@@ -56,6 +56,29 @@ def test_sites_ft_vd_match_oracle(gpu_ctx, name, occ):
         assert np.array_equal(fin[k], L["fin"][k]), k
 
 
+FT_VOLS = [VOLS[0], VOLS[2], VOLS[3], VOLS[4],
+           ("rod", (np.random.default_rng(3).uniform(size=(2, 300, 3)) < 0.3).astype(np.uint8)),
+           ("slab", (np.random.default_rng(4).uniform(size=(260, 2, 5)) < 0.05).astype(np.uint8))]
+
+
+@pytest.mark.parametrize("name,occ", FT_VOLS, ids=[v[0] for v in FT_VOLS])
+def test_ft_narrow_and_wide_arithmetic(gpu_ctx, name, occ):
+    """The envelope passes run in 32-bit arithmetic below 2048 points per
+    axis and in 64-bit above; both must give the oracle's exact transform."""
+    ctx = gpu_ctx
+    L = lattice_case(O, occ)
+    try:
+        for wide in (False, True):
+            ctx.debug_ft_wide(wide)
+            ctx.set_volume(occ)
+            ctx.extract_sites()
+            ctx.feature_transform()
+            d2, ids = ctx.ft()
+            assert np.array_equal(d2, L["d2"]) and np.array_equal(ids, L["ids"]), f"wide={wide}"
+    finally:
+        ctx.debug_ft_wide(False)
+
+
 def test_empty_volume(gpu_ctx):
     occ = np.zeros((5, 6, 7), np.uint8)
     gpu_ctx.set_volume(occ)

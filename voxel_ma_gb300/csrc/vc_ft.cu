@@ -9,48 +9,42 @@
 // (distance, index) order, so every pass keeps exactly the lexicographic
 // minimum:
 //   pass 1 (along z, contiguous rows): nearest site in the row, one warp per
-//          row, by a forward max-scan and a backward min-scan over the row;
+//          row: the row's site ids are staged in shared memory, then a
+//          forward max-scan and a backward min-scan of site positions;
 //   pass 2 (along y) and pass 3 (along x): lower envelope of the parabolas
 //          (x - q)^2 + g(q), one thread per line, with integer crossing
 //          thresholds that include the index tie-break (the smallest x at
 //          which the later parabola wins is computed exactly), so the
 //          envelope is the lexicographic minimum at every integer x.
+//
+// Memory behaviour: pass 1 stages each row in shared memory and writes it
+// with streaming stores.  In the envelope passes consecutive lanes own
+// consecutive lines, so the candidate loads of a step are one contiguous
+// warp access, issued a chunk ahead of their use; each point is written as
+// soon as it is final, so the live stack of a line stays a few entries deep
+// and sits in shared memory (vc_ft_line.cuh).
 #include "vc_internal.cuh"
+#include "vc_ft_line.cuh"
 
 namespace vc {
 namespace {
 
-constexpr int64_t kInf = INT64_MAX;
+constexpr int64_t kInf = kFtInf;
+constexpr int kEnvThreads = 256;
+constexpr int kPrefetch = 8;
 
-__device__ __forceinline__ int64_t pack(int64_t g, int32_t id) { return (g << 32) | (uint32_t)id; }
-__device__ __forceinline__ int64_t pk_g(int64_t p) { return p >> 32; }
-__device__ __forceinline__ int32_t pk_id(int64_t p) { return (int32_t)(uint32_t)(p & 0xffffffffLL); }
-
-// floor(n / d) for d > 0
-__device__ __forceinline__ int64_t floordiv(int64_t n, int64_t d) {
-    int64_t q = n / d;
-    if ((n % d) != 0 && n < 0) --q;
-    return q;
-}
-// Smallest integer x at which candidate r (position qr, value gr, index ir)
-// beats candidate p (position qp < qr) in the (value, index) order.
-__device__ __forceinline__ int64_t cross_threshold(int64_t qp, int64_t gp, int32_t ip, int64_t qr, int64_t gr,
-                                                   int32_t ir) {
-    const int64_t den = 2 * (qr - qp);
-    const int64_t num = qr * qr - qp * qp + gr - gp;
-    const int64_t fl = floordiv(num, den);
-    if (fl * den == num && ir < ip) return fl;
-    return fl + 1;
-}
+__device__ __forceinline__ int64_t pack(int64_t g, int32_t id) { return ft_pack(g, id); }
 
 // Pass 1: one warp per lattice row along z (volume b, a, b'), NC = Z_b + 1
-// points; `ncmax` is the longest row of the batch (shared memory per warp).
+// points; `ncmax` is the longest row of the batch.  Per warp the shared
+// memory holds the row's site ids and the forward scan (2 * ncmax int32).
 __global__ void __launch_bounds__(256) ft_rows_kernel(const int32_t* __restrict__ site_id, int64_t* __restrict__ out,
                                                       VolTab T, int ncmax) {
-    extern __shared__ int64_t left_sm[];  // per warp: ncmax entries
+    extern __shared__ int32_t rows_sm[];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
-    int64_t* left = left_sm + (int64_t)wib * ncmax;
+    int32_t* ids = rows_sm + (int64_t)wib * 2 * ncmax;
+    int32_t* left = ids + ncmax;
     const int64_t warps_total = (int64_t)gridDim.x * (blockDim.x >> 5);
     const int64_t nrows = T.total(kLRow);
     for (int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + wib; row < nrows; row += warps_total) {
@@ -58,15 +52,18 @@ __global__ void __launch_bounds__(256) ft_rows_kernel(const int32_t* __restrict_
         const int NC = T.dim(bv).z + 1;
         const int64_t rbase = T.start(kLat, bv) + (row - T.start(kLRow, bv)) * NC;
         const int32_t* in = site_id + rbase;
-        // forward: latest site at or before c, packed (pos << 32 | id); -1 = none
-        int64_t carry = -1;
+        // stage the row (independent loads, all in flight together)
+#pragma unroll 4
+        for (int c = lane; c < NC; c += 32) ids[c] = __ldcs(in + c);
+        __syncwarp();
+        // forward: position of the latest site at or before c (-1: none)
+        int carry = -1;
         for (int c0 = 0; c0 < NC; c0 += 32) {
             const int c = c0 + lane;
-            int32_t s = c < NC ? in[c] : -1;
-            int64_t v = s >= 0 ? (((int64_t)c << 32) | (uint32_t)s) : -1;
+            int v = (c < NC && ids[c] >= 0) ? c : -1;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
-                int64_t n = __shfl_up_sync(0xffffffffu, v, o);
+                const int n = __shfl_up_sync(0xffffffffu, v, o);
                 if (lane >= o) v = max(v, n);
             }
             v = max(v, carry);
@@ -74,32 +71,32 @@ __global__ void __launch_bounds__(256) ft_rows_kernel(const int32_t* __restrict_
             carry = __shfl_sync(0xffffffffu, v, 31);
         }
         __syncwarp();
-        // backward: earliest site at or after c; combine with the left one
-        int64_t rcarry = kInf;
+        // backward: position of the earliest site at or after c; the nearer
+        // of the two (lower index on a tie) is the row's nearest site
+        int rcarry = INT32_MAX;
         const int nchunks = (NC + 31) / 32;
         for (int ch = nchunks - 1; ch >= 0; --ch) {
             const int c = ch * 32 + lane;
-            int32_t s = c < NC ? in[c] : -1;
-            int64_t v = s >= 0 ? (((int64_t)c << 32) | (uint32_t)s) : kInf;
+            int v = (c < NC && ids[c] >= 0) ? c : INT32_MAX;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
-                int64_t n = __shfl_down_sync(0xffffffffu, v, o);
+                const int n = __shfl_down_sync(0xffffffffu, v, o);
                 if (lane + o < 32) v = min(v, n);
             }
             v = min(v, rcarry);
             rcarry = __shfl_sync(0xffffffffu, v, 0);
             if (c < NC) {
                 int64_t best = kInf;
-                int64_t l = left[c];
+                const int l = left[c];
                 if (l >= 0) {
-                    int64_t d = c - (l >> 32);
-                    best = pack(d * d, (int32_t)(uint32_t)(l & 0xffffffffLL));
+                    const int64_t d = c - l;
+                    best = pack(d * d, ids[l]);
                 }
-                if (v != kInf) {
-                    int64_t d = (v >> 32) - c;
-                    best = min(best, pack(d * d, (int32_t)(uint32_t)(v & 0xffffffffLL)));
+                if (v != INT32_MAX) {
+                    const int64_t d = v - c;
+                    best = min(best, pack(d * d, ids[v]));
                 }
-                out[rbase + c] = best;
+                __stcs(out + rbase + c, best);
             }
         }
         __syncwarp();
@@ -108,20 +105,27 @@ __global__ void __launch_bounds__(256) ft_rows_kernel(const int32_t* __restrict_
 
 // Passes 2 and 3: lower envelope along the lattice lines of every volume:
 // PASS 2 along y (local line (a, c), L = Y+1 points, stride Z+1), PASS 3
-// along x (local line (b, c), L = X+1 points, stride (Y+1)(Z+1)).
-// Consecutive lines of a volume are consecutive addresses, so each step is a
-// coalesced access across the warp.  The envelope stack (position | start
-// threshold << 16, both < 2^15) of local line l of volume b lives in `stack`
-// at lattice start of b + l * L + k.
-template <int PASS>
-__global__ void __launch_bounds__(256) ft_envelope_kernel(const int64_t* __restrict__ in, int64_t* __restrict__ out,
-                                                          int32_t* __restrict__ d2o, int32_t* __restrict__ ido,
-                                                          int32_t* __restrict__ stack, VolTab T) {
+// along x (local line (b, c), L = X+1 points, stride (Y+1)(Z+1)), one
+// thread per line (ft_envelope_line).  Consecutive lines of a volume are
+// consecutive addresses, so the candidate loads of a step are one coalesced
+// warp access.  The ring of each line is a column of shared memory (slot j
+// of thread t at j * blockDim + t: no bank conflicts); spilled entry k of
+// local line l of volume b goes to gmeta / gval at lattice start of b +
+// k * (lines of b) + l.
+template <int PASS, int RING, class I>
+__global__ void __launch_bounds__(kEnvThreads) ft_envelope_kernel(const int64_t* __restrict__ in,
+                                                                  int64_t* __restrict__ out, int32_t* __restrict__ d2o,
+                                                                  int32_t* __restrict__ ido,
+                                                                  int32_t* __restrict__ gmeta,
+                                                                  int64_t* __restrict__ gval, VolTab T) {
     constexpr bool FINAL = PASS == 3;
     constexpr int kSpace = PASS == 2 ? kYLine : kXLine;
+    extern __shared__ int64_t env_sm[];
+    int64_t* s_val = env_sm;                                                    // [RING][kEnvThreads]
+    int32_t* s_meta = reinterpret_cast<int32_t*>(env_sm + RING * kEnvThreads);  // [RING][kEnvThreads]
+    const int t = threadIdx.x;
     const int64_t nlines = T.total(kSpace);
-    for (int64_t gl = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; gl < nlines;
-         gl += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t gl = (int64_t)blockIdx.x * blockDim.x + t; gl < nlines; gl += (int64_t)gridDim.x * blockDim.x) {
         const int bv = T.find(kSpace, gl);
         const int4 dm = T.dim(bv);
         const int64_t NB = dm.y + 1, NC = dm.z + 1;
@@ -129,80 +133,49 @@ __global__ void __launch_bounds__(256) ft_envelope_kernel(const int64_t* __restr
         const int64_t l = gl - T.start(kSpace, bv);
         const int L = PASS == 2 ? (int)NB : dm.x + 1;
         const int64_t stride = PASS == 2 ? NC : NB * NC;
+        const int64_t nl = PASS == 2 ? (int64_t)(dm.x + 1) * NC : NB * NC;
         const int64_t base = lat0 + (PASS == 2 ? (l / NC) * NB * NC + (l % NC) : l);
-        int32_t* st = stack + lat0 + l * L;
-        int k = 0;
-        // cached top of stack
-        int64_t tq = 0, tg = 0, tz = 0;
-        int32_t tid = 0;
-        for (int q = 0; q < L; ++q) {
-            const int64_t cv = __ldg(in + base + (int64_t)q * stride);
-            if (cv == kInf) continue;
-            const int64_t g = pk_g(cv);
-            const int32_t id = pk_id(cv);
-            int64_t T = 0;
-            while (k > 0) {
-                T = cross_threshold(tq, tg, tid, q, g, id);
-                if (T <= tz) {
-                    --k;
-                    if (k > 0) {
-                        const int32_t e = st[k - 1];
-                        tq = e & 0xffff;
-                        tz = (e >> 16) & 0xffff;
-                        const int64_t pv = __ldg(in + base + tq * stride);
-                        tg = pk_g(pv);
-                        tid = pk_id(pv);
-                    }
-                    continue;
-                }
-                break;
-            }
-            if (k == 0) {
-                st[0] = q;
-                tq = q; tz = 0; tg = g; tid = id;
-                k = 1;
-            } else if (T < L) {
-                st[k] = q | ((int32_t)T << 16);
-                tq = q; tz = T; tg = g; tid = id;
-                ++k;
-            }
-        }
-        if (k == 0) {
-            for (int x = 0; x < L; ++x) {
-                const int64_t o = base + (int64_t)x * stride;
-                if (FINAL) {
-                    d2o[o] = INT32_MAX;
-                    ido[o] = -1;
-                } else {
-                    out[o] = kInf;
-                }
-            }
-            continue;
-        }
-        int w = 0;
-        int32_t e = st[0];
-        int64_t wq = e & 0xffff;
-        int64_t wv = __ldg(in + base + wq * stride);
-        int32_t nz = k > 1 ? ((st[1] >> 16) & 0xffff) : INT32_MAX;
-        for (int x = 0; x < L; ++x) {
-            while (w + 1 < k && nz <= x) {
-                ++w;
-                e = st[w];
-                wq = e & 0xffff;
-                wv = __ldg(in + base + wq * stride);
-                nz = w + 1 < k ? ((st[w + 1] >> 16) & 0xffff) : INT32_MAX;
-            }
-            const int64_t d = (int64_t)x - wq;
-            const int64_t g = pk_g(wv) + d * d;
+        const int64_t* src = in + base;
+        auto load = [&](int q) -> int64_t { return __ldcs(src + (int64_t)q * stride); };
+        auto emit = [&](int x, int64_t v) {
             const int64_t o = base + (int64_t)x * stride;
             if (FINAL) {
-                d2o[o] = (int32_t)g;
-                ido[o] = pk_id(wv);
+                __stcs(d2o + o, (int32_t)ft_g(v));
+                __stcs(ido + o, ft_id(v));
             } else {
-                out[o] = pack(g, pk_id(wv));
+                __stcs(out + o, v);
             }
-        }
+        };
+        ft_envelope_line<I, RING, kPrefetch>(L, load, emit, s_meta + t, s_val + t, kEnvThreads, gmeta + lat0 + l,
+                                          gval + lat0 + l, nl);
     }
+}
+
+constexpr int kRing = 8;
+constexpr size_t kEnvSmem = (size_t)kRing * kEnvThreads * (sizeof(int64_t) + sizeof(int32_t));
+
+template <int PASS, class I>
+int launch_envelope_t(vc_ctx* c, const int64_t* in, int64_t* out, int32_t* d2o, int32_t* ido, int32_t* gmeta,
+                      int64_t* gval, int64_t nlines) {
+    auto kern = ft_envelope_kernel<PASS, kRing, I>;
+    VC_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kEnvSmem));
+    int per_sm = 0;
+    VC_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kEnvThreads, kEnvSmem));
+    per_sm = std::max(per_sm, 1);
+    const int blocks = (int)std::max<int64_t>(
+        1, std::min<int64_t>((nlines + kEnvThreads - 1) / kEnvThreads, (int64_t)c->num_sms * per_sm));
+    kern<<<blocks, kEnvThreads, kEnvSmem, c->stream>>>(in, out, d2o, ido, gmeta, gval, c->tab);
+    launched(c);
+    VC_CUDA(c, cudaGetLastError());
+    return VC_OK;
+}
+
+// int32 arithmetic when every lattice axis of the batch is below 2048
+template <int PASS>
+int launch_envelope(vc_ctx* c, bool small, const int64_t* in, int64_t* out, int32_t* d2o, int32_t* ido,
+                    int32_t* gmeta, int64_t* gval, int64_t nlines) {
+    return small ? launch_envelope_t<PASS, int32_t>(c, in, out, d2o, ido, gmeta, gval, nlines)
+                 : launch_envelope_t<PASS, int64_t>(c, in, out, d2o, ido, gmeta, gval, nlines);
 }
 
 }  // namespace
@@ -210,22 +183,25 @@ __global__ void __launch_bounds__(256) ft_envelope_kernel(const int64_t* __restr
 int run_ft(vc_ctx* c) {
     if (c->n_sites < 0) return VC_ERR_STATE;
     const int nvol = c->nvol;
-    int ncmax = 0;
+    int ncmax = 0, nmax = 0;
     for (int b = 0; b < nvol; ++b) {
         const int64_t NA = c->h_dims[3 * b] + 1, NB = c->h_dims[3 * b + 1] + 1, NC = c->h_dims[3 * b + 2] + 1;
         if (NA > 32767 || NB > 32767 || NC > 32767) return VC_ERR_ARG;
         ncmax = std::max<int>(ncmax, (int)NC);
+        nmax = std::max<int>(nmax, (int)std::max(NA, std::max(NB, NC)));
     }
+    const bool small = nmax <= 2048 && !c->ft_force_wide;
     const int64_t N = c->h_off[kLat][nvol];
     VC_TRY(ensure_n<int32_t>(c, c->ft_d2, N));
     VC_TRY(ensure_n<int32_t>(c, c->ft_id, N));
-    VC_TRY(ensure_n<int64_t>(c, c->ft_tmp, 2 * N));
+    VC_TRY(ensure_n<int64_t>(c, c->ft_tmp, 3 * N));
     Region stage(c, "stage_ft");
     int64_t* A = ptr<int64_t>(c->ft_tmp);
     int64_t* B = A + N;
+    int64_t* C = B + N;
     {
         const int warps_per_block = 8;
-        const size_t smem = (size_t)warps_per_block * ncmax * sizeof(int64_t);
+        const size_t smem = (size_t)warps_per_block * 2 * ncmax * sizeof(int32_t);
         if (smem > 200 * 1024) return VC_ERR_ARG;
         if (smem > 48 * 1024)
             VC_CUDA(c, cudaFuncSetAttribute(ft_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -239,27 +215,26 @@ int run_ft(vc_ctx* c) {
         VC_CUDA(c, cudaGetLastError());
     }
     {
-        // pass 2 along y; its envelope stacks (one int32 per lattice point)
-        // live in the d2 output, which pass 3 writes last
-        const int64_t nlines = c->h_off[kYLine][nvol];
-        int blocks = (int)std::min<int64_t>((nlines + 255) / 256, (int64_t)c->num_sms * 8);
+        // pass 2 along y: stack spills go to C (values) and to the d2
+        // output (positions), which pass 3 writes last
         Region r(c, "ft_envelope_y");
-        ft_envelope_kernel<2><<<blocks, 256, 0, c->stream>>>(A, B, nullptr, nullptr, ptr<int32_t>(c->ft_d2), c->tab);
-        launched(c);
-        VC_CUDA(c, cudaGetLastError());
+        VC_TRY(launch_envelope<2>(c, small, A, B, nullptr, nullptr, ptr<int32_t>(c->ft_d2), C, c->h_off[kYLine][nvol]));
     }
     {
-        // pass 3 along x; its stacks take the pass-1 buffer, dead by now
-        const int64_t nlines = c->h_off[kXLine][nvol];
-        int blocks = (int)std::min<int64_t>((nlines + 255) / 256, (int64_t)c->num_sms * 8);
+        // pass 3 along x: spills go to the pass-1 buffer A (values) and to C
+        // (positions), both dead by now
         Region r(c, "ft_envelope_x");
-        ft_envelope_kernel<3><<<blocks, 256, 0, c->stream>>>(B, nullptr, ptr<int32_t>(c->ft_d2), ptr<int32_t>(c->ft_id),
-                                                             reinterpret_cast<int32_t*>(A), c->tab);
-        launched(c);
-        VC_CUDA(c, cudaGetLastError());
+        VC_TRY(launch_envelope<3>(c, small, B, nullptr, ptr<int32_t>(c->ft_d2), ptr<int32_t>(c->ft_id),
+                                  reinterpret_cast<int32_t*>(C), A, c->h_off[kXLine][nvol]));
     }
     c->ft_valid = true;
     return VC_OK;
 }
 
 }  // namespace vc
+
+extern "C" int vc_debug_ft_wide(vc_ctx* c, int wide) {
+    if (!c) return VC_ERR_ARG;
+    c->ft_force_wide = wide != 0;
+    return VC_OK;
+}
