@@ -211,10 +211,12 @@ int vc_run_plain(vc_ctx* c, const uint8_t* occ, int X, int Y, int Z, int mem, do
     VC_TRY(vc_set_volume(c, occ, X, Y, Z, mem));
     VC_TRY(run_sites(c, &out->n_sites));
     VC_TRY(run_ft(c));
-    VC_TRY(run_lattice_vd(c, &out->vd, -1.0));
-    // highlevelalgo.cpp:836: float thresh = getInsidePartSize() * t (float * double -> float)
+    // the threshold (highlevelalgo.cpp:836: float thresh = getInsidePartSize()
+    // * t, float * double -> float) is computed on the device and folded into
+    // the thinning records as they are written
+    VC_TRY(run_lattice_vd(c, &out->vd, t));
     out->thresh = (float)((double)out->vd.inside_size * t);
-    VC_TRY(run_thin(c, out->thresh, out->thresh, &out->thin));
+    VC_TRY(run_thin_folded(c, &out->thin));
     VC_TRY(run_remaining(c, &out->rem));
     return sync_check(c);
 }

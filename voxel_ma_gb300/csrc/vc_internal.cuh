@@ -44,20 +44,28 @@ T* ptr(const DevBuf& b) {
 // one cell in one 32-byte DRAM sector (its accesses are random).
 constexpr int32_t kAlive = INT32_MAX;  // removal position of a cell still present
 // An edge's faces (a vertex's edges) still present, as one 64-bit word: their
-// count in the low kRefBits bits and the sum of their ids (mod 2^40) above.
-// Removing incident cell x subtracts (x << kRefBits) + 1 in one atomic; when
-// the count is 1 the sum is the id of the one cell left.
-constexpr int kRefBits = 24;
-constexpr unsigned long long kRefMask = (1ull << kRefBits) - 1ull;
-__host__ __device__ __forceinline__ unsigned long long rs_make(unsigned long long count, unsigned long long id_sum) {
-    return (id_sum << kRefBits) | count;
+// count in bits 0-15, how many of them pass the thinning filter (measure
+// below threshold) in bits 16-31, and the sum of their ids (mod 2^32) in
+// bits 32-63.  Removing incident cell x subtracts (x << 32) + (pass << 16) +
+// 1 in one atomic; when the count is 1 the sum is the id of the one cell
+// left and the pass field says whether it passes the filter.  Vertex words
+// leave the pass field at zero (their filter reads the edge record).
+constexpr int kRefBits = 16;
+constexpr unsigned long long kRefMask = (1ull << kRefBits) - 1ull;  // largest incidence count
+__host__ __device__ __forceinline__ unsigned long long rs_make(unsigned long long count, unsigned long long pass,
+                                                               unsigned long long id_sum) {
+    return (id_sum << 32) | ((pass & kRefMask) << 16) | count;
 }
-__host__ __device__ __forceinline__ unsigned long long rs_drop(int32_t id) {
-    return ~(((unsigned long long)(uint32_t)id << kRefBits) + 1ull) + 1ull;  // -(id << kRefBits) - 1
+__host__ __device__ __forceinline__ unsigned long long rs_drop(int32_t id, unsigned pass) {
+    return ~(((unsigned long long)(uint32_t)id << 32) + ((unsigned long long)pass << 16) + 1ull) + 1ull;
 }
 __host__ __device__ __forceinline__ int32_t rs_count(unsigned long long w) { return (int32_t)(w & kRefMask); }
-__host__ __device__ __forceinline__ int32_t rs_last(unsigned long long w) {
-    return (int32_t)(uint32_t)((w >> kRefBits) & 0xFFFFFFFFull);
+__host__ __device__ __forceinline__ int32_t rs_pass(unsigned long long w) { return (int32_t)((w >> 16) & kRefMask); }
+__host__ __device__ __forceinline__ int32_t rs_last(unsigned long long w) { return (int32_t)(uint32_t)(w >> 32); }
+// trig: the last decrement of a generation, as (queue position << 2 | slot),
+// slot = which of the decrementing item's cells this is (its child slot)
+__host__ __device__ __forceinline__ unsigned long long trig_make(int32_t pos, int slot) {
+    return ((unsigned long long)(uint32_t)pos << 2) | (unsigned)slot;
 }
 struct __align__(32) FaceRec {
     int32_t e0, e1, e2;  // edge ids of the sides, in face order
@@ -67,14 +75,16 @@ struct __align__(32) FaceRec {
 };
 struct __align__(32) EdgeRec {
     int32_t v0, v1;
-    unsigned long long rs;  // faces still present: count | id sum
+    unsigned long long rs;    // faces still present: count | pass | id sum
+    unsigned long long trig;  // last decrement: position << 2 | slot
     float em;
-    int32_t rm, trig, pad;
+    int32_t rm;
 };
 struct __align__(32) VertRec {
-    unsigned long long rs;  // edges still present: count | id sum
-    int32_t rm, trig;
-    int32_t pad0, pad1, pad2, pad3;
+    unsigned long long rs;    // edges still present: count | 0 | id sum
+    unsigned long long trig;  // last decrement: position << 2 | slot
+    int32_t rm;
+    int32_t pad0, pad1, pad2;
 };
 static_assert(sizeof(FaceRec) == 32 && sizeof(EdgeRec) == 32 && sizeof(VertRec) == 32, "record size");
 

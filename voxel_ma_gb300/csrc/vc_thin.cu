@@ -39,12 +39,15 @@
 // Memory layout: the accesses are random, so every cell's static data and
 // thinning state share one 32-byte record (one DRAM sector per touch):
 //   face   {e0, e1, e2, fm, rm}
-//   edge   {v0, v1, rs, em, rm, trig}
-//   vertex {rs, rm, trig}
-// rs packs the count of incident faces (edges) still present with the sum of
-// their ids: one atomic removes an incident cell, and when the count is 1
-// the sum names the remaining cell, so no incidence list is read while
-// thinning.
+//   edge   {v0, v1, rs, trig, em, rm}
+//   vertex {rs, trig, rm}
+// rs packs the count of incident faces (edges) still present, how many of
+// them pass the filter, and the sum of their ids: one atomic removes an
+// incident cell, and when the count is 1 the sum names the remaining cell
+// and (for an edge) the pass count says whether its child is pushed, so no
+// incidence list and no face record is read while thinning.  trig packs the
+// position of the last decrement with the slot of the cell in that item, so
+// the child's slot needs no per-item record of the decremented cells.
 #include "vc_internal.cuh"
 
 namespace vc {
@@ -61,7 +64,6 @@ struct ThinArgs {
     const float* thr;  // [0] f_t, [1] l_t
     int2* qa;
     int2* qb;
-    int4* cand;            // per item: the cells it decremented (-1 = none)
     int2* child;           // per item: up to 4 children, by slot
     unsigned* child_mask;  // per item one byte (4 items per word): bit s = child in slot s
     int32_t* cells;        // cells whose count reached 1 in this generation (kEdgeBit: edge)
@@ -86,16 +88,18 @@ __device__ __forceinline__ int2 make_ev(int32_t e, int32_t v) { return make_int2
 __device__ __forceinline__ bool is_fe(int2 it) { return ((unsigned)it.x & kFE) != 0; }
 __device__ __forceinline__ int32_t idx0(int2 it) { return (int32_t)((unsigned)it.x & ~kFE); }
 
-// Build the records from the finalized complex (CSR) and the measures, and
-// reset the thinning state.  A cell with 2^24 or more incident cells cannot
-// be represented (VC_ERR_ARG).
+// Build the records from the finalized complex (CSR), the measures and the
+// thresholds thr = {f_t, l_t}, and reset the thinning state.  A cell with
+// 2^16 or more incident cells cannot be represented (VC_ERR_ARG).
 __global__ void build_records_kernel(const int2* __restrict__ edges, const int32_t* __restrict__ tri_edges,
                                      const int32_t* __restrict__ ve_off, const int32_t* __restrict__ ve_ids,
                                      const int32_t* __restrict__ ef_off, const int32_t* __restrict__ ef_ids,
-                                     const float* __restrict__ em, const float* __restrict__ fm, int32_t nv,
-                                     int32_t ne, int32_t nt, FaceRec* F, EdgeRec* E, VertRec* V, int* err) {
+                                     const float* __restrict__ em, const float* __restrict__ fm,
+                                     const float* __restrict__ thr, int32_t nv, int32_t ne, int32_t nt, FaceRec* F,
+                                     EdgeRec* E, VertRec* V, int* err) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     const int64_t n = (int64_t)nv + ne + nt;
+    const float f_t = thr[0];
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         if (i < nt) {
             FaceRec r;
@@ -109,18 +113,21 @@ __global__ void build_records_kernel(const int2* __restrict__ edges, const int32
         } else if (i < (int64_t)nt + ne) {
             const int64_t e = i - nt;
             const int32_t o0 = ef_off[e], o1 = ef_off[e + 1];
-            unsigned long long idsum = 0;
-            for (int32_t k = o0; k < o1; ++k) idsum += (unsigned)ef_ids[k];
+            unsigned long long idsum = 0, pass = 0;
+            for (int32_t k = o0; k < o1; ++k) {
+                const int32_t f = ef_ids[k];
+                idsum += (unsigned)f;
+                pass += fm[f] < f_t ? 1u : 0u;
+            }
             if ((unsigned long long)(o1 - o0) > kRefMask) set_error(err, VC_ERR_ARG);
             EdgeRec r;
             const int2 ev = edges[e];
             r.v0 = ev.x;
             r.v1 = ev.y;
-            r.rs = rs_make((unsigned)(o1 - o0), idsum);
+            r.rs = rs_make((unsigned)(o1 - o0), pass, idsum);
+            r.trig = 0;
             r.em = em[e];
             r.rm = kAlive;
-            r.trig = -1;
-            r.pad = 0;
             E[e] = r;
         } else {
             const int64_t v = i - nt - ne;
@@ -129,10 +136,10 @@ __global__ void build_records_kernel(const int2* __restrict__ edges, const int32
             for (int32_t k = o0; k < o1; ++k) idsum += (unsigned)ve_ids[k];
             if ((unsigned long long)(o1 - o0) > kRefMask) set_error(err, VC_ERR_ARG);
             VertRec r;
-            r.rs = rs_make((unsigned)(o1 - o0), idsum);
+            r.rs = rs_make((unsigned)(o1 - o0), 0, idsum);
+            r.trig = 0;
             r.rm = kAlive;
-            r.trig = -1;
-            r.pad0 = r.pad1 = r.pad2 = r.pad3 = 0;
+            r.pad0 = r.pad1 = r.pad2 = 0;
             V[v] = r;
         }
     }
@@ -142,12 +149,12 @@ __global__ void build_records_kernel(const int2* __restrict__ edges, const int32
 // of vertices with one edge (vertex order), filtered by the thresholds.
 __global__ void gen0_flags_kernel(ThinArgs A, int32_t nv, int32_t ne, int32_t* __restrict__ flag) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    const float f_t = A.thr[0], l_t = A.thr[1];
+    const float l_t = A.thr[1];
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (int64_t)ne + nv; i += stride) {
         int32_t ok = 0;
         if (i < ne) {
             const unsigned long long rs = A.E[i].rs;
-            if (rs_count(rs) == 1) ok = A.F[rs_last(rs)].fm < f_t;
+            ok = rs_count(rs) == 1 && rs_pass(rs) == 1;
         } else {
             const unsigned long long rs = A.V[i - ne].rs;
             if (rs_count(rs) == 1) ok = A.E[rs_last(rs)].em < l_t;
@@ -228,30 +235,36 @@ __global__ void __launch_bounds__(kThreads) thin_generations_kernel(ThinArgs A) 
             if (i < n) {
                 const int2 it = __ldcg(cur + i);
                 const int32_t p = (int32_t)(base + i);
-                int4 cd = make_int4(-1, -1, -1, -1);
                 if (is_fe(it)) {
                     const int32_t f = idx0(it), e = it.y;
-                    const int32_t frm = __ldcg(&A.F[f].rm);
-                    const int32_t eref = rs_count(__ldcg(&A.E[e].rs));
+                    // both records in one round trip each
+                    const int4 fa = __ldcg(reinterpret_cast<const int4*>(A.F + f));
+                    const int4 fb = __ldcg(reinterpret_cast<const int4*>(A.F + f) + 1);
+                    const int4 ea = __ldcg(reinterpret_cast<const int4*>(A.E + e));
+                    const int4 eb = __ldcg(reinterpret_cast<const int4*>(A.E + e) + 1);
+                    const int32_t frm = fb.x;  // FaceRec: e0 e1 e2 fm | rm ...
+                    const unsigned long long ers =
+                        ((unsigned long long)(uint32_t)ea.w << 32) | (uint32_t)ea.z;  // EdgeRec: v0 v1 rs | trig em rm
                     if (frm != p) {
                         ++my_skipped;
-                    } else if (eref != 1) {
+                    } else if (rs_count(ers) != 1) {
                         set_error(A.err, VC_ERR_INVARIANT);
                     } else {
                         ++my_processed;
                         // the face's other two sides, in face order (the sides of a
                         // live face other than e are never removed)
-                        const int32_t s0 = A.F[f].e0, s1 = A.F[f].e1, s2 = A.F[f].e2;
+                        const int32_t s0 = fa.x, s1 = fa.y, s2 = fa.z;
                         const int32_t sa = s0 == e ? s1 : s0;
                         const int32_t sb = (s0 == e || s1 == e) ? s2 : s1;
-                        const int32_t v0 = A.E[e].v0, v1 = A.E[e].v1;
+                        const int32_t v0 = ea.x, v1 = ea.y;
+                        const float ffm = __int_as_float(fa.w);
                         atomicMin(&A.E[e].rm, p);
                         A.E[e].rs = 0;
-                        atomicMax(&A.E[sa].trig, p);
-                        atomicMax(&A.E[sb].trig, p);
-                        atomicMax(&A.V[v0].trig, p);
-                        atomicMax(&A.V[v1].trig, p);
-                        const unsigned long long df = rs_drop(f), de = rs_drop(e);
+                        atomicMax(&A.E[sa].trig, trig_make(p, 0));
+                        atomicMax(&A.E[sb].trig, trig_make(p, 1));
+                        atomicMax(&A.V[v0].trig, trig_make(p, 2));
+                        atomicMax(&A.V[v1].trig, trig_make(p, 3));
+                        const unsigned long long df = rs_drop(f, ffm < f_t ? 1u : 0u), de = rs_drop(e, 0u);
                         const int oa = rs_count(atomicAdd(&A.E[sa].rs, df));
                         const int ob = rs_count(atomicAdd(&A.E[sb].rs, df));
                         const int o0 = rs_count(atomicAdd(&A.V[v0].rs, de));
@@ -260,7 +273,6 @@ __global__ void __launch_bounds__(kThreads) thin_generations_kernel(ThinArgs A) 
                         if (ob == 2) one[1] = sb | kEdgeBit;
                         if (o0 == 2) one[2] = v0;
                         if (o1 == 2) one[3] = v1;
-                        cd = make_int4(sa, sb, v0, v1);
                     }
                 } else {
                     const int32_t e = it.x, v = it.y;
@@ -276,12 +288,10 @@ __global__ void __launch_bounds__(kThreads) thin_generations_kernel(ThinArgs A) 
                         const int32_t v0 = A.E[e].v0, v1 = A.E[e].v1;
                         const int32_t u = v0 != v ? v0 : v1;
                         A.V[v].rs = 0;
-                        atomicMax(&A.V[u].trig, p);
-                        if (rs_count(atomicAdd(&A.V[u].rs, rs_drop(e))) == 2) one[2] = u;
-                        cd.z = u;
+                        atomicMax(&A.V[u].trig, trig_make(p, 2));
+                        if (rs_count(atomicAdd(&A.V[u].rs, rs_drop(e, 0u))) == 2) one[2] = u;
                     }
                 }
-                __stcg(A.cand + i, cd);
             }
 #pragma unroll
             for (int q = 0; q < 4; ++q) append_cell(s_cells, &s_ncell, one[q] != -1, one[q]);
@@ -304,28 +314,28 @@ __global__ void __launch_bounds__(kThreads) thin_generations_kernel(ThinArgs A) 
             const int64_t j1 = min(m, ((int64_t)b + 1) * mchunk);
             for (int64_t j = (int64_t)b * mchunk + threadIdx.x; j < j1; j += blockDim.x) {
                 const int32_t code = __ldcg(A.cells + j);
-                int64_t i;
-                int slot;
+                unsigned long long tg;
                 int2 ch;
                 if (code & kEdgeBit) {
                     const int32_t e2 = code & ~kEdgeBit;
-                    const unsigned long long rs = __ldcg(&A.E[e2].rs);
-                    if (rs_count(rs) != 1) continue;
-                    i = (int64_t)__ldcg(&A.E[e2].trig) - base;
-                    const int32_t f2 = rs_last(rs);
-                    if (!(A.F[f2].fm < f_t)) continue;
-                    slot = __ldcg(&A.cand[i].x) == e2 ? 0 : 1;
-                    ch = make_fe(f2, e2);
+                    const int4 ea = __ldcg(reinterpret_cast<const int4*>(A.E + e2));
+                    const int4 eb = __ldcg(reinterpret_cast<const int4*>(A.E + e2) + 1);
+                    const unsigned long long rs = ((unsigned long long)(uint32_t)ea.w << 32) | (uint32_t)ea.z;
+                    if (rs_count(rs) != 1 || rs_pass(rs) != 1) continue;
+                    tg = ((unsigned long long)(uint32_t)eb.y << 32) | (uint32_t)eb.x;
+                    ch = make_fe(rs_last(rs), e2);
                 } else {
                     const int32_t u = code;
-                    const unsigned long long rs = __ldcg(&A.V[u].rs);
+                    const int4 va = __ldcg(reinterpret_cast<const int4*>(A.V + u));  // rs | trig
+                    const unsigned long long rs = ((unsigned long long)(uint32_t)va.y << 32) | (uint32_t)va.x;
                     if (rs_count(rs) != 1) continue;
-                    i = (int64_t)__ldcg(&A.V[u].trig) - base;
                     const int32_t e3 = rs_last(rs);
                     if (!(A.E[e3].em < l_t)) continue;
-                    slot = __ldcg(&A.cand[i].z) == u ? 2 : 3;
+                    tg = ((unsigned long long)(uint32_t)va.w << 32) | (uint32_t)va.z;
                     ch = make_ev(e3, u);
                 }
+                const int64_t i = (int64_t)(tg >> 2) - base;
+                const int slot = (int)(tg & 3u);
                 if (i < 0 || i >= n) {
                     set_error(A.err, VC_ERR_INVARIANT);
                     continue;
@@ -482,7 +492,6 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats) {
     }
     VC_TRY(ensure_n<int2>(c, c->q0, qcap));
     VC_TRY(ensure_n<int2>(c, c->q1, qcap));
-    VC_TRY(ensure_n<int4>(c, c->cand, qcap));
     VC_TRY(ensure_n<int2>(c, c->child, 4 * qcap));
     VC_TRY(ensure_n<unsigned>(c, c->child_cnt, qcap / 4 + 2));  // child masks
     VC_TRY(ensure_n<int32_t>(c, c->cells, 4 * qcap));
@@ -499,7 +508,6 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats) {
     A.thr = ptr<float>(c->thr);
     A.qa = ptr<int2>(c->q0);
     A.qb = ptr<int2>(c->q1);
-    A.cand = ptr<int4>(c->cand);
     A.child = ptr<int2>(c->child);
     A.child_mask = ptr<unsigned>(c->child_cnt);
     A.cells = ptr<int32_t>(c->cells);
@@ -522,8 +530,8 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats) {
         } else {
             build_records_kernel<<<grid_for(c, nv + ne + nt, 256), 256, 0, c->stream>>>(
                 ptr<int2>(c->edges), ptr<int32_t>(c->tri_edges), ptr<int32_t>(c->ve_off), ptr<int32_t>(c->ve_ids),
-                ptr<int32_t>(c->ef_off), ptr<int32_t>(c->ef_ids), ptr<float>(c->em), ptr<float>(c->fm), (int32_t)nv,
-                (int32_t)ne, (int32_t)nt, A.F, A.E, A.V, dev_err(c));
+                ptr<int32_t>(c->ef_off), ptr<int32_t>(c->ef_ids), ptr<float>(c->em), ptr<float>(c->fm), A.thr,
+                (int32_t)nv, (int32_t)ne, (int32_t)nt, A.F, A.E, A.V, dev_err(c));
             launched(c);
         }
         int32_t* flag = ptr<int32_t>(c->scratch2);

@@ -420,14 +420,16 @@ __global__ void vd_vertices_kernel(const uint8_t* __restrict__ occ, const int32_
             }
             sort_small<6>(dg, nd);
             for (int i = 0; i < nd; ++i) ve_ids[off + k++] = (int32_t)sh.eb1 + dg[i];
-            unsigned long long idsum = 0;
-            for (int q = 0; q < k; ++q) idsum += (unsigned)ve_ids[off + q];
-            VertRec r;
-            r.rs = rs_make((unsigned)k, idsum);
-            r.rm = kAlive;
-            r.trig = -1;
-            r.pad0 = r.pad1 = r.pad2 = r.pad3 = 0;
-            V[v] = r;
+            if (V) {
+                unsigned long long idsum = 0;
+                for (int q = 0; q < k; ++q) idsum += (unsigned)ve_ids[off + q];
+                VertRec r;
+                r.rs = rs_make((unsigned)k, 0, idsum);
+                r.trig = 0;
+                r.rm = kAlive;
+                r.pad0 = r.pad1 = r.pad2 = 0;
+                V[v] = r;
+            }
             // the volume's bounding box: lanes of the same volume reduce in
             // the warp first, so each warp issues one set of atomics per volume
             const unsigned grp = __match_any_sync(__activemask(), bv);
@@ -481,8 +483,12 @@ __global__ void vd_edges_kernel(const uint8_t* __restrict__ occ, const int32_t* 
         const int k = plaquette_faces(g, flags, a, b, c, d, inc);
         float m = 0.0f;
         int32_t tl[4];
+        unsigned npass = 0;  // incident triangles that pass the thinning filter
+        const float tb = thr ? thr[bv] : 0.0f;
         for (int j = 0; j < k; ++j) {
-            m = fmaxf(m, lam[3 * inc[j].lp + inc[j].axis]);
+            const float lj = lam[3 * inc[j].lp + inc[j].axis];
+            m = fmaxf(m, lj);
+            npass += lj < tb ? 1u : 0u;
             tl[j] = 2 * face_id(flags, o, inc[j].lp, inc[j].axis) + inc[j].tri;
         }
         sort_small<4>(tl, k);
@@ -490,17 +496,18 @@ __global__ void vd_edges_kernel(const uint8_t* __restrict__ occ, const int32_t* 
         for (int j = 0; j < k; ++j) ef_ids[efo + j] = tl[j];
         edges[e] = make_int2(v0, v1);
         em[e] = m;
-        unsigned long long idsum = 0;
-        for (int j = 0; j < k; ++j) idsum += (unsigned)tl[j];
-        EdgeRec r;
-        r.v0 = v0;
-        r.v1 = v1;
-        r.rs = rs_make((unsigned)k, idsum);
-        r.em = rec_measure(m, thr, bv);
-        r.rm = kAlive;
-        r.trig = -1;
-        r.pad = 0;
-        E[e] = r;
+        if (thr) {
+            unsigned long long idsum = 0;
+            for (int j = 0; j < k; ++j) idsum += (unsigned)tl[j];
+            EdgeRec r;
+            r.v0 = v0;
+            r.v1 = v1;
+            r.rs = rs_make((unsigned)k, npass, idsum);
+            r.trig = 0;
+            r.em = rec_measure(m, thr, bv);
+            r.rm = kAlive;
+            E[e] = r;
+        }
     }
 }
 
@@ -568,6 +575,7 @@ __global__ void vd_faces_kernel(const uint8_t* __restrict__ occ, const int32_t* 
                 tri_face[t0] = f - fbs;
                 tri_face[t1] = f - fbs;
                 face_sites[f] = make_int2(s0 - (int32_t)sh.site, s1 - (int32_t)sh.site);
+                if (thr) {
                 const float lr = rec_measure(lm, thr, bv);
                 FaceRec fr;
                 fr.fm = lr;
@@ -581,6 +589,7 @@ __global__ void vd_faces_kernel(const uint8_t* __restrict__ occ, const int32_t* 
                 fr.e1 = e12;
                 fr.e2 = e32;
                 F[t1] = fr;
+                }
                 // the diagonal: new edge of this face, incident to both triangles
                 const int32_t dv0 = min(q[1], q[3]), dv1 = max(q[1], q[3]);
                 const int32_t efo = (int32_t)sh.efb1 + 2 * f;
@@ -589,15 +598,16 @@ __global__ void vd_faces_kernel(const uint8_t* __restrict__ occ, const int32_t* 
                 ef_off[diag] = efo;
                 ef_ids[efo] = (int32_t)t0;
                 ef_ids[efo + 1] = (int32_t)t1;
-                EdgeRec er;
-                er.v0 = dv0;
-                er.v1 = dv1;
-                er.rs = rs_make(2, (unsigned long long)t0 + (unsigned long long)t1);
-                er.em = lr;
-                er.rm = kAlive;
-                er.trig = -1;
-                er.pad = 0;
-                E[diag] = er;
+                if (thr) {
+                    EdgeRec er;
+                    er.v0 = dv0;
+                    er.v1 = dv1;
+                    er.rs = rs_make(2, lm < thr[bv] ? 2u : 0u, (unsigned long long)t0 + (unsigned long long)t1);
+                    er.trig = 0;
+                    er.em = rec_measure(lm, thr, bv);
+                    er.rm = kAlive;
+                    E[diag] = er;
+                }
             }
         }
     }
@@ -784,7 +794,8 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes, double t_thr) {
             Region k(c, "vd_vertices");
             vd_vertices_kernel<<<cell_grid(c, nv), 256, 0, c->stream>>>(
                 occ, lab, c->tab, c->bases, flags, o, lam, ptr<int64_t>(c->vd_vpos), (int32_t)nv, ptr<float>(c->vts),
-                ptr<float>(c->vm), ptr<int32_t>(c->ve_off), ptr<int32_t>(c->ve_ids), ptr<VertRec>(c->vert_rec));
+                ptr<float>(c->vm), ptr<int32_t>(c->ve_off), ptr<int32_t>(c->ve_ids),
+                thr ? ptr<VertRec>(c->vert_rec) : nullptr);
             launched(c);
             inside_size_kernel<<<(nvol + 255) / 256, 256, 0, c->stream>>>(c->bases, nvol, t_thr);
             launched(c);
@@ -824,7 +835,9 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes, double t_thr) {
     c->cc_valid = true;
     c->cc_finalized = true;
     c->meas_valid = true;
-    c->records_fresh = true;
+    // records are written only with the thresholds folded in (their filter
+    // counts need the thresholds); otherwise the thinning builds them
+    c->records_fresh = t_thr >= 0.0;
     c->records_thr_folded = t_thr >= 0.0;
     c->cc_batched = nvol > 1;
     if (sizes) *sizes = c->vd;
