@@ -96,7 +96,7 @@ static_assert(sizeof(FaceRec) == 32 && sizeof(EdgeRec) == 32 && sizeof(VertRec) 
 // along z, lattice lines along y and along x) the table holds the start of
 // every volume and, at index nvol, the total.  With one volume nothing is
 // read from memory: the starts follow from the dims held in the table.
-enum Space : int { kVox = 0, kLat, kVRow, kLRow, kYLine, kXLine, kNumSpaces };
+enum Space : int { kVox = 0, kLat, kVRow, kLRow, kYLine, kXLine, kVWord, kNumSpaces };
 
 __host__ __device__ __forceinline__ int64_t space_size(int s, int X, int Y, int Z) {
     const int64_t x = X, y = Y, z = Z;
@@ -106,7 +106,8 @@ __host__ __device__ __forceinline__ int64_t space_size(int s, int X, int Y, int 
         case kVRow: return x * y;
         case kLRow: return (x + 1) * (y + 1);
         case kYLine: return (x + 1) * (z + 1);
-        default: return (y + 1) * (z + 1);
+        case kXLine: return (y + 1) * (z + 1);
+        default: return x * y * ((z + 31) / 32);  // kVWord: 32-voxel words of the z-rows
     }
 }
 
@@ -179,7 +180,8 @@ struct vc_ctx {
     // sites
     int64_t n_sites = -1;
     vc::DevBuf site_xyz;    // float3 per site
-    vc::DevBuf site_count;  // int32 per-voxel new-corner counts, then offsets
+    vc::DevBuf site_count;  // int32 per-word new-corner counts, then offsets
+    vc::DevBuf site_bits;   // uint32 per 32-voxel word of a z-row: packed occupancy
     vc::DevBuf site_id_lat; // int32 per lattice point: site id or -1
     // feature transform
     bool ft_valid = false;
@@ -214,7 +216,7 @@ struct vc_ctx {
     vc::DevBuf face_rec, edge_rec, vert_rec;  // 32-byte per-cell thinning records
     bool records_fresh = false;               // records already hold this complex in reset state
     bool records_thr_folded = false;          // ... with the per-volume thresholds folded in (threshold 0)
-    vc::DevBuf q0, q1, cand, child, child_cnt, cells, blk_cnt, thr;
+    vc::DevBuf q0, q1, child, child_cnt, cells, blk_cnt, thr;
     vc::DevBuf keep_v, keep_e, keep_f, removed_e;  // uint8 survivor flags of the last thinning
     vc::DevBuf trace;           // optional per-generation trace of the thinning kernel
     int trace_cap = 0, trace_gens = 0;

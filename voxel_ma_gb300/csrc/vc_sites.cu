@@ -9,8 +9,16 @@
 // the first (direction, corner slot) that names it.  Each thread decides this
 // per voxel from the voxel's 3x3x3 neighbourhood, so the site list comes out
 // in the reference's order after one exclusive scan of per-voxel counts.
+//
+// The main path evaluates the rule for 32 voxels of a z-row at once
+// (vc_sites_words.cuh): the occupancy is packed to one bit per voxel (a
+// 512^3 volume becomes 16 MB, resident in L2), one thread per word counts
+// the word's new corners, a scan of the word counts numbers the sites, and
+// one thread per word writes them.  The per-voxel kernels below the word
+// kernels serve the allocation-free entry point.
 #include "vc_internal.cuh"
 #include "vc_scan.cuh"
+#include "vc_sites_words.cuh"
 
 #include <mutex>
 
@@ -155,6 +163,85 @@ __global__ void sites_emit_kernel(const uint8_t* __restrict__ occ, VolTab T, con
     }
 }
 
+// Pack the occupancy: one warp per voxel row (volume b, x, y), one ballot
+// per 32 voxels; bits past the row's end are 0.
+__global__ void sites_pack_kernel(const uint8_t* __restrict__ occ, VolTab T, uint32_t* __restrict__ bits) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    const int64_t nrows = T.total(kVRow);
+    for (int64_t row = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); row < nrows; row += warps) {
+        const int bv = T.find(kVRow, row);
+        const int Z = T.dim(bv).z;
+        const int Wz = (Z + 31) / 32;
+        const int64_t r = row - T.start(kVRow, bv);
+        const uint8_t* src = occ + T.start(kVox, bv) + r * Z;
+        uint32_t* dst = bits + T.start(kVWord, bv) + r * Wz;
+        for (int w = 0; w < Wz; ++w) {
+            const int k = 32 * w + lane;
+            const bool in = k < Z && __ldcs(src + k) > 0;
+            const uint32_t word = __ballot_sync(0xffffffffu, in);
+            if (lane == 0) dst[w] = word;
+        }
+    }
+}
+
+struct WordPos {
+    int bv, i, j, w;
+    int4 d;
+};
+__device__ __forceinline__ WordPos word_pos(const VolTab& T, int64_t gw) {
+    WordPos p;
+    p.bv = T.find(kVWord, gw);
+    p.d = T.dim(p.bv);
+    const uint32_t Wz = (uint32_t)((p.d.z + 31) / 32);
+    const uint64_t lw = (uint64_t)(gw - T.start(kVWord, p.bv));
+    const uint64_t row = lw / Wz;
+    p.w = (int)(lw - row * Wz);
+    p.i = (int)(row / (uint64_t)p.d.y);
+    p.j = (int)(row - (uint64_t)p.i * p.d.y);
+    return p;
+}
+
+// One thread per word: its count of new corners.
+__global__ void __launch_bounds__(256) sites_wcount_kernel(const uint32_t* __restrict__ bits, VolTab T,
+                                                           int32_t* __restrict__ cnt) {
+    const int64_t n = T.total(kVWord);
+    for (int64_t gw = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; gw < n; gw += (int64_t)gridDim.x * blockDim.x) {
+        const WordPos p = word_pos(T, gw);
+        const uint32_t Wz = (uint32_t)((p.d.z + 31) / 32);
+        const uint32_t* vb = bits + T.start(kVWord, p.bv);
+        auto word = [&](int ii, int jj, int ww) { return __ldg(vb + ((int64_t)ii * p.d.y + jj) * Wz + ww); };
+        SiteWords r;
+        site_words(word, p.i, p.j, p.w, p.d.x, p.d.y, p.d.z, r);
+        cnt[gw] = site_word_count(r);
+    }
+}
+
+// One thread per word: its sites at their batch-wide indices (volume b's
+// sites are the contiguous range starting at its first site, in the
+// reference's order) and each site's index at its lattice point.
+__global__ void __launch_bounds__(256) sites_wemit_kernel(const uint32_t* __restrict__ bits, VolTab T,
+                                                          const int32_t* __restrict__ off, float* __restrict__ xyz,
+                                                          int32_t* __restrict__ site_id_lat) {
+    const int64_t n = T.total(kVWord);
+    for (int64_t gw = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; gw < n; gw += (int64_t)gridDim.x * blockDim.x) {
+        const WordPos p = word_pos(T, gw);
+        const uint32_t Wz = (uint32_t)((p.d.z + 31) / 32);
+        const uint32_t* vb = bits + T.start(kVWord, p.bv);
+        auto word = [&](int ii, int jj, int ww) { return __ldg(vb + ((int64_t)ii * p.d.y + jj) * Wz + ww); };
+        SiteWords r;
+        site_words(word, p.i, p.j, p.w, p.d.x, p.d.y, p.d.z, r);
+        const int64_t NB = p.d.y + 1, NC = p.d.z + 1;
+        int32_t* lat = site_id_lat + T.start(kLat, p.bv);
+        site_word_emit(r, p.i, p.j, p.w, (int64_t)off[gw], [&](int64_t o, int a, int b, int c) {
+            xyz[3 * o + 0] = (float)a - 0.5f;
+            xyz[3 * o + 1] = (float)b - 0.5f;
+            xyz[3 * o + 2] = (float)c - 0.5f;
+            lat[((int64_t)a * NB + b) * NC + c] = (int32_t)o;
+        });
+    }
+}
+
 inline int row_grid(int num_sms, int64_t rows) {
     return (int)std::max<int64_t>(1, std::min<int64_t>(rows, (int64_t)num_sms * 32));
 }
@@ -164,30 +251,41 @@ inline int row_grid(int num_sms, int64_t rows) {
 
 int run_sites(vc_ctx* c, int64_t* n_sites) {
     if (!c->occ.p || c->nvol <= 0) return VC_ERR_STATE;
-    const int64_t nvox = c->h_off[kVox][c->nvol];
     const int64_t nlat = c->h_off[kLat][c->nvol];
     const int64_t nrows = c->h_off[kVRow][c->nvol];
-    VC_TRY(ensure_n<int32_t>(c, c->site_count, nvox));
+    const int64_t nwords = c->h_off[kVWord][c->nvol];
+    VC_TRY(ensure_n<uint32_t>(c, c->site_bits, nwords));
+    VC_TRY(ensure_n<int32_t>(c, c->site_count, nwords));
     VC_TRY(ensure_n<int32_t>(c, c->site_id_lat, nlat));
     VC_TRY(ensure_n<int64_t>(c, c->scratch2, 4));
     Region stage(c, "stage_sites");
-    const uint8_t* occ = ptr<uint8_t>(c->occ);
+    uint32_t* bits = ptr<uint32_t>(c->site_bits);
     int32_t* cnt = ptr<int32_t>(c->site_count);
-    sites_count_kernel<<<row_grid(c->num_sms, nrows), 128, 0, c->stream>>>(occ, c->tab, cnt);
-    launched(c);
-    VC_CUDA(c, cudaGetLastError());
+    const int wgrid = (int)std::max<int64_t>(1, std::min<int64_t>((nwords + 255) / 256, (int64_t)c->num_sms * 8));
+    {
+        Region r(c, "sites_count");
+        sites_pack_kernel<<<(int)std::max<int64_t>(1, std::min<int64_t>((nrows + 7) / 8, (int64_t)c->num_sms * 16)),
+                            256, 0, c->stream>>>(ptr<uint8_t>(c->occ), c->tab, bits);
+        launched(c);
+        sites_wcount_kernel<<<wgrid, 256, 0, c->stream>>>(bits, c->tab, cnt);
+        launched(c);
+        VC_CUDA(c, cudaGetLastError());
+    }
     int64_t* total = ptr<int64_t>(c->scratch2);
-    VC_TRY(scan_exclusive_i32(c, cnt, cnt, nvox, total));
-    VC_TRY(fill_bases(c, kBSite, kVox, cnt, total));
+    VC_TRY(scan_exclusive_i32(c, cnt, cnt, nwords, total));
+    VC_TRY(fill_bases(c, kBSite, kVWord, cnt, total));
     int64_t n = 0;
     VC_TRY(read_i64(c, total, &n));
     if (n > INT32_MAX) return VC_ERR_ARG;
     VC_TRY(ensure_n<float>(c, c->site_xyz, 3 * n));
-    VC_CUDA(c, cudaMemsetAsync(c->site_id_lat.p, 0xff, (size_t)nlat * sizeof(int32_t), c->stream));
-    sites_emit_kernel<<<row_grid(c->num_sms, nrows), 128, 0, c->stream>>>(occ, c->tab, cnt, ptr<float>(c->site_xyz),
-                                                                         ptr<int32_t>(c->site_id_lat));
-    launched(c);
-    VC_CUDA(c, cudaGetLastError());
+    {
+        Region r(c, "sites_emit");
+        VC_CUDA(c, cudaMemsetAsync(c->site_id_lat.p, 0xff, (size_t)nlat * sizeof(int32_t), c->stream));
+        sites_wemit_kernel<<<wgrid, 256, 0, c->stream>>>(bits, c->tab, cnt, ptr<float>(c->site_xyz),
+                                                        ptr<int32_t>(c->site_id_lat));
+        launched(c);
+        VC_CUDA(c, cudaGetLastError());
+    }
     c->n_sites = n;
     if (n_sites) *n_sites = n;
     return VC_OK;
