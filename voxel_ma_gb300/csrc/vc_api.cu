@@ -8,6 +8,7 @@ namespace vc {
 int run_sites(vc_ctx* c, int64_t* n_sites);
 int run_ft(vc_ctx* c);
 int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes, double t_thr);
+int ensure_vd_aux(vc_ctx* c, bool meas, bool topo);
 int run_vertex_radii(vc_ctx* c);
 int run_finalize(vc_ctx* c, int64_t* ne_final);
 int build_adjacency(vc_ctx* c);
@@ -91,6 +92,7 @@ int vc_get_vd(vc_ctx* c, float* vts, int32_t* edges, int32_t* tris, int32_t* tri
     VC_TRY(enter(c));
     if (!c->vd_valid) return VC_ERR_STATE;
     if (!good_mem(mem)) return VC_ERR_ARG;
+    VC_TRY(ensure_vd_aux(c, true, false));
     const vc_vd_sizes& s = c->vd;
     VC_TRY(copy_out(c, vts, c->vts.p, (size_t)s.nv * 3 * sizeof(float), mem));
     VC_TRY(copy_out(c, edges, c->edges.p, (size_t)s.ne * 2 * sizeof(int32_t), mem));
@@ -146,6 +148,7 @@ int vc_get_finalized(vc_ctx* c, int32_t* edges, int32_t* tri_edges, int32_t* ve_
     VC_TRY(enter(c));
     if (!c->cc_finalized) return VC_ERR_STATE;
     if (!good_mem(mem)) return VC_ERR_ARG;
+    VC_TRY(ensure_vd_aux(c, false, true));
     VC_TRY(copy_out(c, edges, c->edges.p, (size_t)c->ne * 2 * sizeof(int32_t), mem));
     VC_TRY(copy_out(c, tri_edges, c->tri_edges.p, (size_t)c->nt * 3 * sizeof(int32_t), mem));
     VC_TRY(copy_out(c, ve_off, c->ve_off.p, (size_t)(c->nv + 1) * sizeof(int32_t), mem));
@@ -162,9 +165,13 @@ int vc_set_measures(vc_ctx* c, const float* vm, const float* em, const float* fm
     VC_TRY(ensure_n<float>(c, c->vm, c->nv));
     VC_TRY(ensure_n<float>(c, c->em, c->ne));
     VC_TRY(ensure_n<float>(c, c->fm, c->nt));
+    // a lattice complex's own measures are written first, so that a missing
+    // vm keeps the lattice's values
+    if (!vm) VC_TRY(ensure_vd_aux(c, true, false));
     if (vm) VC_TRY(copy_in(c, c->vm.p, vm, (size_t)c->nv * sizeof(float), mem));
     VC_TRY(copy_in(c, c->em.p, em, (size_t)c->ne * sizeof(float), mem));
     VC_TRY(copy_in(c, c->fm.p, fm, (size_t)c->nt * sizeof(float), mem));
+    c->vd_aux_meas = true;  // the caller's measures: never overwritten by the lattice's
     c->meas_valid = true;
     c->records_fresh = false;
     c->thin_valid = c->rem_valid = false;

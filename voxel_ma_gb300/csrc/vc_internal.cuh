@@ -96,7 +96,7 @@ static_assert(sizeof(FaceRec) == 32 && sizeof(EdgeRec) == 32 && sizeof(VertRec) 
 // along z, lattice lines along y and along x) the table holds the start of
 // every volume and, at index nvol, the total.  With one volume nothing is
 // read from memory: the starts follow from the dims held in the table.
-enum Space : int { kVox = 0, kLat, kVRow, kLRow, kYLine, kXLine, kVWord, kNumSpaces };
+enum Space : int { kVox = 0, kLat, kVRow, kLRow, kYLine, kXLine, kVWord, kLSeg, kNumSpaces };
 
 __host__ __device__ __forceinline__ int64_t space_size(int s, int X, int Y, int Z) {
     const int64_t x = X, y = Y, z = Z;
@@ -107,7 +107,8 @@ __host__ __device__ __forceinline__ int64_t space_size(int s, int X, int Y, int 
         case kLRow: return (x + 1) * (y + 1);
         case kYLine: return (x + 1) * (z + 1);
         case kXLine: return (y + 1) * (z + 1);
-        default: return x * y * ((z + 31) / 32);  // kVWord: 32-voxel words of the z-rows
+        case kVWord: return x * y * ((z + 31) / 32);  // 32-voxel words of the voxel rows
+        default: return (x + 1) * (y + 1) * ((z + 32) / 32);  // kLSeg: 32-point segments of the lattice rows
     }
 }
 
@@ -190,9 +191,11 @@ struct vc_ctx {
     // lattice Voronoi complex
     bool vd_valid = false;
     vc_vd_sizes vd{};
-    vc::DevBuf vd_flags;              // uint8 per lattice point
-    vc::DevBuf vd_voff, vd_eoff, vd_foff;  // int32 exclusive offsets per lattice point
-    vc::DevBuf vd_tri_face, vd_face_sites, vd_vm, vd_lam, vd_efoff, vd_veoff, vd_vpos, vd_epos, vd_fpos;
+    vc::DevBuf vd_seg;                     // per 32-point lattice segment: 7 cell bit planes (32 bytes)
+    vc::DevBuf vd_voff, vd_eoff, vd_foff;  // int32 per segment: cell counts, then first cell ids
+    vc::DevBuf vd_tri_face, vd_face_sites, vd_lam;
+    bool vd_aux_meas = false;  // vm, em, fm, tri_face, face_sites of the lattice complex written
+    bool vd_aux_topo = false;  // tri_edges and the V->E / E->F lists of the lattice complex written
     vc::DevBuf vd_radius;             // float per vertex of the lattice complex
     std::vector<float> vol_inside;  // inside-part size per volume
     bool cc_batched = false;        // the complex is the lattice complex of a batch of > 1 volumes

@@ -75,10 +75,9 @@ __global__ void rem_write_kernel(const uint8_t* __restrict__ kv, const uint8_t* 
 }
 
 // Euler: mark every finalized edge that is a remaining edge or a side of a
-// remaining face.
+// remaining face (the sides are read from the thinning's face records).
 __global__ void euler_mark_kernel(const uint8_t* __restrict__ ke, const uint8_t* __restrict__ kf,
-                                  const int32_t* __restrict__ tri_edges, int32_t ne, int32_t nt,
-                                  int32_t* __restrict__ mark) {
+                                  const FaceRec* __restrict__ F, int32_t ne, int32_t nt, int32_t* __restrict__ mark) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (int64_t)ne + nt; i += stride) {
         if (i < ne) {
@@ -86,9 +85,10 @@ __global__ void euler_mark_kernel(const uint8_t* __restrict__ ke, const uint8_t*
         } else {
             const int64_t f = i - ne;
             if (!kf[f]) continue;
-            mark[tri_edges[3 * f + 0]] = 1;
-            mark[tri_edges[3 * f + 1]] = 1;
-            mark[tri_edges[3 * f + 2]] = 1;
+            const int4 sides = __ldg(reinterpret_cast<const int4*>(F + f));
+            mark[sides.x] = 1;
+            mark[sides.y] = 1;
+            mark[sides.z] = 1;
         }
     }
 }
@@ -230,7 +230,7 @@ int run_euler_remaining(vc_ctx* c, vc_euler_info* out) {
     VC_CUDA(c, cudaMemsetAsync(mark, 0, (ne + 1) * sizeof(int32_t), c->stream));
     VC_CUDA(c, cudaMemsetAsync(cnt, 0, 2 * (size_t)nmap * sizeof(unsigned long long), c->stream));
     euler_mark_kernel<<<grid_for(c, ne + nt, 256), 256, 0, c->stream>>>(
-        ptr<uint8_t>(c->keep_e), ptr<uint8_t>(c->keep_f), ptr<int32_t>(c->tri_edges), (int32_t)ne, (int32_t)nt,
+        ptr<uint8_t>(c->keep_e), ptr<uint8_t>(c->keep_f), ptr<FaceRec>(c->face_rec), (int32_t)ne, (int32_t)nt,
         mark);
     launched(c);
     count_kernel<<<grid_for(c, ne, 256), 256, 0, c->stream>>>(mark, ptr<int2>(c->edges), ne, cnt, c->bases, nmap);

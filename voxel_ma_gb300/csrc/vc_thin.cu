@@ -451,6 +451,7 @@ inline int grid_for(vc_ctx* c, int64_t n, int threads) {
 }  // namespace
 
 int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats);
+int ensure_vd_aux(vc_ctx* c, bool meas, bool topo);
 
 int run_thin(vc_ctx* c, float f_t, float l_t, vc_thin_stats* stats) {
     if (!c->cc_finalized || !c->meas_valid) return VC_ERR_STATE;
@@ -486,6 +487,8 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats) {
     const int64_t qcap = nv + ne + 1;
     Region stage(c, "stage_thin");
     if (!c->records_fresh) {
+        // the records are built from the measures, sides and lists
+        VC_TRY(ensure_vd_aux(c, true, true));
         VC_TRY(ensure_n<FaceRec>(c, c->face_rec, nt));
         VC_TRY(ensure_n<EdgeRec>(c, c->edge_rec, ne));
         VC_TRY(ensure_n<VertRec>(c, c->vert_rec, nv));
