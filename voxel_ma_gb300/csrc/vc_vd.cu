@@ -203,52 +203,19 @@ __device__ __forceinline__ float rec_measure(float m, const float* thr, int bv) 
     return m < thr[bv] ? -1.0f : 1.0f;
 }
 
-// The valid faces of the plaquette shared by voxel (a,b,c) and its +d
-// neighbour (the faces of the axis edge (a,b,c)+d): lattice edges along u
-// from nb + j e_w (j = 0, 1) and along w from nb + (j-2) e_u (j = 2, 3),
-// nb = (a,b,c) + e_d.  For each: lattice point, axis and which of the face's
-// two triangles carries the edge (0: (q3,q0,q1), 1: (q3,q1,q2)).
-struct Inc {
-    int x[3];
-    int axis;
-    int tri;
-};
-__device__ __forceinline__ int plaquette_faces(const Segs& S, int a, int b, int c, int d, Inc out[4]) {
-    const int u = (d + 1) % 3, w = (d + 2) % 3;
-    const int v[3] = {a, b, c};
-    int nb[3] = {a, b, c};
-    nb[d] += 1;
-    int k = 0;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        int cc[3] = {nb[0], nb[1], nb[2]};
-        const int ax = j < 2 ? u : w;
-        if (j < 2) cc[w] += j;
-        else cc[u] += j - 2;
-        if (!fbit_at(S, cc[0], cc[1], cc[2], ax)) continue;
-        // position (s,t) of the edge's lower voxel in the face's quad
-        const int u2 = (ax + 1) % 3, w2 = (ax + 2) % 3;
-        const int s = v[u2] - (cc[u2] - 1), t = v[w2] - (cc[w2] - 1);
-        const int tri = d == u2 ? (t == 0 ? 0 : 1) : (s == 0 ? 0 : 1);
-        out[k++] = Inc{{cc[0], cc[1], cc[2]}, ax, tri};
-    }
-    return k;
-}
-
 // Per lattice point: whether its voxel is a vertex (inside, not all 8
 // corner labels equal -- tagVert plus "corner of some Voronoi face"),
 // whether each axis edge is valid (both voxels inside, the shared square's
 // 4 labels not all equal) and whether each lattice edge carries a valid
-// face (labels differ and the 4 voxels around it inside), with the face's
-// lambda; ballots make the segment's planes.  Also the volumes' vertex
+// face (labels differ and the 4 voxels around it inside); ballots make the
+// segment's planes.  Also the volumes' vertex
 // bounding boxes (VoroInfo::getInsidePartSize reads them), reduced per block.
 // One block per lattice row along z (volume bv, a, b); blockDim is a
 // multiple of 32 so each warp covers one segment.
 __global__ void __launch_bounds__(128) vd_segments_kernel(const uint8_t* __restrict__ occ,
                                                           const int32_t* __restrict__ lab, VolTab T,
-                                                          const float* __restrict__ sxyz, SegPlanes* __restrict__ planes,
-                                                          int32_t* __restrict__ cv, int32_t* __restrict__ ce,
-                                                          int32_t* __restrict__ cf, float* __restrict__ lam_all,
+                                                          SegPlanes* __restrict__ planes, int32_t* __restrict__ cv,
+                                                          int32_t* __restrict__ ce, int32_t* __restrict__ cf,
                                                           int32_t* __restrict__ bbox_all) {
     const int lane = threadIdx.x & 31;
     const int64_t nrows = T.total(kLRow);
@@ -279,8 +246,6 @@ __global__ void __launch_bounds__(128) vd_segments_kernel(const uint8_t* __restr
             cur_bv = bv;
         }
         const Grid g = grid_of(T, bv, occ, lab);
-        const int64_t lat0 = T.start(kLat, bv);
-        float* lam = lam_all + 3 * lat0;
         const int64_t row = grow - T.start(kLRow, bv);
         const int a = (int)(row / g.NB), b = (int)(row - (int64_t)a * g.NB);
         const int nsr = (int)((g.NC + 31) / 32);
@@ -289,17 +254,9 @@ __global__ void __launch_bounds__(128) vd_segments_kernel(const uint8_t* __restr
             const int c = c0 + lane;
             uint32_t f = 0;
             if (c < (int)g.NC) {
-                const int64_t p = row * g.NC + c;
-                float l3[3] = {0.0f, 0.0f, 0.0f};
 #pragma unroll
-                for (int d = 0; d < 3; ++d) {
-                    if (face_valid(g, a, b, c, d)) {
-                        f |= 1u << d;
-                        int e[3] = {a, b, c};
-                        e[d] += 1;
-                        l3[d] = lambda_of(sxyz, g.lab[p], g.label(e[0], e[1], e[2]));
-                    }
-                }
+                for (int d = 0; d < 3; ++d)
+                    if (face_valid(g, a, b, c, d)) f |= 1u << d;
                 if (a < g.X && b < g.Y && c < g.Z && g.inside(a, b, c)) {
                     int32_t L[8];
 #pragma unroll
@@ -332,9 +289,6 @@ __global__ void __launch_bounds__(128) vd_segments_kernel(const uint8_t* __restr
                         }
                     }
                 }
-                lam[3 * p + 0] = l3[0];
-                lam[3 * p + 1] = l3[1];
-                lam[3 * p + 2] = l3[2];
             }
             SegPlanes P;
             P.v = __ballot_sync(0xffffffffu, f & 8u);
@@ -430,12 +384,58 @@ __global__ void __launch_bounds__(128) vd_vertices_kernel(VolTab T, Bases B, con
     }
 }
 
+// The faces of the axis edge (a,b,c)+d: the valid faces of the plaquette
+// shared by voxel (a,b,c) and its +d neighbour, i.e. the lattice edges along
+// u from nb and nb + e_w and along w from nb and nb + e_u, nb = (a,b,c) +
+// e_d (u = d+1, w = d+2 mod 3).  For each, fn(face id, triangle) is called
+// with the triangle of the face that carries the edge (0: (q3,q0,q1),
+// 1: (q3,q1,q2)).  Three segment loads.
+template <int D, class Fn>
+__device__ __forceinline__ void for_plaquette(const Segs& S, int a, int b, int c, Fn fn) {
+    constexpr int U = (D + 1) % 3, W = (D + 2) % 3;
+    int nb[3] = {a, b, c};
+    nb[D] += 1;
+    const int v[3] = {a, b, c};
+#pragma unroll
+    for (int g = 0; g < 3; ++g) {  // g = 0: nb (axes u and w); 1: nb + e_w (axis u); 2: nb + e_u (axis w)
+        int cc[3] = {nb[0], nb[1], nb[2]};
+        if (g == 1) cc[W] += 1;
+        if (g == 2) cc[U] += 1;
+        const int64_t sg = S.at(cc[0], cc[1], cc[2]);
+        const SegPlanes P = load_planes(S.planes + sg);
+        const int z = cc[2];
+        const uint32_t m = below(z);
+        const int32_t f0 = __ldg(S.fb + sg) + __popc(P.f0 & m) + __popc(P.f1 & m) + __popc(P.f2 & m);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            if (g == 1 && h == 1) continue;
+            if (g == 2 && h == 0) continue;
+            const int ax = h == 0 ? U : W;
+            if (!bit(plane_f(P, ax), z)) continue;
+            const int32_t fid = f0 + (ax >= 1 ? (int)bit(P.f0, z) : 0) + (ax >= 2 ? (int)bit(P.f1, z) : 0);
+            // position (s,t) of the edge's lower voxel in the face's quad
+            const int u2 = (ax + 1) % 3, w2 = (ax + 2) % 3;
+            const int s = v[u2] - (cc[u2] - 1), t = v[w2] - (cc[w2] - 1);
+            const int tri = D == u2 ? (t == 0 ? 0 : 1) : (s == 0 ? 0 : 1);
+            fn(fid, tri);
+        }
+    }
+}
+
+template <class Fn>
+__device__ __forceinline__ void for_plaquette_d(int d, const Segs& S, int a, int b, int c, Fn fn) {
+    if (d == 0) for_plaquette<0>(S, a, b, c, fn);
+    else if (d == 1) for_plaquette<1>(S, a, b, c, fn);
+    else for_plaquette<2>(S, a, b, c, fn);
+}
+
 // The row's axis edges: endpoints and, with records, thinning records
 // (incident triangles counted, summed and tested against the threshold;
 // measure = max lambda of the incident faces, voroinfo.cpp:1490-1538).
+// Face lambdas come from lamf (one per face, written by vd_faces_kernel).
 __global__ void __launch_bounds__(128) vd_edges_kernel(VolTab T, Bases B, const SegPlanes* __restrict__ planes,
                                                        const int32_t* __restrict__ vb, const int32_t* __restrict__ eb,
-                                                       const int32_t* __restrict__ fbs, const float* __restrict__ lam_all,
+                                                       const int32_t* __restrict__ fbs, const float* __restrict__ lamf,
                                                        int2* __restrict__ edges, EdgeRec* __restrict__ E,
                                                        const float* __restrict__ thr) {
     const int lane = threadIdx.x & 31;
@@ -444,8 +444,6 @@ __global__ void __launch_bounds__(128) vd_edges_kernel(VolTab T, Bases B, const 
         const int bv = T.find(kLRow, grow);
         const Segs S = segs_of(T, bv, planes, vb, eb, fbs);
         const Shift sh = shift_of(B, bv);
-        const float* lam = lam_all + 3 * T.start(kLat, bv);
-        const int64_t NC = T.dim(bv).z + 1;
         const int64_t row = grow - T.start(kLRow, bv);
         const int a = (int)(row / S.NB), b = (int)(row - (int64_t)a * S.NB);
         const float tb = thr ? thr[bv] : 0.0f;
@@ -454,8 +452,7 @@ __global__ void __launch_bounds__(128) vd_edges_kernel(VolTab T, Bases B, const 
             const int64_t s = S.at(a, b, c);
             const SegPlanes P = load_planes(planes + s);
             const uint32_t m = below(c);
-            const bool any = bit(P.e0 | P.e1 | P.e2, c);
-            if (!any) continue;
+            if (!bit(P.e0 | P.e1 | P.e2, c)) continue;
             int32_t e = __ldg(eb + s) + __popc(P.e0 & m) + __popc(P.e1 & m) + __popc(P.e2 & m) + (int32_t)sh.fb;
             const int32_t v0 = __ldg(vb + s) + __popc(P.v & m);
 #pragma unroll
@@ -466,23 +463,20 @@ __global__ void __launch_bounds__(128) vd_edges_kernel(VolTab T, Bases B, const 
                 const int32_t v1 = vid_at(S, nb[0], nb[1], nb[2]);
                 edges[e] = make_int2(v0, v1);
                 if (E) {
-                    Inc inc[4];
-                    const int k = plaquette_faces(S, a, b, c, d, inc);
                     float mx = 0.0f;
-                    unsigned npass = 0;
+                    unsigned k = 0, npass = 0;
                     unsigned long long idsum = 0;
-                    for (int j = 0; j < k; ++j) {
-                        const int64_t lp = ((int64_t)inc[j].x[0] * S.NB + inc[j].x[1]) * NC + inc[j].x[2];
-                        const float lj = lam[3 * lp + inc[j].axis];
+                    for_plaquette_d(d, S, a, b, c, [&](int32_t fid, int tri) {
+                        const float lj = __ldg(lamf + fid);
                         mx = fmaxf(mx, lj);
                         npass += lj < tb ? 1u : 0u;
-                        idsum += (unsigned)(2 * fid_at(S, inc[j].x[0], inc[j].x[1], inc[j].x[2], inc[j].axis) +
-                                            inc[j].tri);
-                    }
+                        idsum += (unsigned)(2 * fid + tri);
+                        ++k;
+                    });
                     EdgeRec r;
                     r.v0 = v0;
                     r.v1 = v1;
-                    r.rs = rs_make((unsigned)k, npass, idsum);
+                    r.rs = rs_make(k, npass, idsum);
                     r.trig = 0;
                     r.em = rec_measure(mx, thr, bv);
                     r.rm = kAlive;
@@ -499,7 +493,8 @@ __global__ void __launch_bounds__(128) vd_edges_kernel(VolTab T, Bases B, const 
 // with records, the thinning records of both triangles and the diagonal.
 __global__ void __launch_bounds__(128) vd_faces_kernel(VolTab T, Bases B, const SegPlanes* __restrict__ planes,
                                                        const int32_t* __restrict__ vb, const int32_t* __restrict__ eb,
-                                                       const int32_t* __restrict__ fbs, const float* __restrict__ lam_all,
+                                                       const int32_t* __restrict__ fbs, const int32_t* __restrict__ lab,
+                                                       const float* __restrict__ sxyz, float* __restrict__ lamf,
                                                        int32_t* __restrict__ tris, int2* __restrict__ edges,
                                                        FaceRec* __restrict__ F, EdgeRec* __restrict__ E,
                                                        const float* __restrict__ thr) {
@@ -509,7 +504,7 @@ __global__ void __launch_bounds__(128) vd_faces_kernel(VolTab T, Bases B, const 
         const int bv = T.find(kLRow, grow);
         const Segs S = segs_of(T, bv, planes, vb, eb, fbs);
         const Shift sh = shift_of(B, bv);
-        const float* lam = lam_all + 3 * T.start(kLat, bv);
+        const int32_t* lb = lab + T.start(kLat, bv);
         const int64_t NC = T.dim(bv).z + 1;
         const int64_t row = grow - T.start(kLRow, bv);
         const int a = (int)(row / S.NB), b = (int)(row - (int64_t)a * S.NB);
@@ -522,6 +517,7 @@ __global__ void __launch_bounds__(128) vd_faces_kernel(VolTab T, Bases B, const 
             const uint32_t m = below(c);
             int32_t f = __ldg(fbs + s) + __popc(P.f0 & m) + __popc(P.f1 & m) + __popc(P.f2 & m);
             const int64_t p = row * NC + c;
+            const int32_t l0 = __ldg(lb + p);
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
                 if (!bit(plane_f(P, d), c)) continue;
@@ -543,13 +539,16 @@ __global__ void __launch_bounds__(128) vd_faces_kernel(VolTab T, Bases B, const 
                 tris[3 * t1 + 2] = q[2];
                 const int32_t dv0 = min(q[1], q[3]), dv1 = max(q[1], q[3]);
                 edges[diag] = make_int2(dv0, dv1);
+                // lambda of the face: distance of its two sites (measureforMA_imp.h:1-4)
+                const int64_t p1 = p + (d == 0 ? S.NB * NC : (d == 1 ? NC : 1));
+                const float lm = lambda_of(sxyz, l0, __ldg(lb + p1));
+                lamf[f] = lm;
                 if (F) {
                     // sides in traceFace order: (t0,t1), (t1,t2), (t2,t0)
                     const int32_t e01 = erank_at(S, qv[0][0], qv[0][1], qv[0][2], u) + fbv;
                     const int32_t e12 = erank_at(S, qv[1][0], qv[1][1], qv[1][2], w) + fbv;
                     const int32_t e32 = erank_at(S, qv[3][0], qv[3][1], qv[3][2], u) + fbv;
                     const int32_t e03 = erank_at(S, qv[0][0], qv[0][1], qv[0][2], w) + fbv;
-                    const float lm = lam[3 * p + d];
                     const float lr = rec_measure(lm, thr, bv);
                     FaceRec fr;
                     fr.fm = lr;
@@ -586,7 +585,7 @@ __global__ void __launch_bounds__(128) vd_faces_kernel(VolTab T, Bases B, const 
 __global__ void __launch_bounds__(128) vd_aux_kernel(VolTab T, Bases B, const SegPlanes* __restrict__ planes,
                                                      const int32_t* __restrict__ vb, const int32_t* __restrict__ eb,
                                                      const int32_t* __restrict__ fbs, const int32_t* __restrict__ lab,
-                                                     const float* __restrict__ lam_all, float* __restrict__ vm,
+                                                     const float* __restrict__ lamf, float* __restrict__ vm,
                                                      float* __restrict__ em, float* __restrict__ fm,
                                                      int32_t* __restrict__ tri_face, int2* __restrict__ face_sites,
                                                      int32_t* __restrict__ tri_edges) {
@@ -597,7 +596,6 @@ __global__ void __launch_bounds__(128) vd_aux_kernel(VolTab T, Bases B, const Se
         const Segs S = segs_of(T, bv, planes, vb, eb, fbs);
         const Shift sh = shift_of(B, bv);
         const int64_t lat0 = T.start(kLat, bv);
-        const float* lam = lam_all + 3 * lat0;
         const int32_t* lb = lab + lat0;
         const int64_t NC = T.dim(bv).z + 1;
         const int64_t row = grow - T.start(kLRow, bv);
@@ -622,7 +620,8 @@ __global__ void __launch_bounds__(128) vd_aux_kernel(VolTab T, Bases B, const Se
                             int q[3] = {a, b, c};
                             q[(d + 1) % 3] += s2;
                             q[(d + 2) % 3] += t2;
-                            if (fbit_at(S, q[0], q[1], q[2], d)) mv = fmaxf(mv, lam[3 * lid(q[0], q[1], q[2]) + d]);
+                            if (fbit_at(S, q[0], q[1], q[2], d))
+                                mv = fmaxf(mv, __ldg(lamf + fid_at(S, q[0], q[1], q[2], d)));
                         }
                 vm[v] = mv;
             }
@@ -631,11 +630,8 @@ __global__ void __launch_bounds__(128) vd_aux_kernel(VolTab T, Bases B, const Se
 #pragma unroll
                 for (int d = 0; d < 3; ++d) {
                     if (!bit(plane_e(P, d), c)) continue;
-                    Inc inc[4];
-                    const int k = plaquette_faces(S, a, b, c, d, inc);
                     float mx = 0.0f;
-                    for (int j = 0; j < k; ++j)
-                        mx = fmaxf(mx, lam[3 * lid(inc[j].x[0], inc[j].x[1], inc[j].x[2]) + inc[j].axis]);
+                    for_plaquette_d(d, S, a, b, c, [&](int32_t fid, int) { mx = fmaxf(mx, __ldg(lamf + fid)); });
                     em[e++] = mx;
                 }
             }
@@ -660,7 +656,7 @@ __global__ void __launch_bounds__(128) vd_aux_kernel(VolTab T, Bases B, const Se
                     tri_edges[3 * t1 + 0] = diag;
                     tri_edges[3 * t1 + 1] = e12;
                     tri_edges[3 * t1 + 2] = e32;
-                    const float lm = lam[3 * p + d];
+                    const float lm = __ldg(lamf + f);
                     fm[t0] = lm;
                     fm[t1] = lm;
                     tri_face[t0] = f - fbv;
@@ -780,7 +776,6 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes, double t_thr) {
     const int64_t nrows = c->h_off[kLRow][nvol];
     Region stage(c, "stage_vd");
     VC_TRY(ensure_n<SegPlanes>(c, c->vd_seg, nseg));
-    VC_TRY(ensure_n<float>(c, c->vd_lam, 3 * N));
     VC_TRY(ensure_n<int32_t>(c, c->vd_voff, nseg));
     VC_TRY(ensure_n<int32_t>(c, c->vd_eoff, nseg));
     VC_TRY(ensure_n<int32_t>(c, c->vd_foff, nseg));
@@ -794,8 +789,7 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes, double t_thr) {
     {
         Region r(c, "vd_flags");
         vd_segments_kernel<<<row_grid(c, nrows), 128, 0, c->stream>>>(ptr<uint8_t>(c->occ), ptr<int32_t>(c->ft_id),
-                                                                       c->tab, ptr<float>(c->site_xyz), planes, vb, eb,
-                                                                       fb, ptr<float>(c->vd_lam), c->bases.bbox);
+                                                                       c->tab, planes, vb, eb, fb, c->bases.bbox);
         launched(c);
         VC_CUDA(c, cudaGetLastError());
     }
@@ -825,6 +819,7 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes, double t_thr) {
     VC_TRY(ensure_n<float>(c, c->vts, 3 * nv));
     VC_TRY(ensure_n<int2>(c, c->edges, ne));
     VC_TRY(ensure_n<int32_t>(c, c->tris, 3 * nt));
+    VC_TRY(ensure_n<float>(c, c->vd_lam, nface));  // lambda per face
     if (folded) {
         VC_TRY(ensure_n<FaceRec>(c, c->face_rec, nt));
         VC_TRY(ensure_n<EdgeRec>(c, c->edge_rec, ne));
@@ -840,17 +835,17 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes, double t_thr) {
             launched(c);
         }
         {
-            Region k(c, "vd_edges");
-            vd_edges_kernel<<<row_grid(c, nrows), 128, 0, c->stream>>>(
-                c->tab, c->bases, planes, vb, eb, fb, ptr<float>(c->vd_lam), ptr<int2>(c->edges),
-                folded ? ptr<EdgeRec>(c->edge_rec) : nullptr, thr);
+            Region k(c, "vd_faces");
+            vd_faces_kernel<<<row_grid(c, nrows), 128, 0, c->stream>>>(
+                c->tab, c->bases, planes, vb, eb, fb, ptr<int32_t>(c->ft_id), ptr<float>(c->site_xyz),
+                ptr<float>(c->vd_lam), ptr<int32_t>(c->tris), ptr<int2>(c->edges),
+                folded ? ptr<FaceRec>(c->face_rec) : nullptr, folded ? ptr<EdgeRec>(c->edge_rec) : nullptr, thr);
             launched(c);
         }
         {
-            Region k(c, "vd_faces");
-            vd_faces_kernel<<<row_grid(c, nrows), 128, 0, c->stream>>>(
-                c->tab, c->bases, planes, vb, eb, fb, ptr<float>(c->vd_lam), ptr<int32_t>(c->tris),
-                ptr<int2>(c->edges), folded ? ptr<FaceRec>(c->face_rec) : nullptr,
+            Region k(c, "vd_edges");
+            vd_edges_kernel<<<row_grid(c, nrows), 128, 0, c->stream>>>(
+                c->tab, c->bases, planes, vb, eb, fb, ptr<float>(c->vd_lam), ptr<int2>(c->edges),
                 folded ? ptr<EdgeRec>(c->edge_rec) : nullptr, thr);
             launched(c);
         }
