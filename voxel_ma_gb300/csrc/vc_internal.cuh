@@ -219,7 +219,7 @@ struct vc_ctx {
     vc::DevBuf face_rec, edge_rec, vert_rec;  // 32-byte per-cell thinning records
     bool records_fresh = false;               // records already hold this complex in reset state
     bool records_thr_folded = false;          // ... with the per-volume thresholds folded in (threshold 0)
-    vc::DevBuf q0, q1, child, child_cnt, cells, blk_cnt, thr;
+    vc::DevBuf q0, q1, child, cells, blk_cnt, thr;
     vc::DevBuf keep_v, keep_e, keep_f, removed_e;  // uint8 survivor flags of the last thinning
     vc::DevBuf trace;           // optional per-generation trace of the thinning kernel
     int trace_cap = 0, trace_gens = 0;

@@ -64,8 +64,7 @@ struct ThinArgs {
     const float* thr;  // [0] f_t, [1] l_t
     int2* qa;
     int2* qb;
-    int2* child;           // per item: up to 4 children, by slot
-    unsigned* child_mask;  // per item one byte (4 items per word): bit s = child in slot s
+    int2* child;           // per item: up to 4 children, by slot ({-1, -1}: none)
     int32_t* cells;        // cells whose count reached 1 in this generation (kEdgeBit: edge)
     int* counters;         // [2][4] by generation parity: list length, phase-A work cursor
     int64_t* blk_cnt;      // [2 * G] children per block, by generation parity
@@ -206,6 +205,8 @@ __global__ void __launch_bounds__(kThreads) thin_generations_kernel(ThinArgs A) 
     int64_t base = 0, pushes = n;
     int gen = 0;
     int64_t my_processed = 0, my_skipped = 0;
+    int64_t slots_ready = 0;  // child slots [0, 4 slots_ready) hold {-1, -1} or this generation's children
+    const int lane = threadIdx.x & 31;
     while (n > 0) {
         const int par = gen & 1;
         const int2* cur = par ? A.qb : A.qa;
@@ -218,6 +219,14 @@ __global__ void __launch_bounds__(kThreads) thin_generations_kernel(ThinArgs A) 
         if (tr) {
             A.trace[4 * gen + 0] = n;
             A.trace[4 * gen + 1] = global_ns();
+        }
+        // the child slots of items beyond any earlier generation start empty
+        // (phase B of this generation writes them after the barrier below)
+        if (n > slots_ready) {
+            const int64_t lo4 = 4 * slots_ready, hi4 = 4 * n;
+            for (int64_t k = lo4 + (int64_t)b * blockDim.x + threadIdx.x; k < hi4; k += (int64_t)G * blockDim.x)
+                __stcg(A.child + k, make_int2(-1, -1));
+            slots_ready = n;
         }
         // ---- phase A: apply the removals of the items that won their claim
         // items are taken in 256-item pieces from a shared cursor, so that
@@ -312,37 +321,45 @@ __global__ void __launch_bounds__(kThreads) thin_generations_kernel(ThinArgs A) 
             const int64_t m = __ldcg(ctr + 0);
             const int64_t mchunk = (m + G - 1) / G;
             const int64_t j1 = min(m, ((int64_t)b + 1) * mchunk);
-            for (int64_t j = (int64_t)b * mchunk + threadIdx.x; j < j1; j += blockDim.x) {
-                const int32_t code = __ldcg(A.cells + j);
-                unsigned long long tg;
-                int2 ch;
-                if (code & kEdgeBit) {
-                    const int32_t e2 = code & ~kEdgeBit;
-                    const int4 ea = __ldcg(reinterpret_cast<const int4*>(A.E + e2));
-                    const int4 eb = __ldcg(reinterpret_cast<const int4*>(A.E + e2) + 1);
-                    const unsigned long long rs = ((unsigned long long)(uint32_t)ea.w << 32) | (uint32_t)ea.z;
-                    if (rs_count(rs) != 1 || rs_pass(rs) != 1) continue;
-                    tg = ((unsigned long long)(uint32_t)eb.y << 32) | (uint32_t)eb.x;
-                    ch = make_fe(rs_last(rs), e2);
-                } else {
-                    const int32_t u = code;
-                    const int4 va = __ldcg(reinterpret_cast<const int4*>(A.V + u));  // rs | trig
-                    const unsigned long long rs = ((unsigned long long)(uint32_t)va.y << 32) | (uint32_t)va.x;
-                    if (rs_count(rs) != 1) continue;
-                    const int32_t e3 = rs_last(rs);
-                    if (!(A.E[e3].em < l_t)) continue;
-                    tg = ((unsigned long long)(uint32_t)va.w << 32) | (uint32_t)va.z;
-                    ch = make_ev(e3, u);
+            for (int64_t jb = (int64_t)b * mchunk; jb < j1; jb += blockDim.x) {
+                const int64_t j = jb + threadIdx.x;
+                bool want = false;
+                int64_t i = 0;
+                int slot = 0;
+                int2 ch = make_int2(-1, -1);
+                if (j < j1) {
+                    const int32_t code = __ldcg(A.cells + j);
+                    unsigned long long tg = 0;
+                    if (code & kEdgeBit) {
+                        const int32_t e2 = code & ~kEdgeBit;
+                        const int4 ea = __ldcg(reinterpret_cast<const int4*>(A.E + e2));
+                        const int4 eb = __ldcg(reinterpret_cast<const int4*>(A.E + e2) + 1);
+                        const unsigned long long rs = ((unsigned long long)(uint32_t)ea.w << 32) | (uint32_t)ea.z;
+                        want = rs_count(rs) == 1 && rs_pass(rs) == 1;
+                        tg = ((unsigned long long)(uint32_t)eb.y << 32) | (uint32_t)eb.x;
+                        ch = make_fe(rs_last(rs), e2);
+                    } else {
+                        const int32_t u = code;
+                        const int4 va = __ldcg(reinterpret_cast<const int4*>(A.V + u));  // rs | trig
+                        const unsigned long long rs = ((unsigned long long)(uint32_t)va.y << 32) | (uint32_t)va.x;
+                        const int32_t e3 = rs_last(rs);
+                        want = rs_count(rs) == 1 && A.E[e3].em < l_t;
+                        tg = ((unsigned long long)(uint32_t)va.w << 32) | (uint32_t)va.z;
+                        ch = make_ev(e3, u);
+                    }
+                    i = (int64_t)(tg >> 2) - base;
+                    slot = (int)(tg & 3u);
+                    if (want && (i < 0 || i >= n)) {
+                        set_error(A.err, VC_ERR_INVARIANT);
+                        want = false;
+                    }
                 }
-                const int64_t i = (int64_t)(tg >> 2) - base;
-                const int slot = (int)(tg & 3u);
-                if (i < 0 || i >= n) {
-                    set_error(A.err, VC_ERR_INVARIANT);
-                    continue;
-                }
-                __stcg(A.child + 4 * i + slot, ch);
-                atomicOr(A.child_mask + (i >> 2), 1u << (((unsigned)i & 3u) * 8u + (unsigned)slot));
-                atomicAdd((unsigned long long*)(blk + i / chunk), 1ull);
+                if (want) __stcg(A.child + 4 * i + slot, ch);
+                // children per phase-C block, one atomic per warp and block
+                const int64_t bi = want ? i / chunk : -1;
+                const unsigned grp = __match_any_sync(0xffffffffu, bi);
+                if (want && lane == __ffs(grp) - 1)
+                    atomicAdd((unsigned long long*)(blk + bi), (unsigned long long)__popc(grp));
             }
         }
         grid_barrier(A.bar, A.err, A.spin_limit);
@@ -370,11 +387,20 @@ __global__ void __launch_bounds__(kThreads) thin_generations_kernel(ThinArgs A) 
         int64_t running = prefix;
         for (int64_t r0 = i0; r0 < i1; r0 += blockDim.x) {
             const int64_t i = r0 + threadIdx.x;
+            int2 cs[4] = {make_int2(-1, -1), make_int2(-1, -1), make_int2(-1, -1), make_int2(-1, -1)};
             unsigned msk = 0;
             if (i < i1) {
-                const unsigned sh = ((unsigned)i & 3u) * 8u;
-                msk = (__ldcg(A.child_mask + (i >> 2)) >> sh) & 0xFu;
-                if (msk) atomicAnd(A.child_mask + (i >> 2), ~(0xFFu << sh));
+                int4* sp = reinterpret_cast<int4*>(A.child + 4 * i);
+                const int4 s01 = __ldcg(sp), s23 = __ldcg(sp + 1);
+                cs[0] = make_int2(s01.x, s01.y);
+                cs[1] = make_int2(s01.z, s01.w);
+                cs[2] = make_int2(s23.x, s23.y);
+                cs[3] = make_int2(s23.z, s23.w);
+#pragma unroll
+                for (int sl = 0; sl < 4; ++sl) msk |= cs[sl].y >= 0 ? (1u << sl) : 0u;
+                // empty the slots for the next generation
+                if (msk & 3u) __stcg(sp, make_int4(-1, -1, -1, -1));
+                if (msk & 12u) __stcg(sp + 1, make_int4(-1, -1, -1, -1));
             }
             int64_t tot;
             const int64_t ex = block_exclusive_sum<int64_t>((int64_t)__popc(msk), sm, &tot);
@@ -382,7 +408,7 @@ __global__ void __launch_bounds__(kThreads) thin_generations_kernel(ThinArgs A) 
 #pragma unroll
             for (int sl = 0; sl < 4; ++sl) {
                 if (!(msk & (1u << sl))) continue;
-                const int2 ch = __ldcg(A.child + 4 * i + sl);
+                const int2 ch = cs[sl];
                 const int64_t slot = running + ex + k;
                 ++k;
                 __stcg(nxt + slot, ch);
@@ -496,7 +522,6 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats) {
     VC_TRY(ensure_n<int2>(c, c->q0, qcap));
     VC_TRY(ensure_n<int2>(c, c->q1, qcap));
     VC_TRY(ensure_n<int2>(c, c->child, 4 * qcap));
-    VC_TRY(ensure_n<unsigned>(c, c->child_cnt, qcap / 4 + 2));  // child masks
     VC_TRY(ensure_n<int32_t>(c, c->cells, 4 * qcap));
     VC_TRY(ensure_n<int32_t>(c, c->scratch2, 2 * (nv + ne) + 2));
     VC_TRY(ensure_n<int64_t>(c, c->euler_tmp, 16));
@@ -512,7 +537,6 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats) {
     A.qa = ptr<int2>(c->q0);
     A.qb = ptr<int2>(c->q1);
     A.child = ptr<int2>(c->child);
-    A.child_mask = ptr<unsigned>(c->child_cnt);
     A.cells = ptr<int32_t>(c->cells);
     A.err = dev_err(c);
     int64_t* ctl = ptr<int64_t>(c->euler_tmp);
@@ -542,7 +566,6 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats) {
         gen0_flags_kernel<<<grid_for(c, nv + ne, 256), 256, 0, c->stream>>>(A, (int32_t)nv, (int32_t)ne, flag);
         launched(c);
         VC_CUDA(c, cudaMemsetAsync(ctl, 0, 16 * sizeof(int64_t), c->stream));
-        VC_CUDA(c, cudaMemsetAsync(c->child_cnt.p, 0, (qcap / 4 + 2) * sizeof(unsigned), c->stream));
         VC_TRY(scan_exclusive_i32(c, flag, pos, nv + ne, ctl + 0));
         gen0_write_kernel<<<grid_for(c, nv + ne, 256), 256, 0, c->stream>>>(A, (int32_t)nv, (int32_t)ne, flag,
                                                                              pos);
