@@ -214,7 +214,7 @@ std::vector<DevBuf*> ctx_buffers(vc_ctx* c) {
             &c->ft_id, &c->ft_tmp, &c->vd_seg, &c->vd_voff, &c->vd_eoff, &c->vd_foff, &c->vd_tri_face,
             &c->vd_face_sites, &c->vd_lam, &c->vd_radius, &c->tab_buf, &c->bases_buf, &c->vts, &c->edges_in, &c->edges, &c->tris,
             &c->tri_edges, &c->ve_off, &c->ve_ids, &c->ef_off, &c->ef_ids, &c->hash_keys, &c->hash_pos,
-            &c->hash_id, &c->side_slot, &c->vm, &c->em, &c->fm, &c->face_rec, &c->edge_rec, &c->vert_rec, &c->q0,
+            &c->hash_id, &c->side_slot, &c->vm, &c->em, &c->fm, &c->face_rec, &c->edge_rec, &c->vert_rec, &c->thin_g0, &c->q0,
             &c->q1, &c->child, &c->cells, &c->blk_cnt, &c->keep_v, &c->keep_e,
             &c->keep_f, &c->removed_e, &c->trace, &c->thr, &c->rem_voff, &c->rem_eoff, &c->rem_foff,
             &c->rem_vts, &c->rem_edges, &c->rem_tris, &c->uf_parent, &c->euler_tmp};

@@ -217,6 +217,10 @@ struct vc_ctx {
     bool thin_valid = false;
     vc_thin_stats thin_stats{};
     vc::DevBuf face_rec, edge_rec, vert_rec;  // 32-byte per-cell thinning records
+    // generation 0 of the thinning queue, written with the records: per edge
+    // the face of its FE pair, then per vertex the edge of its EV pair, -1
+    // where the cell starts no pair (ne + nv int32)
+    vc::DevBuf thin_g0;
     bool records_fresh = false;               // records already hold this complex in reset state
     bool records_thr_folded = false;          // ... with the per-volume thresholds folded in (threshold 0)
     vc::DevBuf q0, q1, child, cells, blk_cnt, thr;

@@ -49,6 +49,7 @@
 // position of the last decrement with the slot of the cell in that item, so
 // the child's slot needs no per-item record of the decremented cells.
 #include "vc_internal.cuh"
+#include "vc_scan.cuh"
 
 namespace vc {
 namespace {
@@ -95,10 +96,10 @@ __global__ void build_records_kernel(const int2* __restrict__ edges, const int32
                                      const int32_t* __restrict__ ef_off, const int32_t* __restrict__ ef_ids,
                                      const float* __restrict__ em, const float* __restrict__ fm,
                                      const float* __restrict__ thr, int32_t nv, int32_t ne, int32_t nt, FaceRec* F,
-                                     EdgeRec* E, VertRec* V, int* err) {
+                                     EdgeRec* E, VertRec* V, int32_t* __restrict__ g0, int* err) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     const int64_t n = (int64_t)nv + ne + nt;
-    const float f_t = thr[0];
+    const float f_t = thr[0], l_t = thr[1];
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         if (i < nt) {
             FaceRec r;
@@ -128,6 +129,7 @@ __global__ void build_records_kernel(const int2* __restrict__ edges, const int32
             r.em = em[e];
             r.rm = kAlive;
             E[e] = r;
+            g0[e] = (o1 - o0 == 1 && pass == 1) ? (int32_t)idsum : -1;
         } else {
             const int64_t v = i - nt - ne;
             const int32_t o0 = ve_off[v], o1 = ve_off[v + 1];
@@ -140,44 +142,54 @@ __global__ void build_records_kernel(const int2* __restrict__ edges, const int32
             r.rm = kAlive;
             r.pad0 = r.pad1 = r.pad2 = 0;
             V[v] = r;
+            g0[(int64_t)ne + v] = (o1 - o0 == 1 && em[idsum] < l_t) ? (int32_t)idsum : -1;
         }
     }
 }
 
 // Generation 0: FE pairs of edges with one face (edge order), then EV pairs
-// of vertices with one edge (vertex order), filtered by the thresholds.
-__global__ void gen0_flags_kernel(ThinArgs A, int32_t nv, int32_t ne, int32_t* __restrict__ flag) {
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    const float l_t = A.thr[1];
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (int64_t)ne + nv; i += stride) {
-        int32_t ok = 0;
-        if (i < ne) {
-            const unsigned long long rs = A.E[i].rs;
-            ok = rs_count(rs) == 1 && rs_pass(rs) == 1;
-        } else {
-            const unsigned long long rs = A.V[i - ne].rs;
-            if (rs_count(rs) == 1) ok = A.E[rs_last(rs)].em < l_t;
-        }
-        flag[i] = ok;
+// of vertices with one edge (vertex order), filtered by the thresholds: the
+// entries of g0 that are not -1, compacted in order (tile counts, one scan
+// of the tile counts, then each tile writes its items and their claims).
+constexpr int kG0Items = 8;
+constexpr int64_t kG0Tile = (int64_t)kThreads * kG0Items;
+
+__global__ void __launch_bounds__(kThreads) gen0_count_kernel(const int32_t* __restrict__ g0, int64_t n,
+                                                              int64_t* __restrict__ sums) {
+    __shared__ int64_t sm[33];
+    const int64_t base = (int64_t)blockIdx.x * kG0Tile;
+    int64_t acc = 0;
+#pragma unroll
+    for (int r = 0; r < kG0Items; ++r) {
+        const int64_t i = base + (int64_t)r * kThreads + threadIdx.x;
+        if (i < n) acc += __ldcs(g0 + i) >= 0 ? 1 : 0;
     }
+    int64_t tot;
+    block_exclusive_sum<int64_t>(acc, sm, &tot);
+    if (threadIdx.x == 0) sums[blockIdx.x] = tot;
 }
 
-__global__ void gen0_write_kernel(ThinArgs A, int32_t nv, int32_t ne, const int32_t* __restrict__ flag,
-                                  const int32_t* __restrict__ pos) {
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (int64_t)ne + nv; i += stride) {
-        if (!flag[i]) continue;
-        const int32_t p = pos[i];
-        if (i < ne) {
-            const int32_t f = rs_last(A.E[i].rs);
-            A.qa[p] = make_fe(f, (int32_t)i);
-            atomicMin(&A.F[f].rm, p);
-        } else {
-            const int32_t v = (int32_t)(i - ne);
-            const int32_t e = rs_last(A.V[v].rs);
-            A.qa[p] = make_ev(e, v);
-            atomicMin(&A.E[e].rm, p);
+__global__ void __launch_bounds__(kThreads) gen0_write_kernel(ThinArgs A, int32_t ne, const int32_t* __restrict__ g0,
+                                                              int64_t n, const int64_t* __restrict__ sums) {
+    __shared__ int64_t sm[33];
+    const int64_t base = (int64_t)blockIdx.x * kG0Tile;
+    int64_t carry = sums[blockIdx.x];
+    for (int r = 0; r < kG0Items; ++r) {
+        const int64_t i = base + (int64_t)r * kThreads + threadIdx.x;
+        const int32_t x = i < n ? __ldcs(g0 + i) : -1;
+        int64_t tot;
+        const int64_t ex = block_exclusive_sum<int64_t>(x >= 0 ? 1 : 0, sm, &tot);
+        if (x >= 0) {
+            const int32_t p = (int32_t)(carry + ex);
+            if (i < ne) {
+                A.qa[p] = make_fe(x, (int32_t)i);
+                atomicMin(&A.F[x].rm, p);
+            } else {
+                A.qa[p] = make_ev(x, (int32_t)(i - ne));
+                atomicMin(&A.E[x].rm, p);
+            }
         }
+        carry += tot;
     }
 }
 
@@ -518,12 +530,12 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats) {
         VC_TRY(ensure_n<FaceRec>(c, c->face_rec, nt));
         VC_TRY(ensure_n<EdgeRec>(c, c->edge_rec, ne));
         VC_TRY(ensure_n<VertRec>(c, c->vert_rec, nv));
+        VC_TRY(ensure_n<int32_t>(c, c->thin_g0, nv + ne));
     }
     VC_TRY(ensure_n<int2>(c, c->q0, qcap));
     VC_TRY(ensure_n<int2>(c, c->q1, qcap));
     VC_TRY(ensure_n<int2>(c, c->child, 4 * qcap));
     VC_TRY(ensure_n<int32_t>(c, c->cells, 4 * qcap));
-    VC_TRY(ensure_n<int32_t>(c, c->scratch2, 2 * (nv + ne) + 2));
     VC_TRY(ensure_n<int64_t>(c, c->euler_tmp, 16));
     VC_TRY(ensure_n<uint8_t>(c, c->keep_v, nv));
     VC_TRY(ensure_n<uint8_t>(c, c->keep_e, ne));
@@ -558,18 +570,21 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats) {
             build_records_kernel<<<grid_for(c, nv + ne + nt, 256), 256, 0, c->stream>>>(
                 ptr<int2>(c->edges), ptr<int32_t>(c->tri_edges), ptr<int32_t>(c->ve_off), ptr<int32_t>(c->ve_ids),
                 ptr<int32_t>(c->ef_off), ptr<int32_t>(c->ef_ids), ptr<float>(c->em), ptr<float>(c->fm), A.thr,
-                (int32_t)nv, (int32_t)ne, (int32_t)nt, A.F, A.E, A.V, dev_err(c));
+                (int32_t)nv, (int32_t)ne, (int32_t)nt, A.F, A.E, A.V, ptr<int32_t>(c->thin_g0), dev_err(c));
             launched(c);
         }
-        int32_t* flag = ptr<int32_t>(c->scratch2);
-        int32_t* pos = flag + (nv + ne + 1);
-        gen0_flags_kernel<<<grid_for(c, nv + ne, 256), 256, 0, c->stream>>>(A, (int32_t)nv, (int32_t)ne, flag);
-        launched(c);
         VC_CUDA(c, cudaMemsetAsync(ctl, 0, 16 * sizeof(int64_t), c->stream));
-        VC_TRY(scan_exclusive_i32(c, flag, pos, nv + ne, ctl + 0));
-        gen0_write_kernel<<<grid_for(c, nv + ne, 256), 256, 0, c->stream>>>(A, (int32_t)nv, (int32_t)ne, flag,
-                                                                             pos);
-        launched(c);
+        const int64_t ng = nv + ne;
+        const int64_t tiles = (ng + kG0Tile - 1) / kG0Tile;
+        if (tiles > 0) {
+            VC_TRY(ensure_n<int64_t>(c, c->scratch, tiles + 1));
+            int64_t* sums = ptr<int64_t>(c->scratch);
+            const int32_t* g0 = ptr<int32_t>(c->thin_g0);
+            gen0_count_kernel<<<(unsigned)tiles, kThreads, 0, c->stream>>>(g0, ng, sums);
+            scan_sums_single<<<1, 1024, 0, c->stream>>>(sums, tiles, ctl + 0);
+            gen0_write_kernel<<<(unsigned)tiles, kThreads, 0, c->stream>>>(A, (int32_t)ne, g0, ng, sums);
+            launched(c, 3);
+        }
         VC_CUDA(c, cudaGetLastError());
     }
     // persistent cooperative launch: every block resident

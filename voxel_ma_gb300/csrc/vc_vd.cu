@@ -321,7 +321,8 @@ __global__ void __launch_bounds__(128) vd_segments_kernel(const uint8_t* __restr
 __global__ void __launch_bounds__(128) vd_vertices_kernel(VolTab T, Bases B, const SegPlanes* __restrict__ planes,
                                                           const int32_t* __restrict__ vb, const int32_t* __restrict__ eb,
                                                           const int32_t* __restrict__ fbs, float* __restrict__ vts,
-                                                          VertRec* __restrict__ V) {
+                                                          VertRec* __restrict__ V, const EdgeRec* __restrict__ E,
+                                                          int32_t* __restrict__ g0, int64_t ne) {
     const int lane = threadIdx.x & 31;
     const int64_t nrows = T.total(kLRow);
     for (int64_t grow = blockIdx.x; grow < nrows; grow += gridDim.x) {
@@ -380,6 +381,9 @@ __global__ void __launch_bounds__(128) vd_vertices_kernel(VolTab T, Bases B, con
             r.rm = kAlive;
             r.pad0 = r.pad1 = r.pad2 = 0;
             V[v] = r;
+            // generation 0: an EV pair when the one edge passes the filter
+            // (its record, written before, holds the folded measure)
+            g0[ne + v] = (k == 1 && E[idsum].em < 0.0f) ? (int32_t)idsum : -1;
         }
     }
 }
@@ -437,7 +441,7 @@ __global__ void __launch_bounds__(128) vd_edges_kernel(VolTab T, Bases B, const 
                                                        const int32_t* __restrict__ vb, const int32_t* __restrict__ eb,
                                                        const int32_t* __restrict__ fbs, const float* __restrict__ lamf,
                                                        int2* __restrict__ edges, EdgeRec* __restrict__ E,
-                                                       const float* __restrict__ thr) {
+                                                       int32_t* __restrict__ g0, const float* __restrict__ thr) {
     const int lane = threadIdx.x & 31;
     const int64_t nrows = T.total(kLRow);
     for (int64_t grow = blockIdx.x; grow < nrows; grow += gridDim.x) {
@@ -481,6 +485,8 @@ __global__ void __launch_bounds__(128) vd_edges_kernel(VolTab T, Bases B, const 
                     r.em = rec_measure(mx, thr, bv);
                     r.rm = kAlive;
                     E[e] = r;
+                    // generation 0: an FE pair when the one face passes the filter
+                    g0[e] = (k == 1 && npass == 1) ? (int32_t)idsum : -1;
                 }
                 ++e;
             }
@@ -497,7 +503,7 @@ __global__ void __launch_bounds__(128) vd_faces_kernel(VolTab T, Bases B, const 
                                                        const float* __restrict__ sxyz, float* __restrict__ lamf,
                                                        int32_t* __restrict__ tris, int2* __restrict__ edges,
                                                        FaceRec* __restrict__ F, EdgeRec* __restrict__ E,
-                                                       const float* __restrict__ thr) {
+                                                       int32_t* __restrict__ g0, const float* __restrict__ thr) {
     const int lane = threadIdx.x & 31;
     const int64_t nrows = T.total(kLRow);
     for (int64_t grow = blockIdx.x; grow < nrows; grow += gridDim.x) {
@@ -570,6 +576,7 @@ __global__ void __launch_bounds__(128) vd_faces_kernel(VolTab T, Bases B, const 
                     er.em = lr;
                     er.rm = kAlive;
                     E[diag] = er;
+                    g0[diag] = -1;  // two triangles: no FE pair
                 }
                 ++f;
             }
@@ -824,29 +831,32 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes, double t_thr) {
         VC_TRY(ensure_n<FaceRec>(c, c->face_rec, nt));
         VC_TRY(ensure_n<EdgeRec>(c, c->edge_rec, ne));
         VC_TRY(ensure_n<VertRec>(c, c->vert_rec, nv));
+        VC_TRY(ensure_n<int32_t>(c, c->thin_g0, nv + ne));
     }
     const float* thr = folded ? c->bases.thr : nullptr;
     {
         Region r(c, "vd_emit");
-        {
-            Region k(c, "vd_vertices");
-            vd_vertices_kernel<<<row_grid(c, nrows), 128, 0, c->stream>>>(
-                c->tab, c->bases, planes, vb, eb, fb, ptr<float>(c->vts), folded ? ptr<VertRec>(c->vert_rec) : nullptr);
-            launched(c);
-        }
+        int32_t* g0 = folded ? ptr<int32_t>(c->thin_g0) : nullptr;
         {
             Region k(c, "vd_faces");
             vd_faces_kernel<<<row_grid(c, nrows), 128, 0, c->stream>>>(
                 c->tab, c->bases, planes, vb, eb, fb, ptr<int32_t>(c->ft_id), ptr<float>(c->site_xyz),
                 ptr<float>(c->vd_lam), ptr<int32_t>(c->tris), ptr<int2>(c->edges),
-                folded ? ptr<FaceRec>(c->face_rec) : nullptr, folded ? ptr<EdgeRec>(c->edge_rec) : nullptr, thr);
+                folded ? ptr<FaceRec>(c->face_rec) : nullptr, folded ? ptr<EdgeRec>(c->edge_rec) : nullptr, g0, thr);
             launched(c);
         }
         {
             Region k(c, "vd_edges");
             vd_edges_kernel<<<row_grid(c, nrows), 128, 0, c->stream>>>(
                 c->tab, c->bases, planes, vb, eb, fb, ptr<float>(c->vd_lam), ptr<int2>(c->edges),
-                folded ? ptr<EdgeRec>(c->edge_rec) : nullptr, thr);
+                folded ? ptr<EdgeRec>(c->edge_rec) : nullptr, g0, thr);
+            launched(c);
+        }
+        {
+            Region k(c, "vd_vertices");
+            vd_vertices_kernel<<<row_grid(c, nrows), 128, 0, c->stream>>>(
+                c->tab, c->bases, planes, vb, eb, fb, ptr<float>(c->vts), folded ? ptr<VertRec>(c->vert_rec) : nullptr,
+                folded ? ptr<EdgeRec>(c->edge_rec) : nullptr, g0, ne);
             launched(c);
         }
         VC_CUDA(c, cudaGetLastError());
