@@ -216,7 +216,7 @@ std::vector<DevBuf*> ctx_buffers(vc_ctx* c) {
             &c->tri_edges, &c->ve_off, &c->ve_ids, &c->ef_off, &c->ef_ids, &c->hash_keys, &c->hash_pos,
             &c->hash_id, &c->side_slot, &c->vm, &c->em, &c->fm, &c->face_rec, &c->edge_rec, &c->vert_rec, &c->thin_g0, &c->q0,
             &c->q1, &c->child, &c->cells, &c->blk_cnt, &c->keep_v, &c->keep_e,
-            &c->keep_f, &c->removed_e, &c->trace, &c->thr, &c->rem_voff, &c->rem_eoff, &c->rem_foff,
+            &c->keep_f, &c->removed_e, &c->keep_bits, &c->keep_wv, &c->keep_we, &c->keep_wf, &c->trace, &c->thr,
             &c->rem_vts, &c->rem_edges, &c->rem_tris, &c->uf_parent, &c->euler_tmp};
 }
 

@@ -225,6 +225,9 @@ struct vc_ctx {
     bool records_thr_folded = false;          // ... with the per-volume thresholds folded in (threshold 0)
     vc::DevBuf q0, q1, child, cells, blk_cnt, thr;
     vc::DevBuf keep_v, keep_e, keep_f, removed_e;  // uint8 survivor flags of the last thinning
+    // the same survivor flags as 32-bit words, vertices | edges | faces, and
+    // per word its count of survivors (then, scanned, the survivors before it)
+    vc::DevBuf keep_bits, keep_wv, keep_we, keep_wf;
     vc::DevBuf trace;           // optional per-generation trace of the thinning kernel
     int trace_cap = 0, trace_gens = 0;
     int thin_blocks_per_sm = 0;  // 0 = library default
@@ -233,7 +236,6 @@ struct vc_ctx {
     // remaining complex
     bool rem_valid = false;
     vc_rem_sizes rem{};
-    vc::DevBuf rem_voff, rem_eoff, rem_foff;
     vc::DevBuf rem_vts, rem_edges, rem_tris;
     vc::DevBuf uf_parent, euler_tmp;
     std::vector<int64_t> h_rem_bases;         // batches: remaining V / E / T starts, nvol + 1 each
@@ -282,6 +284,15 @@ int* dev_err(vc_ctx* c);
 // per-volume base arrays.
 int set_volume_table(vc_ctx* c, int nvol, const int32_t* dims);
 // The entry of a base array (nvol + 1 ascending starts) whose range holds x.
+// Rank of cell x among the kept cells of its kind: the kept cells are bit
+// words (bit x & 31 of word x >> 5) and base[w] is the number kept before
+// word w (an exclusive scan of the words' population counts).
+__device__ __forceinline__ int32_t kept_rank(const uint32_t* __restrict__ bits, const int32_t* __restrict__ base,
+                                             int64_t x) {
+    const int64_t w = x >> 5;
+    return __ldg(base + w) + __popc(__ldg(bits + w) & ((1u << (x & 31)) - 1u));
+}
+
 __device__ __forceinline__ int find_base(const int64_t* base, int nvol, int64_t x) {
     if (nvol <= 1) return 0;
     int lo = 0, hi = nvol - 1;

@@ -15,61 +15,70 @@
 namespace vc {
 namespace {
 
-__global__ void rem_flags_kernel(const uint8_t* __restrict__ kv, const uint8_t* __restrict__ ke,
-                                 const uint8_t* __restrict__ kf, int32_t nv, int32_t ne, int32_t nt,
-                                 int32_t* __restrict__ fv, int32_t* __restrict__ fe, int32_t* __restrict__ ff) {
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (int64_t)nv + ne + nt; i += stride) {
-        if (i < nv) fv[i] = kv[i];
-        else if (i < (int64_t)nv + ne) fe[i - nv] = ke[i - nv];
-        else ff[i - nv - ne] = kf[i - nv - ne];
-    }
-}
+// Survivors are bit words (vertices | edges | faces) with scanned per-word
+// counts: a survivor's output position is its kept_rank.
+struct Kept {
+    const uint32_t* bv;  // vertex words
+    const uint32_t* be;  // edge words
+    const uint32_t* bf;  // face words
+    const int32_t* pv;
+    const int32_t* pe;
+    const int32_t* pf;
+};
 
-// Per-volume starts of the remaining complex (batches): the scans at each
-// volume's first vertex, edge and triangle.
-__global__ void rem_bases_kernel(Bases B, int nvol, int32_t nv, int32_t ne, int32_t nt, const int32_t* __restrict__ pv,
-                                 const int32_t* __restrict__ pe, const int32_t* __restrict__ pf,
+// Per-volume starts of the remaining complex (batches): the survivors before
+// each volume's first vertex, edge and triangle.
+__global__ void rem_bases_kernel(Bases B, int nvol, int32_t nv, int32_t ne, int32_t nt, Kept K,
                                  const int64_t* __restrict__ tot) {
     for (int b = blockIdx.x * blockDim.x + threadIdx.x; b <= nvol; b += gridDim.x * blockDim.x) {
         const int64_t v0 = B.b[kBVert][b], e0 = B.b[kBAxis][b] + B.b[kBFace][b], t0 = 2 * B.b[kBFace][b];
-        B.b[kBRemV][b] = v0 < nv ? pv[v0] : tot[0];
-        B.b[kBRemE][b] = e0 < ne ? pe[e0] : tot[1];
-        B.b[kBRemT][b] = t0 < nt ? pf[t0] : tot[2];
+        B.b[kBRemV][b] = v0 < nv ? kept_rank(K.bv, K.pv, v0) : tot[0];
+        B.b[kBRemE][b] = e0 < ne ? kept_rank(K.be, K.pe, e0) : tot[1];
+        B.b[kBRemT][b] = t0 < nt ? kept_rank(K.bf, K.pf, t0) : tot[2];
     }
 }
 
-// After the exclusive scans pv/pe/pf hold output positions.  In a batch
-// (nmap > 1) vertex ids are made local to each volume's remaining complex.
-__global__ void rem_write_kernel(const uint8_t* __restrict__ kv, const uint8_t* __restrict__ ke,
-                                 const uint8_t* __restrict__ kf, int32_t nv, int32_t ne, int32_t nt,
-                                 const int32_t* __restrict__ pv, const int32_t* __restrict__ pe,
-                                 const int32_t* __restrict__ pf, const float* __restrict__ vts,
+// One warp per 32 cells of a kind: the survivors at their kept ranks.  In a
+// batch (nmap > 1) vertex ids are made local to each volume's remaining
+// complex.
+__global__ void rem_write_kernel(int32_t nv, int32_t ne, int32_t nt, Kept K, const float* __restrict__ vts,
                                  const int2* __restrict__ edges, const int32_t* __restrict__ tris,
                                  float* __restrict__ ovts, int2* __restrict__ oedges, int32_t* __restrict__ otris,
                                  Bases B, int nmap) {
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (int64_t)nv + ne + nt; i += stride) {
-        if (i < nv) {
-            if (!kv[i]) continue;
-            const int64_t o = pv[i];
+    const int lane = threadIdx.x & 31;
+    const uint32_t lowm = (1u << lane) - 1u;
+    const int64_t nwv = ((int64_t)nv + 31) / 32, nwe = ((int64_t)ne + 31) / 32, nwf = ((int64_t)nt + 31) / 32;
+    const int64_t nw = nwv + nwe + nwf;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < nw; w += warps) {
+        if (w < nwv) {
+            const uint32_t word = __ldg(K.bv + w);
+            if (!((word >> lane) & 1u)) continue;
+            const int64_t i = w * 32 + lane;
+            const int64_t o = __ldg(K.pv + w) + __popc(word & lowm);
             ovts[3 * o + 0] = vts[3 * i + 0];
             ovts[3 * o + 1] = vts[3 * i + 1];
             ovts[3 * o + 2] = vts[3 * i + 2];
-        } else if (i < (int64_t)nv + ne) {
-            const int64_t e = i - nv;
-            if (!ke[e]) continue;
+        } else if (w < nwv + nwe) {
+            const int64_t we = w - nwv;
+            const uint32_t word = __ldg(K.be + we);
+            if (!((word >> lane) & 1u)) continue;
+            const int64_t e = we * 32 + lane;
             const int2 ev = edges[e];
             const int32_t sh = nmap > 1 ? (int32_t)B.b[kBRemV][find_base(B.b[kBVert], nmap, ev.x)] : 0;
-            oedges[pe[e]] = make_int2(pv[ev.x] - sh, pv[ev.y] - sh);
+            oedges[__ldg(K.pe + we) + __popc(word & lowm)] =
+                make_int2(kept_rank(K.bv, K.pv, ev.x) - sh, kept_rank(K.bv, K.pv, ev.y) - sh);
         } else {
-            const int64_t f = i - nv - ne;
-            if (!kf[f]) continue;
-            const int64_t o = pf[f];
-            const int32_t sh = nmap > 1 ? (int32_t)B.b[kBRemV][find_base(B.b[kBVert], nmap, tris[3 * f])] : 0;
-            otris[3 * o + 0] = pv[tris[3 * f + 2]] - sh;
-            otris[3 * o + 1] = pv[tris[3 * f + 0]] - sh;
-            otris[3 * o + 2] = pv[tris[3 * f + 1]] - sh;
+            const int64_t wf = w - nwv - nwe;
+            const uint32_t word = __ldg(K.bf + wf);
+            if (!((word >> lane) & 1u)) continue;
+            const int64_t f = wf * 32 + lane;
+            const int64_t o = __ldg(K.pf + wf) + __popc(word & lowm);
+            const int32_t t0 = tris[3 * f], t1 = tris[3 * f + 1], t2 = tris[3 * f + 2];
+            const int32_t sh = nmap > 1 ? (int32_t)B.b[kBRemV][find_base(B.b[kBVert], nmap, t0)] : 0;
+            otris[3 * o + 0] = kept_rank(K.bv, K.pv, t2) - sh;
+            otris[3 * o + 1] = kept_rank(K.bv, K.pv, t0) - sh;
+            otris[3 * o + 2] = kept_rank(K.bv, K.pv, t1) - sh;
         }
     }
 }
@@ -109,13 +118,13 @@ __global__ void uf_init_kernel(int32_t* parent, int32_t n) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) parent[i] = (int32_t)i;
 }
 
-__global__ void uf_union_kernel(const int32_t* __restrict__ mark, const int2* __restrict__ edges,
-                                const int32_t* __restrict__ pv, int32_t ne, int32_t* parent, int* err) {
+__global__ void uf_union_kernel(const int32_t* __restrict__ mark, const int2* __restrict__ edges, Kept K, int32_t ne,
+                                int32_t* parent, int* err) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += stride) {
         if (!mark[e]) continue;
         const int2 ev = edges[e];
-        int32_t a = pv[ev.x], b = pv[ev.y];
+        int32_t a = kept_rank(K.bv, K.pv, ev.x), b = kept_rank(K.bv, K.pv, ev.y);
         bool done = false;
         for (int it = 0; it < (1 << 20); ++it) {
             a = uf_find(parent, a);
@@ -171,28 +180,29 @@ inline int grid_for(vc_ctx* c, int64_t n, int threads) {
 
 }  // namespace
 
+Kept kept_of(vc_ctx* c) {
+    const int64_t nwv = (c->nv + 31) / 32, nwe = (c->ne + 31) / 32;
+    const uint32_t* bits = ptr<uint32_t>(c->keep_bits);
+    return Kept{bits, bits + nwv, bits + nwv + nwe, ptr<int32_t>(c->keep_wv), ptr<int32_t>(c->keep_we),
+                ptr<int32_t>(c->keep_wf)};
+}
+
 int run_remaining(vc_ctx* c, vc_rem_sizes* sizes) {
     if (!c->thin_valid) return VC_ERR_STATE;
     const int64_t nv = c->nv, ne = c->ne, nt = c->nt;
-    VC_TRY(ensure_n<int32_t>(c, c->rem_voff, nv + 1));
-    VC_TRY(ensure_n<int32_t>(c, c->rem_eoff, ne + 1));
-    VC_TRY(ensure_n<int32_t>(c, c->rem_foff, nt + 1));
+    const int64_t nwv = (nv + 31) / 32, nwe = (ne + 31) / 32, nwf = (nt + 31) / 32;
     VC_TRY(ensure_n<int64_t>(c, c->scratch2, 4));
     Region stage(c, "stage_remaining");
-    int32_t *pv = ptr<int32_t>(c->rem_voff), *pe = ptr<int32_t>(c->rem_eoff), *pf = ptr<int32_t>(c->rem_foff);
-    rem_flags_kernel<<<grid_for(c, nv + ne + nt, 256), 256, 0, c->stream>>>(
-        ptr<uint8_t>(c->keep_v), ptr<uint8_t>(c->keep_e), ptr<uint8_t>(c->keep_f), (int32_t)nv, (int32_t)ne,
-        (int32_t)nt, pv, pe, pf);
-    launched(c);
-    VC_CUDA(c, cudaGetLastError());
+    // the thinning left the survivors as bit words with per-word counts
     int64_t* tot = ptr<int64_t>(c->scratch2);
-    VC_TRY(scan_exclusive_i32(c, pv, pv, nv, tot + 0));
-    VC_TRY(scan_exclusive_i32(c, pe, pe, ne, tot + 1));
-    VC_TRY(scan_exclusive_i32(c, pf, pf, nt, tot + 2));
+    VC_TRY(scan_exclusive_i32(c, ptr<int32_t>(c->keep_wv), ptr<int32_t>(c->keep_wv), nwv, tot + 0));
+    VC_TRY(scan_exclusive_i32(c, ptr<int32_t>(c->keep_we), ptr<int32_t>(c->keep_we), nwe, tot + 1));
+    VC_TRY(scan_exclusive_i32(c, ptr<int32_t>(c->keep_wf), ptr<int32_t>(c->keep_wf), nwf, tot + 2));
+    const Kept K = kept_of(c);
     const int nmap = c->cc_batched ? c->nvol : 1;
     if (nmap > 1) {
         rem_bases_kernel<<<(nmap + 256) / 256, 256, 0, c->stream>>>(c->bases, nmap, (int32_t)nv, (int32_t)ne,
-                                                                    (int32_t)nt, pv, pe, pf, tot);
+                                                                    (int32_t)nt, K, tot);
         launched(c);
         c->h_rem_bases.resize(3 * ((size_t)nmap + 1));
         for (int k = 0; k < 3; ++k)
@@ -205,9 +215,8 @@ int run_remaining(vc_ctx* c, vc_rem_sizes* sizes) {
     VC_TRY(ensure_n<float>(c, c->rem_vts, 3 * h[0]));
     VC_TRY(ensure_n<int2>(c, c->rem_edges, h[1]));
     VC_TRY(ensure_n<int32_t>(c, c->rem_tris, 3 * h[2]));
-    rem_write_kernel<<<grid_for(c, nv + ne + nt, 256), 256, 0, c->stream>>>(
-        ptr<uint8_t>(c->keep_v), ptr<uint8_t>(c->keep_e), ptr<uint8_t>(c->keep_f), (int32_t)nv, (int32_t)ne,
-        (int32_t)nt, pv, pe, pf, ptr<float>(c->vts), ptr<int2>(c->edges), ptr<int32_t>(c->tris),
+    rem_write_kernel<<<grid_for(c, 32 * (nwv + nwe + nwf), 256), 256, 0, c->stream>>>(
+        (int32_t)nv, (int32_t)ne, (int32_t)nt, K, ptr<float>(c->vts), ptr<int2>(c->edges), ptr<int32_t>(c->tris),
         ptr<float>(c->rem_vts), ptr<int2>(c->rem_edges), ptr<int32_t>(c->rem_tris), c->bases, nmap);
     launched(c);
     VC_CUDA(c, cudaGetLastError());
@@ -239,9 +248,8 @@ int run_euler_remaining(vc_ctx* c, vc_euler_info* out) {
     if (nvr > 0) {
         uf_init_kernel<<<grid_for(c, nvr, 256), 256, 0, c->stream>>>(parent, (int32_t)nvr);
         launched(c);
-        uf_union_kernel<<<grid_for(c, ne, 256), 256, 0, c->stream>>>(mark, ptr<int2>(c->edges),
-                                                                      ptr<int32_t>(c->rem_voff), (int32_t)ne, parent,
-                                                                      dev_err(c));
+        uf_union_kernel<<<grid_for(c, ne, 256), 256, 0, c->stream>>>(mark, ptr<int2>(c->edges), kept_of(c),
+                                                                      (int32_t)ne, parent, dev_err(c));
         launched(c);
         uf_roots_kernel<<<grid_for(c, nvr, 256), 256, 0, c->stream>>>(parent, (int32_t)nvr, cnt + nmap, c->bases,
                                                                        nmap);

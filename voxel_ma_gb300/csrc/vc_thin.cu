@@ -461,22 +461,49 @@ __global__ void set_thr_kernel(float* thr, float f_t, float l_t) {
 
 // Survivor flags from the records: keep_v = vertex not removed; keep_e =
 // edge not removed and referenced by no remaining face (getRemainedEdges);
-// keep_f = face not removed; removed_e = edge removal tag.
+// keep_f = face not removed; removed_e = edge removal tag.  One warp per 32
+// cells of a kind (vertices, then edges, then faces): the same flags also go
+// out as one bit word per warp with its population count, for the remaining
+// complex's compaction.
 __global__ void export_flags_kernel(const FaceRec* __restrict__ F, const EdgeRec* __restrict__ E,
                                     const VertRec* __restrict__ V, int32_t nv, int32_t ne, int32_t nt, uint8_t* kv,
-                                    uint8_t* ke, uint8_t* kf, uint8_t* re) {
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (int64_t)nv + ne + nt; i += stride) {
-        if (i < nv) {
-            kv[i] = V[i].rm == kAlive;
-        } else if (i < (int64_t)nv + ne) {
-            const int64_t e = i - nv;
-            const int32_t rm = E[e].rm, ref = rs_count(E[e].rs);
-            ke[e] = rm == kAlive && ref == 0;
-            re[e] = rm != kAlive;
+                                    uint8_t* ke, uint8_t* kf, uint8_t* re, uint32_t* __restrict__ bits,
+                                    int32_t* __restrict__ wv, int32_t* __restrict__ we, int32_t* __restrict__ wf) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nwv = ((int64_t)nv + 31) / 32, nwe = ((int64_t)ne + 31) / 32, nwf = ((int64_t)nt + 31) / 32;
+    const int64_t nw = nwv + nwe + nwf;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < nw; w += warps) {
+        bool keep = false;
+        if (w < nwv) {
+            const int64_t i = w * 32 + lane;
+            if (i < nv) {
+                keep = __ldcs(&V[i].rm) == kAlive;
+                kv[i] = keep;
+            }
+        } else if (w < nwv + nwe) {
+            const int64_t e = (w - nwv) * 32 + lane;
+            if (e < ne) {
+                const int4 ea = __ldcs(reinterpret_cast<const int4*>(E + e));
+                const int4 eb = __ldcs(reinterpret_cast<const int4*>(E + e) + 1);
+                const int32_t rm = eb.w, ref = rs_count(((unsigned long long)(uint32_t)ea.w << 32) | (uint32_t)ea.z);
+                keep = rm == kAlive && ref == 0;
+                ke[e] = keep;
+                re[e] = rm != kAlive;
+            }
         } else {
-            const int64_t f = i - nv - ne;
-            kf[f] = F[f].rm == kAlive;
+            const int64_t f = (w - nwv - nwe) * 32 + lane;
+            if (f < nt) {
+                keep = __ldcs(&F[f].rm) == kAlive;
+                kf[f] = keep;
+            }
+        }
+        const uint32_t word = __ballot_sync(0xffffffffu, keep);
+        if (lane == 0) {
+            bits[w] = word;
+            if (w < nwv) wv[w] = __popc(word);
+            else if (w < nwv + nwe) we[w - nwv] = __popc(word);
+            else wf[w - nwv - nwe] = __popc(word);
         }
     }
 }
@@ -612,10 +639,18 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats) {
         launched(c);
         if (c->thin_lock) VC_CUDA(c, cudaStreamSynchronize(c->stream));
     }
-    export_flags_kernel<<<grid_for(c, nv + ne + nt, 256), 256, 0, c->stream>>>(
-        A.F, A.E, A.V, (int32_t)nv, (int32_t)ne, (int32_t)nt, ptr<uint8_t>(c->keep_v), ptr<uint8_t>(c->keep_e),
-        ptr<uint8_t>(c->keep_f), ptr<uint8_t>(c->removed_e));
-    launched(c);
+    {
+        const int64_t nwv = (nv + 31) / 32, nwe = (ne + 31) / 32, nwf = (nt + 31) / 32;
+        VC_TRY(ensure_n<uint32_t>(c, c->keep_bits, nwv + nwe + nwf + 1));
+        VC_TRY(ensure_n<int32_t>(c, c->keep_wv, nwv + 1));
+        VC_TRY(ensure_n<int32_t>(c, c->keep_we, nwe + 1));
+        VC_TRY(ensure_n<int32_t>(c, c->keep_wf, nwf + 1));
+        export_flags_kernel<<<grid_for(c, 32 * (nwv + nwe + nwf), 256), 256, 0, c->stream>>>(
+            A.F, A.E, A.V, (int32_t)nv, (int32_t)ne, (int32_t)nt, ptr<uint8_t>(c->keep_v), ptr<uint8_t>(c->keep_e),
+            ptr<uint8_t>(c->keep_f), ptr<uint8_t>(c->removed_e), ptr<uint32_t>(c->keep_bits), ptr<int32_t>(c->keep_wv),
+            ptr<int32_t>(c->keep_we), ptr<int32_t>(c->keep_wf));
+        launched(c);
+    }
     int64_t h[5];
     VC_CUDA(c, cudaMemcpyAsync(h, ctl, 5 * sizeof(int64_t), cudaMemcpyDeviceToHost, c->stream));
     int s = sync_check(c);
