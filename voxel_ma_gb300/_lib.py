@@ -105,6 +105,7 @@ SIGNATURES = {
     "vc_debug_thin_trace": (c_int, [c_vp, c_int, c_int]),
     "vc_debug_get_thin_trace": (c_int, [c_vp, c_vp, c_int, ctypes.POINTER(c_int)]),
     "vc_debug_ft_wide": (c_int, [c_vp, c_int]),
+    "vc_debug_thin_shape": (c_int, [c_vp, c_int, c_int]),
     "vc_run_plain": (c_int, [c_vp, c_vp, c_int, c_int, c_int, c_int, ctypes.c_double, ctypes.POINTER(PlainResult)]),
 }
 

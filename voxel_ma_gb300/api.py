@@ -114,6 +114,10 @@ class Context:
     def debug_thin_trace(self, cap: int = 4096, blocks_per_sm: int = 0):
         self.check(self.lib.vc_debug_thin_trace(self.h, cap, blocks_per_sm), "vc_debug_thin_trace")
 
+    def debug_thin_shape(self, threads: int = 0, blocks_per_sm: int = 0):
+        """Launch shape of the thinning kernel (identical results)."""
+        self.check(self.lib.vc_debug_thin_shape(self.h, threads, blocks_per_sm), "vc_debug_thin_shape")
+
     def debug_ft_wide(self, wide: bool = True):
         """Force 64-bit arithmetic in the feature transform (identical results)."""
         self.check(self.lib.vc_debug_ft_wide(self.h, 1 if wide else 0), "vc_debug_ft_wide")

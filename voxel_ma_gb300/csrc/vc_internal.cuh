@@ -231,6 +231,7 @@ struct vc_ctx {
     vc::DevBuf trace;           // optional per-generation trace of the thinning kernel
     int trace_cap = 0, trace_gens = 0;
     int thin_blocks_per_sm = 0;  // 0 = library default
+    int thin_threads = 0;        // threads per block of the thinning kernel (0 = library default)
     bool ft_force_wide = false;  // feature transform: 64-bit arithmetic at every size
     std::mutex* thin_lock = nullptr;  // shared by contexts whose thinning kernels must not overlap
     // remaining complex

@@ -206,11 +206,12 @@ __device__ __forceinline__ void append_cell(int32_t* region, int* s_count, bool 
     if (want) region[basei + __popc(m & ((1u << lane) - 1u))] = code;
 }
 
-__global__ void __launch_bounds__(kThreads) thin_generations_kernel(ThinArgs A) {
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS) thin_generations_kernel(ThinArgs A) {
     __shared__ int64_t sm[33];
     __shared__ int64_t s_red[2];
     __shared__ int s_ncell, s_start, s_gbase;
-    __shared__ int32_t s_cells[4 * kThreads];
+    __shared__ int32_t s_cells[4 * THREADS];
     const int G = gridDim.x, b = blockIdx.x;
     const float f_t = A.thr[0], l_t = A.thr[1];
     int64_t n = A.ctl[0];
@@ -241,16 +242,19 @@ __global__ void __launch_bounds__(kThreads) thin_generations_kernel(ThinArgs A) 
             slots_ready = n;
         }
         // ---- phase A: apply the removals of the items that won their claim
-        // items are taken in 256-item pieces from a shared cursor, so that
-        // blocks finishing early take more (the per-item cost varies)
+        // items are taken in blockDim-item pieces from a shared cursor, so
+        // that blocks finishing early take more (the per-item cost varies);
+        // the next piece is claimed while the current one is processed
+        if (threadIdx.x == 0) {
+            s_start = atomicAdd(ctr + 1, (int)blockDim.x);
+            s_ncell = 0;
+        }
         for (;;) {
-            if (threadIdx.x == 0) {
-                s_start = atomicAdd(ctr + 1, (int)blockDim.x);
-                s_ncell = 0;
-            }
             __syncthreads();
             const int64_t r0 = s_start;
             if (r0 >= n) break;
+            int next_start = 0;
+            if (threadIdx.x == 0) next_start = atomicAdd(ctr + 1, (int)blockDim.x);
             const int64_t i = r0 + threadIdx.x;
             int32_t one[4] = {-1, -1, -1, -1};  // cells whose count fell to 1 here
             if (i < n) {
@@ -321,6 +325,10 @@ __global__ void __launch_bounds__(kThreads) thin_generations_kernel(ThinArgs A) 
             __syncthreads();
             for (int k = threadIdx.x; k < s_ncell; k += blockDim.x) A.cells[s_gbase + k] = s_cells[k];
             __syncthreads();
+            if (threadIdx.x == 0) {
+                s_start = next_start;
+                s_ncell = 0;
+            }
         }
         grid_barrier(A.bar, A.err, A.spin_limit);
         if (*((volatile int*)A.err)) break;
@@ -615,10 +623,12 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats) {
         VC_CUDA(c, cudaGetLastError());
     }
     // persistent cooperative launch: every block resident
+    const int threads = c->thin_threads == 256 ? 256 : 512;
+    void* kern = threads == 512 ? (void*)thin_generations_kernel<512> : (void*)thin_generations_kernel<256>;
     int per_sm = 0;
-    VC_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, thin_generations_kernel, kThreads, 0));
+    VC_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, 0));
     if (per_sm <= 0) return VC_ERR_CUDA;
-    const int G = c->num_sms * std::min(per_sm, c->thin_blocks_per_sm > 0 ? c->thin_blocks_per_sm : 8);
+    const int G = c->num_sms * std::min(per_sm, c->thin_blocks_per_sm > 0 ? c->thin_blocks_per_sm : 2048 / threads);
     VC_TRY(ensure_n<int64_t>(c, c->blk_cnt, 2 * (int64_t)G + 8));
     VC_CUDA(c, cudaMemsetAsync(c->blk_cnt.p, 0, (2 * (int64_t)G + 8) * sizeof(int64_t), c->stream));
     A.blk_cnt = ptr<int64_t>(c->blk_cnt);
@@ -634,8 +644,7 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats) {
             lk = std::unique_lock<std::mutex>(*c->thin_lock);
         }
         Region r(c, "thin_generations");
-        VC_CUDA(c, cudaLaunchCooperativeKernel((void*)thin_generations_kernel, dim3(G), dim3(kThreads), args, 0,
-                                               c->stream));
+        VC_CUDA(c, cudaLaunchCooperativeKernel(kern, dim3(G), dim3(threads), args, 0, c->stream));
         launched(c);
         if (c->thin_lock) VC_CUDA(c, cudaStreamSynchronize(c->stream));
     }
@@ -679,6 +688,13 @@ extern "C" {
 int vc_debug_thin_trace(vc_ctx* c, int cap, int blocks_per_sm) {
     if (!c) return VC_ERR_ARG;
     c->trace_cap = cap > 0 ? cap : 0;
+    c->thin_blocks_per_sm = blocks_per_sm;
+    return VC_OK;
+}
+
+int vc_debug_thin_shape(vc_ctx* c, int threads, int blocks_per_sm) {
+    if (!c || (threads != 0 && threads != 256 && threads != 512) || blocks_per_sm < 0) return VC_ERR_ARG;
+    c->thin_threads = threads;
     c->thin_blocks_per_sm = blocks_per_sm;
     return VC_OK;
 }
