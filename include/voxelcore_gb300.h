@@ -268,9 +268,9 @@ int vc_extract_sites_noalloc(const uint8_t* occ, int X, int Y, int Z, float* xyz
  * blocks per SM (0 = default).                                             */
 int vc_debug_thin_trace(vc_ctx* ctx, int cap, int blocks_per_sm);
 int vc_debug_get_thin_trace(vc_ctx* ctx, int64_t* out, int cap, int* ngen);
-/* Launch shape of the thinning kernel: threads per block (256 or 512; 0 =
- * library default) and blocks per SM (0 = as many as fit).  Results do not
- * depend on it.                                                            */
+/* Launch shape of the thinning kernel: threads per block (256, 512 or 1024;
+ * 0 = library default) and blocks per SM (0 = library default).  Results do
+ * not depend on it.                                                        */
 int vc_debug_thin_shape(vc_ctx* ctx, int threads, int blocks_per_sm);
 /* With wide != 0 the feature transform's envelope passes use 64-bit
  * arithmetic even when every lattice axis is below 2048 (where 32-bit

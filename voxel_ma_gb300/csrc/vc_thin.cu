@@ -206,8 +206,8 @@ __device__ __forceinline__ void append_cell(int32_t* region, int* s_count, bool 
     if (want) region[basei + __popc(m & ((1u << lane) - 1u))] = code;
 }
 
-template <int THREADS>
-__global__ void __launch_bounds__(THREADS) thin_generations_kernel(ThinArgs A) {
+template <int THREADS, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArgs A) {
     __shared__ int64_t sm[33];
     __shared__ int64_t s_red[2];
     __shared__ int s_ncell, s_start, s_gbase;
@@ -623,8 +623,12 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats) {
         VC_CUDA(c, cudaGetLastError());
     }
     // persistent cooperative launch: every block resident
-    const int threads = c->thin_threads == 256 ? 256 : 512;
-    void* kern = threads == 512 ? (void*)thin_generations_kernel<512> : (void*)thin_generations_kernel<256>;
+    // launch shapes: 256 x 8, 512 x 4 (32 registers), 512 x 2, 1024 x 1 per SM
+    const int threads = c->thin_threads == 256 ? 256 : (c->thin_threads == 1024 ? 1024 : 512);
+    void* kern = threads == 256    ? (void*)thin_generations_kernel<256, 8>
+                 : threads == 1024 ? (void*)thin_generations_kernel<1024, 1>
+                 : (c->thin_blocks_per_sm >= 3) ? (void*)thin_generations_kernel<512, 4>
+                                                : (void*)thin_generations_kernel<512, 2>;
     int per_sm = 0;
     VC_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, 0));
     if (per_sm <= 0) return VC_ERR_CUDA;
@@ -693,7 +697,8 @@ int vc_debug_thin_trace(vc_ctx* c, int cap, int blocks_per_sm) {
 }
 
 int vc_debug_thin_shape(vc_ctx* c, int threads, int blocks_per_sm) {
-    if (!c || (threads != 0 && threads != 256 && threads != 512) || blocks_per_sm < 0) return VC_ERR_ARG;
+    if (!c || (threads != 0 && threads != 256 && threads != 512 && threads != 1024) || blocks_per_sm < 0)
+        return VC_ERR_ARG;
     c->thin_threads = threads;
     c->thin_blocks_per_sm = blocks_per_sm;
     return VC_OK;
