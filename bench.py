@@ -276,6 +276,12 @@ def run_gpu(args):
         torch.cuda.synchronize(dev)
         ctx.sync()
 
+    # ---- autotuner (outside the timed region): launch shapes for this input
+    tuned = None
+    if not args.no_tune:
+        ctx.set_volume(occ_dev)
+        tuned = ctx.autotune(args.t)
+
     # ---- device-resident value ------------------------------------------
     clocks = ClockSampler(local)
     clocks.wait_ready()
@@ -375,6 +381,7 @@ def run_gpu(args):
         "clocks": clk,
         "fp64_rescues": 0,
         "lambda_note": "lambda = sqrt of an exact integer squared distance (< 2^24) in IEEE f32: no FP64 rescue needed",
+        "tuned": tuned,
     }
     if not args.no_batch:
         line["batched"] = run_batched(ctx, dev, args, stream)
@@ -421,6 +428,11 @@ def run_batched(ctx, dev, args, stream):
     def batched():
         ctx.batch_set_volumes(occ=occ_dev, dims=dims)
         return ctx.batch_run(args.t, euler=False)
+
+    tuned = None
+    if not args.no_tune:  # the batch's own launch shapes (outside the timed region)
+        ctx.batch_set_volumes(occ=occ_dev, dims=dims)
+        tuned = ctx.autotune(args.t)
 
     def loop():
         return [ctx.run_plain(v, args.t)["rem"] for v in views]
@@ -479,6 +491,7 @@ def run_batched(ctx, dev, args, stream):
         "e2e": {"value": nvox / (e_mean / 1e3), "unit": UNIT, "h2d_bytes_per_step": nvox,
                 "d2h_bytes_per_step": s["nv"] * 12 + s["ne"] * 8 + s["nt"] * 12, "ms_per_step": e_mean},
         "parity": f"{same}/{BATCH_N} volumes: batched remaining-complex sizes equal the plain path's",
+        "tuned": tuned,
         "thin_generations": ctx.batch_stats["generations"],
         "cells": {"V": ctx.vd_sizes["nv"], "E": ctx.vd_sizes["ne"], "T": ctx.vd_sizes["nt"]},
     }
@@ -600,6 +613,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-path measurement")
     ap.add_argument("--no-serve", action="store_true", help="skip the request-stream measurement")
+    ap.add_argument("--no-tune", action="store_true", help="keep the library's default launch shapes")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -261,6 +261,27 @@ int vc_plan_batches(int n, const int64_t* voxels, const double* t, int64_t share
 int vc_extract_sites_noalloc(const uint8_t* occ, int X, int Y, int Z, float* xyz, int64_t capacity, int64_t* n_sites,
                              void* stream);
 
+/* ---- autotuner -----------------------------------------------------------
+ * Chooses, for the volume or batch installed in the context (vc_set_volume
+ * or vc_batch_set_volumes), the launch shapes of the two kernels whose best
+ * shape depends on the input: the feature transform's envelope passes (how
+ * many stack entries of each line stay in shared memory: 4, 8 or 16) and
+ * the thinning kernel (threads per block and blocks per SM: 512 x 2,
+ * 512 x 4, 256 x 8, 1024 x 1).  Each candidate runs on the installed input
+ * and is timed with CUDA events on the context's stream (after one untimed
+ * run); the fastest stays in the context for every later run of it.  Results
+ * never depend on these shapes.  t is the thinning's threshold factor, as
+ * in vc_run_plain.  The reference has no counterpart (it is single-threaded
+ * C++).                                                                    */
+typedef struct {
+    int ft_ring;                /* chosen */
+    int thin_threads;           /* chosen */
+    int thin_blocks_per_sm;     /* chosen */
+    float ft_ms[3];             /* both envelope passes, ring 4 / 8 / 16 */
+    float thin_ms[4];           /* thinning kernel, 512x2 / 512x4 / 256x8 / 1024x1 */
+} vc_tune_result;
+int vc_autotune(vc_ctx* ctx, double t, vc_tune_result* out);
+
 /* ---- diagnostics ---------------------------------------------------------
  * Per-generation trace of the thinning kernel: with cap > 0 the next vc_thin
  * records, for up to `cap` generations, {items, t_phaseA, t_phaseB, t_phaseC}

@@ -114,6 +114,16 @@ class Context:
     def debug_thin_trace(self, cap: int = 4096, blocks_per_sm: int = 0):
         self.check(self.lib.vc_debug_thin_trace(self.h, cap, blocks_per_sm), "vc_debug_thin_trace")
 
+    def autotune(self, t: float = 0.04) -> dict:
+        """Time the input-dependent launch shapes on the installed volume or
+        batch and keep the fastest (vc_autotune); returns the choice and the
+        measured milliseconds per candidate."""
+        r = L.TuneResult()
+        self.check(self.lib.vc_autotune(self.h, ctypes.c_double(t), ctypes.byref(r)), "vc_autotune")
+        return dict(ft_ring=r.ft_ring, thin_threads=r.thin_threads, thin_blocks_per_sm=r.thin_blocks_per_sm,
+                    ft_ms={k: round(float(v), 4) for k, v in zip((4, 8, 16), r.ft_ms)},
+                    thin_ms={k: round(float(v), 4) for k, v in zip(("512x2", "512x4", "256x8", "1024x1"), r.thin_ms)})
+
     def debug_thin_shape(self, threads: int = 0, blocks_per_sm: int = 0):
         """Launch shape of the thinning kernel (identical results)."""
         self.check(self.lib.vc_debug_thin_shape(self.h, threads, blocks_per_sm), "vc_debug_thin_shape")

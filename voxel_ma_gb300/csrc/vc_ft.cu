@@ -151,31 +151,38 @@ __global__ void __launch_bounds__(kEnvThreads) ft_envelope_kernel(const int64_t*
     }
 }
 
-constexpr int kRing = 8;
-constexpr size_t kEnvSmem = (size_t)kRing * kEnvThreads * (sizeof(int64_t) + sizeof(int32_t));
+template <int RING>
+constexpr size_t env_smem() {
+    return (size_t)RING * kEnvThreads * (sizeof(int64_t) + sizeof(int32_t));
+}
 
-template <int PASS, class I>
+template <int PASS, class I, int RING>
 int launch_envelope_t(vc_ctx* c, const int64_t* in, int64_t* out, int32_t* d2o, int32_t* ido, int32_t* gmeta,
                       int64_t* gval, int64_t nlines) {
-    auto kern = ft_envelope_kernel<PASS, kRing, I>;
-    VC_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kEnvSmem));
+    auto kern = ft_envelope_kernel<PASS, RING, I>;
+    constexpr size_t smem = env_smem<RING>();
+    VC_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
-    VC_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kEnvThreads, kEnvSmem));
+    VC_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kEnvThreads, smem));
     per_sm = std::max(per_sm, 1);
     const int blocks = (int)std::max<int64_t>(
         1, std::min<int64_t>((nlines + kEnvThreads - 1) / kEnvThreads, (int64_t)c->num_sms * per_sm));
-    kern<<<blocks, kEnvThreads, kEnvSmem, c->stream>>>(in, out, d2o, ido, gmeta, gval, c->tab);
+    kern<<<blocks, kEnvThreads, smem, c->stream>>>(in, out, d2o, ido, gmeta, gval, c->tab);
     launched(c);
     VC_CUDA(c, cudaGetLastError());
     return VC_OK;
 }
 
-// int32 arithmetic when every lattice axis of the batch is below 2048
+// int32 arithmetic when every lattice axis of the batch is below 2048; the
+// ring (stack entries kept in shared memory per line) is the context's
+// tuned size (4, 8 or 16; 8 by default)
 template <int PASS>
 int launch_envelope(vc_ctx* c, bool small, const int64_t* in, int64_t* out, int32_t* d2o, int32_t* ido,
                     int32_t* gmeta, int64_t* gval, int64_t nlines) {
-    return small ? launch_envelope_t<PASS, int32_t>(c, in, out, d2o, ido, gmeta, gval, nlines)
-                 : launch_envelope_t<PASS, int64_t>(c, in, out, d2o, ido, gmeta, gval, nlines);
+    if (!small) return launch_envelope_t<PASS, int64_t, 8>(c, in, out, d2o, ido, gmeta, gval, nlines);
+    if (c->ft_ring == 4) return launch_envelope_t<PASS, int32_t, 4>(c, in, out, d2o, ido, gmeta, gval, nlines);
+    if (c->ft_ring == 16) return launch_envelope_t<PASS, int32_t, 16>(c, in, out, d2o, ido, gmeta, gval, nlines);
+    return launch_envelope_t<PASS, int32_t, 8>(c, in, out, d2o, ido, gmeta, gval, nlines);
 }
 
 }  // namespace

@@ -233,6 +233,7 @@ struct vc_ctx {
     int thin_blocks_per_sm = 0;  // 0 = library default
     int thin_threads = 0;        // threads per block of the thinning kernel (0 = library default)
     bool ft_force_wide = false;  // feature transform: 64-bit arithmetic at every size
+    int ft_ring = 8;             // feature transform: envelope stack entries in shared memory per line
     std::mutex* thin_lock = nullptr;  // shared by contexts whose thinning kernels must not overlap
     // remaining complex
     bool rem_valid = false;
