@@ -212,7 +212,7 @@ __device__ __forceinline__ float rec_measure(float m, const float* thr, int bv) 
 // bounding boxes (VoroInfo::getInsidePartSize reads them), reduced per block.
 // One block per lattice row along z (volume bv, a, b); blockDim is a
 // multiple of 32 so each warp covers one segment.
-__global__ void __launch_bounds__(128) vd_segments_kernel(const uint8_t* __restrict__ occ,
+__global__ void __launch_bounds__(128, 6) vd_segments_kernel(const uint8_t* __restrict__ occ,
                                                           const int32_t* __restrict__ lab, VolTab T,
                                                           SegPlanes* __restrict__ planes, int32_t* __restrict__ cv,
                                                           int32_t* __restrict__ ce, int32_t* __restrict__ cf,
