@@ -437,7 +437,7 @@ __device__ __forceinline__ void for_plaquette_d(int d, const Segs& S, int a, int
 // (incident triangles counted, summed and tested against the threshold;
 // measure = max lambda of the incident faces, voroinfo.cpp:1490-1538).
 // Face lambdas come from lamf (one per face, written by vd_faces_kernel).
-__global__ void __launch_bounds__(128) vd_edges_kernel(VolTab T, Bases B, const SegPlanes* __restrict__ planes,
+__global__ void __launch_bounds__(128, 8) vd_edges_kernel(VolTab T, Bases B, const SegPlanes* __restrict__ planes,
                                                        const int32_t* __restrict__ vb, const int32_t* __restrict__ eb,
                                                        const int32_t* __restrict__ fbs, const float* __restrict__ lamf,
                                                        int2* __restrict__ edges, EdgeRec* __restrict__ E,
@@ -497,7 +497,7 @@ __global__ void __launch_bounds__(128) vd_edges_kernel(VolTab T, Bases B, const 
 // The row's faces: two triangles each (util::simpleTriangulate of the quad
 // (q0,q1,q2,q3): (q3,q0,q1), (q3,q1,q2)), the diagonal edge (q1,q3) and,
 // with records, the thinning records of both triangles and the diagonal.
-__global__ void __launch_bounds__(128) vd_faces_kernel(VolTab T, Bases B, const SegPlanes* __restrict__ planes,
+__global__ void __launch_bounds__(128, 8) vd_faces_kernel(VolTab T, Bases B, const SegPlanes* __restrict__ planes,
                                                        const int32_t* __restrict__ vb, const int32_t* __restrict__ eb,
                                                        const int32_t* __restrict__ fbs, const int32_t* __restrict__ lab,
                                                        const float* __restrict__ sxyz, float* __restrict__ lamf,
