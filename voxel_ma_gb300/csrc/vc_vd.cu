@@ -181,6 +181,17 @@ __device__ __forceinline__ bool fbit_at(const Segs& S, int a, int b, int c, int 
     return bit(plane_f(load_planes(S.planes + S.at(a, b, c)), d), c);
 }
 
+// Segment loop of the emission kernels: each block takes kSegChunk
+// consecutive segments at a time and its warps walk them in order, so the
+// neighbouring segments a warp reads stay in the block's L1 (rows of every
+// length pack into chunks, which keeps small volumes of a batch busy).
+constexpr int kSegChunk = 64;
+#define SEG_LOOP(gs, nseg)                                                                                \
+    for (int64_t seg_base_ = (int64_t)blockIdx.x * kSegChunk; seg_base_ < (nseg);                          \
+         seg_base_ += (int64_t)gridDim.x * kSegChunk)                                                        \
+        for (int64_t gs = seg_base_ + (threadIdx.x >> 5), seg_end_ = min((int64_t)(nseg), seg_base_ + kSegChunk); \
+             gs < seg_end_; gs += blockDim.x >> 5)
+
 // Batch-wide cell ids are volume-major (vertices; axis edges then
 // diagonals; triangles).  The scans count axis edges and faces over the
 // whole batch, so in volume bv an axis edge of scan rank e has id
@@ -218,7 +229,6 @@ __global__ void __launch_bounds__(128, 6) vd_segments_kernel(const uint8_t* __re
                                                           int32_t* __restrict__ ce, int32_t* __restrict__ cf,
                                                           int32_t* __restrict__ bbox_all) {
     const int lane = threadIdx.x & 31;
-    const int64_t nrows = T.total(kLRow);
     int cur_bv = -1;
     int mn0 = INT32_MAX, mn1 = INT32_MAX, mn2 = INT32_MAX, mx0 = INT32_MIN, mx1 = INT32_MIN, mx2 = INT32_MIN;
     auto flush = [&]() {
@@ -239,18 +249,20 @@ __global__ void __launch_bounds__(128, 6) vd_segments_kernel(const uint8_t* __re
         mn0 = mn1 = mn2 = INT32_MAX;
         mx0 = mx1 = mx2 = INT32_MIN;
     };
-    for (int64_t grow = blockIdx.x; grow < nrows; grow += gridDim.x) {
-        const int bv = T.find(kLRow, grow);
+    const int64_t nseg = T.total(kLSeg);
+    SEG_LOOP(gs, nseg) {
+        const int bv = T.find(kLSeg, gs);
         if (bv != cur_bv) {
             flush();
             cur_bv = bv;
         }
         const Grid g = grid_of(T, bv, occ, lab);
-        const int64_t row = grow - T.start(kLRow, bv);
+        const int nsr_ = (T.dim(bv).z + 32) / 32;
+        const int64_t ls_ = gs - T.start(kLSeg, bv);
+        const int64_t row = ls_ / nsr_;
+        const int c0 = (int)(ls_ - row * nsr_) * 32;
         const int a = (int)(row / g.NB), b = (int)(row - (int64_t)a * g.NB);
-        const int nsr = (int)((g.NC + 31) / 32);
-        const int64_t seg_row = T.start(kLSeg, bv) + row * nsr;
-        for (int c0 = threadIdx.x & ~31; c0 < nsr * 32; c0 += blockDim.x) {
+        {
             const int c = c0 + lane;
             uint32_t f = 0;
             if (c < (int)g.NC) {
@@ -300,7 +312,7 @@ __global__ void __launch_bounds__(128, 6) vd_segments_kernel(const uint8_t* __re
             P.f2 = __ballot_sync(0xffffffffu, f & 4u);
             P.pad = 0;
             if (lane == 0) {
-                const int64_t s = seg_row + (c0 >> 5);
+                const int64_t s = gs;
                 reinterpret_cast<uint4*>(planes + s)[0] = make_uint4(P.v, P.e0, P.e1, P.e2);
                 reinterpret_cast<uint4*>(planes + s)[1] = make_uint4(P.f0, P.f1, P.f2, 0u);
                 cv[s] = __popc(P.v);
@@ -324,14 +336,17 @@ __global__ void __launch_bounds__(128) vd_vertices_kernel(VolTab T, Bases B, con
                                                           VertRec* __restrict__ V, const EdgeRec* __restrict__ E,
                                                           int32_t* __restrict__ g0, int64_t ne) {
     const int lane = threadIdx.x & 31;
-    const int64_t nrows = T.total(kLRow);
-    for (int64_t grow = blockIdx.x; grow < nrows; grow += gridDim.x) {
-        const int bv = T.find(kLRow, grow);
+    const int64_t nseg = T.total(kLSeg);
+    SEG_LOOP(gs, nseg) {
+        const int bv = T.find(kLSeg, gs);
         const Segs S = segs_of(T, bv, planes, vb, eb, fbs);
         const Shift sh = shift_of(B, bv);
-        const int64_t row = grow - T.start(kLRow, bv);
+        const int nsr_ = (T.dim(bv).z + 32) / 32;
+        const int64_t ls_ = gs - T.start(kLSeg, bv);
+        const int64_t row = ls_ / nsr_;
+        const int c0 = (int)(ls_ - row * nsr_) * 32;
         const int a = (int)(row / S.NB), b = (int)(row - (int64_t)a * S.NB);
-        for (int c0 = threadIdx.x & ~31; c0 < S.nsr * 32; c0 += blockDim.x) {
+        {
             const int c = c0 + lane;
             const int64_t s = S.at(a, b, c);
             const SegPlanes P = load_planes(planes + s);
@@ -443,15 +458,18 @@ __global__ void __launch_bounds__(128, 8) vd_edges_kernel(VolTab T, Bases B, con
                                                        int2* __restrict__ edges, EdgeRec* __restrict__ E,
                                                        int32_t* __restrict__ g0, const float* __restrict__ thr) {
     const int lane = threadIdx.x & 31;
-    const int64_t nrows = T.total(kLRow);
-    for (int64_t grow = blockIdx.x; grow < nrows; grow += gridDim.x) {
-        const int bv = T.find(kLRow, grow);
+    const int64_t nseg = T.total(kLSeg);
+    SEG_LOOP(gs, nseg) {
+        const int bv = T.find(kLSeg, gs);
         const Segs S = segs_of(T, bv, planes, vb, eb, fbs);
         const Shift sh = shift_of(B, bv);
-        const int64_t row = grow - T.start(kLRow, bv);
+        const int nsr_ = (T.dim(bv).z + 32) / 32;
+        const int64_t ls_ = gs - T.start(kLSeg, bv);
+        const int64_t row = ls_ / nsr_;
+        const int c0 = (int)(ls_ - row * nsr_) * 32;
         const int a = (int)(row / S.NB), b = (int)(row - (int64_t)a * S.NB);
         const float tb = thr ? thr[bv] : 0.0f;
-        for (int c0 = threadIdx.x & ~31; c0 < S.nsr * 32; c0 += blockDim.x) {
+        {
             const int c = c0 + lane;
             const int64_t s = S.at(a, b, c);
             const SegPlanes P = load_planes(planes + s);
@@ -505,17 +523,20 @@ __global__ void __launch_bounds__(128, 8) vd_faces_kernel(VolTab T, Bases B, con
                                                        FaceRec* __restrict__ F, EdgeRec* __restrict__ E,
                                                        int32_t* __restrict__ g0, const float* __restrict__ thr) {
     const int lane = threadIdx.x & 31;
-    const int64_t nrows = T.total(kLRow);
-    for (int64_t grow = blockIdx.x; grow < nrows; grow += gridDim.x) {
-        const int bv = T.find(kLRow, grow);
+    const int64_t nseg = T.total(kLSeg);
+    SEG_LOOP(gs, nseg) {
+        const int bv = T.find(kLSeg, gs);
         const Segs S = segs_of(T, bv, planes, vb, eb, fbs);
         const Shift sh = shift_of(B, bv);
         const int32_t* lb = lab + T.start(kLat, bv);
         const int64_t NC = T.dim(bv).z + 1;
-        const int64_t row = grow - T.start(kLRow, bv);
+        const int nsr_ = (T.dim(bv).z + 32) / 32;
+        const int64_t ls_ = gs - T.start(kLSeg, bv);
+        const int64_t row = ls_ / nsr_;
+        const int c0 = (int)(ls_ - row * nsr_) * 32;
         const int a = (int)(row / S.NB), b = (int)(row - (int64_t)a * S.NB);
         const int32_t fbv = (int32_t)sh.fb;
-        for (int c0 = threadIdx.x & ~31; c0 < S.nsr * 32; c0 += blockDim.x) {
+        {
             const int c = c0 + lane;
             const int64_t s = S.at(a, b, c);
             const SegPlanes P = load_planes(planes + s);
@@ -597,19 +618,22 @@ __global__ void __launch_bounds__(128) vd_aux_kernel(VolTab T, Bases B, const Se
                                                      int32_t* __restrict__ tri_face, int2* __restrict__ face_sites,
                                                      int32_t* __restrict__ tri_edges) {
     const int lane = threadIdx.x & 31;
-    const int64_t nrows = T.total(kLRow);
-    for (int64_t grow = blockIdx.x; grow < nrows; grow += gridDim.x) {
-        const int bv = T.find(kLRow, grow);
+    const int64_t nseg = T.total(kLSeg);
+    SEG_LOOP(gs, nseg) {
+        const int bv = T.find(kLSeg, gs);
         const Segs S = segs_of(T, bv, planes, vb, eb, fbs);
         const Shift sh = shift_of(B, bv);
         const int64_t lat0 = T.start(kLat, bv);
         const int32_t* lb = lab + lat0;
         const int64_t NC = T.dim(bv).z + 1;
-        const int64_t row = grow - T.start(kLRow, bv);
+        const int nsr_ = (T.dim(bv).z + 32) / 32;
+        const int64_t ls_ = gs - T.start(kLSeg, bv);
+        const int64_t row = ls_ / nsr_;
+        const int c0 = (int)(ls_ - row * nsr_) * 32;
         const int a = (int)(row / S.NB), b = (int)(row - (int64_t)a * S.NB);
         const int32_t fbv = (int32_t)sh.fb;
         auto lid = [&](int x, int y, int z) { return ((int64_t)x * S.NB + y) * NC + z; };
-        for (int c0 = threadIdx.x & ~31; c0 < S.nsr * 32; c0 += blockDim.x) {
+        {
             const int c = c0 + lane;
             const int64_t s = S.at(a, b, c);
             const SegPlanes P = load_planes(planes + s);
@@ -761,8 +785,9 @@ __global__ void vd_radius_kernel(const uint8_t* __restrict__ occ, const int32_t*
     }
 }
 
-inline int row_grid(vc_ctx* c, int64_t rows) {
-    return (int)std::max<int64_t>(1, std::min<int64_t>(rows, (int64_t)c->num_sms * 32));
+// 128-thread blocks, kSegChunk segments per block at a time (grid-stride)
+inline int seg_grid(vc_ctx* c, int64_t nseg) {
+    return (int)std::max<int64_t>(1, std::min<int64_t>((nseg + kSegChunk - 1) / kSegChunk, (int64_t)c->num_sms * 16));
 }
 
 }  // namespace
@@ -780,7 +805,6 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes, double t_thr) {
             return VC_ERR_ARG;
     const int64_t N = c->h_off[kLat][nvol];
     const int64_t nseg = c->h_off[kLSeg][nvol];
-    const int64_t nrows = c->h_off[kLRow][nvol];
     Region stage(c, "stage_vd");
     VC_TRY(ensure_n<SegPlanes>(c, c->vd_seg, nseg));
     VC_TRY(ensure_n<int32_t>(c, c->vd_voff, nseg));
@@ -795,7 +819,7 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes, double t_thr) {
     launched(c);
     {
         Region r(c, "vd_flags");
-        vd_segments_kernel<<<row_grid(c, nrows), 128, 0, c->stream>>>(ptr<uint8_t>(c->occ), ptr<int32_t>(c->ft_id),
+        vd_segments_kernel<<<seg_grid(c, nseg), 128, 0, c->stream>>>(ptr<uint8_t>(c->occ), ptr<int32_t>(c->ft_id),
                                                                        c->tab, planes, vb, eb, fb, c->bases.bbox);
         launched(c);
         VC_CUDA(c, cudaGetLastError());
@@ -839,7 +863,7 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes, double t_thr) {
         int32_t* g0 = folded ? ptr<int32_t>(c->thin_g0) : nullptr;
         {
             Region k(c, "vd_faces");
-            vd_faces_kernel<<<row_grid(c, nrows), 128, 0, c->stream>>>(
+            vd_faces_kernel<<<seg_grid(c, nseg), 128, 0, c->stream>>>(
                 c->tab, c->bases, planes, vb, eb, fb, ptr<int32_t>(c->ft_id), ptr<float>(c->site_xyz),
                 ptr<float>(c->vd_lam), ptr<int32_t>(c->tris), ptr<int2>(c->edges),
                 folded ? ptr<FaceRec>(c->face_rec) : nullptr, folded ? ptr<EdgeRec>(c->edge_rec) : nullptr, g0, thr);
@@ -847,14 +871,14 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes, double t_thr) {
         }
         {
             Region k(c, "vd_edges");
-            vd_edges_kernel<<<row_grid(c, nrows), 128, 0, c->stream>>>(
+            vd_edges_kernel<<<seg_grid(c, nseg), 128, 0, c->stream>>>(
                 c->tab, c->bases, planes, vb, eb, fb, ptr<float>(c->vd_lam), ptr<int2>(c->edges),
                 folded ? ptr<EdgeRec>(c->edge_rec) : nullptr, g0, thr);
             launched(c);
         }
         {
             Region k(c, "vd_vertices");
-            vd_vertices_kernel<<<row_grid(c, nrows), 128, 0, c->stream>>>(
+            vd_vertices_kernel<<<seg_grid(c, nseg), 128, 0, c->stream>>>(
                 c->tab, c->bases, planes, vb, eb, fb, ptr<float>(c->vts), folded ? ptr<VertRec>(c->vert_rec) : nullptr,
                 folded ? ptr<EdgeRec>(c->edge_rec) : nullptr, g0, ne);
             launched(c);
@@ -913,7 +937,7 @@ int ensure_vd_aux(vc_ctx* c, bool meas, bool topo) {
     }
     {
         Region r(c, "vd_aux");
-        vd_aux_kernel<<<row_grid(c, c->h_off[kLRow][c->nvol]), 128, 0, c->stream>>>(
+        vd_aux_kernel<<<seg_grid(c, c->h_off[kLSeg][c->nvol]), 128, 0, c->stream>>>(
             c->tab, c->bases, ptr<SegPlanes>(c->vd_seg), ptr<int32_t>(c->vd_voff), ptr<int32_t>(c->vd_eoff),
             ptr<int32_t>(c->vd_foff), ptr<int32_t>(c->ft_id), ptr<float>(c->vd_lam), vm, em, fm,
             ptr<int32_t>(c->vd_tri_face), ptr<int2>(c->vd_face_sites), te);
