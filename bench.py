@@ -505,6 +505,7 @@ def run_batched(ctx, dev, args, stream):
 # first come first served (vc_run_plain per request).
 
 SERVE_RATE, SERVE_SECONDS, SERVE_POOL, SERVE_CAP = 200.0, 6.0, 18, 120 << 30
+SERVE_WORKERS, SERVE_MAX_BATCH = 3, 8
 
 
 def serve_pool(dev):
@@ -524,7 +525,7 @@ def serve_pool(dev):
     return pool
 
 
-def run_serving(dev, args):
+def run_serving(dev, args, workers=None, max_batch=None, with_plain=True):
     import threading
 
     from voxel_ma_gb300 import api
@@ -537,7 +538,9 @@ def run_serving(dev, args):
     voxels = np.array([pool[k].size for k in picks], np.int64)
 
     # continuous batching
-    srv = api.Server(dev.index or 0, workers=2, mem_cap_bytes=SERVE_CAP, max_batch=64)
+    workers = workers or SERVE_WORKERS
+    max_batch = max_batch or SERVE_MAX_BATCH
+    srv = api.Server(dev.index or 0, workers=workers, mem_cap_bytes=SERVE_CAP, max_batch=max_batch)
     warm = [srv.submit(pool[k], args.t) for k in range(len(pool))]
     for i in warm:
         srv.wait(i)
@@ -558,6 +561,10 @@ def run_serving(dev, args):
     srv.close()
     lat = np.array([r["latency_ms"] for r in res])
     span = t_end - t0
+    if not with_plain:
+        return {"workers": workers, "max_batch": max_batch, "throughput_req_s": len(arrivals) / span,
+                "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
+                "batches": st["batches"] - SERVE_POOL}
 
     # the plain path: one context, first come first served, same arrivals
     ctx = api.Context(dev.index or 0)
@@ -582,7 +589,7 @@ def run_serving(dev, args):
         "workload": f"poisson{int(SERVE_RATE)}_torus_spheres_grf_edge32_384",
         "arrival_rate_req_s": SERVE_RATE, "requests": n, "duration_s": SERVE_SECONDS,
         "pool": f"{SERVE_POOL} volumes (torus mesh, 32 spheres, GRF sigma 6), edge log-uniform in [32, 384]",
-        "mem_cap_bytes": SERVE_CAP, "workers": 2, "max_batch": 64,
+        "mem_cap_bytes": SERVE_CAP, "workers": workers, "max_batch": max_batch,
         "value": float(voxels.sum() / span), "unit": UNIT, "throughput_req_s": n / span,
         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
         "batches": st["batches"] - SERVE_POOL,  # the warm-up served each pool volume alone
@@ -596,10 +603,10 @@ def run_serving(dev, args):
 
 # DRAM traffic per cell of the complex (V + E + T) of the thinning kernel,
 # from one ncu capture of the 192^3 case of this workload
-# (profiles/kernels_grf192.md: 8.655 GB read + 2.297 GB written for
+# (profiles/kernels_grf192.md: 4.680 GB read + 2.143 GB written for
 # 3,385,169 + 14,026,594 + 10,679,482 cells); the traffic grows with the
 # complex, so the per-launch figure at 512^3 is this rate times its cells.
-TRAFFIC_PER_CELL = {"thin_generations": (8.655230e9 + 2.296893e9) / (3385169 + 14026594 + 10679482)}
+TRAFFIC_PER_CELL = {"thin_generations": (4.679887e9 + 2.142997e9) / (3385169 + 14026594 + 10679482)}
 
 
 def main():

@@ -184,6 +184,40 @@ def test_plain_path_matches_oracle(gpu_ctx, name, occ, t):
     assert eu == O.euler(len(rv), re_, rt)
 
 
+def _boundary_shapes():
+    # lattice rows of 32, 33, 64 and 96 points (segment and word edges), odd
+    # and one-voxel extents
+    rng = np.random.default_rng(21)
+    for shape in [(6, 5, 31), (4, 7, 32), (5, 3, 63), (3, 4, 95), (9, 1, 40), (1, 9, 33), (40, 6, 1)]:
+        yield f"box{shape}", volumes.grf(max(shape), sigma=2.5, seed=sum(shape))[: shape[0], : shape[1], : shape[2]]
+        yield f"noise{shape}", (rng.uniform(size=shape) < 0.6).astype(np.uint8)
+
+
+BOUNDARY = list(_boundary_shapes())
+
+
+@pytest.mark.parametrize("name,occ", BOUNDARY, ids=[v[0] for v in BOUNDARY])
+def test_plain_path_at_segment_boundaries(gpu_ctx, name, occ):
+    """Rows whose lengths sit on the 32-point segment and 32-voxel word edges:
+    every stage of the plain path equals the oracle."""
+    occ = np.ascontiguousarray(occ)
+    ref = O.run_plain(occ, t=0.04)
+    r = gpu_ctx.run_plain(occ, 0.04)
+    assert r["n_sites"] == len(ref["sites"])
+    assert np.array_equal(gpu_ctx.sites(), ref["sites"])
+    d2, ids = gpu_ctx.ft()
+    assert np.array_equal(d2, ref["d2"]) and np.array_equal(ids, ref["ids"])
+    vd = gpu_ctx.vd()
+    for k in ("vts", "edges", "tris", "vm", "em", "fm", "tri_face", "face_sites"):
+        assert np.array_equal(vd[k], ref["vd"][k]), k
+    fl = gpu_ctx.thin_flags()
+    for k in ("keep_v", "keep_e", "keep_f", "removed_e"):
+        assert np.array_equal(fl[k], ref["thin"][k]), k
+    rv, re_, rt = gpu_ctx.remaining_arrays()
+    assert np.array_equal(rv, ref["rem_vts"]) and np.array_equal(re_, ref["rem_edges"])
+    assert np.array_equal(rt, ref["rem_tris"])
+
+
 def test_closed_pocket_and_errors(gpu_ctx):
     vts, edges, tris = octahedron_shell()
     st, fl = _gpu_thin(gpu_ctx, vts, edges, tris, np.zeros(12, np.float32), np.zeros(8, np.float32), 1.0)
