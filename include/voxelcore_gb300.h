@@ -267,7 +267,7 @@ int vc_extract_sites_noalloc(const uint8_t* occ, int X, int Y, int Z, float* xyz
  * shape depends on the input: the feature transform's envelope passes (how
  * many stack entries of each line stay in shared memory: 4, 8 or 16) and
  * the thinning kernel (threads per block and blocks per SM: 512 x 2,
- * 512 x 4, 256 x 8, 1024 x 1).  Each candidate runs on the installed input
+ * 512 x 2 with two items per thread, 512 x 4, 256 x 8, 1024 x 1).  Each candidate runs on the installed input
  * and is timed with CUDA events on the context's stream (after one untimed
  * run); the fastest stays in the context for every later run of it.  Results
  * never depend on these shapes.  t is the thinning's threshold factor, as
@@ -278,7 +278,8 @@ typedef struct {
     int thin_threads;           /* chosen */
     int thin_blocks_per_sm;     /* chosen */
     float ft_ms[3];             /* both envelope passes, ring 4 / 8 / 16 */
-    float thin_ms[4];           /* thinning kernel, 512x2 / 512x4 / 256x8 / 1024x1 */
+    int thin_items;             /* chosen: items per thread in the thinning's first phase */
+    float thin_ms[5];           /* thinning kernel, 512x2 / 512x2 with 2 items / 512x4 / 256x8 / 1024x1 */
 } vc_tune_result;
 int vc_autotune(vc_ctx* ctx, double t, vc_tune_result* out);
 
@@ -290,9 +291,10 @@ int vc_autotune(vc_ctx* ctx, double t, vc_tune_result* out);
 int vc_debug_thin_trace(vc_ctx* ctx, int cap, int blocks_per_sm);
 int vc_debug_get_thin_trace(vc_ctx* ctx, int64_t* out, int cap, int* ngen);
 /* Launch shape of the thinning kernel: threads per block (256, 512 or 1024;
- * 0 = library default) and blocks per SM (0 = library default).  Results do
- * not depend on it.                                                        */
-int vc_debug_thin_shape(vc_ctx* ctx, int threads, int blocks_per_sm);
+ * 0 = library default), blocks per SM (0 = library default) and items per
+ * thread in its first phase (1 or 2, 512 x 2 only; 0 = 1).  Results do not
+ * depend on it.                                                            */
+int vc_debug_thin_shape(vc_ctx* ctx, int threads, int blocks_per_sm, int items);
 /* With wide != 0 the feature transform's envelope passes use 64-bit
  * arithmetic even when every lattice axis is below 2048 (where 32-bit
  * arithmetic is exact and is the default); results are identical.         */

@@ -18,7 +18,8 @@ def test_autotune_keeps_results(gpu_ctx):
     ctx.set_volume(occ)
     tuned = ctx.autotune(0.04)
     assert tuned["ft_ring"] in (4, 8, 16)
-    assert (tuned["thin_threads"], tuned["thin_blocks_per_sm"]) in ((512, 2), (512, 4), (256, 8), (1024, 1))
+    assert (tuned["thin_threads"], tuned["thin_blocks_per_sm"], tuned["thin_items"]) in (
+        (512, 2, 1), (512, 2, 2), (512, 4, 1), (256, 8, 1), (1024, 1, 1))
     assert all(v > 0 for v in tuned["ft_ms"].values()) and all(v > 0 for v in tuned["thin_ms"].values())
     r = ctx.run_plain(occ, 0.04)
     fl = ctx.thin_flags()
@@ -26,13 +27,13 @@ def test_autotune_keeps_results(gpu_ctx):
     for k in ("keep_v", "keep_e", "keep_f"):
         assert np.array_equal(fl[k], ref["thin"][k]), k
     # every shape gives the same surviving set
-    for shape in ((512, 4), (256, 8), (1024, 1), (512, 2)):
+    for shape in ((512, 4, 1), (256, 8, 1), (1024, 1, 1), (512, 2, 2), (512, 2, 1)):
         ctx.debug_thin_shape(*shape)
         ctx.run_plain(occ, 0.04)
         fl2 = ctx.thin_flags()
         for k in ("keep_v", "keep_e", "keep_f"):
             assert np.array_equal(fl2[k], ref["thin"][k]), (shape, k)
-    ctx.debug_thin_shape(0, 0)
+    ctx.debug_thin_shape(0, 0, 0)
 
 
 def test_autotune_on_a_batch(gpu_ctx):
@@ -45,4 +46,4 @@ def test_autotune_on_a_batch(gpu_ctx):
         ref = O.run_plain(v, t=0.04)
         assert (r["rem"]["nv"], r["rem"]["ne"], r["rem"]["nt"]) == (
             len(ref["rem_vts"]), len(ref["rem_edges"]), len(ref["rem_tris"]))
-    ctx.debug_thin_shape(0, 0)
+    ctx.debug_thin_shape(0, 0, 0)

@@ -60,7 +60,7 @@ class ServerStats(ctypes.Structure):
 
 class TuneResult(ctypes.Structure):
     _fields_ = [("ft_ring", c_int), ("thin_threads", c_int), ("thin_blocks_per_sm", c_int),
-                ("ft_ms", c_float * 3), ("thin_ms", c_float * 4)]
+                ("ft_ms", c_float * 3), ("thin_items", c_int), ("thin_ms", c_float * 5)]
 
 
 # name -> (restype, argtypes)
@@ -110,7 +110,7 @@ SIGNATURES = {
     "vc_debug_thin_trace": (c_int, [c_vp, c_int, c_int]),
     "vc_debug_get_thin_trace": (c_int, [c_vp, c_vp, c_int, ctypes.POINTER(c_int)]),
     "vc_debug_ft_wide": (c_int, [c_vp, c_int]),
-    "vc_debug_thin_shape": (c_int, [c_vp, c_int, c_int]),
+    "vc_debug_thin_shape": (c_int, [c_vp, c_int, c_int, c_int]),
     "vc_autotune": (c_int, [c_vp, ctypes.c_double, ctypes.POINTER(TuneResult)]),
     "vc_run_plain": (c_int, [c_vp, c_vp, c_int, c_int, c_int, c_int, ctypes.c_double, ctypes.POINTER(PlainResult)]),
 }

@@ -121,12 +121,13 @@ class Context:
         r = L.TuneResult()
         self.check(self.lib.vc_autotune(self.h, ctypes.c_double(t), ctypes.byref(r)), "vc_autotune")
         return dict(ft_ring=r.ft_ring, thin_threads=r.thin_threads, thin_blocks_per_sm=r.thin_blocks_per_sm,
-                    ft_ms={k: round(float(v), 4) for k, v in zip((4, 8, 16), r.ft_ms)},
-                    thin_ms={k: round(float(v), 4) for k, v in zip(("512x2", "512x4", "256x8", "1024x1"), r.thin_ms)})
+                    thin_items=r.thin_items, ft_ms={k: round(float(v), 4) for k, v in zip((4, 8, 16), r.ft_ms)},
+                    thin_ms={k: round(float(v), 4)
+                             for k, v in zip(("512x2", "512x2x2", "512x4", "256x8", "1024x1"), r.thin_ms)})
 
-    def debug_thin_shape(self, threads: int = 0, blocks_per_sm: int = 0):
+    def debug_thin_shape(self, threads: int = 0, blocks_per_sm: int = 0, items: int = 0):
         """Launch shape of the thinning kernel (identical results)."""
-        self.check(self.lib.vc_debug_thin_shape(self.h, threads, blocks_per_sm), "vc_debug_thin_shape")
+        self.check(self.lib.vc_debug_thin_shape(self.h, threads, blocks_per_sm, items), "vc_debug_thin_shape")
 
     def debug_ft_wide(self, wide: bool = True):
         """Force 64-bit arithmetic in the feature transform (identical results)."""

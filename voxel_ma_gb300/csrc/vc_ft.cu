@@ -175,14 +175,14 @@ int launch_envelope_t(vc_ctx* c, const int64_t* in, int64_t* out, int32_t* d2o, 
 
 // int32 arithmetic when every lattice axis of the batch is below 2048; the
 // ring (stack entries kept in shared memory per line) is the context's
-// tuned size (4, 8 or 16; 8 by default)
+// tuned size (4, 8 or 16; 16 by default)
 template <int PASS>
 int launch_envelope(vc_ctx* c, bool small, const int64_t* in, int64_t* out, int32_t* d2o, int32_t* ido,
                     int32_t* gmeta, int64_t* gval, int64_t nlines) {
     if (!small) return launch_envelope_t<PASS, int64_t, 8>(c, in, out, d2o, ido, gmeta, gval, nlines);
     if (c->ft_ring == 4) return launch_envelope_t<PASS, int32_t, 4>(c, in, out, d2o, ido, gmeta, gval, nlines);
-    if (c->ft_ring == 16) return launch_envelope_t<PASS, int32_t, 16>(c, in, out, d2o, ido, gmeta, gval, nlines);
-    return launch_envelope_t<PASS, int32_t, 8>(c, in, out, d2o, ido, gmeta, gval, nlines);
+    if (c->ft_ring == 8) return launch_envelope_t<PASS, int32_t, 8>(c, in, out, d2o, ido, gmeta, gval, nlines);
+    return launch_envelope_t<PASS, int32_t, 16>(c, in, out, d2o, ido, gmeta, gval, nlines);
 }
 
 }  // namespace

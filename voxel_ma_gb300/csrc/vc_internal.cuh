@@ -124,6 +124,19 @@ struct VolTab {
         return off[s][b];
     }
     __device__ __forceinline__ int64_t total(int s) const { return start(s, nvol); }
+    // find() with a per-thread cache of the last volume and its range: a
+    // thread walking nearby indices searches only when it leaves the range
+    struct Cache {
+        int bv = -1;
+        int64_t lo = 0, hi = 0;
+    };
+    __device__ __forceinline__ int find_cached(int s, int64_t x, Cache& c) const {
+        if (x >= c.lo && x < c.hi) return c.bv;
+        c.bv = find(s, x);
+        c.lo = start(s, c.bv);
+        c.hi = start(s, c.bv + 1);
+        return c.bv;
+    }
     // the volume whose range of space s holds index x
     __device__ __forceinline__ int find(int s, int64_t x) const {
         if (nvol == 1) return 0;
@@ -232,8 +245,9 @@ struct vc_ctx {
     int trace_cap = 0, trace_gens = 0;
     int thin_blocks_per_sm = 0;  // 0 = library default
     int thin_threads = 0;        // threads per block of the thinning kernel (0 = library default)
+    int thin_items = 1;          // items per thread and piece in the thinning's phase A (1 or 2)
     bool ft_force_wide = false;  // feature transform: 64-bit arithmetic at every size
-    int ft_ring = 8;             // feature transform: envelope stack entries in shared memory per line
+    int ft_ring = 16;            // feature transform: envelope stack entries in shared memory per line
     std::mutex* thin_lock = nullptr;  // shared by contexts whose thinning kernels must not overlap
     // remaining complex
     bool rem_valid = false;

@@ -206,12 +206,12 @@ __device__ __forceinline__ void append_cell(int32_t* region, int* s_count, bool 
     if (want) region[basei + __popc(m & ((1u << lane) - 1u))] = code;
 }
 
-template <int THREADS, int MINB>
+template <int THREADS, int MINB, int ITEMS>
 __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArgs A) {
     __shared__ int64_t sm[33];
     __shared__ int64_t s_red[2];
     __shared__ int s_ncell, s_start, s_gbase;
-    __shared__ int32_t s_cells[4 * THREADS];
+    __shared__ int32_t s_cells[4 * THREADS * ITEMS];
     const int G = gridDim.x, b = blockIdx.x;
     const float f_t = A.thr[0], l_t = A.thr[1];
     int64_t n = A.ctl[0];
@@ -246,7 +246,7 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
         // that blocks finishing early take more (the per-item cost varies);
         // the next piece is claimed while the current one is processed
         if (threadIdx.x == 0) {
-            s_start = atomicAdd(ctr + 1, (int)blockDim.x);
+            s_start = atomicAdd(ctr + 1, (int)blockDim.x * ITEMS);
             s_ncell = 0;
         }
         for (;;) {
@@ -254,22 +254,45 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
             const int64_t r0 = s_start;
             if (r0 >= n) break;
             int next_start = 0;
-            if (threadIdx.x == 0) next_start = atomicAdd(ctr + 1, (int)blockDim.x);
-            const int64_t i = r0 + threadIdx.x;
-            int32_t one[4] = {-1, -1, -1, -1};  // cells whose count fell to 1 here
-            if (i < n) {
-                const int2 it = __ldcg(cur + i);
-                const int32_t p = (int32_t)(base + i);
-                if (is_fe(it)) {
-                    const int32_t f = idx0(it), e = it.y;
-                    // both records in one round trip each
-                    const int4 fa = __ldcg(reinterpret_cast<const int4*>(A.F + f));
-                    const int4 fb = __ldcg(reinterpret_cast<const int4*>(A.F + f) + 1);
-                    const int4 ea = __ldcg(reinterpret_cast<const int4*>(A.E + e));
-                    const int4 eb = __ldcg(reinterpret_cast<const int4*>(A.E + e) + 1);
-                    const int32_t frm = fb.x;  // FaceRec: e0 e1 e2 fm | rm ...
+            if (threadIdx.x == 0) next_start = atomicAdd(ctr + 1, (int)blockDim.x * ITEMS);
+            // each thread takes ITEMS items of the piece; their loads are issued
+            // together (items, then all their records) before any is used
+            int2 it[ITEMS];
+            bool has[ITEMS];
+#pragma unroll
+            for (int k = 0; k < ITEMS; ++k) {
+                const int64_t i = r0 + threadIdx.x + (int64_t)k * blockDim.x;
+                has[k] = i < n;
+                it[k] = has[k] ? __ldcg(cur + i) : make_int2(0, 0);
+            }
+            // FE item: face record (ra, rb) and edge record (ea, eb); EV item:
+            // vertex record (ra) and edge record (ea, eb)
+            int4 ra[ITEMS], rb[ITEMS], ea[ITEMS], eb[ITEMS];
+#pragma unroll
+            for (int k = 0; k < ITEMS; ++k) {
+                ra[k] = rb[k] = ea[k] = eb[k] = make_int4(0, 0, 0, 0);
+                if (!has[k]) continue;
+                const bool fe = is_fe(it[k]);
+                const int32_t e = fe ? it[k].y : it[k].x;
+                const int4* r1 = fe ? reinterpret_cast<const int4*>(A.F + idx0(it[k]))
+                                    : reinterpret_cast<const int4*>(A.V + it[k].y);
+                ra[k] = __ldcg(r1);
+                if (fe) rb[k] = __ldcg(r1 + 1);
+                ea[k] = __ldcg(reinterpret_cast<const int4*>(A.E + e));
+                eb[k] = __ldcg(reinterpret_cast<const int4*>(A.E + e) + 1);
+            }
+            int32_t one[4 * ITEMS];  // cells whose count fell to 1 here
+#pragma unroll
+            for (int q = 0; q < 4 * ITEMS; ++q) one[q] = -1;
+#pragma unroll
+            for (int k = 0; k < ITEMS; ++k) {
+                if (!has[k]) continue;
+                const int32_t p = (int32_t)(base + r0 + threadIdx.x + (int64_t)k * blockDim.x);
+                if (is_fe(it[k])) {
+                    const int32_t f = idx0(it[k]), e = it[k].y;
+                    const int32_t frm = rb[k].x;  // FaceRec: e0 e1 e2 fm | rm ...
                     const unsigned long long ers =
-                        ((unsigned long long)(uint32_t)ea.w << 32) | (uint32_t)ea.z;  // EdgeRec: v0 v1 rs | trig em rm
+                        ((unsigned long long)(uint32_t)ea[k].w << 32) | (uint32_t)ea[k].z;  // EdgeRec: v0 v1 rs | trig em rm
                     if (frm != p) {
                         ++my_skipped;
                     } else if (rs_count(ers) != 1) {
@@ -278,11 +301,11 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                         ++my_processed;
                         // the face's other two sides, in face order (the sides of a
                         // live face other than e are never removed)
-                        const int32_t s0 = fa.x, s1 = fa.y, s2 = fa.z;
+                        const int32_t s0 = ra[k].x, s1 = ra[k].y, s2 = ra[k].z;
                         const int32_t sa = s0 == e ? s1 : s0;
                         const int32_t sb = (s0 == e || s1 == e) ? s2 : s1;
-                        const int32_t v0 = ea.x, v1 = ea.y;
-                        const float ffm = __int_as_float(fa.w);
+                        const int32_t v0 = ea[k].x, v1 = ea[k].y;
+                        const float ffm = __int_as_float(ra[k].w);
                         atomicMin(&A.E[e].rm, p);
                         A.E[e].rs = 0;
                         atomicMax(&A.E[sa].trig, trig_make(p, 0));
@@ -294,15 +317,16 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                         const int ob = rs_count(atomicAdd(&A.E[sb].rs, df));
                         const int o0 = rs_count(atomicAdd(&A.V[v0].rs, de));
                         const int o1 = rs_count(atomicAdd(&A.V[v1].rs, de));
-                        if (oa == 2) one[0] = sa | kEdgeBit;
-                        if (ob == 2) one[1] = sb | kEdgeBit;
-                        if (o0 == 2) one[2] = v0;
-                        if (o1 == 2) one[3] = v1;
+                        if (oa == 2) one[4 * k + 0] = sa | kEdgeBit;
+                        if (ob == 2) one[4 * k + 1] = sb | kEdgeBit;
+                        if (o0 == 2) one[4 * k + 2] = v0;
+                        if (o1 == 2) one[4 * k + 3] = v1;
                     }
                 } else {
-                    const int32_t e = it.x, v = it.y;
-                    const int32_t erm = __ldcg(&A.E[e].rm);
-                    const int32_t vref = rs_count(__ldcg(&A.V[v].rs));
+                    const int32_t e = it[k].x, v = it[k].y;
+                    const int32_t erm = eb[k].w;  // EdgeRec ... | trig em rm
+                    const int32_t vref =
+                        rs_count(((unsigned long long)(uint32_t)ra[k].y << 32) | (uint32_t)ra[k].x);  // VertRec: rs | trig
                     if (erm != p) {
                         ++my_skipped;
                     } else if (vref != 1) {
@@ -310,16 +334,16 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                     } else {
                         ++my_processed;
                         A.V[v].rm = p;
-                        const int32_t v0 = A.E[e].v0, v1 = A.E[e].v1;
+                        const int32_t v0 = ea[k].x, v1 = ea[k].y;
                         const int32_t u = v0 != v ? v0 : v1;
                         A.V[v].rs = 0;
                         atomicMax(&A.V[u].trig, trig_make(p, 2));
-                        if (rs_count(atomicAdd(&A.V[u].rs, rs_drop(e, 0u))) == 2) one[2] = u;
+                        if (rs_count(atomicAdd(&A.V[u].rs, rs_drop(e, 0u))) == 2) one[4 * k + 2] = u;
                     }
                 }
             }
 #pragma unroll
-            for (int q = 0; q < 4; ++q) append_cell(s_cells, &s_ncell, one[q] != -1, one[q]);
+            for (int q = 0; q < 4 * ITEMS; ++q) append_cell(s_cells, &s_ncell, one[q] != -1, one[q]);
             __syncthreads();
             if (threadIdx.x == 0) s_gbase = s_ncell ? atomicAdd(ctr + 0, s_ncell) : 0;
             __syncthreads();
@@ -623,12 +647,16 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats) {
         VC_CUDA(c, cudaGetLastError());
     }
     // persistent cooperative launch: every block resident
-    // launch shapes: 256 x 8, 512 x 4 (32 registers), 512 x 2, 1024 x 1 per SM
+    // launch shapes (threads per block x blocks per SM, items per thread and
+    // piece): 512 x 2 (default), 512 x 2 with 2 items, 512 x 4, 256 x 8,
+    // 1024 x 1
     const int threads = c->thin_threads == 256 ? 256 : (c->thin_threads == 1024 ? 1024 : 512);
-    void* kern = threads == 256    ? (void*)thin_generations_kernel<256, 8>
-                 : threads == 1024 ? (void*)thin_generations_kernel<1024, 1>
-                 : (c->thin_blocks_per_sm >= 3) ? (void*)thin_generations_kernel<512, 4>
-                                                : (void*)thin_generations_kernel<512, 2>;
+    void* kern = threads == 256    ? (void*)thin_generations_kernel<256, 8, 1>
+                 : threads == 1024 ? (void*)thin_generations_kernel<1024, 1, 1>
+                 : (c->thin_blocks_per_sm >= 3)
+                     ? (void*)thin_generations_kernel<512, 4, 1>
+                     : (c->thin_items == 2 ? (void*)thin_generations_kernel<512, 2, 2>
+                                           : (void*)thin_generations_kernel<512, 2, 1>);
     int per_sm = 0;
     VC_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, 0));
     if (per_sm <= 0) return VC_ERR_CUDA;
@@ -696,11 +724,13 @@ int vc_debug_thin_trace(vc_ctx* c, int cap, int blocks_per_sm) {
     return VC_OK;
 }
 
-int vc_debug_thin_shape(vc_ctx* c, int threads, int blocks_per_sm) {
-    if (!c || (threads != 0 && threads != 256 && threads != 512 && threads != 1024) || blocks_per_sm < 0)
+int vc_debug_thin_shape(vc_ctx* c, int threads, int blocks_per_sm, int items) {
+    if (!c || (threads != 0 && threads != 256 && threads != 512 && threads != 1024) || blocks_per_sm < 0 ||
+        (items != 0 && items != 1 && items != 2))
         return VC_ERR_ARG;
     c->thin_threads = threads;
     c->thin_blocks_per_sm = blocks_per_sm;
+    c->thin_items = items == 2 ? 2 : 1;
     return VC_OK;
 }
 

@@ -67,12 +67,13 @@ extern "C" int vc_autotune(vc_ctx* c, double t, vc_tune_result* out) {
     VC_TRY(run_ft(c));
     // thinning: threads per block and blocks per SM; every trial thins a
     // fresh copy of the same records (the lattice complex is rebuilt)
-    const int shapes[4][2] = {{512, 2}, {512, 4}, {256, 8}, {1024, 1}};
+    const int shapes[5][3] = {{512, 2, 1}, {512, 2, 2}, {512, 4, 1}, {256, 8, 1}, {1024, 1, 1}};
     int best_shape = 0;
     best = 1e30f;
-    for (int k = 0; k < 4; ++k) {
+    for (int k = 0; k < 5; ++k) {
         c->thin_threads = shapes[k][0];
         c->thin_blocks_per_sm = shapes[k][1];
+        c->thin_items = shapes[k][2];
         float ms = 0.0f;
         for (int rep = 0; rep < 2; ++rep) {  // the first run is untimed
             VC_TRY(run_lattice_vd(c, nullptr, t));
@@ -86,8 +87,10 @@ extern "C" int vc_autotune(vc_ctx* c, double t, vc_tune_result* out) {
     }
     c->thin_threads = shapes[best_shape][0];
     c->thin_blocks_per_sm = shapes[best_shape][1];
+    c->thin_items = shapes[best_shape][2];
     out->ft_ring = c->ft_ring;
     out->thin_threads = c->thin_threads;
     out->thin_blocks_per_sm = c->thin_blocks_per_sm;
+    out->thin_items = c->thin_items;
     return sync_check(c);
 }

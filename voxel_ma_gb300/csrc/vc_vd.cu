@@ -218,107 +218,126 @@ __device__ __forceinline__ float rec_measure(float m, const float* thr, int bv) 
 // corner labels equal -- tagVert plus "corner of some Voronoi face"),
 // whether each axis edge is valid (both voxels inside, the shared square's
 // 4 labels not all equal) and whether each lattice edge carries a valid
-// face (labels differ and the 4 voxels around it inside); ballots make the
-// segment's planes.  Also the volumes' vertex
-// bounding boxes (VoroInfo::getInsidePartSize reads them), reduced per block.
-// One block per lattice row along z (volume bv, a, b); blockDim is a
-// multiple of 32 so each warp covers one segment.
-__global__ void __launch_bounds__(128, 6) vd_segments_kernel(const uint8_t* __restrict__ occ,
+// face (labels differ and the 4 voxels around it inside).  One warp per
+// 32-point segment of a lattice row, lane = point: the occupancy tests run
+// for the whole segment at once on the packed voxel words (bit t of a row's
+// word = voxel c0 + t; shifted copies give c0 + t - 1 and c0 + t + 1), the
+// label tests run per lane (the c + 1 labels come from the next lane) and
+// ballots turn them into bit planes.  Also the volumes' vertex bounding
+// boxes (VoroInfo::getInsidePartSize reads them).
+__global__ void __launch_bounds__(128) vd_segments_kernel(const uint32_t* __restrict__ obits,
                                                           const int32_t* __restrict__ lab, VolTab T,
                                                           SegPlanes* __restrict__ planes, int32_t* __restrict__ cv,
                                                           int32_t* __restrict__ ce, int32_t* __restrict__ cf,
                                                           int32_t* __restrict__ bbox_all) {
     const int lane = threadIdx.x & 31;
     int cur_bv = -1;
+    // warp-uniform bounding box of the current volume's vertices
     int mn0 = INT32_MAX, mn1 = INT32_MAX, mn2 = INT32_MAX, mx0 = INT32_MIN, mx1 = INT32_MIN, mx2 = INT32_MIN;
     auto flush = [&]() {
-        // warp-reduce, then one lane per warp updates the volume's box
-        const int r0 = __reduce_min_sync(0xffffffffu, mn0), r1 = __reduce_min_sync(0xffffffffu, mn1),
-                  r2 = __reduce_min_sync(0xffffffffu, mn2);
-        const int r3 = __reduce_max_sync(0xffffffffu, mx0), r4 = __reduce_max_sync(0xffffffffu, mx1),
-                  r5 = __reduce_max_sync(0xffffffffu, mx2);
-        if (lane == 0 && cur_bv >= 0 && r0 != INT32_MAX) {
+        if (lane == 0 && cur_bv >= 0 && mn0 != INT32_MAX) {
             int32_t* bb = bbox_all + 6 * cur_bv;
-            atomicMin(&bb[0], r0);
-            atomicMin(&bb[1], r1);
-            atomicMin(&bb[2], r2);
-            atomicMax(&bb[3], r3);
-            atomicMax(&bb[4], r4);
-            atomicMax(&bb[5], r5);
+            atomicMin(&bb[0], mn0);
+            atomicMin(&bb[1], mn1);
+            atomicMin(&bb[2], mn2);
+            atomicMax(&bb[3], mx0);
+            atomicMax(&bb[4], mx1);
+            atomicMax(&bb[5], mx2);
         }
         mn0 = mn1 = mn2 = INT32_MAX;
         mx0 = mx1 = mx2 = INT32_MIN;
     };
     const int64_t nseg = T.total(kLSeg);
+    VolTab::Cache vcache;
     SEG_LOOP(gs, nseg) {
-        const int bv = T.find(kLSeg, gs);
+        const int bv = T.find_cached(kLSeg, gs, vcache);
         if (bv != cur_bv) {
             flush();
             cur_bv = bv;
         }
-        const Grid g = grid_of(T, bv, occ, lab);
-        const int nsr_ = (T.dim(bv).z + 32) / 32;
-        const int64_t ls_ = gs - T.start(kLSeg, bv);
-        const int64_t row = ls_ / nsr_;
-        const int c0 = (int)(ls_ - row * nsr_) * 32;
-        const int a = (int)(row / g.NB), b = (int)(row - (int64_t)a * g.NB);
-        {
-            const int c = c0 + lane;
-            uint32_t f = 0;
-            if (c < (int)g.NC) {
+        const int4 dm = T.dim(bv);
+        const int X = dm.x, Y = dm.y, Z = dm.z;
+        const int64_t NB = Y + 1, NC = Z + 1;
+        const int nsr = (Z + 32) / 32;
+        const int64_t ls = gs - T.start(kLSeg, bv);
+        const int64_t row = ls / nsr;
+        const int c0 = (int)(ls - row * nsr) * 32;
+        const int a = (int)(row / NB), b = (int)(row - (int64_t)a * NB);
+        // occupancy words of the voxel rows around the segment
+        const int sw = c0 >> 5, Wz = (Z + 31) >> 5;
+        const uint32_t* ob = obits + T.start(kVWord, bv);
+        auto word = [&](int i, int j, int w) -> uint32_t {
+            return (i >= 0 && i < X && j >= 0 && j < Y && w >= 0 && w < Wz) ? __ldg(ob + ((int64_t)i * Y + j) * Wz + w)
+                                                                           : 0u;
+        };
+        // bit t: voxel (i, j, c0 + t - 1) / (i, j, c0 + t) / (i, j, c0 + t + 1) inside
+        struct Rw {
+            uint32_t m1, z0, p1;
+        };
+        auto rw = [&](int i, int j) {
+            const uint32_t prv = word(i, j, sw - 1), cur = word(i, j, sw), nxt = word(i, j, sw + 1);
+            return Rw{(cur << 1) | (prv >> 31), cur, (cur >> 1) | (nxt << 31)};
+        };
+        const Rw Rmm = rw(a - 1, b - 1), Rm0 = rw(a - 1, b), R0m = rw(a, b - 1), R00 = rw(a, b), Rp0 = rw(a + 1, b),
+                 R0p = rw(a, b + 1);
+        const uint32_t qx = R0m.m1 & R0m.z0 & R00.m1 & R00.z0;  // voxels (a, b-1..b, c-1..c)
+        const uint32_t qy = Rm0.m1 & Rm0.z0 & R00.m1 & R00.z0;  // voxels (a-1..a, b, c-1..c)
+        const uint32_t qz = Rmm.z0 & Rm0.z0 & R0m.z0 & R00.z0;  // voxels (a-1..a, b-1..b, c)
+        // labels of the voxel's 8 corners (a + qx, b + qy, c + qz), -1 outside the lattice
+        const int c = c0 + lane;
+        const bool valid = c < NC;
+        const int32_t* lb = lab + T.start(kLat, bv);
+        auto lat = [&](int i, int j, int k) -> int32_t {
+            return (i <= X && j <= Y && k <= Z) ? __ldg(lb + ((int64_t)i * NB + j) * NC + k) : -1;
+        };
+        int32_t L[8];
+        L[0] = valid ? lat(a, b, c) : -1;
+        L[2] = valid ? lat(a, b + 1, c) : -1;
+        L[4] = valid ? lat(a + 1, b, c) : -1;
+        L[6] = valid ? lat(a + 1, b + 1, c) : -1;
 #pragma unroll
-                for (int d = 0; d < 3; ++d)
-                    if (face_valid(g, a, b, c, d)) f |= 1u << d;
-                if (a < g.X && b < g.Y && c < g.Z && g.inside(a, b, c)) {
-                    int32_t L[8];
+        for (int q = 0; q < 8; q += 2) {
+            L[q + 1] = __shfl_down_sync(0xffffffffu, L[q], 1);
+            if (lane == 31) L[q + 1] = valid ? lat(a + (q >> 2), b + ((q >> 1) & 1), c + 1) : -1;
+        }
+        bool alleq = true;
 #pragma unroll
-                    for (int q = 0; q < 8; ++q) L[q] = g.label(a + ((q >> 2) & 1), b + ((q >> 1) & 1), c + (q & 1));
-                    bool alleq = true;
+        for (int q = 1; q < 8; ++q) alleq &= (L[q] == L[0]);
+        auto differ = [](int32_t x, int32_t y) { return x >= 0 && y >= 0 && x != y; };
+        auto square_differs = [&](int bitd) {
+            int32_t ref = -2;
+            bool eq = true;
 #pragma unroll
-                    for (int q = 1; q < 8; ++q) alleq &= (L[q] == L[0]);
-                    if (!alleq) {
-                        f |= 8u;
-                        mn0 = min(mn0, a);
-                        mn1 = min(mn1, b);
-                        mn2 = min(mn2, c);
-                        mx0 = max(mx0, a);
-                        mx1 = max(mx1, b);
-                        mx2 = max(mx2, c);
-#pragma unroll
-                        for (int d = 0; d < 3; ++d) {
-                            const int ni = a + (d == 0), nj = b + (d == 1), nk = c + (d == 2);
-                            if (!g.inside(ni, nj, nk)) continue;
-                            const int bitd = 1 << (2 - d);  // corner offset bit of axis d: x->4, y->2, z->1
-                            int32_t ref = -2;
-                            bool eq = true;
-#pragma unroll
-                            for (int q = 0; q < 8; ++q) {
-                                if (!(q & bitd)) continue;
-                                if (ref == -2) ref = L[q];
-                                else eq &= (L[q] == ref);
-                            }
-                            if (!eq) f |= 16u << d;
-                        }
-                    }
-                }
+            for (int q = 0; q < 8; ++q) {
+                if (!(q & bitd)) continue;
+                if (ref == -2) ref = L[q];
+                else eq &= (L[q] == ref);
             }
-            SegPlanes P;
-            P.v = __ballot_sync(0xffffffffu, f & 8u);
-            P.e0 = __ballot_sync(0xffffffffu, f & 16u);
-            P.e1 = __ballot_sync(0xffffffffu, f & 32u);
-            P.e2 = __ballot_sync(0xffffffffu, f & 64u);
-            P.f0 = __ballot_sync(0xffffffffu, f & 1u);
-            P.f1 = __ballot_sync(0xffffffffu, f & 2u);
-            P.f2 = __ballot_sync(0xffffffffu, f & 4u);
-            P.pad = 0;
-            if (lane == 0) {
-                const int64_t s = gs;
-                reinterpret_cast<uint4*>(planes + s)[0] = make_uint4(P.v, P.e0, P.e1, P.e2);
-                reinterpret_cast<uint4*>(planes + s)[1] = make_uint4(P.f0, P.f1, P.f2, 0u);
-                cv[s] = __popc(P.v);
-                ce[s] = __popc(P.e0) + __popc(P.e1) + __popc(P.e2);
-                cf[s] = __popc(P.f0) + __popc(P.f1) + __popc(P.f2);
-            }
+            return !eq;
+        };
+        SegPlanes P;
+        P.f0 = qx & __ballot_sync(0xffffffffu, valid && differ(L[0], L[4]));
+        P.f1 = qy & __ballot_sync(0xffffffffu, valid && differ(L[0], L[2]));
+        P.f2 = qz & __ballot_sync(0xffffffffu, valid && differ(L[0], L[1]));
+        P.v = R00.z0 & __ballot_sync(0xffffffffu, valid && !alleq);
+        P.e0 = P.v & Rp0.z0 & __ballot_sync(0xffffffffu, square_differs(4));
+        P.e1 = P.v & R0p.z0 & __ballot_sync(0xffffffffu, square_differs(2));
+        P.e2 = P.v & R00.p1 & __ballot_sync(0xffffffffu, square_differs(1));
+        P.pad = 0;
+        if (P.v) {
+            mn0 = min(mn0, a);
+            mn1 = min(mn1, b);
+            mn2 = min(mn2, c0 + __ffs(P.v) - 1);
+            mx0 = max(mx0, a);
+            mx1 = max(mx1, b);
+            mx2 = max(mx2, c0 + 31 - __clz(P.v));
+        }
+        if (lane == 0) {
+            reinterpret_cast<uint4*>(planes + gs)[0] = make_uint4(P.v, P.e0, P.e1, P.e2);
+            reinterpret_cast<uint4*>(planes + gs)[1] = make_uint4(P.f0, P.f1, P.f2, 0u);
+            cv[gs] = __popc(P.v);
+            ce[gs] = __popc(P.e0) + __popc(P.e1) + __popc(P.e2);
+            cf[gs] = __popc(P.f0) + __popc(P.f1) + __popc(P.f2);
         }
     }
     flush();
@@ -337,8 +356,9 @@ __global__ void __launch_bounds__(128) vd_vertices_kernel(VolTab T, Bases B, con
                                                           int32_t* __restrict__ g0, int64_t ne) {
     const int lane = threadIdx.x & 31;
     const int64_t nseg = T.total(kLSeg);
+    VolTab::Cache vcache;
     SEG_LOOP(gs, nseg) {
-        const int bv = T.find(kLSeg, gs);
+        const int bv = T.find_cached(kLSeg, gs, vcache);
         const Segs S = segs_of(T, bv, planes, vb, eb, fbs);
         const Shift sh = shift_of(B, bv);
         const int nsr_ = (T.dim(bv).z + 32) / 32;
@@ -459,8 +479,9 @@ __global__ void __launch_bounds__(128, 8) vd_edges_kernel(VolTab T, Bases B, con
                                                        int32_t* __restrict__ g0, const float* __restrict__ thr) {
     const int lane = threadIdx.x & 31;
     const int64_t nseg = T.total(kLSeg);
+    VolTab::Cache vcache;
     SEG_LOOP(gs, nseg) {
-        const int bv = T.find(kLSeg, gs);
+        const int bv = T.find_cached(kLSeg, gs, vcache);
         const Segs S = segs_of(T, bv, planes, vb, eb, fbs);
         const Shift sh = shift_of(B, bv);
         const int nsr_ = (T.dim(bv).z + 32) / 32;
@@ -524,8 +545,9 @@ __global__ void __launch_bounds__(128, 8) vd_faces_kernel(VolTab T, Bases B, con
                                                        int32_t* __restrict__ g0, const float* __restrict__ thr) {
     const int lane = threadIdx.x & 31;
     const int64_t nseg = T.total(kLSeg);
+    VolTab::Cache vcache;
     SEG_LOOP(gs, nseg) {
-        const int bv = T.find(kLSeg, gs);
+        const int bv = T.find_cached(kLSeg, gs, vcache);
         const Segs S = segs_of(T, bv, planes, vb, eb, fbs);
         const Shift sh = shift_of(B, bv);
         const int32_t* lb = lab + T.start(kLat, bv);
@@ -619,8 +641,9 @@ __global__ void __launch_bounds__(128) vd_aux_kernel(VolTab T, Bases B, const Se
                                                      int32_t* __restrict__ tri_edges) {
     const int lane = threadIdx.x & 31;
     const int64_t nseg = T.total(kLSeg);
+    VolTab::Cache vcache;
     SEG_LOOP(gs, nseg) {
-        const int bv = T.find(kLSeg, gs);
+        const int bv = T.find_cached(kLSeg, gs, vcache);
         const Segs S = segs_of(T, bv, planes, vb, eb, fbs);
         const Shift sh = shift_of(B, bv);
         const int64_t lat0 = T.start(kLat, bv);
@@ -819,8 +842,10 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes, double t_thr) {
     launched(c);
     {
         Region r(c, "vd_flags");
-        vd_segments_kernel<<<seg_grid(c, nseg), 128, 0, c->stream>>>(ptr<uint8_t>(c->occ), ptr<int32_t>(c->ft_id),
-                                                                       c->tab, planes, vb, eb, fb, c->bases.bbox);
+        // the packed occupancy words of the site extraction (same volumes)
+        vd_segments_kernel<<<seg_grid(c, nseg), 128, 0, c->stream>>>(ptr<uint32_t>(c->site_bits),
+                                                                       ptr<int32_t>(c->ft_id), c->tab, planes, vb, eb,
+                                                                       fb, c->bases.bbox);
         launched(c);
         VC_CUDA(c, cudaGetLastError());
     }
