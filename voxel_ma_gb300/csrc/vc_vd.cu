@@ -90,21 +90,6 @@ __device__ __forceinline__ float lambda_of(const float* __restrict__ sxyz, int32
     return __fsqrt_rn(s);
 }
 
-// Face validity of lattice edge (a,b,c)+d: labels differ and the 4 voxels are inside.
-__device__ __forceinline__ bool face_valid(const Grid& g, int a, int b, int c, int d) {
-    int e[3] = {a, b, c};
-    e[d] += 1;
-    if (e[0] > g.X || e[1] > g.Y || e[2] > g.Z) return false;
-    const int32_t l0 = g.label(a, b, c), l1 = g.label(e[0], e[1], e[2]);
-    if (l0 < 0 || l1 < 0 || l0 == l1) return false;
-#pragma unroll
-    for (int m = 0; m < 4; ++m) {
-        int i, j, k;
-        quad_voxel(a, b, c, d, m, i, j, k);
-        if (!g.inside(i, j, k)) return false;
-    }
-    return true;
-}
 
 // ---------------------------------------------------------------------------
 // Cell bit planes.  Each lattice row along z is cut into 32-point segments;
