@@ -383,6 +383,8 @@ def run_gpu(args):
         "lambda_note": "lambda = sqrt of an exact integer squared distance (< 2^24) in IEEE f32: no FP64 rescue needed",
         "tuned": tuned,
     }
+    # FP32 measures against FP64 on this workload's complex (outside the timed region)
+    line["fp64_check"] = ctx.lambda_fp64_check()
     if not args.no_batch:
         line["batched"] = run_batched(ctx, dev, args, stream)
         line["config"]["batched_workload"] = line["batched"]["workload"]
@@ -476,6 +478,7 @@ def run_batched(ctx, dev, args, stream):
     e2e()
     _, e_ms = timed(e2e, args.steps)
     s = ctx.rem_sizes
+    fp64 = ctx.lambda_fp64_check()  # the batch's complex, outside the timed regions
     b_mean, l_mean, e_mean = statistics.mean(b_ms), statistics.mean(l_ms), statistics.mean(e_ms)
     return {
         "workload": f"csg{BATCH_N}_loguniform_{BATCH_LO}_{BATCH_HI}",
@@ -492,6 +495,7 @@ def run_batched(ctx, dev, args, stream):
                 "d2h_bytes_per_step": s["nv"] * 12 + s["ne"] * 8 + s["nt"] * 12, "ms_per_step": e_mean},
         "parity": f"{same}/{BATCH_N} volumes: batched remaining-complex sizes equal the plain path's",
         "tuned": tuned,
+        "fp64_check": fp64,
         "thin_generations": ctx.batch_stats["generations"],
         "cells": {"V": ctx.vd_sizes["nv"], "E": ctx.vd_sizes["ne"], "T": ctx.vd_sizes["nt"]},
     }

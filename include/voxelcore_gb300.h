@@ -261,6 +261,16 @@ int vc_plan_batches(int n, const int64_t* voxels, const double* t, int64_t share
 int vc_extract_sites_noalloc(const uint8_t* occ, int X, int Y, int Z, float* xyz, int64_t capacity, int64_t* n_sites,
                              void* stream);
 
+/* FP64 cross-check of the lattice complex's face measures: every face's
+ * lambda is recomputed in double from its two sites.  *max_rel_err = the
+ * largest |lambda_float - lambda_double| / lambda_double; *flips = how many
+ * faces' threshold test (lambda < the volume's threshold) differs in double
+ * (-1 when the complex was built without thresholds, vc_lattice_vd).  The
+ * path keeps the reference's float semantics (trimesh::dist in float,
+ * measureforMA_imp.h:1-4); lambda is the correctly rounded square root of
+ * an exact integer, so no FP64 rescue is needed and this is a report.     */
+int vc_lambda_fp64_check(vc_ctx* ctx, double* max_rel_err, int64_t* flips);
+
 /* ---- autotuner -----------------------------------------------------------
  * Chooses, for the volume or batch installed in the context (vc_set_volume
  * or vc_batch_set_volumes), the launch shapes of the two kernels whose best

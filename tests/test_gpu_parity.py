@@ -252,3 +252,20 @@ def test_device_resident_inputs(gpu_ctx):
     fl = gpu_ctx.thin_flags(device=True)
     assert np.array_equal(fl["keep_f"].cpu().numpy(), ref["thin"]["keep_f"])
     assert r["rem"]["nt"] == len(ref["rem_tris"])
+
+
+def test_lambda_fp64_check(gpu_ctx):
+    """Face lambdas are correctly rounded square roots of exact integers, so
+    against an FP64 recomputation their relative error is at most 2^-24; the
+    threshold-flip count is reported (the path keeps float semantics)."""
+    occ = volumes.grf(40, sigma=3.0, seed=11)
+    gpu_ctx.run_plain(occ, 0.04)
+    chk = gpu_ctx.lambda_fp64_check()
+    assert 0.0 <= chk["max_rel_err"] <= 2.0 ** -24
+    assert chk["flips"] >= 0
+    gpu_ctx.set_volume(occ)
+    gpu_ctx.extract_sites()
+    gpu_ctx.feature_transform()
+    gpu_ctx.lattice_vd()  # no thresholds: flips not counted
+    assert gpu_ctx.lambda_fp64_check()["flips"] == -1
+

@@ -112,6 +112,7 @@ SIGNATURES = {
     "vc_debug_ft_wide": (c_int, [c_vp, c_int]),
     "vc_debug_thin_shape": (c_int, [c_vp, c_int, c_int, c_int]),
     "vc_autotune": (c_int, [c_vp, ctypes.c_double, ctypes.POINTER(TuneResult)]),
+    "vc_lambda_fp64_check": (c_int, [c_vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(c_i64)]),
     "vc_run_plain": (c_int, [c_vp, c_vp, c_int, c_int, c_int, c_int, ctypes.c_double, ctypes.POINTER(PlainResult)]),
 }
 

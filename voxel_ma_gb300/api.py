@@ -114,6 +114,14 @@ class Context:
     def debug_thin_trace(self, cap: int = 4096, blocks_per_sm: int = 0):
         self.check(self.lib.vc_debug_thin_trace(self.h, cap, blocks_per_sm), "vc_debug_thin_trace")
 
+    def lambda_fp64_check(self) -> dict:
+        """Face measures of the current lattice complex against an FP64
+        recomputation: the largest relative error and the threshold flips."""
+        e = ctypes.c_double()
+        n = ctypes.c_int64()
+        self.check(self.lib.vc_lambda_fp64_check(self.h, ctypes.byref(e), ctypes.byref(n)), "vc_lambda_fp64_check")
+        return dict(max_rel_err=e.value, flips=n.value)
+
     def autotune(self, t: float = 0.04) -> dict:
         """Time the input-dependent launch shapes on the installed volume or
         batch and keep the fastest (vc_autotune); returns the choice and the

@@ -9,6 +9,7 @@ int run_sites(vc_ctx* c, int64_t* n_sites);
 int run_ft(vc_ctx* c);
 int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes, double t_thr);
 int ensure_vd_aux(vc_ctx* c, bool meas, bool topo);
+int run_lambda_check(vc_ctx* c, double* max_rel_err, int64_t* flips);
 int run_vertex_radii(vc_ctx* c);
 int run_finalize(vc_ctx* c, int64_t* ne_final);
 int build_adjacency(vc_ctx* c);
@@ -103,6 +104,12 @@ int vc_get_vd(vc_ctx* c, float* vts, int32_t* edges, int32_t* tris, int32_t* tri
     VC_TRY(copy_out(c, fm, c->fm.p, (size_t)s.nt * sizeof(float), mem));
     VC_TRY(copy_out(c, face_sites, c->vd_face_sites.p, (size_t)s.nface * 2 * sizeof(int32_t), mem));
     return sync_check(c);
+}
+
+int vc_lambda_fp64_check(vc_ctx* c, double* max_rel_err, int64_t* flips) {
+    VC_TRY(enter(c));
+    if (!max_rel_err || !flips) return VC_ERR_ARG;
+    return run_lambda_check(c, max_rel_err, flips);
 }
 
 int vc_vertex_radii(vc_ctx* c, float* radius, int mem) {

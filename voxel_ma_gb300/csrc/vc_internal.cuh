@@ -209,6 +209,7 @@ struct vc_ctx {
     vc::DevBuf vd_tri_face, vd_face_sites, vd_lam;
     bool vd_aux_meas = false;  // vm, em, fm, tri_face, face_sites of the lattice complex written
     bool vd_aux_topo = false;  // tri_edges and the V->E / E->F lists of the lattice complex written
+    bool vd_thr_valid = false; // bases.thr holds the volumes' thinning thresholds of this complex
     vc::DevBuf vd_radius;             // float per vertex of the lattice complex
     std::vector<float> vol_inside;  // inside-part size per volume
     bool cc_batched = false;        // the complex is the lattice complex of a batch of > 1 volumes

@@ -38,6 +38,7 @@
 #include "vc_internal.cuh"
 
 #include <algorithm>
+#include <cstring>
 
 namespace vc {
 
@@ -735,6 +736,36 @@ __global__ void inside_size_kernel(Bases B, int nvol, double t) {
     }
 }
 
+// FP64 cross-check of the face measures (the north star's "FP32 with FP64
+// rescue" report): every face's lambda recomputed in double from its two
+// sites; out[0] = the largest relative difference to the float lambda the
+// path uses (as the bits of a non-negative double, so atomicMax orders
+// them), out[1] = how many faces' threshold test (lambda < the volume's
+// thinning threshold) comes out differently in double (thr null: not
+// counted).  The path keeps the reference's float semantics either way.
+__global__ void lambda_fp64_kernel(const int2* __restrict__ face_sites, const float* __restrict__ sxyz, Bases B,
+                                   int nvol, const float* __restrict__ lamf, const float* __restrict__ thr,
+                                   int64_t nface, unsigned long long* out) {
+    double worst = 0.0;
+    unsigned long long flips = 0;
+    for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < nface; f += (int64_t)gridDim.x * blockDim.x) {
+        const int bv = nvol > 1 ? find_base(B.b[kBFace], nvol, f) : 0;
+        const int64_t sb = B.b[kBSite][bv];
+        const int2 st = face_sites[f];
+        const int64_t s0 = sb + st.x, s1 = sb + st.y;
+        const double dx = (double)sxyz[3 * s0] - (double)sxyz[3 * s1];
+        const double dy = (double)sxyz[3 * s0 + 1] - (double)sxyz[3 * s1 + 1];
+        const double dz = (double)sxyz[3 * s0 + 2] - (double)sxyz[3 * s1 + 2];
+        const double l64 = sqrt(dx * dx + dy * dy + dz * dz);
+        const float l32 = lamf[f];
+        if (l64 > 0.0) worst = fmax(worst, fabs((double)l32 - l64) / l64);
+        if (thr && ((double)l32 < (double)thr[bv]) != (l64 < (double)thr[bv])) ++flips;
+    }
+    const unsigned long long wb = (unsigned long long)__double_as_longlong(worst);
+    atomicMax(out, wb);
+    if (flips) atomicAdd(out + 1, flips);
+}
+
 inline int cell_grid(vc_ctx* c, int64_t n) {
     return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)c->num_sms * 16));
 }
@@ -910,6 +941,7 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes, double t_thr) {
     c->meas_valid = true;  // written on demand (ensure_vd_aux)
     c->records_fresh = folded;
     c->records_thr_folded = folded;
+    c->vd_thr_valid = folded;
     c->cc_batched = nvol > 1;
     if (sizes) *sizes = c->vd;
     return VC_OK;
@@ -959,6 +991,30 @@ int ensure_vd_aux(vc_ctx* c, bool meas, bool topo) {
         VC_TRY(build_adjacency(c));
         c->vd_aux_topo = true;
     }
+    return VC_OK;
+}
+
+int run_lambda_check(vc_ctx* c, double* max_rel_err, int64_t* flips) {
+    if (!c->vd_valid) return VC_ERR_STATE;
+    VC_TRY(ensure_vd_aux(c, true, false));  // the faces' sites
+    VC_TRY(ensure_n<int64_t>(c, c->scratch2, 4));
+    unsigned long long* out = reinterpret_cast<unsigned long long*>(ptr<int64_t>(c->scratch2));
+    VC_CUDA(c, cudaMemsetAsync(out, 0, 2 * sizeof(unsigned long long), c->stream));
+    const int64_t nface = c->vd.nface;
+    if (nface > 0) {
+        lambda_fp64_kernel<<<cell_grid(c, nface), 256, 0, c->stream>>>(
+            ptr<int2>(c->vd_face_sites), ptr<float>(c->site_xyz), c->bases, c->nvol, ptr<float>(c->vd_lam),
+            c->vd_thr_valid ? c->bases.thr : nullptr, nface, out);
+        launched(c);
+        VC_CUDA(c, cudaGetLastError());
+    }
+    unsigned long long h[2] = {0, 0};
+    VC_CUDA(c, cudaMemcpyAsync(h, out, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    VC_TRY(sync_check(c));
+    double w;
+    std::memcpy(&w, &h[0], sizeof(w));
+    *max_rel_err = w;
+    *flips = c->vd_thr_valid ? (int64_t)h[1] : -1;
     return VC_OK;
 }
 
