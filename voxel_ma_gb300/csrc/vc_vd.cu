@@ -365,36 +365,56 @@ __global__ void __launch_bounds__(128) vd_vertices_kernel(VolTab T, Bases B, con
             unsigned k = 0;
             unsigned long long idsum = 0;
             const int p[3] = {a, b, c};
+            // each neighbour segment is read once (its edge or face planes)
+            auto add_edge = [&](int x, int y, int z, int d) {  // axis edge (x,y,z)+d, if valid
+                const int64_t sq = S.at(x, y, z);
+                const uint4 pe = __ldg(reinterpret_cast<const uint4*>(planes + sq));  // v e0 e1 e2
+                const uint32_t pd = d == 0 ? pe.y : (d == 1 ? pe.z : pe.w);
+                if (!bit(pd, z)) return;
+                const uint32_t mk = below(z);
+                int32_t r = __ldg(eb + sq) + __popc(pe.y & mk) + __popc(pe.z & mk) + __popc(pe.w & mk);
+                if (d >= 1) r += bit(pe.y, z);
+                if (d >= 2) r += bit(pe.z, z);
+                ++k;
+                idsum += (unsigned)(r + (int32_t)sh.fb);
+            };
+            auto add_diag = [&](int x, int y, int z, int d) {  // diagonal of face (x,y,z)+d, if valid
+                const int64_t sq = S.at(x, y, z);
+                const uint4 pf = __ldg(reinterpret_cast<const uint4*>(planes + sq) + 1);  // f0 f1 f2 -
+                const uint32_t pd = d == 0 ? pf.x : (d == 1 ? pf.y : pf.z);
+                if (!bit(pd, z)) return;
+                const uint32_t mk = below(z);
+                int32_t r = __ldg(fbs + sq) + __popc(pf.x & mk) + __popc(pf.y & mk) + __popc(pf.z & mk);
+                if (d >= 1) r += bit(pf.x, z);
+                if (d >= 2) r += bit(pf.y, z);
+                ++k;
+                idsum += (unsigned)((int32_t)sh.eb1 + r);
+            };
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
                 if (p[d] == 0) continue;
                 int q[3] = {a, b, c};
                 q[d] -= 1;
-                if (ebit_at(S, q[0], q[1], q[2], d)) {
-                    ++k;
-                    idsum += (unsigned)(erank_at(S, q[0], q[1], q[2], d) + (int32_t)sh.fb);
-                }
+                add_edge(q[0], q[1], q[2], d);
             }
+            {
+                const uint32_t mk = below(c);
+                int32_t r = __ldg(eb + s) + __popc(P.e0 & mk) + __popc(P.e1 & mk) + __popc(P.e2 & mk);
 #pragma unroll
-            for (int d = 0; d < 3; ++d)
-                if (bit(plane_e(P, d), c)) {
-                    ++k;
-                    idsum += (unsigned)(erank_at(S, a, b, c, d) + (int32_t)sh.fb);
-                }
+                for (int d = 0; d < 3; ++d)
+                    if (bit(plane_e(P, d), c)) {
+                        ++k;
+                        idsum += (unsigned)(r++ + (int32_t)sh.fb);
+                    }
+            }
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
                 const int u = (d + 1) % 3, w = (d + 2) % 3;
                 int p1[3] = {a, b, c}, p3[3] = {a, b, c};
                 p1[w] += 1;  // the vertex is q1 of face (p1, d)
                 p3[u] += 1;  // the vertex is q3 of face (p3, d)
-                if (fbit_at(S, p1[0], p1[1], p1[2], d)) {
-                    ++k;
-                    idsum += (unsigned)((int32_t)sh.eb1 + fid_at(S, p1[0], p1[1], p1[2], d));
-                }
-                if (fbit_at(S, p3[0], p3[1], p3[2], d)) {
-                    ++k;
-                    idsum += (unsigned)((int32_t)sh.eb1 + fid_at(S, p3[0], p3[1], p3[2], d));
-                }
+                add_diag(p1[0], p1[1], p1[2], d);
+                add_diag(p3[0], p3[1], p3[2], d);
             }
             VertRec r;
             r.rs = rs_make(k, 0, idsum);
@@ -557,13 +577,28 @@ __global__ void __launch_bounds__(128, 8) vd_faces_kernel(VolTab T, Bases B, con
             for (int d = 0; d < 3; ++d) {
                 if (!bit(plane_f(P, d), c)) continue;
                 const int u = (d + 1) % 3, w = (d + 2) % 3;
-                int qv[4][3];
-                int32_t q[4];
+                // the quad's voxels: vertex ids and (q0, q1, q3) their axis-edge
+                // ranks, one 16-byte plane load (v, e0, e1, e2) per voxel
+                int32_t q[4], er[4];
+                uint4 pl[4];
+                int qz[4];
 #pragma unroll
                 for (int mm = 0; mm < 4; ++mm) {
-                    quad_voxel(a, b, c, d, mm, qv[mm][0], qv[mm][1], qv[mm][2]);
-                    q[mm] = vid_at(S, qv[mm][0], qv[mm][1], qv[mm][2]);
+                    int x, y, z;
+                    quad_voxel(a, b, c, d, mm, x, y, z);
+                    const int64_t sm = S.at(x, y, z);
+                    pl[mm] = __ldg(reinterpret_cast<const uint4*>(S.planes + sm));
+                    qz[mm] = z;
+                    const uint32_t mk = below(z);
+                    q[mm] = __ldg(S.vb + sm) + __popc(pl[mm].x & mk);
+                    er[mm] = mm == 2 ? 0 : __ldg(S.eb + sm) + __popc(pl[mm].y & mk) + __popc(pl[mm].z & mk) +
+                                           __popc(pl[mm].w & mk);
                 }
+                // rank of voxel mm's axis edge along dd
+                auto erank = [&](int mm, int dd) {
+                    return er[mm] + (dd >= 1 ? (int)bit(pl[mm].y, qz[mm]) : 0) +
+                           (dd >= 2 ? (int)bit(pl[mm].z, qz[mm]) : 0);
+                };
                 const int32_t diag = (int32_t)sh.eb1 + f;
                 const int64_t t0 = 2 * (int64_t)f, t1 = t0 + 1;
                 tris[3 * t0 + 0] = q[3];
@@ -580,10 +615,10 @@ __global__ void __launch_bounds__(128, 8) vd_faces_kernel(VolTab T, Bases B, con
                 lamf[f] = lm;
                 if (F) {
                     // sides in traceFace order: (t0,t1), (t1,t2), (t2,t0)
-                    const int32_t e01 = erank_at(S, qv[0][0], qv[0][1], qv[0][2], u) + fbv;
-                    const int32_t e12 = erank_at(S, qv[1][0], qv[1][1], qv[1][2], w) + fbv;
-                    const int32_t e32 = erank_at(S, qv[3][0], qv[3][1], qv[3][2], u) + fbv;
-                    const int32_t e03 = erank_at(S, qv[0][0], qv[0][1], qv[0][2], w) + fbv;
+                    const int32_t e01 = erank(0, u) + fbv;
+                    const int32_t e12 = erank(1, w) + fbv;
+                    const int32_t e32 = erank(3, u) + fbv;
+                    const int32_t e03 = erank(0, w) + fbv;
                     const float lr = rec_measure(lm, thr, bv);
                     FaceRec fr;
                     fr.fm = lr;
