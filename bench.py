@@ -248,6 +248,22 @@ def algorithmic_bytes(region: str, shape, vd: dict, nsites: int) -> float:
     return 0.0
 
 
+def max_over_ranks(ms: float, dist=None, device=None) -> float:
+    """The slowest rank's time (every rank calls it; one process: unchanged)."""
+    if dist is None:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(world: int, voxels_per_rank: int, steps: int, max_ms: float) -> float:
+    """Whole-job voxels/s of `world` independent replicas (one volume per rank
+    per step, weak scaling) timed by the slowest rank."""
+    return world * voxels_per_rank * steps / (max_ms / 1e3)
+
+
 def run_gpu(args):
     import torch
 
@@ -303,12 +319,8 @@ def run_gpu(args):
     timings = ctx.timings()
     ctx.set_timing(False)
     step_ms = [evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)]
-    total_ms = evs[0].elapsed_time(evs[-1])
-    if dist is not None:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * nvox * args.steps / (total_ms / 1e3)
+    total_ms = max_over_ranks(evs[0].elapsed_time(evs[-1]), dist, dev)
+    value = replica_throughput(world, nvox, args.steps, total_ms)
 
     # ---- end to end through the C ABI with host buffers -------------------
     rem = r["rem"]
@@ -333,15 +345,11 @@ def run_gpu(args):
     e1.record(stream)
     torch.cuda.synchronize(dev)
     wall_e2e = time.perf_counter() - w0
-    e2e_ms = e0.elapsed_time(e1)
-    if dist is not None:
-        t = torch.tensor([e2e_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks(e0.elapsed_time(e1), dist, dev)
     clk = clocks.stop()
     s = rr["rem"]
     d2h = s["nv"] * 12 + s["ne"] * 8 + s["nt"] * 12
-    e2e_value = world * nvox * args.steps / (e2e_ms / 1e3)
+    e2e_value = replica_throughput(world, nvox, args.steps, e2e_ms)
 
     # ---- roofline of the dominant kernel -----------------------------------
     peak, peak_kind = measured_hbm_peak()
