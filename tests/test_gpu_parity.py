@@ -58,7 +58,9 @@ def test_sites_ft_vd_match_oracle(gpu_ctx, name, occ):
 
 FT_VOLS = [VOLS[0], VOLS[2], VOLS[3], VOLS[4],
            ("rod", (np.random.default_rng(3).uniform(size=(2, 300, 3)) < 0.3).astype(np.uint8)),
-           ("slab", (np.random.default_rng(4).uniform(size=(260, 2, 5)) < 0.05).astype(np.uint8))]
+           ("slab", (np.random.default_rng(4).uniform(size=(260, 2, 5)) < 0.05).astype(np.uint8)),
+           # more than 2048 points along z: the 64-bit path is the default there
+           ("long", (np.random.default_rng(6).uniform(size=(2, 3, 2100)) < 0.02).astype(np.uint8))]
 
 
 @pytest.mark.parametrize("name,occ", FT_VOLS, ids=[v[0] for v in FT_VOLS])
