@@ -41,7 +41,12 @@ T* ptr(const DevBuf& b) {
 }
 
 // Per-cell records of the thinning kernel: static data and thinning state of
-// one cell in one 32-byte DRAM sector (its accesses are random).
+// one cell in one DRAM sector (its accesses are random).  Random accesses
+// cost per request, not per byte, so each phase of the thinning finds what it
+// needs about a cell in one aligned 16-byte piece: a face record is one piece,
+// a vertex record is one piece, and an edge record's first piece is what an
+// item removing the edge reads and its second piece what a decrement and the
+// child step touch.
 constexpr int32_t kAlive = INT32_MAX;  // removal position of a cell still present
 // An edge's faces (a vertex's edges) still present, as one 64-bit word: their
 // count in bits 0-15, how many of them pass the thinning filter (measure
@@ -62,31 +67,36 @@ __host__ __device__ __forceinline__ unsigned long long rs_drop(int32_t id, unsig
 __host__ __device__ __forceinline__ int32_t rs_count(unsigned long long w) { return (int32_t)(w & kRefMask); }
 __host__ __device__ __forceinline__ int32_t rs_pass(unsigned long long w) { return (int32_t)((w >> 16) & kRefMask); }
 __host__ __device__ __forceinline__ int32_t rs_last(unsigned long long w) { return (int32_t)(uint32_t)(w >> 32); }
-// trig: the last decrement of a generation, as (queue position << 2 | slot),
-// slot = which of the decrementing item's cells this is (its child slot)
-__host__ __device__ __forceinline__ unsigned long long trig_make(int32_t pos, int slot) {
-    return ((unsigned long long)(uint32_t)pos << 2) | (unsigned)slot;
+// trig: the last decrement of a generation, as (queue position << 1 | bit),
+// bit = which of the decrementing item's cells of that kind this is: for an
+// edge, the first or second of the face's other sides (child slot 0 or 1);
+// for a vertex, the first or second end of the removed edge (child slot 2 or
+// 3).  Queue positions stay below 2^31, so the word fits 32 bits.
+__host__ __device__ __forceinline__ uint32_t trig_make(int32_t pos, int bit) {
+    return ((uint32_t)pos << 1) | (uint32_t)bit;
 }
-struct __align__(32) FaceRec {
-    int32_t e0, e1, e2;  // edge ids of the sides, in face order
-    float fm;
+constexpr int32_t kFacePass = (int32_t)0x80000000u;  // FaceRec::e2 bit: the face passes the filter
+struct __align__(16) FaceRec {
+    int32_t e0, e1;  // edge ids of the sides, in face order
+    int32_t e2;      // third side; bit 31 (kFacePass): measure below the face threshold
     int32_t rm;
-    int32_t pad0, pad1, pad2;
 };
 struct __align__(32) EdgeRec {
+    // first piece: ends, removal position, measure
     int32_t v0, v1;
-    unsigned long long rs;    // faces still present: count | pass | id sum
-    unsigned long long trig;  // last decrement: position << 2 | slot
+    int32_t rm;
     float em;
+    // second piece: faces still present (count | pass | id sum), last decrement
+    unsigned long long rs;
+    uint32_t trig;
+    int32_t pad;
+};
+struct __align__(16) VertRec {
+    unsigned long long rs;  // edges still present: count | 0 | id sum
+    uint32_t trig;          // last decrement: position << 1 | end bit
     int32_t rm;
 };
-struct __align__(32) VertRec {
-    unsigned long long rs;    // edges still present: count | 0 | id sum
-    unsigned long long trig;  // last decrement: position << 2 | slot
-    int32_t rm;
-    int32_t pad0, pad1, pad2;
-};
-static_assert(sizeof(FaceRec) == 32 && sizeof(EdgeRec) == 32 && sizeof(VertRec) == 32, "record size");
+static_assert(sizeof(FaceRec) == 16 && sizeof(EdgeRec) == 32 && sizeof(VertRec) == 16, "record size");
 
 // ---------------------------------------------------------------------------
 // Volume table.  Every stage runs over a batch of volumes stored one after
@@ -230,7 +240,7 @@ struct vc_ctx {
     // thinning state
     bool thin_valid = false;
     vc_thin_stats thin_stats{};
-    vc::DevBuf face_rec, edge_rec, vert_rec;  // 32-byte per-cell thinning records
+    vc::DevBuf face_rec, edge_rec, vert_rec;  // per-cell thinning records (16, 32, 16 bytes)
     // generation 0 of the thinning queue, written with the records: per edge
     // the face of its FE pair, then per vertex the edge of its EV pair, -1
     // where the cell starts no pair (ne + nv int32)

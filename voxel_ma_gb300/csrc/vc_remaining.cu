@@ -97,7 +97,7 @@ __global__ void euler_mark_kernel(const uint8_t* __restrict__ ke, const uint8_t*
             const int4 sides = __ldg(reinterpret_cast<const int4*>(F + f));
             mark[sides.x] = 1;
             mark[sides.y] = 1;
-            mark[sides.z] = 1;
+            mark[sides.z & ~kFacePass] = 1;
         }
     }
 }

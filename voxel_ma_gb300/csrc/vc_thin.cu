@@ -36,11 +36,15 @@
 // Removal state is the queue position of the removing item (INT32_MAX =
 // alive), so every check is position-exact.
 //
-// Memory layout: the accesses are random, so every cell's static data and
-// thinning state share one 32-byte record (one DRAM sector per touch):
-//   face   {e0, e1, e2, fm, rm}
-//   edge   {v0, v1, rs, trig, em, rm}
-//   vertex {rs, trig, rm}
+// Memory layout: the accesses are random and cost per request, so every
+// cell's static data and thinning state share one record, and each phase
+// reads what it needs about a cell with one 16-byte load:
+//   face   {e0, e1, e2 | pass bit, rm}                  16 B
+//   edge   {v0, v1, rm, em} {rs, trig, -}               32 B
+//   vertex {rs, trig, rm}                               16 B
+// Phase A reads a face record and an edge's first piece (FE) or a vertex
+// record and an edge's first piece (EV); the decrements and phase B touch an
+// edge's second piece or a vertex record.
 // rs packs the count of incident faces (edges) still present, how many of
 // them pass the filter, and the sum of their ids: one atomic removes an
 // incident cell, and when the count is 1 the sum names the remaining cell
@@ -105,10 +109,8 @@ __global__ void build_records_kernel(const int2* __restrict__ edges, const int32
             FaceRec r;
             r.e0 = tri_edges[3 * i];
             r.e1 = tri_edges[3 * i + 1];
-            r.e2 = tri_edges[3 * i + 2];
-            r.fm = fm[i];
+            r.e2 = tri_edges[3 * i + 2] | (fm[i] < f_t ? kFacePass : 0);
             r.rm = kAlive;
-            r.pad0 = r.pad1 = r.pad2 = 0;
             F[i] = r;
         } else if (i < (int64_t)nt + ne) {
             const int64_t e = i - nt;
@@ -128,6 +130,7 @@ __global__ void build_records_kernel(const int2* __restrict__ edges, const int32
             r.trig = 0;
             r.em = em[e];
             r.rm = kAlive;
+            r.pad = 0;
             E[e] = r;
             g0[e] = (o1 - o0 == 1 && pass == 1) ? (int32_t)idsum : -1;
         } else {
@@ -140,7 +143,6 @@ __global__ void build_records_kernel(const int2* __restrict__ edges, const int32
             r.rs = rs_make((unsigned)(o1 - o0), 0, idsum);
             r.trig = 0;
             r.rm = kAlive;
-            r.pad0 = r.pad1 = r.pad2 = 0;
             V[v] = r;
             g0[(int64_t)ne + v] = (o1 - o0 == 1 && em[idsum] < l_t) ? (int32_t)idsum : -1;
         }
@@ -213,7 +215,7 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
     __shared__ int s_ncell, s_start, s_gbase;
     __shared__ int32_t s_cells[4 * THREADS * ITEMS];
     const int G = gridDim.x, b = blockIdx.x;
-    const float f_t = A.thr[0], l_t = A.thr[1];
+    const float l_t = A.thr[1];
     int64_t n = A.ctl[0];
     int64_t base = 0, pushes = n;
     int gen = 0;
@@ -265,21 +267,18 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                 has[k] = i < n;
                 it[k] = has[k] ? __ldcg(cur + i) : make_int2(0, 0);
             }
-            // FE item: face record (ra, rb) and edge record (ea, eb); EV item:
-            // vertex record (ra) and edge record (ea, eb)
-            int4 ra[ITEMS], rb[ITEMS], ea[ITEMS], eb[ITEMS];
+            // FE item: face record (ra) and the edge's first piece (ea); EV
+            // item: vertex record (ra) and the edge's first piece (ea)
+            int4 ra[ITEMS], ea[ITEMS];
 #pragma unroll
             for (int k = 0; k < ITEMS; ++k) {
-                ra[k] = rb[k] = ea[k] = eb[k] = make_int4(0, 0, 0, 0);
+                ra[k] = ea[k] = make_int4(0, 0, 0, 0);
                 if (!has[k]) continue;
                 const bool fe = is_fe(it[k]);
                 const int32_t e = fe ? it[k].y : it[k].x;
-                const int4* r1 = fe ? reinterpret_cast<const int4*>(A.F + idx0(it[k]))
-                                    : reinterpret_cast<const int4*>(A.V + it[k].y);
-                ra[k] = __ldcg(r1);
-                if (fe) rb[k] = __ldcg(r1 + 1);
+                ra[k] = __ldcg(fe ? reinterpret_cast<const int4*>(A.F + idx0(it[k]))
+                                  : reinterpret_cast<const int4*>(A.V + it[k].y));
                 ea[k] = __ldcg(reinterpret_cast<const int4*>(A.E + e));
-                eb[k] = __ldcg(reinterpret_cast<const int4*>(A.E + e) + 1);
             }
             int32_t one[4 * ITEMS];  // cells whose count fell to 1 here
 #pragma unroll
@@ -289,34 +288,33 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                 if (!has[k]) continue;
                 const int32_t p = (int32_t)(base + r0 + threadIdx.x + (int64_t)k * blockDim.x);
                 if (is_fe(it[k])) {
+                    // the edge of an FE item has exactly one face, the item's:
+                    // its count fell to 1 once, and only removing that face
+                    // lowers it further
                     const int32_t f = idx0(it[k]), e = it[k].y;
-                    const int32_t frm = rb[k].x;  // FaceRec: e0 e1 e2 fm | rm ...
-                    const unsigned long long ers =
-                        ((unsigned long long)(uint32_t)ea[k].w << 32) | (uint32_t)ea[k].z;  // EdgeRec: v0 v1 rs | trig em rm
+                    const int32_t frm = ra[k].w;  // FaceRec: e0 e1 e2|pass rm
                     if (frm != p) {
                         ++my_skipped;
-                    } else if (rs_count(ers) != 1) {
-                        set_error(A.err, VC_ERR_INVARIANT);
                     } else {
                         ++my_processed;
                         // the face's other two sides, in face order (the sides of a
                         // live face other than e are never removed)
-                        const int32_t s0 = ra[k].x, s1 = ra[k].y, s2 = ra[k].z;
+                        const int32_t s0 = ra[k].x, s1 = ra[k].y, s2 = ra[k].z & ~kFacePass;
+                        const unsigned fpass = ra[k].z < 0 ? 1u : 0u;
                         const int32_t sa = s0 == e ? s1 : s0;
                         const int32_t sb = (s0 == e || s1 == e) ? s2 : s1;
-                        const int32_t v0 = ea[k].x, v1 = ea[k].y;
-                        const float ffm = __int_as_float(ra[k].w);
-                        atomicMin(&A.E[e].rm, p);
-                        A.E[e].rs = 0;
-                        atomicMax(&A.E[sa].trig, trig_make(p, 0));
-                        atomicMax(&A.E[sb].trig, trig_make(p, 1));
-                        atomicMax(&A.V[v0].trig, trig_make(p, 2));
-                        atomicMax(&A.V[v1].trig, trig_make(p, 3));
-                        const unsigned long long df = rs_drop(f, ffm < f_t ? 1u : 0u), de = rs_drop(e, 0u);
+                        const int32_t v0 = ea[k].x, v1 = ea[k].y;  // EdgeRec first piece: v0 v1 rm em
+                        // the edge is named by no other item of this generation
+                        A.E[e].rm = p;
+                        const unsigned long long df = rs_drop(f, fpass), de = rs_drop(e, 0u);
                         const int oa = rs_count(atomicAdd(&A.E[sa].rs, df));
                         const int ob = rs_count(atomicAdd(&A.E[sb].rs, df));
                         const int o0 = rs_count(atomicAdd(&A.V[v0].rs, de));
                         const int o1 = rs_count(atomicAdd(&A.V[v1].rs, de));
+                        atomicMax(&A.E[sa].trig, trig_make(p, 0));
+                        atomicMax(&A.E[sb].trig, trig_make(p, 1));
+                        atomicMax(&A.V[v0].trig, trig_make(p, 0));
+                        atomicMax(&A.V[v1].trig, trig_make(p, 1));
                         if (oa == 2) one[4 * k + 0] = sa | kEdgeBit;
                         if (ob == 2) one[4 * k + 1] = sb | kEdgeBit;
                         if (o0 == 2) one[4 * k + 2] = v0;
@@ -324,21 +322,21 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                     }
                 } else {
                     const int32_t e = it[k].x, v = it[k].y;
-                    const int32_t erm = eb[k].w;  // EdgeRec ... | trig em rm
+                    const int32_t erm = ea[k].z;  // EdgeRec first piece: v0 v1 rm em
                     const int32_t vref =
-                        rs_count(((unsigned long long)(uint32_t)ra[k].y << 32) | (uint32_t)ra[k].x);  // VertRec: rs | trig
+                        rs_count(((unsigned long long)(uint32_t)ra[k].y << 32) | (uint32_t)ra[k].x);  // VertRec: rs trig rm
                     if (erm != p) {
                         ++my_skipped;
                     } else if (vref != 1) {
                         set_error(A.err, VC_ERR_INVARIANT);
                     } else {
                         ++my_processed;
+                        // nothing else touches v in this generation (its one edge is e)
                         A.V[v].rm = p;
                         const int32_t v0 = ea[k].x, v1 = ea[k].y;
                         const int32_t u = v0 != v ? v0 : v1;
-                        A.V[v].rs = 0;
-                        atomicMax(&A.V[u].trig, trig_make(p, 2));
                         if (rs_count(atomicAdd(&A.V[u].rs, rs_drop(e, 0u))) == 2) one[4 * k + 2] = u;
+                        atomicMax(&A.V[u].trig, trig_make(p, 0));
                     }
                 }
             }
@@ -373,26 +371,26 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                 int2 ch = make_int2(-1, -1);
                 if (j < j1) {
                     const int32_t code = __ldcg(A.cells + j);
-                    unsigned long long tg = 0;
+                    uint32_t tg = 0;
                     if (code & kEdgeBit) {
                         const int32_t e2 = code & ~kEdgeBit;
-                        const int4 ea = __ldcg(reinterpret_cast<const int4*>(A.E + e2));
-                        const int4 eb = __ldcg(reinterpret_cast<const int4*>(A.E + e2) + 1);
-                        const unsigned long long rs = ((unsigned long long)(uint32_t)ea.w << 32) | (uint32_t)ea.z;
+                        const int4 eb = __ldcg(reinterpret_cast<const int4*>(A.E + e2) + 1);  // rs trig -
+                        const unsigned long long rs = ((unsigned long long)(uint32_t)eb.y << 32) | (uint32_t)eb.x;
                         want = rs_count(rs) == 1 && rs_pass(rs) == 1;
-                        tg = ((unsigned long long)(uint32_t)eb.y << 32) | (uint32_t)eb.x;
+                        tg = (uint32_t)eb.z;
+                        slot = (int)(tg & 1u);
                         ch = make_fe(rs_last(rs), e2);
                     } else {
                         const int32_t u = code;
-                        const int4 va = __ldcg(reinterpret_cast<const int4*>(A.V + u));  // rs | trig
+                        const int4 va = __ldcg(reinterpret_cast<const int4*>(A.V + u));  // rs trig rm
                         const unsigned long long rs = ((unsigned long long)(uint32_t)va.y << 32) | (uint32_t)va.x;
                         const int32_t e3 = rs_last(rs);
                         want = rs_count(rs) == 1 && A.E[e3].em < l_t;
-                        tg = ((unsigned long long)(uint32_t)va.w << 32) | (uint32_t)va.z;
+                        tg = (uint32_t)va.z;
+                        slot = 2 + (int)(tg & 1u);
                         ch = make_ev(e3, u);
                     }
-                    i = (int64_t)(tg >> 2) - base;
-                    slot = (int)(tg & 3u);
+                    i = (int64_t)(tg >> 1) - base;
                     if (want && (i < 0 || i >= n)) {
                         set_error(A.err, VC_ERR_INVARIANT);
                         want = false;
@@ -516,9 +514,9 @@ __global__ void export_flags_kernel(const FaceRec* __restrict__ F, const EdgeRec
         } else if (w < nwv + nwe) {
             const int64_t e = (w - nwv) * 32 + lane;
             if (e < ne) {
-                const int4 ea = __ldcs(reinterpret_cast<const int4*>(E + e));
-                const int4 eb = __ldcs(reinterpret_cast<const int4*>(E + e) + 1);
-                const int32_t rm = eb.w, ref = rs_count(((unsigned long long)(uint32_t)ea.w << 32) | (uint32_t)ea.z);
+                const int4 ea = __ldcs(reinterpret_cast<const int4*>(E + e));      // v0 v1 rm em
+                const int4 eb = __ldcs(reinterpret_cast<const int4*>(E + e) + 1);  // rs trig -
+                const int32_t rm = ea.z, ref = rs_count(((unsigned long long)(uint32_t)eb.y << 32) | (uint32_t)eb.x);
                 keep = rm == kAlive && ref == 0;
                 ke[e] = keep;
                 re[e] = rm != kAlive;

@@ -420,7 +420,6 @@ __global__ void __launch_bounds__(128) vd_vertices_kernel(VolTab T, Bases B, con
             r.rs = rs_make(k, 0, idsum);
             r.trig = 0;
             r.rm = kAlive;
-            r.pad0 = r.pad1 = r.pad2 = 0;
             V[v] = r;
             // generation 0: an EV pair when the one edge passes the filter
             // (its record, written before, holds the folded measure)
@@ -529,6 +528,7 @@ __global__ void __launch_bounds__(128, 8) vd_edges_kernel(VolTab T, Bases B, con
                     r.trig = 0;
                     r.em = rec_measure(mx, thr, bv);
                     r.rm = kAlive;
+                    r.pad = 0;
                     E[e] = r;
                     // generation 0: an FE pair when the one face passes the filter
                     g0[e] = (k == 1 && npass == 1) ? (int32_t)idsum : -1;
@@ -620,17 +620,17 @@ __global__ void __launch_bounds__(128, 8) vd_faces_kernel(VolTab T, Bases B, con
                     const int32_t e32 = erank(3, u) + fbv;
                     const int32_t e03 = erank(0, w) + fbv;
                     const float lr = rec_measure(lm, thr, bv);
+                    const int32_t pass = lr < 0.0f ? kFacePass : 0;
+                    // both triangles' records: one 32-byte sector
                     FaceRec fr;
-                    fr.fm = lr;
                     fr.rm = kAlive;
-                    fr.pad0 = fr.pad1 = fr.pad2 = 0;
                     fr.e0 = e03;
                     fr.e1 = e01;
-                    fr.e2 = diag;
+                    fr.e2 = diag | pass;
                     F[t0] = fr;
                     fr.e0 = diag;
                     fr.e1 = e12;
-                    fr.e2 = e32;
+                    fr.e2 = e32 | pass;
                     F[t1] = fr;
                     EdgeRec er;
                     er.v0 = dv0;
@@ -639,6 +639,7 @@ __global__ void __launch_bounds__(128, 8) vd_faces_kernel(VolTab T, Bases B, con
                     er.trig = 0;
                     er.em = lr;
                     er.rm = kAlive;
+                    er.pad = 0;
                     E[diag] = er;
                     g0[diag] = -1;  // two triangles: no FE pair
                 }
