@@ -224,7 +224,9 @@ KERNEL_REGIONS = ("thin_generations", "ft_rows", "ft_envelope_y", "ft_envelope_x
 
 
 def algorithmic_bytes(region: str, shape, vd: dict, nsites: int) -> float:
-    """Compulsory bytes one launch of `region` moves (definitions in the design doc)."""
+    """Compulsory bytes one launch of `region` moves: every input read once and
+    every output written once (for the thinning: each record, the measures and
+    the incidences of the complex once)."""
     X, Y, Z = shape
     N = (X + 1) * (Y + 1) * (Z + 1)
     nvox = X * Y * Z
@@ -365,7 +367,7 @@ def run_gpu(args):
                 "frac": ach / peak, "peak_kind": peak_kind, "algorithmic_bytes_per_launch": ab,
                 "traffic": (TRAFFIC_PER_CELL[dom] * (r["vd"]["nv"] + r["vd"]["ne"] + r["vd"]["nt"])
                             if dom in TRAFFIC_PER_CELL else None),
-                "traffic_source": ("ncu capture of the 192^3 case scaled by cells (profiles/kernels_grf192.md)"
+                "traffic_source": ("ncu capture of the 192^3 case of this workload, scaled by cells"
                                    if dom in TRAFFIC_PER_CELL else None)}
     stage_ms = {k: v[0] / max(v[1], 1) for k, v in sorted(timings.items())}
 
@@ -614,11 +616,11 @@ def run_serving(dev, args, workers=None, max_batch=None, with_plain=True):
 
 
 # DRAM traffic per cell of the complex (V + E + T) of the thinning kernel,
-# from one ncu capture of the 192^3 case of this workload
-# (profiles/kernels_grf192.md: 4.680 GB read + 2.143 GB written for
-# 3,385,169 + 14,026,594 + 10,679,482 cells); the traffic grows with the
-# complex, so the per-launch figure at 512^3 is this rate times its cells.
-TRAFFIC_PER_CELL = {"thin_generations": (4.679887e9 + 2.142997e9) / (3385169 + 14026594 + 10679482)}
+# from one ncu capture of the 192^3 case of this workload (4.066 GB read +
+# 1.978 GB written for 3,385,169 + 14,026,594 + 10,679,482 cells); the
+# traffic grows with the complex, so the per-launch figure at 512^3 is this
+# rate times its cells.
+TRAFFIC_PER_CELL = {"thin_generations": (4.065976e9 + 1.978346e9) / (3385169 + 14026594 + 10679482)}
 
 
 def main():
