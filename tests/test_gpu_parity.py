@@ -56,17 +56,29 @@ def test_sites_ft_vd_match_oracle(gpu_ctx, name, occ):
         assert np.array_equal(fin[k], L["fin"][k]), k
 
 
+def _sparse_volume():
+    occ = np.zeros((150, 140, 130), np.uint8)
+    occ[10:14, 12:15, 9:13] = 1
+    occ[120:125, 100:104, 90:95] = 1
+    return occ
+
+
 FT_VOLS = [VOLS[0], VOLS[2], VOLS[3], VOLS[4],
            ("rod", (np.random.default_rng(3).uniform(size=(2, 300, 3)) < 0.3).astype(np.uint8)),
            ("slab", (np.random.default_rng(4).uniform(size=(260, 2, 5)) < 0.05).astype(np.uint8)),
            # more than 2048 points along z: the 64-bit path is the default there
-           ("long", (np.random.default_rng(6).uniform(size=(2, 3, 2100)) < 0.02).astype(np.uint8))]
+           ("long", (np.random.default_rng(6).uniform(size=(2, 3, 2100)) < 0.02).astype(np.uint8)),
+           # two small blocks in a large box: most lines have points farther
+           # than the window kernel scans, and go to the envelope kernel
+           ("sparse", _sparse_volume())]
 
 
 @pytest.mark.parametrize("name,occ", FT_VOLS, ids=[v[0] for v in FT_VOLS])
 def test_ft_narrow_and_wide_arithmetic(gpu_ctx, name, occ):
-    """The envelope passes run in 32-bit arithmetic below 2048 points per
-    axis and in 64-bit above; both must give the oracle's exact transform."""
+    """Below 2048 points per axis the y and x passes run the window kernel
+    in 32-bit arithmetic, with the envelope kernel for the lines it leaves;
+    above (or forced) they run the envelope kernel in 64-bit.  Both must give
+    the oracle's exact transform."""
     ctx = gpu_ctx
     L = lattice_case(O, occ)
     try:

@@ -11,18 +11,30 @@
 //   pass 1 (along z, contiguous rows): nearest site in the row, one warp per
 //          row: the row's site ids are staged in shared memory, then a
 //          forward max-scan and a backward min-scan of site positions;
-//   pass 2 (along y) and pass 3 (along x): lower envelope of the parabolas
-//          (x - q)^2 + g(q), one thread per line, with integer crossing
-//          thresholds that include the index tie-break (the smallest x at
-//          which the later parabola wins is computed exactly), so the
-//          envelope is the lexicographic minimum at every integer x.
+//   pass 2 (along y) and pass 3 (along x): the minimum over q of the
+//          packed ((x - q)^2 + g(q), id(q)) at every point x of a line.
+//          Window kernel first: tiles of 32 consecutive lines are staged
+//          in shared memory 64 points at a time, and each point scans
+//          outward from itself until r^2 exceeds its best distance (a
+//          candidate r away is worth at least r^2, so none further can win
+//          or tie); a point whose scan would pass 64 marks its line, and
+//          the marked lines are redone by the envelope kernel: lower
+//          envelope of the parabolas (x - q)^2 + g(q), one thread per line,
+//          with integer crossing thresholds that include the index
+//          tie-break (the smallest x at which the later parabola wins is
+//          computed exactly), so the envelope is the lexicographic minimum
+//          at every integer x.  Both give that minimum exactly, so a line's
+//          result does not depend on which kernel wrote it.
 //
 // Memory behaviour: pass 1 stages each row in shared memory and writes it
-// with streaming stores.  In the envelope passes consecutive lanes own
-// consecutive lines, so the candidate loads of a step are one contiguous
-// warp access, issued a chunk ahead of their use; each point is written as
-// soon as it is final, so the live stack of a line stays a few entries deep
-// and sits in shared memory (vc_ft_line.cuh).
+// with streaming stores.  In the window kernel a warp's lanes are the tile's
+// 32 lines at one point, so every global load and store is one contiguous
+// warp access and the shared-memory scans are free of bank conflicts.  In
+// the envelope kernel consecutive lanes own consecutive lines, so the
+// candidate loads of a step are one contiguous warp access, issued a chunk
+// ahead of their use; each point is written as soon as it is final, so the
+// live stack of a line stays a few entries deep and sits in shared memory
+// (vc_ft_line.cuh).
 #include "vc_internal.cuh"
 #include "vc_ft_line.cuh"
 
@@ -103,6 +115,210 @@ __global__ void __launch_bounds__(256) ft_rows_kernel(const int32_t* __restrict_
     }
 }
 
+// Geometry of lattice line gl of pass PASS: its length, first point and stride.
+template <int PASS>
+__device__ __forceinline__ void line_geom(const VolTab& T, int64_t gl, int& L, int64_t& base, int64_t& stride) {
+    constexpr int kSpace = PASS == 2 ? kYLine : kXLine;
+    const int bv = T.find(kSpace, gl);
+    const int4 dm = T.dim(bv);
+    const int64_t NB = dm.y + 1, NC = dm.z + 1;
+    const int64_t l = gl - T.start(kSpace, bv);
+    L = PASS == 2 ? (int)NB : dm.x + 1;
+    stride = PASS == 2 ? NC : NB * NC;
+    base = T.start(kLat, bv) + (PASS == 2 ? (l / NC) * NB * NC + (l % NC) : l);
+}
+
+// Passes 2 and 3, window kernel (every axis below 2048).  A tile is
+// kWinLines consecutive lines (consecutive addresses within a volume); its
+// points are staged kWinChunk at a time in a ring of four chunks per line,
+// so that while chunk k is computed, chunks k - 1 and k + 1 (every candidate
+// within kWinChunk of it) are in shared memory.  Positions outside the line
+// hold kWinNone, a packed value above every distance that stays exact when a
+// squared offset is added, so the scans need no bounds checks.  Warp w
+// computes points w, w + 8, ... of chunk k, lane j for line j: every global
+// access of a warp is contiguous and every shared-memory access is free of
+// bank conflicts.  The first kWinNear offsets on both sides are evaluated for
+// every point; a point whose best is still (kWinNear + 1)^2 or more goes to its warp's
+// queue, and the queue is scanned further outward 32 points at a time (one
+// point per lane), so the long scans of a few points do not hold up the
+// other lanes.
+constexpr int kWinLines = 32;
+constexpr int kWinChunk = 64;
+constexpr int kWinRing = 4 * kWinChunk;   // power of two: ring index = position & (kWinRing - 1)
+constexpr int kWinPitch = kWinRing + 1;   // odd pitch: line j's column starts at bank 2j
+constexpr int kWinThreads = 256;
+constexpr int64_t kWinNone = ((int64_t)1 << 62) | 0xffffffffLL;  // distance 2^30, index -1
+constexpr int kWinWarps = kWinThreads / 32;
+constexpr int kWinQueue = 64;  // continuing points queued per warp
+constexpr int kWinNear = 6;    // offsets evaluated for every point
+constexpr size_t kWinSmem = (size_t)kWinLines * kWinPitch * sizeof(int64_t) +
+                            (size_t)kWinWarps * kWinQueue * (sizeof(int64_t) + sizeof(int32_t));
+
+template <int PASS>
+__global__ void __launch_bounds__(kWinThreads) ft_window_kernel(const int64_t* __restrict__ in,
+                                                                int64_t* __restrict__ out, int32_t* __restrict__ d2o,
+                                                                int32_t* __restrict__ ido, VolTab T,
+                                                                int32_t* __restrict__ hard, int* __restrict__ nhard) {
+    constexpr bool FINAL = PASS == 3;
+    constexpr int kSpace = PASS == 2 ? kYLine : kXLine;
+    constexpr int kRows = kWinThreads / kWinLines;  // points of a chunk per warp row
+    constexpr int kMask = kWinRing - 1;
+    extern __shared__ int64_t win_sm[];  // [kWinLines][kWinPitch], then the warps' queues
+    __shared__ int64_t s_base[kWinLines], s_stride[kWinLines];
+    __shared__ int s_len[kWinLines], s_hard[kWinLines], s_lmax;
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    int64_t* qbest = win_sm + kWinLines * kWinPitch + w * kWinQueue;                           // [kWinQueue]
+    int32_t* qpt = reinterpret_cast<int32_t*>(win_sm + kWinLines * kWinPitch + kWinWarps * kWinQueue) +
+                   w * kWinQueue;                                                              // q << 5 | line
+    const int64_t nlines = T.total(kSpace);
+    const int64_t ntiles = (nlines + kWinLines - 1) / kWinLines;
+    // the result of the point at lattice index o
+    auto emit_at = [&](int64_t o, int64_t best) {
+        const bool none = (best >> 32) >= ((int64_t)1 << 30);
+        if (FINAL) {
+            __stcs(d2o + o, none ? INT32_MAX : (int32_t)ft_g(best));
+            __stcs(ido + o, none ? -1 : ft_id(best));
+        } else {
+            __stcs(out + o, none ? kFtInf : best);
+        }
+    };
+    // continue a queued point from offset kWinNear + 1 on (one per lane, n lanes)
+    auto drain = [&](int n) {
+        if (lane < n) {
+            const int32_t m = qpt[lane];
+            const int j = m & 31, q = m >> 5;
+            const int64_t* svj = win_sm + j * kWinPitch;
+            const int qm = q & kMask;
+            int64_t best = qbest[lane];
+            bool far = false;
+            for (int r = kWinNear + 1;; ++r) {
+                const int64_t r2 = (int64_t)r * r;
+                if (r2 > (best >> 32)) break;  // a candidate r away is worth at least r^2
+                if (r > kWinChunk) {
+                    far = true;
+                    break;
+                }
+                const int64_t add = r2 << 32;
+                best = min(best, svj[(qm - r) & kMask] + add);
+                best = min(best, svj[(qm + r) & kMask] + add);
+            }
+            if (far) s_hard[j] = 1;
+            else emit_at(s_base[j] + (int64_t)q * s_stride[j], best);
+        }
+        __syncwarp();
+    };
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        if (t == 0) s_lmax = 0;
+        if (t < kWinLines) {
+            const int64_t gl = tile * kWinLines + t;
+            int L = 0;
+            int64_t base = 0, stride = 0;
+            if (gl < nlines) line_geom<PASS>(T, gl, L, base, stride);
+            s_len[t] = L;
+            s_base[t] = base;
+            s_stride[t] = stride;
+            s_hard[t] = 0;
+        }
+        __syncthreads();
+        if (t < kWinLines) atomicMax(&s_lmax, s_len[t]);
+        __syncthreads();
+        const int nch = (s_lmax + kWinChunk - 1) / kWinChunk;
+        // this lane's line
+        const int L = s_len[lane];
+        const int64_t base = s_base[lane], stride = s_stride[lane];
+        int64_t* sv = win_sm + lane * kWinPitch;
+        // chunk k is loaded into registers (fetch) while chunk k - 2 is
+        // computed, and stored into its ring slot (put) after that
+        const int64_t rstep = (int64_t)kRows * stride;  // lattice step between a warp's points
+        int64_t pre[kWinChunk / kRows];
+        auto fetch = [&](int k) {
+            const int p0 = k * kWinChunk + w;
+            const int64_t* src = in + base + (int64_t)p0 * stride;
+#pragma unroll
+            for (int i = 0; i < kWinChunk / kRows; ++i, src += rstep) {
+                const int p = p0 + i * kRows;
+                pre[i] = (p >= 0 && p < L) ? __ldcs(src) : kFtInf;
+            }
+        };
+        auto put = [&](int k) {
+#pragma unroll
+            for (int i = 0; i < kWinChunk / kRows; ++i) {
+                const int p = k * kWinChunk + w + i * kRows;
+                sv[p & kMask] = pre[i] == kFtInf ? kWinNone : pre[i];
+            }
+        };
+        fetch(-1);  // the positions before the line: nothing
+        put(-1);
+        fetch(0);
+        put(0);
+        fetch(1);
+        put(1);
+        for (int k = 0; k < nch; ++k) {
+            fetch(k + 2);  // in flight while chunk k is computed
+            __syncthreads();
+            int qn = 0;  // queued points of this warp (warp-uniform)
+            int64_t o = base + (int64_t)(k * kWinChunk + w) * stride;
+#pragma unroll 1
+            for (int i = 0; i < kWinChunk / kRows; ++i, o += rstep) {
+                const int q = k * kWinChunk + w + i * kRows;  // the same for the whole warp
+                const bool active = q < L;
+                const int qm = q & kMask;
+                int64_t best;
+                if (qm >= kWinNear && qm <= kMask - kWinNear) {  // no wrap around the ring
+                    const int64_t* c = sv + qm;
+                    best = c[0];
+#pragma unroll
+                    for (int r = 1; r <= kWinNear; ++r) {
+                        const int64_t add = (int64_t)(r * r) << 32;
+                        best = min(best, c[-r] + add);
+                        best = min(best, c[r] + add);
+                    }
+                } else {
+                    best = sv[qm];
+#pragma unroll
+                    for (int r = 1; r <= kWinNear; ++r) {
+                        const int64_t add = (int64_t)(r * r) << 32;
+                        best = min(best, sv[(qm - r) & kMask] + add);
+                        best = min(best, sv[(qm + r) & kMask] + add);
+                    }
+                }
+                const bool cont = active && (best >> 32) >= (kWinNear + 1) * (kWinNear + 1);
+                if (active && !cont) emit_at(o, best);
+                const unsigned mk = __ballot_sync(0xffffffffu, cont);
+                if (cont) {
+                    const int pos = qn + __popc(mk & ((1u << lane) - 1u));
+                    qbest[pos] = best;
+                    qpt[pos] = (q << 5) | lane;
+                }
+                qn += __popc(mk);
+                __syncwarp();
+                if (qn >= 32) {
+                    drain(32);
+                    // move the rest to the front
+                    int64_t b2 = 0;
+                    int32_t m2 = 0;
+                    if (lane < qn - 32) {
+                        b2 = qbest[32 + lane];
+                        m2 = qpt[32 + lane];
+                    }
+                    __syncwarp();
+                    if (lane < qn - 32) {
+                        qbest[lane] = b2;
+                        qpt[lane] = m2;
+                    }
+                    qn -= 32;
+                    __syncwarp();
+                }
+            }
+            drain(qn);
+            __syncthreads();
+            put(k + 2);  // the slot of chunk k - 2
+        }
+        // lines with a point beyond the window go to the envelope kernel
+        if (t < kWinLines && s_hard[t]) hard[atomicAdd(nhard, 1)] = (int32_t)(tile * kWinLines + t);
+    }
+}
+
 // Passes 2 and 3: lower envelope along the lattice lines of every volume:
 // PASS 2 along y (local line (a, c), L = Y+1 points, stride Z+1), PASS 3
 // along x (local line (b, c), L = X+1 points, stride (Y+1)(Z+1)), one
@@ -117,15 +333,19 @@ __global__ void __launch_bounds__(kEnvThreads) ft_envelope_kernel(const int64_t*
                                                                   int64_t* __restrict__ out, int32_t* __restrict__ d2o,
                                                                   int32_t* __restrict__ ido,
                                                                   int32_t* __restrict__ gmeta,
-                                                                  int64_t* __restrict__ gval, VolTab T) {
+                                                                  int64_t* __restrict__ gval, VolTab T,
+                                                                  const int32_t* __restrict__ list,
+                                                                  const int* __restrict__ list_len) {
     constexpr bool FINAL = PASS == 3;
     constexpr int kSpace = PASS == 2 ? kYLine : kXLine;
     extern __shared__ int64_t env_sm[];
     int64_t* s_val = env_sm;                                                    // [RING][kEnvThreads]
     int32_t* s_meta = reinterpret_cast<int32_t*>(env_sm + RING * kEnvThreads);  // [RING][kEnvThreads]
     const int t = threadIdx.x;
-    const int64_t nlines = T.total(kSpace);
-    for (int64_t gl = (int64_t)blockIdx.x * blockDim.x + t; gl < nlines; gl += (int64_t)gridDim.x * blockDim.x) {
+    // every line, or the lines of a list (those the window kernel left)
+    const int64_t nlines = list ? (int64_t)*list_len : T.total(kSpace);
+    for (int64_t li = (int64_t)blockIdx.x * blockDim.x + t; li < nlines; li += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t gl = list ? (int64_t)list[li] : li;
         const int bv = T.find(kSpace, gl);
         const int4 dm = T.dim(bv);
         const int64_t NB = dm.y + 1, NC = dm.z + 1;
@@ -158,7 +378,7 @@ constexpr size_t env_smem() {
 
 template <int PASS, class I, int RING>
 int launch_envelope_t(vc_ctx* c, const int64_t* in, int64_t* out, int32_t* d2o, int32_t* ido, int32_t* gmeta,
-                      int64_t* gval, int64_t nlines) {
+                      int64_t* gval, int64_t nlines, const int32_t* list, const int* list_len) {
     auto kern = ft_envelope_kernel<PASS, RING, I>;
     constexpr size_t smem = env_smem<RING>();
     VC_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -167,7 +387,7 @@ int launch_envelope_t(vc_ctx* c, const int64_t* in, int64_t* out, int32_t* d2o, 
     per_sm = std::max(per_sm, 1);
     const int blocks = (int)std::max<int64_t>(
         1, std::min<int64_t>((nlines + kEnvThreads - 1) / kEnvThreads, (int64_t)c->num_sms * per_sm));
-    kern<<<blocks, kEnvThreads, smem, c->stream>>>(in, out, d2o, ido, gmeta, gval, c->tab);
+    kern<<<blocks, kEnvThreads, smem, c->stream>>>(in, out, d2o, ido, gmeta, gval, c->tab, list, list_len);
     launched(c);
     VC_CUDA(c, cudaGetLastError());
     return VC_OK;
@@ -178,11 +398,37 @@ int launch_envelope_t(vc_ctx* c, const int64_t* in, int64_t* out, int32_t* d2o, 
 // tuned size (4, 8 or 16; 16 by default)
 template <int PASS>
 int launch_envelope(vc_ctx* c, bool small, const int64_t* in, int64_t* out, int32_t* d2o, int32_t* ido,
-                    int32_t* gmeta, int64_t* gval, int64_t nlines) {
-    if (!small) return launch_envelope_t<PASS, int64_t, 8>(c, in, out, d2o, ido, gmeta, gval, nlines);
-    if (c->ft_ring == 4) return launch_envelope_t<PASS, int32_t, 4>(c, in, out, d2o, ido, gmeta, gval, nlines);
-    if (c->ft_ring == 8) return launch_envelope_t<PASS, int32_t, 8>(c, in, out, d2o, ido, gmeta, gval, nlines);
-    return launch_envelope_t<PASS, int32_t, 16>(c, in, out, d2o, ido, gmeta, gval, nlines);
+                    int32_t* gmeta, int64_t* gval, int64_t nlines, const int32_t* list = nullptr,
+                    const int* list_len = nullptr) {
+    if (!small) return launch_envelope_t<PASS, int64_t, 8>(c, in, out, d2o, ido, gmeta, gval, nlines, list, list_len);
+    if (c->ft_ring == 4)
+        return launch_envelope_t<PASS, int32_t, 4>(c, in, out, d2o, ido, gmeta, gval, nlines, list, list_len);
+    if (c->ft_ring == 8)
+        return launch_envelope_t<PASS, int32_t, 8>(c, in, out, d2o, ido, gmeta, gval, nlines, list, list_len);
+    return launch_envelope_t<PASS, int32_t, 16>(c, in, out, d2o, ido, gmeta, gval, nlines, list, list_len);
+}
+
+// A pass with 32-bit arithmetic: the window kernel over every line, then the
+// envelope kernel over the lines it left (their count stays on the device;
+// the envelope launch walks the list up to it).
+template <int PASS>
+int launch_window(vc_ctx* c, const int64_t* in, int64_t* out, int32_t* d2o, int32_t* ido, int32_t* gmeta,
+                  int64_t* gval, int64_t nlines, int32_t* hard, int* nhard) {
+    auto kern = ft_window_kernel<PASS>;
+    VC_CUDA(c, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kWinSmem));
+    int per_sm = 0;
+    VC_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kWinThreads, kWinSmem));
+    per_sm = std::max(per_sm, 1);
+    const int64_t ntiles = (nlines + kWinLines - 1) / kWinLines;
+    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, (int64_t)c->num_sms * per_sm));
+    {
+        Region r(c, PASS == 2 ? "ft_window_y" : "ft_window_x");
+        kern<<<blocks, kWinThreads, kWinSmem, c->stream>>>(in, out, d2o, ido, c->tab, hard, nhard);
+        launched(c);
+        VC_CUDA(c, cudaGetLastError());
+    }
+    Region r(c, PASS == 2 ? "ft_far_y" : "ft_far_x");
+    return launch_envelope<PASS>(c, true, in, out, d2o, ido, gmeta, gval, nlines, hard, nhard);
 }
 
 }  // namespace
@@ -202,6 +448,14 @@ int run_ft(vc_ctx* c) {
     VC_TRY(ensure_n<int32_t>(c, c->ft_d2, N));
     VC_TRY(ensure_n<int32_t>(c, c->ft_id, N));
     VC_TRY(ensure_n<int64_t>(c, c->ft_tmp, 3 * N));
+    // far-line lists of the window kernel: [0], [1] counts of passes 2 and 3, then the list
+    const int64_t nlmax = std::max(c->h_off[kYLine][nvol], c->h_off[kXLine][nvol]);
+    if (small) {
+        VC_TRY(ensure_n<int32_t>(c, c->ft_far, nlmax + 2));
+        VC_CUDA(c, cudaMemsetAsync(c->ft_far.p, 0, 2 * sizeof(int32_t), c->stream));
+    }
+    int32_t* far_cnt = small ? ptr<int32_t>(c->ft_far) : nullptr;
+    int32_t* far_list = small ? far_cnt + 2 : nullptr;
     Region stage(c, "stage_ft");
     int64_t* A = ptr<int64_t>(c->ft_tmp);
     int64_t* B = A + N;
@@ -225,14 +479,23 @@ int run_ft(vc_ctx* c) {
         // pass 2 along y: stack spills go to C (values) and to the d2
         // output (positions), which pass 3 writes last
         Region r(c, "ft_envelope_y");
-        VC_TRY(launch_envelope<2>(c, small, A, B, nullptr, nullptr, ptr<int32_t>(c->ft_d2), C, c->h_off[kYLine][nvol]));
+        if (small)
+            VC_TRY(launch_window<2>(c, A, B, nullptr, nullptr, ptr<int32_t>(c->ft_d2), C, c->h_off[kYLine][nvol],
+                                    far_list, far_cnt + 0));
+        else
+            VC_TRY(launch_envelope<2>(c, small, A, B, nullptr, nullptr, ptr<int32_t>(c->ft_d2), C,
+                                      c->h_off[kYLine][nvol]));
     }
     {
         // pass 3 along x: spills go to the pass-1 buffer A (values) and to C
         // (positions), both dead by now
         Region r(c, "ft_envelope_x");
-        VC_TRY(launch_envelope<3>(c, small, B, nullptr, ptr<int32_t>(c->ft_d2), ptr<int32_t>(c->ft_id),
-                                  reinterpret_cast<int32_t*>(C), A, c->h_off[kXLine][nvol]));
+        if (small)
+            VC_TRY(launch_window<3>(c, B, nullptr, ptr<int32_t>(c->ft_d2), ptr<int32_t>(c->ft_id),
+                                    reinterpret_cast<int32_t*>(C), A, c->h_off[kXLine][nvol], far_list, far_cnt + 1));
+        else
+            VC_TRY(launch_envelope<3>(c, small, B, nullptr, ptr<int32_t>(c->ft_d2), ptr<int32_t>(c->ft_id),
+                                      reinterpret_cast<int32_t*>(C), A, c->h_off[kXLine][nvol]));
     }
     c->ft_valid = true;
     return VC_OK;
