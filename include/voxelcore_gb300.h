@@ -275,7 +275,8 @@ int vc_lambda_fp64_check(vc_ctx* ctx, double* max_rel_err, int64_t* flips);
  * Chooses, for the volume or batch installed in the context (vc_set_volume
  * or vc_batch_set_volumes), the launch shapes of the two kernels whose best
  * shape depends on the input: the feature transform's envelope passes (how
- * many stack entries of each line stay in shared memory: 4, 8 or 16) and
+ * many stack entries of each line stay in shared memory: 4, 8 or 16; then
+ * the envelope or the window method, see vc_set_ft_method) and
  * the thinning kernel (threads per block and blocks per SM: 512 x 2,
  * 512 x 2 with two items per thread, 512 x 4, 256 x 8, 1024 x 1).  Each candidate runs on the installed input
  * and is timed with CUDA events on the context's stream (after one untimed
@@ -284,14 +285,29 @@ int vc_lambda_fp64_check(vc_ctx* ctx, double* max_rel_err, int64_t* flips);
  * in vc_run_plain.  The reference has no counterpart (it is single-threaded
  * C++).                                                                    */
 typedef struct {
-    int ft_ring;                /* chosen */
+    int ft_ring;                /* chosen (envelope kernel) */
     int thin_threads;           /* chosen */
     int thin_blocks_per_sm;     /* chosen */
     float ft_ms[3];             /* both envelope passes, ring 4 / 8 / 16 */
     int thin_items;             /* chosen: items per thread in the thinning's first phase */
     float thin_ms[5];           /* thinning kernel, 512x2 / 512x2 with 2 items / 512x4 / 256x8 / 1024x1 */
+    int ft_method;              /* chosen: VC_FT_ENVELOPE or VC_FT_WINDOW */
+    float ft_window_ms;         /* both passes with the window kernel (envelope ring: the best of ft_ms) */
 } vc_tune_result;
 int vc_autotune(vc_ctx* ctx, double t, vc_tune_result* out);
+
+/* Method of the feature transform's y and x passes (results are identical):
+ * VC_FT_ENVELOPE (the default): lower envelope of the parabolas, one thread
+ *   per line; its cost per point does not depend on the distances.
+ * VC_FT_WINDOW: a window kernel first -- each point scans outward from
+ *   itself until no farther candidate can win or tie, over tiles of 32 lines
+ *   staged in shared memory -- which is faster on dense inputs (distances of
+ *   a few voxels, e.g. random fields); tiles whose scans run long are left to
+ *   the envelope kernel.  Only below 2048 points per axis (otherwise the
+ *   envelope runs).  vc_autotune picks the faster for the installed input. */
+#define VC_FT_ENVELOPE 0
+#define VC_FT_WINDOW 1
+int vc_set_ft_method(vc_ctx* ctx, int method);
 
 /* ---- diagnostics ---------------------------------------------------------
  * Per-generation trace of the thinning kernel: with cap > 0 the next vc_thin

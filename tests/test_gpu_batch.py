@@ -31,11 +31,16 @@ def plain_ctx(gpu_ctx):
     c.close()
 
 
-@pytest.mark.parametrize("t", [0.04, 0.2])
-def test_batch_equals_each_volume_alone(gpu_ctx, plain_ctx, t):
+@pytest.mark.parametrize("t,method", [(0.04, "envelope"), (0.2, "envelope"), (0.04, "window")])
+def test_batch_equals_each_volume_alone(gpu_ctx, plain_ctx, t, method):
+    """(The window method's tiles span several of these small volumes.)"""
     vols = _batch()
+    gpu_ctx.set_ft_method(method)
     gpu_ctx.batch_set_volumes(vols)
-    res = gpu_ctx.batch_run(t=t, euler=True)
+    try:
+        res = gpu_ctx.batch_run(t=t, euler=True)
+    finally:
+        gpu_ctx.set_ft_method("envelope")
     parts = gpu_ctx.batch_split(res)
     assert len(res) == len(vols)
     for i, (occ, r, part) in enumerate(zip(vols, res, parts)):

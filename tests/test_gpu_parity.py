@@ -75,22 +75,24 @@ FT_VOLS = [VOLS[0], VOLS[2], VOLS[3], VOLS[4],
 
 @pytest.mark.parametrize("name,occ", FT_VOLS, ids=[v[0] for v in FT_VOLS])
 def test_ft_narrow_and_wide_arithmetic(gpu_ctx, name, occ):
-    """Below 2048 points per axis the y and x passes run the window kernel
-    in 32-bit arithmetic, with the envelope kernel for the lines it leaves;
-    above (or forced) they run the envelope kernel in 64-bit.  Both must give
-    the oracle's exact transform."""
+    """Below 2048 points per axis the y and x passes run in 32-bit
+    arithmetic, by the envelope kernel or by the window kernel (with the
+    envelope kernel for the tiles it leaves); above (or forced) the envelope
+    kernel runs in 64-bit.  Every way must give the oracle's exact transform."""
     ctx = gpu_ctx
     L = lattice_case(O, occ)
     try:
-        for wide in (False, True):
+        for method, wide in (("envelope", False), ("window", False), ("envelope", True)):
+            ctx.set_ft_method(method)
             ctx.debug_ft_wide(wide)
             ctx.set_volume(occ)
             ctx.extract_sites()
             ctx.feature_transform()
             d2, ids = ctx.ft()
-            assert np.array_equal(d2, L["d2"]) and np.array_equal(ids, L["ids"]), f"wide={wide}"
+            assert np.array_equal(d2, L["d2"]) and np.array_equal(ids, L["ids"]), (method, wide)
     finally:
         ctx.debug_ft_wide(False)
+        ctx.set_ft_method("envelope")
 
 
 def test_empty_volume(gpu_ctx):

@@ -17,7 +17,8 @@ def test_autotune_keeps_results(gpu_ctx):
     ref = O.run_plain(occ, t=0.04)
     ctx.set_volume(occ)
     tuned = ctx.autotune(0.04)
-    assert tuned["ft_ring"] in (4, 8, 16)
+    assert tuned["ft_ring"] in (4, 8, 16) and tuned["ft_method"] in ("envelope", "window")
+    assert tuned["ft_window_ms"] > 0
     assert (tuned["thin_threads"], tuned["thin_blocks_per_sm"], tuned["thin_items"]) in (
         (512, 2, 1), (512, 2, 2), (512, 4, 1), (256, 8, 1), (1024, 1, 1))
     assert all(v > 0 for v in tuned["ft_ms"].values()) and all(v > 0 for v in tuned["thin_ms"].values())
@@ -34,6 +35,7 @@ def test_autotune_keeps_results(gpu_ctx):
         for k in ("keep_v", "keep_e", "keep_f"):
             assert np.array_equal(fl2[k], ref["thin"][k]), (shape, k)
     ctx.debug_thin_shape(0, 0, 0)
+    ctx.set_ft_method("envelope")
 
 
 def test_autotune_on_a_batch(gpu_ctx):
@@ -47,3 +49,4 @@ def test_autotune_on_a_batch(gpu_ctx):
         assert (r["rem"]["nv"], r["rem"]["ne"], r["rem"]["nt"]) == (
             len(ref["rem_vts"]), len(ref["rem_edges"]), len(ref["rem_tris"]))
     ctx.debug_thin_shape(0, 0, 0)
+    ctx.set_ft_method("envelope")

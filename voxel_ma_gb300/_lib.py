@@ -60,7 +60,8 @@ class ServerStats(ctypes.Structure):
 
 class TuneResult(ctypes.Structure):
     _fields_ = [("ft_ring", c_int), ("thin_threads", c_int), ("thin_blocks_per_sm", c_int),
-                ("ft_ms", c_float * 3), ("thin_items", c_int), ("thin_ms", c_float * 5)]
+                ("ft_ms", c_float * 3), ("thin_items", c_int), ("thin_ms", c_float * 5),
+                ("ft_method", c_int), ("ft_window_ms", c_float)]
 
 
 # name -> (restype, argtypes)
@@ -110,6 +111,7 @@ SIGNATURES = {
     "vc_debug_thin_trace": (c_int, [c_vp, c_int, c_int]),
     "vc_debug_get_thin_trace": (c_int, [c_vp, c_vp, c_int, ctypes.POINTER(c_int)]),
     "vc_debug_ft_wide": (c_int, [c_vp, c_int]),
+    "vc_set_ft_method": (c_int, [c_vp, c_int]),
     "vc_debug_thin_shape": (c_int, [c_vp, c_int, c_int, c_int]),
     "vc_autotune": (c_int, [c_vp, ctypes.c_double, ctypes.POINTER(TuneResult)]),
     "vc_lambda_fp64_check": (c_int, [c_vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(c_i64)]),

@@ -129,13 +129,21 @@ class Context:
         r = L.TuneResult()
         self.check(self.lib.vc_autotune(self.h, ctypes.c_double(t), ctypes.byref(r)), "vc_autotune")
         return dict(ft_ring=r.ft_ring, thin_threads=r.thin_threads, thin_blocks_per_sm=r.thin_blocks_per_sm,
-                    thin_items=r.thin_items, ft_ms={k: round(float(v), 4) for k, v in zip((4, 8, 16), r.ft_ms)},
+                    thin_items=r.thin_items, ft_method="window" if r.ft_method == 1 else "envelope",
+                    ft_ms={k: round(float(v), 4) for k, v in zip((4, 8, 16), r.ft_ms)},
+                    ft_window_ms=round(float(r.ft_window_ms), 4),
                     thin_ms={k: round(float(v), 4)
                              for k, v in zip(("512x2", "512x2x2", "512x4", "256x8", "1024x1"), r.thin_ms)})
 
     def debug_thin_shape(self, threads: int = 0, blocks_per_sm: int = 0, items: int = 0):
         """Launch shape of the thinning kernel (identical results)."""
         self.check(self.lib.vc_debug_thin_shape(self.h, threads, blocks_per_sm, items), "vc_debug_thin_shape")
+
+    def set_ft_method(self, method: str = "envelope"):
+        """Method of the feature transform's y and x passes: "envelope" or
+        "window" (vc_set_ft_method; identical results)."""
+        m = {"envelope": 0, "window": 1}[method]
+        self.check(self.lib.vc_set_ft_method(self.h, m), "vc_set_ft_method")
 
     def debug_ft_wide(self, wide: bool = True):
         """Force 64-bit arithmetic in the feature transform (identical results)."""

@@ -17,8 +17,8 @@
 //          in shared memory 64 points at a time, and each point scans
 //          outward from itself until r^2 exceeds its best distance (a
 //          candidate r away is worth at least r^2, so none further can win
-//          or tie); a point whose scan would pass 64 marks its line, and
-//          the marked lines are redone by the envelope kernel: lower
+//          or tie); a tile with a point whose scan would pass 64 is left
+//          to the envelope kernel: lower
 //          envelope of the parabolas (x - q)^2 + g(q), one thread per line,
 //          with integer crossing thresholds that include the index
 //          tie-break (the smallest x at which the later parabola wins is
@@ -141,7 +141,11 @@ __device__ __forceinline__ void line_geom(const VolTab& T, int64_t gl, int& L, i
 // every point; a point whose best is still (kWinNear + 1)^2 or more goes to its warp's
 // queue, and the queue is scanned further outward 32 points at a time (one
 // point per lane), so the long scans of a few points do not hold up the
-// other lanes.
+// other lanes.  A tile is left to the envelope kernel (all its lines, which
+// keeps that kernel's loads coalesced) as soon as one of its points needs an
+// offset beyond kWinFar.  The envelope kernel's cost per point is about
+// constant while a scan grows with the distance, so on sparse inputs (large
+// distances) the envelope method is the faster one; vc_autotune times both.
 constexpr int kWinLines = 32;
 constexpr int kWinChunk = 64;
 constexpr int kWinRing = 4 * kWinChunk;   // power of two: ring index = position & (kWinRing - 1)
@@ -151,6 +155,7 @@ constexpr int64_t kWinNone = ((int64_t)1 << 62) | 0xffffffffLL;  // distance 2^3
 constexpr int kWinWarps = kWinThreads / 32;
 constexpr int kWinQueue = 64;  // continuing points queued per warp
 constexpr int kWinNear = 6;    // offsets evaluated for every point
+constexpr int kWinFar = 64;    // largest offset scanned (the ring holds +-kWinChunk)
 constexpr size_t kWinSmem = (size_t)kWinLines * kWinPitch * sizeof(int64_t) +
                             (size_t)kWinWarps * kWinQueue * (sizeof(int64_t) + sizeof(int32_t));
 
@@ -158,14 +163,15 @@ template <int PASS>
 __global__ void __launch_bounds__(kWinThreads) ft_window_kernel(const int64_t* __restrict__ in,
                                                                 int64_t* __restrict__ out, int32_t* __restrict__ d2o,
                                                                 int32_t* __restrict__ ido, VolTab T,
-                                                                int32_t* __restrict__ hard, int* __restrict__ nhard) {
+                                                                int32_t* __restrict__ far_tiles,
+                                                                int* __restrict__ nfar) {
     constexpr bool FINAL = PASS == 3;
     constexpr int kSpace = PASS == 2 ? kYLine : kXLine;
     constexpr int kRows = kWinThreads / kWinLines;  // points of a chunk per warp row
     constexpr int kMask = kWinRing - 1;
     extern __shared__ int64_t win_sm[];  // [kWinLines][kWinPitch], then the warps' queues
     __shared__ int64_t s_base[kWinLines], s_stride[kWinLines];
-    __shared__ int s_len[kWinLines], s_hard[kWinLines], s_lmax;
+    __shared__ int s_len[kWinLines], s_lmax, s_far;
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
     int64_t* qbest = win_sm + kWinLines * kWinPitch + w * kWinQueue;                           // [kWinQueue]
     int32_t* qpt = reinterpret_cast<int32_t*>(win_sm + kWinLines * kWinPitch + kWinWarps * kWinQueue) +
@@ -194,7 +200,7 @@ __global__ void __launch_bounds__(kWinThreads) ft_window_kernel(const int64_t* _
             for (int r = kWinNear + 1;; ++r) {
                 const int64_t r2 = (int64_t)r * r;
                 if (r2 > (best >> 32)) break;  // a candidate r away is worth at least r^2
-                if (r > kWinChunk) {
+                if (r > kWinFar) {
                     far = true;
                     break;
                 }
@@ -202,13 +208,17 @@ __global__ void __launch_bounds__(kWinThreads) ft_window_kernel(const int64_t* _
                 best = min(best, svj[(qm - r) & kMask] + add);
                 best = min(best, svj[(qm + r) & kMask] + add);
             }
-            if (far) s_hard[j] = 1;
+            if (far) s_far = 1;
             else emit_at(s_base[j] + (int64_t)q * s_stride[j], best);
         }
         __syncwarp();
     };
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        if (t == 0) s_lmax = 0;
+        __syncthreads();  // every thread is done with the previous tile's flags
+        if (t == 0) {
+            s_lmax = 0;
+            s_far = 0;
+        }
         if (t < kWinLines) {
             const int64_t gl = tile * kWinLines + t;
             int L = 0;
@@ -217,7 +227,6 @@ __global__ void __launch_bounds__(kWinThreads) ft_window_kernel(const int64_t* _
             s_len[t] = L;
             s_base[t] = base;
             s_stride[t] = stride;
-            s_hard[t] = 0;
         }
         __syncthreads();
         if (t < kWinLines) atomicMax(&s_lmax, s_len[t]);
@@ -253,6 +262,7 @@ __global__ void __launch_bounds__(kWinThreads) ft_window_kernel(const int64_t* _
         put(0);
         fetch(1);
         put(1);
+        bool give_up = false;
         for (int k = 0; k < nch; ++k) {
             fetch(k + 2);  // in flight while chunk k is computed
             __syncthreads();
@@ -312,10 +322,13 @@ __global__ void __launch_bounds__(kWinThreads) ft_window_kernel(const int64_t* _
             }
             drain(qn);
             __syncthreads();
+            // the same decision in every thread (flags read after the barrier)
+            give_up = s_far != 0;
+            if (give_up) break;
             put(k + 2);  // the slot of chunk k - 2
         }
-        // lines with a point beyond the window go to the envelope kernel
-        if (t < kWinLines && s_hard[t]) hard[atomicAdd(nhard, 1)] = (int32_t)(tile * kWinLines + t);
+        // the envelope kernel does the whole tile
+        if (give_up && t == 0) far_tiles[atomicAdd(nfar, 1)] = (int32_t)tile;
     }
 }
 
@@ -342,10 +355,13 @@ __global__ void __launch_bounds__(kEnvThreads) ft_envelope_kernel(const int64_t*
     int64_t* s_val = env_sm;                                                    // [RING][kEnvThreads]
     int32_t* s_meta = reinterpret_cast<int32_t*>(env_sm + RING * kEnvThreads);  // [RING][kEnvThreads]
     const int t = threadIdx.x;
-    // every line, or the lines of a list (those the window kernel left)
-    const int64_t nlines = list ? (int64_t)*list_len : T.total(kSpace);
+    // every line, or the lines of the tiles of a list (those the window
+    // kernel left: kWinLines consecutive lines each)
+    const int64_t all = T.total(kSpace);
+    const int64_t nlines = list ? (int64_t)*list_len * kWinLines : all;
     for (int64_t li = (int64_t)blockIdx.x * blockDim.x + t; li < nlines; li += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t gl = list ? (int64_t)list[li] : li;
+        const int64_t gl = list ? (int64_t)list[li / kWinLines] * kWinLines + li % kWinLines : li;
+        if (gl >= all) continue;
         const int bv = T.find(kSpace, gl);
         const int4 dm = T.dim(bv);
         const int64_t NB = dm.y + 1, NC = dm.z + 1;
@@ -408,8 +424,8 @@ int launch_envelope(vc_ctx* c, bool small, const int64_t* in, int64_t* out, int3
     return launch_envelope_t<PASS, int32_t, 16>(c, in, out, d2o, ido, gmeta, gval, nlines, list, list_len);
 }
 
-// A pass with 32-bit arithmetic: the window kernel over every line, then the
-// envelope kernel over the lines it left (their count stays on the device;
+// A pass with 32-bit arithmetic: the window kernel over every tile, then the
+// envelope kernel over the tiles it left (their count stays on the device;
 // the envelope launch walks the list up to it).
 template <int PASS>
 int launch_window(vc_ctx* c, const int64_t* in, int64_t* out, int32_t* d2o, int32_t* ido, int32_t* gmeta,
@@ -444,18 +460,19 @@ int run_ft(vc_ctx* c) {
         nmax = std::max<int>(nmax, (int)std::max(NA, std::max(NB, NC)));
     }
     const bool small = nmax <= 2048 && !c->ft_force_wide;
+    const bool win = small && c->ft_window;
     const int64_t N = c->h_off[kLat][nvol];
     VC_TRY(ensure_n<int32_t>(c, c->ft_d2, N));
     VC_TRY(ensure_n<int32_t>(c, c->ft_id, N));
     VC_TRY(ensure_n<int64_t>(c, c->ft_tmp, 3 * N));
-    // far-line lists of the window kernel: [0], [1] counts of passes 2 and 3, then the list
+    // tiles the window kernel leaves: [0], [1] counts of passes 2 and 3, then the list
     const int64_t nlmax = std::max(c->h_off[kYLine][nvol], c->h_off[kXLine][nvol]);
-    if (small) {
-        VC_TRY(ensure_n<int32_t>(c, c->ft_far, nlmax + 2));
+    if (win) {
+        VC_TRY(ensure_n<int32_t>(c, c->ft_far, (nlmax + kWinLines - 1) / kWinLines + 2));
         VC_CUDA(c, cudaMemsetAsync(c->ft_far.p, 0, 2 * sizeof(int32_t), c->stream));
     }
-    int32_t* far_cnt = small ? ptr<int32_t>(c->ft_far) : nullptr;
-    int32_t* far_list = small ? far_cnt + 2 : nullptr;
+    int32_t* far_cnt = win ? ptr<int32_t>(c->ft_far) : nullptr;
+    int32_t* far_list = win ? far_cnt + 2 : nullptr;
     Region stage(c, "stage_ft");
     int64_t* A = ptr<int64_t>(c->ft_tmp);
     int64_t* B = A + N;
@@ -479,7 +496,7 @@ int run_ft(vc_ctx* c) {
         // pass 2 along y: stack spills go to C (values) and to the d2
         // output (positions), which pass 3 writes last
         Region r(c, "ft_envelope_y");
-        if (small)
+        if (win)
             VC_TRY(launch_window<2>(c, A, B, nullptr, nullptr, ptr<int32_t>(c->ft_d2), C, c->h_off[kYLine][nvol],
                                     far_list, far_cnt + 0));
         else
@@ -490,7 +507,7 @@ int run_ft(vc_ctx* c) {
         // pass 3 along x: spills go to the pass-1 buffer A (values) and to C
         // (positions), both dead by now
         Region r(c, "ft_envelope_x");
-        if (small)
+        if (win)
             VC_TRY(launch_window<3>(c, B, nullptr, ptr<int32_t>(c->ft_d2), ptr<int32_t>(c->ft_id),
                                     reinterpret_cast<int32_t*>(C), A, c->h_off[kXLine][nvol], far_list, far_cnt + 1));
         else
@@ -502,6 +519,12 @@ int run_ft(vc_ctx* c) {
 }
 
 }  // namespace vc
+
+extern "C" int vc_set_ft_method(vc_ctx* c, int method) {
+    if (!c || (method != VC_FT_ENVELOPE && method != VC_FT_WINDOW)) return VC_ERR_ARG;
+    c->ft_window = method == VC_FT_WINDOW;
+    return VC_OK;
+}
 
 extern "C" int vc_debug_ft_wide(vc_ctx* c, int wide) {
     if (!c) return VC_ERR_ARG;

@@ -259,7 +259,8 @@ struct vc_ctx {
     int thin_items = 1;          // items per thread and piece in the thinning's phase A (1 or 2)
     bool ft_force_wide = false;  // feature transform: 64-bit arithmetic at every size
     int ft_ring = 16;            // feature transform: envelope stack entries in shared memory per line
-    vc::DevBuf ft_far;           // feature transform: lines the window kernel left to the envelope kernel
+    vc::DevBuf ft_far;           // feature transform: tiles the window kernel left to the envelope kernel
+    bool ft_window = false;      // feature transform: window kernel first (VC_FT_WINDOW)
     std::mutex* thin_lock = nullptr;  // shared by contexts whose thinning kernels must not overlap
     // remaining complex
     bool rem_valid = false;
