@@ -299,6 +299,8 @@ def run_gpu(args):
     if not args.no_tune:
         ctx.set_volume(occ_dev)
         tuned = ctx.autotune(args.t)
+    elif args.ft_method:
+        ctx.set_ft_method(args.ft_method)
 
     # ---- device-resident value ------------------------------------------
     clocks = ClockSampler(local)
@@ -635,6 +637,8 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-path measurement")
     ap.add_argument("--no-serve", action="store_true", help="skip the request-stream measurement")
     ap.add_argument("--no-tune", action="store_true", help="keep the library's default launch shapes")
+    ap.add_argument("--ft-method", choices=["envelope", "window"], default=None,
+                    help="with --no-tune: the feature transform's method for the plain path")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
