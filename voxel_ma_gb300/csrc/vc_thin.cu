@@ -72,7 +72,7 @@ struct ThinArgs {
     int2* child;           // per item: up to 4 children, by slot ({-1, -1}: none)
     int32_t* cells;        // cells whose count reached 1 in this generation (kEdgeBit: edge)
     int* counters;         // [2][4] by generation parity: list length, phase-A work cursor
-    int64_t* blk_cnt;      // [2 * G] children per block, by generation parity
+    int64_t* blk_cnt;      // [2][G][warps per block] children per phase-C warp range, by generation parity
     unsigned* bar;
     int* err;
     int64_t* ctl;  // [0] gen-0 size; out: [1] pushes, [2] processed, [3] skipped, [4] generations
@@ -211,7 +211,7 @@ __device__ __forceinline__ void append_cell(int32_t* region, int* s_count, bool 
 template <int THREADS, int MINB, int ITEMS>
 __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArgs A) {
     __shared__ int64_t sm[33];
-    __shared__ int64_t s_red[2];
+    __shared__ int64_t s_red[2], s_wpre[32];
     __shared__ int s_ncell, s_start, s_gbase;
     __shared__ int32_t s_cells[4 * THREADS * ITEMS];
     const int G = gridDim.x, b = blockIdx.x;
@@ -226,8 +226,17 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
         const int par = gen & 1;
         const int2* cur = par ? A.qb : A.qa;
         int2* nxt = par ? A.qa : A.qb;
-        int64_t* blk = A.blk_cnt + (int64_t)par * G;
+        // phase C: block b writes the children of items [b chunk, (b + 1) chunk),
+        // its warp w those of a wchunk-item range of that; the children of each
+        // warp range are counted (blk) by the phase that places them
+        const int W = blockDim.x >> 5;
+        int64_t* blk = A.blk_cnt + (int64_t)par * G * W;
         const int64_t chunk = (n + G - 1) / G;
+        const int64_t wchunk = (chunk + W - 1) / W;
+        auto range_of = [&](int64_t i) {
+            const int64_t bi = i / chunk;
+            return bi * W + (i - bi * chunk) / wchunk;
+        };
         int* ctr = A.counters + 4 * par;  // [0] list length, [1] phase-A cursor
         const int64_t i0 = min(n, (int64_t)b * chunk), i1 = min(n, i0 + chunk);
         const bool tr = A.trace && b == 0 && threadIdx.x == 0 && gen < A.trace_cap;
@@ -397,8 +406,8 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                     }
                 }
                 if (want) __stcg(A.child + 4 * i + slot, ch);
-                // children per phase-C block, one atomic per warp and block
-                const int64_t bi = want ? i / chunk : -1;
+                // children per phase-C warp range, one atomic per warp and range
+                const int64_t bi = want ? range_of(i) : -1;
                 const unsigned grp = __match_any_sync(0xffffffffu, bi);
                 if (want && lane == __ffs(grp) - 1)
                     atomicAdd((unsigned long long*)(blk + bi), (unsigned long long)__popc(grp));
@@ -406,32 +415,42 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
         }
         grid_barrier(A.bar, A.err, A.spin_limit);
         if (*((volatile int*)A.err)) break;
-        // ---- phase C: block prefix, write generation g+1 and make its claims
+        // ---- phase C: prefixes, write generation g+1 and make its claims;
+        // each warp writes its range on its own (no block-wide step per item)
         if (tr) A.trace[4 * gen + 3] = global_ns();
         {
             int64_t before = 0, all = 0;
-            for (int k = threadIdx.x; k < G; k += blockDim.x) {
+            const int64_t nr = (int64_t)G * W, mine = (int64_t)b * W;
+            for (int64_t k = threadIdx.x; k < nr; k += blockDim.x) {
                 const int64_t v = __ldcg(blk + k);
                 all += v;
-                if (k < b) before += v;
+                if (k < mine) before += v;
             }
             int64_t t1, t2;
             block_exclusive_sum<int64_t>(before, sm, &t1);
             block_exclusive_sum<int64_t>(all, sm, &t2);
+            if (threadIdx.x < 32) {
+                // the earlier warp ranges of this block
+                const int64_t v = threadIdx.x < W ? __ldcg(blk + mine + threadIdx.x) : 0;
+                const int64_t inc = warp_inclusive_sum(v);
+                if (threadIdx.x < W) s_wpre[threadIdx.x] = inc - v;
+            }
             if (threadIdx.x == 0) {
                 s_red[0] = t1;
                 s_red[1] = t2;
             }
             __syncthreads();
         }
-        const int64_t prefix = s_red[0], total = s_red[1];
+        const int64_t total = s_red[1];
         const int64_t nbase = base + n;
-        int64_t running = prefix;
-        for (int64_t r0 = i0; r0 < i1; r0 += blockDim.x) {
-            const int64_t i = r0 + threadIdx.x;
+        const int wid = threadIdx.x >> 5;
+        int64_t running = s_red[0] + s_wpre[wid];
+        const int64_t w0 = min(i1, i0 + (int64_t)wid * wchunk), w1 = min(i1, w0 + wchunk);
+        for (int64_t r0 = w0; r0 < w1; r0 += 32) {
+            const int64_t i = r0 + lane;
             int2 cs[4] = {make_int2(-1, -1), make_int2(-1, -1), make_int2(-1, -1), make_int2(-1, -1)};
             unsigned msk = 0;
-            if (i < i1) {
+            if (i < w1) {
                 int4* sp = reinterpret_cast<int4*>(A.child + 4 * i);
                 const int4 s01 = __ldcg(sp), s23 = __ldcg(sp + 1);
                 cs[0] = make_int2(s01.x, s01.y);
@@ -444,8 +463,9 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                 if (msk & 3u) __stcg(sp, make_int4(-1, -1, -1, -1));
                 if (msk & 12u) __stcg(sp + 1, make_int4(-1, -1, -1, -1));
             }
-            int64_t tot;
-            const int64_t ex = block_exclusive_sum<int64_t>((int64_t)__popc(msk), sm, &tot);
+            const int cnt = __popc(msk);
+            const int inc = warp_inclusive_sum(cnt);
+            const int64_t ex = inc - cnt, tot = __shfl_sync(0xffffffffu, inc, 31);
             int k = 0;
 #pragma unroll
             for (int sl = 0; sl < 4; ++sl) {
@@ -461,8 +481,8 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
             running += tot;
         }
         // counters of the next generation start at zero
+        if (threadIdx.x < W) A.blk_cnt[(int64_t)(par ^ 1) * G * W + (int64_t)b * W + threadIdx.x] = 0;
         if (threadIdx.x == 0) {
-            A.blk_cnt[(int64_t)(par ^ 1) * G + b] = 0;
             if (b == 0) {
                 int* nc = A.counters + 4 * (par ^ 1);
                 nc[0] = nc[1] = nc[2] = 0;
@@ -659,10 +679,11 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats) {
     VC_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, 0));
     if (per_sm <= 0) return VC_ERR_CUDA;
     const int G = c->num_sms * std::min(per_sm, c->thin_blocks_per_sm > 0 ? c->thin_blocks_per_sm : 2048 / threads);
-    VC_TRY(ensure_n<int64_t>(c, c->blk_cnt, 2 * (int64_t)G + 8));
-    VC_CUDA(c, cudaMemsetAsync(c->blk_cnt.p, 0, (2 * (int64_t)G + 8) * sizeof(int64_t), c->stream));
+    const int64_t nrange = 2 * (int64_t)G * (threads / 32);  // phase-C warp ranges, both parities
+    VC_TRY(ensure_n<int64_t>(c, c->blk_cnt, nrange + 8));
+    VC_CUDA(c, cudaMemsetAsync(c->blk_cnt.p, 0, (nrange + 8) * sizeof(int64_t), c->stream));
     A.blk_cnt = ptr<int64_t>(c->blk_cnt);
-    A.counters = reinterpret_cast<int*>(A.blk_cnt + 2 * (int64_t)G);
+    A.counters = reinterpret_cast<int*>(A.blk_cnt + nrange);
     void* args[] = {&A};
     {
         // Contexts that share a thinning lock (the request loop's workers)
