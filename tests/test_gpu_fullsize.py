@@ -7,7 +7,7 @@ on the smaller cases of the other tests):
   * simple-pair collapses preserve homotopy type, so the remaining complex has
     the Euler characteristic of the full complex;
   * two runs give identical results; the float measures are within 2^-24 of
-    FP64."""
+    FP64; both feature-transform methods give the same transform."""
 import hashlib
 
 import numpy as np
@@ -70,3 +70,21 @@ def test_full_size_properties(gpu_ctx, grf512):
         assert np.array_equal(fl[k], fl2[k]), k
     chk = ctx.lambda_fp64_check()
     assert chk["max_rel_err"] <= 2.0 ** -24 and chk["flips"] >= 0
+
+
+def test_full_size_ft_methods_agree(gpu_ctx, grf512):
+    """The window and envelope methods give the same transform at 512^3 (the
+    window method is the one the autotuner keeps for this workload), and so
+    the same remaining complex."""
+    ctx = gpu_ctx
+    occ = grf512
+    try:
+        out = {}
+        for method in ("envelope", "window"):
+            ctx.set_ft_method(method)
+            r = ctx.run_plain(occ, 0.04)
+            d2, ids = ctx.ft()
+            out[method] = (_digest(d2, ids), r["rem"], _digest(*ctx.remaining_arrays()))
+        assert out["envelope"] == out["window"]
+    finally:
+        ctx.set_ft_method("envelope")
