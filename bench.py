@@ -371,6 +371,19 @@ def run_gpu(args):
                             if dom in TRAFFIC_PER_CELL else None),
                 "traffic_source": ("ncu capture of the 192^3 case of this workload, scaled by cells"
                                    if dom in TRAFFIC_PER_CELL else None)}
+        if dom in L2_REQUESTS_PER_CELL and not args.no_probe:
+            # the thinning touches random records: its L2 request rate beside
+            # the rates this GPU serves random 32-byte record touches at
+            cells = r["vd"]["nv"] + r["vd"]["ne"] + r["vd"]["nt"]
+            req_s = L2_REQUESTS_PER_CELL[dom] * cells / per_launch_s
+            probe = {}
+            for op, name in ((0, "load_8B"), (1, "two_loads_16B"), (2, "atomic_add"), (3, "atomic_max_and_add")):
+                probe[name] = ctx.debug_random_rate(op, PROBE_BYTES)
+            roof["random_access"] = {
+                "l2_requests_per_s": req_s,
+                "l2_requests_source": "ncu capture of the 192^3 case (requests per cell) x cells / kernel time",
+                "probe_record_touches_per_s": probe, "probe_array_bytes": PROBE_BYTES,
+                "note": "probe: random 32-byte records in a 16 GB array (vc_debug_random_rate), best of 3"}
     stage_ms = {k: v[0] / max(v[1], 1) for k, v in sorted(timings.items())}
 
     line = {
@@ -623,6 +636,10 @@ def run_serving(dev, args, workers=None, max_batch=None, with_plain=True):
 # traffic grows with the complex, so the per-launch figure at 512^3 is this
 # rate times its cells.
 TRAFFIC_PER_CELL = {"thin_generations": (4.065976e9 + 1.978346e9) / (3385169 + 14026594 + 10679482)}
+# L2 requests (atomics + reads + writes from the SMs) per cell of the same
+# capture: 78.4 M + 43.4 M + 25.7 M for the same cells.
+L2_REQUESTS_PER_CELL = {"thin_generations": (78366741 + 43409625 + 25718621) / (3385169 + 14026594 + 10679482)}
+PROBE_BYTES = 16 << 30
 
 
 def main():
@@ -637,6 +654,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-path measurement")
     ap.add_argument("--no-serve", action="store_true", help="skip the request-stream measurement")
     ap.add_argument("--no-tune", action="store_true", help="keep the library's default launch shapes")
+    ap.add_argument("--no-probe", action="store_true", help="skip the random-access probe")
     ap.add_argument("--ft-method", choices=["envelope", "window"], default=None,
                     help="with --no-tune: the feature transform's method for the plain path")
     args = ap.parse_args()

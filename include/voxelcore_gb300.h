@@ -321,6 +321,13 @@ int vc_debug_get_thin_trace(vc_ctx* ctx, int64_t* out, int cap, int* ngen);
  * thread in its first phase (1 or 2, 512 x 2 only; 0 = 1).  Results do not
  * depend on it.                                                            */
 int vc_debug_thin_shape(vc_ctx* ctx, int threads, int blocks_per_sm, int items);
+/* Rate at which this GPU serves random touches of 32-byte records in an
+ * array of `bytes` (allocated for the call; rounded down to a power-of-two
+ * number of records), the access pattern of the thinning kernel's records:
+ * op 0 one 8-byte load per record, 1 two 16-byte loads, 2 one 64-bit
+ * atomicAdd whose result is used, 3 an atomicMax and an atomicAdd.  Touches
+ * per second, best of three launches of 201 M touches.                     */
+int vc_debug_random_rate(vc_ctx* ctx, int op, int64_t bytes, double* touches_per_s);
 /* With wide != 0 the feature transform's envelope passes use 64-bit
  * arithmetic even when every lattice axis is below 2048 (where 32-bit
  * arithmetic is exact and is the default); results are identical.         */

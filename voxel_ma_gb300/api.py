@@ -145,6 +145,14 @@ class Context:
         m = {"envelope": 0, "window": 1}[method]
         self.check(self.lib.vc_set_ft_method(self.h, m), "vc_set_ft_method")
 
+    def debug_random_rate(self, op: int, nbytes: int) -> float:
+        """Random 32-byte record touches per second in an nbytes array
+        (vc_debug_random_rate; op 0 load, 1 two 16-byte loads, 2 atomicAdd,
+        3 atomicMax + atomicAdd)."""
+        out = ctypes.c_double()
+        self.check(self.lib.vc_debug_random_rate(self.h, op, nbytes, ctypes.byref(out)), "vc_debug_random_rate")
+        return out.value
+
     def debug_ft_wide(self, wide: bool = True):
         """Force 64-bit arithmetic in the feature transform (identical results)."""
         self.check(self.lib.vc_debug_ft_wide(self.h, 1 if wide else 0), "vc_debug_ft_wide")
