@@ -297,16 +297,21 @@ typedef struct {
 int vc_autotune(vc_ctx* ctx, double t, vc_tune_result* out);
 
 /* Method of the feature transform's y and x passes (results are identical):
- * VC_FT_ENVELOPE (the default): lower envelope of the parabolas, one thread
- *   per line; its cost per point does not depend on the distances.
+ * VC_FT_ENVELOPE: lower envelope of the parabolas, one thread per line; its
+ *   cost per point does not depend on the distances.
  * VC_FT_WINDOW: a window kernel first -- each point scans outward from
  *   itself until no farther candidate can win or tie, over tiles of 32 lines
  *   staged in shared memory -- which is faster on dense inputs (distances of
  *   a few voxels, e.g. random fields); tiles whose scans run long are left to
  *   the envelope kernel.  Only below 2048 points per axis (otherwise the
- *   envelope runs).  vc_autotune picks the faster for the installed input. */
+ *   envelope runs).
+ * VC_FT_AUTO (the default): the window method when the volume or batch has
+ *   at least one site per 10 lattice points, else the envelope.
+ * vc_autotune times the envelope and the window method on the installed
+ * input and keeps the faster.                                              */
 #define VC_FT_ENVELOPE 0
 #define VC_FT_WINDOW 1
+#define VC_FT_AUTO 2
 int vc_set_ft_method(vc_ctx* ctx, int method);
 
 /* ---- diagnostics ---------------------------------------------------------

@@ -40,7 +40,7 @@ def test_batch_equals_each_volume_alone(gpu_ctx, plain_ctx, t, method):
     try:
         res = gpu_ctx.batch_run(t=t, euler=True)
     finally:
-        gpu_ctx.set_ft_method("envelope")
+        gpu_ctx.set_ft_method("auto")
     parts = gpu_ctx.batch_split(res)
     assert len(res) == len(vols)
     for i, (occ, r, part) in enumerate(zip(vols, res, parts)):

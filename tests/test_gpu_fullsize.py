@@ -87,4 +87,4 @@ def test_full_size_ft_methods_agree(gpu_ctx, grf512):
             out[method] = (_digest(d2, ids), r["rem"], _digest(*ctx.remaining_arrays()))
         assert out["envelope"] == out["window"]
     finally:
-        ctx.set_ft_method("envelope")
+        ctx.set_ft_method("auto")

@@ -82,7 +82,7 @@ def test_ft_narrow_and_wide_arithmetic(gpu_ctx, name, occ):
     ctx = gpu_ctx
     L = lattice_case(O, occ)
     try:
-        for method, wide in (("envelope", False), ("window", False), ("envelope", True)):
+        for method, wide in (("envelope", False), ("window", False), ("auto", False), ("envelope", True)):
             ctx.set_ft_method(method)
             ctx.debug_ft_wide(wide)
             ctx.set_volume(occ)
@@ -92,7 +92,7 @@ def test_ft_narrow_and_wide_arithmetic(gpu_ctx, name, occ):
             assert np.array_equal(d2, L["d2"]) and np.array_equal(ids, L["ids"]), (method, wide)
     finally:
         ctx.debug_ft_wide(False)
-        ctx.set_ft_method("envelope")
+        ctx.set_ft_method("auto")
 
 
 def test_empty_volume(gpu_ctx):

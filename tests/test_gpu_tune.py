@@ -35,7 +35,7 @@ def test_autotune_keeps_results(gpu_ctx):
         for k in ("keep_v", "keep_e", "keep_f"):
             assert np.array_equal(fl2[k], ref["thin"][k]), (shape, k)
     ctx.debug_thin_shape(0, 0, 0)
-    ctx.set_ft_method("envelope")
+    ctx.set_ft_method("auto")
 
 
 def test_autotune_on_a_batch(gpu_ctx):
@@ -49,4 +49,4 @@ def test_autotune_on_a_batch(gpu_ctx):
         assert (r["rem"]["nv"], r["rem"]["ne"], r["rem"]["nt"]) == (
             len(ref["rem_vts"]), len(ref["rem_edges"]), len(ref["rem_tris"]))
     ctx.debug_thin_shape(0, 0, 0)
-    ctx.set_ft_method("envelope")
+    ctx.set_ft_method("auto")

@@ -139,10 +139,10 @@ class Context:
         """Launch shape of the thinning kernel (identical results)."""
         self.check(self.lib.vc_debug_thin_shape(self.h, threads, blocks_per_sm, items), "vc_debug_thin_shape")
 
-    def set_ft_method(self, method: str = "envelope"):
-        """Method of the feature transform's y and x passes: "envelope" or
-        "window" (vc_set_ft_method; identical results)."""
-        m = {"envelope": 0, "window": 1}[method]
+    def set_ft_method(self, method: str = "auto"):
+        """Method of the feature transform's y and x passes: "envelope",
+        "window" or "auto" (vc_set_ft_method; identical results)."""
+        m = {"envelope": 0, "window": 1, "auto": 2}[method]
         self.check(self.lib.vc_set_ft_method(self.h, m), "vc_set_ft_method")
 
     def debug_random_rate(self, op: int, nbytes: int) -> float:

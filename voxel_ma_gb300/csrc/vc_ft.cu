@@ -156,6 +156,10 @@ constexpr int kWinWarps = kWinThreads / 32;
 constexpr int kWinQueue = 64;  // continuing points queued per warp
 constexpr int kWinNear = 6;    // offsets evaluated for every point
 constexpr int kWinFar = 64;    // largest offset scanned (the ring holds +-kWinChunk)
+// VC_FT_AUTO takes the window method when there is at least one site per
+// kWinDensity lattice points: random fields at level 0 have 0.14-0.16 sites
+// per point, meshes and sphere or box unions at these sizes 0.004-0.07.
+constexpr double kWinDensity = 10.0;
 constexpr size_t kWinSmem = (size_t)kWinLines * kWinPitch * sizeof(int64_t) +
                             (size_t)kWinWarps * kWinQueue * (sizeof(int64_t) + sizeof(int32_t));
 
@@ -460,8 +464,11 @@ int run_ft(vc_ctx* c) {
         nmax = std::max<int>(nmax, (int)std::max(NA, std::max(NB, NC)));
     }
     const bool small = nmax <= 2048 && !c->ft_force_wide;
-    const bool win = small && c->ft_window;
     const int64_t N = c->h_off[kLat][nvol];
+    // the window method where the sites are dense (then the distances are a
+    // few voxels): at least one site per kWinDensity lattice points
+    const bool dense = (double)c->n_sites * kWinDensity >= (double)N;
+    const bool win = small && (c->ft_method == VC_FT_WINDOW || (c->ft_method == VC_FT_AUTO && dense));
     VC_TRY(ensure_n<int32_t>(c, c->ft_d2, N));
     VC_TRY(ensure_n<int32_t>(c, c->ft_id, N));
     VC_TRY(ensure_n<int64_t>(c, c->ft_tmp, 3 * N));
@@ -521,8 +528,8 @@ int run_ft(vc_ctx* c) {
 }  // namespace vc
 
 extern "C" int vc_set_ft_method(vc_ctx* c, int method) {
-    if (!c || (method != VC_FT_ENVELOPE && method != VC_FT_WINDOW)) return VC_ERR_ARG;
-    c->ft_window = method == VC_FT_WINDOW;
+    if (!c || (method != VC_FT_ENVELOPE && method != VC_FT_WINDOW && method != VC_FT_AUTO)) return VC_ERR_ARG;
+    c->ft_method = method;
     return VC_OK;
 }
 

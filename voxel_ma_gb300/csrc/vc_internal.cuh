@@ -260,7 +260,7 @@ struct vc_ctx {
     bool ft_force_wide = false;  // feature transform: 64-bit arithmetic at every size
     int ft_ring = 16;            // feature transform: envelope stack entries in shared memory per line
     vc::DevBuf ft_far;           // feature transform: tiles the window kernel left to the envelope kernel
-    bool ft_window = false;      // feature transform: window kernel first (VC_FT_WINDOW)
+    int ft_method = 2;           // feature transform: VC_FT_ENVELOPE, VC_FT_WINDOW or VC_FT_AUTO (default)
     std::mutex* thin_lock = nullptr;  // shared by contexts whose thinning kernels must not overlap
     // remaining complex
     bool rem_valid = false;

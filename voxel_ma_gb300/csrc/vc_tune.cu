@@ -49,7 +49,7 @@ extern "C" int vc_autotune(vc_ctx* c, double t, vc_tune_result* out) {
     *out = vc_tune_result{};
     VC_TRY(run_sites(c, nullptr));
     // feature transform: ring size of the envelope kernel
-    c->ft_window = false;
+    c->ft_method = VC_FT_ENVELOPE;
     const int rings[3] = {4, 8, 16};
     int best_ring = 8;
     float best = 1e30f;
@@ -67,14 +67,14 @@ extern "C" int vc_autotune(vc_ctx* c, double t, vc_tune_result* out) {
     c->ft_ring = best_ring;
     // then the window method (its far tiles use the chosen ring)
     {
-        c->ft_window = true;
+        c->ft_method = VC_FT_WINDOW;
         VC_TRY(run_ft(c));  // untimed
         float ms = 0.0f;
         VC_TRY(time_on_stream(c, [&] { return run_ft(c); }, &ms));
         out->ft_window_ms = ms;
-        c->ft_window = ms < best;
+        c->ft_method = ms < best ? VC_FT_WINDOW : VC_FT_ENVELOPE;
     }
-    out->ft_method = c->ft_window ? VC_FT_WINDOW : VC_FT_ENVELOPE;
+    out->ft_method = c->ft_method;
     VC_TRY(run_ft(c));
     // thinning: threads per block and blocks per SM; every trial thins a
     // fresh copy of the same records (the lattice complex is rebuilt)
