@@ -290,8 +290,10 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                 ea[k] = __ldcg(reinterpret_cast<const int4*>(A.E + e));
             }
             int32_t one[4 * ITEMS];  // cells whose count fell to 1 here
+            int32_t dec[4 * ITEMS];  // cells decremented here (kEdgeBit: edge) and this item's trig there,
+            uint32_t dtg[4 * ITEMS];  // recorded once the decrements have come back (measured faster)
 #pragma unroll
-            for (int q = 0; q < 4 * ITEMS; ++q) one[q] = -1;
+            for (int q = 0; q < 4 * ITEMS; ++q) one[q] = dec[q] = -1;
 #pragma unroll
             for (int k = 0; k < ITEMS; ++k) {
                 if (!has[k]) continue;
@@ -320,10 +322,12 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                         const int ob = rs_count(atomicAdd(&A.E[sb].rs, df));
                         const int o0 = rs_count(atomicAdd(&A.V[v0].rs, de));
                         const int o1 = rs_count(atomicAdd(&A.V[v1].rs, de));
-                        atomicMax(&A.E[sa].trig, trig_make(p, 0));
-                        atomicMax(&A.E[sb].trig, trig_make(p, 1));
-                        atomicMax(&A.V[v0].trig, trig_make(p, 0));
-                        atomicMax(&A.V[v1].trig, trig_make(p, 1));
+                        dec[4 * k + 0] = sa | kEdgeBit;
+                        dec[4 * k + 1] = sb | kEdgeBit;
+                        dec[4 * k + 2] = v0;
+                        dec[4 * k + 3] = v1;
+                        dtg[4 * k + 0] = dtg[4 * k + 2] = trig_make(p, 0);
+                        dtg[4 * k + 1] = dtg[4 * k + 3] = trig_make(p, 1);
                         if (oa == 2) one[4 * k + 0] = sa | kEdgeBit;
                         if (ob == 2) one[4 * k + 1] = sb | kEdgeBit;
                         if (o0 == 2) one[4 * k + 2] = v0;
@@ -345,12 +349,19 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                         const int32_t v0 = ea[k].x, v1 = ea[k].y;
                         const int32_t u = v0 != v ? v0 : v1;
                         if (rs_count(atomicAdd(&A.V[u].rs, rs_drop(e, 0u))) == 2) one[4 * k + 2] = u;
-                        atomicMax(&A.V[u].trig, trig_make(p, 0));
+                        dec[4 * k + 2] = u;
+                        dtg[4 * k + 2] = trig_make(p, 0);
                     }
                 }
             }
 #pragma unroll
             for (int q = 0; q < 4 * ITEMS; ++q) append_cell(s_cells, &s_ncell, one[q] != -1, one[q]);
+#pragma unroll
+            for (int q = 0; q < 4 * ITEMS; ++q) {
+                if (dec[q] == -1) continue;
+                if (dec[q] & kEdgeBit) atomicMax(&A.E[dec[q] & ~kEdgeBit].trig, dtg[q]);
+                else atomicMax(&A.V[dec[q]].trig, dtg[q]);
+            }
             __syncthreads();
             if (threadIdx.x == 0) s_gbase = s_ncell ? atomicAdd(ctr + 0, s_ncell) : 0;
             __syncthreads();
