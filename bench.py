@@ -631,14 +631,14 @@ def run_serving(dev, args, workers=None, max_batch=None, with_plain=True):
 
 
 # DRAM traffic per cell of the complex (V + E + T) of the thinning kernel,
-# from one ncu capture of the 192^3 case of this workload (4.066 GB read +
-# 1.978 GB written for 3,385,169 + 14,026,594 + 10,679,482 cells); the
+# from one ncu capture of the 192^3 case of this workload (4.072 GB read +
+# 1.988 GB written for 3,385,169 + 14,026,594 + 10,679,482 cells); the
 # traffic grows with the complex, so the per-launch figure at 512^3 is this
 # rate times its cells.
-TRAFFIC_PER_CELL = {"thin_generations": (4.065976e9 + 1.978346e9) / (3385169 + 14026594 + 10679482)}
+TRAFFIC_PER_CELL = {"thin_generations": (4.071764e9 + 1.988158e9) / (3385169 + 14026594 + 10679482)}
 # L2 requests (atomics + reads + writes from the SMs) per cell of the same
-# capture: 78.4 M + 43.4 M + 25.7 M for the same cells.
-L2_REQUESTS_PER_CELL = {"thin_generations": (78366741 + 43409625 + 25718621) / (3385169 + 14026594 + 10679482)}
+# capture: 78.5 M + 48.5 M + 26.2 M for the same cells.
+L2_REQUESTS_PER_CELL = {"thin_generations": (78454799 + 48482036 + 26165270) / (3385169 + 14026594 + 10679482)}
 PROBE_BYTES = 16 << 30
 
 
