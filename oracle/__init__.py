@@ -78,6 +78,11 @@ def ref_available() -> bool:
     return os.path.exists(os.path.join(_HERE, "_ref", "libvcref.so"))
 
 
+def reference_tree_present() -> bool:
+    """Whether the reference's source tree is on this host (the recipe builds from it)."""
+    return os.path.isdir(os.path.join(_REFERENCE_TREE, "src"))
+
+
 def ref():
     """The reference's own compiled sources (raises if not built here)."""
     global _REF

@@ -8,7 +8,7 @@ from complexes import grid_surface, octahedron_shell, random_measures
 from helpers import lattice_case
 from voxel_ma_gb300 import volumes
 
-pytestmark = pytest.mark.skipif(not O.ref_available() and not __import__("os").path.isdir("/root/reference/src"),
+pytestmark = pytest.mark.skipif(not O.ref_available() and not O.reference_tree_present(),
                                 reason="reference tree not present on this host")
 
 

@@ -772,8 +772,8 @@ __global__ void inside_size_kernel(Bases B, int nvol, double t) {
     }
 }
 
-// FP64 cross-check of the face measures (the north star's "FP32 with FP64
-// rescue" report): every face's lambda recomputed in double from its two
+// FP64 cross-check of the face measures (the report of an FP32 path with
+// FP64 rescue): every face's lambda recomputed in double from its two
 // sites; out[0] = the largest relative difference to the float lambda the
 // path uses (as the bits of a non-negative double, so atomicMax orders
 // them), out[1] = how many faces' threshold test (lambda < the volume's
