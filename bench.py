@@ -377,8 +377,11 @@ def run_gpu(args):
             cells = r["vd"]["nv"] + r["vd"]["ne"] + r["vd"]["nt"]
             req_s = L2_REQUESTS_PER_CELL[dom] * cells / per_launch_s
             probe = {}
-            for op, name in ((0, "load_8B"), (1, "two_loads_16B"), (2, "atomic_add"), (3, "atomic_max_and_add")):
-                probe[name] = ctx.debug_random_rate(op, PROBE_BYTES)
+            try:
+                for op, name in ((0, "load_8B"), (1, "two_loads_16B"), (2, "atomic_add"), (3, "atomic_max_and_add")):
+                    probe[name] = ctx.debug_random_rate(op, PROBE_BYTES)
+            except RuntimeError as exc:  # e.g. not enough free device memory for the probe's array
+                probe = {"unavailable": str(exc)[:200]}
             roof["random_access"] = {
                 "l2_requests_per_s": req_s,
                 "l2_requests_source": "ncu capture of the 192^3 case (requests per cell) x cells / kernel time",
