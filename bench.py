@@ -355,6 +355,18 @@ def run_gpu(args):
     d2h = s["nv"] * 12 + s["ne"] * 8 + s["nt"] * 12
     e2e_value = replica_throughput(world, nvox, args.steps, e2e_ms)
 
+    # ---- topology (outside the timed regions): nClosedComponents of the
+    # workload's complex -- an all-pass thinning plus face components
+    closed = None
+    if not args.no_probe:
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        n_closed = ctx.closed_components()
+        closed = {"value": n_closed, "ms": (time.perf_counter() - t0) * 1e3,
+                  "note": "nClosedComponents of the 512^3 lattice complex (all-pass thinning + face components), "
+                          "host wall time of one call"}
+        ctx.run_plain(occ_dev, args.t)  # the context holds the workload's own thinning again
+
     # ---- roofline of the dominant kernel -----------------------------------
     peak, peak_kind = measured_hbm_peak()
     regions = {k: v for k, v in timings.items() if k in KERNEL_REGIONS}
@@ -403,6 +415,7 @@ def run_gpu(args):
                     "processed": r["thin"]["processed"], "remaining": r["rem"]},
         "region_ms_per_step": stage_ms,
         "roofline": roof,
+        "closed_components": closed,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nvox, "d2h_bytes_per_step": d2h,
                 "ms_per_step": e2e_ms / args.steps, "wall_s": wall_e2e},
         "gpu_launches": launches,

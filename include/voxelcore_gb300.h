@@ -148,6 +148,16 @@ typedef struct {
 } vc_euler_info;
 int vc_euler_remaining(vc_ctx* ctx, vc_euler_info* out);
 
+/* nClosedComponents(cc) (src/highlevelalgo.cpp:993-1020) on the installed
+ * finalized complex (vc_finalize, or the lattice complex after
+ * vc_lattice_vd): the thinning with every measure 0 and both thresholds 1 --
+ * every pair passes, so only closed pockets survive -- then the number of
+ * face-connected components of the remaining faces (cellcomplex::
+ * compute_conn_cmpnts, src/cellcomplex.cpp:73-147), 0 when no face remains.
+ * Installed measures are neither read nor changed; the thinning flags and
+ * statistics of the context are this thinning's afterwards.                 */
+int vc_closed_components(vc_ctx* ctx, int64_t* n_closed);
+
 /* ---- the plain single-volume path ---------------------------------------
  * Sites, feature transform, lattice Voronoi complex with measures,
  * thinning at thresh = float(inside_size * t) (highlevelalgo.cpp:825-837)

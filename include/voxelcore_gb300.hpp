@@ -235,4 +235,12 @@ private:
     std::vector<uint8_t> kv_, ke_, kf_, re_;
 };
 
+// nClosedComponents(cc) (highlevelalgo.cpp:993-1020): the closed pockets an
+// all-pass thinning of the complex leaves, as face-connected components.
+inline int nClosedComponents(const cellcomplex& cc) {
+    int64_t n = 0;
+    check(cc.context().get(), vc_closed_components(cc.context().get(), &n), "vc_closed_components");
+    return (int)n;
+}
+
 }  // namespace vcgpu

@@ -70,6 +70,8 @@ def lib():
         L.vco_remaining.argtypes = [c_i64, c_vp, c_i64, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp,
                                     c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]
         L.vco_euler.argtypes = [c_i64, c_i64, c_vp, c_i64, c_vp, c_vp]
+        L.vco_closed_components.restype = c_i64
+        L.vco_closed_components.argtypes = [c_i64, c_i64, c_vp, c_i64, c_vp]
         _LIB = L
     return _LIB
 
@@ -103,6 +105,8 @@ def ref():
         R.vcref_cc_adj_size.restype = c_i64
         R.vcref_cc_adj_size.argtypes = [c_vp, ctypes.c_int]
         R.vcref_cc_get_adj.argtypes = [c_vp, ctypes.c_int, c_vp, c_vp]
+        R.vcref_closed_components.restype = ctypes.c_int
+        R.vcref_closed_components.argtypes = [ctypes.c_int, c_vp, ctypes.c_int, c_vp, ctypes.c_int, c_vp]
         R.vcref_thin.restype = ctypes.c_int
         R.vcref_thin.argtypes = [c_vp, c_vp, c_vp, c_vp, ctypes.c_float, ctypes.c_float, c_vp, c_vp, c_vp, c_vp]
         R.vcref_remaining_sizes.argtypes = [c_vp, c_vp, c_vp, c_vp]
@@ -194,6 +198,21 @@ def thin(nv: int, edges: np.ndarray, tris: np.ndarray, em_fin: np.ndarray, fm: n
                         ctypes.c_float(f_t), ctypes.c_float(l_t), _ptr(kv), _ptr(ke), _ptr(kf), _ptr(re), _ptr(st))
     return dict(rc=rc, keep_v=kv, keep_e=ke, keep_f=kf, removed_e=re,
                 stats=dict(pushes=int(st[0]), processed=int(st[1]), skipped=int(st[2]), generations=int(st[3])))
+
+
+def closed_components(nv: int, edges: np.ndarray, tris: np.ndarray) -> int:
+    """nClosedComponents (highlevelalgo.cpp:993-1020) restated."""
+    edges = np.ascontiguousarray(edges, dtype=np.int32).reshape(-1, 2)
+    tris = np.ascontiguousarray(tris, dtype=np.int32).reshape(-1, 3)
+    return int(lib().vco_closed_components(nv, len(edges), _ptr(edges), len(tris), _ptr(tris)))
+
+
+def ref_closed_components(vts, edges, tris) -> int:
+    """The reference's own thinning, remainingCC() and compute_conn_cmpnts()."""
+    vts = np.ascontiguousarray(vts, dtype=np.float32).reshape(-1, 3)
+    edges = np.ascontiguousarray(edges, dtype=np.int32).reshape(-1, 2)
+    tris = np.ascontiguousarray(tris, dtype=np.int32).reshape(-1, 3)
+    return int(ref().vcref_closed_components(len(vts), _ptr(vts), len(edges), _ptr(edges), len(tris), _ptr(tris)))
 
 
 def remaining(vts, edges_fin, tris, keep_v, keep_e, keep_f):

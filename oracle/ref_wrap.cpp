@@ -10,6 +10,8 @@
 //   CellComplexThinning::prune              src/ccthin.cpp:201-424
 //   CellComplexThinning::remainingCC        src/ccthin.cpp:467-512
 //   util::computeEulerChar                  src/geomalgo.cpp:181-214
+//   CellComplexThinning::remainingCC()      src/ccthin.cpp:426-464
+//   cellcomplex::compute_conn_cmpnts        src/cellcomplex.cpp:73-147
 #include <voxelcore/ccthin.h>
 #include <voxelcore/cellcomplex.h>
 #include <voxelcore/densevolume.h>
@@ -169,6 +171,24 @@ void vcref_remaining_get(void* hv, float* vts, int* edges, int* tris) {
         for (int k = 0; k < 2; ++k) edges[2 * i + k] = h->rem_edges[i][k];
     for (size_t i = 0; i < h->rem_tris.size(); ++i)
         for (int k = 0; k < 3; ++k) tris[3 * i + k] = (int)h->rem_tris[i][k];
+}
+
+// The steps of nClosedComponents (src/highlevelalgo.cpp:993-1020, a file
+// not built here) with the reference's own classes: a fresh thinning with
+// every measure 0 pruned at thresholds 1, its remaining complex, and that
+// complex's face-connected components (0 when it has no face).
+int vcref_closed_components(int nv, const float* vts, int ne, const int* edges, int nt, const int* tris) {
+    QuietCout q;
+    void* hv = vcref_cc_create(nv, vts, ne, edges, nt, tris);
+    auto* h = static_cast<RefComplex*>(hv);
+    std::vector<float> V(h->cc.numVts(), 0.0f), E(h->cc.numEdges(), 0.0f), F(h->cc.numFaces(), 0.0f);
+    h->thin.assignElementValues(V, E, F);
+    h->thin.preprocess();
+    h->thin.prune(1.0f, 1.0f, false);
+    cellcomplex rest = h->thin.remainingCC();
+    const int n = rest.numFaces() == 0 ? 0 : rest.compute_conn_cmpnts();
+    vcref_cc_destroy(hv);
+    return n;
 }
 
 // util::computeEulerChar(vts, edges, tris): out = {V, E, F, C, euler}.

@@ -779,3 +779,42 @@ void vco_euler(long long nv, long long ne, const int32_t* edges, long long nt, c
 }
 
 }  // extern "C"
+
+long long vco_closed_components(long long nv, long long ne, const int32_t* edges, long long nt, const int32_t* tris) {
+    Fin F;
+    finalize(nv, ne, edges, nt, tris, F);
+    const long long E = (long long)F.edges.size() / 2;
+    // every measure 0, thresholds 1: every pair passes the filter
+    std::vector<float> em((size_t)E, 0.0f), fm((size_t)nt, 0.0f);
+    std::vector<uint8_t> kv((size_t)nv), ke((size_t)E), kf((size_t)nt), re((size_t)E);
+    if (vco_thin(nv, ne, edges, nt, tris, em.data(), fm.data(), 1.0f, 1.0f, kv.data(), ke.data(), kf.data(),
+                 re.data(), nullptr) != 0)
+        return -1;
+    // breadth-first over the remaining faces, through their sides
+    std::vector<uint8_t> seen_f((size_t)nt, 0), seen_e((size_t)E, 0);
+    std::vector<int32_t> stack;
+    long long ncc = 0;
+    for (long long f0 = 0; f0 < nt; ++f0) {
+        if (!kf[f0] || seen_f[f0]) continue;
+        ++ncc;
+        seen_f[f0] = 1;
+        stack.assign(1, (int32_t)f0);
+        while (!stack.empty()) {
+            const int32_t f = stack.back();
+            stack.pop_back();
+            for (int s = 0; s < 3; ++s) {
+                const int32_t e = F.tri_edges[3 * f + s];
+                if (seen_e[e]) continue;
+                seen_e[e] = 1;
+                for (int32_t k = F.ef_off[e]; k < F.ef_off[e + 1]; ++k) {
+                    const int32_t g = F.ef_ids[k];
+                    if (kf[g] && !seen_f[g]) {
+                        seen_f[g] = 1;
+                        stack.push_back(g);
+                    }
+                }
+            }
+        }
+    }
+    return ncc;
+}

@@ -85,6 +85,13 @@ void vco_remaining(long long nv, const float* vts, long long ne_fin, const int32
 // out = {V, E, F, C, euler}.
 void vco_euler(long long nv, long long ne, const int32_t* edges, long long nt, const int32_t* tris, long long* out);
 
+// nClosedComponents(cc) (highlevelalgo.cpp:993-1020): the thinning with every
+// measure 0 and both thresholds 1 (every pair passes), then the number of
+// face-connected components of the remaining faces (cellcomplex::
+// compute_conn_cmpnts, cellcomplex.cpp:73-147: faces joined through shared
+// edges), 0 when no face remains; -1 on the invariant case of vco_thin.
+long long vco_closed_components(long long nv, long long ne, const int32_t* edges, long long nt, const int32_t* tris);
+
 #ifdef __cplusplus
 }
 #endif

@@ -285,3 +285,46 @@ def test_lambda_fp64_check(gpu_ctx):
     gpu_ctx.lattice_vd()  # no thresholds: flips not counted
     assert gpu_ctx.lambda_fp64_check()["flips"] == -1
 
+
+
+def _closed_cases():
+    yield "octahedron", octahedron_shell()
+    for seed in range(3):
+        rng = np.random.default_rng(100 + seed)
+        yield f"grid{seed}", grid_surface(int(rng.integers(3, 30)), int(rng.integers(3, 30)), seed=seed)
+
+
+@pytest.mark.parametrize("name,cx", list(_closed_cases()), ids=[c[0] for c in _closed_cases()])
+def test_closed_components_generic(gpu_ctx, name, cx):
+    vts, edges, tris = cx
+    gpu_ctx.set_complex(vts, edges, tris)
+    gpu_ctx.finalize()
+    assert gpu_ctx.closed_components() == O.closed_components(len(vts), edges, tris)
+
+
+@pytest.mark.parametrize("name,occ", VOLS[:4], ids=[v[0] for v in VOLS[:4]])
+def test_closed_components_lattice(gpu_ctx, name, occ):
+    """nClosedComponents of the lattice complex: the pockets of the discrete
+    Voronoi regions; also the all-pass thinning's flags against the oracle."""
+    ctx = gpu_ctx
+    L = lattice_case(O, occ)
+    vd = L["vd"]
+    ctx.set_volume(occ)
+    ctx.extract_sites()
+    ctx.feature_transform()
+    ctx.lattice_vd()
+    ctx.use_vd_as_complex()
+    n = ctx.closed_components()
+    assert n == O.closed_components(len(vd["vts"]), vd["edges"], vd["tris"])
+    ref = O.thin(len(vd["vts"]), vd["edges"], vd["tris"], np.zeros(len(L["em_fin"]), np.float32),
+                 np.zeros(len(vd["tris"]), np.float32), 1.0, 1.0)
+    fl = ctx.thin_flags()
+    for k in ("keep_v", "keep_e", "keep_f", "removed_e"):
+        assert np.array_equal(fl[k], ref[k]), k
+    # the thinning with the lattice complex's own measures is unaffected
+    thr = float(np.float32(np.float64(vd["inside_size"]) * 0.04))
+    st = ctx.thin(thr, thr)
+    r = O.thin(len(vd["vts"]), vd["edges"], vd["tris"], L["em_fin"], vd["fm"], thr, thr)
+    fl = ctx.thin_flags()
+    for k in ("keep_v", "keep_e", "keep_f"):
+        assert np.array_equal(fl[k], r[k]), k

@@ -81,3 +81,25 @@ def test_lattice_vd_thin_vs_reference(name, occ):
         ref = rc.thin(vd["vm"], L["em_fin"], vd["fm"], thr, thr)
         for key in ("keep_v", "keep_e", "keep_f", "removed_e"):
             assert np.array_equal(r[key], ref[key]), (t, key)
+
+
+def _topology_cases():
+    yield "octahedron", octahedron_shell()
+    for seed in range(3):
+        rng = np.random.default_rng(seed)
+        yield f"grid{seed}", grid_surface(int(rng.integers(3, 12)), int(rng.integers(3, 12)), seed=seed)
+    for name, occ in (("torus40", volumes.torus_mesh(40)), ("grf32", volumes.grf(32, sigma=4.0, seed=11)),
+                      ("spheres40", volumes.spheres(40, count=12, seed=2)), ("csg", volumes.csg(21, 20, 40))):
+        vd = lattice_case(O, occ)["vd"]
+        yield name, (vd["vts"], vd["edges"], vd["tris"])
+
+
+@pytest.mark.parametrize("name,cx", list(_topology_cases()), ids=[c[0] for c in _topology_cases()])
+def test_closed_components_vs_reference(name, cx):
+    """nClosedComponents: the oracle's restatement against the reference's own
+    thinning, remainingCC() and compute_conn_cmpnts()."""
+    vts, edges, tris = cx
+    n = O.closed_components(len(vts), edges, tris)
+    assert n == O.ref_closed_components(vts, edges, tris)
+    if name == "octahedron":
+        assert n == 1

@@ -139,6 +139,13 @@ class Context:
         """Launch shape of the thinning kernel (identical results)."""
         self.check(self.lib.vc_debug_thin_shape(self.h, threads, blocks_per_sm, items), "vc_debug_thin_shape")
 
+    def closed_components(self) -> int:
+        """nClosedComponents of the installed finalized complex
+        (vc_closed_components): the closed pockets left by an all-pass thinning."""
+        n = ctypes.c_int64()
+        self.check(self.lib.vc_closed_components(self.h, ctypes.byref(n)), "vc_closed_components")
+        return n.value
+
     def set_ft_method(self, method: str = "auto"):
         """Method of the feature transform's y and x passes: "envelope",
         "window" or "auto" (vc_set_ft_method; identical results)."""

@@ -18,6 +18,7 @@ int run_thin_folded(vc_ctx* c, vc_thin_stats* stats);
 int get_thin_flags(vc_ctx* c, uint8_t* kv, uint8_t* ke, uint8_t* kf, uint8_t* re, int mem);
 int run_remaining(vc_ctx* c, vc_rem_sizes* sizes);
 int run_euler_remaining(vc_ctx* c, vc_euler_info* out);
+int run_closed_components(vc_ctx* c, int64_t* n);
 }  // namespace vc
 
 using namespace vc;
@@ -217,6 +218,12 @@ int vc_euler_remaining(vc_ctx* c, vc_euler_info* out) {
     VC_TRY(enter(c));
     if (!out) return VC_ERR_ARG;
     return run_euler_remaining(c, out);
+}
+
+int vc_closed_components(vc_ctx* c, int64_t* n) {
+    VC_TRY(enter(c));
+    if (!n) return VC_ERR_ARG;
+    return run_closed_components(c, n);
 }
 
 int vc_run_plain(vc_ctx* c, const uint8_t* occ, int X, int Y, int Z, int mem, double t, vc_plain_result* out) {

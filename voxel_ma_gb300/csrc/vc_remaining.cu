@@ -113,6 +113,23 @@ __device__ __forceinline__ int32_t uf_find(int32_t* parent, int32_t x) {
     return x;
 }
 
+// Join the sets of a and b (the smaller root becomes the root); false when
+// the bounded retries ran out.
+__device__ __forceinline__ bool uf_join(int32_t* parent, int32_t a, int32_t b) {
+    for (int it = 0; it < (1 << 20); ++it) {
+        a = uf_find(parent, a);
+        b = uf_find(parent, b);
+        if (a == b) return true;
+        if (a > b) {
+            const int32_t t = a;
+            a = b;
+            b = t;
+        }
+        if (atomicCAS(&parent[b], b, a) == b) return true;
+    }
+    return false;
+}
+
 __global__ void uf_init_kernel(int32_t* parent, int32_t n) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) parent[i] = (int32_t)i;
@@ -124,26 +141,7 @@ __global__ void uf_union_kernel(const int32_t* __restrict__ mark, const int2* __
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += stride) {
         if (!mark[e]) continue;
         const int2 ev = edges[e];
-        int32_t a = kept_rank(K.bv, K.pv, ev.x), b = kept_rank(K.bv, K.pv, ev.y);
-        bool done = false;
-        for (int it = 0; it < (1 << 20); ++it) {
-            a = uf_find(parent, a);
-            b = uf_find(parent, b);
-            if (a == b) {
-                done = true;
-                break;
-            }
-            if (a > b) {
-                const int32_t t = a;
-                a = b;
-                b = t;
-            }
-            if (atomicCAS(&parent[b], b, a) == b) {
-                done = true;
-                break;
-            }
-        }
-        if (!done) set_error(err, VC_ERR_TIMEOUT);
+        if (!uf_join(parent, kept_rank(K.bv, K.pv, ev.x), kept_rank(K.bv, K.pv, ev.y))) set_error(err, VC_ERR_TIMEOUT);
     }
 }
 
@@ -171,6 +169,32 @@ __global__ void count_kernel(const int32_t* __restrict__ mark, const int2* __res
         else ++local;
     }
     if (local) atomicAdd(cnt, local);
+}
+
+// Closed components: the remaining faces joined through their sides (node f
+// for face f, node nt + e for edge e), then one count per set holding a face.
+__global__ void cc_join_kernel(const uint8_t* __restrict__ kf, const FaceRec* __restrict__ F, int32_t nt,
+                               int32_t* parent, int* err) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < nt; f += stride) {
+        if (!kf[f]) continue;
+        const int4 r = __ldg(reinterpret_cast<const int4*>(F + f));  // e0 e1 e2|pass rm
+        const int32_t side[3] = {r.x, r.y, r.z & ~kFacePass};
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+            if (!uf_join(parent, (int32_t)f, nt + side[k])) set_error(err, VC_ERR_TIMEOUT);
+    }
+}
+
+__global__ void cc_count_kernel(const uint8_t* __restrict__ kf, int32_t* parent, int32_t nt, int32_t* seen,
+                                unsigned long long* count) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    unsigned long long local = 0;
+    for (int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; f < nt; f += stride) {
+        if (!kf[f]) continue;
+        if (atomicExch(seen + uf_find(parent, (int32_t)f), 1) == 0) ++local;
+    }
+    if (local) atomicAdd(count, local);
 }
 
 inline int grid_for(vc_ctx* c, int64_t n, int threads) {
@@ -223,6 +247,40 @@ int run_remaining(vc_ctx* c, vc_rem_sizes* sizes) {
     c->rem = vc_rem_sizes{h[0], h[1], h[2]};
     c->rem_valid = true;
     if (sizes) *sizes = c->rem;
+    return VC_OK;
+}
+
+int run_thin_all_pass(vc_ctx* c, vc_thin_stats* stats);
+
+// nClosedComponents (highlevelalgo.cpp:993-1020): the thinning with every
+// pair passing, then the face-connected components of the remaining faces
+// (cellcomplex::compute_conn_cmpnts, cellcomplex.cpp:73-147).  The thinning
+// flags of the context are this thinning's afterwards.
+int run_closed_components(vc_ctx* c, int64_t* n) {
+    if (c->nt + c->ne >= INT32_MAX) return VC_ERR_ARG;
+    VC_TRY(run_thin_all_pass(c, nullptr));
+    const int64_t ne = c->ne, nt = c->nt, nodes = nt + ne;
+    *n = 0;
+    if (nt == 0) return VC_OK;
+    VC_TRY(ensure_n<int32_t>(c, c->uf_parent, nodes + 1));
+    VC_TRY(ensure_n<int32_t>(c, c->scratch, nodes + 1));
+    VC_TRY(ensure_n<int64_t>(c, c->scratch2, 2));
+    int32_t* parent = ptr<int32_t>(c->uf_parent);
+    int32_t* seen = ptr<int32_t>(c->scratch);
+    auto* cnt = reinterpret_cast<unsigned long long*>(ptr<int64_t>(c->scratch2));
+    VC_CUDA(c, cudaMemsetAsync(seen, 0, (size_t)nodes * sizeof(int32_t), c->stream));
+    VC_CUDA(c, cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), c->stream));
+    uf_init_kernel<<<grid_for(c, nodes, 256), 256, 0, c->stream>>>(parent, (int32_t)nodes);
+    cc_join_kernel<<<grid_for(c, nt, 256), 256, 0, c->stream>>>(ptr<uint8_t>(c->keep_f), ptr<FaceRec>(c->face_rec),
+                                                                 (int32_t)nt, parent, dev_err(c));
+    cc_count_kernel<<<grid_for(c, nt, 256), 256, 0, c->stream>>>(ptr<uint8_t>(c->keep_f), parent, (int32_t)nt, seen,
+                                                                  cnt);
+    launched(c, 3);
+    VC_CUDA(c, cudaGetLastError());
+    unsigned long long h = 0;
+    VC_CUDA(c, cudaMemcpyAsync(&h, cnt, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    VC_TRY(sync_check(c));
+    *n = (int64_t)h;
     return VC_OK;
 }
 

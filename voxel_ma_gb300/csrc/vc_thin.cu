@@ -93,13 +93,16 @@ __device__ __forceinline__ bool is_fe(int2 it) { return ((unsigned)it.x & kFE) !
 __device__ __forceinline__ int32_t idx0(int2 it) { return (int32_t)((unsigned)it.x & ~kFE); }
 
 // Build the records from the finalized complex (CSR), the measures and the
-// thresholds thr = {f_t, l_t}, and reset the thinning state.  A cell with
-// 2^16 or more incident cells cannot be represented (VC_ERR_ARG).
+// thresholds thr = {f_t, l_t}, and reset the thinning state; with all_pass
+// every cell passes the filter and no measure is read (measures 0 under
+// thresholds 1, as nClosedComponents thins).  A cell with 2^16 or more
+// incident cells cannot be represented (VC_ERR_ARG).
 __global__ void build_records_kernel(const int2* __restrict__ edges, const int32_t* __restrict__ tri_edges,
                                      const int32_t* __restrict__ ve_off, const int32_t* __restrict__ ve_ids,
                                      const int32_t* __restrict__ ef_off, const int32_t* __restrict__ ef_ids,
                                      const float* __restrict__ em, const float* __restrict__ fm,
-                                     const float* __restrict__ thr, int32_t nv, int32_t ne, int32_t nt, FaceRec* F,
+                                     const float* __restrict__ thr, int all_pass, int32_t nv, int32_t ne, int32_t nt,
+                                     FaceRec* F,
                                      EdgeRec* E, VertRec* V, int32_t* __restrict__ g0, int* err) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     const int64_t n = (int64_t)nv + ne + nt;
@@ -109,7 +112,7 @@ __global__ void build_records_kernel(const int2* __restrict__ edges, const int32
             FaceRec r;
             r.e0 = tri_edges[3 * i];
             r.e1 = tri_edges[3 * i + 1];
-            r.e2 = tri_edges[3 * i + 2] | (fm[i] < f_t ? kFacePass : 0);
+            r.e2 = tri_edges[3 * i + 2] | ((all_pass || fm[i] < f_t) ? kFacePass : 0);
             r.rm = kAlive;
             F[i] = r;
         } else if (i < (int64_t)nt + ne) {
@@ -119,7 +122,7 @@ __global__ void build_records_kernel(const int2* __restrict__ edges, const int32
             for (int32_t k = o0; k < o1; ++k) {
                 const int32_t f = ef_ids[k];
                 idsum += (unsigned)f;
-                pass += fm[f] < f_t ? 1u : 0u;
+                pass += (all_pass || fm[f] < f_t) ? 1u : 0u;
             }
             if ((unsigned long long)(o1 - o0) > kRefMask) set_error(err, VC_ERR_ARG);
             EdgeRec r;
@@ -128,7 +131,7 @@ __global__ void build_records_kernel(const int2* __restrict__ edges, const int32
             r.v1 = ev.y;
             r.rs = rs_make((unsigned)(o1 - o0), pass, idsum);
             r.trig = 0;
-            r.em = em[e];
+            r.em = all_pass ? 0.0f : em[e];
             r.rm = kAlive;
             r.pad = 0;
             E[e] = r;
@@ -144,7 +147,7 @@ __global__ void build_records_kernel(const int2* __restrict__ edges, const int32
             r.trig = 0;
             r.rm = kAlive;
             V[v] = r;
-            g0[(int64_t)ne + v] = (o1 - o0 == 1 && em[idsum] < l_t) ? (int32_t)idsum : -1;
+            g0[(int64_t)ne + v] = (o1 - o0 == 1 && (all_pass || em[idsum] < l_t)) ? (int32_t)idsum : -1;
         }
     }
 }
@@ -576,7 +579,7 @@ inline int grid_for(vc_ctx* c, int64_t n, int threads) {
 
 }  // namespace
 
-int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats);
+int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats, bool all_pass = false);
 int ensure_vd_aux(vc_ctx* c, bool meas, bool topo);
 
 int run_thin(vc_ctx* c, float f_t, float l_t, vc_thin_stats* stats) {
@@ -605,16 +608,30 @@ int run_thin_folded(vc_ctx* c, vc_thin_stats* stats) {
     return run_thin_with_device_thr(c, stats);
 }
 
+// Thinning in which every pair passes the filter, whatever the measures:
+// the reference's nClosedComponents sets every measure to 0 and thins at
+// thresholds 1 (highlevelalgo.cpp:993-1020).
+int run_thin_all_pass(vc_ctx* c, vc_thin_stats* stats) {
+    if (!c->cc_finalized) return VC_ERR_STATE;
+    VC_TRY(ensure_n<float>(c, c->thr, 2));
+    set_thr_kernel<<<1, 1, 0, c->stream>>>(ptr<float>(c->thr), 1.0f, 1.0f);
+    launched(c);
+    VC_CUDA(c, cudaGetLastError());
+    c->records_fresh = false;  // the records are rebuilt with every cell passing
+    c->records_thr_folded = false;
+    return run_thin_with_device_thr(c, stats, true);
+}
+
 // Thinning with thresholds already in c->thr (device).
-int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats) {
-    if (!c->cc_finalized || !c->meas_valid) return VC_ERR_STATE;
+int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats, bool all_pass) {
+    if (!c->cc_finalized || (!all_pass && !c->meas_valid)) return VC_ERR_STATE;
     const int64_t nv = c->nv, ne = c->ne, nt = c->nt;
     if (nv + ne >= INT32_MAX || nt >= INT32_MAX) return VC_ERR_ARG;
     const int64_t qcap = nv + ne + 1;
     Region stage(c, "stage_thin");
     if (!c->records_fresh) {
         // the records are built from the measures, sides and lists
-        VC_TRY(ensure_vd_aux(c, true, true));
+        VC_TRY(ensure_vd_aux(c, !all_pass, true));
         VC_TRY(ensure_n<FaceRec>(c, c->face_rec, nt));
         VC_TRY(ensure_n<EdgeRec>(c, c->edge_rec, ne));
         VC_TRY(ensure_n<VertRec>(c, c->vert_rec, nv));
@@ -658,7 +675,8 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats) {
             build_records_kernel<<<grid_for(c, nv + ne + nt, 256), 256, 0, c->stream>>>(
                 ptr<int2>(c->edges), ptr<int32_t>(c->tri_edges), ptr<int32_t>(c->ve_off), ptr<int32_t>(c->ve_ids),
                 ptr<int32_t>(c->ef_off), ptr<int32_t>(c->ef_ids), ptr<float>(c->em), ptr<float>(c->fm), A.thr,
-                (int32_t)nv, (int32_t)ne, (int32_t)nt, A.F, A.E, A.V, ptr<int32_t>(c->thin_g0), dev_err(c));
+                all_pass ? 1 : 0, (int32_t)nv, (int32_t)ne, (int32_t)nt, A.F, A.E, A.V, ptr<int32_t>(c->thin_g0),
+                dev_err(c));
             launched(c);
         }
         VC_CUDA(c, cudaMemsetAsync(ctl, 0, 16 * sizeof(int64_t), c->stream));
