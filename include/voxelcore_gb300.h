@@ -63,6 +63,17 @@ int vc_ctx_get_timings(vc_ctx* ctx, char* names, int name_len, double* ms, int64
  * the box count as outside (include/spaceinfo.h:122-129).  Sites come out in
  * the reference's first-encounter order as float xyz voxel coordinates.   */
 int vc_set_volume(vc_ctx* ctx, const uint8_t* occ, int X, int Y, int Z, int mem);
+/* An octree volume from the bytes of a .sof file (OctreeVolume::
+ * read_sof_file, src/octree.cpp:259-357): decoded on the GPU into the
+ * (R+1)^3 occupancy the reference's OctreeVolume::getDataAt gives
+ * (src/octree.cpp:233-256), and *size = R+1.  vc_extract_sites then follows
+ * the reference's octree rule (Surfacer::extractBoundaryVts,
+ * src/surfacing.cpp:286-301, 666-685): the centres of the leaves whose
+ * corners differ, in the file's order.  VC_ERR_ARG for a malformed stream,
+ * a resolution that is not a power of two, or a leaf above the cell level. */
+int vc_set_volume_sof(vc_ctx* ctx, const void* bytes, int64_t nbytes, int* size);
+/* The installed occupancy (all volumes of a batch, one after another).     */
+int vc_get_volume(vc_ctx* ctx, uint8_t* occ, int mem);
 int vc_extract_sites(vc_ctx* ctx, int64_t* n_sites);
 int vc_get_sites(vc_ctx* ctx, float* xyz, int mem);
 

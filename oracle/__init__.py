@@ -70,6 +70,8 @@ def lib():
         L.vco_remaining.argtypes = [c_i64, c_vp, c_i64, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp,
                                     c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]
         L.vco_euler.argtypes = [c_i64, c_i64, c_vp, c_i64, c_vp, c_vp]
+        L.vco_sof_decode.restype = ctypes.c_int
+        L.vco_sof_decode.argtypes = [c_vp, c_i64, c_vp, c_vp, c_vp, c_vp]
         L.vco_closed_components.restype = c_i64
         L.vco_closed_components.argtypes = [c_i64, c_i64, c_vp, c_i64, c_vp]
         _LIB = L
@@ -105,6 +107,12 @@ def ref():
         R.vcref_cc_adj_size.restype = c_i64
         R.vcref_cc_adj_size.argtypes = [c_vp, ctypes.c_int]
         R.vcref_cc_get_adj.argtypes = [c_vp, ctypes.c_int, c_vp, c_vp]
+        R.vcref_sof_write.restype = ctypes.c_int
+        R.vcref_sof_write.argtypes = [c_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_char_p]
+        R.vcref_sof_occupancy.restype = ctypes.c_int
+        R.vcref_sof_occupancy.argtypes = [ctypes.c_char_p, c_vp]
+        R.vcref_sof_sites.restype = c_i64
+        R.vcref_sof_sites.argtypes = [ctypes.c_char_p, c_vp, c_i64]
         R.vcref_closed_components.restype = ctypes.c_int
         R.vcref_closed_components.argtypes = [ctypes.c_int, c_vp, ctypes.c_int, c_vp, ctypes.c_int, c_vp]
         R.vcref_thin.restype = ctypes.c_int
@@ -205,6 +213,38 @@ def closed_components(nv: int, edges: np.ndarray, tris: np.ndarray) -> int:
     edges = np.ascontiguousarray(edges, dtype=np.int32).reshape(-1, 2)
     tris = np.ascontiguousarray(tris, dtype=np.int32).reshape(-1, 3)
     return int(lib().vco_closed_components(nv, len(edges), _ptr(edges), len(tris), _ptr(tris)))
+
+
+def sof_decode(data: bytes):
+    """A .sof octree file decoded as the reference reads it: (occupancy of the
+    (R+1)^3 voxels, the octree sites in pre-order); None when malformed."""
+    buf = np.frombuffer(data, dtype=np.uint8)
+    size, ns = ctypes.c_int(), ctypes.c_longlong()
+    if lib().vco_sof_decode(_ptr(buf), len(buf), ctypes.byref(size), None, None, ctypes.byref(ns)) != 0:
+        return None
+    n = size.value
+    occ = np.zeros((n, n, n), np.uint8)
+    sites = np.zeros((ns.value, 3), np.float32)
+    lib().vco_sof_decode(_ptr(buf), len(buf), ctypes.byref(size), _ptr(occ), _ptr(sites), ctypes.byref(ns))
+    return occ, sites
+
+
+def ref_sof_write(occ: np.ndarray, path: str) -> None:
+    """The reference's octree of a dense occupancy volume, written as .sof."""
+    occ = np.ascontiguousarray(occ, dtype=np.uint8)
+    X, Y, Z = occ.shape
+    assert ref().vcref_sof_write(_ptr(occ), X, Y, Z, path.encode()) == 0
+
+
+def ref_sof_read(path: str):
+    """The reference's reading of a .sof file: (occupancy, octree sites)."""
+    n = ref().vcref_sof_occupancy(path.encode(), None)
+    occ = np.zeros((n, n, n), np.uint8)
+    ref().vcref_sof_occupancy(path.encode(), _ptr(occ))
+    ns = ref().vcref_sof_sites(path.encode(), None, 0)
+    sites = np.zeros((ns, 3), np.float32)
+    ref().vcref_sof_sites(path.encode(), _ptr(sites), ns)
+    return occ, sites
 
 
 def ref_closed_components(vts, edges, tris) -> int:

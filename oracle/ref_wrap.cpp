@@ -1,5 +1,5 @@
 // C entry points over the reference's own C++ sources (ccthin.cpp,
-// cellcomplex.cpp, geomalgo.cpp, spaceinfo.cpp, surfacing.cpp), compiled
+// cellcomplex.cpp, geomalgo.cpp, octree.cpp, spaceinfo.cpp, surfacing.cpp), compiled
 // unmodified against the API shim in oracle/shim.  TEST INFRASTRUCTURE: only
 // tests/ and the golden-fixture script load the resulting library
 // (oracle/_ref/libvcref.so); the product never does.
@@ -11,11 +11,16 @@
 //   CellComplexThinning::remainingCC        src/ccthin.cpp:467-512
 //   util::computeEulerChar                  src/geomalgo.cpp:181-214
 //   CellComplexThinning::remainingCC()      src/ccthin.cpp:426-464
+//   OctreeVolume (build, .sof write/read)   src/octree.cpp:50-63, 259-357, 499-560, 864-930
+//   OctreeVolume::getDataAt                 src/octree.cpp:233-256
+//   Surfacer::extractBoundaryVts (octree)   src/surfacing.cpp:286-301, 666-685
 //   cellcomplex::compute_conn_cmpnts        src/cellcomplex.cpp:73-147
 #include <voxelcore/ccthin.h>
 #include <voxelcore/cellcomplex.h>
 #include <voxelcore/densevolume.h>
 #include <voxelcore/geomalgo.h>
+#include <voxelcore/octree.h>
+#include <voxelcore/spaceinfo.h>
 #include <voxelcore/surfacing.h>
 
 #include <cstdint>
@@ -62,6 +67,47 @@ long long vcref_extract_sites(const std::uint8_t* occ, int X, int Y, int Z, floa
         out_xyz[3 * i + 1] = sites[i][1];
         out_xyz[3 * i + 2] = sites[i][2];
     }
+    return n;
+}
+
+// The reference's octree of an X*Y*Z occupancy volume written as a .sof
+// file (OctreeVolume(const Volume3DScalar*) then writeToFile).  0 on success.
+int vcref_sof_write(const std::uint8_t* occ, int X, int Y, int Z, const char* path) {
+    QuietCout q;
+    auto vol = std::make_shared<Volume>(occ, X, Y, Z);
+    DenseVolume dv(vol);
+    OctreeVolume oct(&dv);
+    return oct.writeToFile(path) ? 0 : -1;
+}
+
+// The reference's reading of a .sof file: the occupancy of every voxel of
+// its (R+1)^3 grid (SpaceConverter::get_occupancy_at_vox on the octree,
+// x-major, z fastest).  Returns R+1; `out` may be null to get the size.
+int vcref_sof_occupancy(const char* path, std::uint8_t* out) {
+    QuietCout q;
+    OctreeVolume oct(path);
+    const int n = oct.getSizeX();
+    if (out)
+        for (int x = 0; x < n; ++x)
+            for (int y = 0; y < n; ++y)
+                for (int z = 0; z < n; ++z)
+                    out[((long long)x * n + y) * n + z] =
+                        (std::uint8_t)SpaceConverter::get_occupancy_at_vox(ivec3(x, y, z), &oct);
+    return n;
+}
+
+// Surfacer::extractBoundaryVts on the octree read from a .sof file (its
+// octree branch: the centres of the leaves with mixed corners, in tree
+// order).  Returns the number of sites; writes up to `cap` xyz triples.
+long long vcref_sof_sites(const char* path, float* out_xyz, long long cap) {
+    QuietCout q;
+    std::shared_ptr<Volume3DScalar> oct = std::make_shared<OctreeVolume>(path);
+    Surfacer surf;
+    std::vector<point> sites;
+    if (surf.extractBoundaryVts(oct, sites) != SurfacerErrCode::SUCCESS) return -1;
+    long long n = static_cast<long long>(sites.size());
+    for (long long i = 0; i < n && i < cap; ++i)
+        for (int k = 0; k < 3; ++k) out_xyz[3 * i + k] = sites[i][k];
     return n;
 }
 

@@ -28,6 +28,10 @@ public:
     template <class S> explicit Vec(const S* p) { for (std::size_t i = 0; i < D; ++i) v[i] = T(p[i]); }
     template <class S> explicit Vec(const Vec<D, S>& o) { for (std::size_t i = 0; i < D; ++i) v[i] = T(o[i]); }
 
+    // a scalar assigned to a vector sets every component (octree.cpp assigns
+    // an int to its ivec3 sizes)
+    Vec& operator=(T x) { for (std::size_t i = 0; i < D; ++i) v[i] = x; return *this; }
+
     T& operator[](std::size_t i) { return v[i]; }
     const T& operator[](std::size_t i) const { return v[i]; }
     T* data() { return v; }

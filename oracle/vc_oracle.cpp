@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstring>
 #include <deque>
+#include <functional>
 #include <queue>
 #include <thread>
 #include <unordered_map>
@@ -817,4 +818,75 @@ long long vco_closed_components(long long nv, long long ne, const int32_t* edges
         }
     }
     return ncc;
+}
+
+int vco_sof_decode(const uint8_t* b, long long nbytes, int* size_out, uint8_t* occ, float* sites,
+                   long long* nsites) {
+    if (nbytes < 4) return -1;
+    int32_t R = 0;
+    std::memcpy(&R, b, 4);
+    if (R < 1 || (R & (R - 1)) != 0 || R > 16384) return -1;
+    const long long S = (long long)R + 1;
+    std::vector<uint8_t> cell;
+    if (occ) cell.assign((size_t)R * R * R, 0);
+    long long pos = 4, ns = 0;
+    bool ok = true;
+    std::function<void(int, int, int, int)> node = [&](int x, int y, int z, int len) {
+        if (!ok || pos >= nbytes) {
+            ok = false;
+            return;
+        }
+        const uint8_t type = b[pos++];
+        if (type == 2) {  // leaf: one cell
+            if (len != 1 || pos >= nbytes) {
+                ok = false;
+                return;
+            }
+            const uint8_t v = b[pos++];
+            if (occ) cell[((size_t)x * R + y) * R + z] = v;
+            if (v != 0x00 && v != 0xFF) {
+                if (sites) {
+                    sites[3 * ns + 0] = (float)x + 0.5f;
+                    sites[3 * ns + 1] = (float)y + 0.5f;
+                    sites[3 * ns + 2] = (float)z + 0.5f;
+                }
+                ++ns;
+            }
+        } else if (type == 1) {  // empty: one sign for the whole cube
+            if (pos >= nbytes) {
+                ok = false;
+                return;
+            }
+            const uint8_t v = b[pos++] == 1 ? 0xFF : 0x00;
+            if (occ)
+                for (int i = 0; i < len; ++i)
+                    for (int j = 0; j < len; ++j)
+                        for (int k = 0; k < len; ++k) cell[((size_t)(x + i) * R + (y + j)) * R + (z + k)] = v;
+        } else if (type == 0) {  // internal: eight children
+            if (len < 2) {
+                ok = false;
+                return;
+            }
+            const int h = len / 2;
+            for (int i = 0; i < 2; ++i)
+                for (int j = 0; j < 2; ++j)
+                    for (int k = 0; k < 2; ++k) node(x + i * h, y + j * h, z + k * h, h);
+        } else {
+            ok = false;
+        }
+    };
+    node(0, 0, 0, R);
+    if (!ok) return -1;
+    *size_out = (int)S;
+    *nsites = ns;
+    if (occ)
+        for (long long x = 0; x < S; ++x)
+            for (long long y = 0; y < S; ++y)
+                for (long long z = 0; z < S; ++z) {
+                    const int off = (x == R ? 4 : 0) | (y == R ? 2 : 0) | (z == R ? 1 : 0);
+                    const long long cx = x == R ? R - 1 : x, cy = y == R ? R - 1 : y, cz = z == R ? R - 1 : z;
+                    const uint8_t v = cell[((size_t)cx * R + cy) * R + cz];
+                    occ[(x * S + y) * S + z] = ((v >> off) & 1) == 0 ? 1 : 0;
+                }
+    return 0;
 }

@@ -92,6 +92,22 @@ void vco_euler(long long nv, long long ne, const int32_t* edges, long long nt, c
 // edges), 0 when no face remains; -1 on the invariant case of vco_thin.
 long long vco_closed_components(long long nv, long long ne, const int32_t* edges, long long nt, const int32_t* tris);
 
+// A .sof octree file (OctreeVolume::read_sof_file, octree.cpp:259-357): an
+// int32 resolution R (a power of two), then the nodes in pre-order, each a
+// type byte -- 0 internal (eight children, x outermost, z innermost), 1
+// empty (a sign byte: 1 outside, else inside, for every cell below), 2 leaf
+// (one cell; bit 4x+2y+z = corner (x,y,z) outside).  Decoded as the
+// reference reads it: the occupancy of the (R+1)^3 voxels (getDataAt,
+// octree.cpp:233-256: the voxel's own cell, its lowest corner, or for a
+// coordinate R the last cell's far corner; get_occupancy_at_vox) and the
+// sites of its octree branch of Surfacer::extractBoundaryVts
+// (surfacing.cpp:286-301, 666-685: the centre (x+.5,y+.5,z+.5) of every
+// leaf whose corners differ, in pre-order).  Two-call: with occ and sites
+// null only *size_out = R+1 and *nsites are set.  Returns 0, or -1 when the
+// stream is malformed.
+int vco_sof_decode(const uint8_t* bytes, long long nbytes, int* size_out, uint8_t* occ, float* sites,
+                   long long* nsites);
+
 #ifdef __cplusplus
 }
 #endif

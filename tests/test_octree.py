@@ -1,0 +1,66 @@
+"""Octree (.sof) volumes: the oracle's decoding against the fixtures the
+reference's own octree code wrote and read (tests/golden/golden_sof.npz,
+made by tests/golden/make_golden_sof.py), and against the reference itself
+on fresh volumes where its tree is present."""
+import os
+import tempfile
+
+import numpy as np
+import pytest
+
+import oracle as O
+from voxel_ma_gb300 import volumes
+
+ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
+
+
+@pytest.fixture(scope="module")
+def sof_golden():
+    return dict(np.load(os.path.join(ROOT, "tests", "golden", "golden_sof.npz")))
+
+
+def sof_names(g):
+    return sorted(k[len("sof_"):] for k in g if k.startswith("sof_"))
+
+
+def test_oracle_decodes_reference_files(oracle_lib, sof_golden):
+    g = sof_golden
+    for name in sof_names(g):
+        occ, sites = O.sof_decode(g[f"sof_{name}"].tobytes())
+        n = int(g[f"sofsize_{name}"][0])
+        assert occ.shape == (n, n, n), name
+        assert np.array_equal(np.packbits(occ.ravel()), g[f"sofocc_{name}"]), name
+        assert np.array_equal(sites, g[f"sofsites_{name}"].astype(np.float32) - 0.5), name
+
+
+def test_malformed_streams_are_rejected(oracle_lib, sof_golden):
+    data = sof_golden["sof_grf32"].tobytes()
+    assert O.sof_decode(data[:-3]) is None                       # truncated
+    assert O.sof_decode(np.int32(24).tobytes() + data[4:]) is None  # resolution not a power of two
+    bad = bytearray(data)
+    bad[4] = 7                                                  # unknown node type
+    assert O.sof_decode(bytes(bad)) is None
+    assert O.sof_decode(b"\x01") is None
+
+
+@pytest.mark.skipif(not O.ref_available() and not O.reference_tree_present(),
+                    reason="reference tree not present on this host")
+@pytest.mark.parametrize("seed", range(4))
+def test_oracle_vs_reference_fresh_volumes(oracle_lib, seed):
+    rng = np.random.default_rng(300 + seed)
+    shape = tuple(int(s) for s in rng.integers(3, 40, 3))
+    occ = (rng.uniform(size=shape) < rng.uniform(0.2, 0.8)).astype(np.uint8)
+    if seed == 3:
+        occ = volumes.csg(40 + seed, 10, 36)
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "v.sof")
+        O.ref_sof_write(occ, path)
+        occ_ref, sites_ref = O.ref_sof_read(path)
+        occ_o, sites_o = O.sof_decode(open(path, "rb").read())
+    assert np.array_equal(occ_o, occ_ref)
+    assert np.array_equal(sites_o, sites_ref)
+    # the octree holds the volume: its voxels beyond the volume are outside
+    S = occ_ref.shape[0]
+    emb = np.zeros((S, S, S), np.uint8)
+    emb[: occ.shape[0], : occ.shape[1], : occ.shape[2]] = occ > 0
+    assert np.array_equal(occ_o, emb)

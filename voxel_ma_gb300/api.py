@@ -186,6 +186,24 @@ class Context:
         self.check(self.lib.vc_set_volume(self.h, p, X, Y, Z, mem), "vc_set_volume")
         self.shape = (X, Y, Z)
 
+    def set_volume_sof(self, data: bytes) -> int:
+        """Install an octree volume from the bytes of a .sof file
+        (vc_set_volume_sof); returns its voxels per axis (R + 1)."""
+        buf = np.frombuffer(data, dtype=np.uint8)
+        size = ctypes.c_int()
+        self.check(self.lib.vc_set_volume_sof(self.h, buf.ctypes.data_as(ctypes.c_void_p), len(buf),
+                                              ctypes.byref(size)), "vc_set_volume_sof")
+        n = int(size.value)
+        self.shape = (n, n, n)
+        return n
+
+    def volume(self, device: bool = False):
+        """The installed occupancy (vc_get_volume)."""
+        out = self._out(self.shape, np.uint8, device)
+        p, mem = _ptr_mem(out)
+        self.check(self.lib.vc_get_volume(self.h, p, mem), "vc_get_volume")
+        return out
+
     def extract_sites(self) -> int:
         n = ctypes.c_int64()
         self.check(self.lib.vc_extract_sites(self.h, ctypes.byref(n)), "vc_extract_sites")

@@ -50,7 +50,17 @@ int vc_set_volume(vc_ctx* c, const uint8_t* occ, int X, int Y, int Z, int mem) {
     c->Z = Z;
     c->n_sites = -1;
     c->ft_valid = c->vd_valid = false;
+    c->sites_from_octree = false;
+    c->oct_sites.clear();
     return VC_OK;
+}
+
+int vc_get_volume(vc_ctx* c, uint8_t* occ, int mem) {
+    VC_TRY(enter(c));
+    if (!occ || !good_mem(mem)) return VC_ERR_ARG;
+    if (!c->occ.p || c->nvol <= 0) return VC_ERR_STATE;
+    VC_TRY(copy_out(c, occ, c->occ.p, (size_t)c->h_off[kVox][c->nvol], mem));
+    return sync_check(c);
 }
 
 int vc_extract_sites(vc_ctx* c, int64_t* n_sites) {
@@ -260,6 +270,8 @@ int vc_batch_set_volumes(vc_ctx* c, int nvol, const int32_t* dims, const uint8_t
     c->Z = dims[2];
     c->n_sites = -1;
     c->ft_valid = c->vd_valid = false;
+    c->sites_from_octree = false;
+    c->oct_sites.clear();
     return VC_OK;
 }
 

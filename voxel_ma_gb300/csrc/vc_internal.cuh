@@ -201,6 +201,10 @@ struct vc_ctx {
     vc::Bases bases;
     vc::DevBuf bases_buf;
     vc::DevBuf occ;  // uint8, all voxels of all volumes
+    // an octree (.sof) volume: its mixed leaves give the sites (vc_set_volume_sof)
+    bool sites_from_octree = false;
+    std::vector<int4> oct_sites;        // mixed leaves (x, y, z, -) in stream order
+    vc::DevBuf oct_cells, oct_nodes;    // decode scratch: corner byte per cell; node / leaf lists
     // sites
     int64_t n_sites = -1;
     vc::DevBuf site_xyz;    // float3 per site

@@ -1,0 +1,222 @@
+// Octree volume input: the .sof files of the reference's OctreeVolume
+// (read_sof_file, src/octree.cpp:259-357), decoded on the GPU into the dense
+// occupancy the rest of the path reads, and the reference's octree rule for
+// the sites (Surfacer::extractBoundaryVts on an OctreeVolume,
+// src/surfacing.cpp:286-301, 666-685).
+//
+// The stream is an int32 resolution R (a power of two), then the nodes in
+// pre-order: a type byte -- 0 internal (eight children, x outermost, z
+// innermost), 1 empty (a sign byte: 1 outside, anything else inside, for
+// every cell of the cube), 2 leaf (one cell; bit 4x + 2y + z = corner
+// (x, y, z) outside).  The host walks the stream once (a few bytes per node)
+// into the list of terminal nodes -- they tile the R^3 cells -- and the list
+// of leaves whose corners differ; the GPU writes every cell's corner byte
+// (one thread per small node, one block per large one), then every voxel of
+// the (R + 1)^3 grid reads its cell as OctreeVolume::getDataAt does
+// (src/octree.cpp:233-256): its own cell's lowest corner, or, at a
+// coordinate R, the last cell's far corner.  The sites are the centres of
+// the mixed leaves in stream order (the order of the reference's tree walk).
+#include "vc_internal.cuh"
+
+#include <cstring>
+
+namespace vc {
+namespace {
+
+constexpr int kSmallNode = 4;  // nodes up to 4^3 cells: one thread each
+
+// node: {x, y, z, len | sign byte << 24}
+__global__ void oct_small_kernel(const int4* __restrict__ nodes, int64_t n, uint8_t* __restrict__ cell, int R) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const int4 nd = __ldg(nodes + i);
+        const int len = nd.w & 0xffffff;
+        const uint8_t v = (uint8_t)((uint32_t)nd.w >> 24);
+        for (int a = 0; a < len; ++a)
+            for (int b = 0; b < len; ++b) {
+                uint8_t* row = cell + ((int64_t)(nd.x + a) * R + (nd.y + b)) * R + nd.z;
+                for (int c = 0; c < len; ++c) row[c] = v;
+            }
+    }
+}
+
+__global__ void oct_large_kernel(const int4* __restrict__ nodes, int64_t n, uint8_t* __restrict__ cell, int R) {
+    for (int64_t i = blockIdx.x; i < n; i += gridDim.x) {
+        const int4 nd = __ldg(nodes + i);
+        const int len = nd.w & 0xffffff;
+        const uint8_t v = (uint8_t)((uint32_t)nd.w >> 24);
+        const int64_t cells = (int64_t)len * len * len;
+        for (int64_t k = threadIdx.x; k < cells; k += blockDim.x) {
+            const int c = (int)(k % len);
+            const int64_t ab = k / len;
+            const int b = (int)(ab % len), a = (int)(ab / len);
+            cell[((int64_t)(nd.x + a) * R + (nd.y + b)) * R + nd.z + c] = v;
+        }
+    }
+}
+
+// voxel (x, y, z) of the (R + 1)^3 grid: inside iff its corner bit is 0
+__global__ void oct_voxels_kernel(const uint8_t* __restrict__ cell, int R, uint8_t* __restrict__ occ) {
+    const int64_t S = (int64_t)R + 1, n = S * S * S;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const int z = (int)(i % S);
+        const int64_t xy = i / S;
+        const int y = (int)(xy % S), x = (int)(xy / S);
+        const int off = (x == R ? 4 : 0) | (y == R ? 2 : 0) | (z == R ? 1 : 0);
+        const int cx = min(x, R - 1), cy = min(y, R - 1), cz = min(z, R - 1);
+        const uint8_t v = __ldg(cell + ((int64_t)cx * R + cy) * R + cz);
+        occ[i] = ((v >> off) & 1) == 0 ? 1 : 0;
+    }
+}
+
+// the octree sites: centre of mixed leaf (x, y, z) = lattice point (x+1, y+1, z+1)
+__global__ void oct_sites_kernel(const int4* __restrict__ leaves, int64_t n, int S, float* __restrict__ xyz,
+                                 int32_t* __restrict__ site_id_lat) {
+    const int64_t L = (int64_t)S + 1;  // lattice points per axis
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const int4 p = __ldg(leaves + i);
+        xyz[3 * i + 0] = (float)p.x + 0.5f;
+        xyz[3 * i + 1] = (float)p.y + 0.5f;
+        xyz[3 * i + 2] = (float)p.z + 0.5f;
+        site_id_lat[((int64_t)(p.x + 1) * L + (p.y + 1)) * L + (p.z + 1)] = (int32_t)i;
+    }
+}
+
+inline int grid_of(vc_ctx* c, int64_t n, int threads) {
+    return (int)std::max<int64_t>(1, std::min<int64_t>((n + threads - 1) / threads, (int64_t)c->num_sms * 16));
+}
+
+// Walk the node stream: terminal nodes by size, mixed leaves in order.
+int parse_sof(const uint8_t* b, int64_t nbytes, int& R, std::vector<int4>& small, std::vector<int4>& large,
+              std::vector<int4>& mixed) {
+    if (nbytes < 4) return VC_ERR_ARG;
+    int32_t r = 0;
+    std::memcpy(&r, b, 4);
+    if (r < 1 || (r & (r - 1)) != 0 || r > 16384) return VC_ERR_ARG;
+    R = r;
+    struct Frame {
+        int x, y, z, len, child;
+    };
+    std::vector<Frame> stack;
+    int64_t pos = 4;
+    // read one node at (x, y, z, len); internal nodes are pushed
+    auto visit = [&](int x, int y, int z, int len) -> int {
+        if (pos >= nbytes) return VC_ERR_ARG;
+        const uint8_t type = b[pos++];
+        if (type == 0) {
+            if (len < 2) return VC_ERR_ARG;
+            stack.push_back(Frame{x, y, z, len, 0});
+            return VC_OK;
+        }
+        if (type != 1 && type != 2) return VC_ERR_ARG;
+        if (pos >= nbytes) return VC_ERR_ARG;
+        const uint8_t raw = b[pos++];
+        uint8_t v;
+        if (type == 2) {  // a leaf is one cell
+            if (len != 1) return VC_ERR_ARG;
+            v = raw;
+            if (v != 0x00 && v != 0xff) mixed.push_back(make_int4(x, y, z, 0));
+        } else {
+            v = raw == 1 ? 0xff : 0x00;
+        }
+        const int4 nd = make_int4(x, y, z, len | ((int)v << 24));
+        (len <= kSmallNode ? small : large).push_back(nd);
+        return VC_OK;
+    };
+    VC_TRY(visit(0, 0, 0, R));
+    while (!stack.empty()) {
+        Frame& f = stack.back();
+        if (f.child == 8) {
+            stack.pop_back();
+            continue;
+        }
+        const int h = f.len / 2, i = f.child >> 2, j = (f.child >> 1) & 1, k = f.child & 1;
+        ++f.child;
+        const Frame cur = f;  // visit() may grow the stack
+        VC_TRY(visit(cur.x + i * h, cur.y + j * h, cur.z + k * h, h));
+    }
+    return VC_OK;
+}
+
+}  // namespace
+
+int install_octree(vc_ctx* c, const uint8_t* bytes, int64_t nbytes, int* size_out) {
+    int R = 0;
+    std::vector<int4> small, large, mixed;
+    VC_TRY(parse_sof(bytes, nbytes, R, small, large, mixed));
+    const int S = R + 1;
+    if ((int64_t)(S + 1) * (S + 1) * (S + 1) >= ((int64_t)1 << 33) || S > 32766) return VC_ERR_ARG;
+    const int64_t ncell = (int64_t)R * R * R, nvox = (int64_t)S * S * S;
+    VC_TRY(ensure_n<uint8_t>(c, c->oct_cells, ncell));
+    VC_TRY(ensure_n<int4>(c, c->oct_nodes, (int64_t)(small.size() + large.size()) + 1));
+    VC_TRY(ensure_n<uint8_t>(c, c->occ, nvox));
+    int4* dn = ptr<int4>(c->oct_nodes);
+    uint8_t* cell = ptr<uint8_t>(c->oct_cells);
+    if (!small.empty())
+        VC_CUDA(c, cudaMemcpyAsync(dn, small.data(), small.size() * sizeof(int4), cudaMemcpyHostToDevice, c->stream));
+    if (!large.empty())
+        VC_CUDA(c, cudaMemcpyAsync(dn + small.size(), large.data(), large.size() * sizeof(int4),
+                                   cudaMemcpyHostToDevice, c->stream));
+    {
+        Region r(c, "octree_decode");
+        if (!small.empty()) {
+            oct_small_kernel<<<grid_of(c, (int64_t)small.size(), 256), 256, 0, c->stream>>>(
+                dn, (int64_t)small.size(), cell, R);
+            launched(c);
+        }
+        if (!large.empty()) {
+            oct_large_kernel<<<(int)std::min<int64_t>((int64_t)large.size(), (int64_t)c->num_sms * 8), 256, 0,
+                               c->stream>>>(dn + small.size(), (int64_t)large.size(), cell, R);
+            launched(c);
+        }
+        oct_voxels_kernel<<<grid_of(c, nvox, 256), 256, 0, c->stream>>>(cell, R, ptr<uint8_t>(c->occ));
+        launched(c);
+        VC_CUDA(c, cudaGetLastError());
+    }
+    const int32_t dims[3] = {S, S, S};
+    VC_TRY(set_volume_table(c, 1, dims));
+    c->X = c->Y = c->Z = S;
+    c->n_sites = -1;
+    c->ft_valid = c->vd_valid = false;
+    c->oct_sites = std::move(mixed);
+    c->sites_from_octree = true;
+    if (size_out) *size_out = S;
+    return sync_check(c);  // the host node lists go out of scope
+}
+
+// The octree rule for the sites (run_sites calls it for an octree volume):
+// the centres of the mixed leaves, in stream order; the packed occupancy
+// words are written as for a dense volume.
+int octree_sites(vc_ctx* c, uint32_t* bits, int32_t* cnt, int64_t nwords, int64_t* total, int64_t* n_out) {
+    const int64_t n = (int64_t)c->oct_sites.size();
+    const int64_t nlat = c->h_off[kLat][c->nvol];
+    VC_TRY(ensure_n<int4>(c, c->oct_nodes, n + 1));
+    VC_TRY(ensure_n<float>(c, c->site_xyz, 3 * n + 3));
+    int4* dl = ptr<int4>(c->oct_nodes);
+    if (n > 0)
+        VC_CUDA(c, cudaMemcpyAsync(dl, c->oct_sites.data(), n * sizeof(int4), cudaMemcpyHostToDevice, c->stream));
+    // per-volume site bases: one volume, n sites
+    VC_CUDA(c, cudaMemsetAsync(cnt, 0, (size_t)std::max<int64_t>(nwords, 1) * sizeof(int32_t), c->stream));
+    VC_CUDA(c, cudaMemcpyAsync(total, &n, sizeof(int64_t), cudaMemcpyHostToDevice, c->stream));
+    VC_TRY(fill_bases(c, kBSite, kVWord, cnt, total));
+    VC_CUDA(c, cudaMemsetAsync(c->site_id_lat.p, 0xff, (size_t)nlat * sizeof(int32_t), c->stream));
+    if (n > 0) {
+        oct_sites_kernel<<<grid_of(c, n, 256), 256, 0, c->stream>>>(dl, n, c->X, ptr<float>(c->site_xyz),
+                                                                     ptr<int32_t>(c->site_id_lat));
+        launched(c);
+    }
+    VC_CUDA(c, cudaGetLastError());
+    (void)bits;
+    *n_out = n;
+    return sync_check(c);  // n is read from host memory by the copy above
+}
+
+}  // namespace vc
+
+extern "C" int vc_set_volume_sof(vc_ctx* c, const void* bytes, int64_t nbytes, int* size) {
+    if (!c || !bytes || nbytes < 0) return VC_ERR_ARG;
+    if (cudaSetDevice(c->device) != cudaSuccess) return vc::cuda_fail(c, cudaGetLastError(), "cudaSetDevice");
+    return vc::install_octree(c, static_cast<const uint8_t*>(bytes), nbytes, size);
+}

@@ -249,6 +249,8 @@ inline int row_grid(int num_sms, int64_t rows) {
 
 }  // namespace
 
+int octree_sites(vc_ctx* c, uint32_t* bits, int32_t* cnt, int64_t nwords, int64_t* total, int64_t* n_out);
+
 int run_sites(vc_ctx* c, int64_t* n_sites) {
     if (!c->occ.p || c->nvol <= 0) return VC_ERR_STATE;
     const int64_t nlat = c->h_off[kLat][c->nvol];
@@ -272,6 +274,14 @@ int run_sites(vc_ctx* c, int64_t* n_sites) {
         VC_CUDA(c, cudaGetLastError());
     }
     int64_t* total = ptr<int64_t>(c->scratch2);
+    if (c->sites_from_octree) {
+        // an octree volume: the sites are its mixed leaves (Surfacer's octree rule)
+        int64_t n = 0;
+        VC_TRY(octree_sites(c, bits, cnt, nwords, total, &n));
+        c->n_sites = n;
+        if (n_sites) *n_sites = n;
+        return VC_OK;
+    }
     VC_TRY(scan_exclusive_i32(c, cnt, cnt, nwords, total));
     VC_TRY(fill_bases(c, kBSite, kVWord, cnt, total));
     int64_t n = 0;
