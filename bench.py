@@ -367,6 +367,29 @@ def run_gpu(args):
                           "host wall time of one call"}
         ctx.run_plain(occ_dev, args.t)  # the context holds the workload's own thinning again
 
+    # ---- octree input (outside the timed regions): the workload written as the
+    # reference's .sof octree (host encoder), then decoded on the GPU
+    octree = None
+    if not args.no_probe:
+        t0 = time.perf_counter()
+        sof = api.encode_sof(occ_np)
+        enc_s = time.perf_counter() - t0
+        oct_ctx = api.Context(local)
+        dec = []
+        for _ in range(4):
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            size = oct_ctx.set_volume_sof(sof)
+            dec.append(time.perf_counter() - t0)
+        n_oct_sites = oct_ctx.extract_sites()
+        same = bool(np.array_equal(oct_ctx.volume()[: shape[0], : shape[1], : shape[2]], occ_np > 0))
+        oct_ctx.close()
+        dec_s = min(dec[1:])
+        octree = {"file_bytes": len(sof), "voxels": size ** 3, "decode_ms": dec_s * 1e3,
+                  "decode_voxels_per_s": size ** 3 / dec_s, "encode_ms_host": enc_s * 1e3,
+                  "octree_sites": n_oct_sites, "round_trip": same,
+                  "note": "vc_set_volume_sof (host stream walk + GPU fill), best of 3 after one untimed call"}
+
     # ---- roofline of the dominant kernel -----------------------------------
     peak, peak_kind = measured_hbm_peak()
     regions = {k: v for k, v in timings.items() if k in KERNEL_REGIONS}
@@ -416,6 +439,7 @@ def run_gpu(args):
         "region_ms_per_step": stage_ms,
         "roofline": roof,
         "closed_components": closed,
+        "octree": octree,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nvox, "d2h_bytes_per_step": d2h,
                 "ms_per_step": e2e_ms / args.steps, "wall_s": wall_e2e},
         "gpu_launches": launches,
@@ -670,7 +694,8 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-path measurement")
     ap.add_argument("--no-serve", action="store_true", help="skip the request-stream measurement")
     ap.add_argument("--no-tune", action="store_true", help="keep the library's default launch shapes")
-    ap.add_argument("--no-probe", action="store_true", help="skip the random-access probe")
+    ap.add_argument("--no-probe", action="store_true",
+                    help="skip the random-access probe and the topology and octree measurements")
     ap.add_argument("--ft-method", choices=["envelope", "window"], default=None,
                     help="with --no-tune: the feature transform's method for the plain path")
     args = ap.parse_args()

@@ -74,6 +74,12 @@ int vc_set_volume(vc_ctx* ctx, const uint8_t* occ, int X, int Y, int Z, int mem)
 int vc_set_volume_sof(vc_ctx* ctx, const void* bytes, int64_t nbytes, int* size);
 /* The installed occupancy (all volumes of a batch, one after another).     */
 int vc_get_volume(vc_ctx* ctx, uint8_t* occ, int mem);
+/* The .sof stream of an X*Y*Z host occupancy volume (x-major, z fastest) as
+ * the reference writes it (OctreeVolume(const Volume3DScalar*) and
+ * write_sof_file, src/octree.cpp:50-63, 499-560, 864-930).  Host code, no
+ * context.  *nbytes = the stream's length; with out non-null and cap at
+ * least that, the stream is copied to out.                                 */
+int vc_encode_sof(const uint8_t* occ, int X, int Y, int Z, uint8_t* out, int64_t cap, int64_t* nbytes);
 int vc_extract_sites(vc_ctx* ctx, int64_t* n_sites);
 int vc_get_sites(vc_ctx* ctx, float* xyz, int mem);
 

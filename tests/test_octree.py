@@ -64,3 +64,38 @@ def test_oracle_vs_reference_fresh_volumes(oracle_lib, seed):
     emb = np.zeros((S, S, S), np.uint8)
     emb[: occ.shape[0], : occ.shape[1], : occ.shape[2]] = occ > 0
     assert np.array_equal(occ_o, emb)
+
+
+def _golden_sof_volumes():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(
+        "make_golden_sof", os.path.join(ROOT, "tests", "golden", "make_golden_sof.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.sof_volumes()
+
+
+def test_encoder_writes_the_reference_bytes(sof_golden):
+    """vc_encode_sof (host code of the library, no GPU) against the files the
+    reference's OctreeVolume wrote for the same volumes."""
+    from voxel_ma_gb300 import api
+    for name, occ in _golden_sof_volumes().items():
+        assert api.encode_sof(np.asarray(occ)) == sof_golden[f"sof_{name}"].tobytes(), name
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_encode_decode_round_trip(oracle_lib, seed):
+    from voxel_ma_gb300 import api
+    rng = np.random.default_rng(500 + seed)
+    shape = tuple(int(s) for s in rng.integers(1, 34, 3))
+    occ = (rng.uniform(size=shape) < rng.uniform(0.1, 0.9)).astype(np.uint8)
+    occ_d, _ = O.sof_decode(api.encode_sof(occ))
+    S = occ_d.shape[0]
+    emb = np.zeros((S, S, S), np.uint8)
+    emb[: shape[0], : shape[1], : shape[2]] = occ
+    assert np.array_equal(occ_d, emb)
+    if O.ref_available():
+        with tempfile.TemporaryDirectory() as d:
+            path = os.path.join(d, "v.sof")
+            O.ref_sof_write(occ, path)
+            assert open(path, "rb").read() == api.encode_sof(occ)

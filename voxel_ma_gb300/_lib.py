@@ -115,6 +115,7 @@ SIGNATURES = {
     "vc_closed_components": (c_int, [c_vp, ctypes.POINTER(c_i64)]),
     "vc_set_volume_sof": (c_int, [c_vp, c_vp, c_i64, ctypes.POINTER(c_int)]),
     "vc_get_volume": (c_int, [c_vp, c_vp, c_int]),
+    "vc_encode_sof": (c_int, [c_vp, c_int, c_int, c_int, c_vp, c_i64, ctypes.POINTER(c_i64)]),
     "vc_debug_random_rate": (c_int, [c_vp, c_int, c_i64, ctypes.POINTER(ctypes.c_double)]),
     "vc_debug_thin_shape": (c_int, [c_vp, c_int, c_int, c_int]),
     "vc_autotune": (c_int, [c_vp, ctypes.c_double, ctypes.POINTER(TuneResult)]),

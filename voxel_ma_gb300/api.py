@@ -472,6 +472,24 @@ class Server:
             pass
 
 
+def encode_sof(occ) -> bytes:
+    """The .sof octree stream of a dense occupancy volume (host numpy array),
+    as the reference's OctreeVolume writes it (vc_encode_sof)."""
+    lib = L.load()
+    occ = np.ascontiguousarray(occ, dtype=np.uint8)
+    X, Y, Z = (int(s) for s in occ.shape)
+    p = occ.ctypes.data_as(ctypes.c_void_p)
+    n = ctypes.c_int64()
+    st = lib.vc_encode_sof(p, X, Y, Z, None, 0, ctypes.byref(n))
+    if st != L.VC_OK:
+        raise L.VoxelCoreError(st, "vc_encode_sof")
+    out = np.zeros(n.value, np.uint8)
+    st = lib.vc_encode_sof(p, X, Y, Z, out.ctypes.data_as(ctypes.c_void_p), n.value, ctypes.byref(n))
+    if st != L.VC_OK:
+        raise L.VoxelCoreError(st, "vc_encode_sof")
+    return out.tobytes()
+
+
 def plan_batches(voxels, t, share_bytes: int, bytes_per_voxel: float = 640.0, max_batch: int = 64) -> np.ndarray:
     """vc_plan_batches: the batch number each request (in arrival order) gets."""
     lib = L.load()

@@ -19,6 +19,7 @@
 #include "vc_internal.cuh"
 
 #include <cstring>
+#include <thread>
 
 namespace vc {
 namespace {
@@ -219,4 +220,149 @@ extern "C" int vc_set_volume_sof(vc_ctx* c, const void* bytes, int64_t nbytes, i
     if (!c || !bytes || nbytes < 0) return VC_ERR_ARG;
     if (cudaSetDevice(c->device) != cudaSuccess) return vc::cuda_fail(c, cudaGetLastError(), "cudaSetDevice");
     return vc::install_octree(c, static_cast<const uint8_t*>(bytes), nbytes, size);
+}
+
+// ---------------------------------------------------------------------------
+// Writing: the .sof stream of a dense occupancy volume as the reference
+// writes it (OctreeVolume(const Volume3DScalar*), src/octree.cpp:50-63 and
+// build, :864-930; write_sof_file, :499-560).  R is the smallest power of two
+// >= max(X, Y, Z) - 1 (util::log2Int); a cube that does not touch the volume
+// (closed boxes, util::intersect) is an empty node with sign 1; a cell is a
+// leaf whose bit 4i + 2j + k is set when voxel (x+i, y+j, z+k) is outside;
+// eight children that are all uniform with one sign merge into an empty
+// node.  Built bottom-up (one byte of state per node and level), then
+// written in pre-order.
+namespace vc {
+namespace {
+
+// node state: bit 7 uniform, bit 0 its sign; bits 1-2 the type to write
+// (0 internal, 1 empty, 2 leaf); leaves keep their corner byte separately
+constexpr uint8_t kUni = 0x80;
+
+inline int log2_int(int n) {  // util::log2Int: ceil(log2(n)), 0 for n <= 1
+    int hib = 0;
+    if (n) {
+        int m = n, r = 1;
+        while (m >>= 1) ++r;
+        hib = r - 1;
+    }
+    return hib + ((1 << hib) < n ? 1 : 0);
+}
+
+}  // namespace
+
+int encode_sof(const uint8_t* occ, int X, int Y, int Z, std::vector<uint8_t>& out) {
+    const int mx = std::max(X, std::max(Y, Z));
+    const int R = 1 << log2_int(mx - 1);
+    auto inside = [&](int x, int y, int z) -> bool {
+        return x >= 0 && y >= 0 && z >= 0 && x < X && y < Y && z < Z && occ[((int64_t)x * Y + y) * Z + z] > 0;
+    };
+    auto touches = [&](int x, int y, int z, int l) {  // closed boxes [p, p+l] and [0, size]
+        return !(x > X || y > Y || z > Z);  // p >= 0 and 0 <= p + l always
+    };
+    // levels: level k holds (R >> k)^3 nodes
+    int nlev = 0;
+    while ((1 << nlev) <= R) ++nlev;  // len 1 .. R
+    std::vector<std::vector<uint8_t>> st(nlev);
+    std::vector<uint8_t> leafv((size_t)R * R * R);
+    // level 0: cells
+    st[0].assign((size_t)R * R * R, 0);
+    {
+        const int nth = (int)std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+        std::vector<std::thread> th;
+        for (int t = 0; t < nth; ++t)
+            th.emplace_back([&, t] {
+                for (int x = t; x < R; x += nth)
+                    for (int y = 0; y < R; ++y)
+                        for (int z = 0; z < R; ++z) {
+                            const size_t i = ((size_t)x * R + y) * R + z;
+                            if (!touches(x, y, z, 1)) {
+                                st[0][i] = kUni | 1 | (1 << 1);  // empty, sign 1
+                                continue;
+                            }
+                            uint8_t b = 0;
+                            for (int a = 0; a < 2; ++a)
+                                for (int c = 0; c < 2; ++c)
+                                    for (int d = 0; d < 2; ++d)
+                                        if (!inside(x + a, y + c, z + d)) b |= (uint8_t)(1 << (4 * a + 2 * c + d));
+                            leafv[i] = b;
+                            st[0][i] = (uint8_t)((b == 0x00 || b == 0xff ? kUni : 0) | (b & 1) | (2 << 1));  // leaf
+                        }
+            });
+        for (auto& t : th) t.join();
+    }
+    for (int k = 1; k < nlev; ++k) {
+        const int n = R >> k, l = 1 << k, nc = n * 2;
+        st[k].assign((size_t)n * n * n, 0);
+        for (int x = 0; x < n; ++x)
+            for (int y = 0; y < n; ++y)
+                for (int z = 0; z < n; ++z) {
+                    uint8_t& s = st[k][((size_t)x * n + y) * n + z];
+                    if (!touches(x * l, y * l, z * l, l)) {
+                        s = kUni | 1 | (1 << 1);
+                        continue;
+                    }
+                    bool uni = true;
+                    int sign = -1;
+                    for (int a = 0; a < 2 && uni; ++a)
+                        for (int c = 0; c < 2 && uni; ++c)
+                            for (int d = 0; d < 2 && uni; ++d) {
+                                const uint8_t cs = st[k - 1][((size_t)(2 * x + a) * nc + (2 * y + c)) * nc + 2 * z + d];
+                                if (!(cs & kUni) || (sign >= 0 && (cs & 1) != sign)) uni = false;
+                                else sign = cs & 1;
+                            }
+                    s = uni ? (uint8_t)(kUni | sign | (1 << 1)) : (uint8_t)0;  // merged empty, or internal
+                }
+    }
+    // pre-order
+    out.clear();
+    const int32_t r32 = R;
+    out.resize(4);
+    std::memcpy(out.data(), &r32, 4);
+    struct F {
+        int k, x, y, z, child;
+    };
+    std::vector<F> stack;
+    auto emit = [&](int k, int x, int y, int z) {
+        const int n = R >> k;
+        const uint8_t s = st[k][((size_t)x * n + y) * n + z];
+        const int type = (s >> 1) & 3;
+        if (type == 0) {
+            out.push_back(0);
+            stack.push_back(F{k, x, y, z, 0});
+        } else if (type == 1) {
+            out.push_back(1);
+            out.push_back((uint8_t)(s & 1));
+        } else {
+            out.push_back(2);
+            out.push_back(leafv[((size_t)x * R + y) * R + z]);
+        }
+    };
+    emit(nlev - 1, 0, 0, 0);
+    while (!stack.empty()) {
+        F& f = stack.back();
+        if (f.child == 8) {
+            stack.pop_back();
+            continue;
+        }
+        const int a = f.child >> 2, c = (f.child >> 1) & 1, d = f.child & 1;
+        ++f.child;
+        const F cur = f;
+        emit(cur.k - 1, 2 * cur.x + a, 2 * cur.y + c, 2 * cur.z + d);
+    }
+    return VC_OK;
+}
+
+}  // namespace vc
+
+extern "C" int vc_encode_sof(const uint8_t* occ, int X, int Y, int Z, uint8_t* out, int64_t cap, int64_t* nbytes) {
+    if (!occ || !nbytes || X <= 0 || Y <= 0 || Z <= 0 || std::max(X, std::max(Y, Z)) > 16385) return VC_ERR_ARG;
+    std::vector<uint8_t> buf;
+    VC_TRY(vc::encode_sof(occ, X, Y, Z, buf));
+    *nbytes = (int64_t)buf.size();
+    if (out) {
+        if (cap < (int64_t)buf.size()) return VC_ERR_ARG;
+        std::memcpy(out, buf.data(), buf.size());
+    }
+    return VC_OK;
 }
