@@ -388,7 +388,7 @@ def run_gpu(args):
         octree = {"file_bytes": len(sof), "voxels": size ** 3, "decode_ms": dec_s * 1e3,
                   "decode_voxels_per_s": size ** 3 / dec_s, "encode_ms_host": enc_s * 1e3,
                   "octree_sites": n_oct_sites, "round_trip": same,
-                  "note": "vc_set_volume_sof (host stream walk + GPU fill), best of 3 after one untimed call"}
+                  "note": "vc_set_volume_sof (host split pass over the type bytes + GPU subtree walks, stream copy included), best of 3 after one untimed call"}
 
     # ---- roofline of the dominant kernel -----------------------------------
     peak, peak_kind = measured_hbm_peak()

@@ -59,3 +59,48 @@ def test_malformed_sof_is_rejected(gpu_ctx, sof_golden):
     occ = np.ones((4, 5, 6), np.uint8)
     gpu_ctx.set_volume(occ)
     assert gpu_ctx.extract_sites() == len(O.extract_sites(occ)[0])
+
+
+def test_uniform_cube_has_no_sites(gpu_ctx):
+    # the whole cube one empty node: no subtree for the walker, no sites
+    for sign, inside in ((1, 0), (0, 1), (2, 1)):
+        data = np.int32(64).tobytes() + bytes([1, sign])
+        assert gpu_ctx.set_volume_sof(data) == 65
+        assert np.array_equal(gpu_ctx.volume(), np.full((65, 65, 65), inside, np.uint8))
+        assert gpu_ctx.extract_sites() == 0
+
+
+def test_malformed_subtree_is_rejected_on_the_device(gpu_ctx, sof_golden):
+    bad = [
+        np.int32(32).tobytes() + bytes([0]) + bytes([2, 0x0F]) * 8,    # a leaf of 16^3 cells
+        np.int32(2).tobytes() + bytes([0, 0]) + bytes([1, 1]) * 15,    # an internal node of one cell
+    ]
+    for data in bad:
+        assert O.sof_decode(data) is None
+        with pytest.raises(_lib.VoxelCoreError) as ei:
+            gpu_ctx.set_volume_sof(data)
+        assert ei.value.status == _lib.VC_ERR_ARG
+    # the context stays usable
+    g = sof_golden
+    n = gpu_ctx.set_volume_sof(g["sof_grf32"].tobytes())
+    assert np.array_equal(np.packbits(gpu_ctx.volume().ravel()), g["sofocc_grf32"])
+    assert n == int(g["sofsize_grf32"][0])
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_encoded_volumes_decode_like_the_oracle(gpu_ctx, seed):
+    # sizes past 16 per axis: empty nodes above the walker's subtrees, and
+    # subtrees of every depth
+    from voxel_ma_gb300 import api, volumes
+    rng = np.random.default_rng(seed)
+    shape = tuple(int(v) for v in rng.integers(20, 140, size=3))
+    occ = volumes.csg(100 + seed, 20, 140)
+    occ = occ[: shape[0], : shape[1], : shape[2]]
+    data = api.encode_sof(occ)
+    occ_ref, sites_ref = O.sof_decode(data)
+    n = gpu_ctx.set_volume_sof(data)
+    assert (n, n, n) == occ_ref.shape
+    assert np.array_equal(gpu_ctx.volume(), occ_ref)
+    assert np.array_equal(gpu_ctx.volume()[: occ.shape[0], : occ.shape[1], : occ.shape[2]], occ > 0)
+    assert gpu_ctx.extract_sites() == len(sites_ref)
+    assert np.array_equal(gpu_ctx.sites(), np.asarray(sites_ref, np.float32))

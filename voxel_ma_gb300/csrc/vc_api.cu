@@ -51,7 +51,7 @@ int vc_set_volume(vc_ctx* c, const uint8_t* occ, int X, int Y, int Z, int mem) {
     c->n_sites = -1;
     c->ft_valid = c->vd_valid = false;
     c->sites_from_octree = false;
-    c->oct_sites.clear();
+    c->oct_n_sites = 0;
     return VC_OK;
 }
 
@@ -271,7 +271,7 @@ int vc_batch_set_volumes(vc_ctx* c, int nvol, const int32_t* dims, const uint8_t
     c->n_sites = -1;
     c->ft_valid = c->vd_valid = false;
     c->sites_from_octree = false;
-    c->oct_sites.clear();
+    c->oct_n_sites = 0;
     return VC_OK;
 }
 

@@ -203,8 +203,9 @@ struct vc_ctx {
     vc::DevBuf occ;  // uint8, all voxels of all volumes
     // an octree (.sof) volume: its mixed leaves give the sites (vc_set_volume_sof)
     bool sites_from_octree = false;
-    std::vector<int4> oct_sites;        // mixed leaves (x, y, z, -) in stream order
-    vc::DevBuf oct_cells, oct_nodes;    // decode scratch: corner byte per cell; node / leaf lists
+    int64_t oct_n_sites = 0;            // mixed leaves of the installed octree
+    vc::DevBuf oct_leaves;              // those leaves (packed x, y, z) in stream order
+    vc::DevBuf oct_stream, oct_cells, oct_nodes;  // decode scratch: the stream; corner byte per cell; node lists
     // sites
     int64_t n_sites = -1;
     vc::DevBuf site_xyz;    // float3 per site

@@ -8,15 +8,19 @@
 // pre-order: a type byte -- 0 internal (eight children, x outermost, z
 // innermost), 1 empty (a sign byte: 1 outside, anything else inside, for
 // every cell of the cube), 2 leaf (one cell; bit 4x + 2y + z = corner
-// (x, y, z) outside).  The host walks the stream once (a few bytes per node)
-// into the list of terminal nodes -- they tile the R^3 cells -- and the list
-// of leaves whose corners differ; the GPU writes every cell's corner byte
-// (one thread per small node, one block per large one), then every voxel of
-// the (R + 1)^3 grid reads its cell as OctreeVolume::getDataAt does
-// (src/octree.cpp:233-256): its own cell's lowest corner, or, at a
-// coordinate R, the last cell's far corner.  The sites are the centres of
-// the mixed leaves in stream order (the order of the reference's tree walk).
+// (x, y, z) outside).  The host walks the nodes larger than 16^3 and skips
+// over each subtree of edge <= 16 (one pass over the type bytes, which only
+// counts open children), recording its root and first byte.  The stream goes
+// to the device once; one thread per subtree walks it (vc_octree_walk.cuh),
+// writing every cell's corner byte and counting its mixed leaves, and after
+// a prefix over the counts a second walk writes the mixed leaves -- the
+// sites, in stream order (the order of the reference's tree walk).  Larger
+// empty nodes are one block each.  Every voxel of the (R + 1)^3 grid then
+// reads its cell as OctreeVolume::getDataAt does (src/octree.cpp:233-256):
+// its own cell's lowest corner, or, at a coordinate R, the last cell's far
+// corner.
 #include "vc_internal.cuh"
+#include "vc_octree_walk.cuh"
 
 #include <cstring>
 #include <thread>
@@ -24,36 +28,35 @@
 namespace vc {
 namespace {
 
-constexpr int kSmallNode = 4;  // nodes up to 4^3 cells: one thread each
-
-// node: {x, y, z, len | sign byte << 24}
-__global__ void oct_small_kernel(const int4* __restrict__ nodes, int64_t n, uint8_t* __restrict__ cell, int R) {
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const int4 nd = __ldg(nodes + i);
-        const int len = nd.w & 0xffffff;
-        const uint8_t v = (uint8_t)((uint32_t)nd.w >> 24);
-        for (int a = 0; a < len; ++a)
-            for (int b = 0; b < len; ++b) {
-                uint8_t* row = cell + ((int64_t)(nd.x + a) * R + (nd.y + b)) * R + nd.z;
-                for (int c = 0; c < len; ++c) row[c] = v;
-            }
+__global__ void oct_large_kernel(const uint64_t* __restrict__ nodes, int64_t n, uint8_t* __restrict__ cell, int R) {
+    for (int64_t i = blockIdx.x; i < n; i += gridDim.x) {
+        const uint64_t nd = __ldg(nodes + i);
+        const int len = 1 << oct_lg(nd), x = oct_x(nd), y = oct_y(nd), z = oct_z(nd);
+        const uint8_t v = oct_v(nd);
+        const int64_t cells = (int64_t)len * len * len;
+        for (int64_t k = threadIdx.x; k < cells; k += blockDim.x) {
+            const int cz = (int)(k % len);
+            const int64_t ab = k / len;
+            const int b = (int)(ab % len), a = (int)(ab / len);
+            cell[((int64_t)(x + a) * R + (y + b)) * R + z + cz] = v;
+        }
     }
 }
 
-__global__ void oct_large_kernel(const int4* __restrict__ nodes, int64_t n, uint8_t* __restrict__ cell, int R) {
-    for (int64_t i = blockIdx.x; i < n; i += gridDim.x) {
-        const int4 nd = __ldg(nodes + i);
-        const int len = nd.w & 0xffffff;
-        const uint8_t v = (uint8_t)((uint32_t)nd.w >> 24);
-        const int64_t cells = (int64_t)len * len * len;
-        for (int64_t k = threadIdx.x; k < cells; k += blockDim.x) {
-            const int c = (int)(k % len);
-            const int64_t ab = k / len;
-            const int b = (int)(ab % len), a = (int)(ab / len);
-            cell[((int64_t)(nd.x + a) * R + (nd.y + b)) * R + nd.z + c] = v;
-        }
+// one thread per subtree; FILL: cells + mixed-leaf counts, else the leaves
+template <bool FILL>
+__global__ void oct_walk_kernel(const uint8_t* __restrict__ b, int64_t nbytes, const uint64_t* __restrict__ sub_node,
+                                const int64_t* __restrict__ sub_pos, int64_t nsub, uint8_t* __restrict__ cell, int R,
+                                int32_t* __restrict__ cnt, const int64_t* __restrict__ base,
+                                uint64_t* __restrict__ leaves, int* err) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nsub) return;
+    int64_t n = 0;
+    if (oct_walk<FILL>(b, nbytes, sub_pos[i], sub_node[i], cell, R, FILL ? nullptr : leaves + base[i], &n) != 0) {
+        set_error(err, VC_ERR_ARG);
+        return;
     }
+    if (FILL) cnt[i] = (int32_t)n;  // a subtree holds at most 16^3 leaves
 }
 
 // voxel (x, y, z) of the (R + 1)^3 grid: inside iff its corner bit is 0
@@ -72,16 +75,17 @@ __global__ void oct_voxels_kernel(const uint8_t* __restrict__ cell, int R, uint8
 }
 
 // the octree sites: centre of mixed leaf (x, y, z) = lattice point (x+1, y+1, z+1)
-__global__ void oct_sites_kernel(const int4* __restrict__ leaves, int64_t n, int S, float* __restrict__ xyz,
+__global__ void oct_sites_kernel(const uint64_t* __restrict__ leaves, int64_t n, int S, float* __restrict__ xyz,
                                  int32_t* __restrict__ site_id_lat) {
     const int64_t L = (int64_t)S + 1;  // lattice points per axis
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const int4 p = __ldg(leaves + i);
-        xyz[3 * i + 0] = (float)p.x + 0.5f;
-        xyz[3 * i + 1] = (float)p.y + 0.5f;
-        xyz[3 * i + 2] = (float)p.z + 0.5f;
-        site_id_lat[((int64_t)(p.x + 1) * L + (p.y + 1)) * L + (p.z + 1)] = (int32_t)i;
+        const uint64_t p = __ldg(leaves + i);
+        const int x = oct_x(p), y = oct_y(p), z = oct_z(p);
+        xyz[3 * i + 0] = (float)x + 0.5f;
+        xyz[3 * i + 1] = (float)y + 0.5f;
+        xyz[3 * i + 2] = (float)z + 0.5f;
+        site_id_lat[((int64_t)(x + 1) * L + (y + 1)) * L + (z + 1)] = (int32_t)i;
     }
 }
 
@@ -89,54 +93,57 @@ inline int grid_of(vc_ctx* c, int64_t n, int threads) {
     return (int)std::max<int64_t>(1, std::min<int64_t>((n + threads - 1) / threads, (int64_t)c->num_sms * 16));
 }
 
-// Walk the node stream: terminal nodes by size, mixed leaves in order.
-int parse_sof(const uint8_t* b, int64_t nbytes, int& R, std::vector<int4>& small, std::vector<int4>& large,
-              std::vector<int4>& mixed) {
+// Walk the nodes of edge > 16: the subtrees of edge <= 16 (root, first
+// byte), in stream order, and the empty nodes above them.
+int split_sof(const uint8_t* b, int64_t nbytes, int& R, std::vector<uint64_t>& sub_node,
+              std::vector<int64_t>& sub_pos, std::vector<uint64_t>& large) {
     if (nbytes < 4) return VC_ERR_ARG;
     int32_t r = 0;
     std::memcpy(&r, b, 4);
     if (r < 1 || (r & (r - 1)) != 0 || r > 16384) return VC_ERR_ARG;
     R = r;
+    int lgR = 0;
+    while ((1 << lgR) < R) ++lgR;
     struct Frame {
-        int x, y, z, len, child;
+        int x, y, z, lg, child;
     };
     std::vector<Frame> stack;
     int64_t pos = 4;
-    // read one node at (x, y, z, len); internal nodes are pushed
-    auto visit = [&](int x, int y, int z, int len) -> int {
+    auto visit = [&](int x, int y, int z, int lg) -> int {
+        if (lg <= kOctSubLg) {
+            sub_node.push_back(oct_pack(x, y, z, lg, 0));
+            sub_pos.push_back(pos);
+            // skip it: each node is one token, an internal one opens eight more
+            int64_t open = 1;
+            while (open > 0) {
+                if (pos >= nbytes) return VC_ERR_ARG;
+                const uint8_t t = b[pos];
+                if (t > 2) return VC_ERR_ARG;
+                pos += 1 + (t != 0);
+                open += t == 0 ? 7 : -1;
+            }
+            return pos > nbytes ? VC_ERR_ARG : VC_OK;
+        }
         if (pos >= nbytes) return VC_ERR_ARG;
         const uint8_t type = b[pos++];
         if (type == 0) {
-            if (len < 2) return VC_ERR_ARG;
-            stack.push_back(Frame{x, y, z, len, 0});
+            stack.push_back(Frame{x, y, z, lg, 0});
             return VC_OK;
         }
-        if (type != 1 && type != 2) return VC_ERR_ARG;
-        if (pos >= nbytes) return VC_ERR_ARG;
-        const uint8_t raw = b[pos++];
-        uint8_t v;
-        if (type == 2) {  // a leaf is one cell
-            if (len != 1) return VC_ERR_ARG;
-            v = raw;
-            if (v != 0x00 && v != 0xff) mixed.push_back(make_int4(x, y, z, 0));
-        } else {
-            v = raw == 1 ? 0xff : 0x00;
-        }
-        const int4 nd = make_int4(x, y, z, len | ((int)v << 24));
-        (len <= kSmallNode ? small : large).push_back(nd);
+        if (type != 1 || pos >= nbytes) return VC_ERR_ARG;  // a leaf is one cell
+        large.push_back(oct_pack(x, y, z, lg, b[pos++] == 1 ? 0xff : 0x00));
         return VC_OK;
     };
-    VC_TRY(visit(0, 0, 0, R));
+    VC_TRY(visit(0, 0, 0, lgR));
     while (!stack.empty()) {
         Frame& f = stack.back();
         if (f.child == 8) {
             stack.pop_back();
             continue;
         }
-        const int h = f.len / 2, i = f.child >> 2, j = (f.child >> 1) & 1, k = f.child & 1;
-        ++f.child;
+        const int h = 1 << (f.lg - 1), ch = f.child++;
         const Frame cur = f;  // visit() may grow the stack
-        VC_TRY(visit(cur.x + i * h, cur.y + j * h, cur.z + k * h, h));
+        VC_TRY(visit(cur.x + (ch >> 2) * h, cur.y + ((ch >> 1) & 1) * h, cur.z + (ch & 1) * h, cur.lg - 1));
     }
     return VC_OK;
 }
@@ -145,31 +152,65 @@ int parse_sof(const uint8_t* b, int64_t nbytes, int& R, std::vector<int4>& small
 
 int install_octree(vc_ctx* c, const uint8_t* bytes, int64_t nbytes, int* size_out) {
     int R = 0;
-    std::vector<int4> small, large, mixed;
-    VC_TRY(parse_sof(bytes, nbytes, R, small, large, mixed));
+    std::vector<uint64_t> sub_node, large;
+    std::vector<int64_t> sub_pos;
+    VC_TRY(split_sof(bytes, nbytes, R, sub_node, sub_pos, large));
     const int S = R + 1;
     if ((int64_t)(S + 1) * (S + 1) * (S + 1) >= ((int64_t)1 << 33) || S > 32766) return VC_ERR_ARG;
     const int64_t ncell = (int64_t)R * R * R, nvox = (int64_t)S * S * S;
+    const int64_t nsub = (int64_t)sub_node.size(), nlarge = (int64_t)large.size();
+    // node lists: sub roots | sub first bytes | leaf bases | large nodes | counts (int32)
+    VC_TRY(ensure_n<uint8_t>(c, c->oct_stream, nbytes));
     VC_TRY(ensure_n<uint8_t>(c, c->oct_cells, ncell));
-    VC_TRY(ensure_n<int4>(c, c->oct_nodes, (int64_t)(small.size() + large.size()) + 1));
-    VC_TRY(ensure_n<uint8_t>(c, c->occ, nvox));
-    int4* dn = ptr<int4>(c->oct_nodes);
+    VC_TRY(ensure_n<uint64_t>(c, c->oct_nodes, 3 * nsub + nlarge + (nsub + 1) / 2 + 1));
+    uint8_t* db = ptr<uint8_t>(c->oct_stream);
     uint8_t* cell = ptr<uint8_t>(c->oct_cells);
-    if (!small.empty())
-        VC_CUDA(c, cudaMemcpyAsync(dn, small.data(), small.size() * sizeof(int4), cudaMemcpyHostToDevice, c->stream));
-    if (!large.empty())
-        VC_CUDA(c, cudaMemcpyAsync(dn + small.size(), large.data(), large.size() * sizeof(int4),
-                                   cudaMemcpyHostToDevice, c->stream));
+    uint64_t* d_node = ptr<uint64_t>(c->oct_nodes);
+    int64_t* d_pos = reinterpret_cast<int64_t*>(d_node + nsub);
+    int64_t* d_base = d_pos + nsub;
+    uint64_t* d_large = reinterpret_cast<uint64_t*>(d_base + nsub);
+    int32_t* d_cnt = reinterpret_cast<int32_t*>(d_large + nlarge);
+    VC_CUDA(c, cudaMemcpyAsync(db, bytes, (size_t)nbytes, cudaMemcpyHostToDevice, c->stream));
+    if (nsub) {
+        VC_CUDA(c, cudaMemcpyAsync(d_node, sub_node.data(), nsub * sizeof(uint64_t), cudaMemcpyHostToDevice,
+                                   c->stream));
+        VC_CUDA(c, cudaMemcpyAsync(d_pos, sub_pos.data(), nsub * sizeof(int64_t), cudaMemcpyHostToDevice, c->stream));
+    }
+    if (nlarge)
+        VC_CUDA(c, cudaMemcpyAsync(d_large, large.data(), nlarge * sizeof(uint64_t), cudaMemcpyHostToDevice,
+                                   c->stream));
+    std::vector<int32_t> cnt((size_t)nsub);
     {
         Region r(c, "octree_decode");
-        if (!small.empty()) {
-            oct_small_kernel<<<grid_of(c, (int64_t)small.size(), 256), 256, 0, c->stream>>>(
-                dn, (int64_t)small.size(), cell, R);
+        if (nlarge) {
+            oct_large_kernel<<<(int)std::min<int64_t>(nlarge, (int64_t)c->num_sms * 8), 256, 0, c->stream>>>(
+                d_large, nlarge, cell, R);
             launched(c);
         }
-        if (!large.empty()) {
-            oct_large_kernel<<<(int)std::min<int64_t>((int64_t)large.size(), (int64_t)c->num_sms * 8), 256, 0,
-                               c->stream>>>(dn + small.size(), (int64_t)large.size(), cell, R);
+        if (nsub) {  // none when the whole cube is one empty node
+            oct_walk_kernel<true><<<(int)((nsub + 127) / 128), 128, 0, c->stream>>>(
+                db, nbytes, d_node, d_pos, nsub, cell, R, d_cnt, nullptr, nullptr, dev_err(c));
+            launched(c);
+            VC_CUDA(c, cudaGetLastError());
+            VC_CUDA(c, cudaMemcpyAsync(cnt.data(), d_cnt, nsub * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
+        }
+    }
+    VC_TRY(sync_check(c));  // a malformed subtree stops here, before the installed volume changes
+    std::vector<int64_t> base((size_t)nsub);
+    int64_t nleaf = 0;
+    for (int64_t i = 0; i < nsub; ++i) {
+        base[i] = nleaf;
+        nleaf += cnt[i];
+    }
+    VC_TRY(ensure_n<uint64_t>(c, c->oct_leaves, nleaf + 1));
+    VC_TRY(ensure_n<uint8_t>(c, c->occ, nvox));
+    {
+        Region r(c, "octree_decode");
+        if (nleaf) {
+            VC_CUDA(c, cudaMemcpyAsync(d_base, base.data(), nsub * sizeof(int64_t), cudaMemcpyHostToDevice,
+                                       c->stream));
+            oct_walk_kernel<false><<<(int)((nsub + 127) / 128), 128, 0, c->stream>>>(
+                db, nbytes, d_node, d_pos, nsub, cell, R, nullptr, d_base, ptr<uint64_t>(c->oct_leaves), dev_err(c));
             launched(c);
         }
         oct_voxels_kernel<<<grid_of(c, nvox, 256), 256, 0, c->stream>>>(cell, R, ptr<uint8_t>(c->occ));
@@ -181,30 +222,27 @@ int install_octree(vc_ctx* c, const uint8_t* bytes, int64_t nbytes, int* size_ou
     c->X = c->Y = c->Z = S;
     c->n_sites = -1;
     c->ft_valid = c->vd_valid = false;
-    c->oct_sites = std::move(mixed);
+    c->oct_n_sites = nleaf;
     c->sites_from_octree = true;
     if (size_out) *size_out = S;
-    return sync_check(c);  // the host node lists go out of scope
+    return sync_check(c);  // the host lists go out of scope
 }
 
 // The octree rule for the sites (run_sites calls it for an octree volume):
 // the centres of the mixed leaves, in stream order; the packed occupancy
 // words are written as for a dense volume.
 int octree_sites(vc_ctx* c, uint32_t* bits, int32_t* cnt, int64_t nwords, int64_t* total, int64_t* n_out) {
-    const int64_t n = (int64_t)c->oct_sites.size();
+    const int64_t n = c->oct_n_sites;
     const int64_t nlat = c->h_off[kLat][c->nvol];
-    VC_TRY(ensure_n<int4>(c, c->oct_nodes, n + 1));
     VC_TRY(ensure_n<float>(c, c->site_xyz, 3 * n + 3));
-    int4* dl = ptr<int4>(c->oct_nodes);
-    if (n > 0)
-        VC_CUDA(c, cudaMemcpyAsync(dl, c->oct_sites.data(), n * sizeof(int4), cudaMemcpyHostToDevice, c->stream));
     // per-volume site bases: one volume, n sites
     VC_CUDA(c, cudaMemsetAsync(cnt, 0, (size_t)std::max<int64_t>(nwords, 1) * sizeof(int32_t), c->stream));
     VC_CUDA(c, cudaMemcpyAsync(total, &n, sizeof(int64_t), cudaMemcpyHostToDevice, c->stream));
     VC_TRY(fill_bases(c, kBSite, kVWord, cnt, total));
     VC_CUDA(c, cudaMemsetAsync(c->site_id_lat.p, 0xff, (size_t)nlat * sizeof(int32_t), c->stream));
     if (n > 0) {
-        oct_sites_kernel<<<grid_of(c, n, 256), 256, 0, c->stream>>>(dl, n, c->X, ptr<float>(c->site_xyz),
+        oct_sites_kernel<<<grid_of(c, n, 256), 256, 0, c->stream>>>(ptr<uint64_t>(c->oct_leaves), n, c->X,
+                                                                     ptr<float>(c->site_xyz),
                                                                      ptr<int32_t>(c->site_id_lat));
         launched(c);
     }
