@@ -367,6 +367,21 @@ def run_gpu(args):
                           "host wall time of one call"}
         ctx.run_plain(occ_dev, args.t)  # the context holds the workload's own thinning again
 
+    # ---- output formats (outside the timed regions): the remaining complex
+    # written as the reference's pipeline writes it after thinning
+    export = None
+    if not args.no_probe:
+        import tempfile
+        with tempfile.TemporaryDirectory() as td:
+            prefix = os.path.join(td, "grf512_thinned")
+            t0 = time.perf_counter()
+            ctx.write_remaining(prefix)
+            ex_ms = (time.perf_counter() - t0) * 1e3
+            sizes = {ext: os.path.getsize(prefix + ext) for ext in (".ply", ".r", ".ma")}
+        export = {"ms": ex_ms, "bytes": sizes, "MB_per_s": sum(sizes.values()) / ex_ms / 1e3,
+                  "note": "vc_write_remaining (.ply + .r + .ma) of the workload's remaining complex, "
+                          "host wall time of one call (device read-back included)"}
+
     # ---- octree input (outside the timed regions): the workload written as the
     # reference's .sof octree (host encoder), then decoded on the GPU
     octree = None
@@ -440,6 +455,7 @@ def run_gpu(args):
         "roofline": roof,
         "closed_components": closed,
         "octree": octree,
+        "export": export,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nvox, "d2h_bytes_per_step": d2h,
                 "ms_per_step": e2e_ms / args.steps, "wall_s": wall_e2e},
         "gpu_launches": launches,

@@ -157,6 +157,37 @@ typedef struct {
 int vc_remaining(vc_ctx* ctx, vc_rem_sizes* sizes);
 int vc_get_remaining(vc_ctx* ctx, float* vts, int32_t* edges, int32_t* tris, int mem);
 
+/* ---- output formats -----------------------------------------------------
+ * The files the reference writes for the remaining complex after thinning at
+ * one threshold (src/highlevelalgo.cpp:855-955), byte for byte:
+ *   vc_write_ply    replaces writeToPLY (src/exporters.cpp:341-476) and
+ *                   ply::PLYWriter::write (src/plyall.cpp:98-171): ASCII PLY,
+ *                   vertex x y z, edge vertex1 vertex2, face vertex_indices.
+ *   vc_write_radii  replaces writeRadiiToFile (src/exporters.cpp:478-552)
+ *                   with the remaining vertex ids and the identity
+ *                   voxel-to-model matrix: "n", then "x y z r" per vertex.
+ *   vc_write_dotma  replaces writeToDotma (src/exporters.cpp:244-287).
+ * Host arrays; VC_ERR_ARG when the file cannot be written.
+ * vc_write_remaining writes <prefix>.ply / .r / .ma (VC_WRITE_* bits) from
+ * the context's remaining complex (vc_remaining); the radii need the lattice
+ * complex of one volume (vc_lattice_vd), else VC_ERR_STATE.  The .ma edge
+ * list is the caller's (src/highlevelalgo.cpp:911-945): the remaining
+ * edges, then the remaining triangles' edges in the order of its
+ * unordered_set<ivec2, ivec2Hash>.                                          */
+#define VC_WRITE_PLY 1
+#define VC_WRITE_RADII 2
+#define VC_WRITE_MA 4
+int vc_write_ply(const char* path, const float* vts, int64_t nv, const int32_t* edges, int64_t ne,
+                 const int32_t* tris, int64_t nt);
+int vc_write_radii(const char* path, const float* vts, const float* radii, int64_t n);
+int vc_write_dotma(const char* path, const float* vts, const float* radii, int64_t nv, const int32_t* edges,
+                   int64_t ne, const int32_t* tris, int64_t nt);
+int vc_write_remaining(vc_ctx* ctx, const char* prefix, int what);
+/* The .ma edge list vc_write_remaining writes, for given remaining edges and
+ * triangles (ne_out pairs; out may be NULL to size it, cap in pairs).       */
+int vc_dotma_edges(const int32_t* edges, int64_t ne, const int32_t* tris, int64_t nt, int32_t* out, int64_t cap,
+                   int64_t* ne_out);
+
 /* ---- topology of the remaining complex ----------------------------------
  * util::computeEulerChar(vts, edges, tris, eulerchar&)
  * (src/geomalgo.cpp:181-214) on the remainingCC output.                    */

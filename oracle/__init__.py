@@ -74,6 +74,13 @@ def lib():
         L.vco_sof_decode.argtypes = [c_vp, c_i64, c_vp, c_vp, c_vp, c_vp]
         L.vco_closed_components.restype = c_i64
         L.vco_closed_components.argtypes = [c_i64, c_i64, c_vp, c_i64, c_vp]
+        for name, args in (("vco_write_dotma", [ctypes.c_char_p, c_vp, c_vp, c_i64, c_vp, c_i64, c_vp, c_i64]),
+                           ("vco_write_radii", [ctypes.c_char_p, c_vp, c_vp, c_i64]),
+                           ("vco_write_ply", [ctypes.c_char_p, c_vp, c_i64, c_vp, c_i64, c_vp, c_i64])):
+            getattr(L, name).restype = ctypes.c_int
+            getattr(L, name).argtypes = args
+        L.vco_dotma_edges.restype = c_i64
+        L.vco_dotma_edges.argtypes = [c_vp, c_i64, c_vp, c_i64, c_vp]
         _LIB = L
     return _LIB
 
@@ -108,6 +115,10 @@ def ref():
         R.vcref_cc_adj_size.argtypes = [c_vp, ctypes.c_int]
         R.vcref_cc_get_adj.argtypes = [c_vp, ctypes.c_int, c_vp, c_vp]
         R.vcref_sof_write.restype = ctypes.c_int
+        R.vcref_write_dotma.restype = ctypes.c_int
+        R.vcref_write_dotma.argtypes = [ctypes.c_char_p, c_vp, c_vp, c_i64, c_vp, c_i64, c_vp, c_i64]
+        R.vcref_dotma_edges.restype = c_i64
+        R.vcref_dotma_edges.argtypes = [c_vp, c_i64, c_vp, c_i64, c_vp]
         R.vcref_sof_write.argtypes = [c_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_char_p]
         R.vcref_sof_occupancy.restype = ctypes.c_int
         R.vcref_sof_occupancy.argtypes = [ctypes.c_char_p, c_vp]
@@ -365,3 +376,55 @@ def ref_euler(vts, edges, tris):
     out = np.zeros(5, np.int32)
     ref().vcref_euler(len(vts), _ptr(vts), len(edges), _ptr(edges), len(tris), _ptr(tris), _ptr(out))
     return dict(V=int(out[0]), E=int(out[1]), F=int(out[2]), C=int(out[3]), euler=int(out[4]))
+
+
+# ---- output formats (highlevelalgo.cpp:855-955) ------------------------------
+
+def _c(a, dtype, cols):
+    a = np.ascontiguousarray(np.asarray(a, dtype).reshape(-1, cols) if cols else np.asarray(a, dtype).ravel())
+    return a, _ptr(a)
+
+
+def write_dotma(path: str, vts, radii, edges, tris) -> None:
+    """writeToDotma (exporters.cpp:244-287), restated on std::ofstream."""
+    (v, pv), (r, pr), (e, pe), (t, pt) = (_c(vts, np.float32, 3), _c(radii, np.float32, 0),
+                                          _c(edges, np.int32, 2), _c(tris, np.int32, 3))
+    assert lib().vco_write_dotma(os.fsencode(path), pv, pr, len(v), pe, len(e), pt, len(t)) == 0
+
+
+def write_radii(path: str, vts, radii) -> None:
+    """writeRadiiToFile (exporters.cpp:478-552) for remaining vertices, identity matrix."""
+    (v, pv), (r, pr) = _c(vts, np.float32, 3), _c(radii, np.float32, 0)
+    assert lib().vco_write_radii(os.fsencode(path), pv, pr, len(v)) == 0
+
+
+def write_ply(path: str, vts, edges, tris) -> None:
+    """ply::PLYWriter::write (plyall.cpp:98-171) with the ply library's ASCII writer."""
+    (v, pv), (e, pe), (t, pt) = _c(vts, np.float32, 3), _c(edges, np.int32, 2), _c(tris, np.int32, 3)
+    assert lib().vco_write_ply(os.fsencode(path), pv, len(v), pe, len(e), pt, len(t)) == 0
+
+
+def _edges_via(fn, edges, tris):
+    (e, pe), (t, pt) = _c(edges, np.int32, 2), _c(tris, np.int32, 3)
+    n = fn(pe, len(e), pt, len(t), None)
+    out = np.zeros((n, 2), np.int32)
+    fn(pe, len(e), pt, len(t), _ptr(out))
+    return out
+
+
+def dotma_edges(edges, tris) -> np.ndarray:
+    """The .ma edge list of highlevelalgo.cpp:911-945 (remaining edges, then the
+    triangles' edges in the order of an unordered_set with ivec2Hash)."""
+    return _edges_via(lib().vco_dotma_edges, edges, tris)
+
+
+def ref_write_dotma(path: str, vts, radii, edges, tris) -> None:
+    """The reference's own writeToDotma."""
+    (v, pv), (r, pr), (e, pe), (t, pt) = (_c(vts, np.float32, 3), _c(radii, np.float32, 0),
+                                          _c(edges, np.int32, 2), _c(tris, np.int32, 3))
+    assert ref().vcref_write_dotma(os.fsencode(path), pv, pr, len(v), pe, len(e), pt, len(t)) == 0
+
+
+def ref_dotma_edges(edges, tris) -> np.ndarray:
+    """The .ma edge assembly on the reference's own ivec2 / ivec2Hash."""
+    return _edges_via(ref().vcref_dotma_edges, edges, tris)

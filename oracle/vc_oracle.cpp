@@ -890,3 +890,112 @@ int vco_sof_decode(const uint8_t* b, long long nbytes, int* size_out, uint8_t* o
                 }
     return 0;
 }
+
+// ---------------------------------------------------------------------------
+// Output formats: the files written for the remaining complex after thinning
+// (highlevelalgo.cpp:855-955).  Written with the same stream facilities the
+// reference uses (std::ofstream with its default formatting, or stdio for the
+// ply library), one value at a time.
+
+#include <fstream>
+
+// writeToDotma (exporters.cpp:244-287)
+extern "C" int vco_write_dotma(const char* path, const float* vts, const float* radii, long long nv,
+                               const int32_t* edges, long long ne, const int32_t* tris, long long nt) {
+    std::ofstream f(path);
+    if (!f.is_open()) return 1;
+    f << (unsigned long)nv << " " << (unsigned long)ne << " " << (unsigned long)nt << std::endl;
+    for (long long k = 0; k < nv; ++k)
+        f << "v " << vts[3 * k] << " " << vts[3 * k + 1] << " " << vts[3 * k + 2] << " " << radii[k] << std::endl;
+    for (long long k = 0; k < ne; ++k) f << "e " << edges[2 * k] << " " << edges[2 * k + 1] << std::endl;
+    for (long long k = 0; k < nt; ++k)
+        f << "f " << (unsigned)tris[3 * k] << " " << (unsigned)tris[3 * k + 1] << " " << (unsigned)tris[3 * k + 2]
+          << std::endl;
+    return f.good() ? 0 : 1;
+}
+
+// writeRadiiToFile (exporters.cpp:478-552), the branch with the remaining
+// vertex ids, identity voxel-to-model matrix: r = len((r, 0, 0))
+extern "C" int vco_write_radii(const char* path, const float* vts, const float* radii, long long n) {
+    std::ofstream f(path);
+    if (!f.is_open()) return 1;
+    f << (unsigned long)n << std::endl;
+    for (long long k = 0; k < n; ++k) {
+        float r = radii[k];
+        r = std::sqrt(r * r + 0.0f * 0.0f + 0.0f * 0.0f);
+        f << vts[3 * k] << " " << vts[3 * k + 1] << " " << vts[3 * k + 2] << " " << r << std::endl;
+    }
+    return f.good() ? 0 : 1;
+}
+
+// ply::PLYWriter::write (plyall.cpp:98-171) through the ply library's ASCII
+// writer (Greg Turk's ply.c, 1998 revision: the reference's 3rdparty/ply
+// submodule, not vendored): header_complete_ply, then put_element_ply per
+// element -- write_ascii_item prints "%g " for floats, "%d " for ints, "%u "
+// for the uchar list count, and each element ends with "\n".
+extern "C" int vco_write_ply(const char* path, const float* vts, long long nv, const int32_t* edges, long long ne,
+                             const int32_t* tris, long long nt) {
+    FILE* f = std::fopen(path, "w");
+    if (!f) return 1;
+    std::fprintf(f, "ply\nformat ascii 1.0\ncomment Generated by VoxelCore\n");
+    std::fprintf(f, "element vertex %lld\n", nv);
+    for (const char* p : {"x", "y", "z"}) std::fprintf(f, "property float32 %s\n", p);
+    std::fprintf(f, "element edge %lld\n", ne);
+    for (const char* p : {"vertex1", "vertex2"}) std::fprintf(f, "property int32 %s\n", p);
+    std::fprintf(f, "element face %lld\n", nt);
+    std::fprintf(f, "property list uint8 int32 vertex_indices\n");
+    std::fprintf(f, "end_header\n");
+    for (long long k = 0; k < nv; ++k) {
+        for (int d = 0; d < 3; ++d) std::fprintf(f, "%g ", (double)vts[3 * k + d]);
+        std::fprintf(f, "\n");
+    }
+    for (long long k = 0; k < ne; ++k) {
+        for (int d = 0; d < 2; ++d) std::fprintf(f, "%d ", edges[2 * k + d]);
+        std::fprintf(f, "\n");
+    }
+    for (long long k = 0; k < nt; ++k) {
+        std::fprintf(f, "%u ", 3u);
+        for (int d = 0; d < 3; ++d) std::fprintf(f, "%d ", tris[3 * k + d]);
+        std::fprintf(f, "\n");
+    }
+    return std::fclose(f) == 0 ? 0 : 1;
+}
+
+// The .ma edge list (highlevelalgo.cpp:911-945): the remaining edges, then
+// each remaining triangle's edges (util::makeEdgesFromTri: (t0,t1), (t1,t2),
+// (t2,t0), each as (min, max)) through an unordered_set with ivec2Hash
+// (commondefs.h:30-43), appended in the set's iteration order.  Returns the
+// number of edges; out (2 ints per edge) may be null.
+namespace {
+struct OEdge {
+    int a, b;
+    bool operator==(const OEdge& o) const { return a == o.a && b == o.b; }
+};
+struct OEdgeHash {
+    size_t operator()(const OEdge& e) const {
+        size_t h = 0;
+        h = ((h << 5) - h) + std::hash<int>()(e.a);
+        h = ((h << 5) - h) + std::hash<int>()(e.b);
+        return h;
+    }
+};
+}  // namespace
+
+extern "C" long long vco_dotma_edges(const int32_t* edges, long long ne, const int32_t* tris, long long nt,
+                                     int32_t* out) {
+    std::vector<OEdge> all;
+    for (long long k = 0; k < ne; ++k) all.push_back(OEdge{edges[2 * k], edges[2 * k + 1]});
+    std::unordered_set<OEdge, OEdgeHash> unique;
+    for (long long k = 0; k < nt; ++k)
+        for (int d = 0; d < 3; ++d) {
+            const int i = tris[3 * k + d], j = tris[3 * k + (d + 1) % 3];
+            unique.insert(i > j ? OEdge{j, i} : OEdge{i, j});
+        }
+    all.insert(all.end(), unique.begin(), unique.end());
+    if (out)
+        for (size_t k = 0; k < all.size(); ++k) {
+            out[2 * k] = all[k].a;
+            out[2 * k + 1] = all[k].b;
+        }
+    return (long long)all.size();
+}

@@ -108,6 +108,14 @@ long long vco_closed_components(long long nv, long long ne, const int32_t* edges
 int vco_sof_decode(const uint8_t* bytes, long long nbytes, int* size_out, uint8_t* occ, float* sites,
                    long long* nsites);
 
+/* Output formats of the remaining complex (see vc_oracle.cpp). */
+int vco_write_dotma(const char* path, const float* vts, const float* radii, long long nv, const int32_t* edges,
+                    long long ne, const int32_t* tris, long long nt);
+int vco_write_radii(const char* path, const float* vts, const float* radii, long long n);
+int vco_write_ply(const char* path, const float* vts, long long nv, const int32_t* edges, long long ne,
+                  const int32_t* tris, long long nt);
+long long vco_dotma_edges(const int32_t* edges, long long ne, const int32_t* tris, long long nt, int32_t* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -14,6 +14,7 @@ LIB_PATH = os.path.join(HERE, "libvoxelcore_gb300.so")
 
 VC_OK, VC_ERR_ARG, VC_ERR_OOM, VC_ERR_TIMEOUT, VC_ERR_INVARIANT, VC_ERR_CUDA, VC_ERR_STATE = range(7)
 VC_MEM_HOST, VC_MEM_DEVICE = 0, 1
+VC_WRITE_PLY, VC_WRITE_RADII, VC_WRITE_MA = 1, 2, 4
 
 c_i64 = ctypes.c_int64
 c_vp = ctypes.c_void_p
@@ -116,6 +117,11 @@ SIGNATURES = {
     "vc_set_volume_sof": (c_int, [c_vp, c_vp, c_i64, ctypes.POINTER(c_int)]),
     "vc_get_volume": (c_int, [c_vp, c_vp, c_int]),
     "vc_encode_sof": (c_int, [c_vp, c_int, c_int, c_int, c_vp, c_i64, ctypes.POINTER(c_i64)]),
+    "vc_write_ply": (c_int, [ctypes.c_char_p, c_vp, c_i64, c_vp, c_i64, c_vp, c_i64]),
+    "vc_write_radii": (c_int, [ctypes.c_char_p, c_vp, c_vp, c_i64]),
+    "vc_write_dotma": (c_int, [ctypes.c_char_p, c_vp, c_vp, c_i64, c_vp, c_i64, c_vp, c_i64]),
+    "vc_dotma_edges": (c_int, [c_vp, c_i64, c_vp, c_i64, c_vp, c_i64, ctypes.POINTER(c_i64)]),
+    "vc_write_remaining": (c_int, [c_vp, ctypes.c_char_p, c_int]),
     "vc_debug_random_rate": (c_int, [c_vp, c_int, c_i64, ctypes.POINTER(ctypes.c_double)]),
     "vc_debug_thin_shape": (c_int, [c_vp, c_int, c_int, c_int]),
     "vc_autotune": (c_int, [c_vp, ctypes.c_double, ctypes.POINTER(TuneResult)]),

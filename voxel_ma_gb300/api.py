@@ -14,6 +14,7 @@ against the reference reads the same.
 from __future__ import annotations
 
 import ctypes
+import os
 from typing import Optional
 
 import numpy as np
@@ -320,6 +321,11 @@ class Context:
         (pv, mem), (pe, _), (pt, _) = _ptr_mem(vts), _ptr_mem(edges), _ptr_mem(tris)
         self.check(self.lib.vc_get_remaining(self.h, pv, pe, pt, mem), "vc_get_remaining")
 
+    def write_remaining(self, prefix: str, ply: bool = True, radii: bool = True, ma: bool = True) -> None:
+        """Write <prefix>.ply / .r / .ma for the remaining complex (vc_write_remaining)."""
+        what = (L.VC_WRITE_PLY if ply else 0) | (L.VC_WRITE_RADII if radii else 0) | (L.VC_WRITE_MA if ma else 0)
+        self.check(self.lib.vc_write_remaining(self.h, os.fsencode(prefix), what), "vc_write_remaining")
+
     def euler_remaining(self) -> dict:
         s = L.EulerInfo()
         self.check(self.lib.vc_euler_remaining(self.h, ctypes.byref(s)), "vc_euler_remaining")
@@ -488,6 +494,56 @@ def encode_sof(occ) -> bytes:
     if st != L.VC_OK:
         raise L.VoxelCoreError(st, "vc_encode_sof")
     return out.tobytes()
+
+
+def _call(name, *args):
+    st = getattr(L.load(), name)(*args)
+    if st != L.VC_OK:
+        raise L.VoxelCoreError(st, name)
+
+
+def _arr(a, dtype, cols):
+    a = np.ascontiguousarray(np.asarray(a, dtype).reshape(-1, cols) if cols else np.asarray(a, dtype).ravel())
+    return a, a.ctypes.data_as(ctypes.c_void_p)
+
+
+def write_ply(path: str, vts, edges, tris) -> None:
+    """writeToPLY: ASCII PLY of a complex (vc_write_ply)."""
+    v, pv = _arr(vts, np.float32, 3)
+    e, pe = _arr(edges, np.int32, 2)
+    t, pt = _arr(tris, np.int32, 3)
+    _call("vc_write_ply", os.fsencode(path), pv, len(v), pe, len(e), pt, len(t))
+
+
+def write_radii(path: str, vts, radii) -> None:
+    """writeRadiiToFile: "n", then "x y z r" per vertex (vc_write_radii)."""
+    v, pv = _arr(vts, np.float32, 3)
+    r, pr = _arr(radii, np.float32, 0)
+    if len(r) != len(v):
+        raise ValueError("one radius per vertex")
+    _call("vc_write_radii", os.fsencode(path), pv, pr, len(v))
+
+
+def write_dotma(path: str, vts, radii, edges, tris) -> None:
+    """writeToDotma: the .ma medial-axis file (vc_write_dotma)."""
+    v, pv = _arr(vts, np.float32, 3)
+    r, pr = _arr(radii, np.float32, 0)
+    e, pe = _arr(edges, np.int32, 2)
+    t, pt = _arr(tris, np.int32, 3)
+    if len(r) != len(v):
+        raise ValueError("one radius per vertex")
+    _call("vc_write_dotma", os.fsencode(path), pv, pr, len(v), pe, len(e), pt, len(t))
+
+
+def dotma_edges(edges, tris) -> np.ndarray:
+    """The .ma edge list for remaining edges and triangles (vc_dotma_edges)."""
+    e, pe = _arr(edges, np.int32, 2)
+    t, pt = _arr(tris, np.int32, 3)
+    n = ctypes.c_int64()
+    _call("vc_dotma_edges", pe, len(e), pt, len(t), None, 0, ctypes.byref(n))
+    out = np.zeros((n.value, 2), np.int32)
+    _call("vc_dotma_edges", pe, len(e), pt, len(t), out.ctypes.data_as(ctypes.c_void_p), n.value, ctypes.byref(n))
+    return out
 
 
 def plan_batches(voxels, t, share_bytes: int, bytes_per_voxel: float = 640.0, max_batch: int = 64) -> np.ndarray:
