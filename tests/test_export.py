@@ -23,7 +23,10 @@ def _complex(seed, nv=400, ne=120, nt=600, id_scale=1):
     radii = np.abs(rng.normal(3.0, 4.0, nv)).astype(np.float32)
     radii[:5] = [0.0, 0.5, 1e-3, 1234567.0, np.float32(np.sqrt(2.0))]
     edges = rng.integers(0, nv, size=(ne, 2)).astype(np.int32) * id_scale
-    tris = np.stack([rng.permutation(nv)[:3] for _ in range(nt)]).astype(np.int32) * id_scale
+    a = rng.integers(0, nv, nt)
+    d1 = rng.integers(1, nv - 1, nt)
+    d2 = d1 + rng.integers(1, nv - d1, nt)             # 0 < d1 < d2 < nv: three distinct ids
+    tris = (np.stack([a, (a + d1) % nv, (a + d2) % nv], 1) * id_scale).astype(np.int32)
     return vts, radii, edges, tris
 
 
@@ -85,3 +88,25 @@ def test_empty_complex_and_errors(tmp_path):
     assert ei.value.status == _lib.VC_ERR_ARG
     with pytest.raises(ValueError):
         api.write_radii(str(tmp_path / "x.r"), np.zeros((2, 3), np.float32), [1.0])
+
+
+def test_large_inputs_use_several_threads(tmp_path):
+    # enough lines and edges that the formatting and the edge de-duplication
+    # run on several threads; the bytes and the order must not change
+    vts, radii, edges, tris = _complex(9, nv=150_000, ne=20_000, nt=120_000)
+    got = api.dotma_edges(edges, tris)
+    assert np.array_equal(got, O.dotma_edges(edges, tris))
+    if O.ref_available():
+        assert np.array_equal(got, O.ref_dotma_edges(edges, tris))
+    for kind in ("ma", "ply", "r"):
+        a, b = str(tmp_path / f"a.{kind}"), str(tmp_path / f"b.{kind}")
+        if kind == "ma":
+            api.write_dotma(a, vts, radii, got, tris)
+            O.write_dotma(b, vts, radii, got, tris)
+        elif kind == "ply":
+            api.write_ply(a, vts, edges, tris)
+            O.write_ply(b, vts, edges, tris)
+        else:
+            api.write_radii(a, vts, radii)
+            O.write_radii(b, vts, radii)
+        assert open(a, "rb").read() == open(b, "rb").read(), kind

@@ -27,7 +27,8 @@
 #include <cmath>
 #include <cstdio>
 #include <string>
-#include <unordered_set>
+#include <bits/hashtable_policy.h>  // std::__detail::_Prime_rehash_policy, the set's growth rule
+#include <thread>
 
 namespace vc {
 namespace {
@@ -48,12 +49,46 @@ struct Text {
     void str(const char* t) { s.append(t); }
 };
 
-int write_file(const char* path, const std::string& s) {
+int worker_threads(size_t n, size_t per_thread) {
+    const size_t hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    return (int)std::max<size_t>(1, std::min(hw, n / per_thread + 1));
+}
+template <class F>
+void parallel_for(int nth, F&& f) {
+    if (nth <= 1) {
+        f(0);
+        return;
+    }
+    std::vector<std::thread> th;
+    for (int t = 0; t < nth; ++t) th.emplace_back([&f, t] { f(t); });
+    for (auto& x : th) x.join();
+}
+
+using Parts = std::vector<std::string>;
+
+int write_file(const char* path, const Parts& parts) {
     FILE* f = std::fopen(path, "wb");
     if (!f) return VC_ERR_ARG;
-    const size_t n = std::fwrite(s.data(), 1, s.size(), f);
+    bool ok = true;
+    for (const std::string& s : parts) ok = ok && std::fwrite(s.data(), 1, s.size(), f) == s.size();
     const int rc = std::fclose(f);
-    return (n == s.size() && rc == 0) ? VC_OK : VC_ERR_ARG;
+    return (ok && rc == 0) ? VC_OK : VC_ERR_ARG;
+}
+
+// lines [0, n) formatted by line(Text&, k), in chunks on worker threads,
+// appended to parts in order
+template <class F>
+void lines(Parts& parts, int64_t n, size_t bytes_per_line, F&& line) {
+    const int nth = worker_threads((size_t)n, 1 << 15);
+    const size_t first = parts.size();
+    parts.resize(first + nth);
+    parallel_for(nth, [&](int t) {
+        const int64_t k0 = n * t / nth, k1 = n * (t + 1) / nth;
+        Text x;
+        x.s.reserve((size_t)(k1 - k0) * bytes_per_line + 64);
+        for (int64_t k = k0; k < k1; ++k) line(x, k);
+        parts[first + t].swap(x.s);
+    });
 }
 
 // ivec2Hash (include/commondefs.h:30-43): h = h * 31 + std::hash<int>(x),
@@ -73,48 +108,46 @@ inline uint64_t edge_key(int a, int b) {  // util::makeEdge: (min, max)
 
 }  // namespace
 
-int format_ply(const float* vts, int64_t nv, const int32_t* edges, int64_t ne, const int32_t* tris, int64_t nt,
-               std::string& out) {
-    Text t;
-    t.s.reserve((size_t)(nv * 30 + ne * 16 + nt * 24 + 256));
-    t.str("ply\nformat ascii 1.0\ncomment Generated by VoxelCore\nelement vertex ");
-    t.i(nv);
-    t.str("\nproperty float32 x\nproperty float32 y\nproperty float32 z\nelement edge ");
-    t.i(ne);
-    t.str("\nproperty int32 vertex1\nproperty int32 vertex2\nelement face ");
-    t.i(nt);
-    t.str("\nproperty list uint8 int32 vertex_indices\nend_header\n");
-    for (int64_t k = 0; k < nv; ++k) {
+void format_ply(const float* vts, int64_t nv, const int32_t* edges, int64_t ne, const int32_t* tris, int64_t nt,
+                Parts& out) {
+    Text h;
+    h.str("ply\nformat ascii 1.0\ncomment Generated by VoxelCore\nelement vertex ");
+    h.i(nv);
+    h.str("\nproperty float32 x\nproperty float32 y\nproperty float32 z\nelement edge ");
+    h.i(ne);
+    h.str("\nproperty int32 vertex1\nproperty int32 vertex2\nelement face ");
+    h.i(nt);
+    h.str("\nproperty list uint8 int32 vertex_indices\nend_header\n");
+    out.push_back(std::move(h.s));
+    lines(out, nv, 32, [&](Text& t, int64_t k) {
         for (int d = 0; d < 3; ++d) {
             t.g(vts[3 * k + d]);
             t.c(' ');
         }
         t.c('\n');
-    }
-    for (int64_t k = 0; k < ne; ++k) {
+    });
+    lines(out, ne, 18, [&](Text& t, int64_t k) {
         t.i(edges[2 * k]);
         t.c(' ');
         t.i(edges[2 * k + 1]);
         t.str(" \n");
-    }
-    for (int64_t k = 0; k < nt; ++k) {
+    });
+    lines(out, nt, 28, [&](Text& t, int64_t k) {
         t.str("3 ");
         for (int d = 0; d < 3; ++d) {
             t.i(tris[3 * k + d]);
             t.c(' ');
         }
         t.c('\n');
-    }
-    out.swap(t.s);
-    return VC_OK;
+    });
 }
 
-int format_radii(const float* vts, const float* radii, int64_t n, std::string& out) {
-    Text t;
-    t.s.reserve((size_t)(n * 40 + 32));
-    t.i(n);
-    t.c('\n');
-    for (int64_t k = 0; k < n; ++k) {
+void format_radii(const float* vts, const float* radii, int64_t n, Parts& out) {
+    Text h;
+    h.i(n);
+    h.c('\n');
+    out.push_back(std::move(h.s));
+    lines(out, n, 40, [&](Text& t, int64_t k) {
         const float r = radii[k];
         for (int d = 0; d < 3; ++d) {
             t.g(vts[3 * k + d]);
@@ -122,22 +155,20 @@ int format_radii(const float* vts, const float* radii, int64_t n, std::string& o
         }
         t.g(std::sqrt(r * r));
         t.c('\n');
-    }
-    out.swap(t.s);
-    return VC_OK;
+    });
 }
 
-int format_dotma(const float* vts, const float* radii, int64_t nv, const int32_t* edges, int64_t ne,
-                 const int32_t* tris, int64_t nt, std::string& out) {
-    Text t;
-    t.s.reserve((size_t)(nv * 40 + ne * 16 + nt * 24 + 64));
-    t.i(nv);
-    t.c(' ');
-    t.i(ne);
-    t.c(' ');
-    t.i(nt);
-    t.c('\n');
-    for (int64_t k = 0; k < nv; ++k) {
+void format_dotma(const float* vts, const float* radii, int64_t nv, const int32_t* edges, int64_t ne,
+                  const int32_t* tris, int64_t nt, Parts& out) {
+    Text h;
+    h.i(nv);
+    h.c(' ');
+    h.i(ne);
+    h.c(' ');
+    h.i(nt);
+    h.c('\n');
+    out.push_back(std::move(h.s));
+    lines(out, nv, 42, [&](Text& t, int64_t k) {
         t.str("v ");
         for (int d = 0; d < 3; ++d) {
             t.g(vts[3 * k + d]);
@@ -145,35 +176,111 @@ int format_dotma(const float* vts, const float* radii, int64_t nv, const int32_t
         }
         t.g(radii[k]);
         t.c('\n');
-    }
-    for (int64_t k = 0; k < ne; ++k) {
+    });
+    lines(out, ne, 18, [&](Text& t, int64_t k) {
         t.str("e ");
         t.i(edges[2 * k]);
         t.c(' ');
         t.i(edges[2 * k + 1]);
         t.c('\n');
-    }
-    for (int64_t k = 0; k < nt; ++k) {
+    });
+    lines(out, nt, 28, [&](Text& t, int64_t k) {
         t.str("f ");
-        t.i((uint32_t)tris[3 * k]);
-        t.c(' ');
-        t.i((uint32_t)tris[3 * k + 1]);
-        t.c(' ');
-        t.i((uint32_t)tris[3 * k + 2]);
-        t.c('\n');
+        for (int d = 0; d < 3; ++d) {
+            t.i((uint32_t)tris[3 * k + d]);
+            t.c(d < 2 ? ' ' : '\n');
+        }
+    });
+}
+
+// Keys in first-insertion order.  Each thread owns a hash shard of the keys
+// and marks their first occurrences; a sequential pass keeps the marked ones.
+std::vector<uint64_t> first_occurrences(const std::vector<uint64_t>& ins) {
+    const size_t n = ins.size();
+    const int nth = worker_threads(n, 1 << 16);
+    std::vector<uint8_t> first(n, 0);
+    parallel_for(nth, [&](int t) {
+        size_t cap = 16;
+        while (cap < 2 * (n / nth) + 16) cap <<= 1;
+        std::vector<uint64_t> tab(cap, ~0ull);
+        for (size_t i = 0; i < n; ++i) {
+            const uint64_t k = ins[i], m = k * 0x9E3779B97F4A7C15ull;
+            if ((int)((m >> 59) % (uint64_t)nth) != t) continue;
+            size_t h = (m >> 7) & (cap - 1);
+            while (tab[h] != ~0ull && tab[h] != k) h = (h + 1) & (cap - 1);
+            if (tab[h] == ~0ull) {
+                tab[h] = k;
+                first[i] = 1;
+            }
+        }
+    });
+    std::vector<uint64_t> u;
+    u.reserve(n);
+    for (size_t i = 0; i < n; ++i)
+        if (first[i]) u.push_back(ins[i]);
+    return u;
+}
+
+// The iteration order of a std::unordered_set<key, EdgeHash> (libstdc++)
+// after inserting ins in order, replayed on arrays: every node goes to the
+// front of its bucket; a bucket that was empty goes to the front of the
+// list; a rehash (when the set's own _Prime_rehash_policy asks for one,
+// starting from one bucket) walks the list in order and re-inserts each node
+// the same way.  Equal to the set's order by construction; faster because no
+// node is allocated and the bucket heads are prefetched.
+std::vector<uint64_t> unordered_set_order(const std::vector<uint64_t>& ins) {
+    const std::vector<uint64_t> uniq = first_occurrences(ins);
+    const size_t n = uniq.size();
+    EdgeHash H;
+    std::vector<size_t> code(n);
+    for (size_t i = 0; i < n; ++i) code[i] = H(uniq[i]);
+    std::__detail::_Prime_rehash_policy pol;
+    size_t nb = 1;
+    std::vector<int32_t> head(1, -1), nxt(n, -1);
+    std::vector<uint32_t> order;  // buckets in the order they became non-empty (the list is its reverse)
+    auto rehash = [&](size_t nbn) {
+        std::vector<int32_t> nh(nbn, -1);
+        std::vector<uint32_t> nord;
+        nord.reserve(std::min(nbn, n));
+        for (size_t oi = order.size(); oi-- > 0;) {
+            if (oi >= 16) __builtin_prefetch(&head[order[oi - 16]]);
+            for (int32_t p = head[order[oi]]; p >= 0;) {
+                const int32_t q = nxt[p];
+                const size_t b = code[p] % nbn;
+                if (nh[b] < 0) nord.push_back((uint32_t)b);
+                nxt[p] = nh[b];
+                nh[b] = p;
+                p = q;
+            }
+        }
+        head.swap(nh);
+        order.swap(nord);
+        nb = nbn;
+    };
+    for (size_t i = 0; i < n; ++i) {
+        if (i + 24 < n) __builtin_prefetch(&head[code[i + 24] % nb]);
+        const auto r = pol._M_need_rehash(nb, i, 1);
+        if (r.first) rehash(r.second);
+        const size_t b = code[i] % nb;
+        if (head[b] < 0) order.push_back((uint32_t)b);
+        nxt[i] = head[b];
+        head[b] = (int32_t)i;
     }
-    out.swap(t.s);
-    return VC_OK;
+    std::vector<uint64_t> out;
+    out.reserve(n);
+    for (size_t oi = order.size(); oi-- > 0;)
+        for (int32_t p = head[order[oi]]; p >= 0; p = nxt[p]) out.push_back(uniq[p]);
+    return out;
 }
 
 // the caller's .ma edge list: remaining edges, then the triangles' edges in
 // the iteration order of a fresh unordered_set filled triangle by triangle
 void dotma_edges(const int32_t* edges, int64_t ne, const int32_t* tris, int64_t nt, std::vector<int32_t>& out) {
     out.assign(edges, edges + 2 * ne);
-    std::unordered_set<uint64_t, EdgeHash> unique;
+    std::vector<uint64_t> ins((size_t)(3 * nt));
     for (int64_t k = 0; k < nt; ++k)
-        for (int d = 0; d < 3; ++d) unique.insert(edge_key(tris[3 * k + d], tris[3 * k + (d + 1) % 3]));
-    for (const uint64_t e : unique) {
+        for (int d = 0; d < 3; ++d) ins[3 * k + d] = edge_key(tris[3 * k + d], tris[3 * k + (d + 1) % 3]);
+    for (const uint64_t e : unordered_set_order(ins)) {
         out.push_back((int32_t)(e >> 32));
         out.push_back((int32_t)(uint32_t)e);
     }
@@ -184,25 +291,25 @@ void dotma_edges(const int32_t* edges, int64_t ne, const int32_t* tris, int64_t 
 extern "C" int vc_write_ply(const char* path, const float* vts, int64_t nv, const int32_t* edges, int64_t ne,
                             const int32_t* tris, int64_t nt) {
     if (!path || nv < 0 || ne < 0 || nt < 0 || (nv && !vts) || (ne && !edges) || (nt && !tris)) return VC_ERR_ARG;
-    std::string s;
-    VC_TRY(vc::format_ply(vts, nv, edges, ne, tris, nt, s));
-    return vc::write_file(path, s);
+    vc::Parts parts;
+    vc::format_ply(vts, nv, edges, ne, tris, nt, parts);
+    return vc::write_file(path, parts);
 }
 
 extern "C" int vc_write_radii(const char* path, const float* vts, const float* radii, int64_t n) {
     if (!path || n < 0 || (n && (!vts || !radii))) return VC_ERR_ARG;
-    std::string s;
-    VC_TRY(vc::format_radii(vts, radii, n, s));
-    return vc::write_file(path, s);
+    vc::Parts parts;
+    vc::format_radii(vts, radii, n, parts);
+    return vc::write_file(path, parts);
 }
 
 extern "C" int vc_write_dotma(const char* path, const float* vts, const float* radii, int64_t nv,
                               const int32_t* edges, int64_t ne, const int32_t* tris, int64_t nt) {
     if (!path || nv < 0 || ne < 0 || nt < 0 || (nv && (!vts || !radii)) || (ne && !edges) || (nt && !tris))
         return VC_ERR_ARG;
-    std::string s;
-    VC_TRY(vc::format_dotma(vts, radii, nv, edges, ne, tris, nt, s));
-    return vc::write_file(path, s);
+    vc::Parts parts;
+    vc::format_dotma(vts, radii, nv, edges, ne, tris, nt, parts);
+    return vc::write_file(path, parts);
 }
 
 extern "C" int vc_dotma_edges(const int32_t* edges, int64_t ne, const int32_t* tris, int64_t nt, int32_t* out,
