@@ -72,6 +72,16 @@ int vc_set_volume(vc_ctx* ctx, const uint8_t* occ, int X, int Y, int Z, int mem)
  * corners differ, in the file's order.  VC_ERR_ARG for a malformed stream,
  * a resolution that is not a power of two, or a leaf above the cell level. */
 int vc_set_volume_sof(vc_ctx* ctx, const void* bytes, int64_t nbytes, int* size);
+/* The same from a .sog file (OctreeVolume::read_sog_file,
+ * src/octree.cpp:351-498): a 128-byte header opening with "SOG.Format 1.0"
+ * (VC_ERR_ARG otherwise), the lower-left corner and bounding-box length as
+ * floats, then R and the nodes, each leaf followed by its feature point
+ * (three floats, skipped).  The volume's voxel-to-model matrix becomes
+ * trans(lower-left) * scale(length / R), as the reference sets it.         */
+int vc_set_volume_sog(vc_ctx* ctx, const void* bytes, int64_t nbytes, int* size);
+/* The installed volume's voxel-to-model matrix (16 doubles, column-major as
+ * trimesh::xform): the identity except for .sog volumes.                   */
+int vc_get_vox_to_model(vc_ctx* ctx, double* m);
 /* The installed occupancy (all volumes of a batch, one after another).     */
 int vc_get_volume(vc_ctx* ctx, uint8_t* occ, int mem);
 /* The .sof stream of an X*Y*Z host occupancy volume (x-major, z fastest) as
@@ -80,6 +90,10 @@ int vc_get_volume(vc_ctx* ctx, uint8_t* occ, int mem);
  * context.  *nbytes = the stream's length; with out non-null and cap at
  * least that, the stream is copied to out.                                 */
 int vc_encode_sof(const uint8_t* occ, int X, int Y, int Z, uint8_t* out, int64_t cap, int64_t* nbytes);
+/* The .sog stream of the same octree (write_sog_file, src/octree.cpp:569-668):
+ * header (title, lower-left 0, length R; the header bytes the reference
+ * leaves uninitialised are zero), R, the nodes with each leaf's cell centre. */
+int vc_encode_sog(const uint8_t* occ, int X, int Y, int Z, uint8_t* out, int64_t cap, int64_t* nbytes);
 int vc_extract_sites(vc_ctx* ctx, int64_t* n_sites);
 int vc_get_sites(vc_ctx* ctx, float* xyz, int mem);
 

@@ -72,6 +72,8 @@ def lib():
         L.vco_euler.argtypes = [c_i64, c_i64, c_vp, c_i64, c_vp, c_vp]
         L.vco_sof_decode.restype = ctypes.c_int
         L.vco_sof_decode.argtypes = [c_vp, c_i64, c_vp, c_vp, c_vp, c_vp]
+        L.vco_sog_decode.restype = ctypes.c_int
+        L.vco_sog_decode.argtypes = [c_vp, c_i64, c_vp, c_vp, c_vp, c_vp]
         L.vco_closed_components.restype = c_i64
         L.vco_closed_components.argtypes = [c_i64, c_i64, c_vp, c_i64, c_vp]
         for name, args in (("vco_write_dotma", [ctypes.c_char_p, c_vp, c_vp, c_i64, c_vp, c_i64, c_vp, c_i64]),
@@ -226,17 +228,19 @@ def closed_components(nv: int, edges: np.ndarray, tris: np.ndarray) -> int:
     return int(lib().vco_closed_components(nv, len(edges), _ptr(edges), len(tris), _ptr(tris)))
 
 
-def sof_decode(data: bytes):
-    """A .sof octree file decoded as the reference reads it: (occupancy of the
-    (R+1)^3 voxels, the octree sites in pre-order); None when malformed."""
+def sof_decode(data: bytes, sog: bool = False):
+    """A .sof (or, with sog, .sog) octree file decoded as the reference reads
+    it: (occupancy of the (R+1)^3 voxels, the octree sites in pre-order);
+    None when malformed."""
+    fn = lib().vco_sog_decode if sog else lib().vco_sof_decode
     buf = np.frombuffer(data, dtype=np.uint8)
     size, ns = ctypes.c_int(), ctypes.c_longlong()
-    if lib().vco_sof_decode(_ptr(buf), len(buf), ctypes.byref(size), None, None, ctypes.byref(ns)) != 0:
+    if fn(_ptr(buf), len(buf), ctypes.byref(size), None, None, ctypes.byref(ns)) != 0:
         return None
     n = size.value
     occ = np.zeros((n, n, n), np.uint8)
     sites = np.zeros((ns.value, 3), np.float32)
-    lib().vco_sof_decode(_ptr(buf), len(buf), ctypes.byref(size), _ptr(occ), _ptr(sites), ctypes.byref(ns))
+    fn(_ptr(buf), len(buf), ctypes.byref(size), _ptr(occ), _ptr(sites), ctypes.byref(ns))
     return occ, sites
 
 

@@ -820,16 +820,19 @@ long long vco_closed_components(long long nv, long long ne, const int32_t* edges
     return ncc;
 }
 
-int vco_sof_decode(const uint8_t* b, long long nbytes, int* size_out, uint8_t* occ, float* sites,
-                   long long* nsites) {
-    if (nbytes < 4) return -1;
+// start: the byte of R (0 in .sof, 128 in .sog); leaf_extra: bytes after a
+// leaf's corner byte (0 in .sof, 12 in .sog: its feature point, read and
+// dropped by read_sog_file, octree.cpp:403-410)
+static int octree_decode(const uint8_t* b, long long nbytes, long long start, int leaf_extra, int* size_out,
+                         uint8_t* occ, float* sites, long long* nsites) {
+    if (nbytes < start + 4) return -1;
     int32_t R = 0;
-    std::memcpy(&R, b, 4);
+    std::memcpy(&R, b + start, 4);
     if (R < 1 || (R & (R - 1)) != 0 || R > 16384) return -1;
     const long long S = (long long)R + 1;
     std::vector<uint8_t> cell;
     if (occ) cell.assign((size_t)R * R * R, 0);
-    long long pos = 4, ns = 0;
+    long long pos = start + 4, ns = 0;
     bool ok = true;
     std::function<void(int, int, int, int)> node = [&](int x, int y, int z, int len) {
         if (!ok || pos >= nbytes) {
@@ -843,6 +846,11 @@ int vco_sof_decode(const uint8_t* b, long long nbytes, int* size_out, uint8_t* o
                 return;
             }
             const uint8_t v = b[pos++];
+            if (nbytes - pos < leaf_extra) {
+                ok = false;
+                return;
+            }
+            pos += leaf_extra;
             if (occ) cell[((size_t)x * R + y) * R + z] = v;
             if (v != 0x00 && v != 0xFF) {
                 if (sites) {
@@ -889,6 +897,20 @@ int vco_sof_decode(const uint8_t* b, long long nbytes, int* size_out, uint8_t* o
                     occ[(x * S + y) * S + z] = ((v >> off) & 1) == 0 ? 1 : 0;
                 }
     return 0;
+}
+
+int vco_sof_decode(const uint8_t* b, long long nbytes, int* size_out, uint8_t* occ, float* sites,
+                   long long* nsites) {
+    return octree_decode(b, nbytes, 0, 0, size_out, occ, sites, nsites);
+}
+
+// read_sog_file (octree.cpp:351-498): the 128-byte header (title "SOG.Format
+// 1.0" and its terminator, lower-left corner, bounding-box length), then R
+// and the nodes; a stream without the title is rejected
+int vco_sog_decode(const uint8_t* b, long long nbytes, int* size_out, uint8_t* occ, float* sites,
+                   long long* nsites) {
+    if (nbytes < 128 || std::memcmp(b, "SOG.Format 1.0", 15) != 0) return -1;
+    return octree_decode(b, nbytes, 128, 12, size_out, occ, sites, nsites);
 }
 
 // ---------------------------------------------------------------------------

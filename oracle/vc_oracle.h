@@ -107,6 +107,10 @@ long long vco_closed_components(long long nv, long long ne, const int32_t* edges
 // stream is malformed.
 int vco_sof_decode(const uint8_t* bytes, long long nbytes, int* size_out, uint8_t* occ, float* sites,
                    long long* nsites);
+/* The same for a .sog file (octree.cpp:351-498): 128-byte header, R, nodes
+ * with 12 bytes after each leaf's corner byte. */
+int vco_sog_decode(const uint8_t* bytes, long long nbytes, int* size_out, uint8_t* occ, float* sites,
+                   long long* nsites);
 
 /* Output formats of the remaining complex (see vc_oracle.cpp). */
 int vco_write_dotma(const char* path, const float* vts, const float* radii, long long nv, const int32_t* edges,

@@ -6,7 +6,9 @@ It builds oracle/_ref/libvcref.so (which includes the reference's octree.cpp)
 and records, for small seeded volumes:
   * the .sof file the reference writes for the volume (OctreeVolume built
     from the dense volume, then writeToFile);
-  * the reference's reading of that file: the occupancy of every voxel of
+  * the .sog file it writes for the same octree (write_sog_file), and its
+    reading of that file;
+  * the reference's reading of the .sof file: the occupancy of every voxel of
     its (R+1)^3 grid (SpaceConverter::get_occupancy_at_vox on the octree)
     and the sites of Surfacer::extractBoundaryVts on it (its octree branch),
     stored as lattice coordinates (site + 0.5).
@@ -53,6 +55,15 @@ def main():
             out[f"sofocc_{name}"] = np.packbits(occ_ref.ravel())
             out[f"sofsize_{name}"] = np.array([occ_ref.shape[0]], np.int32)
             out[f"sofsites_{name}"] = (sites_ref + 0.5).astype(np.int16)
+            # the same octree as .sog (write_sog_file / read_sog_file); bytes
+            # 31..127 of its header are left uninitialised by the reference
+            path = os.path.join(d, f"{name}.sog")
+            oracle.ref_sof_write(np.asarray(occ), path)
+            data = np.frombuffer(open(path, "rb").read(), np.uint8)
+            occ_ref, sites_ref = oracle.ref_sof_read(path)
+            out[f"sog_{name}"] = data
+            out[f"sogocc_{name}"] = np.packbits(occ_ref.ravel())
+            out[f"sogsites_{name}"] = (sites_ref + 0.5).astype(np.int16)
     np.savez_compressed(OUT, **out)
     print("wrote", OUT, len(out), "arrays")
 

@@ -104,3 +104,64 @@ def test_encoded_volumes_decode_like_the_oracle(gpu_ctx, seed):
     assert np.array_equal(gpu_ctx.volume()[: occ.shape[0], : occ.shape[1], : occ.shape[2]], occ > 0)
     assert gpu_ctx.extract_sites() == len(sites_ref)
     assert np.array_equal(gpu_ctx.sites(), np.asarray(sites_ref, np.float32))
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_sog_volume_and_sites_match_reference(gpu_ctx, sof_golden, name):
+    g = sof_golden
+    n = gpu_ctx.set_volume_sog(g[f"sog_{name}"].tobytes())
+    assert n == int(g[f"sofsize_{name}"][0])
+    assert np.array_equal(np.packbits(gpu_ctx.volume().ravel()), g[f"sogocc_{name}"])
+    assert gpu_ctx.extract_sites() == len(g[f"sogsites_{name}"])
+    assert np.array_equal(gpu_ctx.sites(), g[f"sogsites_{name}"].astype(np.float32) - 0.5)
+    assert np.array_equal(gpu_ctx.vox_to_model(), np.eye(4))  # lower-left 0, length R
+
+
+def _run_installed(ctx, t=0.04):
+    ctx.extract_sites()
+    ctx.feature_transform()
+    s = ctx.lattice_vd()
+    thr = float(np.float32(np.float64(s["inside_size"]) * t))
+    ctx.thin(thr, thr)
+    ctx.remaining()
+
+
+def test_sog_transform_reaches_the_written_files(gpu_ctx, sof_golden, tmp_path):
+    """A .sog header with lower-left (1.5, -2, 3.25) and length 2R: the
+    written vertices are 2v + lower-left (one double expression rounded to
+    float, as trimesh's xform * point), the radii len(M (r,0,0) - M 0)."""
+    ctx = gpu_ctx
+    base = sof_golden["sog_torus40"].tobytes()
+    R = int(np.frombuffer(base[128:132], np.int32)[0])
+    ll = np.array([1.5, -2.0, 3.25], np.float32)
+    moved = base[:15] + ll.tobytes() + np.float32(2 * R).tobytes() + base[31:]
+    ctx.set_volume_sog(base)
+    _run_installed(ctx)
+    ctx.write_remaining(str(tmp_path / "id"))
+    v, e, t = ctx.remaining_arrays()
+    keep = ctx.thin_flags()["keep_v"].astype(bool)
+    r = ctx.vertex_radii()[keep]
+    O.write_ply(str(tmp_path / "o_id.ply"), v, e, t)
+    assert open(str(tmp_path / "id.ply"), "rb").read() == open(str(tmp_path / "o_id.ply"), "rb").read()
+    ctx.set_volume_sog(moved)
+    M = ctx.vox_to_model()
+    assert np.array_equal(M, np.array([[2, 0, 0, 1.5], [0, 2, 0, -2], [0, 0, 2, 3.25], [0, 0, 0, 1]], np.float64))
+    _run_installed(ctx)
+    ctx.write_remaining(str(tmp_path / "mv"))
+    tv = (2.0 * v.astype(np.float64) + ll.astype(np.float64)).astype(np.float32)
+    q = (2.0 * r.astype(np.float64) + np.float64(ll[0])).astype(np.float32)
+    d = (q - ll[0]).astype(np.float32)
+    rr = np.sqrt(d * d).astype(np.float32)
+    O.write_ply(str(tmp_path / "o.ply"), tv, e, t)
+    O.write_radii(str(tmp_path / "o.r"), tv, rr)
+    O.write_dotma(str(tmp_path / "o.ma"), tv, rr, O.dotma_edges(e, t), t)
+    for ext in (".ply", ".r", ".ma"):
+        assert open(str(tmp_path / "mv") + ext, "rb").read() == open(str(tmp_path / "o") + ext, "rb").read(), ext
+
+
+def test_malformed_sog_is_rejected(gpu_ctx, sof_golden):
+    data = sof_golden["sog_grf32"].tobytes()
+    for bad in (data[:-5], b"SOG.Format 2.0\0" + data[15:], data[:100]):
+        with pytest.raises(_lib.VoxelCoreError) as ei:
+            gpu_ctx.set_volume_sog(bad)
+        assert ei.value.status == _lib.VC_ERR_ARG

@@ -99,3 +99,39 @@ def test_encode_decode_round_trip(oracle_lib, seed):
             path = os.path.join(d, "v.sof")
             O.ref_sof_write(occ, path)
             assert open(path, "rb").read() == api.encode_sof(occ)
+    occ_g, _ = O.sof_decode(api.encode_sog(occ), sog=True)
+    assert np.array_equal(occ_g, emb)
+
+
+SOG_NAMES = ["csg13", "grf32", "noise", "spheres30", "torus40"]
+
+
+@pytest.mark.parametrize("name", SOG_NAMES)
+def test_sog_oracle_and_encoder_match_the_reference(sof_golden, name):
+    """.sog files written and read by the reference (write_sog_file /
+    read_sog_file): the oracle's decoding equals the reference's reading, and
+    vc_encode_sog writes the same bytes, but for the header bytes 31..127 the
+    reference leaves uninitialised."""
+    g = sof_golden
+    data = g[f"sog_{name}"].tobytes()
+    occ, sites = O.sof_decode(data, sog=True)
+    assert np.array_equal(np.packbits(occ.ravel()), g[f"sogocc_{name}"])
+    assert np.array_equal((sites + 0.5).astype(np.int16), g[f"sogsites_{name}"])
+    assert np.array_equal(g[f"sogocc_{name}"], g[f"sofocc_{name}"])  # same octree as the .sof
+
+
+def test_sog_encoder_bytes(sof_golden):
+    from voxel_ma_gb300 import api
+    for name, occ in _golden_sof_volumes().items():
+        ref = sof_golden[f"sog_{name}"].tobytes()
+        enc = api.encode_sog(np.asarray(occ))
+        assert len(enc) == len(ref), name
+        assert enc[:31] == ref[:31] and enc[128:] == ref[128:], name
+        assert enc[31:128] == bytes(97)
+
+
+def test_malformed_sog_is_rejected_by_the_oracle(sof_golden):
+    data = sof_golden["sog_grf32"].tobytes()
+    assert O.sof_decode(data[:-5], sog=True) is None           # truncated inside a leaf's feature point
+    assert O.sof_decode(b"SOG.Format 2.0\0" + data[15:], sog=True) is None
+    assert O.sof_decode(data[:100], sog=True) is None

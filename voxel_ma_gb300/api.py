@@ -198,6 +198,23 @@ class Context:
         self.shape = (n, n, n)
         return n
 
+    def set_volume_sog(self, data: bytes) -> int:
+        """Install an octree volume from the bytes of a .sog file
+        (vc_set_volume_sog); returns its voxels per axis (R + 1)."""
+        buf = np.frombuffer(data, dtype=np.uint8)
+        size = ctypes.c_int()
+        self.check(self.lib.vc_set_volume_sog(self.h, buf.ctypes.data_as(ctypes.c_void_p), len(buf),
+                                              ctypes.byref(size)), "vc_set_volume_sog")
+        n = int(size.value)
+        self.shape = (n, n, n)
+        return n
+
+    def vox_to_model(self) -> np.ndarray:
+        """The installed volume's voxel-to-model matrix, 4x4 (vc_get_vox_to_model)."""
+        m = np.zeros(16, np.float64)
+        self.check(self.lib.vc_get_vox_to_model(self.h, m.ctypes.data_as(ctypes.c_void_p)), "vc_get_vox_to_model")
+        return m.reshape(4, 4).T  # column-major storage
+
     def volume(self, device: bool = False):
         """The installed occupancy (vc_get_volume)."""
         out = self._out(self.shape, np.uint8, device)
@@ -481,18 +498,27 @@ class Server:
 def encode_sof(occ) -> bytes:
     """The .sof octree stream of a dense occupancy volume (host numpy array),
     as the reference's OctreeVolume writes it (vc_encode_sof)."""
+    return _encode_octree(occ, "vc_encode_sof")
+
+
+def encode_sog(occ) -> bytes:
+    """The .sog octree stream of a dense occupancy volume (vc_encode_sog)."""
+    return _encode_octree(occ, "vc_encode_sog")
+
+
+def _encode_octree(occ, name: str) -> bytes:
     lib = L.load()
     occ = np.ascontiguousarray(occ, dtype=np.uint8)
     X, Y, Z = (int(s) for s in occ.shape)
     p = occ.ctypes.data_as(ctypes.c_void_p)
     n = ctypes.c_int64()
-    st = lib.vc_encode_sof(p, X, Y, Z, None, 0, ctypes.byref(n))
+    st = getattr(lib, name)(p, X, Y, Z, None, 0, ctypes.byref(n))
     if st != L.VC_OK:
-        raise L.VoxelCoreError(st, "vc_encode_sof")
+        raise L.VoxelCoreError(st, name)
     out = np.zeros(n.value, np.uint8)
-    st = lib.vc_encode_sof(p, X, Y, Z, out.ctypes.data_as(ctypes.c_void_p), n.value, ctypes.byref(n))
+    st = getattr(lib, name)(p, X, Y, Z, out.ctypes.data_as(ctypes.c_void_p), n.value, ctypes.byref(n))
     if st != L.VC_OK:
-        raise L.VoxelCoreError(st, "vc_encode_sof")
+        raise L.VoxelCoreError(st, name)
     return out.tobytes()
 
 

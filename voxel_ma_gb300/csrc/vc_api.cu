@@ -52,6 +52,7 @@ int vc_set_volume(vc_ctx* c, const uint8_t* occ, int X, int Y, int Z, int mem) {
     c->ft_valid = c->vd_valid = false;
     c->sites_from_octree = false;
     c->oct_n_sites = 0;
+    set_identity(c->vox_to_model);
     return VC_OK;
 }
 
@@ -272,6 +273,7 @@ int vc_batch_set_volumes(vc_ctx* c, int nvol, const int32_t* dims, const uint8_t
     c->ft_valid = c->vd_valid = false;
     c->sites_from_octree = false;
     c->oct_n_sites = 0;
+    set_identity(c->vox_to_model);
     return VC_OK;
 }
 

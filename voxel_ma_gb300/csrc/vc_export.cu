@@ -19,8 +19,11 @@
 //         first threshold of a run).
 //
 // Floats are written as std::ostream writes them by default (the "%g" rule,
-// 6 significant digits).  The volumes have the identity voxel-to-model
-// matrix, so a radius is written as len((r, 0, 0)) = sqrt(r * r) in float.
+// 6 significant digits).  vc_write_remaining writes vertices and radii in
+// model space: the volume's voxel-to-model matrix (the identity, or a .sog
+// file's) applied as trimesh's xform * point, a radius r as
+// len(M (r, 0, 0) - M (0, 0, 0)) in float; vc_write_radii takes model-space
+// values and writes len((r, 0, 0)) = r.
 #include "vc_internal.cuh"
 
 #include <charconv>
@@ -104,6 +107,14 @@ struct EdgeHash {
 inline uint64_t edge_key(int a, int b) {  // util::makeEdge: (min, max)
     if (a > b) std::swap(a, b);
     return ((uint64_t)(uint32_t)a << 32) | (uint32_t)b;
+}
+
+// trimesh's xform * point (SpaceConverter::fromVoxToModel, src/spaceinfo.cpp):
+// each coordinate one double expression, times 1 / h, rounded to float
+inline void xf_point(const double* m, const float* p, float* q) {
+    float h = (float)(m[3] * p[0] + m[7] * p[1] + m[11] * p[2] + m[15]);
+    h = 1.0f / h;
+    for (int i = 0; i < 3; ++i) q[i] = (float)((m[i] * p[0] + m[i + 4] * p[1] + m[i + 8] * p[2] + m[i + 12]) * h);
 }
 
 }  // namespace
@@ -332,6 +343,12 @@ extern "C" int vc_write_remaining(vc_ctx* c, const char* prefix, int what) {
     std::vector<float> vts((size_t)(3 * rs.nv));
     std::vector<int32_t> edges((size_t)(2 * rs.ne)), tris((size_t)(3 * rs.nt));
     VC_TRY(vc_get_remaining(c, vts.data(), edges.data(), tris.data(), VC_MEM_HOST));
+    // the written vertices are in model space (vts_trans, src/highlevelalgo.cpp:750-760)
+    const double* M = c->vox_to_model;
+    for (int64_t k = 0; k < rs.nv; ++k) {
+        const float p[3] = {vts[3 * k], vts[3 * k + 1], vts[3 * k + 2]};
+        vc::xf_point(M, p, &vts[3 * k]);
+    }
     const std::string base(prefix);
     if (what & VC_WRITE_PLY)
         VC_TRY(vc_write_ply((base + ".ply").c_str(), vts.data(), rs.nv, edges.data(), rs.ne, tris.data(), rs.nt));
@@ -345,13 +362,24 @@ extern "C" int vc_write_remaining(vc_ctx* c, const char* prefix, int what) {
         VC_TRY(vc_vertex_radii(c, all.data(), VC_MEM_HOST));
         VC_TRY(vc_get_thin_flags(c, keep.data(), nullptr, nullptr, nullptr, VC_MEM_HOST));
         radii.reserve((size_t)rs.nv);
+        // r in model space: len(xform * (r, 0, 0) - xform * (0, 0, 0)) in float
+        // (src/exporters.cpp:520-530, src/highlevelalgo.cpp:914-922)
+        const float zero[3] = {0, 0, 0};
+        float o[3];
+        vc::xf_point(M, zero, o);
         for (int64_t v = 0; v < nv; ++v)
-            if (keep[v]) radii.push_back(all[v]);
+            if (keep[v]) {
+                const float p[3] = {all[v], 0, 0};
+                float q[3];
+                vc::xf_point(M, p, q);
+                const float d[3] = {q[0] - o[0], q[1] - o[1], q[2] - o[2]};
+                radii.push_back(std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]));
+            }
         if ((int64_t)radii.size() != rs.nv) return VC_ERR_STATE;
+        // vc_write_radii writes len((r, 0, 0)) = r for these non-negative r
         if (what & VC_WRITE_RADII)
             VC_TRY(vc_write_radii((base + ".r").c_str(), vts.data(), radii.data(), rs.nv));
         if (what & VC_WRITE_MA) {
-            for (float& r : radii) r = std::sqrt(r * r);  // the caller's len(xform * (r, 0, 0))
             std::vector<int32_t> ma_edges;
             vc::dotma_edges(edges.data(), rs.ne, tris.data(), rs.nt, ma_edges);
             VC_TRY(vc_write_dotma((base + ".ma").c_str(), vts.data(), radii.data(), rs.nv, ma_edges.data(),

@@ -27,6 +27,9 @@ enum DeviceError : int {
 };
 
 __device__ __forceinline__ void set_error(int* err, int code) { atomicCAS(err, 0, code); }
+inline void set_identity(double* m) {  // 4x4, column-major
+    for (int i = 0; i < 16; ++i) m[i] = (i % 5 == 0) ? 1.0 : 0.0;
+}
 
 // ---------------------------------------------------------------------------
 // A growable device buffer owned by the context (stream-ordered allocation).
@@ -203,6 +206,7 @@ struct vc_ctx {
     vc::DevBuf occ;  // uint8, all voxels of all volumes
     // an octree (.sof) volume: its mixed leaves give the sites (vc_set_volume_sof)
     bool sites_from_octree = false;
+    double vox_to_model[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};  // column-major, of the volume
     int64_t oct_n_sites = 0;            // mixed leaves of the installed octree
     vc::DevBuf oct_leaves;              // those leaves (packed x, y, z) in stream order
     vc::DevBuf oct_stream, oct_cells, oct_nodes;  // decode scratch: the stream; corner byte per cell; node lists

@@ -28,6 +28,12 @@
 namespace vc {
 namespace {
 
+// .sog: a 128-byte header opening with the title "SOG.Format 1.0" and its
+// terminator (15 bytes), then the lower-left corner and the bounding-box
+// length as floats (src/octree.cpp:353-379, 569-605)
+constexpr int64_t kSogHeader = 128;
+constexpr int kSogTitle = 15;
+
 __global__ void oct_large_kernel(const uint64_t* __restrict__ nodes, int64_t n, uint8_t* __restrict__ cell, int R) {
     for (int64_t i = blockIdx.x; i < n; i += gridDim.x) {
         const uint64_t nd = __ldg(nodes + i);
@@ -44,7 +50,7 @@ __global__ void oct_large_kernel(const uint64_t* __restrict__ nodes, int64_t n, 
 }
 
 // one thread per subtree; FILL: cells + mixed-leaf counts, else the leaves
-template <bool FILL>
+template <bool FILL, int LEAF_EXTRA>
 __global__ void oct_walk_kernel(const uint8_t* __restrict__ b, int64_t nbytes, const uint64_t* __restrict__ sub_node,
                                 const int64_t* __restrict__ sub_pos, int64_t nsub, uint8_t* __restrict__ cell, int R,
                                 int32_t* __restrict__ cnt, const int64_t* __restrict__ base,
@@ -52,7 +58,7 @@ __global__ void oct_walk_kernel(const uint8_t* __restrict__ b, int64_t nbytes, c
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nsub) return;
     int64_t n = 0;
-    if (oct_walk<FILL>(b, nbytes, sub_pos[i], sub_node[i], cell, R, FILL ? nullptr : leaves + base[i], &n) != 0) {
+    if (oct_walk<FILL, LEAF_EXTRA>(b, nbytes, sub_pos[i], sub_node[i], cell, R, FILL ? nullptr : leaves + base[i], &n) != 0) {
         set_error(err, VC_ERR_ARG);
         return;
     }
@@ -95,11 +101,13 @@ inline int grid_of(vc_ctx* c, int64_t n, int threads) {
 
 // Walk the nodes of edge > 16: the subtrees of edge <= 16 (root, first
 // byte), in stream order, and the empty nodes above them.
-int split_sof(const uint8_t* b, int64_t nbytes, int& R, std::vector<uint64_t>& sub_node,
-              std::vector<int64_t>& sub_pos, std::vector<uint64_t>& large) {
-    if (nbytes < 4) return VC_ERR_ARG;
+// The resolution is the int32 at byte `start` (0 in .sof, after the 128-byte
+// header in .sog); a leaf has leaf_extra bytes after its corner byte.
+int split_sof(const uint8_t* b, int64_t nbytes, int64_t start, int leaf_extra, int& R,
+              std::vector<uint64_t>& sub_node, std::vector<int64_t>& sub_pos, std::vector<uint64_t>& large) {
+    if (nbytes < start + 4) return VC_ERR_ARG;
     int32_t r = 0;
-    std::memcpy(&r, b, 4);
+    std::memcpy(&r, b + start, 4);
     if (r < 1 || (r & (r - 1)) != 0 || r > 16384) return VC_ERR_ARG;
     R = r;
     int lgR = 0;
@@ -108,7 +116,7 @@ int split_sof(const uint8_t* b, int64_t nbytes, int& R, std::vector<uint64_t>& s
         int x, y, z, lg, child;
     };
     std::vector<Frame> stack;
-    int64_t pos = 4;
+    int64_t pos = start + 4;
     auto visit = [&](int x, int y, int z, int lg) -> int {
         if (lg <= kOctSubLg) {
             sub_node.push_back(oct_pack(x, y, z, lg, 0));
@@ -119,7 +127,7 @@ int split_sof(const uint8_t* b, int64_t nbytes, int& R, std::vector<uint64_t>& s
                 if (pos >= nbytes) return VC_ERR_ARG;
                 const uint8_t t = b[pos];
                 if (t > 2) return VC_ERR_ARG;
-                pos += 1 + (t != 0);
+                pos += t == 0 ? 1 : t == 1 ? 2 : 2 + leaf_extra;
                 open += t == 0 ? 7 : -1;
             }
             return pos > nbytes ? VC_ERR_ARG : VC_OK;
@@ -150,11 +158,12 @@ int split_sof(const uint8_t* b, int64_t nbytes, int& R, std::vector<uint64_t>& s
 
 }  // namespace
 
-int install_octree(vc_ctx* c, const uint8_t* bytes, int64_t nbytes, int* size_out) {
+int install_octree(vc_ctx* c, const uint8_t* bytes, int64_t nbytes, bool sog, int* size_out) {
     int R = 0;
     std::vector<uint64_t> sub_node, large;
     std::vector<int64_t> sub_pos;
-    VC_TRY(split_sof(bytes, nbytes, R, sub_node, sub_pos, large));
+    const int64_t start = sog ? kSogHeader : 0;
+    VC_TRY(split_sof(bytes, nbytes, start, sog ? 12 : 0, R, sub_node, sub_pos, large));
     const int S = R + 1;
     if ((int64_t)(S + 1) * (S + 1) * (S + 1) >= ((int64_t)1 << 33) || S > 32766) return VC_ERR_ARG;
     const int64_t ncell = (int64_t)R * R * R, nvox = (int64_t)S * S * S;
@@ -188,8 +197,9 @@ int install_octree(vc_ctx* c, const uint8_t* bytes, int64_t nbytes, int* size_ou
             launched(c);
         }
         if (nsub) {  // none when the whole cube is one empty node
-            oct_walk_kernel<true><<<(int)((nsub + 127) / 128), 128, 0, c->stream>>>(
-                db, nbytes, d_node, d_pos, nsub, cell, R, d_cnt, nullptr, nullptr, dev_err(c));
+            auto walk = sog ? oct_walk_kernel<true, 12> : oct_walk_kernel<true, 0>;
+            walk<<<(int)((nsub + 127) / 128), 128, 0, c->stream>>>(db, nbytes, d_node, d_pos, nsub, cell, R, d_cnt,
+                                                                   nullptr, nullptr, dev_err(c));
             launched(c);
             VC_CUDA(c, cudaGetLastError());
             VC_CUDA(c, cudaMemcpyAsync(cnt.data(), d_cnt, nsub * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
@@ -209,8 +219,9 @@ int install_octree(vc_ctx* c, const uint8_t* bytes, int64_t nbytes, int* size_ou
         if (nleaf) {
             VC_CUDA(c, cudaMemcpyAsync(d_base, base.data(), nsub * sizeof(int64_t), cudaMemcpyHostToDevice,
                                        c->stream));
-            oct_walk_kernel<false><<<(int)((nsub + 127) / 128), 128, 0, c->stream>>>(
-                db, nbytes, d_node, d_pos, nsub, cell, R, nullptr, d_base, ptr<uint64_t>(c->oct_leaves), dev_err(c));
+            auto walk = sog ? oct_walk_kernel<false, 12> : oct_walk_kernel<false, 0>;
+            walk<<<(int)((nsub + 127) / 128), 128, 0, c->stream>>>(db, nbytes, d_node, d_pos, nsub, cell, R, nullptr,
+                                                                   d_base, ptr<uint64_t>(c->oct_leaves), dev_err(c));
             launched(c);
         }
         oct_voxels_kernel<<<grid_of(c, nvox, 256), 256, 0, c->stream>>>(cell, R, ptr<uint8_t>(c->occ));
@@ -224,6 +235,19 @@ int install_octree(vc_ctx* c, const uint8_t* bytes, int64_t nbytes, int* size_ou
     c->ft_valid = c->vd_valid = false;
     c->oct_n_sites = nleaf;
     c->sites_from_octree = true;
+    set_identity(c->vox_to_model);
+    if (sog) {
+        // read_sof's header: lower-left corner and bounding-box length (floats
+        // after the title); vox-to-mesh = trans(lower-left) * scale(len / R)
+        float ll[3], len;
+        std::memcpy(ll, bytes + kSogTitle, 12);
+        std::memcpy(&len, bytes + kSogTitle + 12, 4);
+        const double sc = (double)len / (double)R;
+        c->vox_to_model[0] = c->vox_to_model[5] = c->vox_to_model[10] = sc;
+        c->vox_to_model[12] = ll[0];
+        c->vox_to_model[13] = ll[1];
+        c->vox_to_model[14] = ll[2];
+    }
     if (size_out) *size_out = S;
     return sync_check(c);  // the host lists go out of scope
 }
@@ -257,7 +281,20 @@ int octree_sites(vc_ctx* c, uint32_t* bits, int32_t* cnt, int64_t nwords, int64_
 extern "C" int vc_set_volume_sof(vc_ctx* c, const void* bytes, int64_t nbytes, int* size) {
     if (!c || !bytes || nbytes < 0) return VC_ERR_ARG;
     if (cudaSetDevice(c->device) != cudaSuccess) return vc::cuda_fail(c, cudaGetLastError(), "cudaSetDevice");
-    return vc::install_octree(c, static_cast<const uint8_t*>(bytes), nbytes, size);
+    return vc::install_octree(c, static_cast<const uint8_t*>(bytes), nbytes, false, size);
+}
+
+extern "C" int vc_set_volume_sog(vc_ctx* c, const void* bytes, int64_t nbytes, int* size) {
+    if (!c || !bytes || nbytes < 0) return VC_ERR_ARG;
+    if (nbytes < vc::kSogHeader || std::memcmp(bytes, "SOG.Format 1.0", vc::kSogTitle) != 0) return VC_ERR_ARG;
+    if (cudaSetDevice(c->device) != cudaSuccess) return vc::cuda_fail(c, cudaGetLastError(), "cudaSetDevice");
+    return vc::install_octree(c, static_cast<const uint8_t*>(bytes), nbytes, true, size);
+}
+
+extern "C" int vc_get_vox_to_model(vc_ctx* c, double* m) {
+    if (!c || !m) return VC_ERR_ARG;
+    std::memcpy(m, c->vox_to_model, sizeof c->vox_to_model);
+    return VC_OK;
 }
 
 // ---------------------------------------------------------------------------
@@ -289,7 +326,11 @@ inline int log2_int(int n) {  // util::log2Int: ceil(log2(n)), 0 for n <= 1
 
 }  // namespace
 
-int encode_sof(const uint8_t* occ, int X, int Y, int Z, std::vector<uint8_t>& out) {
+// sog: write_sog_file's layout (src/octree.cpp:569-668): the 128-byte header
+// (title, lower-left 0, length R; the reference leaves the rest of the header
+// uninitialised, here it is zero), R, then the nodes with each leaf's feature
+// point, its cell centre, as three floats.
+int encode_sof(const uint8_t* occ, int X, int Y, int Z, bool sog, std::vector<uint8_t>& out) {
     const int mx = std::max(X, std::max(Y, Z));
     const int R = 1 << log2_int(mx - 1);
     auto inside = [&](int x, int y, int z) -> bool {
@@ -355,8 +396,15 @@ int encode_sof(const uint8_t* occ, int X, int Y, int Z, std::vector<uint8_t>& ou
     // pre-order
     out.clear();
     const int32_t r32 = R;
-    out.resize(4);
-    std::memcpy(out.data(), &r32, 4);
+    if (sog) {
+        out.assign((size_t)kSogHeader, 0);
+        std::memcpy(out.data(), "SOG.Format 1.0", kSogTitle);
+        const float len = (float)R;
+        std::memcpy(out.data() + kSogTitle + 12, &len, 4);
+    }
+    const size_t at = out.size();
+    out.resize(at + 4);
+    std::memcpy(out.data() + at, &r32, 4);
     struct F {
         int k, x, y, z, child;
     };
@@ -374,6 +422,12 @@ int encode_sof(const uint8_t* occ, int X, int Y, int Z, std::vector<uint8_t>& ou
         } else {
             out.push_back(2);
             out.push_back(leafv[((size_t)x * R + y) * R + z]);
+            if (sog) {
+                const float feat[3] = {(float)(x + 0.5), (float)(y + 0.5), (float)(z + 0.5)};
+                const size_t q = out.size();
+                out.resize(q + 12);
+                std::memcpy(out.data() + q, feat, 12);
+            }
         }
     };
     emit(nlev - 1, 0, 0, 0);
@@ -393,14 +447,23 @@ int encode_sof(const uint8_t* occ, int X, int Y, int Z, std::vector<uint8_t>& ou
 
 }  // namespace vc
 
-extern "C" int vc_encode_sof(const uint8_t* occ, int X, int Y, int Z, uint8_t* out, int64_t cap, int64_t* nbytes) {
+static int encode_octree(const uint8_t* occ, int X, int Y, int Z, bool sog, uint8_t* out, int64_t cap,
+                         int64_t* nbytes) {
     if (!occ || !nbytes || X <= 0 || Y <= 0 || Z <= 0 || std::max(X, std::max(Y, Z)) > 16385) return VC_ERR_ARG;
     std::vector<uint8_t> buf;
-    VC_TRY(vc::encode_sof(occ, X, Y, Z, buf));
+    VC_TRY(vc::encode_sof(occ, X, Y, Z, sog, buf));
     *nbytes = (int64_t)buf.size();
     if (out) {
         if (cap < (int64_t)buf.size()) return VC_ERR_ARG;
         std::memcpy(out, buf.data(), buf.size());
     }
     return VC_OK;
+}
+
+extern "C" int vc_encode_sof(const uint8_t* occ, int X, int Y, int Z, uint8_t* out, int64_t cap, int64_t* nbytes) {
+    return encode_octree(occ, X, Y, Z, false, out, cap, nbytes);
+}
+
+extern "C" int vc_encode_sog(const uint8_t* occ, int X, int Y, int Z, uint8_t* out, int64_t cap, int64_t* nbytes) {
+    return encode_octree(occ, X, Y, Z, true, out, cap, nbytes);
 }

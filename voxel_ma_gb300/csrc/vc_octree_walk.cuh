@@ -53,13 +53,15 @@ VC_HD inline void oct_fill(uint8_t* cell, int R, int x, int y, int z, int lg, ui
 }
 
 // Walk the subtree whose first token is at byte pos and whose root is the
-// packed node root (corner byte unused).  FILL: write the cells and count
+// packed node root (corner byte unused).  LEAF_EXTRA: bytes after a leaf's
+// corner byte (0 in .sof; 12 in .sog, the three floats of its feature point,
+// src/octree.cpp:403-410).  FILL: write the cells and count
 // the mixed leaves (corner byte neither 0x00 nor 0xff) into *nmixed.
 // !FILL: write the mixed leaves, packed, to out[0 .. *nmixed).  Returns 0, or
 // 1 for a stream that is not a valid subtree (a read past nbytes, an unknown
 // type, an internal node of one cell, a leaf or empty node too large for the
 // walker).
-template <bool FILL>
+template <bool FILL, int LEAF_EXTRA = 0>
 VC_HD inline int oct_walk(const uint8_t* b, int64_t nbytes, int64_t pos, uint64_t root, uint8_t* cell, int R,
                           uint64_t* out, int64_t* nmixed) {
     struct Frame {
@@ -83,6 +85,10 @@ VC_HD inline int oct_walk(const uint8_t* b, int64_t nbytes, int64_t pos, uint64_
             uint8_t v;
             if (type == 2) {
                 if (lg != 0) return 1;
+                if (LEAF_EXTRA) {
+                    if (nbytes - pos < LEAF_EXTRA) return 1;
+                    pos += LEAF_EXTRA;
+                }
                 v = raw;
                 if (v != 0x00 && v != 0xff) {
                     if (!FILL) out[n] = oct_pack(x, y, z, 0, 0);
