@@ -250,6 +250,7 @@ class Context:
         s = L.VdSizes()
         self.check(self.lib.vc_lattice_vd(self.h, ctypes.byref(s)), "vc_lattice_vd")
         self.vd_sizes = dict(nv=s.nv, ne=s.ne, nt=s.nt, nface=s.nface, inside_size=s.inside_size)
+        self.use_vd_as_complex()  # vc_lattice_vd installs it as the context's cell complex
         return self.vd_sizes
 
     def vd(self, device: bool = False) -> dict:
