@@ -390,6 +390,7 @@ def run_gpu(args):
         sof = api.encode_sof(occ_np)
         enc_s = time.perf_counter() - t0
         oct_ctx = api.Context(local)
+        oct_ctx.set_timing(True)
         dec = []
         for _ in range(4):
             torch.cuda.synchronize(dev)

@@ -101,6 +101,23 @@ inline int grid_of(vc_ctx* c, int64_t n, int threads) {
 
 // Walk the nodes of edge > 16: the subtrees of edge <= 16 (root, first
 // byte), in stream order, and the empty nodes above them.
+// Skip one subtree: each node is one token, an internal one opens eight
+// more.  The loop is one dependent chain (the type byte decides where the
+// next one is), so the stride is kept to a compare and an add; LEAF_EXTRA is
+// a constant.  Returns the byte after the subtree, or -1.
+template <int LEAF_EXTRA>
+int64_t skip_subtree(const uint8_t* b, int64_t nbytes, int64_t pos) {
+    int64_t open = 1;
+    while (open > 0) {
+        if (pos >= nbytes) return -1;
+        const uint8_t t = b[pos];
+        if (t > 2) return -1;
+        pos += LEAF_EXTRA ? (t == 0 ? 1 : t == 1 ? 2 : 2 + LEAF_EXTRA) : 1 + (t != 0);
+        open += t == 0 ? 7 : -1;
+    }
+    return pos > nbytes ? -1 : pos;
+}
+
 // The resolution is the int32 at byte `start` (0 in .sof, after the 128-byte
 // header in .sog); a leaf has leaf_extra bytes after its corner byte.
 int split_sof(const uint8_t* b, int64_t nbytes, int64_t start, int leaf_extra, int& R,
@@ -121,16 +138,8 @@ int split_sof(const uint8_t* b, int64_t nbytes, int64_t start, int leaf_extra, i
         if (lg <= kOctSubLg) {
             sub_node.push_back(oct_pack(x, y, z, lg, 0));
             sub_pos.push_back(pos);
-            // skip it: each node is one token, an internal one opens eight more
-            int64_t open = 1;
-            while (open > 0) {
-                if (pos >= nbytes) return VC_ERR_ARG;
-                const uint8_t t = b[pos];
-                if (t > 2) return VC_ERR_ARG;
-                pos += t == 0 ? 1 : t == 1 ? 2 : 2 + leaf_extra;
-                open += t == 0 ? 7 : -1;
-            }
-            return pos > nbytes ? VC_ERR_ARG : VC_OK;
+            pos = leaf_extra ? skip_subtree<12>(b, nbytes, pos) : skip_subtree<0>(b, nbytes, pos);
+            return pos < 0 ? VC_ERR_ARG : VC_OK;
         }
         if (pos >= nbytes) return VC_ERR_ARG;
         const uint8_t type = b[pos++];
