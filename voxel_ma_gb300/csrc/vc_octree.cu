@@ -19,6 +19,12 @@
 // reads its cell as OctreeVolume::getDataAt does (src/octree.cpp:233-256):
 // its own cell's lowest corner, or, at a coordinate R, the last cell's far
 // corner.
+//
+// .sog files (read_sog_file, src/octree.cpp:351-498) hold the same node
+// stream after a 128-byte header (title, lower-left corner, bounding-box
+// length), with R after the header and twelve more bytes after each leaf's
+// corner byte (its feature point, skipped); they also set the volume's
+// voxel-to-model matrix, which the exporters apply.
 #include "vc_internal.cuh"
 #include "vc_octree_walk.cuh"
 

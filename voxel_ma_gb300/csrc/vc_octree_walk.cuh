@@ -1,5 +1,5 @@
-// One subtree of a .sof node stream, walked in pre-order (the order of the
-// reference's read_sof_file, src/octree.cpp:259-357): internal nodes (type
+// One subtree of a .sof / .sog node stream, walked in pre-order (the order
+// of the reference's read_sof_file / read_sog_file, src/octree.cpp:259-498): internal nodes (type
 // 0) have eight children, x outermost and z innermost; an empty node (type 1)
 // sets every cell of its cube to 0xff (sign byte 1) or 0x00 (any other
 // sign); a leaf (type 2, one cell) sets its corner byte.  The same code runs
