@@ -16,6 +16,11 @@
 //   VoroInfo::extractInsideWithMeasure          vcgpu::extractInsideWithMeasure
 //     (include/voroinfo.h:127-131), for the lattice Voronoi complex
 //   VoroInfo::getRadii (voroinfo.cpp:286-325)   vcgpu::getRadii
+//   nClosedComponents (highlevelalgo.cpp:993)   vcgpu::nClosedComponents
+//   OctreeVolume(filename) (.sof / .sog,        vcgpu::OctreeVolume
+//     octree.cpp:22-47), writeToFile (:66-83)
+//   writeToPLY, writeToDotma                    vcgpu::writeToPLY, vcgpu::writeToDotma
+//     (exporters.cpp:244-287, 341-476)
 //
 // Point types are any type with operator[] over 3 floats (trimesh::point),
 // edges any type with operator[] over 2 ints (trimesh::ivec2), triangles any
@@ -26,6 +31,8 @@
 #pragma once
 
 #include <cstdint>
+#include <fstream>
+#include <iterator>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -241,6 +248,87 @@ inline int nClosedComponents(const cellcomplex& cc) {
     int64_t n = 0;
     check(cc.context().get(), vc_closed_components(cc.context().get(), &n), "vc_closed_components");
     return (int)n;
+}
+
+// ---- octree volumes -------------------------------------------------------
+// OctreeVolume(const char* filename) (octree.cpp:22-47): a .sof or .sog file,
+// chosen by its extension, installed as the context's volume ((R+1)^3 voxels,
+// the octree site rule, and for .sog its voxel-to-model matrix).
+class OctreeVolume {
+public:
+    OctreeVolume(Context& ctx, const std::string& filename) : ctx_(ctx) {
+        std::ifstream f(filename, std::ios::binary);
+        if (!f) throw Error(VC_ERR_ARG, "cannot open " + filename);
+        const std::vector<char> bytes((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+        const bool sog = filename.size() >= 4 && filename.compare(filename.size() - 4, 4, ".sog") == 0;
+        const bool sof = filename.size() >= 4 && filename.compare(filename.size() - 4, 4, ".sof") == 0;
+        if (!sog && !sof) throw Error(VC_ERR_ARG, "not a .sof or .sog file: " + filename);
+        vc_ctx* c = ctx.get();
+        check(c, (sog ? vc_set_volume_sog : vc_set_volume_sof)(c, bytes.data(), (int64_t)bytes.size(), &size_),
+              sog ? "vc_set_volume_sog" : "vc_set_volume_sof");
+    }
+    int getMaxRes() const { return size_ - 1; }  // R
+    int size() const { return size_; }           // voxels per axis, R + 1
+
+private:
+    Context& ctx_;
+    int size_ = 0;
+};
+
+// OctreeVolume(const Volume3DScalar*) + writeToFile(filename): the octree of
+// a dense volume written as .sof or .sog (by extension).  Host code.
+inline bool writeOctreeFile(const DenseVolume& vol, const std::string& filename) {
+    const bool sog = filename.size() >= 4 && filename.compare(filename.size() - 4, 4, ".sog") == 0;
+    auto enc = sog ? vc_encode_sog : vc_encode_sof;
+    int64_t n = 0;
+    check(nullptr, enc(vol.data, vol.X, vol.Y, vol.Z, nullptr, 0, &n), "vc_encode_sof");
+    std::vector<uint8_t> buf((size_t)n);
+    check(nullptr, enc(vol.data, vol.X, vol.Y, vol.Z, buf.data(), n, &n), "vc_encode_sof");
+    std::ofstream f(filename, std::ios::binary);
+    f.write(reinterpret_cast<const char*>(buf.data()), (std::streamsize)buf.size());
+    return (bool)f;
+}
+
+// ---- output formats (exporters.h) -----------------------------------------
+enum class ExportErrCode { FAILURE, SUCCESS, INPUT_NOT_OPEN, OUTPUT_NOT_OPEN, INPUT_NOT_SUPPORTED, OUTPUT_NOT_SUPPORTED };
+
+namespace detail {
+template <int N, class T, class V>
+std::vector<T> flatten(const std::vector<V>& v) {
+    std::vector<T> out(v.size() * N);
+    for (size_t i = 0; i < v.size(); ++i)
+        for (int k = 0; k < N; ++k) out[N * i + k] = (T)v[i][k];
+    return out;
+}
+}  // namespace detail
+
+// writeToPLY(filename, vts, edges, tris, ...) (exporters.cpp:341-476): the
+// file holds the vertices, edges and triangles (the measure and site
+// arguments of the reference never reach its file).
+template <class P, class E, class T>
+ExportErrCode writeToPLY(const char* filename, const std::vector<P>& vts, const std::vector<E>& edges,
+                         const std::vector<T>& tris) {
+    const auto v = detail::flatten<3, float>(vts);
+    const auto e = detail::flatten<2, int32_t>(edges);
+    const auto t = detail::flatten<3, int32_t>(tris);
+    return vc_write_ply(filename, v.data(), (int64_t)vts.size(), e.data(), (int64_t)edges.size(), t.data(),
+                        (int64_t)tris.size()) == VC_OK
+               ? ExportErrCode::SUCCESS
+               : ExportErrCode::FAILURE;
+}
+
+// writeToDotma(filename, vts, edges, tri_faces, radii) (exporters.cpp:244-287)
+template <class P, class E, class T>
+ExportErrCode writeToDotma(const std::string& filename, const std::vector<P>& vts, const std::vector<E>& edges,
+                           const std::vector<T>& tris, const std::vector<float>& radii) {
+    if (radii.size() != vts.size()) return ExportErrCode::FAILURE;
+    const auto v = detail::flatten<3, float>(vts);
+    const auto e = detail::flatten<2, int32_t>(edges);
+    const auto t = detail::flatten<3, int32_t>(tris);
+    return vc_write_dotma(filename.c_str(), v.data(), radii.data(), (int64_t)vts.size(), e.data(),
+                          (int64_t)edges.size(), t.data(), (int64_t)tris.size()) == VC_OK
+               ? ExportErrCode::SUCCESS
+               : ExportErrCode::FAILURE;
 }
 
 }  // namespace vcgpu

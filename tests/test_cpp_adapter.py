@@ -58,3 +58,37 @@ def test_adapter_drives_gpu_path_like_the_reference(tmp_path, t):
     assert np.array_equal(radius, lattice_case(oracle, occ)["vd"]["radius"])
     nv, ne, nt = (int(x) for x in lines["remaining"].split())
     assert (nv, ne, nt) == (len(ref["rem_vts"]), len(ref["rem_edges"]), len(ref["rem_tris"]))
+
+
+@pytest.mark.skipif(shutil.which("g++") is None, reason="no g++")
+def test_export_adapters_write_the_library_bytes(tmp_path):
+    """vcgpu::writeToPLY / writeToDotma / writeOctreeFile (host code, no GPU)
+    write the same bytes as the library's C entry points."""
+    from voxel_ma_gb300 import _lib, api
+    _lib.load()
+    exe = str(tmp_path / "export_main")
+    libdir = os.path.join(ROOT, "voxel_ma_gb300")
+    subprocess.run(["g++", "-std=c++17", "-O2", "-I" + os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "export_main.cpp"), "-o", exe, "-L" + libdir,
+                    "-lvoxelcore_gb300", "-Wl,-rpath," + libdir], check=True, capture_output=True, text=True)
+    rng = np.random.default_rng(4)
+    nv, ne, nt = 500, 60, 700
+    vts = rng.uniform(-10, 600, (nv, 3)).astype(np.float32)
+    radii = rng.uniform(0, 30, nv).astype(np.float32)
+    edges = rng.integers(0, nv, (ne, 2)).astype(np.int32)
+    tris = rng.integers(0, nv, (nt, 3)).astype(np.int32)
+    blob = tmp_path / "complex.bin"
+    with open(blob, "wb") as f:
+        f.write(np.array([nv, ne, nt], np.int64).tobytes())
+        for a in (vts, radii, edges, tris):
+            f.write(np.ascontiguousarray(a).tobytes())
+    prefix = str(tmp_path / "cpp")
+    subprocess.run([exe, str(blob), prefix], check=True, capture_output=True, text=True)
+    api.write_ply(str(tmp_path / "py.ply"), vts, edges, tris)
+    api.write_dotma(str(tmp_path / "py.ma"), vts, radii, edges, tris)
+    for ext in (".ply", ".ma"):
+        assert open(prefix + ext, "rb").read() == open(str(tmp_path / "py") + ext, "rb").read(), ext
+    occ = np.ones((9, 7, 5), np.uint8)
+    occ[4, 3, 2] = 0
+    assert open(prefix + ".sof", "rb").read() == api.encode_sof(occ)
+    assert open(prefix + ".sog", "rb").read() == api.encode_sog(occ)
