@@ -178,13 +178,24 @@ int install_octree(vc_ctx* c, const uint8_t* bytes, int64_t nbytes, bool sog, in
     std::vector<uint64_t> sub_node, large;
     std::vector<int64_t> sub_pos;
     const int64_t start = sog ? kSogHeader : 0;
-    VC_TRY(split_sof(bytes, nbytes, start, sog ? 12 : 0, R, sub_node, sub_pos, large));
+    // the stream goes to the device on a second host thread while this one
+    // splits it; the thread is joined before anything else enters the stream
+    VC_TRY(ensure_n<uint8_t>(c, c->oct_stream, nbytes));
+    cudaError_t copy_err = cudaSuccess;
+    std::thread copier([&] {
+        copy_err = cudaSetDevice(c->device);
+        if (copy_err == cudaSuccess)
+            copy_err = cudaMemcpyAsync(c->oct_stream.p, bytes, (size_t)nbytes, cudaMemcpyHostToDevice, c->stream);
+    });
+    const int split_rc = split_sof(bytes, nbytes, start, sog ? 12 : 0, R, sub_node, sub_pos, large);
+    copier.join();
+    VC_CUDA(c, copy_err);
+    VC_TRY(split_rc);
     const int S = R + 1;
     if ((int64_t)(S + 1) * (S + 1) * (S + 1) >= ((int64_t)1 << 33) || S > 32766) return VC_ERR_ARG;
     const int64_t ncell = (int64_t)R * R * R, nvox = (int64_t)S * S * S;
     const int64_t nsub = (int64_t)sub_node.size(), nlarge = (int64_t)large.size();
     // node lists: sub roots | sub first bytes | leaf bases | large nodes | counts (int32)
-    VC_TRY(ensure_n<uint8_t>(c, c->oct_stream, nbytes));
     VC_TRY(ensure_n<uint8_t>(c, c->oct_cells, ncell));
     VC_TRY(ensure_n<uint64_t>(c, c->oct_nodes, 3 * nsub + nlarge + (nsub + 1) / 2 + 1));
     uint8_t* db = ptr<uint8_t>(c->oct_stream);
@@ -194,7 +205,6 @@ int install_octree(vc_ctx* c, const uint8_t* bytes, int64_t nbytes, bool sog, in
     int64_t* d_base = d_pos + nsub;
     uint64_t* d_large = reinterpret_cast<uint64_t*>(d_base + nsub);
     int32_t* d_cnt = reinterpret_cast<int32_t*>(d_large + nlarge);
-    VC_CUDA(c, cudaMemcpyAsync(db, bytes, (size_t)nbytes, cudaMemcpyHostToDevice, c->stream));
     if (nsub) {
         VC_CUDA(c, cudaMemcpyAsync(d_node, sub_node.data(), nsub * sizeof(uint64_t), cudaMemcpyHostToDevice,
                                    c->stream));
