@@ -9,12 +9,15 @@ Two libraries are loaded through ctypes:
 * ``liboracle.so`` -- the project's restatement (``vc_oracle.cpp``) of the
   reference's site sweep, the nearest-site relation, the lattice Voronoi
   inside-extraction with lambda measures, ``cellcomplex::finalize``,
-  ``CellComplexThinning::prune`` / ``remainingCC`` and
-  ``util::computeEulerChar``.  Builds on any host (``make oracle``).
+  ``CellComplexThinning::prune`` / ``remainingCC``,
+  ``util::computeEulerChar``, ``nClosedComponents``, the ``.sof`` / ``.sog``
+  octree readers and the ``.ply`` / ``.r`` / ``.ma`` writers.  Builds on any
+  host (``make oracle``).
 * ``_ref/libvcref.so`` -- the reference's OWN sources (ccthin.cpp,
-  cellcomplex.cpp, geomalgo.cpp, spaceinfo.cpp, surfacing.cpp) compiled
-  against the API shim in ``shim/`` (``make ref``).  Only buildable where the
-  reference tree exists; used to pin the restatement.
+  cellcomplex.cpp, geomalgo.cpp, octree.cpp, spaceinfo.cpp, surfacing.cpp,
+  and writeToDotma cut out of exporters.cpp) compiled against the API shim in
+  ``shim/`` (``make ref``).  Only buildable where the reference tree exists;
+  used to pin the restatement.
 """
 from __future__ import annotations
 
