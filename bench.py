@@ -280,6 +280,10 @@ def run_gpu(args):
     dev = torch.device("cuda", local)
 
     occ_np, workload = make_workload(args.workload, device=dev if args.workload.startswith("grf") else None)
+    from voxel_ma_gb300 import volumes
+    occ_sha = volumes.occupancy_sha256(occ_np)
+    if workload in volumes.WORKLOAD_SHA256 and occ_sha != volumes.WORKLOAD_SHA256[workload]:
+        raise SystemExit(f"{workload}: occupancy digest {occ_sha} is not the tested volume's")
     occ_dev = torch.from_numpy(occ_np).to(dev)
     occ_host = torch.from_numpy(occ_np).pin_memory()
     shape = tuple(occ_np.shape)
@@ -452,8 +456,9 @@ def run_gpu(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int32+f32",
-        "data": "synthetic (seeded thresholded Gaussian random field, generated on device)",
+        "data": "synthetic (seeded thresholded smoothed random field, exact integer generator, blurred on device)",
         "config": {"workload": workload, "shape": list(shape), "t": args.t, "path": "plain single-volume",
+                   "occupancy_sha256": occ_sha,
                    "l2": "inputs larger than L2 (per-step working set %.1f GB)" % (ctx.device_bytes() / 1e9),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99))},

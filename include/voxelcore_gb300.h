@@ -306,6 +306,10 @@ int vc_server_get_remaining(vc_server* server, int64_t request_id, float* vts, i
 int vc_server_release(vc_server* server, int64_t request_id);
 int vc_server_get_stats(vc_server* server, vc_server_stats* out);
 int vc_server_destroy(vc_server* server);
+/* Failure injection: the next batch a worker takes runs with
+ * vc_debug_fail_alloc_after(k) on its context, so its requests fail with
+ * VC_ERR_OOM; later batches run normally.                                  */
+int vc_server_debug_fail_alloc_after(vc_server* server, int64_t k);
 /* The batching rule the workers apply, on a list of requests in arrival
  * order: consecutive requests share a batch while they have the same t, the
  * batch holds fewer than max_batch requests and bytes_per_voxel x voxels
@@ -409,6 +413,24 @@ int vc_debug_random_rate(vc_ctx* ctx, int op, int64_t bytes, double* touches_per
  * arithmetic even when every lattice axis is below 2048 (where 32-bit
  * arithmetic is exact and is the default); results are identical.         */
 int vc_debug_ft_wide(vc_ctx* ctx, int wide);
+
+/* ---- failure injection (host side; no kernel is made to fault) -----------
+ * Every device wait of the library is bounded: the thinning kernel's grid
+ * barriers give up after `polls` polls (about 64 ns each) and the call
+ * returns VC_ERR_TIMEOUT with the context still usable.  polls = 0 restores
+ * the default (2^26).                                                      */
+int vc_debug_set_spin_limit(vc_ctx* ctx, unsigned long long polls);
+/* The next k device allocations of the context succeed and the one after
+ * fails, as cudaMallocAsync failing would (VC_ERR_OOM); k < 0 switches it
+ * off.  The context stays usable after the failure.                       */
+int vc_debug_fail_alloc_after(vc_ctx* ctx, int64_t k);
+/* A broken reference count: the next thinnings raise (delta = +1) or lower
+ * (-1) vertex `vertex`'s count of incident edges by one after its record is
+ * built (delta = 0 switches it off).  An edge-vertex pair popped for that
+ * vertex then fails the check the reference makes before removing a pair
+ * (src/ccthin.cpp:570-584, which exits the process); here vc_thin returns
+ * VC_ERR_INVARIANT.                                                        */
+int vc_debug_ref_bias(vc_ctx* ctx, int64_t vertex, int delta);
 
 #ifdef __cplusplus
 }

@@ -31,7 +31,9 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB = None
 _REF = None
-_REFERENCE_TREE = "/root/reference"
+# The reference's source tree, named by the build recipe or the environment
+# (VOXEL_MA_REFERENCE); no default: hosts without the tree build no _ref.
+_REFERENCE_TREE = os.environ.get("VOXEL_MA_REFERENCE", "")
 
 c_i64 = ctypes.c_longlong
 c_vp = ctypes.c_void_p
@@ -41,10 +43,14 @@ def _ptr(a: Optional[np.ndarray]):
     return None if a is None else a.ctypes.data_as(c_vp)
 
 
-def build(reference: bool = True) -> None:
-    """Compile liboracle.so, and the reference library when its tree exists."""
+def build(reference: bool = True, tree: Optional[str] = None) -> None:
+    """Compile liboracle.so, and the reference library when the reference's
+    tree (`tree`, else $VOXEL_MA_REFERENCE) exists."""
+    global _REFERENCE_TREE
+    if tree:
+        _REFERENCE_TREE = tree
     subprocess.run(["make", "-s", "-C", _HERE, "oracle"], check=True)
-    if reference and os.path.isdir(os.path.join(_REFERENCE_TREE, "src")):
+    if reference and reference_tree_present():
         subprocess.run(["make", "-s", "-C", _HERE, "ref", f"REFERENCE={_REFERENCE_TREE}"], check=True)
 
 
@@ -96,7 +102,7 @@ def ref_available() -> bool:
 
 def reference_tree_present() -> bool:
     """Whether the reference's source tree is on this host (the recipe builds from it)."""
-    return os.path.isdir(os.path.join(_REFERENCE_TREE, "src"))
+    return bool(_REFERENCE_TREE) and os.path.isdir(os.path.join(_REFERENCE_TREE, "src"))
 
 
 def ref():
@@ -208,6 +214,19 @@ def finalize(nv: int, edges: np.ndarray, tris: np.ndarray) -> dict:
     return o
 
 
+def finalize_edges(nv: int, edges: np.ndarray, tris: np.ndarray) -> np.ndarray:
+    """The finalized edge list only (no adjacency lists): what the remaining
+    complex needs, at a fraction of finalize()'s memory."""
+    edges = np.ascontiguousarray(edges, dtype=np.int32).reshape(-1, 2)
+    tris = np.ascontiguousarray(tris, dtype=np.int32).reshape(-1, 3)
+    cap = np.zeros((len(edges) + 3 * len(tris), 2), np.int32)  # upper bound of the finalized edges
+    ne = lib().vco_finalize(nv, len(edges), _ptr(edges), len(tris), _ptr(tris), _ptr(cap), None, None, None, None,
+                            None)
+    out = cap[:ne].copy()
+    del cap
+    return out
+
+
 def thin(nv: int, edges: np.ndarray, tris: np.ndarray, em_fin: np.ndarray, fm: np.ndarray, f_t: float, l_t: float):
     """FIFO prune; em_fin indexed by FINALIZED edge id.  Returns dict of flags + stats."""
     edges = np.ascontiguousarray(edges, dtype=np.int32).reshape(-1, 2)
@@ -302,7 +321,7 @@ def run_plain(occ: np.ndarray, t: float = 0.04, threads: int = 1) -> dict:
     xyz, li = extract_sites(occ)
     d2, ids = ft(occ.shape, li, threads=threads)
     vd = lattice_vd(occ, ids, xyz)
-    fin = finalize(len(vd["vts"]), vd["edges"], vd["tris"])
+    fin = dict(edges=finalize_edges(len(vd["vts"]), vd["edges"], vd["tris"]))
     em_fin = np.zeros(len(fin["edges"]), np.float32)
     em_fin[: len(vd["em"])] = vd["em"]
     thresh = float(np.float32(np.float64(vd["inside_size"]) * t))

@@ -149,16 +149,65 @@ struct Fin {
     std::vector<int32_t> ve_off, ve_ids, ef_off, ef_ids;
 };
 
-void finalize(long long nv, long long ne, const int32_t* edges, long long nt, const int32_t* tris, Fin& F) {
+// Edge key -> first edge id, open addressing with linear probing (keys are
+// ordered vertex pairs, so all-ones never occurs and marks an empty slot).
+// Same mapping as the reference's unordered_map, far less memory at 10^8 keys.
+struct EdgeIndex {
+    std::vector<uint64_t> keys;
+    std::vector<int32_t> vals;
+    size_t mask = 0, count = 0;
+    static constexpr uint64_t kEmpty = ~0ULL;
+    static uint64_t mix(uint64_t z) {
+        z ^= z >> 31;
+        z *= 0x7fb5d329728ea185ULL;
+        z ^= z >> 27;
+        z *= 0x81dadef4bc2dd44dULL;
+        return z ^ (z >> 33);
+    }
+    explicit EdgeIndex(size_t expect) { rehash(std::max<size_t>(64, expect * 2)); }
+    void rehash(size_t want) {
+        size_t cap = 64;
+        while (cap < want) cap <<= 1;
+        std::vector<uint64_t> ok;
+        std::vector<int32_t> ov;
+        ok.swap(keys);
+        ov.swap(vals);
+        keys.assign(cap, kEmpty);
+        vals.assign(cap, 0);
+        mask = cap - 1;
+        for (size_t i = 0; i < ok.size(); ++i)
+            if (ok[i] != kEmpty) place(ok[i], ov[i]);
+    }
+    void place(uint64_t k, int32_t v) {
+        size_t s = mix(k) & mask;
+        while (keys[s] != kEmpty) s = (s + 1) & mask;
+        keys[s] = k;
+        vals[s] = v;
+    }
+    // the id stored for k, or -1 after storing v for it
+    int32_t find_or_insert(uint64_t k, int32_t v) {
+        size_t s = mix(k) & mask;
+        while (keys[s] != kEmpty) {
+            if (keys[s] == k) return vals[s];
+            s = (s + 1) & mask;
+        }
+        keys[s] = k;
+        vals[s] = v;
+        if (++count * 2 > mask + 1) rehash((mask + 1) * 2);
+        return -1;
+    }
+};
+
+void finalize(long long nv, long long ne, const int32_t* edges, long long nt, const int32_t* tris, Fin& F,
+              bool adjacency = true) {
     // cellcomplex::finalize (cellcomplex.cpp:364-491).  Edge keys are ORDERED
     // pairs: given edges keep first-occurrence order, then face sides (made
     // with makeEdge) that are new are appended in face order.
-    std::unordered_map<uint64_t, int32_t> idx;
-    idx.reserve((size_t)(ne + 3 * nt) * 2 + 16);
+    EdgeIndex idx((size_t)ne);
     F.edges.clear();
     for (long long i = 0; i < ne; ++i) {
         uint64_t k = ekey(edges[2 * i], edges[2 * i + 1]);
-        if (idx.emplace(k, (int32_t)(F.edges.size() / 2)).second) {
+        if (idx.find_or_insert(k, (int32_t)(F.edges.size() / 2)) < 0) {
             F.edges.push_back(edges[2 * i]);
             F.edges.push_back(edges[2 * i + 1]);
         }
@@ -168,19 +217,17 @@ void finalize(long long nv, long long ne, const int32_t* edges, long long nt, co
         for (int s = 0; s < 3; ++s) {
             int32_t a, b;
             make_edge(tris[3 * f + s], tris[3 * f + (s + 1) % 3], a, b);
-            auto it = idx.find(ekey(a, b));
-            int32_t id;
-            if (it == idx.end()) {
+            int32_t id = idx.find_or_insert(ekey(a, b), (int32_t)(F.edges.size() / 2));
+            if (id < 0) {
                 id = (int32_t)(F.edges.size() / 2);
-                idx.emplace(ekey(a, b), id);
                 F.edges.push_back(a);
                 F.edges.push_back(b);
-            } else {
-                id = it->second;
             }
             F.tri_edges[3 * f + s] = id;
         }
     }
+    { EdgeIndex drop(0); std::swap(idx, drop); }
+    if (!adjacency) return;
     long long E = (long long)F.edges.size() / 2;
     // V->E: every edge id is appended to both endpoints, in id order.
     F.ve_off.assign((size_t)nv + 1, 0);
@@ -585,7 +632,7 @@ long long vco_finalize(long long nv, long long ne, const int32_t* edges, long lo
                        int32_t* edges_out, int32_t* tri_edges, int32_t* ve_off, int32_t* ve_ids, int32_t* ef_off,
                        int32_t* ef_ids) {
     Fin F;
-    finalize(nv, ne, edges, nt, tris, F);
+    finalize(nv, ne, edges, nt, tris, F, ve_off || ve_ids || ef_off || ef_ids);
     auto cp = [](int32_t* dst, const std::vector<int32_t>& v) {
         if (dst && !v.empty()) std::memcpy(dst, v.data(), v.size() * sizeof(int32_t));
     };

@@ -61,7 +61,7 @@ def edge_touch_volume():
 
 
 def main():
-    oracle.build(reference=True)
+    oracle.build(reference=True, tree=os.environ.get("VOXEL_MA_REFERENCE", "/root/reference"))
     out = {}
     # 1) site lists
     vols = golden_volumes()

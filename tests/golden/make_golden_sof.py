@@ -43,7 +43,7 @@ def sof_volumes():
 
 
 def main():
-    oracle.build(reference=True)
+    oracle.build(reference=True, tree=os.environ.get("VOXEL_MA_REFERENCE", "/root/reference"))
     out = {}
     with tempfile.TemporaryDirectory() as d:
         for name, occ in sof_volumes().items():

@@ -98,6 +98,7 @@ SIGNATURES = {
     "vc_server_release": (c_int, [c_vp, c_i64]),
     "vc_server_get_stats": (c_int, [c_vp, ctypes.POINTER(ServerStats)]),
     "vc_server_destroy": (c_int, [c_vp]),
+    "vc_server_debug_fail_alloc_after": (c_int, [c_vp, c_i64]),
     "vc_plan_batches": (c_int, [c_int, c_vp, c_vp, c_i64, ctypes.c_double, c_int, c_vp]),
     "vc_set_complex": (c_int, [c_vp, c_i64, c_vp, c_i64, c_vp, c_i64, c_vp, c_int]),
     "vc_finalize": (c_int, [c_vp, ctypes.POINTER(c_i64)]),
@@ -127,6 +128,9 @@ SIGNATURES = {
     "vc_write_remaining": (c_int, [c_vp, ctypes.c_char_p, c_int]),
     "vc_debug_random_rate": (c_int, [c_vp, c_int, c_i64, ctypes.POINTER(ctypes.c_double)]),
     "vc_debug_thin_shape": (c_int, [c_vp, c_int, c_int, c_int]),
+    "vc_debug_set_spin_limit": (c_int, [c_vp, ctypes.c_ulonglong]),
+    "vc_debug_fail_alloc_after": (c_int, [c_vp, c_i64]),
+    "vc_debug_ref_bias": (c_int, [c_vp, c_i64, c_int]),
     "vc_autotune": (c_int, [c_vp, ctypes.c_double, ctypes.POINTER(TuneResult)]),
     "vc_lambda_fp64_check": (c_int, [c_vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(c_i64)]),
     "vc_run_plain": (c_int, [c_vp, c_vp, c_int, c_int, c_int, c_int, ctypes.c_double, ctypes.POINTER(PlainResult)]),

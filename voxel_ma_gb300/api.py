@@ -161,6 +161,18 @@ class Context:
         self.check(self.lib.vc_debug_random_rate(self.h, op, nbytes, ctypes.byref(out)), "vc_debug_random_rate")
         return out.value
 
+    def debug_set_spin_limit(self, polls: int = 0):
+        """Polls before a grid barrier of the thinning gives up (0 = default)."""
+        self.check(self.lib.vc_debug_set_spin_limit(self.h, polls), "vc_debug_set_spin_limit")
+
+    def debug_fail_alloc_after(self, k: int = -1):
+        """The next k device allocations succeed, the one after fails (k < 0: off)."""
+        self.check(self.lib.vc_debug_fail_alloc_after(self.h, k), "vc_debug_fail_alloc_after")
+
+    def debug_ref_bias(self, vertex: int = -1, delta: int = 0):
+        """Raise (+1) or lower (-1) one vertex's thinning count after its record is built (0: off)."""
+        self.check(self.lib.vc_debug_ref_bias(self.h, vertex, delta), "vc_debug_ref_bias")
+
     def debug_ft_wide(self, wide: bool = True):
         """Force 64-bit arithmetic in the feature transform (identical results)."""
         self.check(self.lib.vc_debug_ft_wide(self.h, 1 if wide else 0), "vc_debug_ft_wide")
@@ -478,6 +490,10 @@ class Server:
 
     def release(self, rid: int):
         self._check(self.lib.vc_server_release(self.h, rid), "vc_server_release")
+
+    def debug_fail_alloc_after(self, k: int):
+        """The next batch a worker takes fails its (k+1)-th device allocation."""
+        self._check(self.lib.vc_server_debug_fail_alloc_after(self.h, k), "vc_server_debug_fail_alloc_after")
 
     def stats(self) -> dict:
         s = L.ServerStats()

@@ -41,6 +41,10 @@ int vc_set_volume(vc_ctx* c, const uint8_t* occ, int X, int Y, int Z, int mem) {
     if ((int64_t)(X + 1) * (Y + 1) * (Z + 1) >= ((int64_t)1 << 33) || X > 32766 || Y > 32766 || Z > 32766)
         return VC_ERR_ARG;
     const int64_t n = (int64_t)X * Y * Z;
+    // results of the previous volume are stale from here on, even if an
+    // allocation below fails
+    c->n_sites = -1;
+    c->ft_valid = c->vd_valid = false;
     VC_TRY(ensure_n<uint8_t>(c, c->occ, n));
     VC_TRY(copy_in(c, c->occ.p, occ, (size_t)n, mem));
     const int32_t dims[3] = {X, Y, Z};
@@ -263,6 +267,8 @@ int vc_batch_set_volumes(vc_ctx* c, int nvol, const int32_t* dims, const uint8_t
         if (space_size(kLat, X, Y, Z) >= ((int64_t)1 << 32)) return VC_ERR_ARG;
         nvox += (int64_t)X * Y * Z;
     }
+    c->n_sites = -1;
+    c->ft_valid = c->vd_valid = false;
     VC_TRY(ensure_n<uint8_t>(c, c->occ, nvox));
     VC_TRY(copy_in(c, c->occ.p, occ, (size_t)nvox, mem));
     VC_TRY(set_volume_table(c, nvol, dims));

@@ -25,6 +25,10 @@ int ensure_ctx(vc_ctx* c, DevBuf& b, size_t bytes) {
         b.cap = 0;
     }
     size_t want = std::max<size_t>(bytes, 256);
+    if (c->fail_alloc_after >= 0 && c->fail_alloc_after-- == 0) {
+        c->last_error = "cudaMallocAsync: allocation failure injected (vc_debug_fail_alloc_after)";
+        return VC_ERR_OOM;
+    }
     cudaError_t e = cudaMallocAsync(&b.p, want, c->stream);
     if (e != cudaSuccess) {
         b.p = nullptr;

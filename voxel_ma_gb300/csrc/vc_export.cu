@@ -30,8 +30,11 @@
 #include <cmath>
 #include <cstdio>
 #include <string>
-#include <bits/hashtable_policy.h>  // std::__detail::_Prime_rehash_policy, the set's growth rule
 #include <thread>
+#include <unordered_set>
+#if defined(__GLIBCXX__)
+#include <bits/hashtable_policy.h>  // std::__detail::_Prime_rehash_policy, the set's growth rule
+#endif
 
 namespace vc {
 namespace {
@@ -232,6 +235,7 @@ std::vector<uint64_t> first_occurrences(const std::vector<uint64_t>& ins) {
     return u;
 }
 
+#if defined(__GLIBCXX__)
 // The iteration order of a std::unordered_set<key, EdgeHash> (libstdc++)
 // after inserting ins in order, replayed on arrays: every node goes to the
 // front of its bucket; a bucket that was empty goes to the front of the
@@ -283,6 +287,15 @@ std::vector<uint64_t> unordered_set_order(const std::vector<uint64_t>& ins) {
         for (int32_t p = head[order[oi]]; p >= 0; p = nxt[p]) out.push_back(uniq[p]);
     return out;
 }
+#else
+// Other standard libraries: a real std::unordered_set filled in the same
+// order, iterated in its own order (the reference's order is libstdc++'s).
+std::vector<uint64_t> unordered_set_order(const std::vector<uint64_t>& ins) {
+    std::unordered_set<uint64_t, EdgeHash> set;
+    for (const uint64_t k : ins) set.insert(k);
+    return std::vector<uint64_t>(set.begin(), set.end());
+}
+#endif
 
 // the caller's .ma edge list: remaining edges, then the triangles' edges in
 // the iteration order of a fresh unordered_set filled triangle by triangle

@@ -271,6 +271,11 @@ struct vc_ctx {
     vc::DevBuf ft_far;           // feature transform: tiles the window kernel left to the envelope kernel
     int ft_method = 2;           // feature transform: VC_FT_ENVELOPE, VC_FT_WINDOW or VC_FT_AUTO (default)
     std::mutex* thin_lock = nullptr;  // shared by contexts whose thinning kernels must not overlap
+    // failure injection (host side; the kernels only see ordinary inputs)
+    unsigned long long spin_limit = 1ull << 26;  // polls before a grid barrier gives up (VC_ERR_TIMEOUT)
+    int64_t fail_alloc_after = -1;  // >= 0: that many more device allocations succeed, the next fails
+    int64_t ref_bias_vertex = -1;   // >= 0: this vertex's thinning count is raised by ref_bias after
+    int ref_bias = 0;               //   its record is built (a broken reference count)
     // remaining complex
     bool rem_valid = false;
     vc_rem_sizes rem{};
@@ -402,9 +407,12 @@ __device__ __forceinline__ T block_exclusive_sum(T v, T* smem, T* total) {
 // Bounded grid barrier for cooperative launches.  `bar` points to two
 // unsigned words {arrived, generation}.  Every block calls it with all its
 // threads.  A block that waits longer than `limit` polls records
-// VC_ERR_TIMEOUT in *err and proceeds; callers check *err after the barrier
-// and leave their loop, so no block can wait forever.
-__device__ __forceinline__ void grid_barrier(unsigned* bar, int* err, unsigned long long limit) {
+// VC_ERR_TIMEOUT in *err and proceeds.  Returns, the same for every thread of
+// the block, whether *err was set when the block left (thread 0 reads it once
+// and shares it), so callers leave their loop together: no block waits
+// forever, and no thread of a block goes on while another leaves.
+__device__ __forceinline__ bool grid_barrier(unsigned* bar, int* err, unsigned long long limit) {
+    __shared__ int s_stop;
     __syncthreads();
     if (threadIdx.x == 0) {
         volatile unsigned* vgen = bar + 1;
@@ -426,8 +434,10 @@ __device__ __forceinline__ void grid_barrier(unsigned* bar, int* err, unsigned l
             }
         }
         __threadfence();
+        s_stop = *((volatile int*)err) != 0;
     }
     __syncthreads();
+    return s_stop != 0;
 }
 
 __device__ __forceinline__ int ld_cg(const int* p) { return __ldcg(p); }

@@ -29,6 +29,7 @@
 #include "vc_octree_walk.cuh"
 
 #include <cstring>
+#include <new>
 #include <thread>
 
 namespace vc {
@@ -187,7 +188,14 @@ int install_octree(vc_ctx* c, const uint8_t* bytes, int64_t nbytes, bool sog, in
         if (copy_err == cudaSuccess)
             copy_err = cudaMemcpyAsync(c->oct_stream.p, bytes, (size_t)nbytes, cudaMemcpyHostToDevice, c->stream);
     });
-    const int split_rc = split_sof(bytes, nbytes, start, sog ? 12 : 0, R, sub_node, sub_pos, large);
+    // the node lists grow with the stream's contents: running out of host
+    // memory must neither escape the C ABI nor leave the copier joinable
+    int split_rc = VC_OK;
+    try {
+        split_rc = split_sof(bytes, nbytes, start, sog ? 12 : 0, R, sub_node, sub_pos, large);
+    } catch (const std::bad_alloc&) {
+        split_rc = VC_ERR_OOM;
+    }
     copier.join();
     VC_CUDA(c, copy_err);
     VC_TRY(split_rc);

@@ -68,6 +68,7 @@ struct vc_server {
     std::vector<vc_ctx*> ctxs;
     std::vector<std::thread> threads;
     vc_server_stats stats{};
+    int64_t fail_alloc_after = -1;  // failure injection for the next batch taken (-1: off)
 };
 
 extern "C" int vc_plan_batches(int n, const int64_t* voxels, const double* t, int64_t share_bytes,
@@ -223,6 +224,10 @@ void worker_main(vc_server* s, int w) {
             const double ts = now_s();
             for (Request* r : batch) r->t_start = ts;
             if (!s->pending.empty()) s->cv_work.notify_one();
+            if (s->fail_alloc_after >= 0) {  // armed for this batch only
+                c->fail_alloc_after = s->fail_alloc_after;
+                s->fail_alloc_after = -1;
+            }
         }
         try {
             serve_batch(s, c, batch, stage);
@@ -235,6 +240,7 @@ void worker_main(vc_server* s, int w) {
             s->stats.failed += (int64_t)batch.size();
             s->cv_done.notify_all();
         }
+        c->fail_alloc_after = -1;
         if (vc_ctx_device_bytes(c) > s->share) vc::ctx_release_buffers(c);
     }
 }
@@ -346,6 +352,13 @@ int vc_server_get_stats(vc_server* s, vc_server_stats* out) {
     out->pending = (int64_t)s->pending.size();
     out->device_bytes = 0;
     for (vc_ctx* c : s->ctxs) out->device_bytes += vc_ctx_device_bytes(c);
+    return VC_OK;
+}
+
+int vc_server_debug_fail_alloc_after(vc_server* s, int64_t k) {
+    if (!s) return VC_ERR_ARG;
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->fail_alloc_after = k < 0 ? -1 : k;
     return VC_OK;
 }
 

@@ -381,27 +381,44 @@ extern "C" int vc_extract_sites_noalloc(const uint8_t* occ, int X, int Y, int Z,
     one.nvol = 1;
     one.d0 = make_int4(X, Y, Z, 0);
     // every scratch word read below is written first in this call: counts by
-    // the count kernel, tile sums and the total by the scan
-    sites_count_kernel<<<row_grid(s.num_sms, (int64_t)X * Y), 128, 0, st>>>(occ, one, s.counts);
+    // the count kernel, tile sums and the total by the scan.  Each launch's own
+    // status is checked (cudaLaunchKernelEx returns it), so a launch that
+    // fails leaves *n_sites untouched and no stale total is read; an error the
+    // calling thread had pending before this call is neither read nor cleared.
     const int64_t tiles = (nvox + kScanTile - 1) / kScanTile;
-    scan_tile_sums<int32_t><<<(unsigned)tiles, kScanThreads, 0, st>>>(s.counts, nvox, s.tiles);
-    scan_sums_single<<<1, 1024, 0, st>>>(s.tiles, tiles, s.total);
-    scan_apply<int32_t><<<(unsigned)tiles, kScanThreads, 0, st>>>(s.counts, s.counts, nvox, s.tiles);
-    int64_t n = 0;
-    if (cudaMemcpyAsync(&n, s.total, sizeof(int64_t), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-        cudaStreamSynchronize(st) != cudaSuccess) {
-        cudaGetLastError();
+    const unsigned row_blocks = row_grid(s.num_sms, (int64_t)X * Y);
+    auto cfg = [st](unsigned grid, unsigned block) {
+        cudaLaunchConfig_t c = {};
+        c.gridDim = dim3(grid);
+        c.blockDim = dim3(block);
+        c.stream = st;
+        return c;
+    };
+    auto failed = [](cudaError_t e) {
+        if (e == cudaSuccess) return false;
+        cudaGetLastError();  // this call's own launch error: do not leave it to the caller
+        return true;
+    };
+    cudaLaunchConfig_t c_rows = cfg(row_blocks, 128), c_tiles = cfg((unsigned)tiles, kScanThreads),
+                       c_one = cfg(1, 1024);
+    if (failed(cudaLaunchKernelEx(&c_rows, sites_count_kernel, occ, one, s.counts)) ||
+        failed(cudaLaunchKernelEx(&c_tiles, scan_tile_sums<int32_t>, (const int32_t*)s.counts, nvox, s.tiles)) ||
+        failed(cudaLaunchKernelEx(&c_one, scan_sums_single, s.tiles, tiles, s.total)) ||
+        failed(cudaLaunchKernelEx(&c_tiles, scan_apply<int32_t>, (const int32_t*)s.counts, s.counts, nvox,
+                                  (const int64_t*)s.tiles)))
         return VC_ERR_CUDA;
-    }
+    int64_t n = 0;
+    if (failed(cudaMemcpyAsync(&n, s.total, sizeof(int64_t), cudaMemcpyDeviceToHost, st)) ||
+        failed(cudaStreamSynchronize(st)))
+        return VC_ERR_CUDA;
     *n_sites = n;
     if (n > capacity) return VC_ERR_ARG;  // *n_sites tells the caller how much room is needed
     if (n > 0) {
         if (!xyz) return VC_ERR_ARG;
-        sites_emit_kernel<<<row_grid(s.num_sms, (int64_t)X * Y), 128, 0, st>>>(occ, one, s.counts, xyz, nullptr);
+        if (failed(cudaLaunchKernelEx(&c_rows, sites_emit_kernel, occ, one, (const int32_t*)s.counts, xyz,
+                                      (int32_t*)nullptr)))
+            return VC_ERR_CUDA;
     }
-    if (cudaStreamSynchronize(st) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
-        cudaGetLastError();
-        return VC_ERR_CUDA;
-    }
+    if (failed(cudaStreamSynchronize(st))) return VC_ERR_CUDA;
     return VC_OK;
 }

@@ -375,8 +375,7 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                 s_ncell = 0;
             }
         }
-        grid_barrier(A.bar, A.err, A.spin_limit);
-        if (*((volatile int*)A.err)) break;
+        if (grid_barrier(A.bar, A.err, A.spin_limit)) break;
         // ---- phase B: a listed cell still at 1 gives its child to the item
         // that decremented it last (its trig position), in the cell's slot
         if (tr) A.trace[4 * gen + 2] = global_ns();
@@ -427,8 +426,7 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                     atomicAdd((unsigned long long*)(blk + bi), (unsigned long long)__popc(grp));
             }
         }
-        grid_barrier(A.bar, A.err, A.spin_limit);
-        if (*((volatile int*)A.err)) break;
+        if (grid_barrier(A.bar, A.err, A.spin_limit)) break;
         // ---- phase C: prefixes, write generation g+1 and make its claims;
         // each warp writes its range on its own (no block-wide step per item)
         if (tr) A.trace[4 * gen + 3] = global_ns();
@@ -507,8 +505,7 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
         n = total;
         pushes += total;
         ++gen;
-        grid_barrier(A.bar, A.err, A.spin_limit);
-        if (*((volatile int*)A.err)) break;
+        if (grid_barrier(A.bar, A.err, A.spin_limit)) break;
     }
     atomicAdd((unsigned long long*)&A.ctl[2], (unsigned long long)my_processed);
     atomicAdd((unsigned long long*)&A.ctl[3], (unsigned long long)my_skipped);
@@ -516,6 +513,10 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
         A.ctl[1] = pushes;
         A.ctl[4] = gen;
     }
+}
+
+__global__ void bias_vertex_kernel(VertRec* V, int64_t v, int delta) {
+    V[v].rs += (unsigned long long)(long long)delta;  // the count is the low field of rs
 }
 
 __global__ void set_thr_kernel(float* thr, float f_t, float l_t) {
@@ -660,7 +661,7 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats, bool all_pass) {
     A.ctl = ctl;
     A.bar = reinterpret_cast<unsigned*>(ctl + 8);
 
-    A.spin_limit = 1ull << 26;
+    A.spin_limit = c->spin_limit;
     if (c->trace_cap > 0) {
         VC_TRY(ensure_n<int64_t>(c, c->trace, 4 * (int64_t)c->trace_cap));
         VC_CUDA(c, cudaMemsetAsync(c->trace.p, 0, 4 * sizeof(int64_t) * c->trace_cap, c->stream));
@@ -677,6 +678,11 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats, bool all_pass) {
                 ptr<int32_t>(c->ef_off), ptr<int32_t>(c->ef_ids), ptr<float>(c->em), ptr<float>(c->fm), A.thr,
                 all_pass ? 1 : 0, (int32_t)nv, (int32_t)ne, (int32_t)nt, A.F, A.E, A.V, ptr<int32_t>(c->thin_g0),
                 dev_err(c));
+            launched(c);
+        }
+        if (c->ref_bias_vertex >= 0 && c->ref_bias_vertex < nv) {
+            // a broken reference count, as the reference's logic check meets it
+            bias_vertex_kernel<<<1, 1, 0, c->stream>>>(A.V, c->ref_bias_vertex, c->ref_bias);
             launched(c);
         }
         VC_CUDA(c, cudaMemsetAsync(ctl, 0, 16 * sizeof(int64_t), c->stream));
@@ -779,6 +785,25 @@ int vc_debug_thin_shape(vc_ctx* c, int threads, int blocks_per_sm, int items) {
     c->thin_threads = threads;
     c->thin_blocks_per_sm = blocks_per_sm;
     c->thin_items = items == 2 ? 2 : 1;
+    return VC_OK;
+}
+
+int vc_debug_set_spin_limit(vc_ctx* c, unsigned long long polls) {
+    if (!c) return VC_ERR_ARG;
+    c->spin_limit = polls ? polls : (1ull << 26);
+    return VC_OK;
+}
+
+int vc_debug_fail_alloc_after(vc_ctx* c, int64_t k) {
+    if (!c) return VC_ERR_ARG;
+    c->fail_alloc_after = k < 0 ? -1 : k;
+    return VC_OK;
+}
+
+int vc_debug_ref_bias(vc_ctx* c, int64_t vertex, int delta) {
+    if (!c || delta < -1 || delta > 1) return VC_ERR_ARG;
+    c->ref_bias_vertex = delta ? vertex : -1;
+    c->ref_bias = delta;
     return VC_OK;
 }
 

@@ -10,8 +10,9 @@ value distributions follow the workload definitions:
   centred in the unit cube, 64 (u) x 32 (v) segments, voxel centre inside by a
   parity ray test; 64^3.
 * ``spheres``     union of 32 spheres, centres U[0.2,0.8]^3, radii U[0.05,0.20].
-* ``grf``         white noise N(0,1) blurred by a periodic Gaussian of
-  sigma = 6 voxels, thresholded at 0.
+* ``grf``         white noise (integer, zero mean) blurred by a periodic
+  Gaussian of sigma = 6 voxels, thresholded at 0; exact integer arithmetic,
+  so the same field on every host and device.
 * ``csg``         random union/difference of 1-8 spheres, boxes and capsules in
   a box whose per-axis sizes are log-uniform in [lo, hi].
 """
@@ -91,36 +92,113 @@ def spheres(n: int = 256, count: int = 32, seed: int = 0) -> np.ndarray:
     return occ.astype(np.uint8)
 
 
-def _gauss_kernel_fft(n: int, sigma: float) -> np.ndarray:
-    f = np.fft.fftfreq(n)
-    return np.exp(-2.0 * (math.pi * sigma * f) ** 2)
+def _grf_weights(sigma: float) -> np.ndarray:
+    """Integer taps w_k = round(1024 exp(-k^2 / (2 sigma^2))), k = 0..K, K the
+    last k whose tap is at least 1 (sigma = 6: K = 23, taps sum to 15,397)."""
+    w = []
+    k = 0
+    while True:
+        v = int(math.floor(1024.0 * math.exp(-k * k / (2.0 * sigma * sigma)) + 0.5))
+        if v < 1:
+            break
+        w.append(v)
+        k += 1
+    return np.array(w, np.int64)
+
+
+_SPLITMIX_GAMMA = 0x9E3779B97F4A7C15
+_SEED_MUL = 0xD1B54A32D192ED03
+
+
+def grf_noise(shape, seed: int = 0) -> np.ndarray:
+    """White noise of the GRF: int16, in [-510, 510], a pure function of (seed,
+    linear voxel index) -- the sum of the four low bytes of splitmix64(index)
+    minus 510 (Irwin-Hall of four uniform bytes: mean 0, sd 147.8)."""
+    n = int(np.prod(shape))
+    out = np.empty(n, np.int16)
+    base = np.array([((seed + 1) * _SEED_MUL) & 0xFFFFFFFFFFFFFFFF], np.uint64)
+    g = np.uint64(_SPLITMIX_GAMMA)
+    m1, m2 = np.uint64(0xBF58476D1CE4E5B9), np.uint64(0x94D049BB133111EB)
+    s30, s27, s31, b = np.uint64(30), np.uint64(27), np.uint64(31), np.uint64(255)
+    step = 1 << 23
+    for a in range(0, n, step):
+        z = np.arange(a, min(n, a + step), dtype=np.uint64) * g + base
+        z ^= z >> s30
+        z *= m1
+        z ^= z >> s27
+        z *= m2
+        z ^= z >> s31
+        s = (z & b) + ((z >> np.uint64(8)) & b) + ((z >> np.uint64(16)) & b) + ((z >> np.uint64(24)) & b)
+        out[a:a + len(s)] = s.astype(np.int16) - 510
+    return out.reshape(shape)
+
+
+def _blur_exact_numpy(x: np.ndarray, w: np.ndarray) -> np.ndarray:
+    """Periodic separable correlation with the symmetric taps w (float64 in and
+    out, integer values)."""
+    from scipy import ndimage
+    taps = np.concatenate([w[:0:-1], w]).astype(np.float64)
+    K = len(w) - 1
+    for axis in range(3):
+        n = x.shape[axis]
+        xp = np.take(x, np.arange(-K, n + K) % n, axis=axis)
+        y = ndimage.correlate1d(xp, taps, axis=axis, mode="constant", cval=0.0)
+        del xp
+        sl = [slice(None)] * 3
+        sl[axis] = slice(K, K + n)
+        x = np.ascontiguousarray(y[tuple(sl)])
+        del y
+    return x
+
+
+def _blur_exact_torch(x, w: np.ndarray):
+    import torch
+    K = len(w) - 1
+    for axis in range(3):
+        acc = x * float(w[0])
+        for k in range(1, K + 1):
+            acc += float(w[k]) * (torch.roll(x, k, axis) + torch.roll(x, -k, axis))
+        x = acc
+    return x
 
 
 def grf(n: int = 512, sigma: float = 6.0, seed: int = 0, device=None) -> np.ndarray:
-    """Thresholded smoothed Gaussian random field.  ``device`` = a torch CUDA device for large n."""
+    """Thresholded smoothed random field: ``grf_noise`` correlated periodically
+    along x, y and z with the integer Gaussian taps of ``sigma``, inside where
+    the result is > 0.
+
+    Every partial sum is an integer below 2^53 (|noise| <= 510, taps summing
+    to S, 510 S^3 < 2^53), so float64 arithmetic is exact in any summation
+    order: the numpy path (host) and the torch path (``device``, any torch
+    device) give the same field bit for bit on every machine."""
+    w = _grf_weights(sigma)
+    S = int(w[0] + 2 * w[1:].sum())
+    if 510 * S ** 3 >= 1 << 53:
+        raise ValueError(f"sigma {sigma} too large for the exact integer blur")
+    noise = grf_noise((n, n, n), seed)
     if device is not None:
         import torch
-        g = torch.Generator(device="cpu").manual_seed(seed)
-        w = torch.randn((n, n, n), generator=g, dtype=torch.float32).to(device)
-        Wf = torch.fft.rfftn(w)
-        del w
-        f = torch.fft.fftfreq(n, device=device, dtype=torch.float32)
-        fr = torch.fft.rfftfreq(n, device=device, dtype=torch.float32)
-        kx = torch.exp(-2.0 * (math.pi * sigma * f) ** 2)
-        kz = torch.exp(-2.0 * (math.pi * sigma * fr) ** 2)
-        Wf *= kx[:, None, None] * kx[None, :, None] * kz[None, None, :]
-        out = torch.fft.irfftn(Wf, s=(n, n, n))
-        del Wf
-        occ = (out > 0).to(torch.uint8).cpu().numpy()
-        return occ
-    rng = np.random.default_rng(seed)
-    w = rng.standard_normal((n, n, n), dtype=np.float32)
-    Wf = np.fft.rfftn(w)
-    k = _gauss_kernel_fft(n, sigma)
-    kz = np.exp(-2.0 * (math.pi * sigma * np.fft.rfftfreq(n)) ** 2)
-    Wf *= (k[:, None, None] * k[None, :, None] * kz[None, None, :])
-    out = np.fft.irfftn(Wf, s=(n, n, n), axes=(0, 1, 2))
-    return (out > 0).astype(np.uint8)
+        x = torch.from_numpy(noise).to(device=device, dtype=torch.float64)
+        x = _blur_exact_torch(x, w)
+        return (x > 0).to(torch.uint8).cpu().numpy()
+    x = _blur_exact_numpy(noise.astype(np.float64), w)
+    return (x > 0).astype(np.uint8)
+
+
+# occupancy_sha256 of the benchmark's volumes, fixed by the generators above
+WORKLOAD_SHA256 = {
+    "grf512_sigma6_level0": "3837844dac47b0cf6cd54c61271dd70216d12ecd3ceec9ae90c7f9aabb0e94b0",
+}
+
+
+def occupancy_sha256(occ) -> str:
+    """sha256 of a volume's shape (3 little-endian int64) and its voxels as
+    bytes 0/1, z fastest."""
+    import hashlib
+    a = np.ascontiguousarray(np.asarray(occ) > 0, dtype=np.uint8)
+    h = hashlib.sha256(np.array(a.shape, "<i8").tobytes())
+    h.update(a.tobytes())
+    return h.hexdigest()
 
 
 def _csg_plan(seed: int, lo: int, hi: int):
