@@ -79,6 +79,18 @@ int vc_set_volume_sof(vc_ctx* ctx, const void* bytes, int64_t nbytes, int* size)
  * (three floats, skipped).  The volume's voxel-to-model matrix becomes
  * trans(lower-left) * scale(length / R), as the reference sets it.         */
 int vc_set_volume_sog(vc_ctx* ctx, const void* bytes, int64_t nbytes, int* size);
+/* A density map from the bytes of an .mrc file: the reference's readMRC
+ * (src/importers.cpp:45-60: Tao Ju's MRC reader wrapped as a DenseVolume,
+ * inside <=> value > 0).  Tao's reader is not in the reference tree, so this
+ * follows the public MRC2014 layout: a 1024-byte header (column / row /
+ * section counts, mode 0 int8, 1 int16, 2 float32, 6 uint16 or 12 float16,
+ * the axis of columns / rows / sections, the extended-header length, the
+ * machine stamp for the byte order) and the values, columns fastest.  The
+ * map becomes the context's volume, dims = its X, Y, Z.  VC_ERR_ARG for an
+ * unknown mode, a bad size or a truncated file.                            */
+int vc_set_volume_mrc(vc_ctx* ctx, const void* bytes, int64_t nbytes, int* dims);
+/* The X, Y, Z of an .mrc file's map (header only; no context).            */
+int vc_mrc_dims(const void* bytes, int64_t nbytes, int* dims);
 /* The installed volume's voxel-to-model matrix (16 doubles, column-major as
  * trimesh::xform): the identity except for .sog volumes.                   */
 int vc_get_vox_to_model(vc_ctx* ctx, double* m);
@@ -94,6 +106,8 @@ int vc_encode_sof(const uint8_t* occ, int X, int Y, int Z, uint8_t* out, int64_t
  * header (title, lower-left 0, length R; the header bytes the reference
  * leaves uninitialised are zero), R, the nodes with each leaf's cell centre. */
 int vc_encode_sog(const uint8_t* occ, int X, int Y, int Z, uint8_t* out, int64_t cap, int64_t* nbytes);
+/* Sites of the installed volume; a second call for the same volume returns
+ * the count of the sites already on the device without recomputing them.  */
 int vc_extract_sites(vc_ctx* ctx, int64_t* n_sites);
 int vc_get_sites(vc_ctx* ctx, float* xyz, int mem);
 

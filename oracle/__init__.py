@@ -454,3 +454,44 @@ def ref_write_dotma(path: str, vts, radii, edges, tris) -> None:
 def ref_dotma_edges(edges, tris) -> np.ndarray:
     """The .ma edge assembly on the reference's own ivec2 / ivec2Hash."""
     return _edges_via(ref().vcref_dotma_edges, edges, tris)
+
+
+# ---- MRC density maps (readMRC, importers.cpp:45-60) --------------------------
+
+_MRC_DTYPES = {0: "i1", 1: "i2", 2: "f4", 6: "u2", 12: "f2"}
+
+
+def mrc_decode(data: bytes):
+    """The occupancy (value > 0) of an .mrc file's map, x-major and z fastest,
+    or None when malformed.  A restatement of the public MRC2014 layout (Tao
+    Ju's reader, which the reference calls, is not in its tree): header words
+    0-2 column / row / section counts, 3 the mode, 16-18 the axes of columns,
+    rows and sections, 23 the extended-header bytes; bytes 212-213 the
+    machine stamp; values after the header, columns fastest."""
+    b = np.frombuffer(data, np.uint8)
+    if len(b) < 1024:
+        return None
+    s0, s1 = int(b[212]), int(b[213])
+    big = s0 == 0x11 and s1 == 0x11
+    words = {e: np.frombuffer(data[:1024], e + "i4") for e in ("<", ">")}
+    if not (s0 == 0x44 and s1 in (0x44, 0x41)) and not big:
+        big = int(words["<"][3]) not in _MRC_DTYPES and int(words[">"][3]) in _MRC_DTYPES
+    w = words[">" if big else "<"]
+    n = [int(w[0]), int(w[1]), int(w[2])]
+    mode, nsym = int(w[3]), int(w[23])
+    if min(n) <= 0 or max(n) > 32766 or mode not in _MRC_DTYPES or nsym < 0:
+        return None
+    ax = [int(w[16]) - 1, int(w[17]) - 1, int(w[18]) - 1]
+    if sorted(ax) != [0, 1, 2]:
+        ax = [0, 1, 2]
+    dt = np.dtype(_MRC_DTYPES[mode]).newbyteorder(">" if big else "<")
+    off = 1024 + nsym
+    cnt = n[0] * n[1] * n[2]
+    if len(b) < off + cnt * dt.itemsize:
+        return None
+    vals = np.frombuffer(data, dt, count=cnt, offset=off).reshape(n[2], n[1], n[0])  # sections, rows, columns
+    # array axis k of vals runs along volume axis ax[2 - k]; order them x, y, z
+    inv = [0, 0, 0]
+    for k in range(3):
+        inv[ax[2 - k]] = k
+    return np.ascontiguousarray((vals > 0).transpose(inv)).astype(np.uint8)

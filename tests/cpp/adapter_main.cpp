@@ -28,7 +28,7 @@ int main(int argc, char** argv) {
         vcgpu::DenseVolume vol{occ.data(), dims[0], dims[1], dims[2]};
         std::vector<std::array<float, 3>> sites;
         vcgpu::Surfacer surf(ctx);
-        surf.extractBoundaryVts(vol, sites);
+        if (surf.extractBoundaryVts(vol, sites) != vcgpu::SurfacerErrCode::SUCCESS) return 1;
         std::vector<std::array<float, 3>> vts;
         std::vector<std::array<int, 2>> edges;
         std::vector<std::array<int, 3>> tris;

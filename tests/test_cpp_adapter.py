@@ -10,12 +10,13 @@ import pytest
 
 ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
 SRC = os.path.join(ROOT, "tests", "cpp", "adapter_main.cpp")
+DROPIN = os.path.join(ROOT, "tests", "cpp", "dropin_main.cpp")
 
 
-def _compile(out, syntax_only=False):
+def _compile(out, syntax_only=False, src=SRC):
     from voxel_ma_gb300 import _lib
     _lib.load()  # builds the library if needed
-    cmd = ["g++", "-std=c++17", "-O2", "-I" + os.path.join(ROOT, "include"), SRC]
+    cmd = ["g++", "-std=c++17", "-O2", "-I" + os.path.join(ROOT, "include"), src]
     if syntax_only:
         cmd += ["-fsyntax-only"]
     else:
@@ -27,6 +28,56 @@ def _compile(out, syntax_only=False):
 @pytest.mark.skipif(shutil.which("g++") is None, reason="no g++")
 def test_adapter_header_compiles():
     _compile(None, syntax_only=True)
+    _compile(None, syntax_only=True, src=DROPIN)
+
+
+def _write_volume(path, occ):
+    with open(path, "wb") as f:
+        f.write(np.array(occ.shape, np.int32).tobytes())
+        f.write(np.ascontiguousarray(occ).tobytes())
+
+
+@pytest.mark.gpu
+@pytest.mark.skipif(shutil.which("g++") is None, reason="no g++")
+def test_reference_style_caller_runs_unchanged(tmp_path):
+    """tests/cpp/dropin_main.cpp calls Surfacer, VoroInfo, cellcomplex,
+    CellComplexThinning (both remainingCC forms) and nClosedComponents as the
+    reference's own callers do, with no GPU context in sight; its results are
+    the oracle's."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import oracle
+    from voxel_ma_gb300 import volumes
+    exe = str(tmp_path / "dropin_main")
+    _compile(exe, src=DROPIN)
+    occ = volumes.csg(11, 24, 40)
+    vol = tmp_path / "vol.bin"
+    _write_volume(vol, occ)
+    t = 0.04
+    from mrc_files import value_volume, write_mrc
+    mrc = tmp_path / "vol.mrc"
+    mrc.write_bytes(write_mrc(value_volume(occ, 2), 2, axes=(3, 1, 2)))
+    out = subprocess.run([exe, str(vol), str(t), str(mrc)], check=True, capture_output=True, text=True).stdout
+    lines = dict(line.split(" ", 1) if " " in line else (line, "") for line in out.strip().splitlines())
+    ref = oracle.run_plain(occ, t=t)
+    vd = ref["vd"]
+    assert int(lines["sites"]) == len(ref["sites"])
+    assert np.float32(float(lines["thresh"])) == np.float32(ref["thresh"])
+    assert [int(x) for x in lines["complex"].split()] == [len(vd["vts"]), len(ref["fin"]["edges"]), len(vd["tris"])]
+    keep_f = np.nonzero(ref["thin"]["keep_f"])[0]
+    assert np.array_equal(np.array(lines["keep_f"].split(), np.int64), keep_f)
+    assert np.array_equal(np.array(lines["from_fi"].split(), np.int64), keep_f)
+    assert np.array_equal(np.array(lines["rem_tris"].split(), np.int32).reshape(-1, 3), ref["rem_tris"])
+    assert np.array_equal(np.array(lines["rem_edges"].split(), np.int32).reshape(-1, 2), ref["rem_edges"])
+    nv, ne, nt = (int(x) for x in lines["remaining"].split())
+    assert (nv, ne, nt) == (len(ref["rem_vts"]), len(ref["rem_edges"]), len(ref["rem_tris"]))
+    cv, ce, ct = (int(x) for x in lines["remaining_cc"].split())
+    assert (cv, ct) == (nv, nt) and ce == len(oracle.finalize_edges(nv, ref["rem_edges"], ref["rem_tris"]))
+    assert int(lines["closed"]) == oracle.closed_components(len(vd["vts"]), vd["edges"], vd["tris"])
+    assert int(lines["radii"]) == len(vd["vts"])
+    assert int(lines["file_sites"]) == len(ref["sites"])
+    assert [int(x) for x in lines["file_complex"].split()] == [len(vd["vts"]), len(vd["edges"]), len(vd["tris"])]
 
 
 @pytest.mark.gpu

@@ -120,6 +120,8 @@ SIGNATURES = {
     "vc_encode_sof": (c_int, [c_vp, c_int, c_int, c_int, c_vp, c_i64, ctypes.POINTER(c_i64)]),
     "vc_encode_sog": (c_int, [c_vp, c_int, c_int, c_int, c_vp, c_i64, ctypes.POINTER(c_i64)]),
     "vc_set_volume_sog": (c_int, [c_vp, c_vp, c_i64, ctypes.POINTER(c_int)]),
+    "vc_set_volume_mrc": (c_int, [c_vp, c_vp, c_i64, c_vp]),
+    "vc_mrc_dims": (c_int, [c_vp, c_i64, c_vp]),
     "vc_get_vox_to_model": (c_int, [c_vp, c_vp]),
     "vc_write_ply": (c_int, [ctypes.c_char_p, c_vp, c_i64, c_vp, c_i64, c_vp, c_i64]),
     "vc_write_radii": (c_int, [ctypes.c_char_p, c_vp, c_vp, c_i64]),

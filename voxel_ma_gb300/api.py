@@ -221,6 +221,15 @@ class Context:
         self.shape = (n, n, n)
         return n
 
+    def set_volume_mrc(self, data: bytes):
+        """Install the map of an .mrc file (vc_set_volume_mrc); returns (X, Y, Z)."""
+        buf = np.frombuffer(data, dtype=np.uint8)
+        dims = np.zeros(3, np.int32)
+        self.check(self.lib.vc_set_volume_mrc(self.h, buf.ctypes.data_as(ctypes.c_void_p), len(buf),
+                                              dims.ctypes.data_as(ctypes.c_void_p)), "vc_set_volume_mrc")
+        self.shape = tuple(int(x) for x in dims)
+        return self.shape
+
     def vox_to_model(self) -> np.ndarray:
         """The installed volume's voxel-to-model matrix, 4x4 (vc_get_vox_to_model)."""
         m = np.zeros(16, np.float64)

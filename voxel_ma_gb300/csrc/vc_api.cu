@@ -70,6 +70,10 @@ int vc_get_volume(vc_ctx* c, uint8_t* occ, int mem) {
 
 int vc_extract_sites(vc_ctx* c, int64_t* n_sites) {
     VC_TRY(enter(c));
+    if (c->n_sites >= 0) {  // the installed volume's sites are already on the device
+        if (n_sites) *n_sites = c->n_sites;
+        return VC_OK;
+    }
     VC_TRY(run_sites(c, n_sites));
     return sync_check(c);
 }
