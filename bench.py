@@ -481,7 +481,7 @@ def run_gpu(args):
     # FP32 measures against FP64 on this workload's complex (outside the timed region)
     line["fp64_check"] = ctx.lambda_fp64_check()
     if not args.no_batch:
-        line["batched"] = run_batched(ctx, dev, args, stream)
+        line["batched"] = run_batched(ctx, dev, args, stream, dist)
         line["config"]["batched_workload"] = line["batched"]["workload"]
     if not args.no_serve and world == 1:
         ctx.close()
@@ -500,6 +500,19 @@ def run_gpu(args):
     return 0
 
 
+def _rem_digest(v, e, t) -> str:
+    import hashlib
+    h = hashlib.sha256()
+    for a in (v, e, t):
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+def _batch_remaining(ctx, res):
+    """Each volume's remaining arrays (host numpy) of the batch in ctx."""
+    return [(x["rem_vts"], x["rem_edges"], x["rem_tris"]) for x in ctx.batch_split(res)]
+
+
 # ---------------------------------------------------------------------------
 # Batched path: 256 random CSG volumes of per-axis sizes log-uniform in
 # [32, 192] through one vc_batch_run per step, against the plain path looping
@@ -508,11 +521,19 @@ def run_gpu(args):
 BATCH_N, BATCH_LO, BATCH_HI = 256, 32, 192
 
 
-def run_batched(ctx, dev, args, stream):
+def run_batched(ctx, dev, args, stream, dist=None):
+    """Under torchrun each rank takes its share of whole volumes
+    (vc_partition_volumes by voxels) and runs it as one batch; value counts
+    every rank's voxels over the slowest rank's time."""
     import torch
 
-    from voxel_ma_gb300 import volumes
-    vols = [volumes.csg(1000 + i, BATCH_LO, BATCH_HI, device=dev) for i in range(BATCH_N)]
+    from voxel_ma_gb300 import api, volumes
+    rank, world, _ = dist_env()
+    plans = [volumes._csg_plan(1000 + i, BATCH_LO, BATCH_HI)[0] for i in range(BATCH_N)]
+    part = api.partition_volumes([int(np.prod(d)) for d in plans], world)
+    mine = [i for i in range(BATCH_N) if part[i] == rank]
+    all_voxels = int(sum(int(np.prod(d)) for d in plans))
+    vols = [volumes.csg(1000 + i, BATCH_LO, BATCH_HI, device=dev) for i in mine]
     dims = np.array([tuple(v.shape) for v in vols], np.int32)
     sizes = [int(np.prod(d)) for d in dims]
     offs = np.concatenate([[0], np.cumsum(sizes)])
@@ -520,7 +541,8 @@ def run_batched(ctx, dev, args, stream):
     del vols
     occ_host = occ_dev.cpu().pin_memory()
     nvox = int(offs[-1])
-    views = [occ_dev[offs[i]:offs[i + 1]].view(*(int(x) for x in dims[i])) for i in range(BATCH_N)]
+    nmine = len(mine)
+    views = [occ_dev[offs[i]:offs[i + 1]].view(*(int(x) for x in dims[i])) for i in range(nmine)]
 
     def batched():
         ctx.batch_set_volumes(occ=occ_dev, dims=dims)
@@ -547,15 +569,25 @@ def run_batched(ctx, dev, args, stream):
 
     for _ in range(args.warmup):
         res = batched()
+    if dist is not None:
+        dist.barrier()
     launches0 = ctx.launch_count()
     res, b_ms = timed(batched, args.steps)
     b_launches = (ctx.launch_count() - launches0) / args.steps
+    b_total = max_over_ranks(sum(b_ms), dist, dev)
     for _ in range(max(1, args.warmup // 2)):
         loop()
     launches0 = ctx.launch_count()
     rem_loop, l_ms = timed(loop, max(1, args.steps // 2))
     l_launches = (ctx.launch_count() - launches0) / max(1, args.steps // 2)
-    same = sum(1 for r, q in zip(res, rem_loop) if r["rem"] == q)
+    # parity: each volume's remaining arrays, batched against its own plain run (digests)
+    same = 0
+    batch_digests = [_rem_digest(*a) for a in _batch_remaining(ctx, res)]
+    for k, v in enumerate(views):
+        ctx.run_plain(v, args.t)
+        same += int(_rem_digest(*ctx.remaining_arrays()) == batch_digests[k])
+    ctx.batch_set_volumes(occ=occ_dev, dims=dims)
+    res = ctx.batch_run(args.t, euler=False)
 
     # end to end: host volumes in, remaining complexes out, every step
     tot = {k: sum(r["rem"][k] for r in res) for k in ("nv", "ne", "nt")}
@@ -577,9 +609,10 @@ def run_batched(ctx, dev, args, stream):
     b_mean, l_mean, e_mean = statistics.mean(b_ms), statistics.mean(l_ms), statistics.mean(e_ms)
     return {
         "workload": f"csg{BATCH_N}_loguniform_{BATCH_LO}_{BATCH_HI}",
-        "volumes": BATCH_N, "voxels": nvox,
-        "value": nvox / (b_mean / 1e3), "unit": UNIT,
-        "volumes_per_s": BATCH_N / (b_mean / 1e3),
+        "volumes": BATCH_N, "voxels": all_voxels,
+        "value": all_voxels / (b_total / args.steps / 1e3), "unit": UNIT,
+        "volumes_per_s": BATCH_N / (b_total / args.steps / 1e3),
+        "ranks": world, "rank0_volumes": nmine, "rank0_voxels": nvox,
         "ms_per_batch": b_mean,
         "latency_ms": {"p50": float(np.percentile(b_ms, 50)), "p99": float(np.percentile(b_ms, 99))},
         "plain_loop": {"value": nvox / (l_mean / 1e3), "volumes_per_s": BATCH_N / (l_mean / 1e3),
@@ -588,7 +621,7 @@ def run_batched(ctx, dev, args, stream):
         "gpu_launches_per_batch": b_launches,
         "e2e": {"value": nvox / (e_mean / 1e3), "unit": UNIT, "h2d_bytes_per_step": nvox,
                 "d2h_bytes_per_step": s["nv"] * 12 + s["ne"] * 8 + s["nt"] * 12, "ms_per_step": e_mean},
-        "parity": f"{same}/{BATCH_N} volumes: batched remaining-complex sizes equal the plain path's",
+        "parity": f"{same}/{nmine} volumes: batched remaining arrays (sha256) equal the plain path's",
         "tuned": tuned,
         "fp64_check": fp64,
         "thin_generations": ctx.batch_stats["generations"],
@@ -605,6 +638,7 @@ def run_batched(ctx, dev, args, stream):
 
 SERVE_RATE, SERVE_SECONDS, SERVE_POOL, SERVE_CAP = 200.0, 6.0, 18, 120 << 30
 SERVE_WORKERS, SERVE_MAX_BATCH = 3, 8
+SERVE_SWEEP, SERVE_SWEEP_SECONDS = (200.0, 400.0, 800.0, 1600.0), 2.0
 
 
 def serve_pool(dev):
@@ -624,19 +658,60 @@ def serve_pool(dev):
     return pool
 
 
-def run_serving(dev, args, workers=None, max_batch=None, with_plain=True):
-    import threading
+def _arrivals(rate: float, seconds: float, npool: int, seed: int):
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate, size=int(rate * seconds * 1.5) + 16)
+    arrivals = np.cumsum(gaps)
+    arrivals = arrivals[arrivals < seconds]
+    return arrivals, rng.integers(0, npool, size=len(arrivals))
 
+
+def _serve_server(srv, pool, t, arrivals, picks, keep_digests=False):
+    ids = []
+    t0 = time.perf_counter()
+    for a, k in zip(arrivals, picks):
+        d = t0 + a - time.perf_counter()
+        if d > 0:
+            time.sleep(d)
+        ids.append(srv.submit(pool[k], t))
+    res = [srv.wait(i) for i in ids]
+    span = time.perf_counter() - t0
+    digests = [_rem_digest(*srv.remaining(i, r)) for i, r in zip(ids, res)] if keep_digests else None
+    for i in ids:
+        srv.release(i)
+    return np.array([r["latency_ms"] for r in res]), span, digests
+
+
+def _serve_plain(ctx, pool, t, arrivals, picks, keep_digests=False):
+    lat, digests = [], []
+    t0 = time.perf_counter()
+    for a, k in zip(arrivals, picks):
+        d = t0 + a - time.perf_counter()
+        if d > 0:
+            time.sleep(d)
+        ctx.run_plain(pool[k], t)
+        arr = ctx.remaining_arrays()
+        lat.append((time.perf_counter() - (t0 + a)) * 1e3)
+        if keep_digests:
+            digests.append(_rem_digest(*arr))
+    return np.array(lat), time.perf_counter() - t0, (digests if keep_digests else None)
+
+
+def _summary(lat, span, n):
+    return {"throughput_req_s": n / span, "latency_ms": {"p50": float(np.percentile(lat, 50)),
+                                                         "p99": float(np.percentile(lat, 99))}}
+
+
+def run_serving(dev, args, workers=None, max_batch=None, with_plain=True, sweep=True):
+    """Poisson arrivals at SERVE_RATE req/s for SERVE_SECONDS, served by the
+    request loop and by one plain context first come first served (same
+    arrivals, same volumes); then a sweep of offered rates (SERVE_SWEEP, a
+    shorter window each) to the knee of both: the highest offered rate each
+    keeps up with, and its p99 there."""
     from voxel_ma_gb300 import api
     pool = serve_pool(dev)
-    rng = np.random.default_rng(7)
-    gaps = rng.exponential(1.0 / SERVE_RATE, size=int(SERVE_RATE * SERVE_SECONDS * 1.5))
-    arrivals = np.cumsum(gaps)
-    arrivals = arrivals[arrivals < SERVE_SECONDS]
-    picks = rng.integers(0, len(pool), size=len(arrivals))
+    arrivals, picks = _arrivals(SERVE_RATE, SERVE_SECONDS, len(pool), 7)
     voxels = np.array([pool[k].size for k in picks], np.int64)
-
-    # continuous batching
     workers = workers or SERVE_WORKERS
     max_batch = max_batch or SERVE_MAX_BATCH
     srv = api.Server(dev.index or 0, workers=workers, mem_cap_bytes=SERVE_CAP, max_batch=max_batch)
@@ -644,60 +719,55 @@ def run_serving(dev, args, workers=None, max_batch=None, with_plain=True):
     for i in warm:
         srv.wait(i)
         srv.release(i)
-    ids = []
-    t0 = time.perf_counter()
-    for a, k in zip(arrivals, picks):
-        d = t0 + a - time.perf_counter()
-        if d > 0:
-            time.sleep(d)
-        ids.append(srv.submit(pool[k], args.t))
-    res = [srv.wait(i) for i in ids]
-    t_end = time.perf_counter()
-    rem_srv = [r["rem"] for r in res]
-    for i in ids:
-        srv.release(i)
+    b0 = srv.stats()["batches"]
+    lat, span, dig_srv = _serve_server(srv, pool, args.t, arrivals, picks, keep_digests=with_plain)
     st = srv.stats()
-    srv.close()
-    lat = np.array([r["latency_ms"] for r in res])
-    span = t_end - t0
+    n = len(arrivals)
     if not with_plain:
-        return {"workers": workers, "max_batch": max_batch, "throughput_req_s": len(arrivals) / span,
-                "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
-                "batches": st["batches"] - SERVE_POOL}
-
-    # the plain path: one context, first come first served, same arrivals
+        srv.close()
+        out = {"workers": workers, "max_batch": max_batch, "batches": st["batches"] - b0}
+        out.update(_summary(lat, span, n))
+        return out
     ctx = api.Context(dev.index or 0)
     for k in range(len(pool)):
         ctx.run_plain(pool[k], args.t)
-    plain_lat, rem_plain = [], []
-    t0 = time.perf_counter()
-    for a, k in zip(arrivals, picks):
-        d = t0 + a - time.perf_counter()
-        if d > 0:
-            time.sleep(d)
-        r = ctx.run_plain(pool[k], args.t)
-        ctx.remaining_arrays()
-        plain_lat.append((time.perf_counter() - (t0 + a)) * 1e3)
-        rem_plain.append(r["rem"])
-    p_span = time.perf_counter() - t0
-    ctx.close()
-    plain_lat = np.array(plain_lat)
-    same = sum(1 for a, b in zip(rem_srv, rem_plain) if a == b)
-    n = len(arrivals)
-    return {
+    plat, pspan, dig_plain = _serve_plain(ctx, pool, args.t, arrivals, picks, keep_digests=True)
+    same = sum(1 for a, b in zip(dig_srv, dig_plain) if a == b)
+    out = {
         "workload": f"poisson{int(SERVE_RATE)}_torus_spheres_grf_edge32_384",
         "arrival_rate_req_s": SERVE_RATE, "requests": n, "duration_s": SERVE_SECONDS,
         "pool": f"{SERVE_POOL} volumes (torus mesh, 32 spheres, GRF sigma 6), edge log-uniform in [32, 384]",
         "mem_cap_bytes": SERVE_CAP, "workers": workers, "max_batch": max_batch,
-        "value": float(voxels.sum() / span), "unit": UNIT, "throughput_req_s": n / span,
-        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
-        "batches": st["batches"] - SERVE_POOL,  # the warm-up served each pool volume alone
+        "value": float(voxels.sum() / span), "unit": UNIT,
+        "batches": st["batches"] - b0,
         "device_bytes_end": st["device_bytes"],
-        "plain": {"value": float(voxels.sum() / p_span), "throughput_req_s": n / p_span,
-                  "latency_ms": {"p50": float(np.percentile(plain_lat, 50)),
-                                 "p99": float(np.percentile(plain_lat, 99))}},
-        "parity": f"{same}/{n} requests: remaining-complex sizes equal the plain path's",
+        "plain": {"value": float(voxels.sum() / pspan)},
+        "parity": f"{same}/{n} requests: remaining arrays (sha256) equal the plain path's",
     }
+    out.update(_summary(lat, span, n))
+    out["plain"].update(_summary(plat, pspan, n))
+    if sweep:
+        rows = []
+        for rate in SERVE_SWEEP:
+            arr, pk = _arrivals(rate, SERVE_SWEEP_SECONDS, len(pool), 11)
+            sl, ss, _ = _serve_server(srv, pool, args.t, arr, pk)
+            pl, ps, _ = _serve_plain(ctx, pool, args.t, arr, pk)
+            rows.append({"offered_req_s": rate, "requests": len(arr),
+                         "server": _summary(sl, ss, len(arr)), "plain": _summary(pl, ps, len(arr))})
+
+        def knee(side):
+            # the highest offered rate served at >= 95 % of the offer
+            ok = [r for r in rows if r[side]["throughput_req_s"] >= 0.95 * r["offered_req_s"]]
+            best = max(ok, key=lambda r: r["offered_req_s"]) if ok else None
+            return {"offered_req_s": best["offered_req_s"], "p99_ms": best[side]["latency_ms"]["p99"]} if best \
+                else None
+        out["sweep"] = {"window_s": SERVE_SWEEP_SECONDS, "rows": rows,
+                        "knee": {"server": knee("server"), "plain": knee("plain")},
+                        "max_throughput_req_s": {"server": max(r["server"]["throughput_req_s"] for r in rows),
+                                                 "plain": max(r["plain"]["throughput_req_s"] for r in rows)}}
+    ctx.close()
+    srv.close()
+    return out
 
 
 # DRAM traffic per cell of the complex (V + E + T) of the thinning kernel,

@@ -310,6 +310,19 @@ typedef struct {
     int64_t submitted, completed, failed, refused, batches, pending, device_bytes;
 } vc_server_stats;
 int vc_server_create(vc_server** server, int device, int workers, int64_t mem_cap_bytes, int max_batch);
+/* The same server over several GPUs: workers_per_device workers on each of
+ * devices[0..ndev), each device with its own memory cap; a free worker on
+ * any device takes the next batch, so whole volumes go to whichever GPU is
+ * free (a volume is never split across GPUs; the reference thins one volume
+ * per process).  vc_server_create(dev, w, cap, b) is this with one device. */
+int vc_server_create_devices(vc_server** server, const int* devices, int ndev, int workers_per_device,
+                             int64_t mem_cap_per_device, int max_batch);
+/* Whole volumes to nparts parts (GPUs or ranks) by voxels, largest first to
+ * the part with the fewest voxels so far (lowest part on ties); part_of[i]
+ * receives volume i's part.  Host code, no context.  Each part runs its
+ * share as one batch; the union of the parts' results equals the result of
+ * the whole set, volume by volume.                                         */
+int vc_partition_volumes(int n, const int64_t* voxels, int nparts, int32_t* part_of);
 int vc_server_set_bytes_per_voxel(vc_server* server, double bytes_per_voxel);
 int vc_server_submit(vc_server* server, const uint8_t* occ, int X, int Y, int Z, double t, int64_t* request_id);
 /* Blocks until the request is served (timeout_s < 0: no limit; a host-side

@@ -49,6 +49,11 @@ private:
     std::vector<uint8_t> v_;
 };
 
+static int fail(const char* what) {
+    std::cerr << "failed: " << what << "\n";
+    return 1;
+}
+
 int main(int argc, char** argv) {
     if (argc < 3) {
         std::cerr << "usage: dropin_main volume.bin t [same-volume.mrc]\n";
@@ -65,9 +70,10 @@ int main(int argc, char** argv) {
         // sites (Surfacer::extractBoundaryVts)
         Surfacer surf;
         std::vector<point> sites;
-        if (surf.extractBoundaryVts(vol, sites) != SurfacerErrCode::SUCCESS) return 1;
+        if (surf.extractBoundaryVts(vol, sites) != SurfacerErrCode::SUCCESS) return fail("extractBoundaryVts");
         std::shared_ptr<Volume3DScalar> empty;
-        if (surf.extractBoundaryVts(empty, sites) != SurfacerErrCode::EMPTY_VOL) return 1;
+        std::vector<point> none_sites;
+        if (surf.extractBoundaryVts(empty, none_sites) != SurfacerErrCode::EMPTY_VOL) return fail("EMPTY_VOL");
         // the inside part with measures (VoroInfo::extractInsideWithMeasure)
         VoroInfo voro(vol);
         std::vector<point> vts;
@@ -107,14 +113,14 @@ int main(int argc, char** argv) {
         if (argc > 3) {
             // the same volume as a file, through readVolume (importers.h)
             std::shared_ptr<GpuVolume> fv;
-            if (readVolume(argv[3], fv) != ImportErrCode::SUCCESS) return 1;
+            if (readVolume(argv[3], fv) != ImportErrCode::SUCCESS) return fail("readVolume");
             std::vector<point> fsites;
-            if (surf.extractBoundaryVts(fv, fsites) != SurfacerErrCode::SUCCESS) return 1;
+            if (surf.extractBoundaryVts(fv, fsites) != SurfacerErrCode::SUCCESS) return fail("extractBoundaryVts(file)");
             VoroInfo fvoro(fv);
             std::printf("file_sites %zu\nfile_complex %lld %lld %lld\n", fsites.size(), (long long)fvoro.sizes().nv,
                         (long long)fvoro.sizes().ne, (long long)fvoro.sizes().nt);
             std::shared_ptr<GpuVolume> none;
-            if (readVolume("no_such_file.mrc", none) != ImportErrCode::NOOPENINPUT) return 1;
+            if (readVolume("no_such_file.mrc", none) != ImportErrCode::NOOPENINPUT) return fail("NOOPENINPUT");
         }
         std::printf("keep_f");
         for (int i : kf) std::printf(" %d", i);
@@ -126,7 +132,7 @@ int main(int argc, char** argv) {
         for (const auto& e : re) std::printf(" %d %d", e[0], e[1]);
         std::printf("\n");
     } catch (const Error& e) {
-        std::cerr << e.what() << "\n";
+        std::cerr << "vcgpu::Error: " << e.what() << "\n";
         return 1;
     }
     return 0;

@@ -58,7 +58,9 @@ def test_reference_style_caller_runs_unchanged(tmp_path):
     from mrc_files import value_volume, write_mrc
     mrc = tmp_path / "vol.mrc"
     mrc.write_bytes(write_mrc(value_volume(occ, 2), 2, axes=(3, 1, 2)))
-    out = subprocess.run([exe, str(vol), str(t), str(mrc)], check=True, capture_output=True, text=True).stdout
+    run = subprocess.run([exe, str(vol), str(t), str(mrc)], capture_output=True, text=True)
+    assert run.returncode == 0, run.stderr
+    out = run.stdout
     lines = dict(line.split(" ", 1) if " " in line else (line, "") for line in out.strip().splitlines())
     ref = oracle.run_plain(occ, t=t)
     vd = ref["vd"]

@@ -98,6 +98,8 @@ SIGNATURES = {
     "vc_server_release": (c_int, [c_vp, c_i64]),
     "vc_server_get_stats": (c_int, [c_vp, ctypes.POINTER(ServerStats)]),
     "vc_server_destroy": (c_int, [c_vp]),
+    "vc_server_create_devices": (c_int, [c_vp, c_vp, c_int, c_int, c_i64, c_int]),
+    "vc_partition_volumes": (c_int, [c_int, c_vp, c_int, c_vp]),
     "vc_server_debug_fail_alloc_after": (c_int, [c_vp, c_i64]),
     "vc_plan_batches": (c_int, [c_int, c_vp, c_vp, c_i64, ctypes.c_double, c_int, c_vp]),
     "vc_set_complex": (c_int, [c_vp, c_i64, c_vp, c_i64, c_vp, c_i64, c_vp, c_int]),

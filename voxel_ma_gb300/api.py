@@ -453,13 +453,16 @@ class Context:
 class Server:
     """The request loop (vc_server_*): submit host volumes, wait for results."""
 
-    def __init__(self, device: int = 0, workers: int = 2, mem_cap_bytes: int = 120 << 30, max_batch: int = 64,
+    def __init__(self, device=0, workers: int = 2, mem_cap_bytes: int = 120 << 30, max_batch: int = 64,
                  bytes_per_voxel: Optional[float] = None):
+        """device: one GPU, or a list of GPUs (workers and mem_cap_bytes are then per GPU)."""
         self.lib = L.load()
         h = ctypes.c_void_p()
-        st = self.lib.vc_server_create(ctypes.byref(h), device, workers, mem_cap_bytes, max_batch)
+        devs = np.array(device if isinstance(device, (list, tuple)) else [device], np.int32)
+        st = self.lib.vc_server_create_devices(ctypes.byref(h), devs.ctypes.data_as(ctypes.c_void_p), len(devs),
+                                               workers, mem_cap_bytes, max_batch)
         if st != L.VC_OK:
-            raise L.VoxelCoreError(st, "vc_server_create", "")
+            raise L.VoxelCoreError(st, "vc_server_create_devices", "")
         self.h = h
         if bytes_per_voxel is not None:
             self._check(self.lib.vc_server_set_bytes_per_voxel(self.h, float(bytes_per_voxel)),
@@ -595,6 +598,15 @@ def dotma_edges(edges, tris) -> np.ndarray:
     _call("vc_dotma_edges", pe, len(e), pt, len(t), None, 0, ctypes.byref(n))
     out = np.zeros((n.value, 2), np.int32)
     _call("vc_dotma_edges", pe, len(e), pt, len(t), out.ctypes.data_as(ctypes.c_void_p), n.value, ctypes.byref(n))
+    return out
+
+
+def partition_volumes(voxels, nparts: int) -> np.ndarray:
+    """Part (GPU or rank) of each volume: vc_partition_volumes."""
+    v = np.ascontiguousarray(voxels, dtype=np.int64)
+    out = np.zeros(len(v), np.int32)
+    _call("vc_partition_volumes", len(v), v.ctypes.data_as(ctypes.c_void_p), nparts,
+          out.ctypes.data_as(ctypes.c_void_p))
     return out
 
 

@@ -17,6 +17,7 @@
 // submission.
 #include "vc_internal.cuh"
 
+#include <algorithm>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -53,14 +54,14 @@ struct Request {
 }  // namespace
 
 struct vc_server {
-    int device = 0;
+    std::vector<int> devices;  // worker w runs on devices[w % devices.size()]
     int nworkers = 1;
-    int64_t cap = 0, share = 0;
+    int64_t cap = 0, share = 0;  // cap per device; share = a worker's part of its device's cap
     int max_batch = 1;
     double bytes_per_voxel = 640.0;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
-    std::mutex thin_lock;
+    std::vector<std::unique_ptr<std::mutex>> thin_locks;  // one per device
     std::deque<Request*> pending;
     std::unordered_map<int64_t, std::unique_ptr<Request>> reqs;
     int64_t next_id = 1;
@@ -203,7 +204,7 @@ void serve_batch(vc_server* s, vc_ctx* c, std::vector<Request*>& batch, Staging&
 
 void worker_main(vc_server* s, int w) {
     vc_ctx* c = s->ctxs[w];
-    cudaSetDevice(s->device);
+    cudaSetDevice(c->device);
     Staging stage;
     for (;;) {
         std::vector<Request*> batch;
@@ -249,30 +250,61 @@ void worker_main(vc_server* s, int w) {
 
 extern "C" {
 
-int vc_server_create(vc_server** out, int device, int workers, int64_t mem_cap_bytes, int max_batch) {
-    if (!out || workers <= 0 || workers > 16 || mem_cap_bytes <= 0 || max_batch <= 0) return VC_ERR_ARG;
+int vc_server_create_devices(vc_server** out, const int* devices, int ndev, int workers_per_device,
+                             int64_t mem_cap_per_device, int max_batch) {
+    if (!out || !devices || ndev <= 0 || ndev > 64 || workers_per_device <= 0 || workers_per_device > 16 ||
+        mem_cap_per_device <= 0 || max_batch <= 0)
+        return VC_ERR_ARG;
     *out = nullptr;
     auto s = std::make_unique<vc_server>();
-    s->device = device;
-    s->nworkers = workers;
-    s->cap = mem_cap_bytes;
-    s->share = mem_cap_bytes / workers;
+    s->devices.assign(devices, devices + ndev);
+    s->nworkers = ndev * workers_per_device;
+    s->cap = mem_cap_per_device;
+    s->share = mem_cap_per_device / workers_per_device;
     s->max_batch = max_batch;
-    for (int w = 0; w < workers; ++w) {
+    for (int d = 0; d < ndev; ++d) s->thin_locks.push_back(std::make_unique<std::mutex>());
+    for (int w = 0; w < s->nworkers; ++w) {
         vc_ctx* c = nullptr;
-        const int st = vc_ctx_create(&c, device);
+        const int st = vc_ctx_create(&c, devices[w % ndev]);
         if (st != VC_OK) {
             for (vc_ctx* x : s->ctxs) vc_ctx_destroy(x);
             return st;
         }
-        // the workers' persistent thinning kernels each take the whole GPU,
-        // one at a time; their other stages overlap freely
-        c->thin_lock = &s->thin_lock;
+        // the persistent thinning kernels of one device's workers each take
+        // the whole GPU, one at a time; their other stages overlap freely
+        c->thin_lock = s->thin_locks[w % ndev].get();
         s->ctxs.push_back(c);
     }
     vc_server* raw = s.release();
-    for (int w = 0; w < workers; ++w) raw->threads.emplace_back(worker_main, raw, w);
+    for (int w = 0; w < raw->nworkers; ++w) raw->threads.emplace_back(worker_main, raw, w);
     *out = raw;
+    return VC_OK;
+}
+
+int vc_server_create(vc_server** out, int device, int workers, int64_t mem_cap_bytes, int max_batch) {
+    return vc_server_create_devices(out, &device, 1, workers, mem_cap_bytes, max_batch);
+}
+
+int vc_partition_volumes(int n, const int64_t* voxels, int nparts, int32_t* part_of) {
+    // Whole volumes to parts (devices or ranks), largest first, each to the
+    // part with the fewest voxels so far (the lowest part on ties).  Volumes
+    // are independent, so every part runs its share as one batch and the
+    // union of the parts' results is the result of the whole set.
+    if (n < 0 || nparts <= 0 || (n > 0 && (!voxels || !part_of))) return VC_ERR_ARG;
+    std::vector<int> order((size_t)n);
+    for (int i = 0; i < n; ++i) {
+        if (voxels[i] < 0) return VC_ERR_ARG;
+        order[(size_t)i] = i;
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return voxels[a] > voxels[b]; });
+    std::vector<int64_t> load((size_t)nparts, 0);
+    for (const int i : order) {
+        int best = 0;
+        for (int p = 1; p < nparts; ++p)
+            if (load[(size_t)p] < load[(size_t)best]) best = p;
+        part_of[i] = best;
+        load[(size_t)best] += voxels[i];
+    }
     return VC_OK;
 }
 
