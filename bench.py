@@ -279,6 +279,7 @@ def run_gpu(args):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
 
+    scaling = CpuScaling(args.t) if (rank == 0 and not args.no_cpu_baseline and not args.no_cpu_scaling) else None
     occ_np, workload = make_workload(args.workload, device=dev if args.workload.startswith("grf") else None)
     from voxel_ma_gb300 import volumes
     occ_sha = volumes.occupancy_sha256(occ_np)
@@ -492,6 +493,8 @@ def run_gpu(args):
         times = [cpu_path_once(occ_s, args.t) for _ in range(2)]
         line["cpu_baseline"] = {"value": occ_s.size / min(times), "unit": UNIT, "cores": 1, "kind": "port",
                                 "sample": sample + "; best of 2 runs of the oracle restatement"}
+        if scaling is not None:
+            line["cpu_baseline"]["scaling"] = scaling.collect()
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()
@@ -782,6 +785,56 @@ L2_REQUESTS_PER_CELL = {"thin_generations": (78454799 + 48482036 + 26165270) / (
 PROBE_BYTES = 16 << 30
 
 
+# ---------------------------------------------------------------------------
+# How the CPU path's voxels/s changes with the volume's size: single-threaded
+# oracle runs at 128^3, 256^3 and 512^3 in a child process that runs beside
+# the GPU measurements (one host core; its results are read at the end).
+
+CPU_SCALING_SIZES = (128, 256, 512)
+CPU_SCALING_WAIT_S = 720.0  # from the bench's start; sizes not done by then are reported unfinished
+
+
+def cpu_scaling_child(path: str, t: float) -> int:
+    import oracle
+    from voxel_ma_gb300 import volumes
+    oracle.build(reference=False)
+    for n in CPU_SCALING_SIZES:
+        occ = volumes.grf(n, sigma=6.0, seed=0)
+        t0 = time.perf_counter()
+        r = oracle.run_plain(occ, t=t, threads=1)
+        dt = time.perf_counter() - t0
+        rec = {"edge": n, "voxels": int(occ.size), "seconds": dt, "voxels_per_s": occ.size / dt,
+               "processed_pairs": int(r["thin"]["stats"]["processed"])}
+        del r
+        with open(path, "a") as f:
+            f.write(json.dumps(rec) + "\n")
+    return 0
+
+
+class CpuScaling:
+    """The child process running the scaling points (rank 0 only)."""
+
+    def __init__(self, t: float):
+        self.path = tempfile.NamedTemporaryFile("w", suffix=".jsonl", delete=False).name
+        self.t0 = time.time()
+        self.p = subprocess.Popen([sys.executable, os.path.abspath(__file__), "--cpu-scaling-child", self.path,
+                                   "--t", str(t)], stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+
+    def collect(self) -> dict:
+        try:
+            self.p.wait(timeout=max(1.0, CPU_SCALING_WAIT_S - (time.time() - self.t0)))
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+            self.p.wait()
+        rows = [json.loads(x) for x in open(self.path) if x.strip()]
+        os.unlink(self.path)
+        done = {r["edge"] for r in rows}
+        return {"kind": "port", "cores": 1, "workload": "GRF sigma=6 level 0, seed 0, same generator as the GPU "
+                "workload", "points": rows,
+                "unfinished": [n for n in CPU_SCALING_SIZES if n not in done],
+                "note": "oracle restatement of the reference path, one thread, run beside the GPU measurements"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -798,7 +851,11 @@ def main():
                     help="skip the random-access probe and the topology and octree measurements")
     ap.add_argument("--ft-method", choices=["envelope", "window"], default=None,
                     help="with --no-tune: the feature transform's method for the plain path")
+    ap.add_argument("--no-cpu-scaling", action="store_true", help="skip the CPU path's size-scaling points")
+    ap.add_argument("--cpu-scaling-child", default=None, help=argparse.SUPPRESS)
     args = ap.parse_args()
+    if args.cpu_scaling_child:
+        return cpu_scaling_child(args.cpu_scaling_child, args.t)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

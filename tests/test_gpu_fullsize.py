@@ -78,13 +78,13 @@ def test_full_size_stages_bit_exact(gpu_ctx, name):
     assert [r["vd"]["nv"], r["vd"]["ne"], r["vd"]["nt"]] == d["vd_sizes"]
     assert r["vd"]["inside_size"] == d["inside_size"]
     assert r["thresh"] == d["thresh"]
-    # the pairs popped and processed, and the queue's generations (the GPU
-    # drops, instead of pushing, a child whose cell goes in the same
-    # generation: the reference pops and skips it, so pushes and skips differ
-    # by those while processed pairs match)
-    for k in ("processed", "generations"):
-        assert r["thin"][k] == d["thin_stats"][k], k
+    # the pairs popped and processed (the GPU drops, instead of pushing, a
+    # child whose cell goes in the same generation: the reference pops and
+    # skips it, so pushes, skips and a trailing generation of skips only can
+    # differ while the processed pairs match)
+    assert r["thin"]["processed"] == d["thin_stats"]["processed"]
     assert r["thin"]["pushes"] - r["thin"]["skipped"] == r["thin"]["processed"]
+    assert r["thin"]["generations"] <= d["thin_stats"]["generations"]
     fl = ctx.thin_flags()
     for k in ("keep_v", "keep_e", "keep_f", "removed_e"):
         assert _digest(_flags01(fl[k])) == d[k], k

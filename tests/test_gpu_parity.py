@@ -328,3 +328,25 @@ def test_closed_components_lattice(gpu_ctx, name, occ):
     fl = ctx.thin_flags()
     for k in ("keep_v", "keep_e", "keep_f"):
         assert np.array_equal(fl[k], r[k]), k
+
+
+def test_remaining_is_idempotent(gpu_ctx):
+    """vc_remaining called again after the same thinning returns the same
+    complex (the reference's remainingCC can be called any number of times)."""
+    ctx = gpu_ctx
+    vts, edges, tris = grid_surface(12, 9, seed=3, drop=0.2, extra_edges=8)
+    fin = O.finalize(len(vts), edges, tris)
+    _, em, fm = random_measures(len(fin["edges"]), len(tris), seed=3, levels=3)
+    ctx.set_complex(vts, edges, tris)
+    ctx.finalize()
+    ctx.set_measures(np.zeros(len(vts), np.float32), em, fm)
+    ctx.thin(1.0, 1.0)
+    first = (ctx.remaining(), *ctx.remaining_arrays())
+    for _ in range(2):
+        again = (ctx.remaining(), *ctx.remaining_arrays())
+        assert again[0] == first[0]
+        for a, b in zip(again[1:], first[1:]):
+            assert np.array_equal(a, b)
+    r = O.thin(len(vts), edges, tris, em, fm, 1.0, 1.0)
+    rv, re_, rt = O.remaining(vts, fin["edges"], tris, r["keep_v"], r["keep_e"], r["keep_f"])
+    assert np.array_equal(first[1], rv) and np.array_equal(first[2], re_) and np.array_equal(first[3], rt)

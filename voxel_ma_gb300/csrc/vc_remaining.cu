@@ -213,6 +213,10 @@ Kept kept_of(vc_ctx* c) {
 
 int run_remaining(vc_ctx* c, vc_rem_sizes* sizes) {
     if (!c->thin_valid) return VC_ERR_STATE;
+    if (c->rem_valid) {  // this thinning's remaining complex is built already (the word scans below are in place)
+        if (sizes) *sizes = c->rem;
+        return VC_OK;
+    }
     const int64_t nv = c->nv, ne = c->ne, nt = c->nt;
     const int64_t nwv = (nv + 31) / 32, nwe = (ne + 31) / 32, nwf = (nt + 31) / 32;
     VC_TRY(ensure_n<int64_t>(c, c->scratch2, 4));
