@@ -791,7 +791,7 @@ PROBE_BYTES = 16 << 30
 # the GPU measurements (one host core; its results are read at the end).
 
 CPU_SCALING_SIZES = (128, 256, 512)
-CPU_SCALING_WAIT_S = 720.0  # from the bench's start; sizes not done by then are reported unfinished
+CPU_SCALING_WAIT_S = 480.0  # from the bench's start; sizes not done by then are reported unfinished
 
 
 def cpu_scaling_child(path: str, t: float) -> int:
