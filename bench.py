@@ -585,6 +585,8 @@ def run_batched(ctx, dev, args, stream, dist=None):
     l_launches = (ctx.launch_count() - launches0) / max(1, args.steps // 2)
     # parity: each volume's remaining arrays, batched against its own plain run (digests)
     same = 0
+    ctx.batch_set_volumes(occ=occ_dev, dims=dims)
+    res = ctx.batch_run(args.t, euler=False)
     batch_digests = [_rem_digest(*a) for a in _batch_remaining(ctx, res)]
     for k, v in enumerate(views):
         ctx.run_plain(v, args.t)
@@ -726,16 +728,21 @@ def run_serving(dev, args, workers=None, max_batch=None, with_plain=True, sweep=
     lat, span, dig_srv = _serve_server(srv, pool, args.t, arrivals, picks, keep_digests=with_plain)
     st = srv.stats()
     n = len(arrivals)
+    # the digests of the server's results are taken after its timed run; the
+    # plain results they are compared with come from one plain run per pool
+    # volume (a volume's result does not depend on when it runs)
     if not with_plain:
         srv.close()
         out = {"workers": workers, "max_batch": max_batch, "batches": st["batches"] - b0}
         out.update(_summary(lat, span, n))
         return out
     ctx = api.Context(dev.index or 0)
+    pool_digest = []
     for k in range(len(pool)):
         ctx.run_plain(pool[k], args.t)
-    plat, pspan, dig_plain = _serve_plain(ctx, pool, args.t, arrivals, picks, keep_digests=True)
-    same = sum(1 for a, b in zip(dig_srv, dig_plain) if a == b)
+        pool_digest.append(_rem_digest(*ctx.remaining_arrays()))
+    plat, pspan, _ = _serve_plain(ctx, pool, args.t, arrivals, picks)
+    same = sum(1 for a, k in zip(dig_srv, picks) if a == pool_digest[k])
     out = {
         "workload": f"poisson{int(SERVE_RATE)}_torus_spheres_grf_edge32_384",
         "arrival_rate_req_s": SERVE_RATE, "requests": n, "duration_s": SERVE_SECONDS,

@@ -7,7 +7,8 @@ Workloads:
   torus64        the closed triangle-mesh torus voxelized to 64^3;
   spheres256_s*  unions of 32 spheres at 256^3, seeds 0, 1, 2;
   grf512         the thresholded smoothed random field at 512^3 (sigma 6,
-                 level 0, seed 0): the benchmark's own workload.
+                 level 0, seed 0): the benchmark's own workload;
+  grf1024        the same field at 1024^3: sites and feature transform only.
 
 For torus64 and the sphere unions the reference's OWN compiled thinning and
 remainingCC (oracle/_ref, built from the reference tree) are also run on the
@@ -48,7 +49,12 @@ def workloads():
         "spheres256_s1": (lambda: volumes.spheres(256, count=32, seed=1), True),
         "spheres256_s2": (lambda: volumes.spheres(256, count=32, seed=2), True),
         "grf512": (lambda: volumes.grf(512, sigma=6.0, seed=0), False),
+        # sites and feature transform only: the complex of this volume (about
+        # 2.5e9 cells) is beyond 32-bit cell ids and one GPU's memory
+        "grf1024": (lambda: volumes.grf(1024, sigma=6.0, seed=0), False),
     }
+
+FT_ONLY = {"grf1024"}
 
 
 def digest(*arrays) -> str:
@@ -62,7 +68,21 @@ def flags01(a) -> np.ndarray:
     return (np.asarray(a) != 0).astype(np.uint8)
 
 
+def run_ft_case(name: str, gen) -> dict:
+    t0 = time.time()
+    occ = np.ascontiguousarray(gen())
+    xyz, li = oracle.extract_sites(occ)
+    d2, ids = oracle.ft(occ.shape, li, threads=os.cpu_count() or 1)
+    out = {"shape": list(occ.shape), "stages": "sites+ft", "occupancy_sha256": volumes.occupancy_sha256(occ),
+           "n_sites": int(len(xyz)), "sites": digest(xyz), "ft": digest(d2, ids),
+           "oracle_seconds": round(time.time() - t0, 1)}
+    print(name, json.dumps(out), flush=True)
+    return out
+
+
 def run_case(name: str, gen, with_ref: bool) -> dict:
+    if name in FT_ONLY:
+        return run_ft_case(name, gen)
     t0 = time.time()
     occ = np.ascontiguousarray(gen())
     r = oracle.run_plain(occ, T, threads=os.cpu_count() or 1)

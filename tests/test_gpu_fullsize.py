@@ -1,6 +1,6 @@
 """The full-size workloads, bit for bit: the 64^3 torus, the 32-sphere unions at
 256^3 (seeds 0, 1, 2) and the 512^3 thresholded random field that the
-benchmark times.
+benchmark times; at 1024^3, the sites and the feature transform.
 
 The CPU oracle's outputs at these sizes take minutes and tens of GB of host
 memory, so tests/golden/make_fullsize_digests.py ran it once and committed
@@ -50,9 +50,13 @@ def _volume(name):
         return volumes.torus_mesh(64)
     if name.startswith("spheres256_s"):
         return volumes.spheres(256, count=32, seed=int(name[len("spheres256_s"):]))
-    if name == "grf512":
-        return volumes.grf(512, sigma=6.0, seed=0, device=torch.device("cuda"))
+    if name in ("grf512", "grf1024"):
+        return volumes.grf(int(name[3:]), sigma=6.0, seed=0, device=torch.device("cuda"))
     raise KeyError(name)
+
+
+FULL = sorted(k for k, v in DIGESTS.items() if "stages" not in v)
+FT_ONLY = sorted(k for k, v in DIGESTS.items() if v.get("stages") == "sites+ft")
 
 
 @pytest.fixture(scope="module")
@@ -65,7 +69,25 @@ def grf512():
     return occ
 
 
-@pytest.mark.parametrize("name", sorted(DIGESTS))
+@pytest.mark.parametrize("name", FT_ONLY)
+def test_sites_and_transform_at_1024(name):
+    """The 1024^3 field (1.08e9 lattice points, 1.3e8 sites): site list and
+    feature transform bit for bit.  Its complex (about 2.5e9 cells) exceeds
+    32-bit cell ids and one GPU's memory, so the path stops there."""
+    from voxel_ma_gb300 import api
+    d = DIGESTS[name]
+    occ = _volume(name)
+    assert volumes.occupancy_sha256(occ) == d["occupancy_sha256"]
+    with api.Context(0) as ctx:
+        ctx.set_volume(occ)
+        del occ
+        assert ctx.extract_sites() == d["n_sites"]
+        assert _digest(ctx.sites()) == d["sites"]
+        ctx.feature_transform()
+        assert _digest(*ctx.ft()) == d["ft"]
+
+
+@pytest.mark.parametrize("name", FULL)
 def test_full_size_stages_bit_exact(gpu_ctx, name):
     ctx = gpu_ctx
     d = DIGESTS[name]

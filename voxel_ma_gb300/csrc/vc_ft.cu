@@ -208,9 +208,8 @@ __global__ void __launch_bounds__(kWinThreads) ft_window_kernel(const int64_t* _
                     far = true;
                     break;
                 }
-                const int64_t add = r2 << 32;
-                best = min(best, svj[(qm - r) & kMask] + add);
-                best = min(best, svj[(qm + r) & kMask] + add);
+                // both candidates r away get the same r^2: one add for the pair
+                best = min(best, min(svj[(qm - r) & kMask], svj[(qm + r) & kMask]) + (r2 << 32));
             }
             if (far) s_far = 1;
             else emit_at(s_base[j] + (int64_t)q * s_stride[j], best);
@@ -282,19 +281,12 @@ __global__ void __launch_bounds__(kWinThreads) ft_window_kernel(const int64_t* _
                     const int64_t* c = sv + qm;
                     best = c[0];
 #pragma unroll
-                    for (int r = 1; r <= kWinNear; ++r) {
-                        const int64_t add = (int64_t)(r * r) << 32;
-                        best = min(best, c[-r] + add);
-                        best = min(best, c[r] + add);
-                    }
+                    for (int r = 1; r <= kWinNear; ++r) best = min(best, min(c[-r], c[r]) + ((int64_t)(r * r) << 32));
                 } else {
                     best = sv[qm];
 #pragma unroll
-                    for (int r = 1; r <= kWinNear; ++r) {
-                        const int64_t add = (int64_t)(r * r) << 32;
-                        best = min(best, sv[(qm - r) & kMask] + add);
-                        best = min(best, sv[(qm + r) & kMask] + add);
-                    }
+                    for (int r = 1; r <= kWinNear; ++r)
+                        best = min(best, min(sv[(qm - r) & kMask], sv[(qm + r) & kMask]) + ((int64_t)(r * r) << 32));
                 }
                 const bool cont = active && (best >> 32) >= (kWinNear + 1) * (kWinNear + 1);
                 if (active && !cont) emit_at(o, best);
