@@ -429,11 +429,6 @@ int vc_debug_get_thin_trace(vc_ctx* ctx, int64_t* out, int cap, int* ngen);
  * thread in its first phase (1 or 2, 512 x 2 only; 0 = 1).  Results do not
  * depend on it.                                                            */
 int vc_debug_thin_shape(vc_ctx* ctx, int threads, int blocks_per_sm, int items);
-/* Thinning kernel variant: with list_positions != 0 (default) the decrement
- * that takes a count to 1 carries its queue position in the cell list and
- * only decrements that leave a count >= 2 raise the cell's last-decrement
- * position; with 0 every decrement raises it.  Results do not depend on it. */
-int vc_debug_thin_variant(vc_ctx* ctx, int list_positions);
 /* Rate at which this GPU serves random touches of 32-byte records in an
  * array of `bytes` (allocated for the call; rounded down to a power-of-two
  * number of records), the access pattern of the thinning kernel's records:

@@ -161,9 +161,6 @@ class Context:
         self.check(self.lib.vc_debug_random_rate(self.h, op, nbytes, ctypes.byref(out)), "vc_debug_random_rate")
         return out.value
 
-    def debug_thin_variant(self, list_positions: bool = True):
-        self.check(self.lib.vc_debug_thin_variant(self.h, 1 if list_positions else 0), "vc_debug_thin_variant")
-
     def debug_set_spin_limit(self, polls: int = 0):
         """Polls before a grid barrier of the thinning gives up (0 = default)."""
         self.check(self.lib.vc_debug_set_spin_limit(self.h, polls), "vc_debug_set_spin_limit")

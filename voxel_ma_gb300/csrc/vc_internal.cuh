@@ -266,7 +266,6 @@ struct vc_ctx {
     int thin_blocks_per_sm = 0;  // 0 = library default
     int thin_threads = 0;        // threads per block of the thinning kernel (0 = library default)
     int thin_items = 1;          // items per thread and piece in the thinning's phase A (1 or 2)
-    bool thin_lp = true;         // thinning: the decrement to 1 carries its position in the cell list
     bool ft_force_wide = false;  // feature transform: 64-bit arithmetic at every size
     int ft_ring = 16;            // feature transform: envelope stack entries in shared memory per line
     vc::DevBuf ft_far;           // feature transform: tiles the window kernel left to the envelope kernel

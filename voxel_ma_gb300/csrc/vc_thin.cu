@@ -27,8 +27,10 @@
 // grid barriers per generation:
 //   A (per item)  claims are checked, removals applied, counts decremented;
 //                 the decrement that takes a count from 2 to 1 lists its cell
-//                 (items are handed out to blocks in 256-item pieces from a
-//                 shared cursor, so the blocks stay balanced);
+//                 with its own position, decrements that leave 2 or more
+//                 raise the cell's last-decrement position (items are handed
+//                 out to blocks in blockDim-item pieces from a shared cursor,
+//                 so the blocks stay balanced);
 //   B (per listed cell)  a cell still at 1 gives its child to the item at
 //                 its last-decrement position, in the cell's slot;
 //   C (per item)  children are written in order as generation g+1 and that
@@ -70,8 +72,8 @@ struct ThinArgs {
     int2* qa;
     int2* qb;
     int2* child;           // per item: up to 4 children, by slot ({-1, -1}: none)
-    int32_t* cells;        // cells whose count reached 1 in this generation (kEdgeBit: edge); with
-                           // list positions, pairs {cell, trig of the decrement that took it to 1}
+    int2* cells;           // cells whose count reached 1 in this generation (kEdgeBit: edge), each with
+                           // the trig of the decrement that took it to 1
     int* counters;         // [2][4] by generation parity: list length, phase-A work cursor
     int64_t* blk_cnt;      // [2][G][warps per block] children per phase-C warp range, by generation parity
     unsigned* bar;
@@ -199,20 +201,8 @@ __global__ void __launch_bounds__(kThreads) gen0_write_kernel(ThinArgs A, int32_
     }
 }
 
-// Warp-aggregated append of a cell whose count fell from 2 to 1 to the
-// block's shared-memory list of the current 256-item piece (all lanes call).
-__device__ __forceinline__ void append_cell(int32_t* region, int* s_count, bool want, int32_t code) {
-    const unsigned m = __ballot_sync(0xffffffffu, want);
-    if (!m) return;
-    const int lane = threadIdx.x & 31;
-    const int leader = __ffs(m) - 1;
-    int basei = 0;
-    if (lane == leader) basei = atomicAdd(s_count, __popc(m));
-    basei = __shfl_sync(0xffffffffu, basei, leader);
-    if (want) region[basei + __popc(m & ((1u << lane) - 1u))] = code;
-}
-
-// The same for {cell, trig} pairs.
+// Warp-aggregated append of {cell, trig} for a cell whose count fell from 2
+// to 1 to the block's shared-memory list of the current piece (all lanes call).
 __device__ __forceinline__ void append_pair(int2* region, int* s_count, bool want, int2 pair) {
     const unsigned m = __ballot_sync(0xffffffffu, want);
     if (!m) return;
@@ -224,20 +214,21 @@ __device__ __forceinline__ void append_pair(int2* region, int* s_count, bool wan
     if (want) region[basei + __popc(m & ((1u << lane) - 1u))] = pair;
 }
 
-// LP (list positions): the last decrement of a cell that ends a generation
-// at count 1 is the largest position among its decrements in it.  The
-// decrement that takes the count from 2 to 1 carries its own trig in the
-// cell's list entry; only decrements that leave a count of 2 or more (which
-// may be followed by others in the same generation) raise the record's trig
-// with an atomicMax; decrements to 0 need none.  Phase B takes the larger of
-// the two (a trig left by an earlier generation holds an earlier position).
-// Without LP every decrement raises the record's trig.
-template <int THREADS, int MINB, int ITEMS, bool LP>
+// The last decrement of a cell that ends a generation at count 1 is the
+// largest position among its decrements in it.  The decrement that takes the
+// count from 2 to 1 carries its own trig in the cell's list entry; only
+// decrements that leave a count of 2 or more (which may be followed by others
+// in the same generation) raise the record's trig with an atomicMax, and
+// decrements to 0 need none.  Phase B takes the larger of the two (a trig
+// left by an earlier generation holds an earlier position).  Measured at
+// 512^3: 46.3 ms against 46.9 ms with every decrement raising the trig (same
+// box, same build otherwise).
+template <int THREADS, int MINB, int ITEMS>
 __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArgs A) {
     __shared__ int64_t sm[33];
     __shared__ int64_t s_red[2], s_wpre[32];
     __shared__ int s_ncell, s_start, s_gbase;
-    __shared__ __align__(8) int32_t s_cells[(LP ? 8 : 4) * THREADS * ITEMS];
+    __shared__ int2 s_cells[4 * THREADS * ITEMS];
     const int G = gridDim.x, b = blockIdx.x;
     const float l_t = A.thr[1];
     int64_t n = A.ctl[0];
@@ -318,9 +309,9 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
             uint32_t dtg[4 * ITEMS];  // recorded once the decrements have come back (measured faster)
 #pragma unroll
             for (int q = 0; q < 4 * ITEMS; ++q) one[q] = dec[q] = -1;
-            // LP: a decrement that took the count to 1 or 0 raises no trig
+            // a decrement that took the count to 1 or 0 raises no trig
             auto keep_dec = [&](int q, int old_count) {
-                if (LP && old_count <= 2) dec[q] = -1;
+                if (old_count <= 2) dec[q] = -1;
             };
 #pragma unroll
             for (int k = 0; k < ITEMS; ++k) {
@@ -388,15 +379,9 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                     }
                 }
             }
-            if (LP) {
 #pragma unroll
-                for (int q = 0; q < 4 * ITEMS; ++q)
-                    append_pair(reinterpret_cast<int2*>(s_cells), &s_ncell, one[q] != -1,
-                                make_int2(one[q], (int32_t)dtg[q]));
-            } else {
-#pragma unroll
-                for (int q = 0; q < 4 * ITEMS; ++q) append_cell(s_cells, &s_ncell, one[q] != -1, one[q]);
-            }
+            for (int q = 0; q < 4 * ITEMS; ++q)
+                append_pair(s_cells, &s_ncell, one[q] != -1, make_int2(one[q], (int32_t)dtg[q]));
 #pragma unroll
             for (int q = 0; q < 4 * ITEMS; ++q) {
                 if (dec[q] == -1) continue;
@@ -406,12 +391,7 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
             __syncthreads();
             if (threadIdx.x == 0) s_gbase = s_ncell ? atomicAdd(ctr + 0, s_ncell) : 0;
             __syncthreads();
-            if (LP) {
-                for (int k = threadIdx.x; k < s_ncell; k += blockDim.x)
-                    reinterpret_cast<int2*>(A.cells)[s_gbase + k] = reinterpret_cast<const int2*>(s_cells)[k];
-            } else {
-                for (int k = threadIdx.x; k < s_ncell; k += blockDim.x) A.cells[s_gbase + k] = s_cells[k];
-            }
+            for (int k = threadIdx.x; k < s_ncell; k += blockDim.x) A.cells[s_gbase + k] = s_cells[k];
             __syncthreads();
             if (threadIdx.x == 0) {
                 s_start = next_start;
@@ -435,15 +415,9 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                 int slot = 0;
                 int2 ch = make_int2(-1, -1);
                 if (j < j1) {
-                    int32_t code;
-                    uint32_t ltg = 0;  // LP: the trig of the decrement to 1
-                    if (LP) {
-                        const int2 ent = __ldcg(reinterpret_cast<const int2*>(A.cells) + j);
-                        code = ent.x;
-                        ltg = (uint32_t)ent.y;
-                    } else {
-                        code = __ldcg(A.cells + j);
-                    }
+                    const int2 ent = __ldcg(A.cells + j);
+                    const int32_t code = ent.x;
+                    const uint32_t ltg = (uint32_t)ent.y;  // the trig of the decrement to 1
                     uint32_t tg = 0;
                     if (code & kEdgeBit) {
                         const int32_t e2 = code & ~kEdgeBit;
@@ -692,7 +666,7 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats, bool all_pass) {
     VC_TRY(ensure_n<int2>(c, c->q0, qcap));
     VC_TRY(ensure_n<int2>(c, c->q1, qcap));
     VC_TRY(ensure_n<int2>(c, c->child, 4 * qcap));
-    VC_TRY(ensure_n<int32_t>(c, c->cells, (c->thin_lp ? 8 : 4) * qcap));
+    VC_TRY(ensure_n<int2>(c, c->cells, 4 * qcap));
     VC_TRY(ensure_n<int64_t>(c, c->euler_tmp, 16));
     VC_TRY(ensure_n<uint8_t>(c, c->keep_v, nv));
     VC_TRY(ensure_n<uint8_t>(c, c->keep_e, ne));
@@ -706,7 +680,7 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats, bool all_pass) {
     A.qa = ptr<int2>(c->q0);
     A.qb = ptr<int2>(c->q1);
     A.child = ptr<int2>(c->child);
-    A.cells = ptr<int32_t>(c->cells);
+    A.cells = ptr<int2>(c->cells);
     A.err = dev_err(c);
     int64_t* ctl = ptr<int64_t>(c->euler_tmp);
     A.ctl = ctl;
@@ -755,22 +729,12 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats, bool all_pass) {
     // piece): 512 x 2 (default), 512 x 2 with 2 items, 512 x 4, 256 x 8,
     // 1024 x 1
     const int threads = c->thin_threads == 256 ? 256 : (c->thin_threads == 1024 ? 1024 : 512);
-    void* kern = nullptr;
-    if (c->thin_lp) {
-        kern = threads == 256    ? (void*)thin_generations_kernel<256, 8, 1, true>
-               : threads == 1024 ? (void*)thin_generations_kernel<1024, 1, 1, true>
-               : (c->thin_blocks_per_sm >= 3)
-                   ? (void*)thin_generations_kernel<512, 4, 1, true>
-                   : (c->thin_items == 2 ? (void*)thin_generations_kernel<512, 2, 2, true>
-                                         : (void*)thin_generations_kernel<512, 2, 1, true>);
-    } else {
-        kern = threads == 256    ? (void*)thin_generations_kernel<256, 8, 1, false>
-               : threads == 1024 ? (void*)thin_generations_kernel<1024, 1, 1, false>
-               : (c->thin_blocks_per_sm >= 3)
-                   ? (void*)thin_generations_kernel<512, 4, 1, false>
-                   : (c->thin_items == 2 ? (void*)thin_generations_kernel<512, 2, 2, false>
-                                         : (void*)thin_generations_kernel<512, 2, 1, false>);
-    }
+    void* kern = threads == 256    ? (void*)thin_generations_kernel<256, 8, 1>
+                 : threads == 1024 ? (void*)thin_generations_kernel<1024, 1, 1>
+                 : (c->thin_blocks_per_sm >= 3)
+                     ? (void*)thin_generations_kernel<512, 4, 1>
+                     : (c->thin_items == 2 ? (void*)thin_generations_kernel<512, 2, 2>
+                                           : (void*)thin_generations_kernel<512, 2, 1>);
     int per_sm = 0;
     VC_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, 0));
     if (per_sm <= 0) return VC_ERR_CUDA;
@@ -846,12 +810,6 @@ int vc_debug_thin_shape(vc_ctx* c, int threads, int blocks_per_sm, int items) {
     c->thin_threads = threads;
     c->thin_blocks_per_sm = blocks_per_sm;
     c->thin_items = items == 2 ? 2 : 1;
-    return VC_OK;
-}
-
-int vc_debug_thin_variant(vc_ctx* c, int list_positions) {
-    if (!c) return VC_ERR_ARG;
-    c->thin_lp = list_positions != 0;
     return VC_OK;
 }
 
