@@ -781,14 +781,14 @@ def run_serving(dev, args, workers=None, max_batch=None, with_plain=True, sweep=
 
 
 # DRAM traffic per cell of the complex (V + E + T) of the thinning kernel,
-# from one ncu capture of the 192^3 case of this workload (4.072 GB read +
-# 1.988 GB written for 3,385,169 + 14,026,594 + 10,679,482 cells); the
+# from one ncu capture of the 192^3 case of this workload (4.012 GB read +
+# 1.994 GB written for 3,286,553 + 13,677,962 + 10,430,150 cells); the
 # traffic grows with the complex, so the per-launch figure at 512^3 is this
 # rate times its cells.
-TRAFFIC_PER_CELL = {"thin_generations": (4.071764e9 + 1.988158e9) / (3385169 + 14026594 + 10679482)}
+TRAFFIC_PER_CELL = {"thin_generations": (4.012005e9 + 1.993560e9) / (3286553 + 13677962 + 10430150)}
 # L2 requests (atomics + reads + writes from the SMs) per cell of the same
-# capture: 78.5 M + 48.5 M + 26.2 M for the same cells.
-L2_REQUESTS_PER_CELL = {"thin_generations": (78454799 + 48482036 + 26165270) / (3385169 + 14026594 + 10679482)}
+# capture: 62.47 M + 43.82 M + 26.05 M for the same cells.
+L2_REQUESTS_PER_CELL = {"thin_generations": (62473859 + 43820742 + 26047976) / (3286553 + 13677962 + 10430150)}
 PROBE_BYTES = 16 << 30
 
 

@@ -228,6 +228,7 @@ struct vc_ctx {
     vc::DevBuf vd_tri_face, vd_face_sites, vd_lam;
     bool vd_aux_meas = false;  // vm, em, fm, tri_face, face_sites of the lattice complex written
     bool vd_aux_topo = false;  // tri_edges and the V->E / E->F lists of the lattice complex written
+    bool vd_geom = false;      // vts / edges / tris of the lattice complex written (on demand after the timed path)
     bool vd_thr_valid = false; // bases.thr holds the volumes' thinning thresholds of this complex
     vc::DevBuf vd_radius;             // float per vertex of the lattice complex
     std::vector<float> vol_inside;  // inside-part size per volume
@@ -332,6 +333,16 @@ int set_volume_table(vc_ctx* c, int nvol, const int32_t* dims);
 // Rank of cell x among the kept cells of its kind: the kept cells are bit
 // words (bit x & 31 of word x >> 5) and base[w] is the number kept before
 // word w (an exclusive scan of the words' population counts).
+// Survivors of a thinning as bit words (vertices | edges | faces) with
+// scanned per-word counts: a survivor's output position is its kept_rank.
+struct Kept {
+    const uint32_t* bv;  // vertex words
+    const uint32_t* be;  // edge words
+    const uint32_t* bf;  // face words
+    const int32_t* pv;
+    const int32_t* pe;
+    const int32_t* pf;
+};
 __device__ __forceinline__ int32_t kept_rank(const uint32_t* __restrict__ bits, const int32_t* __restrict__ base,
                                              int64_t x) {
     const int64_t w = x >> 5;

@@ -15,16 +15,6 @@
 namespace vc {
 namespace {
 
-// Survivors are bit words (vertices | edges | faces) with scanned per-word
-// counts: a survivor's output position is its kept_rank.
-struct Kept {
-    const uint32_t* bv;  // vertex words
-    const uint32_t* be;  // edge words
-    const uint32_t* bf;  // face words
-    const int32_t* pv;
-    const int32_t* pe;
-    const int32_t* pf;
-};
 
 // Per-volume starts of the remaining complex (batches): the survivors before
 // each volume's first vertex, edge and triangle.
@@ -211,6 +201,9 @@ Kept kept_of(vc_ctx* c) {
                 ptr<int32_t>(c->keep_wf)};
 }
 
+int lattice_rem_write(vc_ctx* c, const Kept& K, int nmap);
+int ensure_vd_geometry(vc_ctx* c);
+
 int run_remaining(vc_ctx* c, vc_rem_sizes* sizes) {
     if (!c->thin_valid) return VC_ERR_STATE;
     if (c->rem_valid) {  // this thinning's remaining complex is built already (the word scans below are in place)
@@ -243,10 +236,16 @@ int run_remaining(vc_ctx* c, vc_rem_sizes* sizes) {
     VC_TRY(ensure_n<float>(c, c->rem_vts, 3 * h[0]));
     VC_TRY(ensure_n<int2>(c, c->rem_edges, h[1]));
     VC_TRY(ensure_n<int32_t>(c, c->rem_tris, 3 * h[2]));
-    rem_write_kernel<<<grid_for(c, 32 * (nwv + nwe + nwf), 256), 256, 0, c->stream>>>(
-        (int32_t)nv, (int32_t)ne, (int32_t)nt, K, ptr<float>(c->vts), ptr<int2>(c->edges), ptr<int32_t>(c->tris),
-        ptr<float>(c->rem_vts), ptr<int2>(c->rem_edges), ptr<int32_t>(c->rem_tris), c->bases, nmap);
-    launched(c);
+    if (c->vd_valid && !c->vd_geom) {
+        // the lattice complex of the timed path keeps no vertex, edge or
+        // triangle arrays: the survivors come from the thinning records
+        VC_TRY(lattice_rem_write(c, K, nmap));
+    } else {
+        rem_write_kernel<<<grid_for(c, 32 * (nwv + nwe + nwf), 256), 256, 0, c->stream>>>(
+            (int32_t)nv, (int32_t)ne, (int32_t)nt, K, ptr<float>(c->vts), ptr<int2>(c->edges), ptr<int32_t>(c->tris),
+            ptr<float>(c->rem_vts), ptr<int2>(c->rem_edges), ptr<int32_t>(c->rem_tris), c->bases, nmap);
+        launched(c);
+    }
     VC_CUDA(c, cudaGetLastError());
     c->rem = vc_rem_sizes{h[0], h[1], h[2]};
     c->rem_valid = true;
