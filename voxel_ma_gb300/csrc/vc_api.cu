@@ -114,6 +114,7 @@ int vc_get_vd(vc_ctx* c, float* vts, int32_t* edges, int32_t* tris, int32_t* tri
     if (!c->vd_valid) return VC_ERR_STATE;
     if (!good_mem(mem)) return VC_ERR_ARG;
     VC_TRY(ensure_vd_aux(c, true, false));
+    if (vts || edges || tris) VC_TRY(ensure_vd_geometry(c));
     const vc_vd_sizes& s = c->vd;
     VC_TRY(copy_out(c, vts, c->vts.p, (size_t)s.nv * 3 * sizeof(float), mem));
     VC_TRY(copy_out(c, edges, c->edges.p, (size_t)s.ne * 2 * sizeof(int32_t), mem));
@@ -175,7 +176,7 @@ int vc_get_finalized(vc_ctx* c, int32_t* edges, int32_t* tri_edges, int32_t* ve_
     VC_TRY(enter(c));
     if (!c->cc_finalized) return VC_ERR_STATE;
     if (!good_mem(mem)) return VC_ERR_ARG;
-    VC_TRY(ensure_vd_aux(c, false, true));
+    VC_TRY(ensure_vd_aux(c, false, true));  // (writes the lattice complex's edges too)
     VC_TRY(copy_out(c, edges, c->edges.p, (size_t)c->ne * 2 * sizeof(int32_t), mem));
     VC_TRY(copy_out(c, tri_edges, c->tri_edges.p, (size_t)c->nt * 3 * sizeof(int32_t), mem));
     VC_TRY(copy_out(c, ve_off, c->ve_off.p, (size_t)(c->nv + 1) * sizeof(int32_t), mem));

@@ -248,6 +248,7 @@ int ctx_release_buffers(vc_ctx* c) {
     c->n_sites = -1;
     c->ft_valid = c->vd_valid = c->cc_valid = c->cc_finalized = c->meas_valid = c->thin_valid = c->rem_valid = false;
     c->records_fresh = c->records_thr_folded = c->cc_batched = false;
+    c->vd_geom = c->vd_aux_meas = c->vd_aux_topo = false;
     c->nvol = 0;
     c->tab = VolTab{};
     c->bases = Bases{};

@@ -329,6 +329,8 @@ int* dev_err(vc_ctx* c);
 // Describe the context's volumes (dims: 3 ints per volume) and size the
 // per-volume base arrays.
 int set_volume_table(vc_ctx* c, int nvol, const int32_t* dims);
+// The lattice complex's vertex / edge / triangle arrays, written on demand.
+int ensure_vd_geometry(vc_ctx* c);
 // The entry of a base array (nvol + 1 ascending starts) whose range holds x.
 // Rank of cell x among the kept cells of its kind: the kept cells are bit
 // words (bit x & 31 of word x >> 5) and base[w] is the number kept before

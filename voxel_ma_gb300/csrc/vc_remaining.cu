@@ -125,12 +125,12 @@ __global__ void uf_init_kernel(int32_t* parent, int32_t n) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) parent[i] = (int32_t)i;
 }
 
-__global__ void uf_union_kernel(const int32_t* __restrict__ mark, const int2* __restrict__ edges, Kept K, int32_t ne,
+__global__ void uf_union_kernel(const int32_t* __restrict__ mark, const EdgeRec* __restrict__ E, Kept K, int32_t ne,
                                 int32_t* parent, int* err) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += stride) {
         if (!mark[e]) continue;
-        const int2 ev = edges[e];
+        const int2 ev = *reinterpret_cast<const int2*>(E + e);  // the record's ends v0, v1
         if (!uf_join(parent, kept_rank(K.bv, K.pv, ev.x), kept_rank(K.bv, K.pv, ev.y))) set_error(err, VC_ERR_TIMEOUT);
     }
 }
@@ -149,13 +149,13 @@ __global__ void uf_roots_kernel(int32_t* parent, int32_t n, unsigned long long* 
 }
 
 // Marked edges, per volume in a batch (edge -> volume through its vertex).
-__global__ void count_kernel(const int32_t* __restrict__ mark, const int2* __restrict__ edges, int64_t n,
+__global__ void count_kernel(const int32_t* __restrict__ mark, const EdgeRec* __restrict__ E, int64_t n,
                              unsigned long long* cnt, Bases B, int nmap) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     unsigned long long local = 0;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         if (mark[i] == 0) continue;
-        if (nmap > 1) atomicAdd(cnt + find_base(B.b[kBVert], nmap, edges[i].x), 1ull);
+        if (nmap > 1) atomicAdd(cnt + find_base(B.b[kBVert], nmap, E[i].v0), 1ull);
         else ++local;
     }
     if (local) atomicAdd(cnt, local);
@@ -202,7 +202,6 @@ Kept kept_of(vc_ctx* c) {
 }
 
 int lattice_rem_write(vc_ctx* c, const Kept& K, int nmap);
-int ensure_vd_geometry(vc_ctx* c);
 
 int run_remaining(vc_ctx* c, vc_rem_sizes* sizes) {
     if (!c->thin_valid) return VC_ERR_STATE;
@@ -303,13 +302,16 @@ int run_euler_remaining(vc_ctx* c, vc_euler_info* out) {
         ptr<uint8_t>(c->keep_e), ptr<uint8_t>(c->keep_f), ptr<FaceRec>(c->face_rec), (int32_t)ne, (int32_t)nt,
         mark);
     launched(c);
-    count_kernel<<<grid_for(c, ne, 256), 256, 0, c->stream>>>(mark, ptr<int2>(c->edges), ne, cnt, c->bases, nmap);
+    // edge ends from the thinning records (the lattice complex of the timed
+    // path keeps no edge array)
+    count_kernel<<<grid_for(c, ne, 256), 256, 0, c->stream>>>(mark, ptr<EdgeRec>(c->edge_rec), ne, cnt, c->bases,
+                                                              nmap);
     launched(c);
     int32_t* parent = ptr<int32_t>(c->uf_parent);
     if (nvr > 0) {
         uf_init_kernel<<<grid_for(c, nvr, 256), 256, 0, c->stream>>>(parent, (int32_t)nvr);
         launched(c);
-        uf_union_kernel<<<grid_for(c, ne, 256), 256, 0, c->stream>>>(mark, ptr<int2>(c->edges), kept_of(c),
+        uf_union_kernel<<<grid_for(c, ne, 256), 256, 0, c->stream>>>(mark, ptr<EdgeRec>(c->edge_rec), kept_of(c),
                                                                       (int32_t)ne, parent, dev_err(c));
         launched(c);
         uf_roots_kernel<<<grid_for(c, nvr, 256), 256, 0, c->stream>>>(parent, (int32_t)nvr, cnt + nmap, c->bases,

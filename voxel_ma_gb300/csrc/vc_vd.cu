@@ -358,9 +358,11 @@ __global__ void __launch_bounds__(128) vd_vertices_kernel(VolTab T, Bases B, con
             const SegPlanes P = load_planes(planes + s);
             if (!bit(P.v, c)) continue;
             const int32_t v = __ldg(vb + s) + __popc(P.v & below(c));
-            vts[3 * (int64_t)v + 0] = (float)a;
-            vts[3 * (int64_t)v + 1] = (float)b;
-            vts[3 * (int64_t)v + 2] = (float)c;
+            if (vts) {
+                vts[3 * (int64_t)v + 0] = (float)a;
+                vts[3 * (int64_t)v + 1] = (float)b;
+                vts[3 * (int64_t)v + 2] = (float)c;
+            }
             if (!V) continue;
             unsigned k = 0;
             unsigned long long idsum = 0;
@@ -509,7 +511,7 @@ __global__ void __launch_bounds__(128, 8) vd_edges_kernel(VolTab T, Bases B, con
                 int nb[3] = {a, b, c};
                 nb[d] += 1;
                 const int32_t v1 = vid_at(S, nb[0], nb[1], nb[2]);
-                edges[e] = make_int2(v0, v1);
+                if (edges) edges[e] = make_int2(v0, v1);
                 if (E) {
                     float mx = 0.0f;
                     unsigned k = 0, npass = 0;
@@ -601,14 +603,16 @@ __global__ void __launch_bounds__(128, 8) vd_faces_kernel(VolTab T, Bases B, con
                 };
                 const int32_t diag = (int32_t)sh.eb1 + f;
                 const int64_t t0 = 2 * (int64_t)f, t1 = t0 + 1;
-                tris[3 * t0 + 0] = q[3];
-                tris[3 * t0 + 1] = q[0];
-                tris[3 * t0 + 2] = q[1];
-                tris[3 * t1 + 0] = q[3];
-                tris[3 * t1 + 1] = q[1];
-                tris[3 * t1 + 2] = q[2];
+                if (tris) {
+                    tris[3 * t0 + 0] = q[3];
+                    tris[3 * t0 + 1] = q[0];
+                    tris[3 * t0 + 2] = q[1];
+                    tris[3 * t1 + 0] = q[3];
+                    tris[3 * t1 + 1] = q[1];
+                    tris[3 * t1 + 2] = q[2];
+                }
                 const int32_t dv0 = min(q[1], q[3]), dv1 = max(q[1], q[3]);
-                edges[diag] = make_int2(dv0, dv1);
+                if (edges) edges[diag] = make_int2(dv0, dv1);
                 // lambda of the face: distance of its two sites (measureforMA_imp.h:1-4)
                 const int64_t p1 = p + (d == 0 ? S.NB * NC : (d == 1 ? NC : 1));
                 const float lm = lambda_of(sxyz, l0, __ldg(lb + p1));
@@ -924,9 +928,17 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes, double t_thr) {
     c->records_fresh = false;
     c->vd_aux_meas = c->vd_aux_topo = false;
     const bool folded = t_thr >= 0.0;
-    VC_TRY(ensure_n<float>(c, c->vts, 3 * nv));
-    VC_TRY(ensure_n<int2>(c, c->edges, ne));
-    VC_TRY(ensure_n<int32_t>(c, c->tris, 3 * nt));
+    // The path that thins at once (records with the thresholds folded in)
+    // writes no vertex, edge or triangle arrays: the thinning and the
+    // remaining complex read the records, and the arrays are written on
+    // demand for the getters (ensure_vd_geometry).
+    const bool geom = !folded;
+    c->vd_geom = false;
+    if (geom) {
+        VC_TRY(ensure_n<float>(c, c->vts, 3 * nv));
+        VC_TRY(ensure_n<int2>(c, c->edges, ne));
+        VC_TRY(ensure_n<int32_t>(c, c->tris, 3 * nt));
+    }
     VC_TRY(ensure_n<float>(c, c->vd_lam, nface));  // lambda per face
     if (folded) {
         VC_TRY(ensure_n<FaceRec>(c, c->face_rec, nt));
@@ -942,22 +954,22 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes, double t_thr) {
             Region k(c, "vd_faces");
             vd_faces_kernel<<<seg_grid(c, nseg), 128, 0, c->stream>>>(
                 c->tab, c->bases, planes, vb, eb, fb, ptr<int32_t>(c->ft_id), ptr<float>(c->site_xyz),
-                ptr<float>(c->vd_lam), ptr<int32_t>(c->tris), ptr<int2>(c->edges),
+                ptr<float>(c->vd_lam), geom ? ptr<int32_t>(c->tris) : nullptr, geom ? ptr<int2>(c->edges) : nullptr,
                 folded ? ptr<FaceRec>(c->face_rec) : nullptr, folded ? ptr<EdgeRec>(c->edge_rec) : nullptr, g0, thr);
             launched(c);
         }
         {
             Region k(c, "vd_edges");
             vd_edges_kernel<<<seg_grid(c, nseg), 128, 0, c->stream>>>(
-                c->tab, c->bases, planes, vb, eb, fb, ptr<float>(c->vd_lam), ptr<int2>(c->edges),
+                c->tab, c->bases, planes, vb, eb, fb, ptr<float>(c->vd_lam), geom ? ptr<int2>(c->edges) : nullptr,
                 folded ? ptr<EdgeRec>(c->edge_rec) : nullptr, g0, thr);
             launched(c);
         }
         {
             Region k(c, "vd_vertices");
             vd_vertices_kernel<<<seg_grid(c, nseg), 128, 0, c->stream>>>(
-                c->tab, c->bases, planes, vb, eb, fb, ptr<float>(c->vts), folded ? ptr<VertRec>(c->vert_rec) : nullptr,
-                folded ? ptr<EdgeRec>(c->edge_rec) : nullptr, g0, ne);
+                c->tab, c->bases, planes, vb, eb, fb, geom ? ptr<float>(c->vts) : nullptr,
+                folded ? ptr<VertRec>(c->vert_rec) : nullptr, folded ? ptr<EdgeRec>(c->edge_rec) : nullptr, g0, ne);
             launched(c);
         }
         VC_CUDA(c, cudaGetLastError());
@@ -972,6 +984,7 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes, double t_thr) {
     c->nt = nt;
     c->vd = vc_vd_sizes{nv, ne, nt, nface, c->vol_inside[0]};
     c->vd_valid = true;
+    c->vd_geom = geom;
     c->cc_valid = true;
     c->cc_finalized = true;
     c->meas_valid = true;  // written on demand (ensure_vd_aux)
@@ -980,6 +993,121 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes, double t_thr) {
     c->vd_thr_valid = folded;
     c->cc_batched = nvol > 1;
     if (sizes) *sizes = c->vd;
+    return VC_OK;
+}
+
+// The lattice complex's vertex, edge and triangle arrays when the fast path
+// did not write them: the emission kernels run again, writing only those.
+int ensure_vd_geometry(vc_ctx* c) {
+    if (!c->vd_valid || c->vd_geom) return VC_OK;
+    const int64_t nv = c->vd.nv, ne = c->vd.ne, nt = c->vd.nt;
+    const int64_t nseg = c->h_off[kLSeg][c->nvol];
+    VC_TRY(ensure_n<float>(c, c->vts, 3 * nv));
+    VC_TRY(ensure_n<int2>(c, c->edges, ne));
+    VC_TRY(ensure_n<int32_t>(c, c->tris, 3 * nt));
+    const SegPlanes* planes = ptr<SegPlanes>(c->vd_seg);
+    const int32_t *vb = ptr<int32_t>(c->vd_voff), *eb = ptr<int32_t>(c->vd_eoff), *fb = ptr<int32_t>(c->vd_foff);
+    Region r(c, "vd_geometry");
+    vd_faces_kernel<<<seg_grid(c, nseg), 128, 0, c->stream>>>(
+        c->tab, c->bases, planes, vb, eb, fb, ptr<int32_t>(c->ft_id), ptr<float>(c->site_xyz), ptr<float>(c->vd_lam),
+        ptr<int32_t>(c->tris), ptr<int2>(c->edges), nullptr, nullptr, nullptr, nullptr);
+    vd_edges_kernel<<<seg_grid(c, nseg), 128, 0, c->stream>>>(c->tab, c->bases, planes, vb, eb, fb,
+                                                               ptr<float>(c->vd_lam), ptr<int2>(c->edges), nullptr,
+                                                               nullptr, nullptr);
+    vd_vertices_kernel<<<seg_grid(c, nseg), 128, 0, c->stream>>>(c->tab, c->bases, planes, vb, eb, fb,
+                                                                  ptr<float>(c->vts), nullptr, nullptr, nullptr, ne);
+    launched(c, 3);
+    VC_CUDA(c, cudaGetLastError());
+    c->vd_geom = true;
+    return VC_OK;
+}
+
+namespace {
+
+// Lattice point (a, b, c) of vertex v: its segment is the last one whose
+// first vertex id is <= v (the first ids are an exclusive scan of the
+// segments' vertex counts), and v is the (v - first)-th vertex bit in it.
+__device__ __forceinline__ void lattice_vertex(const VolTab& T, const SegPlanes* __restrict__ planes,
+                                               const int32_t* __restrict__ vb, int64_t nseg, int32_t v, float* o) {
+    int64_t lo = 0, hi = nseg;
+    while (hi - lo > 1) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (__ldg(vb + mid) <= v) lo = mid;
+        else hi = mid;
+    }
+    const uint32_t m = __ldg(reinterpret_cast<const uint32_t*>(planes + lo));  // the vertex plane
+    const int bitpos = (int)__fns(m, 0, v - __ldg(vb + lo) + 1);
+    const int bv = T.find(kLSeg, lo);
+    const int4 d = T.dim(bv);
+    const int nsr = (d.z + 32) / 32;
+    const int64_t ls = lo - T.start(kLSeg, bv);
+    const int64_t row = ls / nsr;
+    const int NB = d.y + 1;
+    o[0] = (float)(row / NB);
+    o[1] = (float)(row % NB);
+    o[2] = (float)((int)(ls - row * nsr) * 32 + bitpos);
+}
+
+// remainingCC of the lattice complex from the thinning records: a kept
+// vertex's coordinates from the lattice, a kept edge's ends from its record,
+// a kept triangle's corners from the records of its first two sides (sides
+// (a,b), (b,c), (c,a) in face order: b is the vertex the first two share).
+__global__ void vd_rem_write_kernel(int32_t nv, int32_t ne, int32_t nt, Kept K, VolTab T,
+                                    const SegPlanes* __restrict__ planes, const int32_t* __restrict__ vb,
+                                    int64_t nseg, const EdgeRec* __restrict__ E, const FaceRec* __restrict__ F,
+                                    float* __restrict__ ovts, int2* __restrict__ oedges, int32_t* __restrict__ otris,
+                                    Bases B, int nmap) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t lowm = (1u << lane) - 1u;
+    const int64_t nwv = ((int64_t)nv + 31) / 32, nwe = ((int64_t)ne + 31) / 32, nwf = ((int64_t)nt + 31) / 32;
+    const int64_t nw = nwv + nwe + nwf;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < nw; w += warps) {
+        if (w < nwv) {
+            const uint32_t word = __ldg(K.bv + w);
+            if (!((word >> lane) & 1u)) continue;
+            const int64_t o = __ldg(K.pv + w) + __popc(word & lowm);
+            lattice_vertex(T, planes, vb, nseg, (int32_t)(w * 32 + lane), ovts + 3 * o);
+        } else if (w < nwv + nwe) {
+            const int64_t we = w - nwv;
+            const uint32_t word = __ldg(K.be + we);
+            if (!((word >> lane) & 1u)) continue;
+            const int4 er = __ldg(reinterpret_cast<const int4*>(E + we * 32 + lane));  // v0 v1 rm em
+            const int32_t sh = nmap > 1 ? (int32_t)B.b[kBRemV][find_base(B.b[kBVert], nmap, er.x)] : 0;
+            oedges[__ldg(K.pe + we) + __popc(word & lowm)] =
+                make_int2(kept_rank(K.bv, K.pv, er.x) - sh, kept_rank(K.bv, K.pv, er.y) - sh);
+        } else {
+            const int64_t wf = w - nwv - nwe;
+            const uint32_t word = __ldg(K.bf + wf);
+            if (!((word >> lane) & 1u)) continue;
+            const int64_t f = wf * 32 + lane;
+            const int64_t o = __ldg(K.pf + wf) + __popc(word & lowm);
+            const int4 fr = __ldg(reinterpret_cast<const int4*>(F + f));  // e0 e1 e2|pass rm
+            const int2 s0 = *reinterpret_cast<const int2*>(E + fr.x);
+            const int2 s1 = *reinterpret_cast<const int2*>(E + fr.y);
+            const int32_t vb_ = (s0.x == s1.x || s0.x == s1.y) ? s0.x : s0.y;
+            const int32_t va = s0.x == vb_ ? s0.y : s0.x;
+            const int32_t vc = s1.x == vb_ ? s1.y : s1.x;
+            const int32_t sh = nmap > 1 ? (int32_t)B.b[kBRemV][find_base(B.b[kBVert], nmap, va)] : 0;
+            // simpleTriangulate turns (a, b, c) into (c, a, b)
+            otris[3 * o + 0] = kept_rank(K.bv, K.pv, vc) - sh;
+            otris[3 * o + 1] = kept_rank(K.bv, K.pv, va) - sh;
+            otris[3 * o + 2] = kept_rank(K.bv, K.pv, vb_) - sh;
+        }
+    }
+}
+
+}  // namespace
+
+int lattice_rem_write(vc_ctx* c, const Kept& K, int nmap) {
+    const int64_t nv = c->nv, ne = c->ne, nt = c->nt;
+    const int64_t nw = (nv + 31) / 32 + (ne + 31) / 32 + (nt + 31) / 32;
+    vd_rem_write_kernel<<<cell_grid(c, 32 * nw), 256, 0, c->stream>>>(
+        (int32_t)nv, (int32_t)ne, (int32_t)nt, K, c->tab, ptr<SegPlanes>(c->vd_seg), ptr<int32_t>(c->vd_voff),
+        c->h_off[kLSeg][c->nvol], ptr<EdgeRec>(c->edge_rec), ptr<FaceRec>(c->face_rec), ptr<float>(c->rem_vts),
+        ptr<int2>(c->rem_edges), ptr<int32_t>(c->rem_tris), c->bases, nmap);
+    launched(c);
+    VC_CUDA(c, cudaGetLastError());
     return VC_OK;
 }
 
@@ -992,6 +1120,7 @@ int ensure_vd_aux(vc_ctx* c, bool meas, bool topo) {
     const bool need_meas = meas && !c->vd_aux_meas;
     const bool need_topo = topo && !c->vd_aux_topo;
     if (!need_meas && !need_topo) return VC_OK;
+    if (need_topo) VC_TRY(ensure_vd_geometry(c));  // the adjacency is built from the edges
     const int64_t nv = c->nv, ne = c->ne, nt = c->nt, nface = c->vd.nface;
     // the kernel writes both groups; a group already written (possibly by
     // vc_set_measures) goes to scratch copies so it is not overwritten
@@ -1056,6 +1185,7 @@ int run_lambda_check(vc_ctx* c, double* max_rel_err, int64_t* flips) {
 
 int run_vertex_radii(vc_ctx* c) {
     if (!c->vd_valid || !c->ft_valid) return VC_ERR_STATE;
+    VC_TRY(ensure_vd_geometry(c));
     const int64_t nv = c->vd.nv;
     VC_TRY(ensure_n<float>(c, c->vd_radius, nv));
     if (nv == 0) return VC_OK;
