@@ -429,11 +429,6 @@ int vc_debug_get_thin_trace(vc_ctx* ctx, int64_t* out, int cap, int* ngen);
  * thread in its first phase (1 or 2, 512 x 2 only; 0 = 1).  Results do not
  * depend on it.                                                            */
 int vc_debug_thin_shape(vc_ctx* ctx, int threads, int blocks_per_sm, int items);
-/* Tail of the thinning: once a generation has fewer than `items` items, it
- * and every later one run on `blocks` blocks of the persistent grid (cheaper
- * grid barriers for the many small generations at the end); 0 = the whole
- * grid throughout.  Results do not depend on it.                           */
-int vc_debug_thin_tail(vc_ctx* ctx, int64_t items, int blocks);
 /* Rate at which this GPU serves random touches of 32-byte records in an
  * array of `bytes` (allocated for the call; rounded down to a power-of-two
  * number of records), the access pattern of the thinning kernel's records:

@@ -27,18 +27,13 @@ def test_autotune_keeps_results(gpu_ctx):
     assert r["thresh"] == ref["thresh"]
     for k in ("keep_v", "keep_e", "keep_f"):
         assert np.array_equal(fl[k], ref["thin"][k]), k
-    # every shape, and the tail of small generations on fewer blocks, gives
-    # the same surviving set
-    for tail in ((0, 0), (1 << 40, 3), (2000, 1), (500, 7)):
-        ctx.debug_thin_tail(*tail)
-        for shape in ((512, 4, 1), (256, 8, 1), (1024, 1, 1), (512, 2, 2), (512, 2, 1)):
-            ctx.debug_thin_shape(*shape)
-            r2 = ctx.run_plain(occ, 0.04)
-            fl2 = ctx.thin_flags()
-            for k in ("keep_v", "keep_e", "keep_f", "removed_e"):
-                assert np.array_equal(fl2[k], ref["thin"][k]), (tail, shape, k)
-            assert r2["thin"]["processed"] == ref["thin"]["stats"]["processed"]
-    ctx.debug_thin_tail(0, 0)
+    # every shape gives the same surviving set
+    for shape in ((512, 4, 1), (256, 8, 1), (1024, 1, 1), (512, 2, 2), (512, 2, 1)):
+        ctx.debug_thin_shape(*shape)
+        ctx.run_plain(occ, 0.04)
+        fl2 = ctx.thin_flags()
+        for k in ("keep_v", "keep_e", "keep_f", "removed_e"):
+            assert np.array_equal(fl2[k], ref["thin"][k]), (shape, k)
     ctx.debug_thin_shape(0, 0, 0)
     ctx.set_ft_method("auto")
 

@@ -132,7 +132,6 @@ SIGNATURES = {
     "vc_write_remaining": (c_int, [c_vp, ctypes.c_char_p, c_int]),
     "vc_debug_random_rate": (c_int, [c_vp, c_int, c_i64, ctypes.POINTER(ctypes.c_double)]),
     "vc_debug_thin_shape": (c_int, [c_vp, c_int, c_int, c_int]),
-    "vc_debug_thin_tail": (c_int, [c_vp, c_i64, c_int]),
     "vc_debug_set_spin_limit": (c_int, [c_vp, ctypes.c_ulonglong]),
     "vc_debug_fail_alloc_after": (c_int, [c_vp, c_i64]),
     "vc_debug_ref_bias": (c_int, [c_vp, c_i64, c_int]),

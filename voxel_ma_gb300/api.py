@@ -161,10 +161,6 @@ class Context:
         self.check(self.lib.vc_debug_random_rate(self.h, op, nbytes, ctypes.byref(out)), "vc_debug_random_rate")
         return out.value
 
-    def debug_thin_tail(self, items: int = 0, blocks: int = 0):
-        """Generations from the first one below `items` items run on `blocks` blocks (0: off)."""
-        self.check(self.lib.vc_debug_thin_tail(self.h, items, blocks), "vc_debug_thin_tail")
-
     def debug_set_spin_limit(self, polls: int = 0):
         """Polls before a grid barrier of the thinning gives up (0 = default)."""
         self.check(self.lib.vc_debug_set_spin_limit(self.h, polls), "vc_debug_set_spin_limit")

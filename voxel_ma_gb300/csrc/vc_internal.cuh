@@ -231,6 +231,7 @@ struct vc_ctx {
     bool vd_geom = false;      // vts / edges / tris of the lattice complex written (on demand after the timed path)
     bool vd_thr_valid = false; // bases.thr holds the volumes' thinning thresholds of this complex
     vc::DevBuf vd_radius;             // float per vertex of the lattice complex
+    vc::DevBuf vd_vlat;               // uint32 per vertex: its lattice point within its volume (timed path)
     std::vector<float> vol_inside;  // inside-part size per volume
     bool cc_batched = false;        // the complex is the lattice complex of a batch of > 1 volumes
     // cell complex (finalized, CSR)
@@ -267,8 +268,6 @@ struct vc_ctx {
     int thin_blocks_per_sm = 0;  // 0 = library default
     int thin_threads = 0;        // threads per block of the thinning kernel (0 = library default)
     int thin_items = 1;          // items per thread and piece in the thinning's phase A (1 or 2)
-    int thin_tail_items = 0;     // thinning: below this many items a generation runs on thin_tail_blocks
-    int thin_tail_blocks = 0;    //   blocks from then on (0: every generation on the whole grid)
     bool ft_force_wide = false;  // feature transform: 64-bit arithmetic at every size
     int ft_ring = 16;            // feature transform: envelope stack entries in shared memory per line
     vc::DevBuf ft_far;           // feature transform: tiles the window kernel left to the envelope kernel
@@ -426,9 +425,7 @@ __device__ __forceinline__ T block_exclusive_sum(T v, T* smem, T* total) {
 // the block, whether *err was set when the block left (thread 0 reads it once
 // and shares it), so callers leave their loop together: no block waits
 // forever, and no thread of a block goes on while another leaves.
-// `nblocks` blocks take part (blocks 0 .. nblocks - 1; default: the grid).
-__device__ __forceinline__ bool grid_barrier(unsigned* bar, int* err, unsigned long long limit,
-                                             unsigned nblocks = 0) {
+__device__ __forceinline__ bool grid_barrier(unsigned* bar, int* err, unsigned long long limit) {
     __shared__ int s_stop;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -436,7 +433,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned* bar, int* err, unsigned l
         unsigned my_gen = *vgen;
         __threadfence();
         unsigned arrived = atomicAdd(bar, 1u);
-        if (arrived == (nblocks ? nblocks : gridDim.x) - 1) {
+        if (arrived == gridDim.x - 1) {
             atomicExch(bar, 0u);
             __threadfence();
             atomicAdd(bar + 1, 1u);

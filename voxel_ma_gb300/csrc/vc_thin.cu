@@ -82,8 +82,6 @@ struct ThinArgs {
     unsigned long long spin_limit;
     int64_t* trace;  // optional: per generation {items, t_A, t_B, t_C} (global timer, ns)
     int trace_cap;
-    int64_t tail_items;  // a generation below this size and all after it run on tail_blocks blocks
-    int tail_blocks;     // (0: never)
 };
 
 __device__ __forceinline__ int64_t global_ns() {
@@ -232,7 +230,6 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
     __shared__ int s_ncell, s_start, s_gbase;
     __shared__ int2 s_cells[4 * THREADS * ITEMS];
     const int G = gridDim.x, b = blockIdx.x;
-    int act = G;  // blocks taking part (the grid, then tail_blocks once the generations are small)
     const float l_t = A.thr[1];
     int64_t n = A.ctl[0];
     int64_t base = 0, pushes = n;
@@ -249,7 +246,7 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
         // warp range are counted (blk) by the phase that places them
         const int W = blockDim.x >> 5;
         int64_t* blk = A.blk_cnt + (int64_t)par * G * W;
-        const int64_t chunk = (n + act - 1) / act;
+        const int64_t chunk = (n + G - 1) / G;
         const int64_t wchunk = (chunk + W - 1) / W;
         auto range_of = [&](int64_t i) {
             const int64_t bi = i / chunk;
@@ -266,7 +263,7 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
         // (phase B of this generation writes them after the barrier below)
         if (n > slots_ready) {
             const int64_t lo4 = 4 * slots_ready, hi4 = 4 * n;
-            for (int64_t k = lo4 + (int64_t)b * blockDim.x + threadIdx.x; k < hi4; k += (int64_t)act * blockDim.x)
+            for (int64_t k = lo4 + (int64_t)b * blockDim.x + threadIdx.x; k < hi4; k += (int64_t)G * blockDim.x)
                 __stcg(A.child + k, make_int2(-1, -1));
             slots_ready = n;
         }
@@ -401,7 +398,7 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                 s_ncell = 0;
             }
         }
-        if (grid_barrier(A.bar, A.err, A.spin_limit, (unsigned)act)) break;
+        if (grid_barrier(A.bar, A.err, A.spin_limit)) break;
         // ---- phase B: a listed cell still at 1 gives its child to the item
         // that decremented it last (its trig position), in the cell's slot
         if (tr) A.trace[4 * gen + 2] = global_ns();
@@ -409,7 +406,7 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
             // contiguous share of the list: cells listed by neighbouring items
             // stay together, as do the records they touch
             const int64_t m = __ldcg(ctr + 0);
-            const int64_t mchunk = (m + act - 1) / act;
+            const int64_t mchunk = (m + G - 1) / G;
             const int64_t j1 = min(m, ((int64_t)b + 1) * mchunk);
             for (int64_t jb = (int64_t)b * mchunk; jb < j1; jb += blockDim.x) {
                 const int64_t j = jb + threadIdx.x;
@@ -454,13 +451,13 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                     atomicAdd((unsigned long long*)(blk + bi), (unsigned long long)__popc(grp));
             }
         }
-        if (grid_barrier(A.bar, A.err, A.spin_limit, (unsigned)act)) break;
+        if (grid_barrier(A.bar, A.err, A.spin_limit)) break;
         // ---- phase C: prefixes, write generation g+1 and make its claims;
         // each warp writes its range on its own (no block-wide step per item)
         if (tr) A.trace[4 * gen + 3] = global_ns();
         {
             int64_t before = 0, all = 0;
-            const int64_t nr = (int64_t)act * W, mine = (int64_t)b * W;
+            const int64_t nr = (int64_t)G * W, mine = (int64_t)b * W;
             for (int64_t k = threadIdx.x; k < nr; k += blockDim.x) {
                 const int64_t v = __ldcg(blk + k);
                 all += v;
@@ -533,14 +530,7 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
         n = total;
         pushes += total;
         ++gen;
-        if (grid_barrier(A.bar, A.err, A.spin_limit, (unsigned)act)) break;
-        // the small generations at the end: fewer blocks, cheaper barriers
-        // (every block sees the same n, so all decide alike, right after a
-        // barrier that every block has passed)
-        if (act == G && A.tail_blocks > 0 && A.tail_blocks < G && n > 0 && n < A.tail_items) {
-            act = A.tail_blocks;
-            if (b >= act) break;
-        }
+        if (grid_barrier(A.bar, A.err, A.spin_limit)) break;
     }
     atomicAdd((unsigned long long*)&A.ctl[2], (unsigned long long)my_processed);
     atomicAdd((unsigned long long*)&A.ctl[3], (unsigned long long)my_skipped);
@@ -697,8 +687,6 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats, bool all_pass) {
     A.bar = reinterpret_cast<unsigned*>(ctl + 8);
 
     A.spin_limit = c->spin_limit;
-    A.tail_items = c->thin_tail_items;
-    A.tail_blocks = c->thin_tail_blocks;
     if (c->trace_cap > 0) {
         VC_TRY(ensure_n<int64_t>(c, c->trace, 4 * (int64_t)c->trace_cap));
         VC_CUDA(c, cudaMemsetAsync(c->trace.p, 0, 4 * sizeof(int64_t) * c->trace_cap, c->stream));
@@ -822,13 +810,6 @@ int vc_debug_thin_shape(vc_ctx* c, int threads, int blocks_per_sm, int items) {
     c->thin_threads = threads;
     c->thin_blocks_per_sm = blocks_per_sm;
     c->thin_items = items == 2 ? 2 : 1;
-    return VC_OK;
-}
-
-int vc_debug_thin_tail(vc_ctx* c, int64_t items, int blocks) {
-    if (!c || items < 0 || blocks < 0) return VC_ERR_ARG;
-    c->thin_tail_items = items;
-    c->thin_tail_blocks = blocks;
     return VC_OK;
 }
 

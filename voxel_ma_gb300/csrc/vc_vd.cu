@@ -338,8 +338,9 @@ __global__ void __launch_bounds__(128) vd_segments_kernel(const uint32_t* __rest
 __global__ void __launch_bounds__(128) vd_vertices_kernel(VolTab T, Bases B, const SegPlanes* __restrict__ planes,
                                                           const int32_t* __restrict__ vb, const int32_t* __restrict__ eb,
                                                           const int32_t* __restrict__ fbs, float* __restrict__ vts,
-                                                          VertRec* __restrict__ V, const EdgeRec* __restrict__ E,
-                                                          int32_t* __restrict__ g0, int64_t ne) {
+                                                          uint32_t* __restrict__ vlat, VertRec* __restrict__ V,
+                                                          const EdgeRec* __restrict__ E, int32_t* __restrict__ g0,
+                                                          int64_t ne) {
     const int lane = threadIdx.x & 31;
     const int64_t nseg = T.total(kLSeg);
     VolTab::Cache vcache;
@@ -363,6 +364,7 @@ __global__ void __launch_bounds__(128) vd_vertices_kernel(VolTab T, Bases B, con
                 vts[3 * (int64_t)v + 1] = (float)b;
                 vts[3 * (int64_t)v + 2] = (float)c;
             }
+            if (vlat) vlat[v] = (uint32_t)((((int64_t)a * S.NB + b) * (T.dim(bv).z + 1)) + c);  // within its volume
             if (!V) continue;
             unsigned k = 0;
             unsigned long long idsum = 0;
@@ -938,6 +940,8 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes, double t_thr) {
         VC_TRY(ensure_n<float>(c, c->vts, 3 * nv));
         VC_TRY(ensure_n<int2>(c, c->edges, ne));
         VC_TRY(ensure_n<int32_t>(c, c->tris, 3 * nt));
+    } else {
+        VC_TRY(ensure_n<uint32_t>(c, c->vd_vlat, nv));  // each vertex's lattice point, for the remaining complex
     }
     VC_TRY(ensure_n<float>(c, c->vd_lam, nface));  // lambda per face
     if (folded) {
@@ -969,7 +973,8 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes, double t_thr) {
             Region k(c, "vd_vertices");
             vd_vertices_kernel<<<seg_grid(c, nseg), 128, 0, c->stream>>>(
                 c->tab, c->bases, planes, vb, eb, fb, geom ? ptr<float>(c->vts) : nullptr,
-                folded ? ptr<VertRec>(c->vert_rec) : nullptr, folded ? ptr<EdgeRec>(c->edge_rec) : nullptr, g0, ne);
+                geom ? nullptr : ptr<uint32_t>(c->vd_vlat), folded ? ptr<VertRec>(c->vert_rec) : nullptr,
+                folded ? ptr<EdgeRec>(c->edge_rec) : nullptr, g0, ne);
             launched(c);
         }
         VC_CUDA(c, cudaGetLastError());
@@ -1015,7 +1020,8 @@ int ensure_vd_geometry(vc_ctx* c) {
                                                                ptr<float>(c->vd_lam), ptr<int2>(c->edges), nullptr,
                                                                nullptr, nullptr);
     vd_vertices_kernel<<<seg_grid(c, nseg), 128, 0, c->stream>>>(c->tab, c->bases, planes, vb, eb, fb,
-                                                                  ptr<float>(c->vts), nullptr, nullptr, nullptr, ne);
+                                                                  ptr<float>(c->vts), nullptr, nullptr, nullptr,
+                                                                  nullptr, ne);
     launched(c, 3);
     VC_CUDA(c, cudaGetLastError());
     c->vd_geom = true;
@@ -1024,37 +1030,27 @@ int ensure_vd_geometry(vc_ctx* c) {
 
 namespace {
 
-// Lattice point (a, b, c) of vertex v: its segment is the last one whose
-// first vertex id is <= v (the first ids are an exclusive scan of the
-// segments' vertex counts), and v is the (v - first)-th vertex bit in it.
-__device__ __forceinline__ void lattice_vertex(const VolTab& T, const SegPlanes* __restrict__ planes,
-                                               const int32_t* __restrict__ vb, int64_t nseg, int32_t v, float* o) {
-    int64_t lo = 0, hi = nseg;
-    while (hi - lo > 1) {
-        const int64_t mid = (lo + hi) >> 1;
-        if (__ldg(vb + mid) <= v) lo = mid;
-        else hi = mid;
-    }
-    const uint32_t m = __ldg(reinterpret_cast<const uint32_t*>(planes + lo));  // the vertex plane
-    const int bitpos = (int)__fns(m, 0, v - __ldg(vb + lo) + 1);
-    const int bv = T.find(kLSeg, lo);
+// Lattice point (a, b, c) of vertex v, from the lattice index the vertex
+// kernel recorded (within the vertex's volume).
+__device__ __forceinline__ void lattice_vertex(const VolTab& T, const Bases& B, int nvol,
+                                               const uint32_t* __restrict__ vlat, int32_t v, float* o) {
+    const int bv = nvol > 1 ? find_base(B.b[kBVert], nvol, v) : 0;
     const int4 d = T.dim(bv);
-    const int nsr = (d.z + 32) / 32;
-    const int64_t ls = lo - T.start(kLSeg, bv);
-    const int64_t row = ls / nsr;
-    const int NB = d.y + 1;
-    o[0] = (float)(row / NB);
-    o[1] = (float)(row % NB);
-    o[2] = (float)((int)(ls - row * nsr) * 32 + bitpos);
+    const uint32_t p = __ldg(vlat + v);
+    const uint32_t NC = (uint32_t)d.z + 1u, NB = (uint32_t)d.y + 1u;
+    const uint32_t ab = p / NC;
+    o[0] = (float)(ab / NB);
+    o[1] = (float)(ab % NB);
+    o[2] = (float)(p % NC);
 }
 
 // remainingCC of the lattice complex from the thinning records: a kept
-// vertex's coordinates from the lattice, a kept edge's ends from its record,
+// vertex's coordinates from its lattice point, a kept edge's ends from its record,
 // a kept triangle's corners from the records of its first two sides (sides
 // (a,b), (b,c), (c,a) in face order: b is the vertex the first two share).
-__global__ void vd_rem_write_kernel(int32_t nv, int32_t ne, int32_t nt, Kept K, VolTab T,
-                                    const SegPlanes* __restrict__ planes, const int32_t* __restrict__ vb,
-                                    int64_t nseg, const EdgeRec* __restrict__ E, const FaceRec* __restrict__ F,
+__global__ void vd_rem_write_kernel(int32_t nv, int32_t ne, int32_t nt, Kept K, VolTab T, int nvol,
+                                    const uint32_t* __restrict__ vlat, const EdgeRec* __restrict__ E,
+                                    const FaceRec* __restrict__ F,
                                     float* __restrict__ ovts, int2* __restrict__ oedges, int32_t* __restrict__ otris,
                                     Bases B, int nmap) {
     const int lane = threadIdx.x & 31;
@@ -1067,7 +1063,7 @@ __global__ void vd_rem_write_kernel(int32_t nv, int32_t ne, int32_t nt, Kept K, 
             const uint32_t word = __ldg(K.bv + w);
             if (!((word >> lane) & 1u)) continue;
             const int64_t o = __ldg(K.pv + w) + __popc(word & lowm);
-            lattice_vertex(T, planes, vb, nseg, (int32_t)(w * 32 + lane), ovts + 3 * o);
+            lattice_vertex(T, B, nvol, vlat, (int32_t)(w * 32 + lane), ovts + 3 * o);
         } else if (w < nwv + nwe) {
             const int64_t we = w - nwv;
             const uint32_t word = __ldg(K.be + we);
@@ -1103,8 +1099,8 @@ int lattice_rem_write(vc_ctx* c, const Kept& K, int nmap) {
     const int64_t nv = c->nv, ne = c->ne, nt = c->nt;
     const int64_t nw = (nv + 31) / 32 + (ne + 31) / 32 + (nt + 31) / 32;
     vd_rem_write_kernel<<<cell_grid(c, 32 * nw), 256, 0, c->stream>>>(
-        (int32_t)nv, (int32_t)ne, (int32_t)nt, K, c->tab, ptr<SegPlanes>(c->vd_seg), ptr<int32_t>(c->vd_voff),
-        c->h_off[kLSeg][c->nvol], ptr<EdgeRec>(c->edge_rec), ptr<FaceRec>(c->face_rec), ptr<float>(c->rem_vts),
+        (int32_t)nv, (int32_t)ne, (int32_t)nt, K, c->tab, c->nvol, ptr<uint32_t>(c->vd_vlat),
+        ptr<EdgeRec>(c->edge_rec), ptr<FaceRec>(c->face_rec), ptr<float>(c->rem_vts),
         ptr<int2>(c->rem_edges), ptr<int32_t>(c->rem_tris), c->bases, nmap);
     launched(c);
     VC_CUDA(c, cudaGetLastError());
