@@ -277,27 +277,16 @@ __global__ void __launch_bounds__(kWinThreads) ft_window_kernel(const int64_t* _
                 const bool active = q < L;
                 const int qm = q & kMask;
                 int64_t best;
-                // after offsets 1..r, a lane whose best is below (r + 1)^2 is final
-                // (no candidate further out can reach or tie it); the warp stops
-                // as soon as every lane is (every other offset, one vote each)
-                auto settled = [&](int r) {
-                    return __all_sync(0xffffffffu, !active || (best >> 32) < (int64_t)((r + 1) * (r + 1)));
-                };
                 if (qm >= kWinNear && qm <= kMask - kWinNear) {  // no wrap around the ring
                     const int64_t* c = sv + qm;
                     best = c[0];
 #pragma unroll
-                    for (int r = 1; r <= kWinNear; ++r) {
-                        best = min(best, min(c[-r], c[r]) + ((int64_t)(r * r) << 32));
-                        if ((r & 1) == 0 && r < kWinNear && settled(r)) break;
-                    }
+                    for (int r = 1; r <= kWinNear; ++r) best = min(best, min(c[-r], c[r]) + ((int64_t)(r * r) << 32));
                 } else {
                     best = sv[qm];
 #pragma unroll
-                    for (int r = 1; r <= kWinNear; ++r) {
+                    for (int r = 1; r <= kWinNear; ++r)
                         best = min(best, min(sv[(qm - r) & kMask], sv[(qm + r) & kMask]) + ((int64_t)(r * r) << 32));
-                        if ((r & 1) == 0 && r < kWinNear && settled(r)) break;
-                    }
                 }
                 const bool cont = active && (best >> 32) >= (kWinNear + 1) * (kWinNear + 1);
                 if (active && !cont) emit_at(o, best);
