@@ -29,10 +29,11 @@
 // lattice row, seven bit planes (vertex, valid axis edge per axis, valid
 // face per axis) and the three cell counts; after one scan of the segment
 // counts any cell's id is an O(1) population count.  The emission kernels
-// run one thread per lattice point (a warp per segment, so writes of
-// consecutive ids are coalesced) and write what the thinning and the
-// remaining complex read: vertex coordinates, edges, triangles and the
-// thinning records.  The measures, triangle faces, face sites, triangle
+// walk lattice rows, a warp per row and one lane per cell of a segment (so
+// writes of consecutive ids are coalesced), and write what the thinning and
+// the remaining complex read: the thinning records and each vertex's lattice
+// point, or, on demand, vertex coordinates, edges and triangles.  The
+// measures, triangle faces, face sites, triangle
 // sides and adjacency lists are written on demand (ensure_vd_aux), when a
 // getter or a thinning with explicit thresholds asks for them.
 #include "vc_internal.cuh"
@@ -49,10 +50,6 @@ struct Grid {
     const int32_t* lab;
     int X, Y, Z;
     int64_t NB, NC;
-    __device__ __forceinline__ bool inside(int i, int j, int k) const {
-        if (i < 0 || j < 0 || k < 0 || i >= X || j >= Y || k >= Z) return false;
-        return occ[((int64_t)i * Y + j) * Z + k] > 0;
-    }
     __device__ __forceinline__ int64_t lid(int a, int b, int c) const { return ((int64_t)a * NB + b) * NC + c; }
     __device__ __forceinline__ int32_t label(int a, int b, int c) const { return lab[lid(a, b, c)]; }
 };
@@ -135,11 +132,6 @@ __device__ __forceinline__ SegPlanes load_planes(const SegPlanes* p) {
 __device__ __forceinline__ uint32_t below(int c) { return (1u << (c & 31)) - 1u; }
 __device__ __forceinline__ bool bit(uint32_t w, int c) { return (w >> (c & 31)) & 1u; }
 
-// batch-wide vertex id of the voxel at (a, b, c) (which must be a vertex)
-__device__ __forceinline__ int32_t vid_at(const Segs& S, int a, int b, int c) {
-    const int64_t s = S.at(a, b, c);
-    return __ldg(S.vb + s) + __popc(__ldg(&S.planes[s].v) & below(c));
-}
 // scan rank (batch-wide, axis edges only) of the axis edge (a, b, c) + d
 __device__ __forceinline__ int32_t erank_at(const Segs& S, int a, int b, int c, int d) {
     const int64_t s = S.at(a, b, c);
@@ -160,14 +152,11 @@ __device__ __forceinline__ int32_t fid_at(const Segs& S, int a, int b, int c, in
     if (d >= 2) r += bit(P.f1, c);
     return r;
 }
-__device__ __forceinline__ bool ebit_at(const Segs& S, int a, int b, int c, int d) {
-    return bit(plane_e(load_planes(S.planes + S.at(a, b, c)), d), c);
-}
 __device__ __forceinline__ bool fbit_at(const Segs& S, int a, int b, int c, int d) {
     return bit(plane_f(load_planes(S.planes + S.at(a, b, c)), d), c);
 }
 
-// Segment loop of the emission kernels: each block takes kSegChunk
+// Segment loop of the getter-only kernel: each block takes kSegChunk
 // consecutive segments at a time and its warps walk them in order, so the
 // neighbouring segments a warp reads stay in the block's L1 (rows of every
 // length pack into chunks, which keeps small volumes of a batch busy).
@@ -200,22 +189,37 @@ __device__ __forceinline__ float rec_measure(float m, const float* thr, int bv) 
     return m < thr[bv] ? -1.0f : 1.0f;
 }
 
+// Row loop of the row-walking kernels: each block takes kRowChunk
+// consecutive lattice rows at a time and its warps take every fourth one, so
+// the neighbouring rows that warps of a block read at once stay in its L1.
+constexpr int kRowChunk = 16;
+#define ROW_LOOP(gr, nrow)                                                                                 \
+    for (int64_t row_base_ = (int64_t)blockIdx.x * kRowChunk; row_base_ < (nrow);                          \
+         row_base_ += (int64_t)gridDim.x * kRowChunk)                                                        \
+        for (int64_t gr = row_base_ + (threadIdx.x >> 5), row_end_ = min((int64_t)(nrow), row_base_ + kRowChunk); \
+             gr < row_end_; gr += blockDim.x >> 5)
+
 // Per lattice point: whether its voxel is a vertex (inside, not all 8
 // corner labels equal -- tagVert plus "corner of some Voronoi face"),
 // whether each axis edge is valid (both voxels inside, the shared square's
 // 4 labels not all equal) and whether each lattice edge carries a valid
 // face (labels differ and the 4 voxels around it inside).  One warp per
-// 32-point segment of a lattice row, lane = point: the occupancy tests run
-// for the whole segment at once on the packed voxel words (bit t of a row's
-// word = voxel c0 + t; shifted copies give c0 + t - 1 and c0 + t + 1), the
-// label tests run per lane (the c + 1 labels come from the next lane) and
-// ballots turn them into bit planes.  Also the volumes' vertex bounding
-// boxes (VoroInfo::getInsidePartSize reads them).
-__global__ void __launch_bounds__(128) vd_segments_kernel(const uint32_t* __restrict__ obits,
-                                                          const int32_t* __restrict__ lab, VolTab T,
-                                                          SegPlanes* __restrict__ planes, int32_t* __restrict__ cv,
-                                                          int32_t* __restrict__ ce, int32_t* __restrict__ cf,
-                                                          int32_t* __restrict__ bbox_all) {
+// lattice row, walking its 32-point segments in order, lane = point: the
+// occupancy tests run for the whole segment at once on the packed voxel
+// words (bit t of a row's word = voxel c0 + t; shifted copies give
+// c0 + t - 1 and c0 + t + 1).  Lanes 0-5 each own one of the six voxel rows
+// around the lattice row and carry its words; shuffles hand the combined
+// words to the warp.  The label tests run per lane on four label rows (the
+// c + 1 labels come from the next lane, and for lane 31 from the next
+// segment's labels); labels and words are requested two segments ahead of
+// the one computed.  Ballots turn the tests into bit planes.  Also the
+// volumes' vertex bounding boxes (VoroInfo::getInsidePartSize reads them).
+__global__ void __launch_bounds__(128, 6) vd_segments_kernel(const uint32_t* __restrict__ obits,
+                                                             const int32_t* __restrict__ lab, VolTab T,
+                                                             SegPlanes* __restrict__ planes, int32_t* __restrict__ cv,
+                                                             int32_t* __restrict__ ce, int32_t* __restrict__ cf,
+                                                             int32_t* __restrict__ bbox_all) {
+    const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     int cur_bv = -1;
     // warp-uniform bounding box of the current volume's vertices
@@ -233,203 +237,145 @@ __global__ void __launch_bounds__(128) vd_segments_kernel(const uint32_t* __rest
         mn0 = mn1 = mn2 = INT32_MAX;
         mx0 = mx1 = mx2 = INT32_MIN;
     };
-    const int64_t nseg = T.total(kLSeg);
+    // voxel row owned by lanes 0-5: (a-1,b-1), (a-1,b), (a,b-1), (a,b), (a+1,b), (a,b+1)
+    const int di = (lane == 0 || lane == 1) ? -1 : (lane == 4 ? 1 : 0);
+    const int dj = (lane == 0 || lane == 2) ? -1 : (lane == 5 ? 1 : 0);
+    const int64_t nrow = T.total(kLRow);
     VolTab::Cache vcache;
-    SEG_LOOP(gs, nseg) {
-        const int bv = T.find_cached(kLSeg, gs, vcache);
+    ROW_LOOP(gr, nrow) {
+        const int bv = T.find_cached(kLRow, gr, vcache);
         if (bv != cur_bv) {
             flush();
             cur_bv = bv;
         }
         const int4 dm = T.dim(bv);
         const int X = dm.x, Y = dm.y, Z = dm.z;
-        const int64_t NB = Y + 1, NC = Z + 1;
-        const int nsr = (Z + 32) / 32;
-        const int64_t ls = gs - T.start(kLSeg, bv);
-        const int64_t row = ls / nsr;
-        const int c0 = (int)(ls - row * nsr) * 32;
-        const int a = (int)(row / NB), b = (int)(row - (int64_t)a * NB);
-        // occupancy words of the voxel rows around the segment
-        const int sw = c0 >> 5, Wz = (Z + 31) >> 5;
-        const uint32_t* ob = obits + T.start(kVWord, bv);
-        auto word = [&](int i, int j, int w) -> uint32_t {
-            return (i >= 0 && i < X && j >= 0 && j < Y && w >= 0 && w < Wz) ? __ldg(ob + ((int64_t)i * Y + j) * Wz + w)
-                                                                           : 0u;
+        const int NB = Y + 1, NC = Z + 1;
+        const int nsr = (Z + 32) / 32, Wz = (Z + 31) >> 5;
+        const int lr = (int)(gr - T.start(kLRow, bv));
+        const int a = lr / NB, b = lr - a * NB;
+        const int64_t seg_row = T.start(kLSeg, bv) + (int64_t)lr * nsr;
+        // this lane's voxel row (lanes 0-5), or none
+        const int ri = a + di, rj = b + dj;
+        const bool rok = lane < 6 && ri >= 0 && ri < X && rj >= 0 && rj < Y;
+        const uint32_t* rp = obits + T.start(kVWord, bv) + (rok ? ((int64_t)ri * Y + rj) * Wz : 0);
+        auto wload = [&](int w) -> uint32_t { return (rok && w < Wz) ? __ldg(rp + w) : 0u; };
+        // label rows (a,b), (a,b+1), (a+1,b), (a+1,b+1): corners 0, 2, 4, 6 of the voxel
+        const int32_t* l0 = lab + T.start(kLat, bv) + ((int64_t)a * NB + b) * NC;
+        const bool ok2 = b + 1 <= Y, ok4 = a + 1 <= X, ok6 = ok2 && ok4;
+        const int32_t* l2 = l0 + (ok2 ? NC : 0);
+        const int32_t* l4 = l0 + (ok4 ? (int64_t)NB * NC : 0);
+        const int32_t* l6 = l0 + (ok6 ? (int64_t)NB * NC + NC : 0);
+        // labels (corners 0, 2, 4, 6 at the lane's point) and voxel words of
+        // segments k (L*, wcur), k + 1 (M*, w1) and k + 2 (N*, w2)
+        int32_t L0, L2, L4, L6, M0, M2, M4, M6, N0, N2, N4, N6;
+        auto lrow = [&](int cc, int32_t& x0, int32_t& x2, int32_t& x4, int32_t& x6) {
+            const bool v = cc < NC;
+            x0 = v ? __ldg(l0 + cc) : -1;
+            x2 = (v && ok2) ? __ldg(l2 + cc) : -1;
+            x4 = (v && ok4) ? __ldg(l4 + cc) : -1;
+            x6 = (v && ok6) ? __ldg(l6 + cc) : -1;
         };
-        // bit t: voxel (i, j, c0 + t - 1) / (i, j, c0 + t) / (i, j, c0 + t + 1) inside
-        struct Rw {
-            uint32_t m1, z0, p1;
-        };
-        auto rw = [&](int i, int j) {
-            const uint32_t prv = word(i, j, sw - 1), cur = word(i, j, sw), nxt = word(i, j, sw + 1);
-            return Rw{(cur << 1) | (prv >> 31), cur, (cur >> 1) | (nxt << 31)};
-        };
-        const Rw Rmm = rw(a - 1, b - 1), Rm0 = rw(a - 1, b), R0m = rw(a, b - 1), R00 = rw(a, b), Rp0 = rw(a + 1, b),
-                 R0p = rw(a, b + 1);
-        const uint32_t qx = R0m.m1 & R0m.z0 & R00.m1 & R00.z0;  // voxels (a, b-1..b, c-1..c)
-        const uint32_t qy = Rm0.m1 & Rm0.z0 & R00.m1 & R00.z0;  // voxels (a-1..a, b, c-1..c)
-        const uint32_t qz = Rmm.z0 & Rm0.z0 & R0m.z0 & R00.z0;  // voxels (a-1..a, b-1..b, c)
-        // labels of the voxel's 8 corners (a + qx, b + qy, c + qz), -1 outside the lattice
-        const int c = c0 + lane;
-        const bool valid = c < NC;
-        const int32_t* lb = lab + T.start(kLat, bv);
-        auto lat = [&](int i, int j, int k) -> int32_t {
-            return (i <= X && j <= Y && k <= Z) ? __ldg(lb + ((int64_t)i * NB + j) * NC + k) : -1;
-        };
-        int32_t L[8];
-        L[0] = valid ? lat(a, b, c) : -1;
-        L[2] = valid ? lat(a, b + 1, c) : -1;
-        L[4] = valid ? lat(a + 1, b, c) : -1;
-        L[6] = valid ? lat(a + 1, b + 1, c) : -1;
-#pragma unroll
-        for (int q = 0; q < 8; q += 2) {
-            L[q + 1] = __shfl_down_sync(0xffffffffu, L[q], 1);
-            if (lane == 31) L[q + 1] = valid ? lat(a + (q >> 2), b + ((q >> 1) & 1), c + 1) : -1;
-        }
-        bool alleq = true;
-#pragma unroll
-        for (int q = 1; q < 8; ++q) alleq &= (L[q] == L[0]);
-        auto differ = [](int32_t x, int32_t y) { return x >= 0 && y >= 0 && x != y; };
-        auto square_differs = [&](int bitd) {
-            int32_t ref = -2;
-            bool eq = true;
-#pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                if (!(q & bitd)) continue;
-                if (ref == -2) ref = L[q];
-                else eq &= (L[q] == ref);
+        lrow(lane, L0, L2, L4, L6);
+        lrow(32 + lane, M0, M2, M4, M6);
+        uint32_t wprv = 0u, wcur = wload(0), w1 = wload(1);
+        int zlo = -1, zhi = -1;  // first and last vertex point of the row
+        for (int k = 0; k < nsr; ++k) {
+            const int c0 = k * 32, c = c0 + lane;
+            lrow(c + 64, N0, N2, N4, N6);
+            const uint32_t w2 = wload(k + 2);
+            const bool valid = c < NC;
+            // bit t: voxel c0 + t - 1 / c0 + t / c0 + t + 1 inside, for this lane's voxel row
+            const uint32_t z0 = wcur;
+            const uint32_t m1 = (wcur << 1) | (wprv >> 31);
+            const uint32_t p1 = (wcur >> 1) | (w1 << 31);
+            const uint32_t g = m1 & z0;  // voxels c - 1 and c
+            const uint32_t g0m = __shfl_sync(full, g, 2), gm0 = __shfl_sync(full, g, 1), g00 = __shfl_sync(full, g, 3);
+            const uint32_t zmm = __shfl_sync(full, z0, 0), zm0 = __shfl_sync(full, z0, 1);
+            const uint32_t z0m = __shfl_sync(full, z0, 2), z00 = __shfl_sync(full, z0, 3);
+            const uint32_t zp0 = __shfl_sync(full, z0, 4), z0p = __shfl_sync(full, z0, 5);
+            const uint32_t p00 = __shfl_sync(full, p1, 3);
+            const uint32_t qx = g0m & g00;              // voxels (a, b-1..b, c-1..c)
+            const uint32_t qy = gm0 & g00;              // voxels (a-1..a, b, c-1..c)
+            const uint32_t qz = zmm & zm0 & z0m & z00;  // voxels (a-1..a, b-1..b, c)
+            // labels of the voxel's 8 corners (a + qx, b + qy, c + qz), -1 outside the lattice
+            int32_t L[8];
+            L[0] = L0;
+            L[2] = L2;
+            L[4] = L4;
+            L[6] = L6;
+            {
+                const int32_t nx0 = __shfl_sync(full, M0, 0), nx2 = __shfl_sync(full, M2, 0);
+                const int32_t nx4 = __shfl_sync(full, M4, 0), nx6 = __shfl_sync(full, M6, 0);
+                L[1] = __shfl_down_sync(full, L0, 1);
+                L[3] = __shfl_down_sync(full, L2, 1);
+                L[5] = __shfl_down_sync(full, L4, 1);
+                L[7] = __shfl_down_sync(full, L6, 1);
+                if (lane == 31) {
+                    L[1] = nx0;
+                    L[3] = nx2;
+                    L[5] = nx4;
+                    L[7] = nx6;
+                }
             }
-            return !eq;
-        };
-        SegPlanes P;
-        P.f0 = qx & __ballot_sync(0xffffffffu, valid && differ(L[0], L[4]));
-        P.f1 = qy & __ballot_sync(0xffffffffu, valid && differ(L[0], L[2]));
-        P.f2 = qz & __ballot_sync(0xffffffffu, valid && differ(L[0], L[1]));
-        P.v = R00.z0 & __ballot_sync(0xffffffffu, valid && !alleq);
-        P.e0 = P.v & Rp0.z0 & __ballot_sync(0xffffffffu, square_differs(4));
-        P.e1 = P.v & R0p.z0 & __ballot_sync(0xffffffffu, square_differs(2));
-        P.e2 = P.v & R00.p1 & __ballot_sync(0xffffffffu, square_differs(1));
-        P.pad = 0;
-        if (P.v) {
+            bool alleq = true;
+#pragma unroll
+            for (int q = 1; q < 8; ++q) alleq &= (L[q] == L[0]);
+            auto differ = [](int32_t x, int32_t y) { return x >= 0 && y >= 0 && x != y; };
+            // the 4 labels of the corners with bit bitd set not all equal
+            auto square_differs = [&](int bitd) {
+                int32_t ref = -2;
+                bool eq = true;
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    if (!(q & bitd)) continue;
+                    if (ref == -2) ref = L[q];
+                    else eq &= (L[q] == ref);
+                }
+                return !eq;
+            };
+            const uint32_t f0 = qx & __ballot_sync(full, valid && differ(L[0], L[4]));
+            const uint32_t f1 = qy & __ballot_sync(full, valid && differ(L[0], L[2]));
+            const uint32_t f2 = qz & __ballot_sync(full, valid && differ(L[0], L[1]));
+            const uint32_t v = z00 & __ballot_sync(full, valid && !alleq);
+            const uint32_t e0 = v & zp0 & __ballot_sync(full, square_differs(4));
+            const uint32_t e1 = v & z0p & __ballot_sync(full, square_differs(2));
+            const uint32_t e2 = v & p00 & __ballot_sync(full, square_differs(1));
+            if (v) {
+                if (zlo < 0) zlo = c0 + __ffs(v) - 1;
+                zhi = c0 + 31 - __clz(v);
+            }
+            if (lane == 0) {
+                const int64_t gs = seg_row + k;
+                reinterpret_cast<uint4*>(planes + gs)[0] = make_uint4(v, e0, e1, e2);
+                reinterpret_cast<uint4*>(planes + gs)[1] = make_uint4(f0, f1, f2, 0u);
+                cv[gs] = __popc(v);
+                ce[gs] = __popc(e0) + __popc(e1) + __popc(e2);
+                cf[gs] = __popc(f0) + __popc(f1) + __popc(f2);
+            }
+            // advance the pipeline by one segment
+            L0 = M0;
+            L2 = M2;
+            L4 = M4;
+            L6 = M6;
+            M0 = N0;
+            M2 = N2;
+            M4 = N4;
+            M6 = N6;
+            wprv = wcur;
+            wcur = w1;
+            w1 = w2;
+        }
+        if (zlo >= 0) {
             mn0 = min(mn0, a);
             mn1 = min(mn1, b);
-            mn2 = min(mn2, c0 + __ffs(P.v) - 1);
+            mn2 = min(mn2, zlo);
             mx0 = max(mx0, a);
             mx1 = max(mx1, b);
-            mx2 = max(mx2, c0 + 31 - __clz(P.v));
-        }
-        if (lane == 0) {
-            reinterpret_cast<uint4*>(planes + gs)[0] = make_uint4(P.v, P.e0, P.e1, P.e2);
-            reinterpret_cast<uint4*>(planes + gs)[1] = make_uint4(P.f0, P.f1, P.f2, 0u);
-            cv[gs] = __popc(P.v);
-            ce[gs] = __popc(P.e0) + __popc(P.e1) + __popc(P.e2);
-            cf[gs] = __popc(P.f0) + __popc(P.f1) + __popc(P.f2);
+            mx2 = max(mx2, zhi);
         }
     }
     flush();
-}
-
-// One block per lattice row of the batch, one thread per point (c = a
-// multiple of 32 plus the lane, so a warp is one segment): the row's
-// vertices (vts and, with records, their thinning records: incident edges
-// counted and summed).  Incident edges: the axis edges into the voxel from
-// -x, -y, -z, its own axis edges, then the diagonals of the faces (p1, d)
-// and (p3, d) that have it as q1 / q3.
-__global__ void __launch_bounds__(128) vd_vertices_kernel(VolTab T, Bases B, const SegPlanes* __restrict__ planes,
-                                                          const int32_t* __restrict__ vb, const int32_t* __restrict__ eb,
-                                                          const int32_t* __restrict__ fbs, float* __restrict__ vts,
-                                                          uint32_t* __restrict__ vlat, VertRec* __restrict__ V,
-                                                          const EdgeRec* __restrict__ E, int32_t* __restrict__ g0,
-                                                          int64_t ne) {
-    const int lane = threadIdx.x & 31;
-    const int64_t nseg = T.total(kLSeg);
-    VolTab::Cache vcache;
-    SEG_LOOP(gs, nseg) {
-        const int bv = T.find_cached(kLSeg, gs, vcache);
-        const Segs S = segs_of(T, bv, planes, vb, eb, fbs);
-        const Shift sh = shift_of(B, bv);
-        const int nsr_ = (T.dim(bv).z + 32) / 32;
-        const int64_t ls_ = gs - T.start(kLSeg, bv);
-        const int64_t row = ls_ / nsr_;
-        const int c0 = (int)(ls_ - row * nsr_) * 32;
-        const int a = (int)(row / S.NB), b = (int)(row - (int64_t)a * S.NB);
-        {
-            const int c = c0 + lane;
-            const int64_t s = S.at(a, b, c);
-            const SegPlanes P = load_planes(planes + s);
-            if (!bit(P.v, c)) continue;
-            const int32_t v = __ldg(vb + s) + __popc(P.v & below(c));
-            if (vts) {
-                vts[3 * (int64_t)v + 0] = (float)a;
-                vts[3 * (int64_t)v + 1] = (float)b;
-                vts[3 * (int64_t)v + 2] = (float)c;
-            }
-            if (vlat) vlat[v] = (uint32_t)((((int64_t)a * S.NB + b) * (T.dim(bv).z + 1)) + c);  // within its volume
-            if (!V) continue;
-            unsigned k = 0;
-            unsigned long long idsum = 0;
-            const int p[3] = {a, b, c};
-            // each neighbour segment is read once (its edge or face planes)
-            auto add_edge = [&](int x, int y, int z, int d) {  // axis edge (x,y,z)+d, if valid
-                const int64_t sq = S.at(x, y, z);
-                const uint4 pe = __ldg(reinterpret_cast<const uint4*>(planes + sq));  // v e0 e1 e2
-                const uint32_t pd = d == 0 ? pe.y : (d == 1 ? pe.z : pe.w);
-                if (!bit(pd, z)) return;
-                const uint32_t mk = below(z);
-                int32_t r = __ldg(eb + sq) + __popc(pe.y & mk) + __popc(pe.z & mk) + __popc(pe.w & mk);
-                if (d >= 1) r += bit(pe.y, z);
-                if (d >= 2) r += bit(pe.z, z);
-                ++k;
-                idsum += (unsigned)(r + (int32_t)sh.fb);
-            };
-            auto add_diag = [&](int x, int y, int z, int d) {  // diagonal of face (x,y,z)+d, if valid
-                const int64_t sq = S.at(x, y, z);
-                const uint4 pf = __ldg(reinterpret_cast<const uint4*>(planes + sq) + 1);  // f0 f1 f2 -
-                const uint32_t pd = d == 0 ? pf.x : (d == 1 ? pf.y : pf.z);
-                if (!bit(pd, z)) return;
-                const uint32_t mk = below(z);
-                int32_t r = __ldg(fbs + sq) + __popc(pf.x & mk) + __popc(pf.y & mk) + __popc(pf.z & mk);
-                if (d >= 1) r += bit(pf.x, z);
-                if (d >= 2) r += bit(pf.y, z);
-                ++k;
-                idsum += (unsigned)((int32_t)sh.eb1 + r);
-            };
-#pragma unroll
-            for (int d = 0; d < 3; ++d) {
-                if (p[d] == 0) continue;
-                int q[3] = {a, b, c};
-                q[d] -= 1;
-                add_edge(q[0], q[1], q[2], d);
-            }
-            {
-                const uint32_t mk = below(c);
-                int32_t r = __ldg(eb + s) + __popc(P.e0 & mk) + __popc(P.e1 & mk) + __popc(P.e2 & mk);
-#pragma unroll
-                for (int d = 0; d < 3; ++d)
-                    if (bit(plane_e(P, d), c)) {
-                        ++k;
-                        idsum += (unsigned)(r++ + (int32_t)sh.fb);
-                    }
-            }
-#pragma unroll
-            for (int d = 0; d < 3; ++d) {
-                const int u = (d + 1) % 3, w = (d + 2) % 3;
-                int p1[3] = {a, b, c}, p3[3] = {a, b, c};
-                p1[w] += 1;  // the vertex is q1 of face (p1, d)
-                p3[u] += 1;  // the vertex is q3 of face (p3, d)
-                add_diag(p1[0], p1[1], p1[2], d);
-                add_diag(p3[0], p3[1], p3[2], d);
-            }
-            VertRec r;
-            r.rs = rs_make(k, 0, idsum);
-            r.trig = 0;
-            r.rm = kAlive;
-            V[v] = r;
-            // generation 0: an EV pair when the one edge passes the filter
-            // (its record, written before, holds the folded measure)
-            g0[ne + v] = (k == 1 && E[idsum].em < 0.0f) ? (int32_t)idsum : -1;
-        }
-    }
 }
 
 // The faces of the axis edge (a,b,c)+d: the valid faces of the plaquette
@@ -477,157 +423,487 @@ __device__ __forceinline__ void for_plaquette_d(int d, const Segs& S, int a, int
     else for_plaquette<2>(S, a, b, c, fn);
 }
 
-// The row's axis edges: endpoints and, with records, thinning records
-// (incident triangles counted, summed and tested against the threshold;
-// measure = max lambda of the incident faces, voroinfo.cpp:1490-1538).
-// Face lambdas come from lamf (one per face, written by vd_faces_kernel).
-__global__ void __launch_bounds__(128, 8) vd_edges_kernel(VolTab T, Bases B, const SegPlanes* __restrict__ planes,
+// The cells of one segment that up to three of its planes name, in (point,
+// plane) order -- the order of their ids: slot r (r < the returned count)
+// gets point << 2 | plane of the r-th cell.  Lane = point; the warp's slot
+// array holds 96 entries.
+__device__ __forceinline__ int compact_cells(uint32_t p0, uint32_t p1, uint32_t p2, int lane,
+                                             uint8_t* __restrict__ slots) {
+    const uint32_t m = below(lane);
+    int r = __popc(p0 & m) + __popc(p1 & m) + __popc(p2 & m);
+    if (bit(p0, lane)) slots[r++] = (uint8_t)(lane << 2);
+    if (bit(p1, lane)) slots[r++] = (uint8_t)(lane << 2 | 1);
+    if (bit(p2, lane)) slots[r] = (uint8_t)(lane << 2 | 2);
+    __syncwarp();
+    return __popc(p0) + __popc(p1) + __popc(p2);
+}
+
+// The emission kernels walk lattice rows (one warp per row, its segments in
+// order).  Per segment, the planes and first ids of the neighbouring rows
+// that the segment's cells refer to are loaded once by the whole warp (one
+// address per load), then the segment's cells are handed out one per lane in
+// id order (compact_cells), so every lane works and consecutive ids are
+// written by consecutive lanes.  A neighbour's id is then a population count
+// of those words: at point c of a row, the vertex / axis edges / faces before
+// c are first id + popcount(planes & below(c)); a neighbour at c - 1 (which
+// the rules make a vertex, or an edge or face whose bit is tested) is the last
+// one before c, and one at c + 1 the first one after c.  Bits at c - 1 and
+// c + 1 come from plane words shifted by one point, whose end bit is read
+// from the previous / next segment only when lane 0 / lane 31 needs it.
+struct RowPlanes {  // one row's segment: planes and first ids
+    uint32_t v, e0, e1, e2, f0, f1, f2;
+    int32_t vb, eb, fb;
+};
+__device__ __forceinline__ RowPlanes row_planes(const SegPlanes* __restrict__ planes, const int32_t* __restrict__ vb,
+                                                const int32_t* __restrict__ eb, const int32_t* __restrict__ fbs,
+                                                int64_t s, bool want_ve, bool want_f) {
+    RowPlanes R{};
+    if (s < 0) return R;
+    if (want_ve) {
+        const uint4 x = __ldg(reinterpret_cast<const uint4*>(planes + s));
+        R.v = x.x;
+        R.e0 = x.y;
+        R.e1 = x.z;
+        R.e2 = x.w;
+        R.vb = __ldg(vb + s);
+        R.eb = __ldg(eb + s);
+    }
+    if (want_f) {
+        const uint4 y = __ldg(reinterpret_cast<const uint4*>(planes + s) + 1);
+        R.f0 = y.x;
+        R.f1 = y.y;
+        R.f2 = y.z;
+        R.fb = __ldg(fbs + s);
+    }
+    return R;
+}
+__device__ __forceinline__ int32_t pc3(uint32_t a, uint32_t b, uint32_t c, uint32_t m) {
+    return __popc(a & m) + __popc(b & m) + __popc(c & m);
+}
+__device__ __forceinline__ int32_t bt(uint32_t w, int t) { return (int32_t)((w >> t) & 1u); }
+// the face (if any) of row R's lattice edge at point t (t = lane index of c)
+// along axis ax, at c (nx = false) or at c + 1 (nx = true, with the row's
+// face planes shifted down one point in S0..S2); -1 when none
+__device__ __forceinline__ int32_t face_at(const RowPlanes& R, uint32_t S0, uint32_t S1, uint32_t S2, int t, bool nx,
+                                           int ax) {
+    const uint32_t m = below(t);
+    if (!nx) {
+        const uint32_t w = ax == 0 ? R.f0 : (ax == 1 ? R.f1 : R.f2);
+        if (!bt(w, t)) return -1;
+        return R.fb + pc3(R.f0, R.f1, R.f2, m) + (ax >= 1 ? bt(R.f0, t) : 0) + (ax >= 2 ? bt(R.f1, t) : 0);
+    }
+    const uint32_t w = ax == 0 ? S0 : (ax == 1 ? S1 : S2);
+    if (!bt(w, t)) return -1;
+    // faces before c + 1: those before c and those at c
+    const uint32_t mi = m | (1u << t);
+    return R.fb + pc3(R.f0, R.f1, R.f2, mi) + (ax >= 1 ? bt(S0, t) : 0) + (ax >= 2 ? bt(S1, t) : 0);
+}
+
+// Vertices (vts or, in the thinning path, each vertex's lattice point) and,
+// with records, their thinning records: incident edges counted and summed.
+// Incident edges: the axis edges into the voxel from -x, -y, -z, its own
+// axis edges, then the diagonals of the faces (p1, d) and (p3, d) that have
+// it as q1 / q3 (p1 = p + e_w, p3 = p + e_u).
+__global__ void __launch_bounds__(128) vd_vertices_kernel(VolTab T, Bases B, const SegPlanes* __restrict__ planes,
+                                                          const int32_t* __restrict__ vb, const int32_t* __restrict__ eb,
+                                                          const int32_t* __restrict__ fbs, float* __restrict__ vts,
+                                                          uint32_t* __restrict__ vlat, VertRec* __restrict__ V,
+                                                          const EdgeRec* __restrict__ E, int32_t* __restrict__ g0,
+                                                          int64_t ne) {
+    __shared__ uint8_t s_slots[4][96];
+    const int lane = threadIdx.x & 31;
+    uint8_t* slots = s_slots[threadIdx.x >> 5];
+    const int64_t nrow = T.total(kLRow);
+    VolTab::Cache vcache;
+    ROW_LOOP(gr, nrow) {
+        const int bv = T.find_cached(kLRow, gr, vcache);
+        const int4 dm = T.dim(bv);
+        const int NB = dm.y + 1, NC = dm.z + 1, nsr = (dm.z + 32) / 32;
+        const int lr = (int)(gr - T.start(kLRow, bv));
+        const int a = lr / NB, b = lr - a * NB;
+        if (a >= dm.x || b >= dm.y) continue;  // no voxel in this row
+        const Shift sh = shift_of(B, bv);
+        const int32_t fbv = (int32_t)sh.fb, eb1 = (int32_t)sh.eb1;
+        // rows (a,b), (a-1,b), (a,b-1), (a,b+1), (a+1,b)
+        const int64_t s0 = T.start(kLSeg, bv) + (int64_t)lr * nsr;
+        const int64_t sm0 = a >= 1 ? s0 - (int64_t)NB * nsr : -1;
+        const int64_t s0m = b >= 1 ? s0 - nsr : -1;
+        const int64_t s0p = s0 + nsr, sp0 = s0 + (int64_t)NB * nsr;
+        const uint32_t lat_row = (uint32_t)((int64_t)lr * NC);
+        // the vertex and edge planes of the row's segments, one segment ahead
+        uint4 pv_next = __ldg(reinterpret_cast<const uint4*>(planes + s0));
+        for (int k = 0; k < nsr; ++k) {
+            const uint4 pv = pv_next;
+            if (k + 1 < nsr) pv_next = __ldg(reinterpret_cast<const uint4*>(planes + s0 + k + 1));
+            if (pv.x == 0u) continue;
+            const RowPlanes R0 = row_planes(planes, vb, eb, fbs, s0 + k, true, V != nullptr);
+            const int n = compact_cells(R0.v, 0u, 0u, lane, slots);
+            if (V) {
+                const RowPlanes Rm0 = row_planes(planes, vb, eb, fbs, sm0 < 0 ? -1 : sm0 + k, true, false);
+                const RowPlanes R0m = row_planes(planes, vb, eb, fbs, s0m < 0 ? -1 : s0m + k, true, false);
+                const RowPlanes R0p = row_planes(planes, vb, eb, fbs, s0p + k, false, true);
+                const RowPlanes Rp0 = row_planes(planes, vb, eb, fbs, sp0 + k, false, true);
+                // bit t of E2s: axis edge (c0 + t - 1) + z of the row; of F*s: face at c0 + t + 1
+                uint32_t pe2 = 0u, nf0 = 0u, nf1 = 0u;
+                if (k > 0 && (R0.v & 1u)) pe2 = __ldg(&planes[s0 + k - 1].e2);
+                if (k + 1 < nsr && (R0.v >> 31)) {
+                    const uint4 y = __ldg(reinterpret_cast<const uint4*>(planes + s0 + k + 1) + 1);
+                    nf0 = y.x;
+                    nf1 = y.y;
+                }
+                const uint32_t E2s = (R0.e2 << 1) | (pe2 >> 31);
+                const uint32_t F0s = (R0.f0 >> 1) | (nf0 << 31), F1s = (R0.f1 >> 1) | (nf1 << 31);
+                for (int r = lane; r < n; r += 32) {
+                    const int t = slots[r] >> 2;
+                    const int32_t v = R0.vb + r;
+                    const uint32_t m = below(t);
+                    const int c = 32 * k + t;
+                    if (vts) {
+                        vts[3 * (int64_t)v + 0] = (float)a;
+                        vts[3 * (int64_t)v + 1] = (float)b;
+                        vts[3 * (int64_t)v + 2] = (float)c;
+                    }
+                    if (vlat) vlat[v] = lat_row + (uint32_t)c;  // within its volume
+                    unsigned kk = 0;
+                    unsigned long long idsum = 0;
+                    // axis edges into the voxel from -x, -y, -z
+                    if (bt(Rm0.e0, t)) {
+                        ++kk;
+                        idsum += (unsigned)(Rm0.eb + pc3(Rm0.e0, Rm0.e1, Rm0.e2, m) + fbv);
+                    }
+                    if (bt(R0m.e1, t)) {
+                        ++kk;
+                        idsum += (unsigned)(R0m.eb + pc3(R0m.e0, R0m.e1, R0m.e2, m) + bt(R0m.e0, t) + fbv);
+                    }
+                    const int32_t e_own = R0.eb + pc3(R0.e0, R0.e1, R0.e2, m) + fbv;
+                    if (bt(E2s, t)) {  // the z edge of voxel c - 1: the last axis edge before c
+                        ++kk;
+                        idsum += (unsigned)(e_own - 1);
+                    }
+                    // its own axis edges
+                    {
+                        int32_t e = e_own;
+                        if (bt(R0.e0, t)) {
+                            ++kk;
+                            idsum += (unsigned)e++;
+                        }
+                        if (bt(R0.e1, t)) {
+                            ++kk;
+                            idsum += (unsigned)e++;
+                        }
+                        if (bt(R0.e2, t)) {
+                            ++kk;
+                            idsum += (unsigned)e;
+                        }
+                    }
+                    // diagonals: d = 0: (a,b,c+1)+x, (a,b+1,c)+x; d = 1: (a+1,b,c)+y,
+                    // (a,b,c+1)+y; d = 2: (a,b+1,c)+z, (a+1,b,c)+z
+                    const int32_t fd[6] = {face_at(R0, F0s, F1s, 0u, t, true, 0), face_at(R0p, 0u, 0u, 0u, t, false, 0),
+                                           face_at(Rp0, 0u, 0u, 0u, t, false, 1), face_at(R0, F0s, F1s, 0u, t, true, 1),
+                                           face_at(R0p, 0u, 0u, 0u, t, false, 2), face_at(Rp0, 0u, 0u, 0u, t, false, 2)};
+#pragma unroll
+                    for (int i = 0; i < 6; ++i)
+                        if (fd[i] >= 0) {
+                            ++kk;
+                            idsum += (unsigned)(eb1 + fd[i]);
+                        }
+                    VertRec rec;
+                    rec.rs = rs_make(kk, 0, idsum);
+                    rec.trig = 0;
+                    rec.rm = kAlive;
+                    V[v] = rec;
+                    // generation 0: an EV pair when the one edge passes the filter
+                    // (its record, written before, holds the folded measure)
+                    g0[ne + v] = (kk == 1 && E[idsum].em < 0.0f) ? (int32_t)idsum : -1;
+                }
+            } else {
+                for (int r = lane; r < n; r += 32) {
+                    const int t = slots[r] >> 2;
+                    const int32_t v = R0.vb + r;
+                    const int c = 32 * k + t;
+                    if (vts) {
+                        vts[3 * (int64_t)v + 0] = (float)a;
+                        vts[3 * (int64_t)v + 1] = (float)b;
+                        vts[3 * (int64_t)v + 2] = (float)c;
+                    }
+                    if (vlat) vlat[v] = lat_row + (uint32_t)c;
+                }
+            }
+            __syncwarp();
+        }
+    }
+}
+
+// Axis edges: endpoints and, with records, thinning records (incident
+// triangles counted, summed and tested against the threshold; measure = max
+// lambda of the incident faces, voroinfo.cpp:1490-1538).  Face lambdas come
+// from lamf (one per face, written by vd_faces_kernel).  Lane = point: the
+// faces of the plaquettes of the point's three axis edges (the lattice edges
+// along u from nb and nb + e_w and along w from nb and nb + e_u, nb = the
+// point + e_d, u = d+1, w = d+2 mod 3) are nine lattice edges, looked up once
+// and their lambdas loaded together:
+//   d = 0: (a+1,b,c)+y, (a+1,b,c)+z [triangle 1]; (a+1,b,c+1)+y, (a+1,b+1,c)+z [0]
+//   d = 1: (a,b+1,c)+z, (a,b+1,c)+x [1]; (a+1,b+1,c)+z, (a,b+1,c+1)+x [0]
+//   d = 2: (a,b,c+1)+x, (a,b,c+1)+y [1]; (a,b+1,c+1)+x, (a+1,b,c+1)+y [0]
+// (the triangle of each face that carries the edge: 1 for the two faces at
+// nb).
+__global__ void __launch_bounds__(128) vd_edges_kernel(VolTab T, Bases B, const SegPlanes* __restrict__ planes,
                                                        const int32_t* __restrict__ vb, const int32_t* __restrict__ eb,
                                                        const int32_t* __restrict__ fbs, const float* __restrict__ lamf,
                                                        int2* __restrict__ edges, EdgeRec* __restrict__ E,
                                                        int32_t* __restrict__ g0, const float* __restrict__ thr) {
     const int lane = threadIdx.x & 31;
-    const int64_t nseg = T.total(kLSeg);
+    const int64_t nrow = T.total(kLRow);
     VolTab::Cache vcache;
-    SEG_LOOP(gs, nseg) {
-        const int bv = T.find_cached(kLSeg, gs, vcache);
-        const Segs S = segs_of(T, bv, planes, vb, eb, fbs);
-        const Shift sh = shift_of(B, bv);
-        const int nsr_ = (T.dim(bv).z + 32) / 32;
-        const int64_t ls_ = gs - T.start(kLSeg, bv);
-        const int64_t row = ls_ / nsr_;
-        const int c0 = (int)(ls_ - row * nsr_) * 32;
-        const int a = (int)(row / S.NB), b = (int)(row - (int64_t)a * S.NB);
+    ROW_LOOP(gr, nrow) {
+        const int bv = T.find_cached(kLRow, gr, vcache);
+        const int4 dm = T.dim(bv);
+        const int NB = dm.y + 1, nsr = (dm.z + 32) / 32;
+        const int lr = (int)(gr - T.start(kLRow, bv));
+        const int a = lr / NB, b = lr - a * NB;
+        if (a >= dm.x || b >= dm.y) continue;  // no voxel in this row
+        const int32_t fbv = (int32_t)shift_of(B, bv).fb;
         const float tb = thr ? thr[bv] : 0.0f;
-        {
-            const int c = c0 + lane;
-            const int64_t s = S.at(a, b, c);
-            const SegPlanes P = load_planes(planes + s);
-            const uint32_t m = below(c);
-            if (!bit(P.e0 | P.e1 | P.e2, c)) continue;
-            int32_t e = __ldg(eb + s) + __popc(P.e0 & m) + __popc(P.e1 & m) + __popc(P.e2 & m) + (int32_t)sh.fb;
-            const int32_t v0 = __ldg(vb + s) + __popc(P.v & m);
+        // rows (a,b), (a+1,b), (a,b+1), (a+1,b+1): all inside the lattice
+        const int64_t s0 = T.start(kLSeg, bv) + (int64_t)lr * nsr;
+        const int64_t sp0 = s0 + (int64_t)NB * nsr, s0p = s0 + nsr, spp = sp0 + nsr;
+        // the vertex and edge planes of the row's segments, one segment ahead
+        uint4 pv_next = __ldg(reinterpret_cast<const uint4*>(planes + s0));
+        for (int k = 0; k < nsr; ++k) {
+            const uint4 pv = pv_next;
+            if (k + 1 < nsr) pv_next = __ldg(reinterpret_cast<const uint4*>(planes + s0 + k + 1));
+            const uint32_t any_e = pv.y | pv.z | pv.w;
+            if (any_e == 0u) continue;
+            const RowPlanes R0 = row_planes(planes, vb, eb, fbs, s0 + k, true, E != nullptr);
+            const RowPlanes Rp0 = row_planes(planes, vb, eb, fbs, sp0 + k, true, E != nullptr);
+            const RowPlanes R0p = row_planes(planes, vb, eb, fbs, s0p + k, true, E != nullptr);
+            const int t = lane;
+            if (!bt(any_e, t)) continue;
+            const uint32_t m = below(t);
+            const int32_t v0 = R0.vb + __popc(R0.v & m);
+            int32_t e = R0.eb + pc3(R0.e0, R0.e1, R0.e2, m) + fbv;
+            // the +d neighbours: (a+1,b,c), (a,b+1,c), (a,b,c+1) (the vertex after v0 in its row)
+            const int32_t v1[3] = {Rp0.vb + __popc(Rp0.v & m), R0p.vb + __popc(R0p.v & m), v0 + 1};
+            if (!E) {
+#pragma unroll
+                for (int d = 0; d < 3; ++d)
+                    if (bt(d == 0 ? R0.e0 : (d == 1 ? R0.e1 : R0.e2), t)) edges[e++] = make_int2(v0, v1[d]);
+                continue;
+            }
+            const RowPlanes Rpp = row_planes(planes, vb, eb, fbs, spp + k, false, true);
+            // face planes at c + 1: lane 31 reads the next segment's first bits
+            uint4 n0 = make_uint4(0u, 0u, 0u, 0u), np0 = n0, n0p = n0;
+            if (k + 1 < nsr && (any_e >> 31)) {
+                n0 = __ldg(reinterpret_cast<const uint4*>(planes + s0 + k + 1) + 1);
+                np0 = __ldg(reinterpret_cast<const uint4*>(planes + sp0 + k + 1) + 1);
+                n0p = __ldg(reinterpret_cast<const uint4*>(planes + s0p + k + 1) + 1);
+            }
+            const uint32_t S00 = (R0.f0 >> 1) | (n0.x << 31), S01 = (R0.f1 >> 1) | (n0.y << 31);
+            const uint32_t Sp00 = (Rp0.f0 >> 1) | (np0.x << 31), Sp01 = (Rp0.f1 >> 1) | (np0.y << 31);
+            const uint32_t S0p0 = (R0p.f0 >> 1) | (n0p.x << 31);
+            const bool h0 = bt(R0.e0, t), h1 = bt(R0.e1, t), h2 = bt(R0.e2, t);
+            // the nine faces (-1: none), only those an edge of this point needs
+            int32_t fid[9];
+            fid[0] = h0 ? face_at(Rp0, 0u, 0u, 0u, t, false, 1) : -1;                   // (a+1,b,c)+y
+            fid[1] = h0 ? face_at(Rp0, 0u, 0u, 0u, t, false, 2) : -1;                   // (a+1,b,c)+z
+            fid[2] = (h0 || h2) ? face_at(Rp0, Sp00, Sp01, 0u, t, true, 1) : -1;        // (a+1,b,c+1)+y
+            fid[3] = (h0 || h1) ? face_at(Rpp, 0u, 0u, 0u, t, false, 2) : -1;           // (a+1,b+1,c)+z
+            fid[4] = h1 ? face_at(R0p, 0u, 0u, 0u, t, false, 2) : -1;                   // (a,b+1,c)+z
+            fid[5] = h1 ? face_at(R0p, 0u, 0u, 0u, t, false, 0) : -1;                   // (a,b+1,c)+x
+            fid[6] = (h1 || h2) ? face_at(R0p, S0p0, 0u, 0u, t, true, 0) : -1;          // (a,b+1,c+1)+x
+            fid[7] = h2 ? face_at(R0, S00, S01, 0u, t, true, 0) : -1;                   // (a,b,c+1)+x
+            fid[8] = h2 ? face_at(R0, S00, S01, 0u, t, true, 1) : -1;                   // (a,b,c+1)+y
+            float lj[9];
+#pragma unroll
+            for (int i = 0; i < 9; ++i) lj[i] = fid[i] >= 0 ? __ldg(lamf + fid[i]) : 0.0f;
+            // per axis: the four faces' slots (the first two carry the edge as triangle 1)
+            constexpr int kSlot[3][4] = {{0, 1, 2, 3}, {4, 5, 3, 6}, {7, 8, 6, 2}};
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
-                if (!bit(plane_e(P, d), c)) continue;
-                int nb[3] = {a, b, c};
-                nb[d] += 1;
-                const int32_t v1 = vid_at(S, nb[0], nb[1], nb[2]);
-                if (edges) edges[e] = make_int2(v0, v1);
-                if (E) {
-                    float mx = 0.0f;
-                    unsigned k = 0, npass = 0;
-                    unsigned long long idsum = 0;
-                    for_plaquette_d(d, S, a, b, c, [&](int32_t fid, int tri) {
-                        const float lj = __ldg(lamf + fid);
-                        mx = fmaxf(mx, lj);
-                        npass += lj < tb ? 1u : 0u;
-                        idsum += (unsigned)(2 * fid + tri);
-                        ++k;
-                    });
-                    EdgeRec r;
-                    r.v0 = v0;
-                    r.v1 = v1;
-                    r.rs = rs_make(k, npass, idsum);
-                    r.trig = 0;
-                    r.em = rec_measure(mx, thr, bv);
-                    r.rm = kAlive;
-                    r.pad = 0;
-                    E[e] = r;
-                    // generation 0: an FE pair when the one face passes the filter
-                    g0[e] = (k == 1 && npass == 1) ? (int32_t)idsum : -1;
+                if (!(d == 0 ? h0 : (d == 1 ? h1 : h2))) continue;
+                float mx = 0.0f;
+                unsigned kk = 0, npass = 0;
+                unsigned long long idsum = 0;
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const int s = kSlot[d][i];
+                    if (fid[s] >= 0) {
+                        mx = fmaxf(mx, lj[s]);
+                        npass += lj[s] < tb ? 1u : 0u;
+                        idsum += (unsigned)(2 * fid[s] + (i < 2 ? 1 : 0));
+                        ++kk;
+                    }
                 }
+                if (edges) edges[e] = make_int2(v0, v1[d]);
+                EdgeRec rec;
+                rec.v0 = v0;
+                rec.v1 = v1[d];
+                rec.rs = rs_make(kk, npass, idsum);
+                rec.trig = 0;
+                rec.em = rec_measure(mx, thr, bv);
+                rec.rm = kAlive;
+                rec.pad = 0;
+                E[e] = rec;
+                // generation 0: an FE pair when the one face passes the filter
+                g0[e] = (kk == 1 && npass == 1) ? (int32_t)idsum : -1;
                 ++e;
             }
         }
     }
 }
 
-// The row's faces: two triangles each (util::simpleTriangulate of the quad
-// (q0,q1,q2,q3): (q3,q0,q1), (q3,q1,q2)), the diagonal edge (q1,q3) and,
-// with records, the thinning records of both triangles and the diagonal.
-__global__ void __launch_bounds__(128, 8) vd_faces_kernel(VolTab T, Bases B, const SegPlanes* __restrict__ planes,
+// Faces: two triangles each (util::simpleTriangulate of the quad
+// (q0,q1,q2,q3): (q3,q0,q1), (q3,q1,q2)), the diagonal edge (q1,q3), the
+// face's lambda and, with records, the thinning records of both triangles
+// and the diagonal.  The quad of lattice edge (a,b,c)+d lies in rows R0
+// (a,b), R0m (a,b-1), Rm0 (a-1,b), Rmm (a-1,b-1) at points c - 1 and c:
+//   d = 0: q0 (a,b-1,c-1) q1 (a,b,c-1) q2 (a,b,c) q3 (a,b-1,c)
+//   d = 1: q0 (a-1,b,c-1) q1 (a-1,b,c) q2 (a,b,c) q3 (a,b,c-1)
+//   d = 2: q0 (a-1,b-1,c) q1 (a,b-1,c) q2 (a,b,c) q3 (a-1,b,c)
+// All four are vertices (inside, and the face's labels differ), so the one
+// at c - 1 is the last vertex before c in its row; its axis edge along dd is
+// (axis edges before c) minus its edges along the axes >= dd.
+__global__ void __launch_bounds__(128, 6) vd_faces_kernel(VolTab T, Bases B, const SegPlanes* __restrict__ planes,
                                                        const int32_t* __restrict__ vb, const int32_t* __restrict__ eb,
                                                        const int32_t* __restrict__ fbs, const int32_t* __restrict__ lab,
                                                        const float* __restrict__ sxyz, float* __restrict__ lamf,
                                                        int32_t* __restrict__ tris, int2* __restrict__ edges,
                                                        FaceRec* __restrict__ F, EdgeRec* __restrict__ E,
                                                        int32_t* __restrict__ g0, const float* __restrict__ thr) {
+    __shared__ uint8_t s_slots[4][96];
     const int lane = threadIdx.x & 31;
-    const int64_t nseg = T.total(kLSeg);
+    uint8_t* slots = s_slots[threadIdx.x >> 5];
+    const int64_t nrow = T.total(kLRow);
     VolTab::Cache vcache;
-    SEG_LOOP(gs, nseg) {
-        const int bv = T.find_cached(kLSeg, gs, vcache);
-        const Segs S = segs_of(T, bv, planes, vb, eb, fbs);
+    ROW_LOOP(gr, nrow) {
+        const int bv = T.find_cached(kLRow, gr, vcache);
+        const int4 dm = T.dim(bv);
+        const int NB = dm.y + 1, NC = dm.z + 1, nsr = (dm.z + 32) / 32;
+        const int lr = (int)(gr - T.start(kLRow, bv));
+        const int a = lr / NB, b = lr - a * NB;
+        if (a >= dm.x || b >= dm.y) continue;  // no face in this row
         const Shift sh = shift_of(B, bv);
-        const int32_t* lb = lab + T.start(kLat, bv);
-        const int64_t NC = T.dim(bv).z + 1;
-        const int nsr_ = (T.dim(bv).z + 32) / 32;
-        const int64_t ls_ = gs - T.start(kLSeg, bv);
-        const int64_t row = ls_ / nsr_;
-        const int c0 = (int)(ls_ - row * nsr_) * 32;
-        const int a = (int)(row / S.NB), b = (int)(row - (int64_t)a * S.NB);
-        const int32_t fbv = (int32_t)sh.fb;
-        {
-            const int c = c0 + lane;
-            const int64_t s = S.at(a, b, c);
-            const SegPlanes P = load_planes(planes + s);
-            if (!bit(P.f0 | P.f1 | P.f2, c)) continue;
-            const uint32_t m = below(c);
-            int32_t f = __ldg(fbs + s) + __popc(P.f0 & m) + __popc(P.f1 & m) + __popc(P.f2 & m);
-            const int64_t p = row * NC + c;
-            const int32_t l0 = __ldg(lb + p);
-#pragma unroll
-            for (int d = 0; d < 3; ++d) {
-                if (!bit(plane_f(P, d), c)) continue;
-                const int u = (d + 1) % 3, w = (d + 2) % 3;
-                // the quad's voxels: vertex ids and (q0, q1, q3) their axis-edge
-                // ranks, one 16-byte plane load (v, e0, e1, e2) per voxel
-                int32_t q[4], er[4];
-                uint4 pl[4];
-                int qz[4];
-#pragma unroll
-                for (int mm = 0; mm < 4; ++mm) {
-                    int x, y, z;
-                    quad_voxel(a, b, c, d, mm, x, y, z);
-                    const int64_t sm = S.at(x, y, z);
-                    pl[mm] = __ldg(reinterpret_cast<const uint4*>(S.planes + sm));
-                    qz[mm] = z;
-                    const uint32_t mk = below(z);
-                    q[mm] = __ldg(S.vb + sm) + __popc(pl[mm].x & mk);
-                    er[mm] = mm == 2 ? 0 : __ldg(S.eb + sm) + __popc(pl[mm].y & mk) + __popc(pl[mm].z & mk) +
-                                           __popc(pl[mm].w & mk);
+        const int32_t fbv = (int32_t)sh.fb, eb1 = (int32_t)sh.eb1;
+        const float tb = thr ? thr[bv] : 0.0f;
+        const int64_t s0 = T.start(kLSeg, bv) + (int64_t)lr * nsr;
+        const int64_t s0m = b >= 1 ? s0 - nsr : -1;
+        const int64_t sm0 = a >= 1 ? s0 - (int64_t)NB * nsr : -1;
+        const int64_t smm = (a >= 1 && b >= 1) ? sm0 - nsr : -1;
+        const int32_t* lrow = lab + T.start(kLat, bv) + (int64_t)lr * NC;
+        // the face planes (f0 f1 f2 -) of the row's segments, one segment ahead
+        uint4 fo_next = __ldg(reinterpret_cast<const uint4*>(planes + s0) + 1);
+        for (int k = 0; k < nsr; ++k) {
+            const uint4 fo = fo_next;
+            if (k + 1 < nsr) fo_next = __ldg(reinterpret_cast<const uint4*>(planes + s0 + k + 1) + 1);
+            if ((fo.x | fo.y | fo.z) == 0u) continue;
+            // the labels at the lane's point c and at c + e_x, c + e_y, c + e_z
+            // (rows a + 1 and b + 1 exist: a < X, b < Y), loaded with the planes
+            const int cl = 32 * k + lane;
+            const int32_t l_c = cl < NC ? __ldg(lrow + cl) : -1;
+            const int32_t l_x = cl < NC ? __ldg(lrow + (int64_t)NB * NC + cl) : -1;
+            const int32_t l_y = cl < NC ? __ldg(lrow + NC + cl) : -1;
+            const int32_t l_z = cl + 1 < NC ? __ldg(lrow + cl + 1) : -1;
+            const int n = compact_cells(fo.x, fo.y, fo.z, lane, slots);
+            const int32_t f_first = __ldg(fbs + s0 + k);
+            const RowPlanes R0 = row_planes(planes, vb, eb, fbs, s0 + k, true, false);
+            const RowPlanes R0m = row_planes(planes, vb, eb, fbs, s0m < 0 ? -1 : s0m + k, true, false);
+            const RowPlanes Rm0 = row_planes(planes, vb, eb, fbs, sm0 < 0 ? -1 : sm0 + k, true, false);
+            const RowPlanes Rmm = row_planes(planes, vb, eb, fbs, (smm < 0 || fo.z == 0u) ? -1 : smm + k, true, false);
+            // edge planes shifted up one point (bit t = point c - 1): lane 0
+            // reads the previous segment's last bits (faces along x and y
+            // only reach back to c - 1)
+            uint4 p0 = make_uint4(0u, 0u, 0u, 0u), p0m = p0, pm0 = p0;
+            if (k > 0 && ((fo.x | fo.y) & 1u)) {
+                p0 = __ldg(reinterpret_cast<const uint4*>(planes + s0 + k - 1));
+                if (s0m >= 0) p0m = __ldg(reinterpret_cast<const uint4*>(planes + s0m + k - 1));
+                if (sm0 >= 0) pm0 = __ldg(reinterpret_cast<const uint4*>(planes + sm0 + k - 1));
+            }
+            // per point (lane = point): vertices and axis edges before the
+            // point in each row, and the edge bits the quads read, for the
+            // face lanes to fetch by shuffle
+            const uint32_t ml = below(lane);
+            const int32_t pv0 = R0.vb + __popc(R0.v & ml), pv0m = R0m.vb + __popc(R0m.v & ml);
+            const int32_t pvm0 = Rm0.vb + __popc(Rm0.v & ml), pvmm = Rmm.vb + __popc(Rmm.v & ml);
+            const int32_t px0 = R0.eb + pc3(R0.e0, R0.e1, R0.e2, ml) + fbv;
+            const int32_t px0m = R0m.eb + pc3(R0m.e0, R0m.e1, R0m.e2, ml) + fbv;
+            const int32_t pxm0 = Rm0.eb + pc3(Rm0.e0, Rm0.e1, Rm0.e2, ml) + fbv;
+            const int32_t pxmm = Rmm.eb + pc3(Rmm.e0, Rmm.e1, Rmm.e2, ml) + fbv;
+            // bits at the point's c - 1 (edge planes shifted up one point) and at c
+            const int32_t pbits = bt((R0.e2 << 1) | (p0.w >> 31), lane) |                  // 0: (a,b,c-1)+z
+                                  bt((R0m.e1 << 1) | (p0m.z >> 31), lane) << 1 |           // 1: (a,b-1,c-1)+y
+                                  bt((R0m.e2 << 1) | (p0m.w >> 31), lane) << 2 |           // 2: (a,b-1,c-1)+z
+                                  bt(R0m.e0, lane) << 3 |                                  // 3: (a,b-1,c)+x
+                                  bt((Rm0.e0 << 1) | (pm0.y >> 31), lane) << 4 |           // 4: (a-1,b,c-1)+x
+                                  bt((Rm0.e1 << 1) | (pm0.z >> 31), lane) << 5 |           // 5: (a-1,b,c-1)+y
+                                  bt((Rm0.e2 << 1) | (pm0.w >> 31), lane) << 6 |           // 6: (a-1,b,c-1)+z
+                                  bt(Rmm.e0, lane) << 7;                                   // 7: (a-1,b-1,c)+x
+            for (int r0 = 0; r0 < n; r0 += 32) {
+                // every lane takes part in the shuffles; lanes past the last
+                // face skip the rest
+                const int r = r0 + lane;
+                const int sl = r < n ? slots[r] : 0;
+                const int t = sl >> 2, d = sl & 3;
+                const unsigned full = 0xffffffffu;
+                const int32_t s_c = __shfl_sync(full, l_c, t);
+                const int32_t s_x = __shfl_sync(full, l_x, t);
+                const int32_t s_y = __shfl_sync(full, l_y, t);
+                const int32_t s_z = __shfl_sync(full, l_z, t);
+                const int32_t v0 = __shfl_sync(full, pv0, t), v0m = __shfl_sync(full, pv0m, t);
+                const int32_t vm0 = __shfl_sync(full, pvm0, t), vmm = __shfl_sync(full, pvmm, t);
+                const int32_t x0 = __shfl_sync(full, px0, t), x0m = __shfl_sync(full, px0m, t);
+                const int32_t xm0 = __shfl_sync(full, pxm0, t), xmm = __shfl_sync(full, pxmm, t);
+                const int32_t bits = __shfl_sync(full, pbits, t);
+                if (r >= n) continue;
+                auto bb = [&](int i) { return (bits >> i) & 1; };
+                int32_t q0, q1, q2, q3, e01, e12, e32, e03;
+                if (d == 0) {
+                    q0 = v0m - 1;
+                    q1 = v0 - 1;
+                    q2 = v0;
+                    q3 = v0m;
+                    e01 = x0m - bb(2) - bb(1);  // q0 along y
+                    e12 = x0 - bb(0);           // q1 along z
+                    e32 = x0m + bb(3);          // q3 along y
+                    e03 = x0m - bb(2);          // q0 along z
+                } else if (d == 1) {
+                    q0 = vm0 - 1;
+                    q1 = vm0;
+                    q2 = v0;
+                    q3 = v0 - 1;
+                    e01 = xm0 - bb(6);                  // q0 along z
+                    e12 = xm0;                          // q1 along x
+                    e32 = x0 - bb(0);                   // q3 along z
+                    e03 = xm0 - bb(4) - bb(5) - bb(6);  // q0 along x
+                } else {
+                    q0 = vmm;
+                    q1 = v0m;
+                    q2 = v0;
+                    q3 = vm0;
+                    e01 = xmm;           // q0 along x
+                    e12 = x0m + bb(3);   // q1 along y
+                    e32 = xm0;           // q3 along x
+                    e03 = xmm + bb(7);   // q0 along y
                 }
-                // rank of voxel mm's axis edge along dd
-                auto erank = [&](int mm, int dd) {
-                    return er[mm] + (dd >= 1 ? (int)bit(pl[mm].y, qz[mm]) : 0) +
-                           (dd >= 2 ? (int)bit(pl[mm].z, qz[mm]) : 0);
-                };
-                const int32_t diag = (int32_t)sh.eb1 + f;
+                const int32_t f = f_first + r;
+                const int32_t diag = eb1 + f;
                 const int64_t t0 = 2 * (int64_t)f, t1 = t0 + 1;
                 if (tris) {
-                    tris[3 * t0 + 0] = q[3];
-                    tris[3 * t0 + 1] = q[0];
-                    tris[3 * t0 + 2] = q[1];
-                    tris[3 * t1 + 0] = q[3];
-                    tris[3 * t1 + 1] = q[1];
-                    tris[3 * t1 + 2] = q[2];
+                    tris[3 * t0 + 0] = q3;
+                    tris[3 * t0 + 1] = q0;
+                    tris[3 * t0 + 2] = q1;
+                    tris[3 * t1 + 0] = q3;
+                    tris[3 * t1 + 1] = q1;
+                    tris[3 * t1 + 2] = q2;
                 }
-                const int32_t dv0 = min(q[1], q[3]), dv1 = max(q[1], q[3]);
+                const int32_t dv0 = min(q1, q3), dv1 = max(q1, q3);
                 if (edges) edges[diag] = make_int2(dv0, dv1);
                 // lambda of the face: distance of its two sites (measureforMA_imp.h:1-4)
-                const int64_t p1 = p + (d == 0 ? S.NB * NC : (d == 1 ? NC : 1));
-                const float lm = lambda_of(sxyz, l0, __ldg(lb + p1));
+                const float lm = lambda_of(sxyz, s_c, d == 0 ? s_x : (d == 1 ? s_y : s_z));
                 lamf[f] = lm;
                 if (F) {
+                    const float lr_ = rec_measure(lm, thr, bv);
+                    const int32_t pass = lr_ < 0.0f ? kFacePass : 0;
                     // sides in traceFace order: (t0,t1), (t1,t2), (t2,t0)
-                    const int32_t e01 = erank(0, u) + fbv;
-                    const int32_t e12 = erank(1, w) + fbv;
-                    const int32_t e32 = erank(3, u) + fbv;
-                    const int32_t e03 = erank(0, w) + fbv;
-                    const float lr = rec_measure(lm, thr, bv);
-                    const int32_t pass = lr < 0.0f ? kFacePass : 0;
-                    // both triangles' records: one 32-byte sector
                     FaceRec fr;
                     fr.rm = kAlive;
                     fr.e0 = e03;
@@ -641,16 +917,16 @@ __global__ void __launch_bounds__(128, 8) vd_faces_kernel(VolTab T, Bases B, con
                     EdgeRec er;
                     er.v0 = dv0;
                     er.v1 = dv1;
-                    er.rs = rs_make(2, lm < thr[bv] ? 2u : 0u, (unsigned long long)t0 + (unsigned long long)t1);
+                    er.rs = rs_make(2, lm < tb ? 2u : 0u, (unsigned long long)t0 + (unsigned long long)t1);
                     er.trig = 0;
-                    er.em = lr;
+                    er.em = lr_;
                     er.rm = kAlive;
                     er.pad = 0;
                     E[diag] = er;
                     g0[diag] = -1;  // two triangles: no FE pair
                 }
-                ++f;
             }
+            __syncwarp();
         }
     }
 }
@@ -871,6 +1147,11 @@ inline int seg_grid(vc_ctx* c, int64_t nseg) {
     return (int)std::max<int64_t>(1, std::min<int64_t>((nseg + kSegChunk - 1) / kSegChunk, (int64_t)c->num_sms * 16));
 }
 
+// 128-thread blocks, kRowChunk lattice rows per block at a time (grid-stride)
+inline int row_grid(vc_ctx* c, int64_t nrow) {
+    return (int)std::max<int64_t>(1, std::min<int64_t>((nrow + kRowChunk - 1) / kRowChunk, (int64_t)c->num_sms * 16));
+}
+
 }  // namespace
 
 int build_adjacency(vc_ctx* c);
@@ -901,7 +1182,7 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes, double t_thr) {
     {
         Region r(c, "vd_flags");
         // the packed occupancy words of the site extraction (same volumes)
-        vd_segments_kernel<<<seg_grid(c, nseg), 128, 0, c->stream>>>(ptr<uint32_t>(c->site_bits),
+        vd_segments_kernel<<<row_grid(c, c->h_off[kLRow][nvol]), 128, 0, c->stream>>>(ptr<uint32_t>(c->site_bits),
                                                                        ptr<int32_t>(c->ft_id), c->tab, planes, vb, eb,
                                                                        fb, c->bases.bbox);
         launched(c);
@@ -956,7 +1237,7 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes, double t_thr) {
         int32_t* g0 = folded ? ptr<int32_t>(c->thin_g0) : nullptr;
         {
             Region k(c, "vd_faces");
-            vd_faces_kernel<<<seg_grid(c, nseg), 128, 0, c->stream>>>(
+            vd_faces_kernel<<<row_grid(c, c->h_off[kLRow][c->nvol]), 128, 0, c->stream>>>(
                 c->tab, c->bases, planes, vb, eb, fb, ptr<int32_t>(c->ft_id), ptr<float>(c->site_xyz),
                 ptr<float>(c->vd_lam), geom ? ptr<int32_t>(c->tris) : nullptr, geom ? ptr<int2>(c->edges) : nullptr,
                 folded ? ptr<FaceRec>(c->face_rec) : nullptr, folded ? ptr<EdgeRec>(c->edge_rec) : nullptr, g0, thr);
@@ -964,14 +1245,14 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes, double t_thr) {
         }
         {
             Region k(c, "vd_edges");
-            vd_edges_kernel<<<seg_grid(c, nseg), 128, 0, c->stream>>>(
+            vd_edges_kernel<<<row_grid(c, c->h_off[kLRow][c->nvol]), 128, 0, c->stream>>>(
                 c->tab, c->bases, planes, vb, eb, fb, ptr<float>(c->vd_lam), geom ? ptr<int2>(c->edges) : nullptr,
                 folded ? ptr<EdgeRec>(c->edge_rec) : nullptr, g0, thr);
             launched(c);
         }
         {
             Region k(c, "vd_vertices");
-            vd_vertices_kernel<<<seg_grid(c, nseg), 128, 0, c->stream>>>(
+            vd_vertices_kernel<<<row_grid(c, c->h_off[kLRow][c->nvol]), 128, 0, c->stream>>>(
                 c->tab, c->bases, planes, vb, eb, fb, geom ? ptr<float>(c->vts) : nullptr,
                 geom ? nullptr : ptr<uint32_t>(c->vd_vlat), folded ? ptr<VertRec>(c->vert_rec) : nullptr,
                 folded ? ptr<EdgeRec>(c->edge_rec) : nullptr, g0, ne);
@@ -1006,20 +1287,19 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes, double t_thr) {
 int ensure_vd_geometry(vc_ctx* c) {
     if (!c->vd_valid || c->vd_geom) return VC_OK;
     const int64_t nv = c->vd.nv, ne = c->vd.ne, nt = c->vd.nt;
-    const int64_t nseg = c->h_off[kLSeg][c->nvol];
     VC_TRY(ensure_n<float>(c, c->vts, 3 * nv));
     VC_TRY(ensure_n<int2>(c, c->edges, ne));
     VC_TRY(ensure_n<int32_t>(c, c->tris, 3 * nt));
     const SegPlanes* planes = ptr<SegPlanes>(c->vd_seg);
     const int32_t *vb = ptr<int32_t>(c->vd_voff), *eb = ptr<int32_t>(c->vd_eoff), *fb = ptr<int32_t>(c->vd_foff);
     Region r(c, "vd_geometry");
-    vd_faces_kernel<<<seg_grid(c, nseg), 128, 0, c->stream>>>(
+    vd_faces_kernel<<<row_grid(c, c->h_off[kLRow][c->nvol]), 128, 0, c->stream>>>(
         c->tab, c->bases, planes, vb, eb, fb, ptr<int32_t>(c->ft_id), ptr<float>(c->site_xyz), ptr<float>(c->vd_lam),
         ptr<int32_t>(c->tris), ptr<int2>(c->edges), nullptr, nullptr, nullptr, nullptr);
-    vd_edges_kernel<<<seg_grid(c, nseg), 128, 0, c->stream>>>(c->tab, c->bases, planes, vb, eb, fb,
+    vd_edges_kernel<<<row_grid(c, c->h_off[kLRow][c->nvol]), 128, 0, c->stream>>>(c->tab, c->bases, planes, vb, eb, fb,
                                                                ptr<float>(c->vd_lam), ptr<int2>(c->edges), nullptr,
                                                                nullptr, nullptr);
-    vd_vertices_kernel<<<seg_grid(c, nseg), 128, 0, c->stream>>>(c->tab, c->bases, planes, vb, eb, fb,
+    vd_vertices_kernel<<<row_grid(c, c->h_off[kLRow][c->nvol]), 128, 0, c->stream>>>(c->tab, c->bases, planes, vb, eb, fb,
                                                                   ptr<float>(c->vts), nullptr, nullptr, nullptr,
                                                                   nullptr, ne);
     launched(c, 3);
