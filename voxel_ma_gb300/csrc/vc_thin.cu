@@ -162,7 +162,13 @@ __global__ void build_records_kernel(const int2* __restrict__ edges, const int32
 constexpr int kG0Items = 8;
 constexpr int64_t kG0Tile = (int64_t)kThreads * kG0Items;
 
-__global__ void __launch_bounds__(kThreads) gen0_count_kernel(const int32_t* __restrict__ g0, int64_t n,
+// Generation-0 code i (edges first, then vertices) names an item when it is
+// >= 0.  With vfilter set (records written by the lattice complex with the
+// thresholds folded in), a vertex code names the vertex's one edge, and the
+// count pass drops (writes -1 over) the codes whose edge fails the filter,
+// read from the edge's record; otherwise every code >= 0 already passed.
+__global__ void __launch_bounds__(kThreads) gen0_count_kernel(int32_t* __restrict__ g0, int64_t n, int64_t ne,
+                                                              const EdgeRec* __restrict__ vfilter,
                                                               int64_t* __restrict__ sums) {
     __shared__ int64_t sm[33];
     const int64_t base = (int64_t)blockIdx.x * kG0Tile;
@@ -170,7 +176,13 @@ __global__ void __launch_bounds__(kThreads) gen0_count_kernel(const int32_t* __r
 #pragma unroll
     for (int r = 0; r < kG0Items; ++r) {
         const int64_t i = base + (int64_t)r * kThreads + threadIdx.x;
-        if (i < n) acc += __ldcs(g0 + i) >= 0 ? 1 : 0;
+        if (i >= n) continue;
+        int32_t x = __ldcs(g0 + i);
+        if (x >= 0 && vfilter && i >= ne && !(__ldg(&vfilter[x].em) < 0.0f)) {
+            x = -1;
+            g0[i] = -1;
+        }
+        acc += x >= 0 ? 1 : 0;
     }
     int64_t tot;
     block_exclusive_sum<int64_t>(acc, sm, &tot);
@@ -695,6 +707,7 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats, bool all_pass) {
     }
     {
         Region r(c, "thin_setup");
+        const bool folded = c->records_fresh;
         if (c->records_fresh) {
             c->records_fresh = false;  // the next thinning of this complex rebuilds them
         } else {
@@ -716,8 +729,8 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats, bool all_pass) {
         if (tiles > 0) {
             VC_TRY(ensure_n<int64_t>(c, c->scratch, tiles + 1));
             int64_t* sums = ptr<int64_t>(c->scratch);
-            const int32_t* g0 = ptr<int32_t>(c->thin_g0);
-            gen0_count_kernel<<<(unsigned)tiles, kThreads, 0, c->stream>>>(g0, ng, sums);
+            int32_t* g0 = ptr<int32_t>(c->thin_g0);
+            gen0_count_kernel<<<(unsigned)tiles, kThreads, 0, c->stream>>>(g0, ng, ne, folded ? A.E : nullptr, sums);
             scan_sums_single<<<1, 1024, 0, c->stream>>>(sums, tiles, ctl + 0);
             gen0_write_kernel<<<(unsigned)tiles, kThreads, 0, c->stream>>>(A, (int32_t)ne, g0, ng, sums);
             launched(c, 3);

@@ -29,13 +29,14 @@
 // lattice row, seven bit planes (vertex, valid axis edge per axis, valid
 // face per axis) and the three cell counts; after one scan of the segment
 // counts any cell's id is an O(1) population count.  The emission kernels
-// walk lattice rows, a warp per row and one lane per cell of a segment (so
-// writes of consecutive ids are coalesced), and write what the thinning and
-// the remaining complex read: the thinning records and each vertex's lattice
-// point, or, on demand, vertex coordinates, edges and triangles.  The
-// measures, triangle faces, face sites, triangle
-// sides and adjacency lists are written on demand (ensure_vd_aux), when a
-// getter or a thinning with explicit thresholds asks for them.
+// (faces, then vertices with axis edges) walk lattice rows, a warp per row
+// and one lane per face or per point of a segment (so writes of consecutive
+// ids are coalesced), and write what the thinning and the remaining complex
+// read: the thinning records and each vertex's lattice point, or, on
+// demand, vertex coordinates, edges and triangles.  The measures, triangle
+// faces, face sites, triangle sides and adjacency lists are written on
+// demand (ensure_vd_aux), when a getter or a thinning with explicit
+// thresholds asks for them.
 #include "vc_internal.cuh"
 
 #include <algorithm>
@@ -499,20 +500,37 @@ __device__ __forceinline__ int32_t face_at(const RowPlanes& R, uint32_t S0, uint
     return R.fb + pc3(R.f0, R.f1, R.f2, mi) + (ax >= 1 ? bt(S0, t) : 0) + (ax >= 2 ? bt(S1, t) : 0);
 }
 
-// Vertices (vts or, in the thinning path, each vertex's lattice point) and,
-// with records, their thinning records: incident edges counted and summed.
-// Incident edges: the axis edges into the voxel from -x, -y, -z, its own
-// axis edges, then the diagonals of the faces (p1, d) and (p3, d) that have
-// it as q1 / q3 (p1 = p + e_w, p3 = p + e_u).
-__global__ void __launch_bounds__(128) vd_vertices_kernel(VolTab T, Bases B, const SegPlanes* __restrict__ planes,
-                                                          const int32_t* __restrict__ vb, const int32_t* __restrict__ eb,
-                                                          const int32_t* __restrict__ fbs, float* __restrict__ vts,
-                                                          uint32_t* __restrict__ vlat, VertRec* __restrict__ V,
-                                                          const EdgeRec* __restrict__ E, int32_t* __restrict__ g0,
-                                                          int64_t ne) {
-    __shared__ uint8_t s_slots[4][96];
+// Vertices and axis edges of a row, one lane per point.  Vertices: vts or, in
+// the thinning path, each vertex's lattice point, and with records their
+// thinning records: incident edges counted and summed -- the axis edges into
+// the voxel from -x, -y, -z, its own axis edges, and the diagonals of the
+// faces (p1, d) and (p3, d) that have it as q1 / q3 (p1 = p + e_w, p3 = p +
+// e_u).  Axis edges: endpoints and, with records, thinning records
+// (incident triangles counted, summed and tested against the threshold;
+// measure = max lambda of the incident faces, voroinfo.cpp:1490-1538); face
+// lambdas come from lamf (one per face, written by vd_faces_kernel).  The
+// faces of the plaquettes of the point's three axis edges (the lattice edges
+// along u from nb and nb + e_w and along w from nb and nb + e_u, nb = the
+// point + e_d, u = d+1, w = d+2 mod 3) are nine lattice edges, looked up once
+// and their lambdas loaded together:
+//   d = 0: (a+1,b,c)+y, (a+1,b,c)+z [triangle 1]; (a+1,b,c+1)+y, (a+1,b+1,c)+z [0]
+//   d = 1: (a,b+1,c)+z, (a,b+1,c)+x [1]; (a+1,b+1,c)+z, (a,b+1,c+1)+x [0]
+//   d = 2: (a,b,c+1)+x, (a,b,c+1)+y [1]; (a,b+1,c+1)+x, (a+1,b,c+1)+y [0]
+// (the triangle of each face that carries the edge: 1 for the two faces at
+// nb); the vertex's six diagonals are the faces of (a,b,c+1)+x, (a,b+1,c)+x,
+// (a+1,b,c)+y, (a,b,c+1)+y, (a,b+1,c)+z and (a+1,b,c)+z among them.  A
+// vertex with one incident edge is written to the generation-0 codes as
+// that edge; whether the edge passes the filter is read when generation 0
+// is selected (the edge's record may be written by another warp here).
+__global__ void __launch_bounds__(128, 6) vd_vertices_edges_kernel(VolTab T, Bases B, const SegPlanes* __restrict__ planes,
+                                                       const int32_t* __restrict__ vb, const int32_t* __restrict__ eb,
+                                                       const int32_t* __restrict__ fbs, const float* __restrict__ lamf,
+                                                       int2* __restrict__ edges, EdgeRec* __restrict__ E,
+                                                       float* __restrict__ vts, uint32_t* __restrict__ vlat,
+                                                       VertRec* __restrict__ V, int32_t* __restrict__ g0, int64_t ne,
+                                                       const float* __restrict__ thr) {
     const int lane = threadIdx.x & 31;
-    uint8_t* slots = s_slots[threadIdx.x >> 5];
+    const bool rec = E != nullptr;  // records (E and V) or the complex's arrays
     const int64_t nrow = T.total(kLRow);
     VolTab::Cache vcache;
     ROW_LOOP(gr, nrow) {
@@ -524,200 +542,126 @@ __global__ void __launch_bounds__(128) vd_vertices_kernel(VolTab T, Bases B, con
         if (a >= dm.x || b >= dm.y) continue;  // no voxel in this row
         const Shift sh = shift_of(B, bv);
         const int32_t fbv = (int32_t)sh.fb, eb1 = (int32_t)sh.eb1;
-        // rows (a,b), (a-1,b), (a,b-1), (a,b+1), (a+1,b)
+        const float tb = thr ? thr[bv] : 0.0f;
+        // rows (a,b), (a+1,b), (a,b+1), (a+1,b+1) (inside the lattice), (a-1,b), (a,b-1)
         const int64_t s0 = T.start(kLSeg, bv) + (int64_t)lr * nsr;
-        const int64_t sm0 = a >= 1 ? s0 - (int64_t)NB * nsr : -1;
-        const int64_t s0m = b >= 1 ? s0 - nsr : -1;
-        const int64_t s0p = s0 + nsr, sp0 = s0 + (int64_t)NB * nsr;
+        const int64_t sp0 = s0 + (int64_t)NB * nsr, s0p = s0 + nsr, spp = sp0 + nsr;
+        const int64_t sm0 = a >= 1 ? s0 - (int64_t)NB * nsr : -1, s0m = b >= 1 ? s0 - nsr : -1;
         const uint32_t lat_row = (uint32_t)((int64_t)lr * NC);
         // the vertex and edge planes of the row's segments, one segment ahead
         uint4 pv_next = __ldg(reinterpret_cast<const uint4*>(planes + s0));
         for (int k = 0; k < nsr; ++k) {
             const uint4 pv = pv_next;
             if (k + 1 < nsr) pv_next = __ldg(reinterpret_cast<const uint4*>(planes + s0 + k + 1));
-            if (pv.x == 0u) continue;
-            const RowPlanes R0 = row_planes(planes, vb, eb, fbs, s0 + k, true, V != nullptr);
-            const int n = compact_cells(R0.v, 0u, 0u, lane, slots);
-            if (V) {
-                const RowPlanes Rm0 = row_planes(planes, vb, eb, fbs, sm0 < 0 ? -1 : sm0 + k, true, false);
-                const RowPlanes R0m = row_planes(planes, vb, eb, fbs, s0m < 0 ? -1 : s0m + k, true, false);
-                const RowPlanes R0p = row_planes(planes, vb, eb, fbs, s0p + k, false, true);
-                const RowPlanes Rp0 = row_planes(planes, vb, eb, fbs, sp0 + k, false, true);
-                // bit t of E2s: axis edge (c0 + t - 1) + z of the row; of F*s: face at c0 + t + 1
-                uint32_t pe2 = 0u, nf0 = 0u, nf1 = 0u;
-                if (k > 0 && (R0.v & 1u)) pe2 = __ldg(&planes[s0 + k - 1].e2);
-                if (k + 1 < nsr && (R0.v >> 31)) {
-                    const uint4 y = __ldg(reinterpret_cast<const uint4*>(planes + s0 + k + 1) + 1);
-                    nf0 = y.x;
-                    nf1 = y.y;
-                }
-                const uint32_t E2s = (R0.e2 << 1) | (pe2 >> 31);
-                const uint32_t F0s = (R0.f0 >> 1) | (nf0 << 31), F1s = (R0.f1 >> 1) | (nf1 << 31);
-                for (int r = lane; r < n; r += 32) {
-                    const int t = slots[r] >> 2;
-                    const int32_t v = R0.vb + r;
-                    const uint32_t m = below(t);
-                    const int c = 32 * k + t;
-                    if (vts) {
-                        vts[3 * (int64_t)v + 0] = (float)a;
-                        vts[3 * (int64_t)v + 1] = (float)b;
-                        vts[3 * (int64_t)v + 2] = (float)c;
-                    }
-                    if (vlat) vlat[v] = lat_row + (uint32_t)c;  // within its volume
-                    unsigned kk = 0;
-                    unsigned long long idsum = 0;
-                    // axis edges into the voxel from -x, -y, -z
-                    if (bt(Rm0.e0, t)) {
-                        ++kk;
-                        idsum += (unsigned)(Rm0.eb + pc3(Rm0.e0, Rm0.e1, Rm0.e2, m) + fbv);
-                    }
-                    if (bt(R0m.e1, t)) {
-                        ++kk;
-                        idsum += (unsigned)(R0m.eb + pc3(R0m.e0, R0m.e1, R0m.e2, m) + bt(R0m.e0, t) + fbv);
-                    }
-                    const int32_t e_own = R0.eb + pc3(R0.e0, R0.e1, R0.e2, m) + fbv;
-                    if (bt(E2s, t)) {  // the z edge of voxel c - 1: the last axis edge before c
-                        ++kk;
-                        idsum += (unsigned)(e_own - 1);
-                    }
-                    // its own axis edges
-                    {
-                        int32_t e = e_own;
-                        if (bt(R0.e0, t)) {
-                            ++kk;
-                            idsum += (unsigned)e++;
-                        }
-                        if (bt(R0.e1, t)) {
-                            ++kk;
-                            idsum += (unsigned)e++;
-                        }
-                        if (bt(R0.e2, t)) {
-                            ++kk;
-                            idsum += (unsigned)e;
-                        }
-                    }
-                    // diagonals: d = 0: (a,b,c+1)+x, (a,b+1,c)+x; d = 1: (a+1,b,c)+y,
-                    // (a,b,c+1)+y; d = 2: (a,b+1,c)+z, (a+1,b,c)+z
-                    const int32_t fd[6] = {face_at(R0, F0s, F1s, 0u, t, true, 0), face_at(R0p, 0u, 0u, 0u, t, false, 0),
-                                           face_at(Rp0, 0u, 0u, 0u, t, false, 1), face_at(R0, F0s, F1s, 0u, t, true, 1),
-                                           face_at(R0p, 0u, 0u, 0u, t, false, 2), face_at(Rp0, 0u, 0u, 0u, t, false, 2)};
-#pragma unroll
-                    for (int i = 0; i < 6; ++i)
-                        if (fd[i] >= 0) {
-                            ++kk;
-                            idsum += (unsigned)(eb1 + fd[i]);
-                        }
-                    VertRec rec;
-                    rec.rs = rs_make(kk, 0, idsum);
-                    rec.trig = 0;
-                    rec.rm = kAlive;
-                    V[v] = rec;
-                    // generation 0: an EV pair when the one edge passes the filter
-                    // (its record, written before, holds the folded measure)
-                    g0[ne + v] = (kk == 1 && E[idsum].em < 0.0f) ? (int32_t)idsum : -1;
-                }
-            } else {
-                for (int r = lane; r < n; r += 32) {
-                    const int t = slots[r] >> 2;
-                    const int32_t v = R0.vb + r;
-                    const int c = 32 * k + t;
-                    if (vts) {
-                        vts[3 * (int64_t)v + 0] = (float)a;
-                        vts[3 * (int64_t)v + 1] = (float)b;
-                        vts[3 * (int64_t)v + 2] = (float)c;
-                    }
-                    if (vlat) vlat[v] = lat_row + (uint32_t)c;
-                }
-            }
-            __syncwarp();
-        }
-    }
-}
-
-// Axis edges: endpoints and, with records, thinning records (incident
-// triangles counted, summed and tested against the threshold; measure = max
-// lambda of the incident faces, voroinfo.cpp:1490-1538).  Face lambdas come
-// from lamf (one per face, written by vd_faces_kernel).  Lane = point: the
-// faces of the plaquettes of the point's three axis edges (the lattice edges
-// along u from nb and nb + e_w and along w from nb and nb + e_u, nb = the
-// point + e_d, u = d+1, w = d+2 mod 3) are nine lattice edges, looked up once
-// and their lambdas loaded together:
-//   d = 0: (a+1,b,c)+y, (a+1,b,c)+z [triangle 1]; (a+1,b,c+1)+y, (a+1,b+1,c)+z [0]
-//   d = 1: (a,b+1,c)+z, (a,b+1,c)+x [1]; (a+1,b+1,c)+z, (a,b+1,c+1)+x [0]
-//   d = 2: (a,b,c+1)+x, (a,b,c+1)+y [1]; (a,b+1,c+1)+x, (a+1,b,c+1)+y [0]
-// (the triangle of each face that carries the edge: 1 for the two faces at
-// nb).
-__global__ void __launch_bounds__(128) vd_edges_kernel(VolTab T, Bases B, const SegPlanes* __restrict__ planes,
-                                                       const int32_t* __restrict__ vb, const int32_t* __restrict__ eb,
-                                                       const int32_t* __restrict__ fbs, const float* __restrict__ lamf,
-                                                       int2* __restrict__ edges, EdgeRec* __restrict__ E,
-                                                       int32_t* __restrict__ g0, const float* __restrict__ thr) {
-    const int lane = threadIdx.x & 31;
-    const int64_t nrow = T.total(kLRow);
-    VolTab::Cache vcache;
-    ROW_LOOP(gr, nrow) {
-        const int bv = T.find_cached(kLRow, gr, vcache);
-        const int4 dm = T.dim(bv);
-        const int NB = dm.y + 1, nsr = (dm.z + 32) / 32;
-        const int lr = (int)(gr - T.start(kLRow, bv));
-        const int a = lr / NB, b = lr - a * NB;
-        if (a >= dm.x || b >= dm.y) continue;  // no voxel in this row
-        const int32_t fbv = (int32_t)shift_of(B, bv).fb;
-        const float tb = thr ? thr[bv] : 0.0f;
-        // rows (a,b), (a+1,b), (a,b+1), (a+1,b+1): all inside the lattice
-        const int64_t s0 = T.start(kLSeg, bv) + (int64_t)lr * nsr;
-        const int64_t sp0 = s0 + (int64_t)NB * nsr, s0p = s0 + nsr, spp = sp0 + nsr;
-        // the vertex and edge planes of the row's segments, one segment ahead
-        uint4 pv_next = __ldg(reinterpret_cast<const uint4*>(planes + s0));
-        for (int k = 0; k < nsr; ++k) {
-            const uint4 pv = pv_next;
-            if (k + 1 < nsr) pv_next = __ldg(reinterpret_cast<const uint4*>(planes + s0 + k + 1));
-            const uint32_t any_e = pv.y | pv.z | pv.w;
-            if (any_e == 0u) continue;
-            const RowPlanes R0 = row_planes(planes, vb, eb, fbs, s0 + k, true, E != nullptr);
-            const RowPlanes Rp0 = row_planes(planes, vb, eb, fbs, sp0 + k, true, E != nullptr);
-            const RowPlanes R0p = row_planes(planes, vb, eb, fbs, s0p + k, true, E != nullptr);
-            const int t = lane;
-            if (!bt(any_e, t)) continue;
-            const uint32_t m = below(t);
-            const int32_t v0 = R0.vb + __popc(R0.v & m);
-            int32_t e = R0.eb + pc3(R0.e0, R0.e1, R0.e2, m) + fbv;
-            // the +d neighbours: (a+1,b,c), (a,b+1,c), (a,b,c+1) (the vertex after v0 in its row)
-            const int32_t v1[3] = {Rp0.vb + __popc(Rp0.v & m), R0p.vb + __popc(R0p.v & m), v0 + 1};
-            if (!E) {
-#pragma unroll
-                for (int d = 0; d < 3; ++d)
-                    if (bt(d == 0 ? R0.e0 : (d == 1 ? R0.e1 : R0.e2), t)) edges[e++] = make_int2(v0, v1[d]);
-                continue;
-            }
-            const RowPlanes Rpp = row_planes(planes, vb, eb, fbs, spp + k, false, true);
-            // face planes at c + 1: lane 31 reads the next segment's first bits
+            if (pv.x == 0u) continue;  // no vertex, so no axis edge
+            // every load of the segment goes out before any is used
+            const RowPlanes R0 = row_planes(planes, vb, eb, fbs, s0 + k, true, rec);
+            const RowPlanes Rp0 = row_planes(planes, vb, eb, fbs, sp0 + k, true, rec);
+            const RowPlanes R0p = row_planes(planes, vb, eb, fbs, s0p + k, true, rec);
+            const RowPlanes Rpp = row_planes(planes, vb, eb, fbs, rec ? spp + k : -1, false, true);
+            const RowPlanes Rm0 = row_planes(planes, vb, eb, fbs, (rec && sm0 >= 0) ? sm0 + k : -1, true, false);
+            const RowPlanes R0m = row_planes(planes, vb, eb, fbs, (rec && s0m >= 0) ? s0m + k : -1, true, false);
+            // face planes at c + 1: lane 31 reads the next segment's first bits;
+            // the z edge of voxel c - 1: lane 0 reads the previous segment's last bit
             uint4 n0 = make_uint4(0u, 0u, 0u, 0u), np0 = n0, n0p = n0;
-            if (k + 1 < nsr && (any_e >> 31)) {
+            if (rec && k + 1 < nsr && (pv.x >> 31)) {
                 n0 = __ldg(reinterpret_cast<const uint4*>(planes + s0 + k + 1) + 1);
                 np0 = __ldg(reinterpret_cast<const uint4*>(planes + sp0 + k + 1) + 1);
                 n0p = __ldg(reinterpret_cast<const uint4*>(planes + s0p + k + 1) + 1);
             }
+            uint32_t pe2 = 0u;
+            if (rec && k > 0 && (pv.x & 1u)) pe2 = __ldg(&planes[s0 + k - 1].e2);
+            const int t = lane;
+            if (!bt(pv.x, t)) continue;
+            const uint32_t m = below(t);
+            const int c = 32 * k + t;
+            const int32_t v0 = R0.vb + __popc(R0.v & m);
+            if (vts) {
+                vts[3 * (int64_t)v0 + 0] = (float)a;
+                vts[3 * (int64_t)v0 + 1] = (float)b;
+                vts[3 * (int64_t)v0 + 2] = (float)c;
+            }
+            if (vlat) vlat[v0] = lat_row + (uint32_t)c;  // within its volume
+            const int32_t e_own = R0.eb + pc3(R0.e0, R0.e1, R0.e2, m) + fbv;
+            const bool h0 = bt(R0.e0, t), h1 = bt(R0.e1, t), h2 = bt(R0.e2, t);
+            // the +d neighbours: (a+1,b,c), (a,b+1,c), (a,b,c+1) (the vertex after v0 in its row)
+            const int32_t v1[3] = {Rp0.vb + __popc(Rp0.v & m), R0p.vb + __popc(R0p.v & m), v0 + 1};
+            if (!rec) {
+                int32_t e = e_own;
+                if (edges) {
+                    if (h0) edges[e++] = make_int2(v0, v1[0]);
+                    if (h1) edges[e++] = make_int2(v0, v1[1]);
+                    if (h2) edges[e] = make_int2(v0, v1[2]);
+                }
+                continue;
+            }
             const uint32_t S00 = (R0.f0 >> 1) | (n0.x << 31), S01 = (R0.f1 >> 1) | (n0.y << 31);
             const uint32_t Sp00 = (Rp0.f0 >> 1) | (np0.x << 31), Sp01 = (Rp0.f1 >> 1) | (np0.y << 31);
             const uint32_t S0p0 = (R0p.f0 >> 1) | (n0p.x << 31);
-            const bool h0 = bt(R0.e0, t), h1 = bt(R0.e1, t), h2 = bt(R0.e2, t);
-            // the nine faces (-1: none), only those an edge of this point needs
+            // the nine faces (-1: none)
             int32_t fid[9];
-            fid[0] = h0 ? face_at(Rp0, 0u, 0u, 0u, t, false, 1) : -1;                   // (a+1,b,c)+y
-            fid[1] = h0 ? face_at(Rp0, 0u, 0u, 0u, t, false, 2) : -1;                   // (a+1,b,c)+z
+            fid[0] = face_at(Rp0, 0u, 0u, 0u, t, false, 1);                             // (a+1,b,c)+y
+            fid[1] = face_at(Rp0, 0u, 0u, 0u, t, false, 2);                             // (a+1,b,c)+z
             fid[2] = (h0 || h2) ? face_at(Rp0, Sp00, Sp01, 0u, t, true, 1) : -1;        // (a+1,b,c+1)+y
             fid[3] = (h0 || h1) ? face_at(Rpp, 0u, 0u, 0u, t, false, 2) : -1;           // (a+1,b+1,c)+z
-            fid[4] = h1 ? face_at(R0p, 0u, 0u, 0u, t, false, 2) : -1;                   // (a,b+1,c)+z
-            fid[5] = h1 ? face_at(R0p, 0u, 0u, 0u, t, false, 0) : -1;                   // (a,b+1,c)+x
+            fid[4] = face_at(R0p, 0u, 0u, 0u, t, false, 2);                             // (a,b+1,c)+z
+            fid[5] = face_at(R0p, 0u, 0u, 0u, t, false, 0);                             // (a,b+1,c)+x
             fid[6] = (h1 || h2) ? face_at(R0p, S0p0, 0u, 0u, t, true, 0) : -1;          // (a,b+1,c+1)+x
-            fid[7] = h2 ? face_at(R0, S00, S01, 0u, t, true, 0) : -1;                   // (a,b,c+1)+x
-            fid[8] = h2 ? face_at(R0, S00, S01, 0u, t, true, 1) : -1;                   // (a,b,c+1)+y
+            fid[7] = face_at(R0, S00, S01, 0u, t, true, 0);                             // (a,b,c+1)+x
+            fid[8] = face_at(R0, S00, S01, 0u, t, true, 1);                             // (a,b,c+1)+y
+            // lambdas of the faces an axis edge of this point needs
+            const unsigned need = (h0 ? 0x0Fu : 0u) | (h1 ? 0x78u : 0u) | (h2 ? 0x1C4u : 0u);
             float lj[9];
 #pragma unroll
-            for (int i = 0; i < 9; ++i) lj[i] = fid[i] >= 0 ? __ldg(lamf + fid[i]) : 0.0f;
+            for (int i = 0; i < 9; ++i) lj[i] = (fid[i] >= 0 && ((need >> i) & 1u)) ? __ldg(lamf + fid[i]) : 0.0f;
+            // the vertex record
+            {
+                unsigned kk = 0;
+                unsigned long long idsum = 0;
+                if (bt(Rm0.e0, t)) {  // (a-1,b,c)+x
+                    ++kk;
+                    idsum += (unsigned)(Rm0.eb + pc3(Rm0.e0, Rm0.e1, Rm0.e2, m) + fbv);
+                }
+                if (bt(R0m.e1, t)) {  // (a,b-1,c)+y
+                    ++kk;
+                    idsum += (unsigned)(R0m.eb + pc3(R0m.e0, R0m.e1, R0m.e2, m) + bt(R0m.e0, t) + fbv);
+                }
+                if (bt((R0.e2 << 1) | (pe2 >> 31), t)) {  // (a,b,c-1)+z: the last axis edge before c
+                    ++kk;
+                    idsum += (unsigned)(e_own - 1);
+                }
+                {
+                    int32_t e = e_own;
+                    if (h0) {
+                        ++kk;
+                        idsum += (unsigned)e++;
+                    }
+                    if (h1) {
+                        ++kk;
+                        idsum += (unsigned)e++;
+                    }
+                    if (h2) {
+                        ++kk;
+                        idsum += (unsigned)e;
+                    }
+                }
+                const int dg[6] = {7, 5, 0, 8, 4, 1};  // the diagonals' faces
+#pragma unroll
+                for (int i = 0; i < 6; ++i)
+                    if (fid[dg[i]] >= 0) {
+                        ++kk;
+                        idsum += (unsigned)(eb1 + fid[dg[i]]);
+                    }
+                VertRec vr;
+                vr.rs = rs_make(kk, 0, idsum);
+                vr.trig = 0;
+                vr.rm = kAlive;
+                V[v0] = vr;
+                g0[ne + v0] = kk == 1 ? (int32_t)idsum : -1;
+            }
             // per axis: the four faces' slots (the first two carry the edge as triangle 1)
             constexpr int kSlot[3][4] = {{0, 1, 2, 3}, {4, 5, 3, 6}, {7, 8, 6, 2}};
+            int32_t e = e_own;
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
                 if (!(d == 0 ? h0 : (d == 1 ? h1 : h2))) continue;
@@ -735,15 +679,15 @@ __global__ void __launch_bounds__(128) vd_edges_kernel(VolTab T, Bases B, const 
                     }
                 }
                 if (edges) edges[e] = make_int2(v0, v1[d]);
-                EdgeRec rec;
-                rec.v0 = v0;
-                rec.v1 = v1[d];
-                rec.rs = rs_make(kk, npass, idsum);
-                rec.trig = 0;
-                rec.em = rec_measure(mx, thr, bv);
-                rec.rm = kAlive;
-                rec.pad = 0;
-                E[e] = rec;
+                EdgeRec er;
+                er.v0 = v0;
+                er.v1 = v1[d];
+                er.rs = rs_make(kk, npass, idsum);
+                er.trig = 0;
+                er.em = rec_measure(mx, thr, bv);
+                er.rm = kAlive;
+                er.pad = 0;
+                E[e] = er;
                 // generation 0: an FE pair when the one face passes the filter
                 g0[e] = (kk == 1 && npass == 1) ? (int32_t)idsum : -1;
                 ++e;
@@ -1244,18 +1188,12 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes, double t_thr) {
             launched(c);
         }
         {
-            Region k(c, "vd_edges");
-            vd_edges_kernel<<<row_grid(c, c->h_off[kLRow][c->nvol]), 128, 0, c->stream>>>(
+            Region k(c, "vd_vertices_edges");
+            vd_vertices_edges_kernel<<<row_grid(c, c->h_off[kLRow][c->nvol]), 128, 0, c->stream>>>(
                 c->tab, c->bases, planes, vb, eb, fb, ptr<float>(c->vd_lam), geom ? ptr<int2>(c->edges) : nullptr,
-                folded ? ptr<EdgeRec>(c->edge_rec) : nullptr, g0, thr);
-            launched(c);
-        }
-        {
-            Region k(c, "vd_vertices");
-            vd_vertices_kernel<<<row_grid(c, c->h_off[kLRow][c->nvol]), 128, 0, c->stream>>>(
-                c->tab, c->bases, planes, vb, eb, fb, geom ? ptr<float>(c->vts) : nullptr,
-                geom ? nullptr : ptr<uint32_t>(c->vd_vlat), folded ? ptr<VertRec>(c->vert_rec) : nullptr,
-                folded ? ptr<EdgeRec>(c->edge_rec) : nullptr, g0, ne);
+                folded ? ptr<EdgeRec>(c->edge_rec) : nullptr, geom ? ptr<float>(c->vts) : nullptr,
+                geom ? nullptr : ptr<uint32_t>(c->vd_vlat), folded ? ptr<VertRec>(c->vert_rec) : nullptr, g0, ne,
+                thr);
             launched(c);
         }
         VC_CUDA(c, cudaGetLastError());
@@ -1296,13 +1234,10 @@ int ensure_vd_geometry(vc_ctx* c) {
     vd_faces_kernel<<<row_grid(c, c->h_off[kLRow][c->nvol]), 128, 0, c->stream>>>(
         c->tab, c->bases, planes, vb, eb, fb, ptr<int32_t>(c->ft_id), ptr<float>(c->site_xyz), ptr<float>(c->vd_lam),
         ptr<int32_t>(c->tris), ptr<int2>(c->edges), nullptr, nullptr, nullptr, nullptr);
-    vd_edges_kernel<<<row_grid(c, c->h_off[kLRow][c->nvol]), 128, 0, c->stream>>>(c->tab, c->bases, planes, vb, eb, fb,
-                                                               ptr<float>(c->vd_lam), ptr<int2>(c->edges), nullptr,
-                                                               nullptr, nullptr);
-    vd_vertices_kernel<<<row_grid(c, c->h_off[kLRow][c->nvol]), 128, 0, c->stream>>>(c->tab, c->bases, planes, vb, eb, fb,
-                                                                  ptr<float>(c->vts), nullptr, nullptr, nullptr,
-                                                                  nullptr, ne);
-    launched(c, 3);
+    vd_vertices_edges_kernel<<<row_grid(c, c->h_off[kLRow][c->nvol]), 128, 0, c->stream>>>(
+        c->tab, c->bases, planes, vb, eb, fb, ptr<float>(c->vd_lam), ptr<int2>(c->edges), nullptr, ptr<float>(c->vts),
+        nullptr, nullptr, nullptr, ne, nullptr);
+    launched(c, 2);
     VC_CUDA(c, cudaGetLastError());
     c->vd_geom = true;
     return VC_OK;
