@@ -172,17 +172,24 @@ __global__ void __launch_bounds__(kThreads) gen0_count_kernel(int32_t* __restric
                                                               int64_t* __restrict__ sums) {
     __shared__ int64_t sm[33];
     const int64_t base = (int64_t)blockIdx.x * kG0Tile;
-    int64_t acc = 0;
+    // the codes, then the filter's record loads, each batch in flight together
+    int32_t x[kG0Items];
 #pragma unroll
     for (int r = 0; r < kG0Items; ++r) {
         const int64_t i = base + (int64_t)r * kThreads + threadIdx.x;
-        if (i >= n) continue;
-        int32_t x = __ldcs(g0 + i);
-        if (x >= 0 && vfilter && i >= ne && !(__ldg(&vfilter[x].em) < 0.0f)) {
-            x = -1;
-            g0[i] = -1;
-        }
-        acc += x >= 0 ? 1 : 0;
+        x[r] = i < n ? __ldcs(g0 + i) : -1;
+    }
+    bool drop[kG0Items];
+#pragma unroll
+    for (int r = 0; r < kG0Items; ++r) {
+        const int64_t i = base + (int64_t)r * kThreads + threadIdx.x;
+        drop[r] = vfilter && x[r] >= 0 && i >= ne && !(__ldg(&vfilter[x[r]].em) < 0.0f);
+    }
+    int64_t acc = 0;
+#pragma unroll
+    for (int r = 0; r < kG0Items; ++r) {
+        if (drop[r]) g0[base + (int64_t)r * kThreads + threadIdx.x] = -1;
+        acc += (x[r] >= 0 && !drop[r]) ? 1 : 0;
     }
     int64_t tot;
     block_exclusive_sum<int64_t>(acc, sm, &tot);
