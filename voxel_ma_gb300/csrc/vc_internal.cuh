@@ -47,9 +47,10 @@ T* ptr(const DevBuf& b) {
 // one cell in one DRAM sector (its accesses are random).  Random accesses
 // cost per request, not per byte, so each phase of the thinning finds what it
 // needs about a cell in one aligned 16-byte piece: a face record is one piece,
-// a vertex record is one piece, and an edge record's first piece is what an
-// item removing the edge reads and its second piece what a decrement and the
-// child step touch.
+// a vertex record is one piece, and an edge record is two: its head (what an
+// item removing the edge reads) and its count (what a decrement and the child
+// step touch), kept in two arrays, so that the sector a random touch brings
+// in holds the same piece of the neighbouring edge (ids follow the lattice).
 constexpr int32_t kAlive = INT32_MAX;  // removal position of a cell still present
 // An edge's faces (a vertex's edges) still present, as one 64-bit word: their
 // count in bits 0-15, how many of them pass the thinning filter (measure
@@ -84,22 +85,29 @@ struct __align__(16) FaceRec {
     int32_t e2;      // third side; bit 31 (kFacePass): measure below the face threshold
     int32_t rm;
 };
-struct __align__(32) EdgeRec {
-    // first piece: ends, removal position, measure
+struct __align__(16) EdgeHead {  // ends, removal position, measure
     int32_t v0, v1;
     int32_t rm;
     float em;
-    // second piece: faces still present (count | pass | id sum), last decrement
+};
+struct __align__(16) EdgeCnt {  // faces still present (count | pass | id sum), last decrement
     unsigned long long rs;
     uint32_t trig;
     int32_t pad;
+};
+// The edge records of a complex of ne edges: ne heads, then ne counts, in
+// one buffer of 32 bytes per edge.
+struct EdgeRecs {
+    EdgeHead* h = nullptr;
+    EdgeCnt* n = nullptr;
 };
 struct __align__(16) VertRec {
     unsigned long long rs;  // edges still present: count | 0 | id sum
     uint32_t trig;          // last decrement: position << 1 | end bit
     int32_t rm;
 };
-static_assert(sizeof(FaceRec) == 16 && sizeof(EdgeRec) == 32 && sizeof(VertRec) == 16, "record size");
+static_assert(sizeof(FaceRec) == 16 && sizeof(EdgeHead) == 16 && sizeof(EdgeCnt) == 16 && sizeof(VertRec) == 16,
+              "record size");
 
 // ---------------------------------------------------------------------------
 // Volume table.  Every stage runs over a batch of volumes stored one after
@@ -318,6 +326,13 @@ int ensure_ctx(vc_ctx* c, DevBuf& b, size_t bytes);
 template <class T>
 inline int ensure_n(vc_ctx* c, DevBuf& b, int64_t n) {
     return ensure_ctx(c, b, (size_t)(n > 0 ? n : 1) * sizeof(T));
+}
+// The context's edge records for ne edges (heads, then counts), allocated.
+inline int ensure_edge_recs(vc_ctx* c, DevBuf& b, int64_t ne, EdgeRecs* out) {
+    VC_TRY(ensure_n<EdgeHead>(c, b, 2 * ne));
+    out->h = ptr<EdgeHead>(b);
+    out->n = reinterpret_cast<EdgeCnt*>(out->h + ne);
+    return VC_OK;
 }
 // Synchronize the stream and fold the device error word into a status.
 int sync_check(vc_ctx* c);

@@ -125,7 +125,7 @@ __global__ void uf_init_kernel(int32_t* parent, int32_t n) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) parent[i] = (int32_t)i;
 }
 
-__global__ void uf_union_kernel(const int32_t* __restrict__ mark, const EdgeRec* __restrict__ E, Kept K, int32_t ne,
+__global__ void uf_union_kernel(const int32_t* __restrict__ mark, const EdgeHead* __restrict__ E, Kept K, int32_t ne,
                                 int32_t* parent, int* err) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += stride) {
@@ -149,7 +149,7 @@ __global__ void uf_roots_kernel(int32_t* parent, int32_t n, unsigned long long* 
 }
 
 // Marked edges, per volume in a batch (edge -> volume through its vertex).
-__global__ void count_kernel(const int32_t* __restrict__ mark, const EdgeRec* __restrict__ E, int64_t n,
+__global__ void count_kernel(const int32_t* __restrict__ mark, const EdgeHead* __restrict__ E, int64_t n,
                              unsigned long long* cnt, Bases B, int nmap) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     unsigned long long local = 0;
@@ -304,14 +304,14 @@ int run_euler_remaining(vc_ctx* c, vc_euler_info* out) {
     launched(c);
     // edge ends from the thinning records (the lattice complex of the timed
     // path keeps no edge array)
-    count_kernel<<<grid_for(c, ne, 256), 256, 0, c->stream>>>(mark, ptr<EdgeRec>(c->edge_rec), ne, cnt, c->bases,
+    count_kernel<<<grid_for(c, ne, 256), 256, 0, c->stream>>>(mark, ptr<EdgeHead>(c->edge_rec), ne, cnt, c->bases,
                                                               nmap);
     launched(c);
     int32_t* parent = ptr<int32_t>(c->uf_parent);
     if (nvr > 0) {
         uf_init_kernel<<<grid_for(c, nvr, 256), 256, 0, c->stream>>>(parent, (int32_t)nvr);
         launched(c);
-        uf_union_kernel<<<grid_for(c, ne, 256), 256, 0, c->stream>>>(mark, ptr<EdgeRec>(c->edge_rec), kept_of(c),
+        uf_union_kernel<<<grid_for(c, ne, 256), 256, 0, c->stream>>>(mark, ptr<EdgeHead>(c->edge_rec), kept_of(c),
                                                                       (int32_t)ne, parent, dev_err(c));
         launched(c);
         uf_roots_kernel<<<grid_for(c, nvr, 256), 256, 0, c->stream>>>(parent, (int32_t)nvr, cnt + nmap, c->bases,

@@ -44,9 +44,9 @@
 //   face   {e0, e1, e2 | pass bit, rm}                  16 B
 //   edge   {v0, v1, rm, em} {rs, trig, -}               32 B
 //   vertex {rs, trig, rm}                               16 B
-// Phase A reads a face record and an edge's first piece (FE) or a vertex
-// record and an edge's first piece (EV); the decrements and phase B touch an
-// edge's second piece or a vertex record.
+// Phase A reads a face record and an edge's head (FE) or a vertex record and
+// an edge's head (EV); the decrements and phase B touch an edge's count or a
+// vertex record.
 // rs packs the count of incident faces (edges) still present, how many of
 // them pass the filter, and the sum of their ids: one atomic removes an
 // incident cell, and when the count is 1 the sum names the remaining cell
@@ -66,7 +66,8 @@ constexpr int32_t kEdgeBit = (int32_t)0x80000000u;
 
 struct ThinArgs {
     FaceRec* F;
-    EdgeRec* E;
+    EdgeHead* EH;  // edge records: heads and counts
+    EdgeCnt* EN;
     VertRec* V;
     const float* thr;  // [0] f_t, [1] l_t
     int2* qa;
@@ -106,7 +107,7 @@ __global__ void build_records_kernel(const int2* __restrict__ edges, const int32
                                      const float* __restrict__ em, const float* __restrict__ fm,
                                      const float* __restrict__ thr, int all_pass, int32_t nv, int32_t ne, int32_t nt,
                                      FaceRec* F,
-                                     EdgeRec* E, VertRec* V, int32_t* __restrict__ g0, int* err) {
+                                     EdgeRecs E, VertRec* V, int32_t* __restrict__ g0, int* err) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     const int64_t n = (int64_t)nv + ne + nt;
     const float f_t = thr[0], l_t = thr[1];
@@ -128,16 +129,9 @@ __global__ void build_records_kernel(const int2* __restrict__ edges, const int32
                 pass += (all_pass || fm[f] < f_t) ? 1u : 0u;
             }
             if ((unsigned long long)(o1 - o0) > kRefMask) set_error(err, VC_ERR_ARG);
-            EdgeRec r;
             const int2 ev = edges[e];
-            r.v0 = ev.x;
-            r.v1 = ev.y;
-            r.rs = rs_make((unsigned)(o1 - o0), pass, idsum);
-            r.trig = 0;
-            r.em = all_pass ? 0.0f : em[e];
-            r.rm = kAlive;
-            r.pad = 0;
-            E[e] = r;
+            E.h[e] = EdgeHead{ev.x, ev.y, kAlive, all_pass ? 0.0f : em[e]};
+            E.n[e] = EdgeCnt{rs_make((unsigned)(o1 - o0), pass, idsum), 0u, 0};
             g0[e] = (o1 - o0 == 1 && pass == 1) ? (int32_t)idsum : -1;
         } else {
             const int64_t v = i - nt - ne;
@@ -168,7 +162,7 @@ constexpr int64_t kG0Tile = (int64_t)kThreads * kG0Items;
 // count pass drops (writes -1 over) the codes whose edge fails the filter,
 // read from the edge's record; otherwise every code >= 0 already passed.
 __global__ void __launch_bounds__(kThreads) gen0_count_kernel(int32_t* __restrict__ g0, int64_t n, int64_t ne,
-                                                              const EdgeRec* __restrict__ vfilter,
+                                                              const EdgeHead* __restrict__ vfilter,
                                                               int64_t* __restrict__ sums) {
     __shared__ int64_t sm[33];
     const int64_t base = (int64_t)blockIdx.x * kG0Tile;
@@ -213,7 +207,7 @@ __global__ void __launch_bounds__(kThreads) gen0_write_kernel(ThinArgs A, int32_
                 atomicMin(&A.F[x].rm, p);
             } else {
                 A.qa[p] = make_ev(x, (int32_t)(i - ne));
-                atomicMin(&A.E[x].rm, p);
+                atomicMin(&A.EH[x].rm, p);
             }
         }
         carry += tot;
@@ -310,8 +304,8 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                 has[k] = i < n;
                 it[k] = has[k] ? __ldcg(cur + i) : make_int2(0, 0);
             }
-            // FE item: face record (ra) and the edge's first piece (ea); EV
-            // item: vertex record (ra) and the edge's first piece (ea)
+            // FE item: face record (ra) and the edge's head (ea); EV item:
+            // vertex record (ra) and the edge's head (ea)
             int4 ra[ITEMS], ea[ITEMS];
 #pragma unroll
             for (int k = 0; k < ITEMS; ++k) {
@@ -321,7 +315,7 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                 const int32_t e = fe ? it[k].y : it[k].x;
                 ra[k] = __ldcg(fe ? reinterpret_cast<const int4*>(A.F + idx0(it[k]))
                                   : reinterpret_cast<const int4*>(A.V + it[k].y));
-                ea[k] = __ldcg(reinterpret_cast<const int4*>(A.E + e));
+                ea[k] = __ldcg(reinterpret_cast<const int4*>(A.EH + e));
             }
             int32_t one[4 * ITEMS];  // cells whose count fell to 1 here
             int32_t dec[4 * ITEMS];  // cells decremented here (kEdgeBit: edge) and this item's trig there,
@@ -352,12 +346,12 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                         const unsigned fpass = ra[k].z < 0 ? 1u : 0u;
                         const int32_t sa = s0 == e ? s1 : s0;
                         const int32_t sb = (s0 == e || s1 == e) ? s2 : s1;
-                        const int32_t v0 = ea[k].x, v1 = ea[k].y;  // EdgeRec first piece: v0 v1 rm em
+                        const int32_t v0 = ea[k].x, v1 = ea[k].y;  // EdgeHead: v0 v1 rm em
                         // the edge is named by no other item of this generation
-                        A.E[e].rm = p;
+                        A.EH[e].rm = p;
                         const unsigned long long df = rs_drop(f, fpass), de = rs_drop(e, 0u);
-                        const int oa = rs_count(atomicAdd(&A.E[sa].rs, df));
-                        const int ob = rs_count(atomicAdd(&A.E[sb].rs, df));
+                        const int oa = rs_count(atomicAdd(&A.EN[sa].rs, df));
+                        const int ob = rs_count(atomicAdd(&A.EN[sb].rs, df));
                         const int o0 = rs_count(atomicAdd(&A.V[v0].rs, de));
                         const int o1 = rs_count(atomicAdd(&A.V[v1].rs, de));
                         dec[4 * k + 0] = sa | kEdgeBit;
@@ -377,7 +371,7 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                     }
                 } else {
                     const int32_t e = it[k].x, v = it[k].y;
-                    const int32_t erm = ea[k].z;  // EdgeRec first piece: v0 v1 rm em
+                    const int32_t erm = ea[k].z;  // EdgeHead: v0 v1 rm em
                     const int32_t vref =
                         rs_count(((unsigned long long)(uint32_t)ra[k].y << 32) | (uint32_t)ra[k].x);  // VertRec: rs trig rm
                     if (erm != p) {
@@ -404,7 +398,7 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
 #pragma unroll
             for (int q = 0; q < 4 * ITEMS; ++q) {
                 if (dec[q] == -1) continue;
-                if (dec[q] & kEdgeBit) atomicMax(&A.E[dec[q] & ~kEdgeBit].trig, dtg[q]);
+                if (dec[q] & kEdgeBit) atomicMax(&A.EN[dec[q] & ~kEdgeBit].trig, dtg[q]);
                 else atomicMax(&A.V[dec[q]].trig, dtg[q]);
             }
             __syncthreads();
@@ -440,7 +434,7 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                     uint32_t tg = 0;
                     if (code & kEdgeBit) {
                         const int32_t e2 = code & ~kEdgeBit;
-                        const int4 eb = __ldcg(reinterpret_cast<const int4*>(A.E + e2) + 1);  // rs trig -
+                        const int4 eb = __ldcg(reinterpret_cast<const int4*>(A.EN + e2));  // rs trig -
                         const unsigned long long rs = ((unsigned long long)(uint32_t)eb.y << 32) | (uint32_t)eb.x;
                         want = rs_count(rs) == 1 && rs_pass(rs) == 1;
                         tg = max((uint32_t)eb.z, ltg);
@@ -451,7 +445,7 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                         const int4 va = __ldcg(reinterpret_cast<const int4*>(A.V + u));  // rs trig rm
                         const unsigned long long rs = ((unsigned long long)(uint32_t)va.y << 32) | (uint32_t)va.x;
                         const int32_t e3 = rs_last(rs);
-                        want = rs_count(rs) == 1 && A.E[e3].em < l_t;
+                        want = rs_count(rs) == 1 && A.EH[e3].em < l_t;
                         tg = max((uint32_t)va.z, ltg);
                         slot = 2 + (int)(tg & 1u);
                         ch = make_ev(e3, u);
@@ -532,7 +526,7 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                 __stcg(nxt + slot, ch);
                 const int32_t q = (int32_t)(nbase + slot);
                 if (is_fe(ch)) atomicMin(&A.F[idx0(ch)].rm, q);
-                else atomicMin(&A.E[ch.x].rm, q);
+                else atomicMin(&A.EH[ch.x].rm, q);
             }
             running += tot;
         }
@@ -574,7 +568,8 @@ __global__ void set_thr_kernel(float* thr, float f_t, float l_t) {
 // cells of a kind (vertices, then edges, then faces): the same flags also go
 // out as one bit word per warp with its population count, for the remaining
 // complex's compaction.
-__global__ void export_flags_kernel(const FaceRec* __restrict__ F, const EdgeRec* __restrict__ E,
+__global__ void export_flags_kernel(const FaceRec* __restrict__ F, const EdgeHead* __restrict__ EH,
+                                    const EdgeCnt* __restrict__ EN,
                                     const VertRec* __restrict__ V, int32_t nv, int32_t ne, int32_t nt, uint8_t* kv,
                                     uint8_t* ke, uint8_t* kf, uint8_t* re, uint32_t* __restrict__ bits,
                                     int32_t* __restrict__ wv, int32_t* __restrict__ we, int32_t* __restrict__ wf) {
@@ -593,8 +588,8 @@ __global__ void export_flags_kernel(const FaceRec* __restrict__ F, const EdgeRec
         } else if (w < nwv + nwe) {
             const int64_t e = (w - nwv) * 32 + lane;
             if (e < ne) {
-                const int4 ea = __ldcs(reinterpret_cast<const int4*>(E + e));      // v0 v1 rm em
-                const int4 eb = __ldcs(reinterpret_cast<const int4*>(E + e) + 1);  // rs trig -
+                const int4 ea = __ldcs(reinterpret_cast<const int4*>(EH + e));  // v0 v1 rm em
+                const int4 eb = __ldcs(reinterpret_cast<const int4*>(EN + e));  // rs trig -
                 const int32_t rm = ea.z, ref = rs_count(((unsigned long long)(uint32_t)eb.y << 32) | (uint32_t)eb.x);
                 keep = rm == kAlive && ref == 0;
                 ke[e] = keep;
@@ -678,10 +673,11 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats, bool all_pass) {
         // the records are built from the measures, sides and lists
         VC_TRY(ensure_vd_aux(c, !all_pass, true));
         VC_TRY(ensure_n<FaceRec>(c, c->face_rec, nt));
-        VC_TRY(ensure_n<EdgeRec>(c, c->edge_rec, ne));
         VC_TRY(ensure_n<VertRec>(c, c->vert_rec, nv));
         VC_TRY(ensure_n<int32_t>(c, c->thin_g0, nv + ne));
     }
+    EdgeRecs ER;
+    VC_TRY(ensure_edge_recs(c, c->edge_rec, ne, &ER));  // (written by the lattice complex when fresh)
     VC_TRY(ensure_n<int2>(c, c->q0, qcap));
     VC_TRY(ensure_n<int2>(c, c->q1, qcap));
     VC_TRY(ensure_n<int2>(c, c->child, 4 * qcap));
@@ -693,7 +689,8 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats, bool all_pass) {
     VC_TRY(ensure_n<uint8_t>(c, c->removed_e, ne));
     ThinArgs A{};
     A.F = ptr<FaceRec>(c->face_rec);
-    A.E = ptr<EdgeRec>(c->edge_rec);
+    A.EH = ER.h;
+    A.EN = ER.n;
     A.V = ptr<VertRec>(c->vert_rec);
     A.thr = ptr<float>(c->thr);
     A.qa = ptr<int2>(c->q0);
@@ -721,7 +718,7 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats, bool all_pass) {
             build_records_kernel<<<grid_for(c, nv + ne + nt, 256), 256, 0, c->stream>>>(
                 ptr<int2>(c->edges), ptr<int32_t>(c->tri_edges), ptr<int32_t>(c->ve_off), ptr<int32_t>(c->ve_ids),
                 ptr<int32_t>(c->ef_off), ptr<int32_t>(c->ef_ids), ptr<float>(c->em), ptr<float>(c->fm), A.thr,
-                all_pass ? 1 : 0, (int32_t)nv, (int32_t)ne, (int32_t)nt, A.F, A.E, A.V, ptr<int32_t>(c->thin_g0),
+                all_pass ? 1 : 0, (int32_t)nv, (int32_t)ne, (int32_t)nt, A.F, ER, A.V, ptr<int32_t>(c->thin_g0),
                 dev_err(c));
             launched(c);
         }
@@ -737,7 +734,7 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats, bool all_pass) {
             VC_TRY(ensure_n<int64_t>(c, c->scratch, tiles + 1));
             int64_t* sums = ptr<int64_t>(c->scratch);
             int32_t* g0 = ptr<int32_t>(c->thin_g0);
-            gen0_count_kernel<<<(unsigned)tiles, kThreads, 0, c->stream>>>(g0, ng, ne, folded ? A.E : nullptr, sums);
+            gen0_count_kernel<<<(unsigned)tiles, kThreads, 0, c->stream>>>(g0, ng, ne, folded ? A.EH : nullptr, sums);
             scan_sums_single<<<1, 1024, 0, c->stream>>>(sums, tiles, ctl + 0);
             gen0_write_kernel<<<(unsigned)tiles, kThreads, 0, c->stream>>>(A, (int32_t)ne, g0, ng, sums);
             launched(c, 3);
@@ -786,7 +783,7 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats, bool all_pass) {
         VC_TRY(ensure_n<int32_t>(c, c->keep_we, nwe + 1));
         VC_TRY(ensure_n<int32_t>(c, c->keep_wf, nwf + 1));
         export_flags_kernel<<<grid_for(c, 32 * (nwv + nwe + nwf), 256), 256, 0, c->stream>>>(
-            A.F, A.E, A.V, (int32_t)nv, (int32_t)ne, (int32_t)nt, ptr<uint8_t>(c->keep_v), ptr<uint8_t>(c->keep_e),
+            A.F, A.EH, A.EN, A.V, (int32_t)nv, (int32_t)ne, (int32_t)nt, ptr<uint8_t>(c->keep_v), ptr<uint8_t>(c->keep_e),
             ptr<uint8_t>(c->keep_f), ptr<uint8_t>(c->removed_e), ptr<uint32_t>(c->keep_bits), ptr<int32_t>(c->keep_wv),
             ptr<int32_t>(c->keep_we), ptr<int32_t>(c->keep_wf));
         launched(c);

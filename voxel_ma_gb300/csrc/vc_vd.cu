@@ -525,12 +525,12 @@ __device__ __forceinline__ int32_t face_at(const RowPlanes& R, uint32_t S0, uint
 __global__ void __launch_bounds__(128, 6) vd_vertices_edges_kernel(VolTab T, Bases B, const SegPlanes* __restrict__ planes,
                                                        const int32_t* __restrict__ vb, const int32_t* __restrict__ eb,
                                                        const int32_t* __restrict__ fbs, const float* __restrict__ lamf,
-                                                       int2* __restrict__ edges, EdgeRec* __restrict__ E,
+                                                       int2* __restrict__ edges, EdgeRecs E,
                                                        float* __restrict__ vts, uint32_t* __restrict__ vlat,
                                                        VertRec* __restrict__ V, int32_t* __restrict__ g0, int64_t ne,
                                                        const float* __restrict__ thr) {
     const int lane = threadIdx.x & 31;
-    const bool rec = E != nullptr;  // records (E and V) or the complex's arrays
+    const bool rec = E.h != nullptr;  // records (E and V) or the complex's arrays
     const int64_t nrow = T.total(kLRow);
     VolTab::Cache vcache;
     ROW_LOOP(gr, nrow) {
@@ -679,15 +679,8 @@ __global__ void __launch_bounds__(128, 6) vd_vertices_edges_kernel(VolTab T, Bas
                     }
                 }
                 if (edges) edges[e] = make_int2(v0, v1[d]);
-                EdgeRec er;
-                er.v0 = v0;
-                er.v1 = v1[d];
-                er.rs = rs_make(kk, npass, idsum);
-                er.trig = 0;
-                er.em = rec_measure(mx, thr, bv);
-                er.rm = kAlive;
-                er.pad = 0;
-                E[e] = er;
+                E.h[e] = EdgeHead{v0, v1[d], kAlive, rec_measure(mx, thr, bv)};
+                E.n[e] = EdgeCnt{rs_make(kk, npass, idsum), 0u, 0};
                 // generation 0: an FE pair when the one face passes the filter
                 g0[e] = (kk == 1 && npass == 1) ? (int32_t)idsum : -1;
                 ++e;
@@ -712,7 +705,7 @@ __global__ void __launch_bounds__(128, 6) vd_faces_kernel(VolTab T, Bases B, con
                                                        const int32_t* __restrict__ fbs, const int32_t* __restrict__ lab,
                                                        const float* __restrict__ sxyz, float* __restrict__ lamf,
                                                        int32_t* __restrict__ tris, int2* __restrict__ edges,
-                                                       FaceRec* __restrict__ F, EdgeRec* __restrict__ E,
+                                                       FaceRec* __restrict__ F, EdgeRecs E,
                                                        int32_t* __restrict__ g0, const float* __restrict__ thr) {
     __shared__ uint8_t s_slots[4][96];
     const int lane = threadIdx.x & 31;
@@ -858,15 +851,8 @@ __global__ void __launch_bounds__(128, 6) vd_faces_kernel(VolTab T, Bases B, con
                     fr.e1 = e12;
                     fr.e2 = e32 | pass;
                     F[t1] = fr;
-                    EdgeRec er;
-                    er.v0 = dv0;
-                    er.v1 = dv1;
-                    er.rs = rs_make(2, lm < tb ? 2u : 0u, (unsigned long long)t0 + (unsigned long long)t1);
-                    er.trig = 0;
-                    er.em = lr_;
-                    er.rm = kAlive;
-                    er.pad = 0;
-                    E[diag] = er;
+                    E.h[diag] = EdgeHead{dv0, dv1, kAlive, lr_};
+                    E.n[diag] = EdgeCnt{rs_make(2, lm < tb ? 2u : 0u, (unsigned long long)t0 + (unsigned long long)t1), 0u, 0};
                     g0[diag] = -1;  // two triangles: no FE pair
                 }
             }
@@ -1169,9 +1155,10 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes, double t_thr) {
         VC_TRY(ensure_n<uint32_t>(c, c->vd_vlat, nv));  // each vertex's lattice point, for the remaining complex
     }
     VC_TRY(ensure_n<float>(c, c->vd_lam, nface));  // lambda per face
+    EdgeRecs ER;  // none unless folded
     if (folded) {
         VC_TRY(ensure_n<FaceRec>(c, c->face_rec, nt));
-        VC_TRY(ensure_n<EdgeRec>(c, c->edge_rec, ne));
+        VC_TRY(ensure_edge_recs(c, c->edge_rec, ne, &ER));
         VC_TRY(ensure_n<VertRec>(c, c->vert_rec, nv));
         VC_TRY(ensure_n<int32_t>(c, c->thin_g0, nv + ne));
     }
@@ -1184,14 +1171,14 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes, double t_thr) {
             vd_faces_kernel<<<row_grid(c, c->h_off[kLRow][c->nvol]), 128, 0, c->stream>>>(
                 c->tab, c->bases, planes, vb, eb, fb, ptr<int32_t>(c->ft_id), ptr<float>(c->site_xyz),
                 ptr<float>(c->vd_lam), geom ? ptr<int32_t>(c->tris) : nullptr, geom ? ptr<int2>(c->edges) : nullptr,
-                folded ? ptr<FaceRec>(c->face_rec) : nullptr, folded ? ptr<EdgeRec>(c->edge_rec) : nullptr, g0, thr);
+                folded ? ptr<FaceRec>(c->face_rec) : nullptr, ER, g0, thr);
             launched(c);
         }
         {
             Region k(c, "vd_vertices_edges");
             vd_vertices_edges_kernel<<<row_grid(c, c->h_off[kLRow][c->nvol]), 128, 0, c->stream>>>(
-                c->tab, c->bases, planes, vb, eb, fb, ptr<float>(c->vd_lam), geom ? ptr<int2>(c->edges) : nullptr,
-                folded ? ptr<EdgeRec>(c->edge_rec) : nullptr, geom ? ptr<float>(c->vts) : nullptr,
+                c->tab, c->bases, planes, vb, eb, fb, ptr<float>(c->vd_lam), geom ? ptr<int2>(c->edges) : nullptr, ER,
+                geom ? ptr<float>(c->vts) : nullptr,
                 geom ? nullptr : ptr<uint32_t>(c->vd_vlat), folded ? ptr<VertRec>(c->vert_rec) : nullptr, g0, ne,
                 thr);
             launched(c);
@@ -1233,9 +1220,9 @@ int ensure_vd_geometry(vc_ctx* c) {
     Region r(c, "vd_geometry");
     vd_faces_kernel<<<row_grid(c, c->h_off[kLRow][c->nvol]), 128, 0, c->stream>>>(
         c->tab, c->bases, planes, vb, eb, fb, ptr<int32_t>(c->ft_id), ptr<float>(c->site_xyz), ptr<float>(c->vd_lam),
-        ptr<int32_t>(c->tris), ptr<int2>(c->edges), nullptr, nullptr, nullptr, nullptr);
+        ptr<int32_t>(c->tris), ptr<int2>(c->edges), nullptr, EdgeRecs{}, nullptr, nullptr);
     vd_vertices_edges_kernel<<<row_grid(c, c->h_off[kLRow][c->nvol]), 128, 0, c->stream>>>(
-        c->tab, c->bases, planes, vb, eb, fb, ptr<float>(c->vd_lam), ptr<int2>(c->edges), nullptr, ptr<float>(c->vts),
+        c->tab, c->bases, planes, vb, eb, fb, ptr<float>(c->vd_lam), ptr<int2>(c->edges), EdgeRecs{}, ptr<float>(c->vts),
         nullptr, nullptr, nullptr, ne, nullptr);
     launched(c, 2);
     VC_CUDA(c, cudaGetLastError());
@@ -1264,7 +1251,7 @@ __device__ __forceinline__ void lattice_vertex(const VolTab& T, const Bases& B, 
 // a kept triangle's corners from the records of its first two sides (sides
 // (a,b), (b,c), (c,a) in face order: b is the vertex the first two share).
 __global__ void vd_rem_write_kernel(int32_t nv, int32_t ne, int32_t nt, Kept K, VolTab T, int nvol,
-                                    const uint32_t* __restrict__ vlat, const EdgeRec* __restrict__ E,
+                                    const uint32_t* __restrict__ vlat, const EdgeHead* __restrict__ E,
                                     const FaceRec* __restrict__ F,
                                     float* __restrict__ ovts, int2* __restrict__ oedges, int32_t* __restrict__ otris,
                                     Bases B, int nmap) {
@@ -1315,7 +1302,7 @@ int lattice_rem_write(vc_ctx* c, const Kept& K, int nmap) {
     const int64_t nw = (nv + 31) / 32 + (ne + 31) / 32 + (nt + 31) / 32;
     vd_rem_write_kernel<<<cell_grid(c, 32 * nw), 256, 0, c->stream>>>(
         (int32_t)nv, (int32_t)ne, (int32_t)nt, K, c->tab, c->nvol, ptr<uint32_t>(c->vd_vlat),
-        ptr<EdgeRec>(c->edge_rec), ptr<FaceRec>(c->face_rec), ptr<float>(c->rem_vts),
+        ptr<EdgeHead>(c->edge_rec), ptr<FaceRec>(c->face_rec), ptr<float>(c->rem_vts),
         ptr<int2>(c->rem_edges), ptr<int32_t>(c->rem_tris), c->bases, nmap);
     launched(c);
     VC_CUDA(c, cudaGetLastError());
