@@ -58,7 +58,10 @@ constexpr int32_t kAlive = INT32_MAX;  // removal position of a cell still prese
 // bits 32-63.  Removing incident cell x subtracts (x << 32) + (pass << 16) +
 // 1 in one atomic; when the count is 1 the sum is the id of the one cell
 // left and the pass field says whether it passes the filter.  Vertex words
-// leave the pass field at zero (their filter reads the edge record).
+// leave the pass field at zero and sum 2 e + p over their edges e instead of
+// e (p = 1 when edge e passes the filter, its measure below the edge
+// threshold): when the count is 1 the sum is the one edge left, shifted up
+// one bit, with its filter in bit 0.
 constexpr int kRefBits = 16;
 constexpr unsigned long long kRefMask = (1ull << kRefBits) - 1ull;  // largest incidence count
 __host__ __device__ __forceinline__ unsigned long long rs_make(unsigned long long count, unsigned long long pass,

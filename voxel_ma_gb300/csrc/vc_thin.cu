@@ -136,15 +136,18 @@ __global__ void build_records_kernel(const int2* __restrict__ edges, const int32
         } else {
             const int64_t v = i - nt - ne;
             const int32_t o0 = ve_off[v], o1 = ve_off[v + 1];
-            unsigned long long idsum = 0;
-            for (int32_t k = o0; k < o1; ++k) idsum += (unsigned)ve_ids[k];
+            unsigned long long idsum = 0;  // 2 e + (e passes the filter): the measure the edge record holds, below l_t
+            for (int32_t k = o0; k < o1; ++k) {
+                const int32_t e = ve_ids[k];
+                idsum += 2u * (unsigned)e + ((all_pass ? 0.0f : em[e]) < l_t ? 1u : 0u);
+            }
             if ((unsigned long long)(o1 - o0) > kRefMask) set_error(err, VC_ERR_ARG);
             VertRec r;
             r.rs = rs_make((unsigned)(o1 - o0), 0, idsum);
             r.trig = 0;
             r.rm = kAlive;
             V[v] = r;
-            g0[(int64_t)ne + v] = (o1 - o0 == 1 && (all_pass || em[idsum] < l_t)) ? (int32_t)idsum : -1;
+            g0[(int64_t)ne + v] = (o1 - o0 == 1 && (idsum & 1u)) ? (int32_t)(idsum >> 1) : -1;
         }
     }
 }
@@ -157,33 +160,16 @@ constexpr int kG0Items = 8;
 constexpr int64_t kG0Tile = (int64_t)kThreads * kG0Items;
 
 // Generation-0 code i (edges first, then vertices) names an item when it is
-// >= 0.  With vfilter set (records written by the lattice complex with the
-// thresholds folded in), a vertex code names the vertex's one edge, and the
-// count pass drops (writes -1 over) the codes whose edge fails the filter,
-// read from the edge's record; otherwise every code >= 0 already passed.
-__global__ void __launch_bounds__(kThreads) gen0_count_kernel(int32_t* __restrict__ g0, int64_t n, int64_t ne,
-                                                              const EdgeHead* __restrict__ vfilter,
+// >= 0.
+__global__ void __launch_bounds__(kThreads) gen0_count_kernel(const int32_t* __restrict__ g0, int64_t n,
                                                               int64_t* __restrict__ sums) {
     __shared__ int64_t sm[33];
     const int64_t base = (int64_t)blockIdx.x * kG0Tile;
-    // the codes, then the filter's record loads, each batch in flight together
-    int32_t x[kG0Items];
-#pragma unroll
-    for (int r = 0; r < kG0Items; ++r) {
-        const int64_t i = base + (int64_t)r * kThreads + threadIdx.x;
-        x[r] = i < n ? __ldcs(g0 + i) : -1;
-    }
-    bool drop[kG0Items];
-#pragma unroll
-    for (int r = 0; r < kG0Items; ++r) {
-        const int64_t i = base + (int64_t)r * kThreads + threadIdx.x;
-        drop[r] = vfilter && x[r] >= 0 && i >= ne && !(__ldg(&vfilter[x[r]].em) < 0.0f);
-    }
     int64_t acc = 0;
 #pragma unroll
     for (int r = 0; r < kG0Items; ++r) {
-        if (drop[r]) g0[base + (int64_t)r * kThreads + threadIdx.x] = -1;
-        acc += (x[r] >= 0 && !drop[r]) ? 1 : 0;
+        const int64_t i = base + (int64_t)r * kThreads + threadIdx.x;
+        if (i < n) acc += __ldcs(g0 + i) >= 0 ? 1 : 0;
     }
     int64_t tot;
     block_exclusive_sum<int64_t>(acc, sm, &tot);
@@ -349,7 +335,9 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                         const int32_t v0 = ea[k].x, v1 = ea[k].y;  // EdgeHead: v0 v1 rm em
                         // the edge is named by no other item of this generation
                         A.EH[e].rm = p;
-                        const unsigned long long df = rs_drop(f, fpass), de = rs_drop(e, 0u);
+                        // the edge's filter: its measure below the edge threshold
+                        const unsigned epass = __int_as_float(ea[k].w) < l_t ? 1u : 0u;
+                        const unsigned long long df = rs_drop(f, fpass), de = rs_drop((int32_t)(2u * (unsigned)e + epass), 0u);
                         const int oa = rs_count(atomicAdd(&A.EN[sa].rs, df));
                         const int ob = rs_count(atomicAdd(&A.EN[sb].rs, df));
                         const int o0 = rs_count(atomicAdd(&A.V[v0].rs, de));
@@ -384,7 +372,8 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                         A.V[v].rm = p;
                         const int32_t v0 = ea[k].x, v1 = ea[k].y;
                         const int32_t u = v0 != v ? v0 : v1;
-                        const int ou = rs_count(atomicAdd(&A.V[u].rs, rs_drop(e, 0u)));
+                        const unsigned epass = __int_as_float(ea[k].w) < l_t ? 1u : 0u;
+                        const int ou = rs_count(atomicAdd(&A.V[u].rs, rs_drop((int32_t)(2u * (unsigned)e + epass), 0u)));
                         if (ou == 2) one[4 * k + 2] = u;
                         dec[4 * k + 2] = u;
                         dtg[4 * k + 2] = trig_make(p, 0);
@@ -444,8 +433,9 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                         const int32_t u = code;
                         const int4 va = __ldcg(reinterpret_cast<const int4*>(A.V + u));  // rs trig rm
                         const unsigned long long rs = ((unsigned long long)(uint32_t)va.y << 32) | (uint32_t)va.x;
-                        const int32_t e3 = rs_last(rs);
-                        want = rs_count(rs) == 1 && A.EH[e3].em < l_t;
+                        const uint32_t code = (uint32_t)rs_last(rs);  // 2 e + filter of the one edge left
+                        const int32_t e3 = (int32_t)(code >> 1);
+                        want = rs_count(rs) == 1 && (code & 1u);
                         tg = max((uint32_t)va.z, ltg);
                         slot = 2 + (int)(tg & 1u);
                         ch = make_ev(e3, u);
@@ -711,7 +701,6 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats, bool all_pass) {
     }
     {
         Region r(c, "thin_setup");
-        const bool folded = c->records_fresh;
         if (c->records_fresh) {
             c->records_fresh = false;  // the next thinning of this complex rebuilds them
         } else {
@@ -733,8 +722,8 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats, bool all_pass) {
         if (tiles > 0) {
             VC_TRY(ensure_n<int64_t>(c, c->scratch, tiles + 1));
             int64_t* sums = ptr<int64_t>(c->scratch);
-            int32_t* g0 = ptr<int32_t>(c->thin_g0);
-            gen0_count_kernel<<<(unsigned)tiles, kThreads, 0, c->stream>>>(g0, ng, ne, folded ? A.EH : nullptr, sums);
+            const int32_t* g0 = ptr<int32_t>(c->thin_g0);
+            gen0_count_kernel<<<(unsigned)tiles, kThreads, 0, c->stream>>>(g0, ng, sums);
             scan_sums_single<<<1, 1024, 0, c->stream>>>(sums, tiles, ctl + 0);
             gen0_write_kernel<<<(unsigned)tiles, kThreads, 0, c->stream>>>(A, (int32_t)ne, g0, ng, sums);
             launched(c, 3);

@@ -609,81 +609,85 @@ __global__ void __launch_bounds__(128, 6) vd_vertices_edges_kernel(VolTab T, Bas
             fid[6] = (h1 || h2) ? face_at(R0p, S0p0, 0u, 0u, t, true, 0) : -1;          // (a,b+1,c+1)+x
             fid[7] = face_at(R0, S00, S01, 0u, t, true, 0);                             // (a,b,c+1)+x
             fid[8] = face_at(R0, S00, S01, 0u, t, true, 1);                             // (a,b,c+1)+y
-            // lambdas of the faces an axis edge of this point needs
-            const unsigned need = (h0 ? 0x0Fu : 0u) | (h1 ? 0x78u : 0u) | (h2 ? 0x1C4u : 0u);
+            // the faces of the lattice edges from the point itself: with the
+            // nine above they carry the plaquettes of the three axis edges
+            // into the voxel (from -x, -y, -z)
+            const int32_t fx = face_at(R0, 0u, 0u, 0u, t, false, 0), fy = face_at(R0, 0u, 0u, 0u, t, false, 1),
+                          fz = face_at(R0, 0u, 0u, 0u, t, false, 2);
             float lj[9];
 #pragma unroll
-            for (int i = 0; i < 9; ++i) lj[i] = (fid[i] >= 0 && ((need >> i) & 1u)) ? __ldg(lamf + fid[i]) : 0.0f;
-            // the vertex record
+            for (int i = 0; i < 9; ++i) lj[i] = fid[i] >= 0 ? __ldg(lamf + fid[i]) : 0.0f;
+            const float lx = fx >= 0 ? __ldg(lamf + fx) : 0.0f, ly = fy >= 0 ? __ldg(lamf + fy) : 0.0f,
+                        lz = fz >= 0 ? __ldg(lamf + fz) : 0.0f;
+            // the axis edges' records; an edge passes the filter when the
+            // largest lambda of its faces is below the threshold (its measure
+            // is then folded to -1)
+            constexpr int kSlot[3][4] = {{0, 1, 2, 3}, {4, 5, 3, 6}, {7, 8, 6, 2}};
+            bool epass[3] = {false, false, false};
+            {
+                int32_t e = e_own;
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    if (!(d == 0 ? h0 : (d == 1 ? h1 : h2))) continue;
+                    float mx = 0.0f;
+                    unsigned kk = 0, npass = 0;
+                    unsigned long long idsum = 0;
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        const int s = kSlot[d][i];
+                        if (fid[s] >= 0) {
+                            mx = fmaxf(mx, lj[s]);
+                            npass += lj[s] < tb ? 1u : 0u;
+                            idsum += (unsigned)(2 * fid[s] + (i < 2 ? 1 : 0));
+                            ++kk;
+                        }
+                    }
+                    if (edges) edges[e] = make_int2(v0, v1[d]);
+                    const float em = rec_measure(mx, thr, bv);
+                    epass[d] = em < 0.0f;
+                    E.h[e] = EdgeHead{v0, v1[d], kAlive, em};
+                    E.n[e] = EdgeCnt{rs_make(kk, npass, idsum), 0u, 0};
+                    // generation 0: an FE pair when the one face passes the filter
+                    g0[e] = (kk == 1 && npass == 1) ? (int32_t)idsum : -1;
+                    ++e;
+                }
+            }
+            // the vertex record: its incident edges counted, and 2 e + (e
+            // passes the filter) summed over them
             {
                 unsigned kk = 0;
                 unsigned long long idsum = 0;
-                if (bt(Rm0.e0, t)) {  // (a-1,b,c)+x
+                auto add = [&](int32_t e, bool pass) {
                     ++kk;
-                    idsum += (unsigned)(Rm0.eb + pc3(Rm0.e0, Rm0.e1, Rm0.e2, m) + fbv);
-                }
-                if (bt(R0m.e1, t)) {  // (a,b-1,c)+y
-                    ++kk;
-                    idsum += (unsigned)(R0m.eb + pc3(R0m.e0, R0m.e1, R0m.e2, m) + bt(R0m.e0, t) + fbv);
-                }
-                if (bt((R0.e2 << 1) | (pe2 >> 31), t)) {  // (a,b,c-1)+z: the last axis edge before c
-                    ++kk;
-                    idsum += (unsigned)(e_own - 1);
-                }
+                    idsum += 2u * (unsigned)e + (pass ? 1u : 0u);
+                };
+                // the largest lambda of existing faces (0 if none) below the threshold
+                auto passes4 = [&](float a, float b, float c, float d) {
+                    return fmaxf(fmaxf(fmaxf(0.0f, a), b), fmaxf(c, d)) < tb;
+                };
+                if (bt(Rm0.e0, t))  // (a-1,b,c)+x: faces (a,b,c)+y, +z, (a,b,c+1)+y, (a,b+1,c)+z
+                    add(Rm0.eb + pc3(Rm0.e0, Rm0.e1, Rm0.e2, m) + fbv, passes4(ly, lz, lj[8], lj[4]));
+                if (bt(R0m.e1, t))  // (a,b-1,c)+y: faces (a,b,c)+z, +x, (a+1,b,c)+z, (a,b,c+1)+x
+                    add(R0m.eb + pc3(R0m.e0, R0m.e1, R0m.e2, m) + bt(R0m.e0, t) + fbv, passes4(lz, lx, lj[1], lj[7]));
+                if (bt((R0.e2 << 1) | (pe2 >> 31), t))  // (a,b,c-1)+z: the last axis edge before c; faces
+                    add(e_own - 1, passes4(lx, ly, lj[5], lj[0]));  // (a,b,c)+x, +y, (a,b+1,c)+x, (a+1,b,c)+y
                 {
                     int32_t e = e_own;
-                    if (h0) {
-                        ++kk;
-                        idsum += (unsigned)e++;
-                    }
-                    if (h1) {
-                        ++kk;
-                        idsum += (unsigned)e++;
-                    }
-                    if (h2) {
-                        ++kk;
-                        idsum += (unsigned)e;
-                    }
+                    if (h0) add(e++, epass[0]);
+                    if (h1) add(e++, epass[1]);
+                    if (h2) add(e, epass[2]);
                 }
-                const int dg[6] = {7, 5, 0, 8, 4, 1};  // the diagonals' faces
+                const int dg[6] = {7, 5, 0, 8, 4, 1};  // the diagonals' faces (a diagonal's measure is its face's)
 #pragma unroll
                 for (int i = 0; i < 6; ++i)
-                    if (fid[dg[i]] >= 0) {
-                        ++kk;
-                        idsum += (unsigned)(eb1 + fid[dg[i]]);
-                    }
+                    if (fid[dg[i]] >= 0) add(eb1 + fid[dg[i]], lj[dg[i]] < tb);
                 VertRec vr;
                 vr.rs = rs_make(kk, 0, idsum);
                 vr.trig = 0;
                 vr.rm = kAlive;
                 V[v0] = vr;
-                g0[ne + v0] = kk == 1 ? (int32_t)idsum : -1;
-            }
-            // per axis: the four faces' slots (the first two carry the edge as triangle 1)
-            constexpr int kSlot[3][4] = {{0, 1, 2, 3}, {4, 5, 3, 6}, {7, 8, 6, 2}};
-            int32_t e = e_own;
-#pragma unroll
-            for (int d = 0; d < 3; ++d) {
-                if (!(d == 0 ? h0 : (d == 1 ? h1 : h2))) continue;
-                float mx = 0.0f;
-                unsigned kk = 0, npass = 0;
-                unsigned long long idsum = 0;
-#pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    const int s = kSlot[d][i];
-                    if (fid[s] >= 0) {
-                        mx = fmaxf(mx, lj[s]);
-                        npass += lj[s] < tb ? 1u : 0u;
-                        idsum += (unsigned)(2 * fid[s] + (i < 2 ? 1 : 0));
-                        ++kk;
-                    }
-                }
-                if (edges) edges[e] = make_int2(v0, v1[d]);
-                E.h[e] = EdgeHead{v0, v1[d], kAlive, rec_measure(mx, thr, bv)};
-                E.n[e] = EdgeCnt{rs_make(kk, npass, idsum), 0u, 0};
-                // generation 0: an FE pair when the one face passes the filter
-                g0[e] = (kk == 1 && npass == 1) ? (int32_t)idsum : -1;
-                ++e;
+                // generation 0: an EV pair when the one edge passes the filter
+                g0[ne + v0] = (kk == 1 && (idsum & 1u)) ? (int32_t)(idsum >> 1) : -1;
             }
         }
     }
