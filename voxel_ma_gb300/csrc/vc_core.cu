@@ -223,7 +223,7 @@ int scan_exclusive_i64(vc_ctx* c, const int64_t* in, int64_t* out, int64_t n, in
 std::vector<DevBuf*> ctx_buffers(vc_ctx* c) {
     return {&c->scratch, &c->scratch2, &c->occ, &c->oct_cells, &c->oct_nodes, &c->oct_stream, &c->oct_leaves, &c->site_xyz, &c->site_count, &c->site_bits, &c->site_id_lat, &c->ft_d2,
             &c->ft_id, &c->ft_tmp, &c->ft_far, &c->vd_seg, &c->vd_voff, &c->vd_eoff, &c->vd_foff, &c->vd_tri_face,
-            &c->vd_face_sites, &c->vd_lam, &c->vd_radius, &c->vd_vlat, &c->tab_buf, &c->bases_buf, &c->vts, &c->edges_in, &c->edges, &c->tris,
+            &c->vd_face_sites, &c->vd_lam, &c->vd_radius, &c->vd_vlat, &c->vd_fpass, &c->tab_buf, &c->bases_buf, &c->vts, &c->edges_in, &c->edges, &c->tris,
             &c->tri_edges, &c->ve_off, &c->ve_ids, &c->ef_off, &c->ef_ids, &c->hash_keys, &c->hash_pos,
             &c->hash_id, &c->side_slot, &c->vm, &c->em, &c->fm, &c->face_rec, &c->edge_rec, &c->vert_rec, &c->thin_g0, &c->q0,
             &c->q1, &c->child, &c->cells, &c->blk_cnt, &c->keep_v, &c->keep_e,

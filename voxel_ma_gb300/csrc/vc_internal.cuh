@@ -243,6 +243,7 @@ struct vc_ctx {
     bool vd_thr_valid = false; // bases.thr holds the volumes' thinning thresholds of this complex
     vc::DevBuf vd_radius;             // float per vertex of the lattice complex
     vc::DevBuf vd_vlat;               // uint32 per vertex: its lattice point within its volume (timed path)
+    vc::DevBuf vd_fpass;              // uint4 per segment: faces whose lambda is below the threshold (timed path)
     std::vector<float> vol_inside;  // inside-part size per volume
     bool cc_batched = false;        // the complex is the lattice complex of a batch of > 1 volumes
     // cell complex (finalized, CSR)

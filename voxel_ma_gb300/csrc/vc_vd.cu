@@ -507,24 +507,25 @@ __device__ __forceinline__ int32_t face_at(const RowPlanes& R, uint32_t S0, uint
 // faces (p1, d) and (p3, d) that have it as q1 / q3 (p1 = p + e_w, p3 = p +
 // e_u).  Axis edges: endpoints and, with records, thinning records
 // (incident triangles counted, summed and tested against the threshold;
-// measure = max lambda of the incident faces, voroinfo.cpp:1490-1538); face
-// lambdas come from lamf (one per face, written by vd_faces_kernel).  The
-// faces of the plaquettes of the point's three axis edges (the lattice edges
-// along u from nb and nb + e_w and along w from nb and nb + e_u, nb = the
-// point + e_d, u = d+1, w = d+2 mod 3) are nine lattice edges, looked up once
-// and their lambdas loaded together:
+// measure = max lambda of the incident faces, voroinfo.cpp:1490-1538, folded
+// to -1 below the threshold and +1 otherwise).  With the threshold folded in,
+// only whether each face's lambda is below it matters: the faces kernel
+// writes that per segment as three bit planes (fpass), read here beside the
+// face planes.  The faces of the plaquettes of the point's three axis edges
+// (the lattice edges along u from nb and nb + e_w and along w from nb and
+// nb + e_u, nb = the point + e_d, u = d+1, w = d+2 mod 3) are nine lattice
+// edges, looked up once:
 //   d = 0: (a+1,b,c)+y, (a+1,b,c)+z [triangle 1]; (a+1,b,c+1)+y, (a+1,b+1,c)+z [0]
 //   d = 1: (a,b+1,c)+z, (a,b+1,c)+x [1]; (a+1,b+1,c)+z, (a,b+1,c+1)+x [0]
 //   d = 2: (a,b,c+1)+x, (a,b,c+1)+y [1]; (a,b+1,c+1)+x, (a+1,b,c+1)+y [0]
 // (the triangle of each face that carries the edge: 1 for the two faces at
 // nb); the vertex's six diagonals are the faces of (a,b,c+1)+x, (a,b+1,c)+x,
-// (a+1,b,c)+y, (a,b,c+1)+y, (a,b+1,c)+z and (a+1,b,c)+z among them.  A
-// vertex with one incident edge is written to the generation-0 codes as
-// that edge; whether the edge passes the filter is read when generation 0
-// is selected (the edge's record may be written by another warp here).
-__global__ void __launch_bounds__(128, 6) vd_vertices_edges_kernel(VolTab T, Bases B, const SegPlanes* __restrict__ planes,
+// (a+1,b,c)+y, (a,b,c+1)+y, (a,b+1,c)+z and (a+1,b,c)+z among them, and the
+// plaquettes of the edges into the voxel take three more: the lattice edges
+// from the point itself.
+__global__ void __launch_bounds__(128, 5) vd_vertices_edges_kernel(VolTab T, Bases B, const SegPlanes* __restrict__ planes,
                                                        const int32_t* __restrict__ vb, const int32_t* __restrict__ eb,
-                                                       const int32_t* __restrict__ fbs, const float* __restrict__ lamf,
+                                                       const int32_t* __restrict__ fbs, const uint4* __restrict__ fpass,
                                                        int2* __restrict__ edges, EdgeRecs E,
                                                        float* __restrict__ vts, uint32_t* __restrict__ vlat,
                                                        VertRec* __restrict__ V, int32_t* __restrict__ g0, int64_t ne,
@@ -571,6 +572,19 @@ __global__ void __launch_bounds__(128, 6) vd_vertices_edges_kernel(VolTab T, Bas
             }
             uint32_t pe2 = 0u;
             if (rec && k > 0 && (pv.x & 1u)) pe2 = __ldg(&planes[s0 + k - 1].e2);
+            // the faces' filter planes of the same rows (and segments)
+            uint4 q0 = make_uint4(0u, 0u, 0u, 0u), qp0 = q0, q0p = q0, qpp = q0, m0 = q0, mp0 = q0, m0p = q0;
+            if (rec) {
+                q0 = __ldg(fpass + s0 + k);
+                qp0 = __ldg(fpass + sp0 + k);
+                q0p = __ldg(fpass + s0p + k);
+                qpp = __ldg(fpass + spp + k);
+                if (k + 1 < nsr && (pv.x >> 31)) {
+                    m0 = __ldg(fpass + s0 + k + 1);
+                    mp0 = __ldg(fpass + sp0 + k + 1);
+                    m0p = __ldg(fpass + s0p + k + 1);
+                }
+            }
             const int t = lane;
             if (!bt(pv.x, t)) continue;
             const uint32_t m = below(t);
@@ -614,14 +628,27 @@ __global__ void __launch_bounds__(128, 6) vd_vertices_edges_kernel(VolTab T, Bas
             // into the voxel (from -x, -y, -z)
             const int32_t fx = face_at(R0, 0u, 0u, 0u, t, false, 0), fy = face_at(R0, 0u, 0u, 0u, t, false, 1),
                           fz = face_at(R0, 0u, 0u, 0u, t, false, 2);
-            float lj[9];
-#pragma unroll
-            for (int i = 0; i < 9; ++i) lj[i] = fid[i] >= 0 ? __ldg(lamf + fid[i]) : 0.0f;
-            const float lx = fx >= 0 ? __ldg(lamf + fx) : 0.0f, ly = fy >= 0 ? __ldg(lamf + fy) : 0.0f,
-                        lz = fz >= 0 ? __ldg(lamf + fz) : 0.0f;
-            // the axis edges' records; an edge passes the filter when the
-            // largest lambda of its faces is below the threshold (its measure
-            // is then folded to -1)
+            // whether each of these faces passes the filter (read where the face exists)
+            auto at_c = [&](const uint4& q, int ax) { return bt(ax == 0 ? q.x : (ax == 1 ? q.y : q.z), t) != 0; };
+            auto at_c1 = [&](const uint4& q, const uint4& qn, int ax) {  // at c + 1
+                const uint32_t w = ax == 0 ? q.x : q.y, wn = ax == 0 ? qn.x : qn.y;
+                return bt((w >> 1) | (wn << 31), t) != 0;
+            };
+            bool pj[9];
+            pj[0] = at_c(qp0, 1);
+            pj[1] = at_c(qp0, 2);
+            pj[2] = at_c1(qp0, mp0, 1);
+            pj[3] = at_c(qpp, 2);
+            pj[4] = at_c(q0p, 2);
+            pj[5] = at_c(q0p, 0);
+            pj[6] = at_c1(q0p, m0p, 0);
+            pj[7] = at_c1(q0, m0, 0);
+            pj[8] = at_c1(q0, m0, 1);
+            const bool px = at_c(q0, 0), py = at_c(q0, 1), pz = at_c(q0, 2);
+            // an edge passes when its largest face lambda (0 without faces) is
+            // below the threshold: every face passes, and 0 < threshold
+            const bool zero_passes = 0.0f < tb;
+            // the axis edges' records
             constexpr int kSlot[3][4] = {{0, 1, 2, 3}, {4, 5, 3, 6}, {7, 8, 6, 2}};
             bool epass[3] = {false, false, false};
             {
@@ -629,23 +656,21 @@ __global__ void __launch_bounds__(128, 6) vd_vertices_edges_kernel(VolTab T, Bas
 #pragma unroll
                 for (int d = 0; d < 3; ++d) {
                     if (!(d == 0 ? h0 : (d == 1 ? h1 : h2))) continue;
-                    float mx = 0.0f;
                     unsigned kk = 0, npass = 0;
                     unsigned long long idsum = 0;
 #pragma unroll
                     for (int i = 0; i < 4; ++i) {
                         const int s = kSlot[d][i];
                         if (fid[s] >= 0) {
-                            mx = fmaxf(mx, lj[s]);
-                            npass += lj[s] < tb ? 1u : 0u;
+                            npass += pj[s] ? 1u : 0u;
                             idsum += (unsigned)(2 * fid[s] + (i < 2 ? 1 : 0));
                             ++kk;
                         }
                     }
                     if (edges) edges[e] = make_int2(v0, v1[d]);
-                    const float em = rec_measure(mx, thr, bv);
-                    epass[d] = em < 0.0f;
-                    E.h[e] = EdgeHead{v0, v1[d], kAlive, em};
+                    // the measure folded to -1 below the threshold, +1 otherwise
+                    epass[d] = npass == kk && zero_passes;
+                    E.h[e] = EdgeHead{v0, v1[d], kAlive, epass[d] ? -1.0f : 1.0f};
                     E.n[e] = EdgeCnt{rs_make(kk, npass, idsum), 0u, 0};
                     // generation 0: an FE pair when the one face passes the filter
                     g0[e] = (kk == 1 && npass == 1) ? (int32_t)idsum : -1;
@@ -661,16 +686,18 @@ __global__ void __launch_bounds__(128, 6) vd_vertices_edges_kernel(VolTab T, Bas
                     ++kk;
                     idsum += 2u * (unsigned)e + (pass ? 1u : 0u);
                 };
-                // the largest lambda of existing faces (0 if none) below the threshold
-                auto passes4 = [&](float a, float b, float c, float d) {
-                    return fmaxf(fmaxf(fmaxf(0.0f, a), b), fmaxf(c, d)) < tb;
+                // every existing face of the four passes (and 0 < threshold)
+                auto passes4 = [&](int32_t f1, bool p1, int32_t f2, bool p2, int32_t f3, bool p3, int32_t f4, bool p4) {
+                    return (f1 < 0 || p1) && (f2 < 0 || p2) && (f3 < 0 || p3) && (f4 < 0 || p4) && zero_passes;
                 };
                 if (bt(Rm0.e0, t))  // (a-1,b,c)+x: faces (a,b,c)+y, +z, (a,b,c+1)+y, (a,b+1,c)+z
-                    add(Rm0.eb + pc3(Rm0.e0, Rm0.e1, Rm0.e2, m) + fbv, passes4(ly, lz, lj[8], lj[4]));
+                    add(Rm0.eb + pc3(Rm0.e0, Rm0.e1, Rm0.e2, m) + fbv,
+                        passes4(fy, py, fz, pz, fid[8], pj[8], fid[4], pj[4]));
                 if (bt(R0m.e1, t))  // (a,b-1,c)+y: faces (a,b,c)+z, +x, (a+1,b,c)+z, (a,b,c+1)+x
-                    add(R0m.eb + pc3(R0m.e0, R0m.e1, R0m.e2, m) + bt(R0m.e0, t) + fbv, passes4(lz, lx, lj[1], lj[7]));
+                    add(R0m.eb + pc3(R0m.e0, R0m.e1, R0m.e2, m) + bt(R0m.e0, t) + fbv,
+                        passes4(fz, pz, fx, px, fid[1], pj[1], fid[7], pj[7]));
                 if (bt((R0.e2 << 1) | (pe2 >> 31), t))  // (a,b,c-1)+z: the last axis edge before c; faces
-                    add(e_own - 1, passes4(lx, ly, lj[5], lj[0]));  // (a,b,c)+x, +y, (a,b+1,c)+x, (a+1,b,c)+y
+                    add(e_own - 1, passes4(fx, px, fy, py, fid[5], pj[5], fid[0], pj[0]));  // (a,b,c)+x, +y, (a,b+1,c)+x, (a+1,b,c)+y
                 {
                     int32_t e = e_own;
                     if (h0) add(e++, epass[0]);
@@ -680,7 +707,7 @@ __global__ void __launch_bounds__(128, 6) vd_vertices_edges_kernel(VolTab T, Bas
                 const int dg[6] = {7, 5, 0, 8, 4, 1};  // the diagonals' faces (a diagonal's measure is its face's)
 #pragma unroll
                 for (int i = 0; i < 6; ++i)
-                    if (fid[dg[i]] >= 0) add(eb1 + fid[dg[i]], lj[dg[i]] < tb);
+                    if (fid[dg[i]] >= 0) add(eb1 + fid[dg[i]], pj[dg[i]]);
                 VertRec vr;
                 vr.rs = rs_make(kk, 0, idsum);
                 vr.trig = 0;
@@ -710,7 +737,8 @@ __global__ void __launch_bounds__(128, 6) vd_faces_kernel(VolTab T, Bases B, con
                                                        const float* __restrict__ sxyz, float* __restrict__ lamf,
                                                        int32_t* __restrict__ tris, int2* __restrict__ edges,
                                                        FaceRec* __restrict__ F, EdgeRecs E,
-                                                       int32_t* __restrict__ g0, const float* __restrict__ thr) {
+                                                       int32_t* __restrict__ g0, const float* __restrict__ thr,
+                                                       uint4* __restrict__ fpass) {
     __shared__ uint8_t s_slots[4][96];
     const int lane = threadIdx.x & 31;
     uint8_t* slots = s_slots[threadIdx.x >> 5];
@@ -778,6 +806,7 @@ __global__ void __launch_bounds__(128, 6) vd_faces_kernel(VolTab T, Bases B, con
                                   bt((Rm0.e1 << 1) | (pm0.z >> 31), lane) << 5 |           // 5: (a-1,b,c-1)+y
                                   bt((Rm0.e2 << 1) | (pm0.w >> 31), lane) << 6 |           // 6: (a-1,b,c-1)+z
                                   bt(Rmm.e0, lane) << 7;                                   // 7: (a-1,b-1,c)+x
+            uint32_t fp0 = 0u, fp1 = 0u, fp2 = 0u;  // this lane's faces that pass, by axis
             for (int r0 = 0; r0 < n; r0 += 32) {
                 // every lane takes part in the shuffles; lanes past the last
                 // face skip the rest
@@ -858,7 +887,19 @@ __global__ void __launch_bounds__(128, 6) vd_faces_kernel(VolTab T, Bases B, con
                     E.h[diag] = EdgeHead{dv0, dv1, kAlive, lr_};
                     E.n[diag] = EdgeCnt{rs_make(2, lm < tb ? 2u : 0u, (unsigned long long)t0 + (unsigned long long)t1), 0u, 0};
                     g0[diag] = -1;  // two triangles: no FE pair
+                    if (pass) {
+                        if (d == 0) fp0 |= 1u << t;
+                        else if (d == 1) fp1 |= 1u << t;
+                        else fp2 |= 1u << t;
+                    }
                 }
+            }
+            if (fpass) {
+                // the segment's filter planes: bit t of word d = the face of
+                // lattice edge (c0 + t) + d passes (its lambda below the threshold)
+                const uint32_t w0 = __reduce_or_sync(0xffffffffu, fp0), w1 = __reduce_or_sync(0xffffffffu, fp1),
+                               w2 = __reduce_or_sync(0xffffffffu, fp2);
+                if (lane == 0) fpass[s0 + k] = make_uint4(w0, w1, w2, 0u);
             }
             __syncwarp();
         }
@@ -1160,7 +1201,10 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes, double t_thr) {
     }
     VC_TRY(ensure_n<float>(c, c->vd_lam, nface));  // lambda per face
     EdgeRecs ER;  // none unless folded
+    uint4* fpass = nullptr;
     if (folded) {
+        VC_TRY(ensure_n<uint4>(c, c->vd_fpass, nseg));  // the faces' filter bits per segment
+        fpass = ptr<uint4>(c->vd_fpass);
         VC_TRY(ensure_n<FaceRec>(c, c->face_rec, nt));
         VC_TRY(ensure_edge_recs(c, c->edge_rec, ne, &ER));
         VC_TRY(ensure_n<VertRec>(c, c->vert_rec, nv));
@@ -1175,13 +1219,13 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes, double t_thr) {
             vd_faces_kernel<<<row_grid(c, c->h_off[kLRow][c->nvol]), 128, 0, c->stream>>>(
                 c->tab, c->bases, planes, vb, eb, fb, ptr<int32_t>(c->ft_id), ptr<float>(c->site_xyz),
                 ptr<float>(c->vd_lam), geom ? ptr<int32_t>(c->tris) : nullptr, geom ? ptr<int2>(c->edges) : nullptr,
-                folded ? ptr<FaceRec>(c->face_rec) : nullptr, ER, g0, thr);
+                folded ? ptr<FaceRec>(c->face_rec) : nullptr, ER, g0, thr, fpass);
             launched(c);
         }
         {
             Region k(c, "vd_vertices_edges");
             vd_vertices_edges_kernel<<<row_grid(c, c->h_off[kLRow][c->nvol]), 128, 0, c->stream>>>(
-                c->tab, c->bases, planes, vb, eb, fb, ptr<float>(c->vd_lam), geom ? ptr<int2>(c->edges) : nullptr, ER,
+                c->tab, c->bases, planes, vb, eb, fb, fpass, geom ? ptr<int2>(c->edges) : nullptr, ER,
                 geom ? ptr<float>(c->vts) : nullptr,
                 geom ? nullptr : ptr<uint32_t>(c->vd_vlat), folded ? ptr<VertRec>(c->vert_rec) : nullptr, g0, ne,
                 thr);
@@ -1224,9 +1268,9 @@ int ensure_vd_geometry(vc_ctx* c) {
     Region r(c, "vd_geometry");
     vd_faces_kernel<<<row_grid(c, c->h_off[kLRow][c->nvol]), 128, 0, c->stream>>>(
         c->tab, c->bases, planes, vb, eb, fb, ptr<int32_t>(c->ft_id), ptr<float>(c->site_xyz), ptr<float>(c->vd_lam),
-        ptr<int32_t>(c->tris), ptr<int2>(c->edges), nullptr, EdgeRecs{}, nullptr, nullptr);
+        ptr<int32_t>(c->tris), ptr<int2>(c->edges), nullptr, EdgeRecs{}, nullptr, nullptr, nullptr);
     vd_vertices_edges_kernel<<<row_grid(c, c->h_off[kLRow][c->nvol]), 128, 0, c->stream>>>(
-        c->tab, c->bases, planes, vb, eb, fb, ptr<float>(c->vd_lam), ptr<int2>(c->edges), EdgeRecs{}, ptr<float>(c->vts),
+        c->tab, c->bases, planes, vb, eb, fb, nullptr, ptr<int2>(c->edges), EdgeRecs{}, ptr<float>(c->vts),
         nullptr, nullptr, nullptr, ne, nullptr);
     launched(c, 2);
     VC_CUDA(c, cudaGetLastError());
