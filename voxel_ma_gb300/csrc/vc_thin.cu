@@ -97,13 +97,17 @@ __device__ __forceinline__ bool is_fe(int2 it) { return ((unsigned)it.x & kFE) !
 
 // Queue items, cell lists and child slots are written in one phase and read
 // in the next (the list by phase B, the slots by phase C, the next
-// generation's items by phase A).  Their accesses (cached at L2 only, as
-// every access of the generation kernel to data another block wrote is) carry
-// an evict-last L2 policy, so that they are still in L2 when read while the
-// random record touches, which mostly miss anyway, take the rest.  Measured
-// at 512^3 on one box: 44.0 ms with the default policy, 43.0 ms with this
-// one, 43.2 ms with half of these lines evict-last, 45.2 ms with evict-first.
-__device__ __forceinline__ unsigned long long stream_policy() {
+// generation's items by phase A); vertex records (16 bytes per vertex, the
+// smallest record array) take two decrements per face-edge pair besides
+// their own pairs and phase B.  Their accesses (cached at L2 only, as every
+// access of the generation kernel to data another block wrote is) carry an
+// evict-last L2 policy, so that they stay in L2 while the random touches of
+// edge and face records, which mostly miss anyway, take the rest.  Measured
+// at 512^3 on one box: default policy 44.0 ms, the streams evict-last 43.0 ms
+// (half of their lines 43.2 ms, evict-first 45.2 ms); on another box the
+// vertex records as well 39.9 against 40.3 ms, the edge counts as well 0.06
+// ms less again, the face records as well 0.3 ms more.
+__device__ __forceinline__ unsigned long long keep_policy() {
     unsigned long long p;
     asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
     return p;
@@ -123,6 +127,18 @@ __device__ __forceinline__ int4 ld_stream4(const int4* a, unsigned long long pol
 __device__ __forceinline__ void st_stream(int2* a, int2 v, unsigned long long pol) {
     asm volatile("st.global.cg.L2::cache_hint.v2.s32 [%0], {%1, %2}, %3;" ::"l"(a), "r"(v.x), "r"(v.y), "l"(pol)
                  : "memory");
+}
+__device__ __forceinline__ unsigned long long atom_add_keep(unsigned long long* a, unsigned long long v,
+                                                            unsigned long long pol) {
+    unsigned long long old;
+    asm volatile("atom.global.add.L2::cache_hint.u64 %0, [%1], %2, %3;" : "=l"(old) : "l"(a), "l"(v), "l"(pol) : "memory");
+    return old;
+}
+__device__ __forceinline__ void red_max_keep(uint32_t* a, uint32_t v, unsigned long long pol) {
+    asm volatile("red.global.max.L2::cache_hint.u32 [%0], %1, %2;" ::"l"(a), "r"(v), "l"(pol) : "memory");
+}
+__device__ __forceinline__ void st_keep(int32_t* a, int32_t v, unsigned long long pol) {
+    asm volatile("st.global.cg.L2::cache_hint.s32 [%0], %1, %2;" ::"l"(a), "r"(v), "l"(pol) : "memory");
 }
 __device__ __forceinline__ void st_stream4(int4* a, int4 v, unsigned long long pol) {
     asm volatile("st.global.cg.L2::cache_hint.v4.s32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(a), "r"(v.x), "r"(v.y),
@@ -271,7 +287,7 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
     int64_t my_processed = 0, my_skipped = 0;
     int64_t slots_ready = 0;  // child slots [0, 4 slots_ready) hold {-1, -1} or this generation's children
     const int lane = threadIdx.x & 31;
-    const unsigned long long stream_pol = stream_policy();
+    const unsigned long long keep_pol = keep_policy();
     while (n > 0) {
         const int par = gen & 1;
         const int2* cur = par ? A.qb : A.qa;
@@ -299,7 +315,7 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
         if (n > slots_ready) {
             const int64_t lo4 = 4 * slots_ready, hi4 = 4 * n;
             for (int64_t k = lo4 + (int64_t)b * blockDim.x + threadIdx.x; k < hi4; k += (int64_t)G * blockDim.x)
-                st_stream(A.child + k, make_int2(-1, -1), stream_pol);
+                st_stream(A.child + k, make_int2(-1, -1), keep_pol);
             slots_ready = n;
         }
         // ---- phase A: apply the removals of the items that won their claim
@@ -324,7 +340,7 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
             for (int k = 0; k < ITEMS; ++k) {
                 const int64_t i = r0 + threadIdx.x + (int64_t)k * blockDim.x;
                 has[k] = i < n;
-                it[k] = has[k] ? ld_stream(cur + i, stream_pol) : make_int2(0, 0);
+                it[k] = has[k] ? ld_stream(cur + i, keep_pol) : make_int2(0, 0);
             }
             // FE item: face record (ra) and the edge's head (ea); EV item:
             // vertex record (ra) and the edge's head (ea)
@@ -335,8 +351,8 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                 if (!has[k]) continue;
                 const bool fe = is_fe(it[k]);
                 const int32_t e = fe ? it[k].y : it[k].x;
-                ra[k] = __ldcg(fe ? reinterpret_cast<const int4*>(A.F + idx0(it[k]))
-                                  : reinterpret_cast<const int4*>(A.V + it[k].y));
+                ra[k] = fe ? __ldcg(reinterpret_cast<const int4*>(A.F + idx0(it[k])))
+                           : ld_stream4(reinterpret_cast<const int4*>(A.V + it[k].y), keep_pol);
                 ea[k] = __ldcg(reinterpret_cast<const int4*>(A.EH + e));
             }
             int32_t one[4 * ITEMS];  // cells whose count fell to 1 here
@@ -376,8 +392,8 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                         const unsigned long long df = rs_drop(f, fpass), de = rs_drop((int32_t)(2u * (unsigned)e + epass), 0u);
                         const int oa = rs_count(atomicAdd(&A.EN[sa].rs, df));
                         const int ob = rs_count(atomicAdd(&A.EN[sb].rs, df));
-                        const int o0 = rs_count(atomicAdd(&A.V[v0].rs, de));
-                        const int o1 = rs_count(atomicAdd(&A.V[v1].rs, de));
+                        const int o0 = rs_count(atom_add_keep(&A.V[v0].rs, de, keep_pol));
+                        const int o1 = rs_count(atom_add_keep(&A.V[v1].rs, de, keep_pol));
                         dec[4 * k + 0] = sa | kEdgeBit;
                         dec[4 * k + 1] = sb | kEdgeBit;
                         dec[4 * k + 2] = v0;
@@ -405,11 +421,12 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                     } else {
                         ++my_processed;
                         // nothing else touches v in this generation (its one edge is e)
-                        A.V[v].rm = p;
+                        st_keep(&A.V[v].rm, p, keep_pol);
                         const int32_t v0 = ea[k].x, v1 = ea[k].y;
                         const int32_t u = v0 != v ? v0 : v1;
                         const unsigned epass = __int_as_float(ea[k].w) < l_t ? 1u : 0u;
-                        const int ou = rs_count(atomicAdd(&A.V[u].rs, rs_drop((int32_t)(2u * (unsigned)e + epass), 0u)));
+                        const int ou =
+                            rs_count(atom_add_keep(&A.V[u].rs, rs_drop((int32_t)(2u * (unsigned)e + epass), 0u), keep_pol));
                         if (ou == 2) one[4 * k + 2] = u;
                         dec[4 * k + 2] = u;
                         dtg[4 * k + 2] = trig_make(p, 0);
@@ -424,12 +441,12 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
             for (int q = 0; q < 4 * ITEMS; ++q) {
                 if (dec[q] == -1) continue;
                 if (dec[q] & kEdgeBit) atomicMax(&A.EN[dec[q] & ~kEdgeBit].trig, dtg[q]);
-                else atomicMax(&A.V[dec[q]].trig, dtg[q]);
+                else red_max_keep(&A.V[dec[q]].trig, dtg[q], keep_pol);
             }
             __syncthreads();
             if (threadIdx.x == 0) s_gbase = s_ncell ? atomicAdd(ctr + 0, s_ncell) : 0;
             __syncthreads();
-            for (int k = threadIdx.x; k < s_ncell; k += blockDim.x) st_stream(A.cells + s_gbase + k, s_cells[k], stream_pol);
+            for (int k = threadIdx.x; k < s_ncell; k += blockDim.x) st_stream(A.cells + s_gbase + k, s_cells[k], keep_pol);
             __syncthreads();
             if (threadIdx.x == 0) {
                 s_start = next_start;
@@ -453,7 +470,7 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                 int slot = 0;
                 int2 ch = make_int2(-1, -1);
                 if (j < j1) {
-                    const int2 ent = ld_stream(A.cells + j, stream_pol);
+                    const int2 ent = ld_stream(A.cells + j, keep_pol);
                     const int32_t code = ent.x;
                     const uint32_t ltg = (uint32_t)ent.y;  // the trig of the decrement to 1
                     uint32_t tg = 0;
@@ -467,7 +484,7 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                         ch = make_fe(rs_last(rs), e2);
                     } else {
                         const int32_t u = code;
-                        const int4 va = __ldcg(reinterpret_cast<const int4*>(A.V + u));  // rs trig rm
+                        const int4 va = ld_stream4(reinterpret_cast<const int4*>(A.V + u), keep_pol);  // rs trig rm
                         const unsigned long long rs = ((unsigned long long)(uint32_t)va.y << 32) | (uint32_t)va.x;
                         const uint32_t code = (uint32_t)rs_last(rs);  // 2 e + filter of the one edge left
                         const int32_t e3 = (int32_t)(code >> 1);
@@ -482,7 +499,7 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                         want = false;
                     }
                 }
-                if (want) st_stream(A.child + 4 * i + slot, ch, stream_pol);
+                if (want) st_stream(A.child + 4 * i + slot, ch, keep_pol);
                 // children per phase-C warp range, one atomic per warp and range
                 const int64_t bi = want ? range_of(i) : -1;
                 const unsigned grp = __match_any_sync(0xffffffffu, bi);
@@ -528,7 +545,7 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
             unsigned msk = 0;
             if (i < w1) {
                 int4* sp = reinterpret_cast<int4*>(A.child + 4 * i);
-                const int4 s01 = ld_stream4(sp, stream_pol), s23 = ld_stream4(sp + 1, stream_pol);
+                const int4 s01 = ld_stream4(sp, keep_pol), s23 = ld_stream4(sp + 1, keep_pol);
                 cs[0] = make_int2(s01.x, s01.y);
                 cs[1] = make_int2(s01.z, s01.w);
                 cs[2] = make_int2(s23.x, s23.y);
@@ -536,8 +553,8 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
 #pragma unroll
                 for (int sl = 0; sl < 4; ++sl) msk |= cs[sl].y >= 0 ? (1u << sl) : 0u;
                 // empty the slots for the next generation
-                if (msk & 3u) st_stream4(sp, make_int4(-1, -1, -1, -1), stream_pol);
-                if (msk & 12u) st_stream4(sp + 1, make_int4(-1, -1, -1, -1), stream_pol);
+                if (msk & 3u) st_stream4(sp, make_int4(-1, -1, -1, -1), keep_pol);
+                if (msk & 12u) st_stream4(sp + 1, make_int4(-1, -1, -1, -1), keep_pol);
             }
             const int cnt = __popc(msk);
             const int inc = warp_inclusive_sum(cnt);
@@ -549,7 +566,7 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                 const int2 ch = cs[sl];
                 const int64_t slot = running + ex + k;
                 ++k;
-                st_stream(nxt + slot, ch, stream_pol);
+                st_stream(nxt + slot, ch, keep_pol);
                 const int32_t q = (int32_t)(nbase + slot);
                 if (is_fe(ch)) atomicMin(&A.F[idx0(ch)].rm, q);
                 else atomicMin(&A.EH[ch.x].rm, q);
