@@ -1298,47 +1298,86 @@ __device__ __forceinline__ void lattice_vertex(const VolTab& T, const Bases& B, 
 // vertex's coordinates from its lattice point, a kept edge's ends from its record,
 // a kept triangle's corners from the records of its first two sides (sides
 // (a,b), (b,c), (c,a) in face order: b is the vertex the first two share).
-__global__ void vd_rem_write_kernel(int32_t nv, int32_t ne, int32_t nt, Kept K, VolTab T, int nvol,
-                                    const uint32_t* __restrict__ vlat, const EdgeHead* __restrict__ E,
-                                    const FaceRec* __restrict__ F,
-                                    float* __restrict__ ovts, int2* __restrict__ oedges, int32_t* __restrict__ otris,
-                                    Bases B, int nmap) {
+// One warp per 32 consecutive survivor words (vertices, then edges, then
+// triangles, in one index space of words): the kept cells of those words are
+// handed out one per lane in index order, and lane r finds its cell's word by
+// a binary search over the warp's running counts and its bit by one over the
+// word's population counts, so every lane works on a kept cell.
+__device__ __forceinline__ int select_bit(uint32_t w, int k) {  // position of the k-th set bit (k < popc(w))
+    int p = 0;
+#pragma unroll
+    for (int s = 16; s >= 1; s >>= 1) {
+        const int c = __popc(w & ((1u << (p + s)) - 1u));  // set bits below p + s
+        if (c <= k) p += s;
+    }
+    return p;
+}
+__global__ void __launch_bounds__(256) vd_rem_write_kernel(int32_t nv, int32_t ne, int32_t nt, Kept K, VolTab T,
+                                                           int nvol, const uint32_t* __restrict__ vlat,
+                                                           const EdgeHead* __restrict__ E, const FaceRec* __restrict__ F,
+                                                           float* __restrict__ ovts, int2* __restrict__ oedges,
+                                                           int32_t* __restrict__ otris, Bases B, int nmap) {
+    const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
-    const uint32_t lowm = (1u << lane) - 1u;
     const int64_t nwv = ((int64_t)nv + 31) / 32, nwe = ((int64_t)ne + 31) / 32, nwf = ((int64_t)nt + 31) / 32;
     const int64_t nw = nwv + nwe + nwf;
+    const int64_t nchunk = (nw + 31) / 32;
     const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
-    for (int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < nw; w += warps) {
-        if (w < nwv) {
-            const uint32_t word = __ldg(K.bv + w);
-            if (!((word >> lane) & 1u)) continue;
-            const int64_t o = __ldg(K.pv + w) + __popc(word & lowm);
-            lattice_vertex(T, B, nvol, vlat, (int32_t)(w * 32 + lane), ovts + 3 * o);
-        } else if (w < nwv + nwe) {
-            const int64_t we = w - nwv;
-            const uint32_t word = __ldg(K.be + we);
-            if (!((word >> lane) & 1u)) continue;
-            const int4 er = __ldg(reinterpret_cast<const int4*>(E + we * 32 + lane));  // v0 v1 rm em
-            const int32_t sh = nmap > 1 ? (int32_t)B.b[kBRemV][find_base(B.b[kBVert], nmap, er.x)] : 0;
-            oedges[__ldg(K.pe + we) + __popc(word & lowm)] =
-                make_int2(kept_rank(K.bv, K.pv, er.x) - sh, kept_rank(K.bv, K.pv, er.y) - sh);
-        } else {
-            const int64_t wf = w - nwv - nwe;
-            const uint32_t word = __ldg(K.bf + wf);
-            if (!((word >> lane) & 1u)) continue;
-            const int64_t f = wf * 32 + lane;
-            const int64_t o = __ldg(K.pf + wf) + __popc(word & lowm);
-            const int4 fr = __ldg(reinterpret_cast<const int4*>(F + f));  // e0 e1 e2|pass rm
-            const int2 s0 = *reinterpret_cast<const int2*>(E + fr.x);
-            const int2 s1 = *reinterpret_cast<const int2*>(E + fr.y);
-            const int32_t vb_ = (s0.x == s1.x || s0.x == s1.y) ? s0.x : s0.y;
-            const int32_t va = s0.x == vb_ ? s0.y : s0.x;
-            const int32_t vc = s1.x == vb_ ? s1.y : s1.x;
-            const int32_t sh = nmap > 1 ? (int32_t)B.b[kBRemV][find_base(B.b[kBVert], nmap, va)] : 0;
-            // simpleTriangulate turns (a, b, c) into (c, a, b)
-            otris[3 * o + 0] = kept_rank(K.bv, K.pv, vc) - sh;
-            otris[3 * o + 1] = kept_rank(K.bv, K.pv, va) - sh;
-            otris[3 * o + 2] = kept_rank(K.bv, K.pv, vb_) - sh;
+    for (int64_t ch = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); ch < nchunk; ch += warps) {
+        // this lane's word and the kept cells before it in the chunk
+        const int64_t w = ch * 32 + lane;
+        uint32_t word = 0u;
+        if (w < nwv) word = __ldg(K.bv + w);
+        else if (w < nwv + nwe) word = __ldg(K.be + (w - nwv));
+        else if (w < nw) word = __ldg(K.bf + (w - nwv - nwe));
+        const int cnt = __popc(word);
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(full, incl, o);
+            if (lane >= o) incl += y;
+        }
+        const int total = __shfl_sync(full, incl, 31);
+        for (int base = 0; base < total; base += 32) {
+            const int r = base + lane;
+            // the lane L whose word holds kept cell r: the number of lanes with incl <= r
+            int L = 0;
+#pragma unroll
+            for (int s = 16; s >= 1; s >>= 1) {
+                const int y = __shfl_sync(full, incl, L + s - 1);
+                if (y <= r) L += s;
+            }
+            const uint32_t wordL = __shfl_sync(full, word, L & 31);
+            const int exclL = __shfl_sync(full, incl, L & 31) - __shfl_sync(full, cnt, L & 31);
+            if (r >= total) continue;
+            const int k = r - exclL;  // kept cells of word L before this one
+            const int bitp = select_bit(wordL, k);
+            const int64_t wl = ch * 32 + L;
+            if (wl < nwv) {
+                const int64_t o = __ldg(K.pv + wl) + k;
+                lattice_vertex(T, B, nvol, vlat, (int32_t)(wl * 32 + bitp), ovts + 3 * o);
+            } else if (wl < nwv + nwe) {
+                const int64_t we = wl - nwv;
+                const int4 er = __ldg(reinterpret_cast<const int4*>(E + we * 32 + bitp));  // v0 v1 rm em
+                const int32_t sh = nmap > 1 ? (int32_t)B.b[kBRemV][find_base(B.b[kBVert], nmap, er.x)] : 0;
+                oedges[__ldg(K.pe + we) + k] =
+                    make_int2(kept_rank(K.bv, K.pv, er.x) - sh, kept_rank(K.bv, K.pv, er.y) - sh);
+            } else {
+                const int64_t wf = wl - nwv - nwe;
+                const int64_t f = wf * 32 + bitp;
+                const int64_t o = __ldg(K.pf + wf) + k;
+                const int4 fr = __ldg(reinterpret_cast<const int4*>(F + f));  // e0 e1 e2|pass rm
+                const int2 s0 = *reinterpret_cast<const int2*>(E + fr.x);
+                const int2 s1 = *reinterpret_cast<const int2*>(E + fr.y);
+                const int32_t vb_ = (s0.x == s1.x || s0.x == s1.y) ? s0.x : s0.y;
+                const int32_t va = s0.x == vb_ ? s0.y : s0.x;
+                const int32_t vc = s1.x == vb_ ? s1.y : s1.x;
+                const int32_t sh = nmap > 1 ? (int32_t)B.b[kBRemV][find_base(B.b[kBVert], nmap, va)] : 0;
+                // simpleTriangulate turns (a, b, c) into (c, a, b)
+                otris[3 * o + 0] = kept_rank(K.bv, K.pv, vc) - sh;
+                otris[3 * o + 1] = kept_rank(K.bv, K.pv, va) - sh;
+                otris[3 * o + 2] = kept_rank(K.bv, K.pv, vb_) - sh;
+            }
         }
     }
 }
@@ -1348,7 +1387,7 @@ __global__ void vd_rem_write_kernel(int32_t nv, int32_t ne, int32_t nt, Kept K, 
 int lattice_rem_write(vc_ctx* c, const Kept& K, int nmap) {
     const int64_t nv = c->nv, ne = c->ne, nt = c->nt;
     const int64_t nw = (nv + 31) / 32 + (ne + 31) / 32 + (nt + 31) / 32;
-    vd_rem_write_kernel<<<cell_grid(c, 32 * nw), 256, 0, c->stream>>>(
+    vd_rem_write_kernel<<<cell_grid(c, nw), 256, 0, c->stream>>>(
         (int32_t)nv, (int32_t)ne, (int32_t)nt, K, c->tab, c->nvol, ptr<uint32_t>(c->vd_vlat),
         ptr<EdgeHead>(c->edge_rec), ptr<FaceRec>(c->face_rec), ptr<float>(c->rem_vts),
         ptr<int2>(c->rem_edges), ptr<int32_t>(c->rem_tris), c->bases, nmap);
