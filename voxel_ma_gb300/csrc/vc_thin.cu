@@ -227,27 +227,41 @@ __global__ void __launch_bounds__(kThreads) gen0_count_kernel(const int32_t* __r
     if (threadIdx.x == 0) sums[blockIdx.x] = tot;
 }
 
+// Each thread takes kG0Items consecutive codes of the tile (the tile's items
+// then come out in code order with one block scan) and writes their items
+// with the queue's evict-last policy (generation 0 reads them next).
 __global__ void __launch_bounds__(kThreads) gen0_write_kernel(ThinArgs A, int32_t ne, const int32_t* __restrict__ g0,
                                                               int64_t n, const int64_t* __restrict__ sums) {
+    static_assert(kG0Items == 8, "two 16-byte loads per thread");
     __shared__ int64_t sm[33];
-    const int64_t base = (int64_t)blockIdx.x * kG0Tile;
-    int64_t carry = sums[blockIdx.x];
+    const unsigned long long keep_pol = keep_policy();
+    const int64_t i0 = (int64_t)blockIdx.x * kG0Tile + (int64_t)threadIdx.x * kG0Items;
+    int32_t x[kG0Items];
+    if (i0 + kG0Items <= n) {
+        const int4 a = __ldcs(reinterpret_cast<const int4*>(g0 + i0));
+        const int4 b = __ldcs(reinterpret_cast<const int4*>(g0 + i0) + 1);
+        x[0] = a.x, x[1] = a.y, x[2] = a.z, x[3] = a.w, x[4] = b.x, x[5] = b.y, x[6] = b.z, x[7] = b.w;
+    } else {
+#pragma unroll
+        for (int r = 0; r < kG0Items; ++r) x[r] = i0 + r < n ? __ldcs(g0 + i0 + r) : -1;
+    }
+    int cnt = 0;
+#pragma unroll
+    for (int r = 0; r < kG0Items; ++r) cnt += x[r] >= 0 ? 1 : 0;
+    int64_t tot;
+    int64_t p = sums[blockIdx.x] + block_exclusive_sum<int64_t>(cnt, sm, &tot);
+#pragma unroll
     for (int r = 0; r < kG0Items; ++r) {
-        const int64_t i = base + (int64_t)r * kThreads + threadIdx.x;
-        const int32_t x = i < n ? __ldcs(g0 + i) : -1;
-        int64_t tot;
-        const int64_t ex = block_exclusive_sum<int64_t>(x >= 0 ? 1 : 0, sm, &tot);
-        if (x >= 0) {
-            const int32_t p = (int32_t)(carry + ex);
-            if (i < ne) {
-                A.qa[p] = make_fe(x, (int32_t)i);
-                atomicMin(&A.F[x].rm, p);
-            } else {
-                A.qa[p] = make_ev(x, (int32_t)(i - ne));
-                atomicMin(&A.EH[x].rm, p);
-            }
+        if (x[r] < 0) continue;
+        const int64_t i = i0 + r;
+        const int32_t q = (int32_t)p++;
+        if (i < ne) {
+            st_stream(A.qa + q, make_fe(x[r], (int32_t)i), keep_pol);
+            atomicMin(&A.F[x[r]].rm, q);
+        } else {
+            st_stream(A.qa + q, make_ev(x[r], (int32_t)(i - ne)), keep_pol);
+            atomicMin(&A.EH[x[r]].rm, q);
         }
-        carry += tot;
     }
 }
 
