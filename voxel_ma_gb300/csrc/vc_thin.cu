@@ -215,12 +215,15 @@ constexpr int64_t kG0Tile = (int64_t)kThreads * kG0Items;
 __global__ void __launch_bounds__(kThreads) gen0_count_kernel(const int32_t* __restrict__ g0, int64_t n,
                                                               int64_t* __restrict__ sums) {
     __shared__ int64_t sm[33];
-    const int64_t base = (int64_t)blockIdx.x * kG0Tile;
+    const int64_t i0 = (int64_t)blockIdx.x * kG0Tile + (int64_t)threadIdx.x * kG0Items;
     int64_t acc = 0;
-#pragma unroll
-    for (int r = 0; r < kG0Items; ++r) {
-        const int64_t i = base + (int64_t)r * kThreads + threadIdx.x;
-        if (i < n) acc += __ldcs(g0 + i) >= 0 ? 1 : 0;
+    if (i0 + kG0Items <= n) {
+        const int4 a = __ldcs(reinterpret_cast<const int4*>(g0 + i0));
+        const int4 b = __ldcs(reinterpret_cast<const int4*>(g0 + i0) + 1);
+        acc = (a.x >= 0) + (a.y >= 0) + (a.z >= 0) + (a.w >= 0) + (b.x >= 0) + (b.y >= 0) + (b.z >= 0) + (b.w >= 0);
+    } else {
+        for (int r = 0; r < kG0Items; ++r)
+            if (i0 + r < n) acc += __ldcs(g0 + i0 + r) >= 0 ? 1 : 0;
     }
     int64_t tot;
     block_exclusive_sum<int64_t>(acc, sm, &tot);

@@ -626,8 +626,10 @@ __global__ void __launch_bounds__(128, 5) vd_vertices_edges_kernel(VolTab T, Bas
             // the faces of the lattice edges from the point itself: with the
             // nine above they carry the plaquettes of the three axis edges
             // into the voxel (from -x, -y, -z)
-            const int32_t fx = face_at(R0, 0u, 0u, 0u, t, false, 0), fy = face_at(R0, 0u, 0u, 0u, t, false, 1),
-                          fz = face_at(R0, 0u, 0u, 0u, t, false, 2);
+            const bool hx = bt(Rm0.e0, t), hy = bt(R0m.e1, t), hz = bt((R0.e2 << 1) | (pe2 >> 31), t);
+            const int32_t fx = (hy || hz) ? face_at(R0, 0u, 0u, 0u, t, false, 0) : -1;
+            const int32_t fy = (hx || hz) ? face_at(R0, 0u, 0u, 0u, t, false, 1) : -1;
+            const int32_t fz = (hx || hy) ? face_at(R0, 0u, 0u, 0u, t, false, 2) : -1;
             // whether each of these faces passes the filter (read where the face exists)
             auto at_c = [&](const uint4& q, int ax) { return bt(ax == 0 ? q.x : (ax == 1 ? q.y : q.z), t) != 0; };
             auto at_c1 = [&](const uint4& q, const uint4& qn, int ax) {  // at c + 1
@@ -690,13 +692,13 @@ __global__ void __launch_bounds__(128, 5) vd_vertices_edges_kernel(VolTab T, Bas
                 auto passes4 = [&](int32_t f1, bool p1, int32_t f2, bool p2, int32_t f3, bool p3, int32_t f4, bool p4) {
                     return (f1 < 0 || p1) && (f2 < 0 || p2) && (f3 < 0 || p3) && (f4 < 0 || p4) && zero_passes;
                 };
-                if (bt(Rm0.e0, t))  // (a-1,b,c)+x: faces (a,b,c)+y, +z, (a,b,c+1)+y, (a,b+1,c)+z
+                if (hx)  // (a-1,b,c)+x: faces (a,b,c)+y, +z, (a,b,c+1)+y, (a,b+1,c)+z
                     add(Rm0.eb + pc3(Rm0.e0, Rm0.e1, Rm0.e2, m) + fbv,
                         passes4(fy, py, fz, pz, fid[8], pj[8], fid[4], pj[4]));
-                if (bt(R0m.e1, t))  // (a,b-1,c)+y: faces (a,b,c)+z, +x, (a+1,b,c)+z, (a,b,c+1)+x
+                if (hy)  // (a,b-1,c)+y: faces (a,b,c)+z, +x, (a+1,b,c)+z, (a,b,c+1)+x
                     add(R0m.eb + pc3(R0m.e0, R0m.e1, R0m.e2, m) + bt(R0m.e0, t) + fbv,
                         passes4(fz, pz, fx, px, fid[1], pj[1], fid[7], pj[7]));
-                if (bt((R0.e2 << 1) | (pe2 >> 31), t))  // (a,b,c-1)+z: the last axis edge before c; faces
+                if (hz)  // (a,b,c-1)+z: the last axis edge before c; faces
                     add(e_own - 1, passes4(fx, px, fy, py, fid[5], pj[5], fid[0], pj[0]));  // (a,b,c)+x, +y, (a,b+1,c)+x, (a+1,b,c)+y
                 {
                     int32_t e = e_own;
