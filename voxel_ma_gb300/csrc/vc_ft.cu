@@ -135,7 +135,7 @@ __device__ __forceinline__ void line_geom(const VolTab& T, int64_t gl, int& L, i
 // within kWinChunk of it) are in shared memory.  Positions outside the line
 // hold kWinNone, a packed value above every distance that stays exact when a
 // squared offset is added, so the scans need no bounds checks.  Warp w
-// computes points w, w + 8, ... of chunk k, lane j for line j: every global
+// computes points w, w + kWinWarps, ... of chunk k, lane j for line j: every global
 // access of a warp is contiguous and every shared-memory access is free of
 // bank conflicts.  The first kWinNear offsets on both sides are evaluated for
 // every point; a point whose best is still (kWinNear + 1)^2 or more goes to its warp's
@@ -150,7 +150,7 @@ constexpr int kWinLines = 32;
 constexpr int kWinChunk = 64;
 constexpr int kWinRing = 4 * kWinChunk;   // power of two: ring index = position & (kWinRing - 1)
 constexpr int kWinPitch = kWinRing + 1;   // odd pitch: line j's column starts at bank 2j
-constexpr int kWinThreads = 256;
+constexpr int kWinThreads = 512;  // 16 warps (8 and 32 measured slower at 512^3)
 constexpr int64_t kWinNone = ((int64_t)1 << 62) | 0xffffffffLL;  // distance 2^30, index -1
 constexpr int kWinWarps = kWinThreads / 32;
 constexpr int kWinQueue = 64;  // continuing points queued per warp
