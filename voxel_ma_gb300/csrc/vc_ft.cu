@@ -491,7 +491,7 @@ int run_ft(vc_ctx* c) {
             VC_CUDA(c, cudaFuncSetAttribute(ft_rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         const int64_t nrows = c->h_off[kLRow][nvol];
         int blocks = (int)std::min<int64_t>((nrows + warps_per_block - 1) / warps_per_block,
-                                            (int64_t)c->num_sms * 8);
+                                            (int64_t)c->num_sms * 16);  // as many as fit (0.54 -> 0.46 ms against 8 per SM)
         Region r(c, "ft_rows");
         ft_rows_kernel<<<blocks, warps_per_block * 32, smem, c->stream>>>(ptr<int32_t>(c->site_id_lat), A, c->tab,
                                                                           ncmax);
