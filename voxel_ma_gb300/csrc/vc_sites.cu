@@ -263,7 +263,8 @@ int run_sites(vc_ctx* c, int64_t* n_sites) {
     Region stage(c, "stage_sites");
     uint32_t* bits = ptr<uint32_t>(c->site_bits);
     int32_t* cnt = ptr<int32_t>(c->site_count);
-    const int wgrid = (int)std::max<int64_t>(1, std::min<int64_t>((nwords + 255) / 256, (int64_t)c->num_sms * 8));
+    // as many blocks as fit (the emission at 512^3: 0.72 -> 0.56 ms against 8 per SM)
+    const int wgrid = (int)std::max<int64_t>(1, std::min<int64_t>((nwords + 255) / 256, (int64_t)c->num_sms * 32));
     {
         Region r(c, "sites_count");
         sites_pack_kernel<<<(int)std::max<int64_t>(1, std::min<int64_t>((nrows + 7) / 8, (int64_t)c->num_sms * 16)),
