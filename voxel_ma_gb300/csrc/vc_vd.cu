@@ -1061,8 +1061,9 @@ __global__ void lambda_fp64_kernel(const int2* __restrict__ face_sites, const fl
     if (flips) atomicAdd(out + 1, flips);
 }
 
+// up to 64 blocks of 256 threads per SM (16 measured 0.025 ms slower on the remaining complex's write at 512^3)
 inline int cell_grid(vc_ctx* c, int64_t n) {
-    return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)c->num_sms * 16));
+    return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)c->num_sms * 64));
 }
 
 // Radius per vertex, VoroInfo::computeInfoRelatedtoSites
@@ -1124,9 +1125,12 @@ inline int seg_grid(vc_ctx* c, int64_t nseg) {
     return (int)std::max<int64_t>(1, std::min<int64_t>((nseg + kSegChunk - 1) / kSegChunk, (int64_t)c->num_sms * 16));
 }
 
-// 128-thread blocks, kRowChunk lattice rows per block at a time (grid-stride)
+// 128-thread blocks, one chunk of kRowChunk lattice rows per block (the loop is grid-stride past 2^20 blocks):
+// capping the grid at 16 or 32 blocks per SM left a tail (faces and vertex/edge kernels 0.73 / 0.29 ms longer at
+// 512^3)
 inline int row_grid(vc_ctx* c, int64_t nrow) {
-    return (int)std::max<int64_t>(1, std::min<int64_t>((nrow + kRowChunk - 1) / kRowChunk, (int64_t)c->num_sms * 16));
+    (void)c;
+    return (int)std::max<int64_t>(1, std::min<int64_t>((nrow + kRowChunk - 1) / kRowChunk, (int64_t)1 << 20));
 }
 
 }  // namespace
