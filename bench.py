@@ -488,6 +488,11 @@ def run_gpu(args):
         ctx.close()
         line["serving"] = run_serving(dev, args)
         line["config"]["serving_workload"] = line["serving"]["workload"]
+    if not args.no_1024 and world == 1:
+        ctx.close()
+        del occ_dev, occ_host
+        torch.cuda.empty_cache()
+        line["grf1024"] = run_grf1024(dev, args)
     if rank == 0 and not args.no_cpu_baseline:
         occ_s, sample = cpu_sample()
         times = [cpu_path_once(occ_s, args.t) for _ in range(2)]
@@ -802,6 +807,76 @@ CPU_SCALING_SIZES = (128, 256, 512)
 CPU_SCALING_WAIT_S = 480.0  # from the bench's start; sizes not done by then are reported unfinished
 
 
+def run_grf1024(dev, args):
+    """Configuration 3 at 1024^3: the plain path on the 1024^3 field (same
+    generator, sigma 6, seed 0; 1.07e9 voxels, a complex of about 4.2e9
+    cells), in a context of its own once every other leg has closed its
+    contexts.  Device-resident steps and end-to-end steps (host volume in,
+    remaining complex out) as in the headline; the site list and feature
+    transform of this volume are pinned to the oracle's digests and the rest
+    of the path by its properties in the GPU tests."""
+    import torch
+
+    from voxel_ma_gb300 import api, volumes
+
+    t0 = time.perf_counter()
+    occ_np = volumes.grf(1024, sigma=6.0, seed=0, device=dev)
+    gen_s = time.perf_counter() - t0
+    torch.cuda.empty_cache()  # the blur's temporaries
+    occ_dev = torch.from_numpy(occ_np).to(dev)
+    occ_host = torch.from_numpy(occ_np).pin_memory()
+    nvox = int(occ_np.size)
+    steps = max(1, min(args.steps, 3))
+    out = {"workload": "grf1024_sigma6_level0", "shape": list(occ_np.shape),
+           "occupancy_sha256": volumes.occupancy_sha256(occ_np), "generate_s": gen_s}
+    del occ_np
+    with api.Context(dev.index if dev.index is not None else 0) as ctx:
+        stream = ctx.torch_stream()
+        r = ctx.run_plain(occ_dev, args.t)  # allocations
+        r = ctx.run_plain(occ_dev, args.t)
+        torch.cuda.synchronize(dev)
+        ctx.sync()
+        ctx.set_timing(True)
+        ctx.reset_timings()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            r = ctx.run_plain(occ_dev, args.t)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ctx.sync()
+        ms = e0.elapsed_time(e1) / steps
+        timings = ctx.timings()
+        ctx.set_timing(False)
+        rem = r["rem"]
+        h_v = torch.empty((max(rem["nv"], 1), 3), dtype=torch.float32).pin_memory()
+        h_e = torch.empty((max(rem["ne"], 1), 2), dtype=torch.int32).pin_memory()
+        h_t = torch.empty((max(rem["nt"], 1), 3), dtype=torch.int32).pin_memory()
+        e0.record(stream)
+        for _ in range(steps):
+            rr = ctx.run_plain(occ_host, args.t)
+            q = rr["rem"]
+            ctx.remaining_arrays_into(h_v[: q["nv"]], h_e[: q["ne"]], h_t[: q["nt"]])
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        e2e_ms = e0.elapsed_time(e1) / steps
+        eu = ctx.euler_remaining()
+        vd = r["vd"]
+        out.update({
+            "value": nvox / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "steps": steps,
+            "e2e": {"value": nvox / (e2e_ms / 1e3), "unit": UNIT, "ms_per_step": e2e_ms,
+                    "h2d_bytes_per_step": nvox, "d2h_bytes_per_step": q["nv"] * 12 + q["ne"] * 8 + q["nt"] * 12},
+            "complex": {"sites": r["n_sites"], "V": vd["nv"], "E": vd["ne"], "T": vd["nt"], "thresh": r["thresh"],
+                        "generations": r["thin"]["generations"], "pushes": r["thin"]["pushes"],
+                        "processed": r["thin"]["processed"], "remaining": rem},
+            "euler_kept": eu["euler"] == vd["nv"] - vd["ne"] + vd["nt"],
+            "same_as_previous_step": rr == r,
+            "device_bytes": ctx.device_bytes(),
+            "region_ms_per_step": {k: v[0] / max(v[1], 1) for k, v in sorted(timings.items())},
+        })
+    return out
+
+
 def cpu_scaling_child(path: str, t: float) -> int:
     import oracle
     from voxel_ma_gb300 import volumes
@@ -860,6 +935,7 @@ def main():
     ap.add_argument("--ft-method", choices=["envelope", "window"], default=None,
                     help="with --no-tune: the feature transform's method for the plain path")
     ap.add_argument("--no-cpu-scaling", action="store_true", help="skip the CPU path's size-scaling points")
+    ap.add_argument("--no-1024", action="store_true", help="skip the 1024^3 field")
     ap.add_argument("--cpu-scaling-child", default=None, help=argparse.SUPPRESS)
     args = ap.parse_args()
     if args.cpu_scaling_child:

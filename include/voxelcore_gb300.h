@@ -451,6 +451,14 @@ int vc_debug_set_spin_limit(vc_ctx* ctx, unsigned long long polls);
  * fails, as cudaMallocAsync failing would (VC_ERR_OOM); k < 0 switches it
  * off.  The context stays usable after the failure.                       */
 int vc_debug_fail_alloc_after(vc_ctx* ctx, int64_t k);
+/* The thinning queue: `capacity` > 0 caps the items one generation may hold
+ * (0 = library default: V + E + 1, or the room the device has left when that
+ * does not fit), and the queue positions start at `first_position` instead
+ * of 0 (positions are unsigned 32-bit; VC_ERR_ARG when first_position + V +
+ * E + 1 passes 2^32 - 1).  Results do not depend on either while the largest
+ * generation fits; a generation larger than the capacity ends vc_thin with
+ * VC_ERR_OOM and the context stays usable.                                */
+int vc_debug_thin_queue(vc_ctx* ctx, int64_t capacity, uint32_t first_position);
 /* A broken reference count: the next thinnings raise (delta = +1) or lower
  * (-1) vertex `vertex`'s count of incident edges by one after its record is
  * built (delta = 0 switches it off).  An edge-vertex pair popped for that

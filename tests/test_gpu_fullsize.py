@@ -1,6 +1,7 @@
 """The full-size workloads, bit for bit: the 64^3 torus, the 32-sphere unions at
 256^3 (seeds 0, 1, 2) and the 512^3 thresholded random field that the
-benchmark times; at 1024^3, the sites and the feature transform.
+benchmark times; at 1024^3, the sites and the feature transform (the rest of
+the path there by its properties).
 
 The CPU oracle's outputs at these sizes take minutes and tens of GB of host
 memory, so tests/golden/make_fullsize_digests.py ran it once and committed
@@ -70,21 +71,38 @@ def grf512():
 
 
 @pytest.mark.parametrize("name", FT_ONLY)
-def test_sites_and_transform_at_1024(name):
-    """The 1024^3 field (1.08e9 lattice points, 1.3e8 sites): site list and
-    feature transform bit for bit.  Its complex (about 2.5e9 cells) exceeds
-    32-bit cell ids and one GPU's memory, so the path stops there."""
+def test_full_path_at_1024(name):
+    """The 1024^3 field (1.08e9 lattice points, 1.24e8 sites; a complex of
+    about 5e8 vertices, 2.1e9 edges and 1.6e9 triangles).  Site list and
+    feature transform bit for bit against the oracle's digests; the oracle's
+    complex at this size does not fit the host it ran on, so the rest is
+    checked by properties: the queue positions pass 2^31 (V + E > 2^31), the
+    processed pairs are the pushes less the skips, simple-pair collapses keep
+    the Euler characteristic, and a second run gives the same thinning and
+    the same remaining complex.  (The same kernels are pinned to the oracle
+    at 512^3 above, and with positions above 2^31 and the queue capacity at
+    its limit in test_gpu_thin_queue.py.)"""
+    import torch
     from voxel_ma_gb300 import api
     d = DIGESTS[name]
     occ = _volume(name)
     assert volumes.occupancy_sha256(occ) == d["occupancy_sha256"]
+    torch.cuda.empty_cache()  # the field's blur temporaries
     with api.Context(0) as ctx:
-        ctx.set_volume(occ)
-        del occ
-        assert ctx.extract_sites() == d["n_sites"]
+        r = ctx.run_plain(occ, 0.04)
+        assert r["n_sites"] == d["n_sites"]
         assert _digest(ctx.sites()) == d["sites"]
-        ctx.feature_transform()
         assert _digest(*ctx.ft()) == d["ft"]
+        vd = r["vd"]
+        assert vd["nv"] + vd["ne"] > 2**31, vd
+        th = r["thin"]
+        assert th["pushes"] - th["skipped"] == th["processed"] > 0
+        eu = ctx.euler_remaining()
+        assert eu["euler"] == vd["nv"] - vd["ne"] + vd["nt"], (eu, vd)
+        first = _digest(*ctx.remaining_arrays())
+        r2 = ctx.run_plain(occ, 0.04)
+        assert r2 == r
+        assert _digest(*ctx.remaining_arrays()) == first
 
 
 @pytest.mark.parametrize("name", FULL)

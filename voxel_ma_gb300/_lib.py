@@ -135,6 +135,7 @@ SIGNATURES = {
     "vc_debug_set_spin_limit": (c_int, [c_vp, ctypes.c_ulonglong]),
     "vc_debug_fail_alloc_after": (c_int, [c_vp, c_i64]),
     "vc_debug_ref_bias": (c_int, [c_vp, c_i64, c_int]),
+    "vc_debug_thin_queue": (c_int, [c_vp, c_i64, ctypes.c_uint32]),
     "vc_autotune": (c_int, [c_vp, ctypes.c_double, ctypes.POINTER(TuneResult)]),
     "vc_lambda_fp64_check": (c_int, [c_vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(c_i64)]),
     "vc_run_plain": (c_int, [c_vp, c_vp, c_int, c_int, c_int, c_int, ctypes.c_double, ctypes.POINTER(PlainResult)]),

@@ -173,6 +173,11 @@ class Context:
         """Raise (+1) or lower (-1) one vertex's thinning count after its record is built (0: off)."""
         self.check(self.lib.vc_debug_ref_bias(self.h, vertex, delta), "vc_debug_ref_bias")
 
+    def debug_thin_queue(self, capacity: int = 0, first_position: int = 0):
+        """Cap the thinning queue at `capacity` items per generation (0 = default) and start its positions at
+        `first_position`; results are the same while the largest generation fits, else vc_thin fails (OOM)."""
+        self.check(self.lib.vc_debug_thin_queue(self.h, capacity, first_position), "vc_debug_thin_queue")
+
     def debug_ft_wide(self, wide: bool = True):
         """Force 64-bit arithmetic in the feature transform (identical results)."""
         self.check(self.lib.vc_debug_ft_wide(self.h, 1 if wide else 0), "vc_debug_ft_wide")

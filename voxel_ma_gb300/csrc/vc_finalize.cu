@@ -169,6 +169,7 @@ inline int grid_for(vc_ctx* c, int64_t n, int threads) {
 // Build V->E and E->F lists of the context's finalized edges / tri_edges.
 int build_adjacency(vc_ctx* c) {
     const int64_t nv = c->nv, ne = c->ne, nt = c->nt;
+    if (2 * ne >= INT32_MAX || 3 * nt >= INT32_MAX) return VC_ERR_ARG;  // 32-bit list offsets
     Region stage(c, "adjacency");
     VC_TRY(ensure_n<int32_t>(c, c->ve_off, nv + 1));
     VC_TRY(ensure_n<int32_t>(c, c->ve_ids, 2 * ne));

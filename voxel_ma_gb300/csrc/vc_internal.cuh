@@ -51,19 +51,24 @@ T* ptr(const DevBuf& b) {
 // item removing the edge reads) and its count (what a decrement and the child
 // step touch), kept in two arrays, so that the sector a random touch brings
 // in holds the same piece of the neighbouring edge (ids follow the lattice).
-constexpr int32_t kAlive = INT32_MAX;  // removal position of a cell still present
+// Removal state of a face or an edge: the queue position of the item that
+// removed it (kAlive while it is present).  Positions are unsigned 32-bit:
+// a thinning pushes at most one item per vertex and edge, so they stay
+// below V + E < 2^32 - 1.
+constexpr uint32_t kAlive = 0xFFFFFFFFu;
 // An edge's faces (a vertex's edges) still present, as one 64-bit word: their
 // count in bits 0-15, how many of them pass the thinning filter (measure
 // below threshold) in bits 16-31, and the sum of their ids (mod 2^32) in
 // bits 32-63.  Removing incident cell x subtracts (x << 32) + (pass << 16) +
 // 1 in one atomic; when the count is 1 the sum is the id of the one cell
 // left and the pass field says whether it passes the filter.  Vertex words
-// leave the pass field at zero and sum 2 e + p over their edges e instead of
-// e (p = 1 when edge e passes the filter, its measure below the edge
-// threshold): when the count is 1 the sum is the one edge left, shifted up
-// one bit, with its filter in bit 0.
+// sum 2 e + p over their edges e instead of e (p = 1 when edge e passes the
+// filter, its measure below the edge threshold): when the count is 1 the sum
+// is the one edge left, shifted up one bit, with its filter in bit 0; their
+// pass field is 1 (kVertGone) once the vertex is removed.
 constexpr int kRefBits = 16;
 constexpr unsigned long long kRefMask = (1ull << kRefBits) - 1ull;  // largest incidence count
+constexpr unsigned long long kVertGone = 1ull << kRefBits;          // vertex word: the vertex was removed
 __host__ __device__ __forceinline__ unsigned long long rs_make(unsigned long long count, unsigned long long pass,
                                                                unsigned long long id_sum) {
     return (id_sum << 32) | ((pass & kRefMask) << 16) | count;
@@ -74,29 +79,25 @@ __host__ __device__ __forceinline__ unsigned long long rs_drop(int32_t id, unsig
 __host__ __device__ __forceinline__ int32_t rs_count(unsigned long long w) { return (int32_t)(w & kRefMask); }
 __host__ __device__ __forceinline__ int32_t rs_pass(unsigned long long w) { return (int32_t)((w >> 16) & kRefMask); }
 __host__ __device__ __forceinline__ int32_t rs_last(unsigned long long w) { return (int32_t)(uint32_t)(w >> 32); }
-// trig: the last decrement of a generation, as (queue position << 1 | bit),
-// bit = which of the decrementing item's cells of that kind this is: for an
-// edge, the first or second of the face's other sides (child slot 0 or 1);
-// for a vertex, the first or second end of the removed edge (child slot 2 or
-// 3).  Queue positions stay below 2^31, so the word fits 32 bits.
-__host__ __device__ __forceinline__ uint32_t trig_make(int32_t pos, int bit) {
-    return ((uint32_t)pos << 1) | (uint32_t)bit;
-}
+// trig: the last decrement of a generation, as (queue position << 1 | bit)
+// in 64 bits, bit = which of the decrementing item's cells of that kind this
+// is: for an edge, the first or second of the face's other sides (child slot
+// 0 or 1); for a vertex, the first or second end of the removed edge (child
+// slot 2 or 3).
 constexpr int32_t kFacePass = (int32_t)0x80000000u;  // FaceRec::e2 bit: the face passes the filter
 struct __align__(16) FaceRec {
     int32_t e0, e1;  // edge ids of the sides, in face order
     int32_t e2;      // third side; bit 31 (kFacePass): measure below the face threshold
-    int32_t rm;
+    uint32_t rm;
 };
 struct __align__(16) EdgeHead {  // ends, removal position, measure
     int32_t v0, v1;
-    int32_t rm;
+    uint32_t rm;
     float em;
 };
 struct __align__(16) EdgeCnt {  // faces still present (count | pass | id sum), last decrement
     unsigned long long rs;
-    uint32_t trig;
-    int32_t pad;
+    unsigned long long trig;
 };
 // The edge records of a complex of ne edges: ne heads, then ne counts, in
 // one buffer of 32 bytes per edge.
@@ -105,9 +106,8 @@ struct EdgeRecs {
     EdgeCnt* n = nullptr;
 };
 struct __align__(16) VertRec {
-    unsigned long long rs;  // edges still present: count | 0 | id sum
-    uint32_t trig;          // last decrement: position << 1 | end bit
-    int32_t rm;
+    unsigned long long rs;    // edges still present: count | kVertGone once removed | id sum
+    unsigned long long trig;  // last decrement: position << 1 | end bit
 };
 static_assert(sizeof(FaceRec) == 16 && sizeof(EdgeHead) == 16 && sizeof(EdgeCnt) == 16 && sizeof(VertRec) == 16,
               "record size");
@@ -287,6 +287,8 @@ struct vc_ctx {
     std::mutex* thin_lock = nullptr;  // shared by contexts whose thinning kernels must not overlap
     // failure injection (host side; the kernels only see ordinary inputs)
     unsigned long long spin_limit = 1ull << 26;  // polls before a grid barrier gives up (VC_ERR_TIMEOUT)
+    int64_t thin_qcap = 0;          // > 0: the thinning queue's capacity (items per generation)
+    uint32_t thin_pos0 = 0;         // queue position of the thinning's first item
     int64_t fail_alloc_after = -1;  // >= 0: that many more device allocations succeed, the next fails
     int64_t ref_bias_vertex = -1;   // >= 0: this vertex's thinning count is raised by ref_bias after
     int ref_bias = 0;               //   its record is built (a broken reference count)

@@ -35,15 +35,16 @@
 //                 its last-decrement position, in the cell's slot;
 //   C (per item)  children are written in order as generation g+1 and that
 //                 generation's claims are made.
-// Removal state is the queue position of the removing item (INT32_MAX =
-// alive), so every check is position-exact.
+// Removal state is the queue position of the removing item (unsigned
+// 32-bit, kAlive = 2^32 - 1 while present), so every check is
+// position-exact.
 //
 // Memory layout: the accesses are random and cost per request, so every
 // cell's static data and thinning state share one record, and each phase
 // reads what it needs about a cell with one 16-byte load:
 //   face   {e0, e1, e2 | pass bit, rm}                  16 B
-//   edge   {v0, v1, rm, em} {rs, trig, -}               32 B
-//   vertex {rs, trig, rm}                               16 B
+//   edge   {v0, v1, rm, em} {rs, trig}                  32 B
+//   vertex {rs (with a removed bit), trig}              16 B
 // Phase A reads a face record and an edge's head (FE) or a vertex record and
 // an edge's head (EV); the decrements and phase B touch an edge's count or a
 // vertex record.
@@ -83,6 +84,8 @@ struct ThinArgs {
     unsigned long long spin_limit;
     int64_t* trace;  // optional: per generation {items, t_A, t_B, t_C} (global timer, ns)
     int trace_cap;
+    int64_t qcap;   // items one generation may hold (qa, qb; 4 child slots and 4 list entries per item)
+    uint32_t pos0;  // queue position of the first item of generation 0
 };
 
 __device__ __forceinline__ int64_t global_ns() {
@@ -134,11 +137,11 @@ __device__ __forceinline__ unsigned long long atom_add_keep(unsigned long long* 
     asm volatile("atom.global.add.L2::cache_hint.u64 %0, [%1], %2, %3;" : "=l"(old) : "l"(a), "l"(v), "l"(pol) : "memory");
     return old;
 }
-__device__ __forceinline__ void red_max_keep(uint32_t* a, uint32_t v, unsigned long long pol) {
-    asm volatile("red.global.max.L2::cache_hint.u32 [%0], %1, %2;" ::"l"(a), "r"(v), "l"(pol) : "memory");
+__device__ __forceinline__ void red_max_keep(unsigned long long* a, unsigned long long v, unsigned long long pol) {
+    asm volatile("red.global.max.L2::cache_hint.u64 [%0], %1, %2;" ::"l"(a), "l"(v), "l"(pol) : "memory");
 }
-__device__ __forceinline__ void st_keep(int32_t* a, int32_t v, unsigned long long pol) {
-    asm volatile("st.global.cg.L2::cache_hint.s32 [%0], %1, %2;" ::"l"(a), "r"(v), "l"(pol) : "memory");
+__device__ __forceinline__ void red_or_keep(unsigned long long* a, unsigned long long v, unsigned long long pol) {
+    asm volatile("red.global.or.L2::cache_hint.b64 [%0], %1, %2;" ::"l"(a), "l"(v), "l"(pol) : "memory");
 }
 __device__ __forceinline__ void st_stream4(int4* a, int4 v, unsigned long long pol) {
     asm volatile("st.global.cg.L2::cache_hint.v4.s32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(a), "r"(v.x), "r"(v.y),
@@ -182,7 +185,7 @@ __global__ void build_records_kernel(const int2* __restrict__ edges, const int32
             if ((unsigned long long)(o1 - o0) > kRefMask) set_error(err, VC_ERR_ARG);
             const int2 ev = edges[e];
             E.h[e] = EdgeHead{ev.x, ev.y, kAlive, all_pass ? 0.0f : em[e]};
-            E.n[e] = EdgeCnt{rs_make((unsigned)(o1 - o0), pass, idsum), 0u, 0};
+            E.n[e] = EdgeCnt{rs_make((unsigned)(o1 - o0), pass, idsum), 0ull};
             g0[e] = (o1 - o0 == 1 && pass == 1) ? (int32_t)idsum : -1;
         } else {
             const int64_t v = i - nt - ne;
@@ -196,7 +199,6 @@ __global__ void build_records_kernel(const int2* __restrict__ edges, const int32
             VertRec r;
             r.rs = rs_make((unsigned)(o1 - o0), 0, idsum);
             r.trig = 0;
-            r.rm = kAlive;
             V[v] = r;
             g0[(int64_t)ne + v] = (o1 - o0 == 1 && (idsum & 1u)) ? (int32_t)(idsum >> 1) : -1;
         }
@@ -232,7 +234,8 @@ __global__ void __launch_bounds__(kThreads) gen0_count_kernel(const int32_t* __r
 
 // Each thread takes kG0Items consecutive codes of the tile (the tile's items
 // then come out in code order with one block scan) and writes their items
-// with the queue's evict-last policy (generation 0 reads them next).
+// with the queue's evict-last policy (generation 0 reads them next); an item
+// beyond the queue's capacity is not written (VC_ERR_OOM).
 __global__ void __launch_bounds__(kThreads) gen0_write_kernel(ThinArgs A, int32_t ne, const int32_t* __restrict__ g0,
                                                               int64_t n, const int64_t* __restrict__ sums) {
     static_assert(kG0Items == 8, "two 16-byte loads per thread");
@@ -256,13 +259,17 @@ __global__ void __launch_bounds__(kThreads) gen0_write_kernel(ThinArgs A, int32_
 #pragma unroll
     for (int r = 0; r < kG0Items; ++r) {
         if (x[r] < 0) continue;
-        const int64_t i = i0 + r;
-        const int32_t q = (int32_t)p++;
+        const int64_t i = i0 + r, li = p++;
+        if (li >= A.qcap) {
+            set_error(A.err, VC_ERR_OOM);
+            continue;
+        }
+        const uint32_t q = A.pos0 + (uint32_t)li;
         if (i < ne) {
-            st_stream(A.qa + q, make_fe(x[r], (int32_t)i), keep_pol);
+            st_stream(A.qa + li, make_fe(x[r], (int32_t)i), keep_pol);
             atomicMin(&A.F[x[r]].rm, q);
         } else {
-            st_stream(A.qa + q, make_ev(x[r], (int32_t)(i - ne)), keep_pol);
+            st_stream(A.qa + li, make_ev(x[r], (int32_t)(i - ne)), keep_pol);
             atomicMin(&A.EH[x[r]].rm, q);
         }
     }
@@ -299,7 +306,8 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
     const int G = gridDim.x, b = blockIdx.x;
     const float l_t = A.thr[1];
     int64_t n = A.ctl[0];
-    int64_t base = 0, pushes = n;
+    int64_t base = A.pos0, pushes = n;
+    if (n > A.qcap) n = 0;  // generation 0 did not fit the queue (VC_ERR_OOM is set)
     int gen = 0;
     int64_t my_processed = 0, my_skipped = 0;
     int64_t slots_ready = 0;  // child slots [0, 4 slots_ready) hold {-1, -1} or this generation's children
@@ -321,6 +329,9 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
             return bi * W + (i - bi * chunk) / wchunk;
         };
         int* ctr = A.counters + 4 * par;  // [0] list length, [1] phase-A cursor
+        // trigs are absolute positions (64-bit); per item and in the cell
+        // list they are kept relative to the generation's first position
+        const unsigned long long tb2 = (unsigned long long)base << 1;
         const int64_t i0 = min(n, (int64_t)b * chunk), i1 = min(n, i0 + chunk);
         const bool tr = A.trace && b == 0 && threadIdx.x == 0 && gen < A.trace_cap;
         if (tr) {
@@ -373,8 +384,8 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                 ea[k] = __ldcg(reinterpret_cast<const int4*>(A.EH + e));
             }
             int32_t one[4 * ITEMS];  // cells whose count fell to 1 here
-            int32_t dec[4 * ITEMS];  // cells decremented here (kEdgeBit: edge) and this item's trig there,
-            uint32_t dtg[4 * ITEMS];  // recorded once the decrements have come back (measured faster)
+            int32_t dec[4 * ITEMS];  // cells decremented here (kEdgeBit: edge) and this item's trig there
+            uint32_t dtg[4 * ITEMS];  // (relative), recorded once the decrements have come back (measured faster)
 #pragma unroll
             for (int q = 0; q < 4 * ITEMS; ++q) one[q] = dec[q] = -1;
             // a decrement that took the count to 1 or 0 raises no trig
@@ -384,13 +395,15 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
 #pragma unroll
             for (int k = 0; k < ITEMS; ++k) {
                 if (!has[k]) continue;
-                const int32_t p = (int32_t)(base + r0 + threadIdx.x + (int64_t)k * blockDim.x);
+                const int64_t li = r0 + threadIdx.x + (int64_t)k * blockDim.x;  // index in the generation
+                const uint32_t p = (uint32_t)(base + li);                        // queue position
+                const uint32_t lt = (uint32_t)li << 1;                           // relative trig, bit 0
                 if (is_fe(it[k])) {
                     // the edge of an FE item has exactly one face, the item's:
                     // its count fell to 1 once, and only removing that face
                     // lowers it further
                     const int32_t f = idx0(it[k]), e = it[k].y;
-                    const int32_t frm = ra[k].w;  // FaceRec: e0 e1 e2|pass rm
+                    const uint32_t frm = (uint32_t)ra[k].w;  // FaceRec: e0 e1 e2|pass rm
                     if (frm != p) {
                         ++my_skipped;
                     } else {
@@ -415,8 +428,8 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                         dec[4 * k + 1] = sb | kEdgeBit;
                         dec[4 * k + 2] = v0;
                         dec[4 * k + 3] = v1;
-                        dtg[4 * k + 0] = dtg[4 * k + 2] = trig_make(p, 0);
-                        dtg[4 * k + 1] = dtg[4 * k + 3] = trig_make(p, 1);
+                        dtg[4 * k + 0] = dtg[4 * k + 2] = lt;
+                        dtg[4 * k + 1] = dtg[4 * k + 3] = lt | 1u;
                         if (oa == 2) one[4 * k + 0] = sa | kEdgeBit;
                         if (ob == 2) one[4 * k + 1] = sb | kEdgeBit;
                         if (o0 == 2) one[4 * k + 2] = v0;
@@ -428,7 +441,7 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                     }
                 } else {
                     const int32_t e = it[k].x, v = it[k].y;
-                    const int32_t erm = ea[k].z;  // EdgeHead: v0 v1 rm em
+                    const uint32_t erm = (uint32_t)ea[k].z;  // EdgeHead: v0 v1 rm em
                     const int32_t vref =
                         rs_count(((unsigned long long)(uint32_t)ra[k].y << 32) | (uint32_t)ra[k].x);  // VertRec: rs trig rm
                     if (erm != p) {
@@ -437,8 +450,8 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                         set_error(A.err, VC_ERR_INVARIANT);
                     } else {
                         ++my_processed;
-                        // nothing else touches v in this generation (its one edge is e)
-                        st_keep(&A.V[v].rm, p, keep_pol);
+                        // v's one edge is e: no later decrement meets v's word
+                        red_or_keep(&A.V[v].rs, kVertGone, keep_pol);
                         const int32_t v0 = ea[k].x, v1 = ea[k].y;
                         const int32_t u = v0 != v ? v0 : v1;
                         const unsigned epass = __int_as_float(ea[k].w) < l_t ? 1u : 0u;
@@ -446,7 +459,7 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                             rs_count(atom_add_keep(&A.V[u].rs, rs_drop((int32_t)(2u * (unsigned)e + epass), 0u), keep_pol));
                         if (ou == 2) one[4 * k + 2] = u;
                         dec[4 * k + 2] = u;
-                        dtg[4 * k + 2] = trig_make(p, 0);
+                        dtg[4 * k + 2] = lt;
                         keep_dec(4 * k + 2, ou);
                     }
                 }
@@ -457,8 +470,8 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
 #pragma unroll
             for (int q = 0; q < 4 * ITEMS; ++q) {
                 if (dec[q] == -1) continue;
-                if (dec[q] & kEdgeBit) atomicMax(&A.EN[dec[q] & ~kEdgeBit].trig, dtg[q]);
-                else red_max_keep(&A.V[dec[q]].trig, dtg[q], keep_pol);
+                if (dec[q] & kEdgeBit) atomicMax(&A.EN[dec[q] & ~kEdgeBit].trig, tb2 + dtg[q]);
+                else red_max_keep(&A.V[dec[q]].trig, tb2 + dtg[q], keep_pol);
             }
             __syncthreads();
             if (threadIdx.x == 0) s_gbase = s_ncell ? atomicAdd(ctr + 0, s_ncell) : 0;
@@ -489,24 +502,24 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                 if (j < j1) {
                     const int2 ent = ld_stream(A.cells + j, keep_pol);
                     const int32_t code = ent.x;
-                    const uint32_t ltg = (uint32_t)ent.y;  // the trig of the decrement to 1
-                    uint32_t tg = 0;
+                    const unsigned long long ltg = tb2 + (uint32_t)ent.y;  // the trig of the decrement to 1
+                    unsigned long long tg = 0;
                     if (code & kEdgeBit) {
                         const int32_t e2 = code & ~kEdgeBit;
-                        const int4 eb = __ldcg(reinterpret_cast<const int4*>(A.EN + e2));  // rs trig -
+                        const int4 eb = __ldcg(reinterpret_cast<const int4*>(A.EN + e2));  // rs trig
                         const unsigned long long rs = ((unsigned long long)(uint32_t)eb.y << 32) | (uint32_t)eb.x;
                         want = rs_count(rs) == 1 && rs_pass(rs) == 1;
-                        tg = max((uint32_t)eb.z, ltg);
+                        tg = max(((unsigned long long)(uint32_t)eb.w << 32) | (uint32_t)eb.z, ltg);
                         slot = (int)(tg & 1u);
                         ch = make_fe(rs_last(rs), e2);
                     } else {
                         const int32_t u = code;
-                        const int4 va = ld_stream4(reinterpret_cast<const int4*>(A.V + u), keep_pol);  // rs trig rm
+                        const int4 va = ld_stream4(reinterpret_cast<const int4*>(A.V + u), keep_pol);  // rs trig
                         const unsigned long long rs = ((unsigned long long)(uint32_t)va.y << 32) | (uint32_t)va.x;
                         const uint32_t code = (uint32_t)rs_last(rs);  // 2 e + filter of the one edge left
                         const int32_t e3 = (int32_t)(code >> 1);
                         want = rs_count(rs) == 1 && (code & 1u);
-                        tg = max((uint32_t)va.z, ltg);
+                        tg = max(((unsigned long long)(uint32_t)va.w << 32) | (uint32_t)va.z, ltg);
                         slot = 2 + (int)(tg & 1u);
                         ch = make_ev(e3, u);
                     }
@@ -553,6 +566,10 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
         }
         const int64_t total = s_red[1];
         const int64_t nbase = base + n;
+        if (total > A.qcap) {  // every block sees the same total and leaves here
+            if (b == 0 && threadIdx.x == 0) set_error(A.err, VC_ERR_OOM);
+            break;
+        }
         const int wid = threadIdx.x >> 5;
         int64_t running = s_red[0] + s_wpre[wid];
         const int64_t w0 = min(i1, i0 + (int64_t)wid * wchunk), w1 = min(i1, w0 + wchunk);
@@ -584,7 +601,7 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
                 const int64_t slot = running + ex + k;
                 ++k;
                 st_stream(nxt + slot, ch, keep_pol);
-                const int32_t q = (int32_t)(nbase + slot);
+                const uint32_t q = (uint32_t)(nbase + slot);
                 if (is_fe(ch)) atomicMin(&A.F[idx0(ch)].rm, q);
                 else atomicMin(&A.EH[ch.x].rm, q);
             }
@@ -642,15 +659,16 @@ __global__ void export_flags_kernel(const FaceRec* __restrict__ F, const EdgeHea
         if (w < nwv) {
             const int64_t i = w * 32 + lane;
             if (i < nv) {
-                keep = __ldcs(&V[i].rm) == kAlive;
+                keep = !(__ldcs(&V[i].rs) & kVertGone);
                 kv[i] = keep;
             }
         } else if (w < nwv + nwe) {
             const int64_t e = (w - nwv) * 32 + lane;
             if (e < ne) {
                 const int4 ea = __ldcs(reinterpret_cast<const int4*>(EH + e));  // v0 v1 rm em
-                const int4 eb = __ldcs(reinterpret_cast<const int4*>(EN + e));  // rs trig -
-                const int32_t rm = ea.z, ref = rs_count(((unsigned long long)(uint32_t)eb.y << 32) | (uint32_t)eb.x);
+                const int4 eb = __ldcs(reinterpret_cast<const int4*>(EN + e));  // rs trig
+                const uint32_t rm = (uint32_t)ea.z;
+                const int32_t ref = rs_count(((unsigned long long)(uint32_t)eb.y << 32) | (uint32_t)eb.x);
                 keep = rm == kAlive && ref == 0;
                 ke[e] = keep;
                 re[e] = rm != kAlive;
@@ -675,6 +693,34 @@ __global__ void export_flags_kernel(const FaceRec* __restrict__ F, const EdgeHea
 inline int grid_for(vc_ctx* c, int64_t n, int threads) {
     int64_t b = (n + threads - 1) / threads;
     return (int)std::max<int64_t>(1, std::min<int64_t>(b, (int64_t)c->num_sms * 16));
+}
+
+// Bytes of queue per item of capacity: two item arrays (generations g and
+// g + 1), four child slots and four cell-list entries.
+constexpr int64_t kQueueBytes = 2 * (int64_t)sizeof(int2) + 4 * (int64_t)sizeof(int2) + 4 * (int64_t)sizeof(int2);
+// A generation's cell list (four entries per item) has a 32-bit length.
+constexpr int64_t kMaxQueue = ((int64_t)1 << 29) - 1;
+// Device memory left for the queue at most: free memory, free memory of the
+// default stream-ordered pool (the context's buffers live there) and what
+// the queue buffers hold already, less a reserve for the rest of the call.
+int64_t queue_room(vc_ctx* c) {
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    int64_t room = (int64_t)fr;
+    cudaMemPool_t pool;
+    uint64_t reserved = 0, used = 0;
+    if (cudaDeviceGetDefaultMemPool(&pool, c->device) != cudaSuccess ||
+        cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &reserved) != cudaSuccess ||
+        cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &used) != cudaSuccess) {
+        cudaGetLastError();
+        reserved = used = 0;
+    }
+    if (reserved > used) room += (int64_t)(reserved - used);
+    room += (int64_t)(c->q0.cap + c->q1.cap + c->child.cap + c->cells.cap);
+    return room - ((int64_t)2 << 30);
 }
 
 }  // namespace
@@ -726,8 +772,10 @@ int run_thin_all_pass(vc_ctx* c, vc_thin_stats* stats) {
 int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats, bool all_pass) {
     if (!c->cc_finalized || (!all_pass && !c->meas_valid)) return VC_ERR_STATE;
     const int64_t nv = c->nv, ne = c->ne, nt = c->nt;
-    if (nv + ne >= INT32_MAX || nt >= INT32_MAX) return VC_ERR_ARG;
-    const int64_t qcap = nv + ne + 1;
+    // ids are 31-bit (items and lists tag them with bit 31); queue positions
+    // are 32-bit: a thinning pushes at most one item per vertex and edge
+    if (nv >= INT32_MAX || ne >= INT32_MAX || nt >= INT32_MAX) return VC_ERR_ARG;
+    if ((int64_t)c->thin_pos0 + nv + ne + 1 >= (int64_t)kAlive) return VC_ERR_ARG;
     Region stage(c, "stage_thin");
     if (!c->records_fresh) {
         // the records are built from the measures, sides and lists
@@ -738,16 +786,36 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats, bool all_pass) {
     }
     EdgeRecs ER;
     VC_TRY(ensure_edge_recs(c, c->edge_rec, ne, &ER));  // (written by the lattice complex when fresh)
-    VC_TRY(ensure_n<int2>(c, c->q0, qcap));
-    VC_TRY(ensure_n<int2>(c, c->q1, qcap));
-    VC_TRY(ensure_n<int2>(c, c->child, 4 * qcap));
-    VC_TRY(ensure_n<int2>(c, c->cells, 4 * qcap));
     VC_TRY(ensure_n<int64_t>(c, c->euler_tmp, 16));
     VC_TRY(ensure_n<uint8_t>(c, c->keep_v, nv));
     VC_TRY(ensure_n<uint8_t>(c, c->keep_e, ne));
     VC_TRY(ensure_n<uint8_t>(c, c->keep_f, nt));
     VC_TRY(ensure_n<uint8_t>(c, c->removed_e, ne));
+    const int64_t nwv = (nv + 31) / 32, nwe = (ne + 31) / 32, nwf = (nt + 31) / 32;
+    VC_TRY(ensure_n<uint32_t>(c, c->keep_bits, nwv + nwe + nwf + 1));
+    VC_TRY(ensure_n<int32_t>(c, c->keep_wv, nwv + 1));
+    VC_TRY(ensure_n<int32_t>(c, c->keep_we, nwe + 1));
+    VC_TRY(ensure_n<int32_t>(c, c->keep_wf, nwf + 1));
+    // Queue capacity: one generation holds at most one item per vertex and
+    // edge, so V + E + 1 items always suffice.  When that does not fit (the
+    // 1024^3 random field: 2.6e9 items, 209 GB, while its largest generation
+    // is a small fraction of it), the queue takes at most 2^29 items and half
+    // of the room the device has left, the other half staying for the stages
+    // after the thinning; a generation beyond the capacity ends the thinning
+    // with VC_ERR_OOM.
+    int64_t qcap = std::min<int64_t>(nv + ne + 1, kMaxQueue);
+    if (c->thin_qcap > 0) {
+        qcap = std::min(qcap, c->thin_qcap);
+    } else if (qcap * kQueueBytes > (int64_t)(c->q0.cap + c->q1.cap + c->child.cap + c->cells.cap)) {
+        qcap = std::max<int64_t>(1, std::min(qcap, queue_room(c) / 2 / kQueueBytes));
+    }
+    VC_TRY(ensure_n<int2>(c, c->q0, qcap));
+    VC_TRY(ensure_n<int2>(c, c->q1, qcap));
+    VC_TRY(ensure_n<int2>(c, c->child, 4 * qcap));
+    VC_TRY(ensure_n<int2>(c, c->cells, 4 * qcap));
     ThinArgs A{};
+    A.qcap = qcap;
+    A.pos0 = c->thin_pos0;
     A.F = ptr<FaceRec>(c->face_rec);
     A.EH = ER.h;
     A.EN = ER.n;
@@ -836,11 +904,6 @@ int run_thin_with_device_thr(vc_ctx* c, vc_thin_stats* stats, bool all_pass) {
         if (c->thin_lock) VC_CUDA(c, cudaStreamSynchronize(c->stream));
     }
     {
-        const int64_t nwv = (nv + 31) / 32, nwe = (ne + 31) / 32, nwf = (nt + 31) / 32;
-        VC_TRY(ensure_n<uint32_t>(c, c->keep_bits, nwv + nwe + nwf + 1));
-        VC_TRY(ensure_n<int32_t>(c, c->keep_wv, nwv + 1));
-        VC_TRY(ensure_n<int32_t>(c, c->keep_we, nwe + 1));
-        VC_TRY(ensure_n<int32_t>(c, c->keep_wf, nwf + 1));
         export_flags_kernel<<<grid_for(c, 32 * (nwv + nwe + nwf), 256), 256, 0, c->stream>>>(
             A.F, A.EH, A.EN, A.V, (int32_t)nv, (int32_t)ne, (int32_t)nt, ptr<uint8_t>(c->keep_v), ptr<uint8_t>(c->keep_e),
             ptr<uint8_t>(c->keep_f), ptr<uint8_t>(c->removed_e), ptr<uint32_t>(c->keep_bits), ptr<int32_t>(c->keep_wv),
@@ -898,6 +961,13 @@ int vc_debug_set_spin_limit(vc_ctx* c, unsigned long long polls) {
 int vc_debug_fail_alloc_after(vc_ctx* c, int64_t k) {
     if (!c) return VC_ERR_ARG;
     c->fail_alloc_after = k < 0 ? -1 : k;
+    return VC_OK;
+}
+
+int vc_debug_thin_queue(vc_ctx* c, int64_t capacity, uint32_t first_position) {
+    if (!c || capacity < 0) return VC_ERR_ARG;
+    c->thin_qcap = capacity;
+    c->thin_pos0 = first_position;
     return VC_OK;
 }
 

@@ -673,7 +673,7 @@ __global__ void __launch_bounds__(128, 5) vd_vertices_edges_kernel(VolTab T, Bas
                     // the measure folded to -1 below the threshold, +1 otherwise
                     epass[d] = npass == kk && zero_passes;
                     E.h[e] = EdgeHead{v0, v1[d], kAlive, epass[d] ? -1.0f : 1.0f};
-                    E.n[e] = EdgeCnt{rs_make(kk, npass, idsum), 0u, 0};
+                    E.n[e] = EdgeCnt{rs_make(kk, npass, idsum), 0ull};
                     // generation 0: an FE pair when the one face passes the filter
                     g0[e] = (kk == 1 && npass == 1) ? (int32_t)idsum : -1;
                     ++e;
@@ -713,7 +713,6 @@ __global__ void __launch_bounds__(128, 5) vd_vertices_edges_kernel(VolTab T, Bas
                 VertRec vr;
                 vr.rs = rs_make(kk, 0, idsum);
                 vr.trig = 0;
-                vr.rm = kAlive;
                 V[v0] = vr;
                 // generation 0: an EV pair when the one edge passes the filter
                 g0[ne + v0] = (kk == 1 && (idsum & 1u)) ? (int32_t)(idsum >> 1) : -1;
@@ -887,7 +886,7 @@ __global__ void __launch_bounds__(128, 6) vd_faces_kernel(VolTab T, Bases B, con
                     fr.e2 = e32 | pass;
                     F[t1] = fr;
                     E.h[diag] = EdgeHead{dv0, dv1, kAlive, lr_};
-                    E.n[diag] = EdgeCnt{rs_make(2, lm < tb ? 2u : 0u, (unsigned long long)t0 + (unsigned long long)t1), 0u, 0};
+                    E.n[diag] = EdgeCnt{rs_make(2, lm < tb ? 2u : 0u, (unsigned long long)t0 + (unsigned long long)t1), 0ull};
                     g0[diag] = -1;  // two triangles: no FE pair
                     if (pass) {
                         if (d == 0) fp0 |= 1u << t;
@@ -1186,7 +1185,10 @@ int run_lattice_vd(vc_ctx* c, vc_vd_sizes* sizes, double t_thr) {
     VC_TRY(sync_check(c));
     const int64_t nv = h[0], ne_axis = h[1], nface = h[2];
     const int64_t ne = ne_axis + nface, nt = 2 * nface;
-    if (ne >= INT32_MAX || 3 * nt >= INT32_MAX || nv >= INT32_MAX) return VC_ERR_ARG;
+    // cell ids are 31-bit (the records tag them with bit 31); the adjacency
+    // lists the getters and the generic thinning use have 32-bit offsets and
+    // check their own sizes (build_adjacency)
+    if (ne >= INT32_MAX || nt >= INT32_MAX || nv >= INT32_MAX) return VC_ERR_ARG;
     // the complex becomes the context's finalized cell complex
     c->cc_valid = c->cc_finalized = c->meas_valid = c->thin_valid = c->rem_valid = false;
     c->records_fresh = false;
@@ -1411,6 +1413,7 @@ int ensure_vd_aux(vc_ctx* c, bool meas, bool topo) {
     const bool need_meas = meas && !c->vd_aux_meas;
     const bool need_topo = topo && !c->vd_aux_topo;
     if (!need_meas && !need_topo) return VC_OK;
+    if (need_topo && (2 * c->ne >= INT32_MAX || 3 * c->nt >= INT32_MAX)) return VC_ERR_ARG;  // (build_adjacency)
     if (need_topo) VC_TRY(ensure_vd_geometry(c));  // the adjacency is built from the edges
     const int64_t nv = c->nv, ne = c->ne, nt = c->nt, nface = c->vd.nface;
     // the kernel writes both groups; a group already written (possibly by
