@@ -631,7 +631,10 @@ __global__ void __launch_bounds__(THREADS, MINB) thin_generations_kernel(ThinArg
 }
 
 __global__ void bias_vertex_kernel(VertRec* V, int64_t v, int delta) {
-    V[v].rs += (unsigned long long)(long long)delta;  // the count is the low field of rs
+    // the count is the low field of rs; a count of 0 is not lowered (the
+    // borrow would reach the removed bit)
+    if (delta < 0 && rs_count(V[v].rs) == 0) return;
+    V[v].rs += (unsigned long long)(long long)delta;
 }
 
 __global__ void set_thr_kernel(float* thr, float f_t, float l_t) {
