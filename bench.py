@@ -790,14 +790,14 @@ def run_serving(dev, args, workers=None, max_batch=None, with_plain=True, sweep=
 
 
 # DRAM traffic per cell of the complex (V + E + T) of the thinning kernel,
-# from one ncu capture of the 192^3 case of this workload (3.931 GB read +
-# 1.835 GB written for 3,286,553 + 13,677,962 + 10,430,150 cells); the
+# from one ncu capture of the 192^3 case of this workload (3.928 GB read +
+# 1.838 GB written for 3,286,553 + 13,677,962 + 10,430,150 cells); the
 # traffic grows with the complex, so the per-launch figure at 512^3 is this
 # rate times its cells.
-TRAFFIC_PER_CELL = {"thin_generations": (3.930761e9 + 1.834827e9) / (3286553 + 13677962 + 10430150)}
+TRAFFIC_PER_CELL = {"thin_generations": (3.928310e9 + 1.838015e9) / (3286553 + 13677962 + 10430150)}
 # L2 requests (atomics + reductions + reads + writes from the SMs) per cell of
-# the same capture: 46.64 M + 13.68 M + 39.05 M + 25.14 M for the same cells.
-L2_REQUESTS_PER_CELL = {"thin_generations": (46639806 + 13684723 + 39045330 + 25144456)
+# the same capture: 46.64 M + 15.86 M + 39.05 M + 22.97 M for the same cells.
+L2_REQUESTS_PER_CELL = {"thin_generations": (46640018 + 15863455 + 39046856 + 22965656)
                         / (3286553 + 13677962 + 10430150)}
 PROBE_BYTES = 16 << 30
 
