@@ -68,6 +68,7 @@ def lib():
         L.vco_lattice_vd.restype = c_vp
         L.vco_lattice_vd.argtypes = [c_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, c_vp, c_vp]
         L.vco_vd_sizes.argtypes = [c_vp] * 6
+        L.vco_lattice_vd_counts.argtypes = [c_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, c_vp, c_vp, c_vp]
         L.vco_vd_get.argtypes = [c_vp] * 9
         L.vco_vd_radius.argtypes = [c_vp, c_vp]
         L.vco_vd_free.argtypes = [c_vp]
@@ -175,6 +176,18 @@ def ft(shape, site_lattice_idx: np.ndarray, brute: bool = False, threads: int = 
     else:
         lib().vco_ft(X, Y, Z, len(li), _ptr(li), _ptr(d2), _ptr(ids), threads)
     return d2.reshape(X + 1, Y + 1, Z + 1), ids.reshape(X + 1, Y + 1, Z + 1)
+
+
+def lattice_vd_counts(occ: np.ndarray, ft_id: np.ndarray) -> dict:
+    """The sizes lattice_vd would give (nv, ne, nt, nface) and its inside size, counted without building the
+    complex (vco_lattice_vd_counts): for volumes whose complex does not fit in host memory."""
+    occ = np.ascontiguousarray(occ, dtype=np.uint8)
+    ft_id = np.ascontiguousarray(ft_id, dtype=np.int32)
+    X, Y, Z = occ.shape
+    sizes = np.zeros(4, np.int64)
+    isz = ctypes.c_float()
+    lib().vco_lattice_vd_counts(_ptr(occ), X, Y, Z, _ptr(ft_id), _ptr(sizes), ctypes.byref(isz))
+    return dict(nv=int(sizes[0]), ne=int(sizes[1]), nt=int(sizes[2]), nface=int(sizes[3]), inside_size=float(isz.value))
 
 
 def lattice_vd(occ: np.ndarray, ft_id: np.ndarray, site_xyz: np.ndarray) -> dict:

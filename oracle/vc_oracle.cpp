@@ -596,6 +596,90 @@ void* vco_lattice_vd(const uint8_t* occ, int X, int Y, int Z, const int32_t* ft_
     return R;
 }
 
+void vco_lattice_vd_counts(const uint8_t* occ, int X, int Y, int Z, const int32_t* ft_id, long long* sizes,
+                           float* inside_size) {
+    // The sizes vco_lattice_vd gives -- vertices, edges (axis edges, then one
+    // diagonal per face), triangles, faces -- and the inside size, counted by
+    // the same validity rules without building the complex: for volumes whose
+    // complex does not fit in host memory (the 1024^3 random field).
+    const int64_t NB = Y + 1, NC = Z + 1;
+    const int64_t NV = (int64_t)X * Y * Z;
+    auto vox = [&](int64_t i, int64_t j, int64_t k) { return (i * Y + j) * Z + k; };
+    auto inside = [&](int64_t i, int64_t j, int64_t k) { return occ_at(occ, X, Y, Z, (int)i, (int)j, (int)k) == 1; };
+    auto lid = [&](int64_t a, int64_t b, int64_t c) { return (a * NB + b) * NC + c; };
+    auto cand = [&](int64_t a, int64_t b, int64_t c, int d) -> bool {
+        int64_t e[3] = {a, b, c};
+        e[d] += 1;
+        if (a < 0 || b < 0 || c < 0 || e[0] > X || e[1] > Y || e[2] > Z) return false;
+        const int32_t i0 = ft_id[lid(a, b, c)], i1 = ft_id[lid(e[0], e[1], e[2])];
+        return i0 >= 0 && i1 >= 0 && i0 != i1;
+    };
+    const int qs[4] = {0, 1, 1, 0}, qt[4] = {0, 0, 1, 1};
+    // vertices: inside voxels at a corner of a candidate face; faces: the
+    // candidates whose four voxels are all inside
+    std::vector<uint8_t> vtx((size_t)NV, 0);
+    long long nface = 0;
+    for (int64_t a = 0; a <= X; ++a)
+        for (int64_t b = 0; b <= Y; ++b)
+            for (int64_t c = 0; c <= Z; ++c)
+                for (int d = 0; d < 3; ++d) {
+                    if (!cand(a, b, c, d)) continue;
+                    const int u = (d + 1) % 3, w = (d + 2) % 3;
+                    const int64_t p[3] = {a, b, c};
+                    bool all = true;
+                    for (int q = 0; q < 4; ++q) {
+                        int64_t v[3];
+                        v[d] = p[d];
+                        v[u] = p[u] - 1 + qs[q];
+                        v[w] = p[w] - 1 + qt[q];
+                        if (inside(v[0], v[1], v[2])) vtx[(size_t)vox(v[0], v[1], v[2])] = 1;
+                        else all = false;
+                    }
+                    if (all) ++nface;
+                }
+    long long nv = 0;
+    int64_t lo[3] = {INT64_MAX, INT64_MAX, INT64_MAX}, hi[3] = {-1, -1, -1};
+    for (int64_t i = 0; i < X; ++i)
+        for (int64_t j = 0; j < Y; ++j)
+            for (int64_t k = 0; k < Z; ++k) {
+                if (!vtx[(size_t)vox(i, j, k)]) continue;
+                ++nv;
+                const int64_t pc[3] = {i, j, k};
+                for (int m = 0; m < 3; ++m) {
+                    lo[m] = std::min(lo[m], pc[m]);
+                    hi[m] = std::max(hi[m], pc[m]);
+                }
+            }
+    // axis edges: both voxels vertices and a candidate lattice edge among the
+    // four bounding the plaquette the two voxels share
+    long long naxis = 0;
+    const int64_t dims[3] = {X, Y, Z};
+    for (int64_t i = 0; i < X; ++i)
+        for (int64_t j = 0; j < Y; ++j)
+            for (int64_t k = 0; k < Z; ++k) {
+                if (!vtx[(size_t)vox(i, j, k)]) continue;
+                for (int d = 0; d < 3; ++d) {
+                    int64_t n2[3] = {i, j, k};
+                    n2[d] += 1;
+                    if (n2[d] >= dims[d] || !vtx[(size_t)vox(n2[0], n2[1], n2[2])]) continue;
+                    const int u = (d + 1) % 3, w = (d + 2) % 3;
+                    int64_t c0[3] = {i, j, k};
+                    c0[d] += 1;
+                    int64_t cu[3] = {c0[0], c0[1], c0[2]}, cw[3] = {c0[0], c0[1], c0[2]};
+                    cw[w] += 1;  // corner + e_w: lattice edge along u
+                    cu[u] += 1;  // corner + e_u: lattice edge along w
+                    if (cand(c0[0], c0[1], c0[2], u) || cand(cw[0], cw[1], cw[2], u) || cand(c0[0], c0[1], c0[2], w) ||
+                        cand(cu[0], cu[1], cu[2], w))
+                        ++naxis;
+                }
+            }
+    sizes[0] = nv;
+    sizes[1] = naxis + nface;
+    sizes[2] = 2 * nface;
+    sizes[3] = nface;
+    *inside_size = nv ? (float)std::max(hi[0] - lo[0], std::max(hi[1] - lo[1], hi[2] - lo[2])) : 0.0f;
+}
+
 void vco_vd_sizes(void* h, long long* nv, long long* ne, long long* nt, long long* nface, float* inside_size) {
     auto* R = static_cast<VD*>(h);
     *nv = (long long)R->vts.size() / 3;

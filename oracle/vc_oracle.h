@@ -43,6 +43,10 @@ void vco_ft(int X, int Y, int Z, long long nsites, const int64_t* site_lattice_i
 // (voroinfo.cpp:624-729).  Returns an opaque handle.
 void* vco_lattice_vd(const uint8_t* occ, int X, int Y, int Z, const int32_t* ft_id, const float* site_xyz);
 void vco_vd_sizes(void* h, long long* nv, long long* ne, long long* nt, long long* nface, float* inside_size);
+// The sizes vco_lattice_vd would give, {nv, ne, nt, nface}, and its inside
+// size, counted without building the complex (same validity rules).
+void vco_lattice_vd_counts(const uint8_t* occ, int X, int Y, int Z, const int32_t* ft_id, long long* sizes,
+                           float* inside_size);
 // vts: nv*3 float; edges: ne*2 int; tris: nt*3 int; vm/em/fm: measures (fm per
 // triangle); tri_face: polygon face index per triangle; face_sites: nface*2.
 void vco_vd_get(void* h, float* vts, int32_t* edges, int32_t* tris, float* vm, float* em, float* fm,

@@ -8,7 +8,10 @@ Workloads:
   spheres256_s*  unions of 32 spheres at 256^3, seeds 0, 1, 2;
   grf512         the thresholded smoothed random field at 512^3 (sigma 6,
                  level 0, seed 0): the benchmark's own workload;
-  grf1024        the same field at 1024^3: sites and feature transform only.
+  grf1024        the same field at 1024^3: sites and feature transform, and the
+                 complex's sizes, inside size and threshold, counted without
+                 building the complex (oracle.lattice_vd_counts; the complex,
+                 about 4.2e9 cells, does not fit in this host's memory).
 
 For torus64 and the sphere unions the reference's OWN compiled thinning and
 remainingCC (oracle/_ref, built from the reference tree) are also run on the
@@ -49,8 +52,8 @@ def workloads():
         "spheres256_s1": (lambda: volumes.spheres(256, count=32, seed=1), True),
         "spheres256_s2": (lambda: volumes.spheres(256, count=32, seed=2), True),
         "grf512": (lambda: volumes.grf(512, sigma=6.0, seed=0), False),
-        # sites and feature transform only: the complex of this volume (about
-        # 2.5e9 cells) is beyond 32-bit cell ids and one GPU's memory
+        # sites, feature transform and the complex's sizes only: its complex
+        # (about 4.2e9 cells) does not fit in this host's memory
         "grf1024": (lambda: volumes.grf(1024, sigma=6.0, seed=0), False),
     }
 
@@ -73,9 +76,13 @@ def run_ft_case(name: str, gen) -> dict:
     occ = np.ascontiguousarray(gen())
     xyz, li = oracle.extract_sites(occ)
     d2, ids = oracle.ft(occ.shape, li, threads=os.cpu_count() or 1)
-    out = {"shape": list(occ.shape), "stages": "sites+ft", "occupancy_sha256": volumes.occupancy_sha256(occ),
-           "n_sites": int(len(xyz)), "sites": digest(xyz), "ft": digest(d2, ids),
-           "oracle_seconds": round(time.time() - t0, 1)}
+    out = {"shape": list(occ.shape), "stages": "sites+ft+sizes", "occupancy_sha256": volumes.occupancy_sha256(occ),
+           "n_sites": int(len(xyz)), "sites": digest(xyz), "ft": digest(d2, ids)}
+    del d2, xyz, li
+    cnt = oracle.lattice_vd_counts(occ, ids)
+    out.update({"t": T, "vd_sizes": [cnt["nv"], cnt["ne"], cnt["nt"]], "inside_size": cnt["inside_size"],
+                "thresh": float(np.float32(np.float64(cnt["inside_size"]) * T)),
+                "oracle_seconds": round(time.time() - t0, 1)})
     print(name, json.dumps(out), flush=True)
     return out
 

@@ -1,7 +1,7 @@
 """The full-size workloads, bit for bit: the 64^3 torus, the 32-sphere unions at
 256^3 (seeds 0, 1, 2) and the 512^3 thresholded random field that the
-benchmark times; at 1024^3, the sites and the feature transform (the rest of
-the path there by its properties).
+benchmark times; at 1024^3, the sites, the feature transform and the
+complex's sizes and threshold (the rest of the path there by its properties).
 
 The CPU oracle's outputs at these sizes take minutes and tens of GB of host
 memory, so tests/golden/make_fullsize_digests.py ran it once and committed
@@ -57,7 +57,7 @@ def _volume(name):
 
 
 FULL = sorted(k for k, v in DIGESTS.items() if "stages" not in v)
-FT_ONLY = sorted(k for k, v in DIGESTS.items() if v.get("stages") == "sites+ft")
+FT_ONLY = sorted(k for k, v in DIGESTS.items() if v.get("stages", "").startswith("sites+ft"))
 
 
 @pytest.fixture(scope="module")
@@ -74,12 +74,13 @@ def grf512():
 def test_full_path_at_1024(name):
     """The 1024^3 field (1.08e9 lattice points, 1.24e8 sites; a complex of
     about 5e8 vertices, 2.1e9 edges and 1.6e9 triangles).  Site list and
-    feature transform bit for bit against the oracle's digests; the oracle's
-    complex at this size does not fit the host it ran on, so the rest is
-    checked by properties: the queue positions pass 2^31 (V + E > 2^31), the
-    processed pairs are the pushes less the skips, simple-pair collapses keep
-    the Euler characteristic, and a second run gives the same thinning and
-    the same remaining complex.  (The same kernels are pinned to the oracle
+    feature transform bit for bit against the oracle's digests, and the
+    complex's sizes, inside size and threshold against the oracle's count of
+    them; the oracle's complex at this size does not fit the host it ran on,
+    so the rest is checked by properties: the queue positions pass 2^31 (V +
+    E > 2^31), the processed pairs are the pushes less the skips, simple-pair
+    collapses keep the Euler characteristic, and a second run gives the same
+    thinning and the same remaining complex.  (The same kernels are pinned to the oracle
     at 512^3 above, and with positions above 2^31 and the queue capacity at
     its limit in test_gpu_thin_queue.py.)"""
     import torch
@@ -94,6 +95,9 @@ def test_full_path_at_1024(name):
         assert _digest(ctx.sites()) == d["sites"]
         assert _digest(*ctx.ft()) == d["ft"]
         vd = r["vd"]
+        if "vd_sizes" in d:
+            assert [vd["nv"], vd["ne"], vd["nt"]] == d["vd_sizes"]
+            assert vd["inside_size"] == d["inside_size"] and r["thresh"] == d["thresh"]
         assert vd["nv"] + vd["ne"] > 2**31, vd
         th = r["thin"]
         assert th["pushes"] - th["skipped"] == th["processed"] > 0

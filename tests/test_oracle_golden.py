@@ -84,3 +84,27 @@ def test_simple_triangulate_golden(golden):
                 i -= 1
             inc = not inc
         assert np.array_equal(np.array(tris, np.int32), golden[f"tri_{n}"]), n
+
+
+@pytest.mark.parametrize("vol", ["grf48", "torus64", "spheres96", "box_edge"])
+def test_lattice_vd_counts_match_the_complex(O, vol):
+    """The counting restatement (used where the complex does not fit in host
+    memory, the 1024^3 field) gives the sizes and inside size of the built
+    complex."""
+    from voxel_ma_gb300 import volumes
+    if vol == "grf48":
+        occ = volumes.grf(48, sigma=3.0, seed=5)
+    elif vol == "torus64":
+        occ = volumes.torus_mesh(64)
+    elif vol == "spheres96":
+        occ = volumes.spheres(96, count=12, seed=3)
+    else:  # a box touching the volume's faces and edges
+        occ = np.zeros((20, 17, 23), np.uint8)
+        occ[:9, 4:, 3:21] = 1
+    xyz, li = O.extract_sites(occ)
+    _, ids = O.ft(occ.shape, li)
+    vd = O.lattice_vd(occ, ids, xyz)
+    cnt = O.lattice_vd_counts(occ, ids)
+    assert [cnt["nv"], cnt["ne"], cnt["nt"]] == [len(vd["vts"]), len(vd["edges"]), len(vd["tris"])]
+    assert cnt["nface"] == len(vd["face_sites"])
+    assert cnt["inside_size"] == vd["inside_size"]
