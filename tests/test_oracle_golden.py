@@ -86,7 +86,7 @@ def test_simple_triangulate_golden(golden):
         assert np.array_equal(np.array(tris, np.int32), golden[f"tri_{n}"]), n
 
 
-@pytest.mark.parametrize("vol", ["grf48", "torus64", "spheres96", "box_edge"])
+@pytest.mark.parametrize("vol", ["grf48", "torus64", "spheres96", "box_edge", "empty", "full"])
 def test_lattice_vd_counts_match_the_complex(O, vol):
     """The counting restatement (used where the complex does not fit in host
     memory, the 1024^3 field) gives the sizes and inside size of the built
@@ -98,6 +98,10 @@ def test_lattice_vd_counts_match_the_complex(O, vol):
         occ = volumes.torus_mesh(64)
     elif vol == "spheres96":
         occ = volumes.spheres(96, count=12, seed=3)
+    elif vol == "empty":
+        occ = np.zeros((9, 11, 7), np.uint8)
+    elif vol == "full":  # every voxel inside: sites on the box's surface only
+        occ = np.ones((12, 9, 10), np.uint8)
     else:  # a box touching the volume's faces and edges
         occ = np.zeros((20, 17, 23), np.uint8)
         occ[:9, 4:, 3:21] = 1
